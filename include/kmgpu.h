@@ -1,0 +1,139 @@
+/*
+ * kmgpu.h -- C ABI of the GB300 k-means discretization library (libkmgpu.so).
+ *
+ * The library replaces the native layer under PyEMMA's clustering estimators.
+ * In the reference that layer is deeptime's pybind11 module, reached from
+ *   pyemma/coordinates/clustering/kmeans.py:211-214, 253-258
+ *       KMeans(n_clusters, max_iter, metric, tolerance, init_strategy,
+ *              fixed_seed, n_jobs).fit(X, callback_init_centers,
+ *              callback_loop).fetch_model()
+ *   pyemma/coordinates/clustering/interface.py:157-167
+ *       ClusterModel(cluster_centers, metric).transform(X)
+ * Each entry point below names the reference call it stands in for.
+ *
+ * Conventions
+ *   - Every array pointer is a DEVICE pointer owned by the caller, except
+ *     where a parameter says "host".  Frames are row-major float32 (n, d);
+ *     centers are row-major float32 (k, d); labels are int32.
+ *   - Scratch memory is a caller-owned device workspace whose size the
+ *     matching *_workspace_size() function returns; pass NULL/0 when it
+ *     returns 0.  Entry points allocate no device memory of their own.
+ *   - `stream` is a cudaStream_t (NULL = legacy default stream).  Work is
+ *     enqueued on it; calls that return host results synchronise it.
+ *   - Every call returns a km_status; km_last_error() gives a message for
+ *     the last failing call on the calling thread.
+ *   - 1 <= d <= 4096, 1 <= k <= 1048576, 0 <= n < 2^31.
+ */
+#ifndef KMGPU_H
+#define KMGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    KM_OK = 0,
+    KM_ERR_BAD_SHAPE = 1,       /* a size is out of range or a required pointer is NULL */
+    KM_ERR_WORKSPACE = 2,       /* workspace missing or smaller than *_workspace_size() */
+    KM_ERR_NON_FINITE = 3,      /* the input holds NaN or infinity where that is not allowed */
+    KM_ERR_TIMEOUT = 4,         /* a bounded device-side wait expired; the context stays usable */
+    KM_ERR_CUDA = 5,            /* a CUDA runtime call failed */
+    KM_ERR_UNSUPPORTED = 6,     /* the requested precision or shape has no kernel on this device */
+    KM_ERR_BAD_LABEL = 7        /* a label is outside [0, k) */
+} km_status;
+
+/* Distance arithmetic of the assignment.
+ *   KM_PREC_FP32: exact float32 difference of squares in feature order
+ *                 (plain CUDA-core kernel).
+ *   KM_PREC_BF16: tensor-core BF16 distances (tcgen05, FP32 accumulate) with
+ *                 an exact FP32 recheck of every frame whose nearest centers
+ *                 lie within the derived error bound; the labels equal the
+ *                 KM_PREC_FP32 labels bit for bit.
+ *   KM_PREC_AUTO: the library picks by (d, k). */
+typedef enum { KM_PREC_FP32 = 0, KM_PREC_BF16 = 1, KM_PREC_AUTO = 2 } km_precision;
+
+/* Progress hook, called on the calling host thread (kmeans.py:241-251
+ * passes callback_init_centers / callback_loop into the native fit). */
+typedef void (*km_callback)(void *user);
+
+/* Counters of one assignment (host struct, filled when a pointer is given). */
+typedef struct {
+    int64_t n_frames;   /* frames assigned */
+    int64_t n_recheck;  /* frames re-evaluated exactly over their candidate list */
+    int64_t n_full;     /* frames re-evaluated exactly over all k centers */
+    int64_t n_flipped;  /* frames whose exact label differs from the tensor-core argmin */
+    int32_t precision;  /* precision actually used (km_precision) */
+    int32_t reserved;
+} km_assign_stats;
+
+int km_version(void);
+const char *km_status_string(int status);
+const char *km_last_error(void);
+
+/* ---- kernel timing with CUDA events (diagnostics; no reference counterpart)
+ * km_profile_enable(1) resets the totals and makes later km_assign /
+ * km_lloyd calls record an event pair around their main kernels, including
+ * inside CUDA-graph replays; the pair is read at the synchronisation points
+ * these calls already have.  kind: 0 tensor-core distance kernel, 1 exact
+ * FP32 assignment kernel, 2 exact recheck kernels, 3 centroid update.
+ * km_profile_read returns the summed milliseconds and the launch count. */
+int km_profile_enable(int on);
+int km_profile_read(int32_t kind, double *ms_total, int64_t *launches);
+
+/* ---- assignment: ClusterModel(centers, 'euclidean').transform(X) ----------
+ * interface.py:157-167.  labels[i] = argmin_j ||X[i]-C[j]||^2, float32
+ * distances summed in feature order, lowest index on ties.  stats (host,
+ * nullable) synchronises the stream. */
+size_t km_assign_workspace_size(int64_t n, int32_t d, int32_t k, int32_t precision);
+int km_assign(const float *X, int64_t n, int32_t d, const float *C, int32_t k, int32_t precision,
+              int32_t *labels, void *workspace, size_t workspace_bytes, km_assign_stats *stats,
+              void *stream);
+
+/* ---- batched assignment of uneven trajectories --------------------------
+ * The get_output loop of datasource.py:402-406 runs transform chunk by chunk
+ * and trajectory by trajectory.  Here all trajectories, packed back to back
+ * in X_packed, go through one launch.  offsets (host, n_traj+1 entries,
+ * offsets[0] = 0, non-decreasing) delimit trajectory t as frames
+ * [offsets[t], offsets[t+1]).  Workspace as km_assign with n = offsets[n_traj]. */
+int km_batch_assign(const float *X_packed, const int64_t *offsets, int32_t n_traj, int32_t d,
+                    const float *C, int32_t k, int32_t precision, int32_t *labels_packed,
+                    void *workspace, size_t workspace_bytes, km_assign_stats *stats, void *stream);
+
+/* ---- one centroid update: the M-step inside KMeans.fit -------------------
+ * kmeans.py:253-258.  C_new[j] = mean of frames labelled j (float64 sums);
+ * an empty cluster keeps C_old[j].  cost (device, 1 double) receives the
+ * inertia sum_i ||X[i] - C_new[labels[i]]||^2 in float64; counts (device,
+ * k int64, nullable) the cluster sizes.  C_new must not alias C_old. */
+size_t km_update_workspace_size(int64_t n, int32_t d, int32_t k);
+int km_update(const float *X, int64_t n, int32_t d, const int32_t *labels, int32_t k,
+              const float *C_old, float *C_new, int64_t *counts, double *cost, void *workspace,
+              size_t workspace_bytes, void *stream);
+
+/* ---- kmeans++ initialisation: KMeans(init_strategy='kmeans++') -----------
+ * kmeans.py:211-212,253; seed = fixed_seed (kmeans.py:146-164).  Writes k
+ * centers into C0 (device, k*d floats) and, when idx is given (device, k
+ * int64), the chosen frame indices.  cb (nullable) fires once per center. */
+size_t km_kmpp_workspace_size(int64_t n, int32_t d, int32_t k);
+int km_kmpp(const float *X, int64_t n, int32_t d, int32_t k, uint32_t seed, float *C0, int64_t *idx,
+            km_callback cb, void *cb_user, void *workspace, size_t workspace_bytes, void *stream);
+
+/* ---- Lloyd iterations: KMeans.fit from given centers ---------------------
+ * kmeans.py:253-258 (fit), stopping rule as kmeans.py:432-436.  C (device,
+ * k*d) holds the initial centers and receives the final ones.  labels
+ * (device, n) receives the assignment of the last iteration.  inertias
+ * (host, max_iter doubles, nullable), n_iter and converged (host) report the
+ * run.  Each iteration is one CUDA-graph launch; cb fires after each. */
+size_t km_lloyd_workspace_size(int64_t n, int32_t d, int32_t k, int32_t precision);
+int km_lloyd(const float *X, int64_t n, int32_t d, int32_t k, float *C, int32_t max_iter,
+             double tolerance, int32_t precision, int32_t *labels, double *inertias,
+             int32_t *n_iter, int32_t *converged, km_callback cb, void *cb_user, void *workspace,
+             size_t workspace_bytes, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* KMGPU_H */

@@ -1,0 +1,372 @@
+/*
+ * kmeans_oracle.c -- CPU restatement of PyEMMA's k-means discretization path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is the parity oracle for the CUDA
+ * kernels in pyemma_gb300/csrc.  Only tests/, __graft_entry__.smoke() and the
+ * CPU-baseline legs of bench.py may load it.  The product path never calls it.
+ *
+ * What it restates
+ * ----------------
+ * PyEMMA delegates the arithmetic of this path to the third-party package
+ * deeptime (unpinned: setup.py:307 requires deeptime>=0.4.2,
+ * devtools/conda-recipe/meta.yaml:38 deeptime>=0.3.0).  deeptime is not part
+ * of the reference tree, so this file restates the published behaviour of its
+ * call sites:
+ *
+ *   assign    pyemma/coordinates/clustering/interface.py:157-167
+ *             (ClusterModel(centers, metric).transform(X), float32 input,
+ *              int32 output).  Squared Euclidean distance, accumulated in
+ *              float32 sequentially over features f = 0..d-1, each term
+ *              rounded as (x-c), (x-c)*(x-c), acc+term with no fused
+ *              multiply-add (the x86-64 baseline build of the reference has
+ *              no FMA instructions).  Lowest index wins ties.  A frame whose
+ *              every distance is NaN gets label 0.
+ *   update    pyemma/coordinates/clustering/kmeans.py:253-258 (KMeans.fit):
+ *             new center = mean of members, summed in float64; an empty
+ *             cluster keeps its previous center (assumption: deeptime's
+ *             behaviour could not be checked, its source is absent).
+ *   inertia   kmeans.py:71-75 docstring: C(S) = sum_i sum_{x in S_i}
+ *             ||x - mu_i||^2, evaluated in float64 for the new centers and
+ *             the assignment of the same iteration.
+ *   stopping  kmeans.py:432-436 (the in-repo copy of the rule):
+ *             rel = |cost - prev| / cost (0 if cost == 0), prev starts at 0,
+ *             converged when rel <= tolerance; at most max_iter iterations.
+ *   kmeans++  kmeans.py:211-212,253 (init_strategy='kmeans++', seeded by
+ *             fixed_seed, an integer in [0, 2^32-1], kmeans.py:146-164):
+ *             first center uniform at random, every later center drawn with
+ *             probability proportional to D^2, the squared distance to the
+ *             nearest center chosen so far (Arthur & Vassilvitskii 2007).
+ *             Random numbers come from Philox4x32-10 (Salmon et al., SC'11);
+ *             D^2 weights are quantised to integers so that every prefix sum
+ *             is exact and any summation order draws the same center.
+ *
+ * Parity status: the float order inside deeptime is unpinned (deeptime is
+ * absent).  The oracle is pinned by the known-answer tests of the reference
+ * (pyemma/coordinates/clustering/tests/test_assign.py and test_kmeans.py),
+ * restated in tests/test_oracle_pins.py.
+ *
+ * Build: gcc -O3 -fopenmp -ffp-contract=off -fPIC -shared (oracle/build.sh).
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define KMO_OK 0
+#define KMO_BAD_ARG -1
+#define KMO_NOMEM -2
+
+int kmo_version(void) { return 1; }
+
+/* ------------------------------------------------------------------ */
+/* Philox4x32-10 (Salmon, Moraes, Dror, Shaw: "Parallel random numbers: */
+/* as easy as 1, 2, 3", SC'11).                                        */
+/* ------------------------------------------------------------------ */
+void kmo_philox4x32_10(const uint32_t ctr_in[4], const uint32_t key_in[2], uint32_t out[4]) {
+    uint32_t c0 = ctr_in[0], c1 = ctr_in[1], c2 = ctr_in[2], c3 = ctr_in[3];
+    uint32_t k0 = key_in[0], k1 = key_in[1];
+    for (int r = 0; r < 10; ++r) {
+        if (r > 0) {
+            k0 += 0x9E3779B9u;
+            k1 += 0xBB67AE85u;
+        }
+        uint64_t p0 = (uint64_t)0xD2511F53u * c0;
+        uint64_t p1 = (uint64_t)0xCD9E8D57u * c2;
+        uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+        uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+        uint32_t n0 = hi1 ^ c1 ^ k0;
+        uint32_t n2 = hi0 ^ c3 ^ k1;
+        c0 = n0;
+        c1 = lo1;
+        c2 = n2;
+        c3 = lo0;
+    }
+    out[0] = c0;
+    out[1] = c1;
+    out[2] = c2;
+    out[3] = c3;
+}
+
+/* The 64-bit draw of kmeans++ round r: counter (r, 0, tag, 0), key (seed, tag2). */
+uint64_t kmo_kmpp_draw(uint32_t seed, uint32_t round) {
+    uint32_t ctr[4] = {round, 0u, 0x6B6D7070u, 0u};
+    uint32_t key[2] = {seed, 0x4B4D4750u};
+    uint32_t out[4];
+    kmo_philox4x32_10(ctr, key, out);
+    return ((uint64_t)out[0] << 32) | (uint64_t)out[1];
+}
+
+static inline uint64_t mulhi64(uint64_t a, uint64_t b) {
+    return (uint64_t)(((unsigned __int128)a * (unsigned __int128)b) >> 64);
+}
+
+/* Exponent E with 2^(E-1) <= m < 2^E for a positive finite float m. */
+static int float_ceil_exp(float m) {
+    uint32_t b;
+    memcpy(&b, &m, 4);
+    int be = (int)((b >> 23) & 0xFFu);
+    if (be) return be - 126;
+    uint32_t mant = b & 0x7FFFFFu;
+    int p = 31 - __builtin_clz(mant);
+    return p - 148;
+}
+
+/* Scale exponent for the integer D^2 weights: with M the largest finite
+ * weight and L = ceil(log2 n), every weight floor(w * 2^e) is below
+ * 2^(62-L), so the sum of all n weights stays below 2^62. */
+int kmo_quant_exponent(float max_weight, int64_t n) {
+    if (!(max_weight > 0.0f) || isinf(max_weight)) return INT32_MIN;
+    int L = 0;
+    while (((int64_t)1 << L) < n) ++L;
+    return 62 - L - float_ceil_exp(max_weight);
+}
+
+static inline uint64_t quant_weight(float w, double scale) {
+    if (!(w > 0.0f) || isinf(w)) return 0;
+    return (uint64_t)((double)w * scale);
+}
+
+/* ------------------------------------------------------------------ */
+/* Distances                                                          */
+/* ------------------------------------------------------------------ */
+float kmo_sqdist(const float *x, const float *c, int32_t d) {
+    float acc = 0.0f;
+    for (int32_t f = 0; f < d; ++f) {
+        float t = x[f] - c[f];
+        float s = t * t;
+        acc = acc + s;
+    }
+    return acc;
+}
+
+#define KMO_CB 8
+
+/* Centers regrouped in blocks of KMO_CB, feature-major inside a block, so
+ * that the compiler can evaluate KMO_CB independent sequential sums at once.
+ * Each sum keeps its own feature order, so the result equals kmo_sqdist. */
+static float *transpose_center_blocks(const float *C, int32_t k, int32_t d) {
+    int32_t nb = k / KMO_CB;
+    if (nb == 0) return NULL;
+    float *ct = (float *)malloc((size_t)nb * KMO_CB * d * sizeof(float));
+    if (!ct) return NULL;
+    for (int32_t b = 0; b < nb; ++b)
+        for (int32_t f = 0; f < d; ++f)
+            for (int32_t u = 0; u < KMO_CB; ++u)
+                ct[((size_t)b * d + f) * KMO_CB + u] = C[(size_t)(b * KMO_CB + u) * d + f];
+    return ct;
+}
+
+static void assign_one(const float *x, int32_t d, const float *C, const float *ct, int32_t k,
+                       int32_t *label, float *dist) {
+    float best = INFINITY;
+    int32_t bj = 0;
+    int32_t j = 0;
+    if (ct) {
+        for (; j + KMO_CB <= k; j += KMO_CB) {
+            const float *blk = ct + (size_t)(j / KMO_CB) * d * KMO_CB;
+            float acc[KMO_CB];
+            for (int u = 0; u < KMO_CB; ++u) acc[u] = 0.0f;
+            for (int32_t f = 0; f < d; ++f) {
+                float xf = x[f];
+                for (int u = 0; u < KMO_CB; ++u) {
+                    float t = xf - blk[f * KMO_CB + u];
+                    float s = t * t;
+                    acc[u] = acc[u] + s;
+                }
+            }
+            for (int u = 0; u < KMO_CB; ++u)
+                if (acc[u] < best) {
+                    best = acc[u];
+                    bj = j + u;
+                }
+        }
+    }
+    for (; j < k; ++j) {
+        float dd = kmo_sqdist(x, C + (size_t)j * d, d);
+        if (dd < best) {
+            best = dd;
+            bj = j;
+        }
+    }
+    *label = bj;
+    if (dist) *dist = best;
+}
+
+/* labels[i] = argmin_j D(x_i, c_j); dist (nullable) receives the minimum. */
+int kmo_assign(const float *X, int64_t n, int32_t d, const float *C, int32_t k, int32_t *labels,
+               float *dist, int32_t n_threads) {
+    if (n < 0 || d <= 0 || k <= 0 || (n > 0 && (!X || !labels)) || !C) return KMO_BAD_ARG;
+    float *ct = transpose_center_blocks(C, k, d);
+    if (n_threads <= 0) n_threads = 1;
+#pragma omp parallel for num_threads(n_threads) schedule(static)
+    for (int64_t i = 0; i < n; ++i)
+        assign_one(X + (size_t)i * d, d, C, ct, k, labels + i, dist ? dist + i : NULL);
+    free(ct);
+    return KMO_OK;
+}
+
+/* ------------------------------------------------------------------ */
+/* Centroid update and inertia (float64)                              */
+/* ------------------------------------------------------------------ */
+/* Sums are taken relative to each cluster's previous center:
+ *   S_j = sum_{i in j} (x_i - c_j),  Q_j = sum_{i in j} ||x_i - c_j||^2
+ * new center  mu_j = float(c_j + S_j / n_j)     (c_j kept when n_j == 0)
+ * inertia_j   = Q_j - 2 delta_j . S_j + n_j ||delta_j||^2,  delta_j = mu_j - c_j
+ * which is sum_{i in j} ||x_i - mu_j||^2 evaluated in float64.  Frames are
+ * visited in index order. */
+int kmo_update(const float *X, int64_t n, int32_t d, const int32_t *labels, int32_t k,
+               const float *C_old, float *C_new, int64_t *counts, double *cost_out,
+               double *cluster_cost) {
+    if (n < 0 || d <= 0 || k <= 0 || !C_old || !C_new || !counts) return KMO_BAD_ARG;
+    double *S = (double *)calloc((size_t)k * d, sizeof(double));
+    double *Q = (double *)calloc((size_t)k, sizeof(double));
+    if (!S || !Q) {
+        free(S);
+        free(Q);
+        return KMO_NOMEM;
+    }
+    memset(counts, 0, (size_t)k * sizeof(int64_t));
+    for (int64_t i = 0; i < n; ++i) {
+        int32_t j = labels[i];
+        if (j < 0 || j >= k) {
+            free(S);
+            free(Q);
+            return KMO_BAD_ARG;
+        }
+        const float *x = X + (size_t)i * d;
+        const float *c = C_old + (size_t)j * d;
+        double *s = S + (size_t)j * d;
+        double q = 0.0;
+        for (int32_t f = 0; f < d; ++f) {
+            double t = (double)x[f] - (double)c[f];
+            s[f] += t;
+            q += t * t;
+        }
+        Q[j] += q;
+        counts[j] += 1;
+    }
+    double cost = 0.0;
+    for (int32_t j = 0; j < k; ++j) {
+        const float *c = C_old + (size_t)j * d;
+        float *m = C_new + (size_t)j * d;
+        double cj = 0.0;
+        if (counts[j] == 0) {
+            memmove(m, c, (size_t)d * sizeof(float));
+        } else {
+            double cnt = (double)counts[j];
+            const double *s = S + (size_t)j * d;
+            double cross = 0.0, sq = 0.0;
+            for (int32_t f = 0; f < d; ++f) {
+                float mu = (float)((double)c[f] + s[f] / cnt);
+                double dl = (double)mu - (double)c[f];
+                cross += dl * s[f];
+                sq += dl * dl;
+                m[f] = mu;
+            }
+            cj = Q[j] - 2.0 * cross + cnt * sq;
+        }
+        if (cluster_cost) cluster_cost[j] = cj;
+        cost += cj;
+    }
+    *cost_out = cost;
+    free(S);
+    free(Q);
+    return KMO_OK;
+}
+
+/* ------------------------------------------------------------------ */
+/* Lloyd iterations                                                   */
+/* ------------------------------------------------------------------ */
+int kmo_lloyd(const float *X, int64_t n, int32_t d, int32_t k, float *C, int32_t max_iter,
+              double tol, int32_t *labels, double *inertias, int32_t *n_iter, int32_t *converged,
+              int32_t n_threads) {
+    if (n <= 0 || d <= 0 || k <= 0 || !C || !labels || max_iter < 0) return KMO_BAD_ARG;
+    float *Cn = (float *)malloc((size_t)k * d * sizeof(float));
+    int64_t *cnt = (int64_t *)malloc((size_t)k * sizeof(int64_t));
+    if (!Cn || !cnt) {
+        free(Cn);
+        free(cnt);
+        return KMO_NOMEM;
+    }
+    double prev = 0.0;
+    int32_t it = 0, conv = 0;
+    int rc = KMO_OK;
+    while (it < max_iter) {
+        rc = kmo_assign(X, n, d, C, k, labels, NULL, n_threads);
+        if (rc) break;
+        double cost;
+        rc = kmo_update(X, n, d, labels, k, C, Cn, cnt, &cost, NULL);
+        if (rc) break;
+        memcpy(C, Cn, (size_t)k * d * sizeof(float));
+        if (inertias) inertias[it] = cost;
+        double rel = cost != 0.0 ? fabs(cost - prev) / cost : 0.0;
+        prev = cost;
+        ++it;
+        if (rel <= tol) {
+            conv = 1;
+            break;
+        }
+    }
+    free(Cn);
+    free(cnt);
+    if (n_iter) *n_iter = it;
+    if (converged) *converged = conv;
+    return rc;
+}
+
+/* ------------------------------------------------------------------ */
+/* kmeans++                                                           */
+/* ------------------------------------------------------------------ */
+int kmo_kmpp(const float *X, int64_t n, int32_t d, int32_t k, uint32_t seed, float *C0,
+             int64_t *idx_out, int32_t n_threads) {
+    if (n <= 0 || d <= 0 || k <= 0 || !X || !C0) return KMO_BAD_ARG;
+    if (n_threads <= 0) n_threads = 1;
+    int64_t p = (int64_t)mulhi64(kmo_kmpp_draw(seed, 0), (uint64_t)n);
+    memcpy(C0, X + (size_t)p * d, (size_t)d * sizeof(float));
+    if (idx_out) idx_out[0] = p;
+    if (k == 1) return KMO_OK;
+    float *mind = (float *)malloc((size_t)n * sizeof(float));
+    if (!mind) return KMO_NOMEM;
+#pragma omp parallel for num_threads(n_threads) schedule(static)
+    for (int64_t i = 0; i < n; ++i) mind[i] = kmo_sqdist(X + (size_t)i * d, C0, d);
+    float M = 0.0f;
+    for (int64_t i = 0; i < n; ++i)
+        if (isfinite(mind[i]) && mind[i] > M) M = mind[i];
+    int e = kmo_quant_exponent(M, n);
+    double scale = (e == INT32_MIN) ? 0.0 : ldexp(1.0, e);
+    for (int32_t r = 1; r < k; ++r) {
+        if (r >= 2) {
+            const float *c = C0 + (size_t)(r - 1) * d;
+#pragma omp parallel for num_threads(n_threads) schedule(static)
+            for (int64_t i = 0; i < n; ++i) {
+                float dd = kmo_sqdist(X + (size_t)i * d, c, d);
+                if (dd < mind[i]) mind[i] = dd;
+            }
+        }
+        uint64_t total = 0;
+#pragma omp parallel for num_threads(n_threads) schedule(static) reduction(+ : total)
+        for (int64_t i = 0; i < n; ++i) total += quant_weight(mind[i], scale);
+        uint64_t r64 = kmo_kmpp_draw(seed, (uint32_t)r);
+        if (total == 0) {
+            p = (int64_t)mulhi64(r64, (uint64_t)n);
+        } else {
+            uint64_t t = mulhi64(r64, total);
+            uint64_t acc = 0;
+            p = n - 1;
+            for (int64_t i = 0; i < n; ++i) {
+                acc += quant_weight(mind[i], scale);
+                if (acc > t) {
+                    p = i;
+                    break;
+                }
+            }
+        }
+        memcpy(C0 + (size_t)r * d, X + (size_t)p * d, (size_t)d * sizeof(float));
+        if (idx_out) idx_out[r] = p;
+    }
+    free(mind);
+    return KMO_OK;
+}

@@ -1,0 +1,178 @@
+"""Python access to the CPU oracle (test infrastructure only).
+
+The oracle restates PyEMMA's k-means discretization path on the CPU
+(``oracle/kmeans_oracle.c``; semantics and reference citations are in that
+file's header).  Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU legs
+of ``bench.py`` import this module: it is the checker, never the product.
+
+Besides the ctypes bindings this module holds a float64 NumPy reference for
+centers and inertia, which is independent of the C code.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "libkmoracle.so")
+_lib = None
+
+
+def build():
+    """Compile ``libkmoracle.so`` next to this file."""
+    subprocess.check_call(["sh", os.path.join(_HERE, "build.sh")])
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_LIB_PATH):
+            build()
+        L = ctypes.CDLL(_LIB_PATH)
+        P = ctypes.c_void_p
+        i64, i32, u32, f64 = ctypes.c_int64, ctypes.c_int32, ctypes.c_uint32, ctypes.c_double
+        L.kmo_philox4x32_10.argtypes = [P, P, P]
+        L.kmo_kmpp_draw.argtypes = [u32, u32]
+        L.kmo_kmpp_draw.restype = ctypes.c_uint64
+        L.kmo_quant_exponent.argtypes = [ctypes.c_float, i64]
+        L.kmo_quant_exponent.restype = i32
+        L.kmo_sqdist.argtypes = [P, P, i32]
+        L.kmo_sqdist.restype = ctypes.c_float
+        L.kmo_assign.argtypes = [P, i64, i32, P, i32, P, P, i32]
+        L.kmo_update.argtypes = [P, i64, i32, P, i32, P, P, P, P, P]
+        L.kmo_lloyd.argtypes = [P, i64, i32, i32, P, i32, f64, P, P, P, P, i32]
+        L.kmo_kmpp.argtypes = [P, i64, i32, i32, u32, P, P, i32]
+        for name in ("kmo_assign", "kmo_update", "kmo_lloyd", "kmo_kmpp"):
+            getattr(L, name).restype = ctypes.c_int
+        _lib = L
+    return _lib
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def default_threads():
+    return max(1, len(os.sched_getaffinity(0)))
+
+
+def _check(rc, what):
+    if rc != 0:
+        raise RuntimeError("oracle %s failed with status %d" % (what, rc))
+
+
+def philox4x32_10(ctr, key):
+    c = (ctypes.c_uint32 * 4)(*ctr)
+    k = (ctypes.c_uint32 * 2)(*key)
+    o = (ctypes.c_uint32 * 4)()
+    lib().kmo_philox4x32_10(c, k, o)
+    return list(o)
+
+
+def kmpp_draw(seed, rnd):
+    return int(lib().kmo_kmpp_draw(seed, rnd))
+
+
+def quant_exponent(max_weight, n):
+    return int(lib().kmo_quant_exponent(max_weight, n))
+
+
+def assign(X, C, n_threads=None, return_dist=False):
+    """int32 labels of the nearest center (float32 sequential distances)."""
+    X = _f32(X)
+    C = _f32(C)
+    n, d = X.shape
+    k = C.shape[0]
+    labels = np.empty(n, dtype=np.int32)
+    dist = np.empty(n, dtype=np.float32) if return_dist else None
+    rc = lib().kmo_assign(_ptr(X), n, d, _ptr(C), k, _ptr(labels), _ptr(dist),
+                          n_threads or default_threads())
+    _check(rc, "assign")
+    return (labels, dist) if return_dist else labels
+
+
+def update(X, labels, C_old):
+    """One centroid update; returns (new centers, counts, inertia, per-cluster inertia)."""
+    X = _f32(X)
+    C_old = _f32(C_old)
+    labels = np.ascontiguousarray(labels, dtype=np.int32)
+    n, d = X.shape
+    k = C_old.shape[0]
+    C_new = np.empty_like(C_old)
+    counts = np.empty(k, dtype=np.int64)
+    cost = np.zeros(1, dtype=np.float64)
+    ccost = np.empty(k, dtype=np.float64)
+    rc = lib().kmo_update(_ptr(X), n, d, _ptr(labels), k, _ptr(C_old), _ptr(C_new),
+                          _ptr(counts), _ptr(cost), _ptr(ccost))
+    _check(rc, "update")
+    return C_new, counts, float(cost[0]), ccost
+
+
+def lloyd(X, C0, max_iter, tol, n_threads=None):
+    """Lloyd iterations from C0; returns dict(centers, labels, inertias, n_iter, converged)."""
+    X = _f32(X)
+    C = _f32(C0).copy()
+    n, d = X.shape
+    k = C.shape[0]
+    labels = np.zeros(n, dtype=np.int32)
+    inertias = np.zeros(max(1, max_iter), dtype=np.float64)
+    n_iter = np.zeros(1, dtype=np.int32)
+    conv = np.zeros(1, dtype=np.int32)
+    rc = lib().kmo_lloyd(_ptr(X), n, d, k, _ptr(C), max_iter, float(tol), _ptr(labels),
+                         _ptr(inertias), _ptr(n_iter), _ptr(conv), n_threads or default_threads())
+    _check(rc, "lloyd")
+    it = int(n_iter[0])
+    return dict(centers=C, labels=labels, inertias=inertias[:it].copy(), n_iter=it,
+                converged=bool(conv[0]))
+
+
+def kmpp(X, k, seed, n_threads=None):
+    """kmeans++ initial centers; returns (centers (k,d) float32, frame indices)."""
+    X = _f32(X)
+    n, d = X.shape
+    C0 = np.empty((k, d), dtype=np.float32)
+    idx = np.empty(k, dtype=np.int64)
+    rc = lib().kmo_kmpp(_ptr(X), n, d, k, int(seed) & 0xFFFFFFFF, _ptr(C0), _ptr(idx),
+                        n_threads or default_threads())
+    _check(rc, "kmpp")
+    return C0, idx
+
+
+# ---------------------------------------------------------------------------
+# float64 NumPy reference (independent of the C code)
+# ---------------------------------------------------------------------------
+def centers_fp64(X, labels, C_old):
+    """Member means in float64; empty clusters keep their previous center."""
+    X = np.asarray(X, dtype=np.float64)
+    k, d = C_old.shape
+    S = np.zeros((k, d))
+    np.add.at(S, labels, X)
+    cnt = np.bincount(labels, minlength=k).astype(np.float64)
+    out = np.asarray(C_old, dtype=np.float64).copy()
+    nz = cnt > 0
+    out[nz] = S[nz] / cnt[nz, None]
+    return out, cnt
+
+
+def inertia_fp64(X, labels, C):
+    """sum_i ||x_i - c_{label_i}||^2 in float64."""
+    X = np.asarray(X, dtype=np.float64)
+    C = np.asarray(C, dtype=np.float64)
+    diff = X - C[labels]
+    return float(np.einsum("ij,ij->", diff, diff))
+
+
+def sqdist_fp32_sequential(X, C):
+    """(n, k) float32 distances with the oracle's feature order (slow; small cases only)."""
+    X = np.asarray(X, dtype=np.float32)
+    C = np.asarray(C, dtype=np.float32)
+    acc = np.zeros((X.shape[0], C.shape[0]), dtype=np.float32)
+    for f in range(X.shape[1]):
+        t = X[:, f][:, None] - C[:, f][None, :]
+        acc = acc + t * t
+    return acc

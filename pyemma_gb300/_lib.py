@@ -1,0 +1,276 @@
+"""ctypes binding of libkmgpu.so (the C ABI in include/kmgpu.h).
+
+Device buffers are torch tensors; only raw pointers, sizes and the CUDA
+stream handle cross the boundary.  There is no CPU implementation behind
+these functions: without the library or without a CUDA device every call
+raises.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import _build
+
+PRECISIONS = {"fp32": 0, "bf16": 1, "auto": 2}
+PRECISION_NAMES = {v: k for k, v in PRECISIONS.items()}
+
+KM_OK = 0
+KM_ERR_BAD_SHAPE = 1
+KM_ERR_WORKSPACE = 2
+KM_ERR_NON_FINITE = 3
+KM_ERR_TIMEOUT = 4
+KM_ERR_CUDA = 5
+KM_ERR_UNSUPPORTED = 6
+KM_ERR_BAD_LABEL = 7
+
+EXPORTED = (
+    "km_version", "km_status_string", "km_last_error", "km_profile_enable", "km_profile_read",
+    "km_assign_workspace_size", "km_assign", "km_batch_assign",
+    "km_update_workspace_size", "km_update",
+    "km_kmpp_workspace_size", "km_kmpp",
+    "km_lloyd_workspace_size", "km_lloyd",
+)
+
+
+class KmError(RuntimeError):
+    """A libkmgpu call returned a non-zero km_status."""
+
+    def __init__(self, status, message):
+        super().__init__(message)
+        self.status = status
+
+
+class AssignStats(ctypes.Structure):
+    _fields_ = [("n_frames", ctypes.c_int64), ("n_recheck", ctypes.c_int64),
+                ("n_full", ctypes.c_int64), ("n_flipped", ctypes.c_int64),
+                ("precision", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+    def as_dict(self):
+        return dict(n_frames=self.n_frames, n_recheck=self.n_recheck, n_full=self.n_full,
+                    n_flipped=self.n_flipped, precision=PRECISION_NAMES.get(self.precision, "?"))
+
+
+CALLBACK = ctypes.CFUNCTYPE(None, ctypes.c_void_p)
+
+_lib = None
+
+
+def library_path():
+    return _build.LIB_PATH
+
+
+def load(build_if_missing=False):
+    """Loads libkmgpu.so and declares its signatures."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = library_path()
+    if not os.path.exists(path):
+        if build_if_missing:
+            _build.build()
+        else:
+            raise ImportError("libkmgpu.so is not built (%s); run __graft_entry__.build()" % path)
+    L = ctypes.CDLL(path)
+    P, i64, i32, u32, f64 = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32, ctypes.c_uint32, ctypes.c_double
+    sz = ctypes.c_size_t
+    L.km_version.restype = ctypes.c_int
+    L.km_status_string.argtypes = [ctypes.c_int]
+    L.km_status_string.restype = ctypes.c_char_p
+    L.km_last_error.restype = ctypes.c_char_p
+    L.km_profile_enable.argtypes = [ctypes.c_int]
+    L.km_profile_enable.restype = ctypes.c_int
+    L.km_profile_read.argtypes = [i32, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int64)]
+    L.km_profile_read.restype = ctypes.c_int
+    L.km_assign_workspace_size.argtypes = [i64, i32, i32, i32]
+    L.km_assign_workspace_size.restype = sz
+    L.km_assign.argtypes = [P, i64, i32, P, i32, i32, P, P, sz, ctypes.POINTER(AssignStats), P]
+    L.km_batch_assign.argtypes = [P, P, i32, i32, P, i32, i32, P, P, sz, ctypes.POINTER(AssignStats), P]
+    L.km_update_workspace_size.argtypes = [i64, i32, i32]
+    L.km_update_workspace_size.restype = sz
+    L.km_update.argtypes = [P, i64, i32, P, i32, P, P, P, P, P, sz, P]
+    L.km_kmpp_workspace_size.argtypes = [i64, i32, i32]
+    L.km_kmpp_workspace_size.restype = sz
+    L.km_kmpp.argtypes = [P, i64, i32, i32, u32, P, P, CALLBACK, P, P, sz, P]
+    L.km_lloyd_workspace_size.argtypes = [i64, i32, i32, i32]
+    L.km_lloyd_workspace_size.restype = sz
+    L.km_lloyd.argtypes = [P, i64, i32, i32, P, i32, f64, i32, P, P, P, P, CALLBACK, P, P, sz, P]
+    for name in ("km_assign", "km_batch_assign", "km_update", "km_kmpp", "km_lloyd"):
+        getattr(L, name).restype = ctypes.c_int
+    _lib = L
+    return L
+
+
+PROFILE_KINDS = {"tc": 0, "fp32": 1, "recheck": 2, "update": 3}
+
+
+def profile_enable(on=True):
+    """Starts (or stops) CUDA-event timing of the main kernels; resets the totals."""
+    check(load().km_profile_enable(1 if on else 0))
+
+
+def profile_read():
+    """{kind: (total ms, launches)} since the last profile_enable."""
+    L = load()
+    out = {}
+    for name, kind in PROFILE_KINDS.items():
+        ms, n = ctypes.c_double(), ctypes.c_int64()
+        check(L.km_profile_read(kind, ctypes.byref(ms), ctypes.byref(n)))
+        out[name] = (ms.value, n.value)
+    return out
+
+
+def check(rc):
+    if rc != KM_OK:
+        L = load()
+        raise KmError(rc, "libkmgpu: %s: %s" % (L.km_status_string(rc).decode(),
+                                                L.km_last_error().decode()))
+
+
+# ---------------------------------------------------------------------------
+# torch-facing helpers
+# ---------------------------------------------------------------------------
+def _torch():
+    import torch
+    if not torch.cuda.is_available():
+        raise RuntimeError("pyemma_gb300 needs a CUDA device; none is available")
+    return torch
+
+
+def _ptr(t):
+    return None if t is None else ctypes.c_void_p(t.data_ptr())
+
+
+def _stream(torch, device):
+    return ctypes.c_void_p(torch.cuda.current_stream(device).cuda_stream)
+
+
+def _workspace(torch, nbytes, device):
+    if nbytes == 0:
+        return None
+    return torch.empty(int(nbytes), dtype=torch.uint8, device=device)
+
+
+def precision_code(precision):
+    if isinstance(precision, str):
+        try:
+            return PRECISIONS[precision.lower()]
+        except KeyError:
+            raise ValueError("precision must be one of %s" % sorted(PRECISIONS))
+    return int(precision)
+
+
+def _check_frames(torch, X, name="X"):
+    if X.device.type != "cuda" or X.dtype != torch.float32 or X.dim() != 2 or not X.is_contiguous():
+        raise ValueError("%s must be a contiguous float32 (n, d) CUDA tensor" % name)
+
+
+def assign(X, C, precision="auto", labels=None):
+    """Labels (int32 CUDA tensor) of the nearest center for every row of X."""
+    torch = _torch()
+    L = load()
+    _check_frames(torch, X)
+    _check_frames(torch, C, "C")
+    n, d = X.shape
+    k = C.shape[0]
+    if C.shape[1] != d:
+        raise ValueError("centers have dimension %d, frames %d" % (C.shape[1], d))
+    p = precision_code(precision)
+    if labels is None:
+        labels = torch.empty(n, dtype=torch.int32, device=X.device)
+    ws_bytes = L.km_assign_workspace_size(n, d, k, p)
+    ws = _workspace(torch, ws_bytes, X.device)
+    stats = AssignStats()
+    check(L.km_assign(_ptr(X), n, d, _ptr(C), k, p, _ptr(labels), _ptr(ws), ws_bytes, ctypes.byref(stats),
+                      _stream(torch, X.device)))
+    return labels, stats.as_dict()
+
+
+def batch_assign(X_packed, offsets, C, precision="auto", labels=None):
+    """Assignment of trajectories packed back to back; offsets has n_traj+1 entries."""
+    torch = _torch()
+    L = load()
+    _check_frames(torch, X_packed)
+    _check_frames(torch, C, "C")
+    offs = np.ascontiguousarray(offsets, dtype=np.int64)
+    n_traj = len(offs) - 1
+    n, d = X_packed.shape
+    if n_traj < 0 or (n_traj >= 0 and offs[-1] != n):
+        raise ValueError("offsets must end at the number of packed frames")
+    k = C.shape[0]
+    p = precision_code(precision)
+    if labels is None:
+        labels = torch.empty(n, dtype=torch.int32, device=X_packed.device)
+    ws_bytes = L.km_assign_workspace_size(n, d, k, p)
+    ws = _workspace(torch, ws_bytes, X_packed.device)
+    stats = AssignStats()
+    check(L.km_batch_assign(_ptr(X_packed), offs.ctypes.data_as(ctypes.c_void_p), n_traj, d, _ptr(C), k, p,
+                            _ptr(labels), _ptr(ws), ws_bytes, ctypes.byref(stats),
+                            _stream(torch, X_packed.device)))
+    return labels, stats.as_dict()
+
+
+def update(X, labels, C_old):
+    """One centroid update; returns (C_new, counts int64, inertia float)."""
+    torch = _torch()
+    L = load()
+    _check_frames(torch, X)
+    n, d = X.shape
+    k = C_old.shape[0]
+    C_new = torch.empty_like(C_old)
+    counts = torch.empty(k, dtype=torch.int64, device=X.device)
+    cost = torch.empty(1, dtype=torch.float64, device=X.device)
+    ws_bytes = L.km_update_workspace_size(n, d, k)
+    ws = _workspace(torch, ws_bytes, X.device)
+    check(L.km_update(_ptr(X), n, d, _ptr(labels), k, _ptr(C_old), _ptr(C_new), _ptr(counts), _ptr(cost),
+                      _ptr(ws), ws_bytes, _stream(torch, X.device)))
+    return C_new, counts, float(cost.item())
+
+
+def _callback(fn):
+    if fn is None:
+        return CALLBACK(0), None
+    cb = CALLBACK(lambda _user: fn())
+    return cb, cb
+
+
+def kmpp(X, k, seed, callback=None):
+    """kmeans++ initial centers (k, d) and chosen frame indices."""
+    torch = _torch()
+    L = load()
+    _check_frames(torch, X)
+    n, d = X.shape
+    C0 = torch.empty((k, d), dtype=torch.float32, device=X.device)
+    idx = torch.empty(k, dtype=torch.int64, device=X.device)
+    ws_bytes = L.km_kmpp_workspace_size(n, d, k)
+    ws = _workspace(torch, ws_bytes, X.device)
+    cb, keep = _callback(callback)
+    check(L.km_kmpp(_ptr(X), n, d, k, int(seed) & 0xFFFFFFFF, _ptr(C0), _ptr(idx), cb, None, _ptr(ws),
+                    ws_bytes, _stream(torch, X.device)))
+    del keep
+    return C0, idx
+
+
+def lloyd(X, C, max_iter, tolerance, precision="auto", callback=None, labels=None):
+    """Lloyd iterations in place on C; returns dict(labels, inertias, n_iter, converged)."""
+    torch = _torch()
+    L = load()
+    _check_frames(torch, X)
+    _check_frames(torch, C, "C")
+    n, d = X.shape
+    k = C.shape[0]
+    p = precision_code(precision)
+    if labels is None:
+        labels = torch.empty(n, dtype=torch.int32, device=X.device)
+    inertias = np.zeros(max(1, max_iter), dtype=np.float64)
+    n_iter = ctypes.c_int32(0)
+    conv = ctypes.c_int32(0)
+    ws_bytes = L.km_lloyd_workspace_size(n, d, k, p)
+    ws = _workspace(torch, ws_bytes, X.device)
+    cb, keep = _callback(callback)
+    check(L.km_lloyd(_ptr(X), n, d, k, _ptr(C), int(max_iter), float(tolerance), p, _ptr(labels),
+                     inertias.ctypes.data_as(ctypes.c_void_p), ctypes.byref(n_iter), ctypes.byref(conv), cb,
+                     None, _ptr(ws), ws_bytes, _stream(torch, X.device)))
+    del keep
+    return dict(labels=labels, inertias=inertias[:n_iter.value].copy(), n_iter=n_iter.value,
+                converged=bool(conv.value))

@@ -1,0 +1,199 @@
+"""k-means estimator on the GPU.
+
+Mirrors KmeansClustering of pyemma/coordinates/clustering/kmeans.py:47-338.
+The reference collects all (strided, skipped) frames into one float32 array
+(_collect_data, kmeans.py:326-338) and hands it to deeptime's KMeans.fit
+(kmeans.py:211-258).  Here the frames are packed into one device-resident
+float32 tensor, kmeans++ runs as kernel (d) (km_kmpp) and the Lloyd loop as
+kernels (a)/(b) + (c), one CUDA graph launch per iteration (km_lloyd).
+"""
+import math
+import random
+
+import numpy as np
+
+from ... import _lib
+from .. import _device
+from .interface import AbstractClustering
+
+__all__ = ["KmeansClustering"]
+
+
+class KmeansClustering(AbstractClustering):
+    r"""Kmeans clustering (kmeans.py:47).
+
+    Parameters
+    ----------
+    n_clusters : int or None
+        Number of centers; None gives min(sqrt(N), 5000) for N frames.
+    max_iter : int
+        Maximum number of Lloyd iterations.
+    metric : str
+        'euclidean' (minRMSD has no kernel in this build).
+    tolerance : float
+        Stop when the relative change of the inertia
+        C(S) = sum_i sum_{x in S_i} ||x - mu_i||^2 is <= tolerance.
+    init_strategy : {'kmeans++', 'uniform'}
+    fixed_seed : bool or int
+        True -> 42, False/None -> a random seed, int in [0, 2^32-1] -> itself.
+    oom_strategy : str
+        Accepted for compatibility; device memory is checked by the caching
+        allocator instead of falling back to a memory map.
+    stride, skip : int
+        Frames used for estimation: traj[skip::stride].
+    n_jobs : int or None
+        Accepted for compatibility.
+    clustercenters : array (k, d) or None
+        Resume from these centers (init_strategy is ignored).
+    keep_data : bool
+        Keep the device copy of the frames for a later resume.
+    precision : {'auto', 'fp32', 'bf16'}
+        Distance arithmetic of the assignment step (labels are exact in all
+        cases).
+    """
+
+    def __init__(self, n_clusters, max_iter=5, metric="euclidean", tolerance=1e-5, init_strategy="kmeans++",
+                 fixed_seed=False, oom_strategy="memmap", stride=1, n_jobs=None, skip=0, clustercenters=None,
+                 keep_data=False, precision="auto"):
+        super(KmeansClustering, self).__init__(metric=metric, n_jobs=n_jobs, precision=precision)
+        if clustercenters is None:
+            clustercenters = []
+        self._in_memory_chunks_set = False
+        self._converged = False
+        self.inertias = np.zeros(0)
+        self.n_iter = 0
+        self.set_params(n_clusters=n_clusters, max_iter=max_iter, tolerance=tolerance,
+                        init_strategy=init_strategy, oom_strategy=oom_strategy, fixed_seed=fixed_seed,
+                        stride=stride, skip=skip, clustercenters=clustercenters, keep_data=keep_data)
+
+    def _param_names(self):
+        return ("n_clusters", "max_iter", "metric", "tolerance", "init_strategy", "fixed_seed", "oom_strategy",
+                "stride", "n_jobs", "skip", "clustercenters", "keep_data", "precision")
+
+    @property
+    def init_strategy(self):
+        """Strategy to get an initial guess for the centers."""
+        return self._init_strategy
+
+    @init_strategy.setter
+    def init_strategy(self, value):
+        valid = ("kmeans++", "uniform")
+        if value not in valid:
+            raise ValueError('invalid parameter "{}" for init_strategy. Should be one of {}'.format(value, valid))
+        self._init_strategy = value
+
+    @property
+    def fixed_seed(self):
+        """Seed of the initial-center draw (kmeans.py:146-164)."""
+        return self._fixed_seed
+
+    @fixed_seed.setter
+    def fixed_seed(self, val):
+        if isinstance(val, bool) or val is None:
+            self._fixed_seed = 42 if val else random.randint(0, 2 ** 32 - 1)
+        elif isinstance(val, (int, np.integer)):
+            if val < 0 or val > 2 ** 32 - 1:
+                self.logger.warning("seed has to be positive (or smaller than 2**32-1). Seed will be chosen randomly.")
+                self.fixed_seed = False
+            else:
+                self._fixed_seed = int(val)
+        else:
+            raise ValueError("fixed seed has to be bool or integer")
+
+    @property
+    def converged(self):
+        return self._converged
+
+    def describe(self):
+        return "[Kmeans, k=%i, inp_dim=%i]" % (self.n_clusters, self.data_producer.dimension())
+
+    def _check_resume_iteration(self):
+        return self.clustercenters.size != 0
+
+    # ------------------------------------------------------------------
+    def _init_in_memory_chunks(self, size, dim):
+        chunks = getattr(self, "_in_memory_chunks", None)
+        if chunks is not None and chunks.numel() == size * dim:
+            self.logger.debug("re-use in memory data.")
+            return True
+        if self._check_resume_iteration() and not self._in_memory_chunks_set and not self.keep_data:
+            self.logger.warning('Resuming kmeans iteration without the setting "keep_data=True", will re-create'
+                                ' the linear in-memory data. This is inefficient! Consider setting keep_data=True,'
+                                ' when you intend to resume the kmeans iteration.')
+        return False
+
+    def _uniform_indices(self, traj_lengths, total_length):
+        # kmeans.py:299-305: per trajectory, a share of the centers proportional to its length.
+        old = random.getstate()
+        random.seed(self.fixed_seed)
+        try:
+            return {idx: random.sample(list(range(0, traj_len)),
+                                       int(math.ceil((traj_len / float(total_length)) * self.n_clusters)))
+                    for idx, traj_len in enumerate(traj_lengths)}
+        finally:
+            random.setstate(old)
+
+    def _uniform_centers(self, trajs, indices):
+        # kmeans.py:314-324: frames in iteration order whose index was drawn, until n_clusters.
+        picked = []
+        for itraj, X in enumerate(trajs):
+            chosen = set(indices.get(itraj, ()))
+            for t in range(len(X)):
+                if len(picked) >= self.n_clusters:
+                    break
+                if t in chosen:
+                    picked.append(X[t])
+        dim = trajs[0].shape[1]
+        return np.asarray(picked).reshape(-1, dim)
+
+    def _estimate(self, source):
+        stride = self.stride if self.stride else 1
+        traj_lengths = source.trajectory_lengths(stride=stride, skip=self.skip)
+        total_length = int(sum(traj_lengths))
+        if total_length == 0:
+            raise ValueError("no frames to cluster (stride=%s, skip=%s)" % (stride, self.skip))
+        if not self.n_clusters:
+            self.n_clusters = min(int(math.sqrt(total_length)), 5000)
+            self.logger.info("The number of cluster centers was not specified, "
+                             "using min(sqrt(N), 5000)=%s as n_clusters." % self.n_clusters)
+        dim = source.dimension()
+        reuse = self._init_in_memory_chunks(total_length, dim)
+
+        if not self._check_resume_iteration() or not self._in_memory_chunks_set or not reuse:
+            trajs = source.frames(stride=stride, skip=self.skip)
+            if not self._check_resume_iteration() and self.init_strategy == "uniform":
+                indices = self._uniform_indices(traj_lengths, total_length)
+                self.clustercenters = self._uniform_centers(trajs, indices)
+            self._in_memory_chunks = _device.pack_to_device(trajs, dim)
+            self.initial_centers_ = self.clustercenters[:]
+            self._in_memory_chunks_set = True
+        else:
+            if len(self.clustercenters) != self.n_clusters:
+                raise RuntimeError("Passed clustercenters do not match n_clusters: {} vs. {}".format(
+                    len(self.clustercenters), self.n_clusters))
+
+        X = self._in_memory_chunks
+        try:
+            if self._check_resume_iteration():
+                if self.clustercenters.ndim != 2 or self.clustercenters.shape[1] != dim:
+                    raise ValueError("initial centers have shape %s, data has dimension %d"
+                                     % (self.clustercenters.shape, dim))
+                C = _device.centers_to_device(self.clustercenters)
+            else:
+                C, _ = _lib.kmpp(X, int(self.n_clusters), self.fixed_seed)
+            res = _lib.lloyd(X, C, int(self.max_iter), float(self.tolerance), precision=self.precision)
+            self.clustercenters = C.cpu().numpy()
+            self._converged = res["converged"]
+            self.inertias = res["inertias"]
+            self.n_iter = res["n_iter"]
+        finally:
+            if not self.keep_data or self._converged:
+                del self._in_memory_chunks
+                self._in_memory_chunks_set = False
+
+        if self.converged:
+            self.logger.debug("Cluster centers converged after %i steps.", self.n_iter)
+        else:
+            self.logger.warning("Algorithm did not reach convergence criterion of %g in %i iterations. "
+                                "Consider increasing max_iter.", self.tolerance, self.max_iter)
+        return self

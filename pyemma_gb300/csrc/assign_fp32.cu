@@ -1,0 +1,220 @@
+// assign_fp32.cu -- kernel (a): exact float32 nearest-center assignment on
+// the CUDA cores, and kernel (b'): exact re-evaluation of candidate lists.
+//
+// Reference: ClusterModel(centers, 'euclidean').transform(X) called from
+// pyemma/coordinates/clustering/interface.py:157-167.  The distance of frame
+// x to center c is sum_f (x_f - c_f)^2 accumulated in float32 in feature
+// order with every subtraction, product and sum rounded on its own; the
+// label is the lowest index among the minima.
+//
+// Layout: a CTA of 8 warps owns a tile of 8*FT frames; lanes own centers
+// (lane + 32 g, g < G) of a block of 32*G centers.  Frames and centers are
+// staged through shared memory in chunks of 32 features with coalesced
+// loads; every (frame, center) sum stays in one register in feature order,
+// and a lexicographic warp-shuffle (distance, index) reduction finishes the
+// argmin.
+#include "km_common.cuh"
+#include "km_internal.h"
+
+namespace km {
+
+namespace {
+
+constexpr int kWarps = 8;
+constexpr int kThreads = kWarps * 32;
+constexpr int kFC = 32;  // features per shared-memory chunk
+
+template <int FT, int G>
+__global__ void __launch_bounds__(kThreads) assign_fp32_kernel(
+    const float *__restrict__ X, const int32_t *__restrict__ frame_idx,
+    const int32_t *__restrict__ n_dev, int64_t n_max, int d, const float *__restrict__ C, int k,
+    int32_t *__restrict__ labels, float *__restrict__ dist, unsigned long long *flipped) {
+    constexpr int BM = kWarps * FT;
+    constexpr int BN = 32 * G;
+    __shared__ float Xs[BM][kFC];
+    __shared__ float Cs[BN][kFC + 1];
+
+    int64_t n = n_max;
+    if (n_dev) {
+        int64_t nd = *n_dev;
+        n = nd < n_max ? nd : n_max;
+    }
+    const int warp = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+    const int64_t ntiles = (n + BM - 1) / BM;
+    unsigned long long nflip = 0;
+
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int64_t t0 = tile * BM;
+        float bd[FT];
+        int bj[FT];
+#pragma unroll
+        for (int t = 0; t < FT; ++t) {
+            bd[t] = __int_as_float(0x7f800000);  // +inf
+            bj[t] = 0;
+        }
+        for (int cb = 0; cb < k; cb += BN) {
+            float acc[FT][G];
+#pragma unroll
+            for (int t = 0; t < FT; ++t)
+#pragma unroll
+                for (int g = 0; g < G; ++g) acc[t][g] = 0.0f;
+
+            for (int fc = 0; fc < d; fc += kFC) {
+                const int fw = min(kFC, d - fc);
+                __syncthreads();
+                for (int e = threadIdx.x; e < BM * fw; e += kThreads) {
+                    const int r = e / fw, f = e - r * fw;
+                    const int64_t i = t0 + r;
+                    float v = 0.0f;
+                    if (i < n) {
+                        const int64_t row = frame_idx ? (int64_t)frame_idx[i] : i;
+                        v = __ldg(X + row * d + fc + f);
+                    }
+                    Xs[r][f] = v;
+                }
+                for (int e = threadIdx.x; e < BN * fw; e += kThreads) {
+                    const int r = e / fw, f = e - r * fw;
+                    const int j = cb + r;
+                    Cs[r][f] = j < k ? __ldg(C + (int64_t)j * d + fc + f) : 0.0f;
+                }
+                __syncthreads();
+                for (int f = 0; f < fw; ++f) {
+                    float xv[FT], cv[G];
+#pragma unroll
+                    for (int t = 0; t < FT; ++t) xv[t] = Xs[warp * FT + t][f];
+#pragma unroll
+                    for (int g = 0; g < G; ++g) cv[g] = Cs[lane + 32 * g][f];
+#pragma unroll
+                    for (int t = 0; t < FT; ++t)
+#pragma unroll
+                        for (int g = 0; g < G; ++g) acc[t][g] = __fadd_rn(acc[t][g], sq_term(xv[t], cv[g]));
+                }
+            }
+#pragma unroll
+            for (int t = 0; t < FT; ++t)
+#pragma unroll
+                for (int g = 0; g < G; ++g) {
+                    const int j = cb + lane + 32 * g;
+                    if (j < k && acc[t][g] < bd[t]) {
+                        bd[t] = acc[t][g];
+                        bj[t] = j;
+                    }
+                }
+        }
+#pragma unroll
+        for (int t = 0; t < FT; ++t) {
+            warp_argmin(bd[t], bj[t]);
+            const int64_t i = t0 + warp * FT + t;
+            if (lane == 0 && i < n) {
+                const int64_t out = frame_idx ? (int64_t)frame_idx[i] : i;
+                if (flipped && labels[out] != bj[t]) ++nflip;
+                labels[out] = bj[t];
+                if (dist) dist[out] = bd[t];
+            }
+        }
+    }
+    if (flipped && nflip) atomicAdd(flipped, nflip);
+}
+
+template <int FT, int G>
+int launch_cfg(const float *X, const int32_t *frame_idx, const int32_t *n_dev, int64_t n, int d,
+               const float *C, int k, int32_t *labels, float *dist, unsigned long long *flipped,
+               cudaStream_t s) {
+    constexpr int BM = kWarps * FT;
+    static int per_sm = -1;  // cached: no queries while a stream is being captured
+    if (per_sm < 0) {
+        int v = 0;
+        KM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, assign_fp32_kernel<FT, G>, kThreads, 0));
+        per_sm = v;
+    }
+    int64_t ntiles = (n + BM - 1) / BM;
+    int64_t grid = (int64_t)num_sms() * (per_sm > 0 ? per_sm : 1);
+    if (grid > ntiles) grid = ntiles;
+    if (grid < 1) grid = 1;
+    assign_fp32_kernel<FT, G><<<(unsigned)grid, kThreads, 0, s>>>(X, frame_idx, n_dev, n, d, C, k,
+                                                                 labels, dist, flipped);
+    KM_CUDA(cudaGetLastError());
+    return KM_OK;
+}
+
+// Kernel (b'): one group of L threads per entry, one thread per candidate.
+__global__ void __launch_bounds__(256) recheck_candidates_kernel(
+    const float *__restrict__ X, int d, const float *__restrict__ C,
+    const int32_t *__restrict__ rc_frames, const int32_t *__restrict__ rc_cands, int L,
+    const int32_t *__restrict__ rc_count, int64_t max_entries, int32_t *__restrict__ labels,
+    unsigned long long *flipped) {
+    int64_t count = *rc_count;
+    if (count > max_entries) count = max_entries;
+    const int per_block = blockDim.x / L;
+    const int sub = threadIdx.x % L;
+    const int grp = threadIdx.x / L;
+    unsigned long long nflip = 0;
+    // Every thread runs the same number of iterations so that the shuffles
+    // below see full warps.
+    const int64_t rounds = (count + (int64_t)per_block * gridDim.x - 1) / ((int64_t)per_block * gridDim.x);
+    for (int64_t it = 0; it < rounds; ++it) {
+        const int64_t e = (it * gridDim.x + blockIdx.x) * per_block + grp;
+        float bd = __int_as_float(0x7f800000);
+        int bj = 0x7fffffff;
+        int64_t frame = -1;
+        if (e < count) {
+            frame = rc_frames[e];
+            const int j = rc_cands[e * L + sub];
+            if (j >= 0) {
+                const float dd = sqdist_exact(X + frame * d, C + (int64_t)j * d, d);
+                if (dd < __int_as_float(0x7f800000)) {  // inf and NaN never win
+                    bd = dd;
+                    bj = j;
+                }
+            }
+        }
+        for (int off = L >> 1; off > 0; off >>= 1) {
+            float od = __shfl_xor_sync(0xffffffffu, bd, off);
+            int oj = __shfl_xor_sync(0xffffffffu, bj, off);
+            if (od < bd || (od == bd && oj < bj)) {
+                bd = od;
+                bj = oj;
+            }
+        }
+        if (sub == 0 && e < count) {
+            const int lbl = bj == 0x7fffffff ? 0 : bj;  // no finite distance: label 0
+            if (labels[frame] != lbl) ++nflip;
+            labels[frame] = lbl;
+        }
+    }
+    if (flipped && nflip) atomicAdd(flipped, nflip);
+}
+
+}  // namespace
+
+int launch_assign_fp32(const float *X, const int32_t *frame_idx, const int32_t *n_dev, int64_t n,
+                       int d, const float *C, int k, int32_t *labels, float *dist,
+                       unsigned long long *flipped, cudaStream_t s) {
+    if (n == 0) return KM_OK;
+    if (k <= 32) return launch_cfg<4, 1>(X, frame_idx, n_dev, n, d, C, k, labels, dist, flipped, s);
+    if (k <= 64) return launch_cfg<4, 2>(X, frame_idx, n_dev, n, d, C, k, labels, dist, flipped, s);
+    if (k <= 128) return launch_cfg<4, 4>(X, frame_idx, n_dev, n, d, C, k, labels, dist, flipped, s);
+    return launch_cfg<4, 8>(X, frame_idx, n_dev, n, d, C, k, labels, dist, flipped, s);
+}
+
+int launch_recheck_candidates(const float *X, int d, const float *C, const int32_t *rc_frames,
+                              const int32_t *rc_cands, int L, const int32_t *rc_count,
+                              int64_t max_entries, int32_t *labels, unsigned long long *flipped,
+                              cudaStream_t s) {
+    if (max_entries == 0) return KM_OK;
+    if (L < 1 || L > 32 || (L & (L - 1))) {
+        set_error("candidate list length %d must be a power of two <= 32", L);
+        return KM_ERR_BAD_SHAPE;
+    }
+    int64_t per_block = 256 / L;
+    int64_t grid = (max_entries + per_block - 1) / per_block;
+    int64_t cap = (int64_t)num_sms() * 8;
+    if (grid > cap) grid = cap;
+    recheck_candidates_kernel<<<(unsigned)grid, 256, 0, s>>>(X, d, C, rc_frames, rc_cands, L, rc_count,
+                                                             max_entries, labels, flipped);
+    KM_CUDA(cudaGetLastError());
+    return KM_OK;
+}
+
+}  // namespace km

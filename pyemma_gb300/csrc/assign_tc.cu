@@ -1,0 +1,824 @@
+// assign_tc.cu -- kernel (b): nearest-center assignment on the tcgen05
+// tensor cores in BF16 with FP32 accumulation, followed by an exact FP32
+// recheck (kernel (b'), assign_fp32.cu) of every frame whose nearest centers
+// are not separated by the derived error bound.  The resulting labels equal
+// those of the exact FP32 kernel bit for bit.
+//
+// Reference: ClusterModel(centers, 'euclidean').transform(X),
+// pyemma/coordinates/clustering/interface.py:157-167 (and the assignment step
+// inside KMeans.fit, kmeans.py:253).
+//
+// Data flow
+//   prep: x' = x - s and c' = c - s in float32 (s = a fixed shift, the mean of
+//         the centers; squared distances are translation invariant), rounded
+//         to BF16, rows padded with zeros to kp = 64 * ceil(d/64).  Per frame
+//         (||x_hat||^2, ||x'||), per center ||c_hat||^2 and max ||c'||.
+//   main: persistent CTA per SM.  A frame tile (128 frames x kp) stays in
+//         shared memory while center tiles (BN x kp) stream through a TMA
+//         ring; one thread issues tcgen05.mma (M=128, N=BN, K=16) into one of
+//         two TMEM accumulators; four epilogue warps read the accumulator
+//         with tcgen05.ld, form e_j = ||c_hat_j||^2 - 2 x_hat.c_hat_j and keep
+//         the L smallest e_j per frame.
+//   decision: with v = ||x_hat||^2 + e an approximation of the exact float32
+//         distance D, the bound below gives an interval [lo(v), hi(v)] that
+//         holds D.  Center j can be the exact argmin only if lo(v_j) <=
+//         hi(v_min).  One candidate: final label.  2..L candidates: exact
+//         recheck of those.  More than L, or a non-finite value: exact
+//         recheck over all centers.
+//
+// Bound (u = 2^-24, ub = 2^-8, kp padded dimension, sx >= ||x'||, sc >=
+// max ||c'||):
+//   | ||x_hat - c_hat|| - ||x - c|| | <= R = (ub + 2^-23) (sx + sc)
+//   | v - ||x_hat - c_hat||^2 |       <= E = (3 kp + 8) u (sx + sc)^2
+//        (norm sums, an FP32 accumulation error of kp 2^-22 per step
+//         assumed for the tensor cores, and the epilogue roundings)
+//   | D - ||x - c||^2 |               <= g ||x - c||^2,  g = (d + 2) u / (1 - (d + 2) u)
+// so lo(v) = (1-g) max(sqrt(max(v-E, 0)) - R, 0)^2 and
+//    hi(v) = (1+g) (sqrt(v+E) + R)^2, each inflated for its own rounding.
+#include <cuda.h>
+
+#include "km_common.cuh"
+#include "km_internal.h"
+
+#include <cuda_bf16.h>
+
+#include <mutex>
+
+namespace km {
+
+namespace {
+
+constexpr int kBM = 128;          // frames per tile (UMMA M)
+constexpr int kKC = 64;           // bf16 elements per K chunk (128 B, one SW128 row)
+constexpr int kL = 4;             // candidates kept per frame
+constexpr int kThreadsTC = 192;   // warp 0 TMA, warp 1 MMA, warps 2-5 epilogue
+constexpr int kMaxNkc = 9;        // resident A tile up to kp = 576
+constexpr int kSmemLimit = 232448;
+constexpr int kABytesPerChunk = kBM * kKC * 2;  // 16 KB
+
+struct TcParams {
+    int64_t n;
+    int k;
+    int d;
+    int kp;
+    int nkc;
+    int ksteps_last;
+    int bn;
+    int stages;
+    int n_ctiles;
+    uint32_t tmem_cols;
+    float r_coef;
+    float e_coef;
+    float g_lo;   // 1 - g, deflated
+    float g_hi;   // 1 + g, inflated
+    const float2 *xnorm;
+    const float *cn2;
+    const uint32_t *cmax;
+    int32_t *labels;
+    int32_t *rc_frames;
+    int32_t *rc_cands;
+    int32_t *full_frames;
+    int32_t *counters;
+    uint32_t *err;
+};
+
+// ---------------------------------------------------------------------------
+// PTX wrappers
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void fence_mbar_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Waits for the phase of the given parity; false after kWaitLimitNs.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const uint64_t t0 = globaltimer_ns();
+    for (uint32_t spin = 1;; ++spin) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if ((spin & 255u) == 0 && globaltimer_ns() - t0 > kWaitLimitNs) return false;
+    }
+}
+
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *tm, int x, int y,
+                                            uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
+        "[%4];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(tm)), "r"(x), "r"(y), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void tmem_alloc(uint32_t *holder, uint32_t ncols) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(holder)),
+                 "r"(ncols)
+                 : "memory");
+}
+
+__device__ __forceinline__ void tmem_relinquish() {
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() {
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+
+__device__ __forceinline__ void tc_fence_after() {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t *bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                     smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+        "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+        "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+          "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]),
+          "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]),
+          "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+}
+
+__device__ __forceinline__ void tmem_wait_ld() {
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+// Shared-memory matrix descriptor: K-major operand in the 128-byte swizzle
+// layout written by TMA (8-row atoms of 128 B, atoms 1024 B apart).
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+    uint64_t desc = 0;
+    desc |= (uint64_t)((saddr & 0x3FFFFu) >> 4);  // start address
+    desc |= (uint64_t)1 << 16;                    // leading byte offset (unused for SW128 K-major)
+    desc |= (uint64_t)(1024 >> 4) << 32;          // stride byte offset: 8 rows x 128 B
+    desc |= (uint64_t)1 << 46;                    // descriptor version
+    desc |= (uint64_t)2 << 61;                    // 128-byte swizzle
+    return desc;
+}
+
+// Instruction descriptor of kind::f16: BF16 x BF16 -> F32, both K-major.
+__host__ __device__ constexpr uint32_t make_idesc(int M, int N) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+// ---------------------------------------------------------------------------
+// Prep kernels
+// ---------------------------------------------------------------------------
+__global__ void shift_mean_kernel(const float *__restrict__ C, int d, int k, float *__restrict__ shift) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= d) return;
+    double s = 0.0;
+    for (int j = 0; j < k; ++j) s += (double)C[(int64_t)j * d + f];
+    shift[f] = (float)(s / k);
+}
+
+// One warp per row: centered BF16 copy padded to kp, and the row's norms.
+// out_norm.x = ||x_hat||^2, out_norm.y = upper bound of ||x - shift||.
+__device__ __forceinline__ void convert_row(const float *__restrict__ src, int d, int kp,
+                                            const float *__restrict__ shift, __nv_bfloat16 *__restrict__ dst,
+                                            float &h2, float &s2) {
+    const int lane = threadIdx.x & 31;
+    h2 = 0.0f;
+    s2 = 0.0f;
+    __nv_bfloat162 *dst2 = reinterpret_cast<__nv_bfloat162 *>(dst);
+    for (int f = 2 * lane; f < kp; f += 64) {
+        float a = 0.0f, b = 0.0f;
+        if (f < d) a = __fsub_rn(src[f], shift[f]);
+        if (f + 1 < d) b = __fsub_rn(src[f + 1], shift[f + 1]);
+        const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+        dst2[f >> 1] = h;
+        const float ha = __low2float(h), hb = __high2float(h);
+        h2 += ha * ha + hb * hb;
+        s2 += a * a + b * b;
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        h2 += __shfl_xor_sync(0xffffffffu, h2, off);
+        s2 += __shfl_xor_sync(0xffffffffu, s2, off);
+    }
+}
+
+__global__ void prep_frames_kernel(const float *__restrict__ X, int64_t n, int d, int kp,
+                                   const float *__restrict__ shift, __nv_bfloat16 *__restrict__ xb,
+                                   float2 *__restrict__ xnorm, float norm_inflate) {
+    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t i = w; i < n; i += nw) {
+        float h2, s2;
+        convert_row(X + i * d, d, kp, shift, xb + i * kp, h2, s2);
+        if ((threadIdx.x & 31) == 0) xnorm[i] = make_float2(h2, __fsqrt_ru(s2 * norm_inflate));
+    }
+}
+
+__global__ void prep_centers_kernel(const float *__restrict__ C, int k, int k_pad, int d, int kp,
+                                    const float *__restrict__ shift, __nv_bfloat16 *__restrict__ cb,
+                                    float *__restrict__ cn2, uint32_t *__restrict__ cmax,
+                                    float norm_inflate) {
+    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t j = w; j < k_pad; j += nw) {
+        if (j < k) {
+            float h2, s2;
+            convert_row(C + j * d, d, kp, shift, cb + j * kp, h2, s2);
+            if ((threadIdx.x & 31) == 0) {
+                cn2[j] = h2;
+                const float nrm = __fsqrt_ru(s2 * norm_inflate);
+                // NaN or inf norms poison the bound on purpose (full recheck).
+                atomicMax(cmax, nrm == nrm ? __float_as_uint(nrm) : 0x7f800000u);
+            }
+        } else if ((threadIdx.x & 31) == 0) {
+            cn2[j] = __int_as_float(0x7f800000);  // padding columns never win
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Main kernel
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float lo_bound(float v, float E, float R, float g_lo) {
+    float a = __fsqrt_rd(fmaxf(__fsub_rd(v, E), 0.0f));
+    a = fmaxf(__fsub_rd(a, R), 0.0f);
+    return __fmul_rd(__fmul_rd(a, a), g_lo) - 1e-37f;
+}
+
+__device__ __forceinline__ float hi_bound(float v, float E, float R, float g_hi) {
+    float a = __fadd_ru(__fsqrt_ru(fmaxf(__fadd_ru(v, E), 0.0f)), R);
+    return __fadd_ru(__fmul_ru(__fmul_ru(a, a), g_hi), 1e-37f);
+}
+
+__global__ void __launch_bounds__(kThreadsTC, 1)
+    tc_assign_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                     const TcParams p) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    uint8_t *sA = smem;
+    uint8_t *sB = sA + p.nkc * kABytesPerChunk;
+    const int b_stage_bytes = p.bn * 128;
+    uint64_t *bars = reinterpret_cast<uint64_t *>(sB + p.stages * b_stage_bytes);
+    uint64_t *a_full = bars;
+    uint64_t *a_empty = a_full + p.nkc;
+    uint64_t *b_full = a_empty + p.nkc;
+    uint64_t *b_empty = b_full + p.stages;
+    uint64_t *acc_full = b_empty + p.stages;
+    uint64_t *acc_empty = acc_full + 2;
+    uint64_t *drain = acc_empty + 2;
+    uint32_t *tmem_holder = reinterpret_cast<uint32_t *>(drain + 1);
+    volatile uint32_t *abort_flag = tmem_holder + 1;
+
+    const int warp = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+
+    if (threadIdx.x == 0) {
+        for (int c = 0; c < p.nkc; ++c) {
+            mbar_init(&a_full[c], 1);
+            mbar_init(&a_empty[c], 1);
+        }
+        for (int s = 0; s < p.stages; ++s) {
+            mbar_init(&b_full[s], 1);
+            mbar_init(&b_empty[s], 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(&acc_full[b], 1);
+            mbar_init(&acc_empty[b], 4);
+        }
+        mbar_init(drain, 1);
+        *abort_flag = 0;
+        fence_mbar_init();
+    }
+    if (warp == 1) {
+        tmem_alloc(tmem_holder, p.tmem_cols);
+        tmem_relinquish();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem_base = *tmem_holder;
+
+    const int64_t n_ftiles = (p.n + kBM - 1) / kBM;
+
+    if (warp == 0 && lane == 0) {
+        // ---------------- TMA producer ----------------
+        uint32_t bq = 0;
+        uint32_t t_local = 0;
+        bool ok = true;
+        for (int64_t ft = blockIdx.x; ft < n_ftiles && ok; ft += gridDim.x, ++t_local) {
+            for (int ct = 0; ct < p.n_ctiles && ok; ++ct) {
+                for (int kc = 0; kc < p.nkc; ++kc) {
+                    if (ct == 0) {
+                        if (!mbar_wait(&a_empty[kc], (t_local & 1u) ^ 1u)) {
+                            ok = false;
+                            break;
+                        }
+                        mbar_arrive_expect_tx(&a_full[kc], kABytesPerChunk);
+                        tma_load_2d(sA + kc * kABytesPerChunk, &tmA, kc * kKC, (int)(ft * kBM), &a_full[kc]);
+                    }
+                    const uint32_t s = bq % p.stages;
+                    const uint32_t ph = (bq / p.stages) & 1u;
+                    if (!mbar_wait(&b_empty[s], ph ^ 1u)) {
+                        ok = false;
+                        break;
+                    }
+                    mbar_arrive_expect_tx(&b_full[s], b_stage_bytes);
+                    tma_load_2d(sB + s * b_stage_bytes, &tmB, kc * kKC, ct * p.bn, &b_full[s]);
+                    ++bq;
+                }
+                if (*abort_flag) ok = false;
+            }
+        }
+        if (!ok) {
+            atomicOr(p.err, (uint32_t)kDevTimeoutTma);
+            *abort_flag = 1;
+        }
+        // Drain: every load issued above has landed before the CTA exits.
+        if (t_local > 0 || bq > 0) {
+            const uint32_t last_a = (t_local - 1u) & 1u;
+            for (int kc = 0; kc < p.nkc && t_local > 0; ++kc) mbar_wait(&a_full[kc], last_a);
+            for (uint32_t s = 0; s < (uint32_t)p.stages && s < bq; ++s) {
+                const uint32_t last_q = bq - 1u - ((bq - 1u - s) % p.stages);
+                mbar_wait(&b_full[s], (last_q / p.stages) & 1u);
+            }
+        }
+    } else if (warp == 1 && lane == 0) {
+        // ---------------- MMA issuer ----------------
+        const uint32_t idesc = make_idesc(kBM, p.bn);
+        uint32_t bq = 0, accq = 0, t_local = 0;
+        bool ok = true;
+        for (int64_t ft = blockIdx.x; ft < n_ftiles && ok; ft += gridDim.x, ++t_local) {
+            for (int ct = 0; ct < p.n_ctiles && ok; ++ct) {
+                const uint32_t buf = accq & 1u;
+                if (!mbar_wait(&acc_empty[buf], ((accq >> 1) & 1u) ^ 1u)) {
+                    ok = false;
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t d_tmem = tmem_base + buf * (uint32_t)p.bn;
+                for (int kc = 0; kc < p.nkc; ++kc) {
+                    if (ct == 0 && !mbar_wait(&a_full[kc], t_local & 1u)) {
+                        ok = false;
+                        break;
+                    }
+                    const uint32_t s = bq % p.stages;
+                    if (!mbar_wait(&b_full[s], (bq / p.stages) & 1u)) {
+                        ok = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    const int nks = (kc == p.nkc - 1) ? p.ksteps_last : (kKC / 16);
+                    const uint32_t a0 = smem_u32(sA + kc * kABytesPerChunk);
+                    const uint32_t b0 = smem_u32(sB + s * b_stage_bytes);
+                    for (int kk = 0; kk < nks; ++kk) {
+                        mma_bf16(d_tmem, sw128_desc(a0 + kk * 32), sw128_desc(b0 + kk * 32), idesc,
+                                 (kc | kk) != 0);
+                    }
+                    mma_commit(&b_empty[s]);
+                    if (ct == p.n_ctiles - 1) mma_commit(&a_empty[kc]);
+                    ++bq;
+                }
+                if (!ok) break;
+                mma_commit(&acc_full[buf]);
+                ++accq;
+                if (*abort_flag) ok = false;
+            }
+        }
+        if (!ok) {
+            atomicOr(p.err, (uint32_t)kDevTimeoutMma);
+            *abort_flag = 1;
+        }
+        // Drain: all issued MMAs complete before TMEM is released.
+        mma_commit(drain);
+        mbar_wait(drain, 0);
+    } else if (warp >= 2) {
+        // ---------------- epilogue ----------------
+        const int quarter = warp & 3;
+        const int row = quarter * 32 + lane;
+        const uint32_t lane_off = (uint32_t)(quarter * 32) << 16;
+        const float sc = __uint_as_float(*p.cmax);
+        uint32_t accq = 0;
+        bool ok = true;
+        for (int64_t ft = blockIdx.x; ft < n_ftiles && ok; ft += gridDim.x) {
+            const int64_t i = ft * kBM + row;
+            const float2 xn = i < p.n ? p.xnorm[i] : make_float2(0.0f, 0.0f);
+            float v[kL];
+            int id[kL];
+#pragma unroll
+            for (int m = 0; m < kL; ++m) {
+                v[m] = __int_as_float(0x7f800000);
+                id[m] = -1;
+            }
+            for (int ct = 0; ct < p.n_ctiles; ++ct) {
+                const uint32_t buf = accq & 1u;
+                const bool got = __all_sync(0xffffffffu, mbar_wait(&acc_full[buf], (accq >> 1) & 1u));
+                if (!got) {
+                    ok = false;
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t tbase = tmem_base + lane_off + buf * (uint32_t)p.bn;
+                for (int cc = 0; cc < p.bn; cc += 32) {
+                    uint32_t r[32];
+                    tmem_ld32(tbase + cc, r);
+                    tmem_wait_ld();
+                    const int j0 = ct * p.bn + cc;
+                    const float4 *c4 = reinterpret_cast<const float4 *>(p.cn2 + j0);
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) {
+                        const float4 cn = __ldg(c4 + q);
+                        const float cv[4] = {cn.x, cn.y, cn.z, cn.w};
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) {
+                            const float e = fmaf(-2.0f, __uint_as_float(r[q * 4 + u]), cv[u]);
+                            if (e < v[kL - 1]) {
+                                float ev = e;
+                                int ej = j0 + q * 4 + u;
+#pragma unroll
+                                for (int m = 0; m < kL; ++m) {
+                                    if (ev < v[m]) {
+                                        const float tv = v[m];
+                                        const int tj = id[m];
+                                        v[m] = ev;
+                                        id[m] = ej;
+                                        ev = tv;
+                                        ej = tj;
+                                    }
+                                }
+                            }
+                        }
+                    }
+                }
+                tc_fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&acc_empty[buf]);
+                ++accq;
+            }
+            if (!ok) break;
+
+            // ---- decision ----
+            bool need_rc = false, need_full = false;
+            int ncand = 0;
+            if (i < p.n) {
+                const float ssum = xn.y + sc;
+                const float R = __fmul_ru(p.r_coef, ssum) + 1e-35f;
+                const float E = __fmul_ru(p.e_coef, __fmul_ru(ssum, ssum));
+                const float v0 = xn.x + v[0];
+                if (!(v0 < __int_as_float(0x7f800000)) || !(R < __int_as_float(0x7f800000)) ||
+                    !(E < __int_as_float(0x7f800000))) {
+                    need_full = true;
+                } else {
+                    const float H = hi_bound(__fadd_ru(xn.x, v[0]), E, R, p.g_hi);
+#pragma unroll
+                    for (int m = 0; m < kL; ++m) {
+                        if (v[m] < __int_as_float(0x7f800000) &&
+                            lo_bound(__fadd_rd(xn.x, v[m]), E, R, p.g_lo) <= H)
+                            ++ncand;
+                    }
+                    if (ncand == kL) need_full = true;  // more candidates may lie beyond the list
+                    else if (ncand > 1) need_rc = true;
+                }
+                p.labels[i] = id[0] >= 0 ? id[0] : 0;
+            }
+            const unsigned m_rc = __ballot_sync(0xffffffffu, need_rc);
+            if (m_rc) {
+                const int leader = __ffs(m_rc) - 1;
+                int base = 0;
+                if (lane == leader) base = atomicAdd(&p.counters[0], __popc(m_rc));
+                base = __shfl_sync(0xffffffffu, base, leader);
+                if (need_rc) {
+                    const int e = base + __popc(m_rc & ((1u << lane) - 1u));
+                    p.rc_frames[e] = (int32_t)i;
+#pragma unroll
+                    for (int m = 0; m < kL; ++m) p.rc_cands[(int64_t)e * kL + m] = m < ncand ? id[m] : -1;
+                }
+            }
+            const unsigned m_full = __ballot_sync(0xffffffffu, need_full);
+            if (m_full) {
+                const int leader = __ffs(m_full) - 1;
+                int base = 0;
+                if (lane == leader) base = atomicAdd(&p.counters[1], __popc(m_full));
+                base = __shfl_sync(0xffffffffu, base, leader);
+                if (need_full) p.full_frames[base + __popc(m_full & ((1u << lane) - 1u))] = (int32_t)i;
+            }
+            if (__any_sync(0xffffffffu, *abort_flag != 0)) ok = false;
+        }
+        if (!ok) {
+            atomicOr(p.err, (uint32_t)kDevTimeoutEpi);
+            *abort_flag = 1;
+        }
+    }
+
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        tc_fence_after();
+        tmem_dealloc(tmem_base, p.tmem_cols);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *,
+                                  CUtensorMapInterleave, CUtensorMapSwizzle, CUtensorMapL2promotion,
+                                  CUtensorMapFloatOOBfill);
+
+EncodeTiledFn get_encode() {
+    static EncodeTiledFn fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+    });
+    return fn;
+}
+
+int make_map(CUtensorMap *tm, const void *base, int64_t rows, int kp, int box_rows) {
+    EncodeTiledFn enc = get_encode();
+    if (!enc) {
+        set_error("cuTensorMapEncodeTiled is not available from the driver");
+        return KM_ERR_UNSUPPORTED;
+    }
+    cuuint64_t dims[2] = {(cuuint64_t)kp, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)kp * 2};
+    cuuint32_t box[2] = {(cuuint32_t)kKC, (cuuint32_t)box_rows};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = enc(tm, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(base), dims, strides, box, estr,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        set_error("cuTensorMapEncodeTiled failed (%d) for %lld x %d rows/box %d", (int)r, (long long)rows, kp,
+                  box_rows);
+        return KM_ERR_CUDA;
+    }
+    return KM_OK;
+}
+
+int kp_of(int d) { return (d + kKC - 1) / kKC * kKC; }
+
+int pick_bn(int k) {
+    if (k >= 256) return 256;
+    int bn = (k + 31) / 32 * 32;
+    return bn < 32 ? 32 : bn;
+}
+
+int k_pad_of(int k) { return (k + 255) / 256 * 256; }
+
+struct Plan {
+    int bn, stages, nkc, smem;
+    uint32_t tmem_cols;
+};
+
+bool make_plan(int d, int k, Plan &pl) {
+    pl.nkc = kp_of(d) / kKC;
+    if (pl.nkc > kMaxNkc) return false;
+    pl.bn = pick_bn(k);
+    const int fixed = 1024 + 512 + pl.nkc * kABytesPerChunk;
+    int stages = (kSmemLimit - fixed) / (pl.bn * 128);
+    if (stages > 6) stages = 6;
+    if (stages < 2) return false;
+    pl.stages = stages;
+    pl.smem = fixed + stages * pl.bn * 128;
+    if (pl.smem < 120 * 1024) pl.smem = 120 * 1024;  // one CTA per SM: TMEM is sized for one
+    uint32_t cols = 32;
+    while (cols < (uint32_t)(2 * pl.bn)) cols <<= 1;
+    pl.tmem_cols = cols;
+    return true;
+}
+
+bool device_is_sm10x() {
+    static int cc = -1;
+    if (cc < 0) {
+        int dev = 0, major = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
+        cc = major;
+    }
+    return cc == 10;
+}
+
+}  // namespace
+
+bool tc_plan_exists(int d, int k) {
+    Plan pl;
+    return make_plan(d, k, pl);
+}
+
+bool tc_supported(int d, int k) {
+    Plan pl;
+    return make_plan(d, k, pl) && device_is_sm10x();
+}
+
+size_t tc_frames_ws_size(int64_t n, int d) {
+    Carver c(nullptr);
+    c.take<uint16_t>((size_t)(n > 0 ? n : 1) * kp_of(d));
+    c.take<float2>(n > 0 ? n : 1);
+    return c.bytes();
+}
+
+void tc_carve_frames(void *ws, int64_t n, int d, TcBuffers &b) {
+    Carver c(ws);
+    b.kp = kp_of(d);
+    b.xb = c.take<uint16_t>((size_t)(n > 0 ? n : 1) * b.kp);
+    b.xnorm = c.take<float2>(n > 0 ? n : 1);
+}
+
+size_t tc_centers_ws_size(int d, int k) {
+    Carver c(nullptr);
+    c.take<uint16_t>((size_t)k_pad_of(k) * kp_of(d));
+    c.take<float>(k_pad_of(k));
+    c.take<float>(d);
+    c.take<uint32_t>(1);
+    return c.bytes();
+}
+
+void tc_carve_centers(void *ws, int d, int k, TcBuffers &b) {
+    Carver c(ws);
+    b.kp = kp_of(d);
+    b.cb = c.take<uint16_t>((size_t)k_pad_of(k) * b.kp);
+    b.cn2 = c.take<float>(k_pad_of(k));
+    b.shift = c.take<float>(d);
+    b.cmax = c.take<uint32_t>(1);
+}
+
+size_t tc_assign_ws_size(int64_t n, int d, int k) {
+    (void)d;
+    (void)k;
+    Carver c(nullptr);
+    const size_t nn = n > 0 ? n : 1;
+    c.take<int32_t>(nn);
+    c.take<int32_t>(nn * kL);
+    c.take<int32_t>(nn);
+    c.take<int32_t>(4);
+    c.take<unsigned long long>(1);
+    c.take<uint32_t>(1);
+    return c.bytes();
+}
+
+void tc_carve_assign(void *ws, int64_t n, int d, int k, TcBuffers &b) {
+    (void)d;
+    (void)k;
+    Carver c(ws);
+    const size_t nn = n > 0 ? n : 1;
+    b.rc_frames = c.take<int32_t>(nn);
+    b.rc_cands = c.take<int32_t>(nn * kL);
+    b.full_frames = c.take<int32_t>(nn);
+    b.counters = c.take<int32_t>(4);
+    b.flipped = c.take<unsigned long long>(1);
+    b.err = c.take<uint32_t>(1);
+}
+
+int tc_prepare_shift_from_centers(const float *C, int d, int k, TcBuffers &b, cudaStream_t s) {
+    shift_mean_kernel<<<(d + 127) / 128, 128, 0, s>>>(C, d, k, b.shift);
+    KM_CUDA(cudaGetLastError());
+    return KM_OK;
+}
+
+static float norm_inflate_of(int d) {
+    // The float32 sum of d squares is within (d+1) u of the true value.
+    return 1.0f + (float)(d + 4) * 5.9604645e-8f + 1e-6f;
+}
+
+int tc_prepare_frames(const float *X, int64_t n, int d, TcBuffers &b, cudaStream_t s) {
+    if (n == 0) return KM_OK;
+    int64_t warps = n;
+    int64_t blocks = (warps * 32 + 255) / 256;
+    const int64_t cap = (int64_t)num_sms() * 16;
+    if (blocks > cap) blocks = cap;
+    prep_frames_kernel<<<(unsigned)blocks, 256, 0, s>>>(X, n, d, b.kp, b.shift,
+                                                       reinterpret_cast<__nv_bfloat16 *>(b.xb), b.xnorm,
+                                                       norm_inflate_of(d));
+    KM_CUDA(cudaGetLastError());
+    return KM_OK;
+}
+
+int tc_prepare_centers(const float *C, int d, int k, TcBuffers &b, cudaStream_t s) {
+    const int kpad = k_pad_of(k);
+    KM_CUDA(cudaMemsetAsync(b.cmax, 0, sizeof(uint32_t), s));
+    KM_CUDA(cudaMemsetAsync(b.cb, 0, (size_t)kpad * b.kp * 2, s));
+    int64_t blocks = ((int64_t)kpad * 32 + 255) / 256;
+    const int64_t cap = (int64_t)num_sms() * 16;
+    if (blocks > cap) blocks = cap;
+    prep_centers_kernel<<<(unsigned)blocks, 256, 0, s>>>(C, k, kpad, d, b.kp, b.shift,
+                                                        reinterpret_cast<__nv_bfloat16 *>(b.cb), b.cn2, b.cmax,
+                                                        norm_inflate_of(d));
+    KM_CUDA(cudaGetLastError());
+    return KM_OK;
+}
+
+int tc_assign(const float *X, int64_t n, int d, const float *C, int k, int32_t *labels, TcBuffers &b,
+              cudaStream_t s, ProfEvents *prof) {
+    if (n == 0) return KM_OK;
+    Plan pl;
+    if (!make_plan(d, k, pl) || !device_is_sm10x()) {
+        set_error("no tensor-core plan for d=%d k=%d on this device", d, k);
+        return KM_ERR_UNSUPPORTED;
+    }
+    static std::once_flag attr_once;
+    static cudaError_t attr_err = cudaSuccess;
+    std::call_once(attr_once, [] {
+        attr_err = cudaFuncSetAttribute(tc_assign_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemLimit);
+    });
+    KM_CUDA(attr_err);
+
+    CUtensorMap tmA, tmB;
+    KM_TRY(make_map(&tmA, b.xb, n, b.kp, kBM));
+    KM_TRY(make_map(&tmB, b.cb, k_pad_of(k), b.kp, pl.bn));
+
+    KM_CUDA(cudaMemsetAsync(b.counters, 0, 4 * sizeof(int32_t), s));
+    KM_CUDA(cudaMemsetAsync(b.flipped, 0, sizeof(unsigned long long), s));
+    KM_CUDA(cudaMemsetAsync(b.err, 0, sizeof(uint32_t), s));
+
+    const double u = 5.9604644775390625e-08;  // 2^-24
+    TcParams p;
+    p.n = n;
+    p.k = k;
+    p.d = d;
+    p.kp = b.kp;
+    p.nkc = pl.nkc;
+    const int rem = d - (pl.nkc - 1) * kKC;
+    p.ksteps_last = (rem + 15) / 16;
+    p.bn = pl.bn;
+    p.stages = pl.stages;
+    p.n_ctiles = (k + pl.bn - 1) / pl.bn;
+    p.tmem_cols = pl.tmem_cols;
+    p.r_coef = (float)((1.0 / 256.0 + 2.0 * u) * 1.01);
+    p.e_coef = (float)((3.0 * b.kp + 8.0) * u * 1.02);
+    const double g = (d + 2) * u / (1.0 - (d + 2) * u) * 1.01;
+    p.g_lo = (float)((1.0 - g) * (1.0 - 4.0 * u));
+    p.g_hi = (float)((1.0 + g) * (1.0 + 4.0 * u));
+    p.xnorm = b.xnorm;
+    p.cn2 = b.cn2;
+    p.cmax = b.cmax;
+    p.labels = labels;
+    p.rc_frames = b.rc_frames;
+    p.rc_cands = b.rc_cands;
+    p.full_frames = b.full_frames;
+    p.counters = b.counters;
+    p.err = b.err;
+
+    const int64_t n_ftiles = (n + kBM - 1) / kBM;
+    int64_t grid = num_sms();
+    if (grid > n_ftiles) grid = n_ftiles;
+    if (prof) prof->begin(kProfTc, s);
+    tc_assign_kernel<<<(unsigned)grid, kThreadsTC, pl.smem, s>>>(tmA, tmB, p);
+    KM_CUDA(cudaGetLastError());
+    if (prof) prof->end(kProfTc, s);
+
+    if (prof) prof->begin(kProfRecheck, s);
+    KM_TRY(launch_recheck_candidates(X, d, C, b.rc_frames, b.rc_cands, kL, b.counters, n, labels, b.flipped, s));
+    KM_TRY(launch_assign_fp32(X, b.full_frames, b.counters + 1, n, d, C, k, labels, nullptr, b.flipped, s));
+    if (prof) prof->end(kProfRecheck, s);
+    return KM_OK;
+}
+
+}  // namespace km

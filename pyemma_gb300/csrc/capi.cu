@@ -1,0 +1,446 @@
+// capi.cu -- the extern "C" entry points of libkmgpu (declared in
+// include/kmgpu.h).  Each one validates its arguments, carves the caller's
+// workspace and enqueues kernels on the caller's stream.
+#include <cstring>
+#include <mutex>
+
+#include "km_common.cuh"
+#include "km_internal.h"
+
+namespace km {
+
+namespace {
+thread_local char g_last_error[512] = "";
+}
+
+void set_error(const char *fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_last_error, sizeof(g_last_error), fmt, ap);
+    va_end(ap);
+}
+
+namespace {
+struct ProfTotals {
+    std::mutex m;
+    bool on = false;
+    double ms[kProfKinds] = {};
+    int64_t n[kProfKinds] = {};
+} g_prof;
+}  // namespace
+
+int ProfEvents::open() {
+    {
+        std::lock_guard<std::mutex> lk(g_prof.m);
+        active = g_prof.on;
+    }
+    if (!active) return KM_OK;
+    for (int i = 0; i < kProfKinds; ++i)
+        for (int j = 0; j < 2; ++j) KM_CUDA(cudaEventCreate(&ev[i][j]));
+    return KM_OK;
+}
+
+void ProfEvents::close() {
+    for (int i = 0; i < kProfKinds; ++i)
+        for (int j = 0; j < 2; ++j)
+            if (ev[i][j]) {
+                cudaEventDestroy(ev[i][j]);
+                ev[i][j] = nullptr;
+            }
+    active = false;
+}
+
+void ProfEvents::begin(int kind, cudaStream_t s) {
+    if (!active) return;
+    cudaEventRecord(ev[kind][0], s);
+    used[kind] = true;
+}
+
+void ProfEvents::end(int kind, cudaStream_t s) {
+    if (active) cudaEventRecord(ev[kind][1], s);
+}
+
+void ProfEvents::collect() {
+    if (!active) return;
+    std::lock_guard<std::mutex> lk(g_prof.m);
+    for (int i = 0; i < kProfKinds; ++i) {
+        if (!used[i]) continue;
+        float ms = 0.0f;
+        if (cudaEventElapsedTime(&ms, ev[i][0], ev[i][1]) == cudaSuccess) {
+            g_prof.ms[i] += ms;
+            g_prof.n[i] += 1;
+        }
+    }
+}
+
+namespace {
+
+int resolve_precision(int precision, int d, int k, bool check_device) {
+    if (precision == KM_PREC_AUTO) {
+        if (d >= 64 && (check_device ? tc_supported(d, k) : tc_plan_exists(d, k)))
+            return KM_PREC_BF16;
+        return KM_PREC_FP32;
+    }
+    return precision;
+}
+
+struct AssignWs {
+    TcBuffers tc;
+};
+
+size_t assign_ws_bytes(int64_t n, int d, int k, int prec) {
+    if (prec != KM_PREC_BF16) return 0;
+    return tc_frames_ws_size(n, d) + tc_centers_ws_size(d, k) + tc_assign_ws_size(n, d, k) + 3 * 256;
+}
+
+void carve_assign(void *ws, int64_t n, int d, int k, TcBuffers &b) {
+    char *p = static_cast<char *>(ws);
+    tc_carve_frames(p, n, d, b);
+    p += (tc_frames_ws_size(n, d) + 255) / 256 * 256;
+    tc_carve_centers(p, d, k, b);
+    p += (tc_centers_ws_size(d, k) + 255) / 256 * 256;
+    tc_carve_assign(p, n, d, k, b);
+}
+
+int check_device_errors(uint32_t e) {
+    if (e & kDevBadLabel) {
+        set_error("a label is outside [0, k)");
+        return KM_ERR_BAD_LABEL;
+    }
+    if (e & (kDevTimeoutTma | kDevTimeoutMma | kDevTimeoutEpi)) {
+        set_error("a device-side wait expired (error word 0x%x)", e);
+        return KM_ERR_TIMEOUT;
+    }
+    return KM_OK;
+}
+
+int assign_impl(const float *X, int64_t n, int32_t d, const float *C, int32_t k, int32_t precision,
+                int32_t *labels, void *ws, size_t ws_bytes, km_assign_stats *stats, cudaStream_t s) {
+    KM_TRY(check_shape(n, d, k));
+    if ((n > 0 && (!X || !labels)) || !C) {
+        set_error("X, C and labels must be non-NULL");
+        return KM_ERR_BAD_SHAPE;
+    }
+    int prec = resolve_precision(precision, d, k, true);
+    if (prec != KM_PREC_FP32 && prec != KM_PREC_BF16) {
+        set_error("unknown precision %d", precision);
+        return KM_ERR_BAD_SHAPE;
+    }
+    if (prec == KM_PREC_BF16 && !tc_supported(d, k)) {
+        set_error("no tensor-core kernel for d=%d, k=%d on this device", d, k);
+        return KM_ERR_UNSUPPORTED;
+    }
+    KM_TRY(check_ws(ws, ws_bytes, assign_ws_bytes(n, d, k, prec)));
+    if (stats) {
+        std::memset(stats, 0, sizeof(*stats));
+        stats->n_frames = n;
+        stats->precision = prec;
+    }
+    if (n == 0) return KM_OK;
+    ProfEvents prof;
+    KM_TRY(prof.open());
+    struct Closer {
+        ProfEvents &p;
+        ~Closer() { p.close(); }
+    } closer{prof};
+    if (prec == KM_PREC_FP32) {
+        prof.begin(kProfFp32, s);
+        KM_TRY(launch_assign_fp32(X, nullptr, nullptr, n, d, C, k, labels, nullptr, nullptr, s));
+        prof.end(kProfFp32, s);
+        if (stats || prof.active) KM_CUDA(cudaStreamSynchronize(s));
+        prof.collect();
+        return KM_OK;
+    }
+    TcBuffers b;
+    carve_assign(ws, n, d, k, b);
+    KM_TRY(tc_prepare_shift_from_centers(C, d, k, b, s));
+    KM_TRY(tc_prepare_centers(C, d, k, b, s));
+    KM_TRY(tc_prepare_frames(X, n, d, b, s));
+    KM_TRY(tc_assign(X, n, d, C, k, labels, b, s, &prof));
+    if (prof.active) {
+        KM_CUDA(cudaStreamSynchronize(s));
+        prof.collect();
+    }
+    if (stats) {
+        int32_t cnt[2];
+        unsigned long long flips = 0;
+        uint32_t err = 0;
+        KM_CUDA(cudaMemcpyAsync(cnt, b.counters, sizeof(cnt), cudaMemcpyDeviceToHost, s));
+        KM_CUDA(cudaMemcpyAsync(&flips, b.flipped, sizeof(flips), cudaMemcpyDeviceToHost, s));
+        KM_CUDA(cudaMemcpyAsync(&err, b.err, sizeof(err), cudaMemcpyDeviceToHost, s));
+        KM_CUDA(cudaStreamSynchronize(s));
+        stats->n_recheck = cnt[0];
+        stats->n_full = cnt[1];
+        stats->n_flipped = (int64_t)flips;
+        KM_TRY(check_device_errors(err));
+    }
+    return KM_OK;
+}
+
+size_t lloyd_ws_bytes(int64_t n, int d, int k, int prec) {
+    Carver c(nullptr);
+    c.take<char>(update_ws_size(n, d, k));
+    c.take<float>((size_t)k * d);  // C_new
+    c.take<double>(1);             // cost
+    c.take<uint32_t>(1);           // error word
+    c.take<char>(assign_ws_bytes(n, d, k, prec));
+    return c.bytes();
+}
+
+}  // namespace
+}  // namespace km
+
+using namespace km;
+
+extern "C" {
+
+int km_version(void) { return 1; }
+
+const char *km_status_string(int status) {
+    switch (status) {
+        case KM_OK: return "ok";
+        case KM_ERR_BAD_SHAPE: return "bad shape or argument";
+        case KM_ERR_WORKSPACE: return "workspace too small";
+        case KM_ERR_NON_FINITE: return "non-finite input";
+        case KM_ERR_TIMEOUT: return "device wait timed out";
+        case KM_ERR_CUDA: return "CUDA error";
+        case KM_ERR_UNSUPPORTED: return "unsupported on this device";
+        case KM_ERR_BAD_LABEL: return "label out of range";
+        default: return "unknown status";
+    }
+}
+
+const char *km_last_error(void) { return g_last_error; }
+
+int km_profile_enable(int on) {
+    std::lock_guard<std::mutex> lk(g_prof.m);
+    g_prof.on = on != 0;
+    for (int i = 0; i < kProfKinds; ++i) {
+        g_prof.ms[i] = 0.0;
+        g_prof.n[i] = 0;
+    }
+    return KM_OK;
+}
+
+int km_profile_read(int32_t kind, double *ms_total, int64_t *launches) {
+    if (kind < 0 || kind >= kProfKinds || !ms_total || !launches) {
+        set_error("kind must be in [0, %d) and the outputs non-NULL", (int)kProfKinds);
+        return KM_ERR_BAD_SHAPE;
+    }
+    std::lock_guard<std::mutex> lk(g_prof.m);
+    *ms_total = g_prof.ms[kind];
+    *launches = g_prof.n[kind];
+    return KM_OK;
+}
+
+size_t km_assign_workspace_size(int64_t n, int32_t d, int32_t k, int32_t precision) {
+    if (check_shape(n, d, k) != KM_OK) return 0;
+    return assign_ws_bytes(n, d, k, resolve_precision(precision, d, k, false));
+}
+
+int km_assign(const float *X, int64_t n, int32_t d, const float *C, int32_t k, int32_t precision,
+              int32_t *labels, void *workspace, size_t workspace_bytes, km_assign_stats *stats,
+              void *stream) {
+    return assign_impl(X, n, d, C, k, precision, labels, workspace, workspace_bytes, stats,
+                       static_cast<cudaStream_t>(stream));
+}
+
+int km_batch_assign(const float *X_packed, const int64_t *offsets, int32_t n_traj, int32_t d,
+                    const float *C, int32_t k, int32_t precision, int32_t *labels_packed,
+                    void *workspace, size_t workspace_bytes, km_assign_stats *stats, void *stream) {
+    if (n_traj < 0 || (n_traj > 0 && !offsets)) {
+        set_error("n_traj must be >= 0 with n_traj+1 offsets");
+        return KM_ERR_BAD_SHAPE;
+    }
+    if (n_traj > 0 && offsets[0] != 0) {
+        set_error("offsets[0] must be 0");
+        return KM_ERR_BAD_SHAPE;
+    }
+    for (int32_t t = 0; t < n_traj; ++t) {
+        if (offsets[t + 1] < offsets[t]) {
+            set_error("offsets must be non-decreasing (trajectory %d)", t);
+            return KM_ERR_BAD_SHAPE;
+        }
+    }
+    const int64_t n = n_traj > 0 ? offsets[n_traj] : 0;
+    return assign_impl(X_packed, n, d, C, k, precision, labels_packed, workspace, workspace_bytes, stats,
+                       static_cast<cudaStream_t>(stream));
+}
+
+size_t km_update_workspace_size(int64_t n, int32_t d, int32_t k) {
+    if (check_shape(n, d, k) != KM_OK) return 0;
+    return update_ws_size(n, d, k) + 256;
+}
+
+int km_update(const float *X, int64_t n, int32_t d, const int32_t *labels, int32_t k,
+              const float *C_old, float *C_new, int64_t *counts, double *cost, void *workspace,
+              size_t workspace_bytes, void *stream) {
+    KM_TRY(check_shape(n, d, k));
+    if ((n > 0 && (!X || !labels)) || !C_old || !C_new || !cost) {
+        set_error("X, labels, C_old, C_new and cost must be non-NULL");
+        return KM_ERR_BAD_SHAPE;
+    }
+    if (C_old == C_new) {
+        set_error("C_new must not alias C_old");
+        return KM_ERR_BAD_SHAPE;
+    }
+    const size_t need = update_ws_size(n, d, k) + 256;
+    KM_TRY(check_ws(workspace, workspace_bytes, need));
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    uint32_t *err = reinterpret_cast<uint32_t *>(static_cast<char *>(workspace) + update_ws_size(n, d, k));
+    KM_CUDA(cudaMemsetAsync(err, 0, sizeof(uint32_t), s));
+    KM_TRY(launch_update(X, n, d, labels, k, C_old, C_new, counts, cost, err, workspace, s));
+    uint32_t e = 0;
+    KM_CUDA(cudaMemcpyAsync(&e, err, sizeof(e), cudaMemcpyDeviceToHost, s));
+    KM_CUDA(cudaStreamSynchronize(s));
+    return check_device_errors(e);
+}
+
+size_t km_kmpp_workspace_size(int64_t n, int32_t d, int32_t k) {
+    if (check_shape(n, d, k) != KM_OK) return 0;
+    return kmpp_ws_size(n, d, k);
+}
+
+int km_kmpp(const float *X, int64_t n, int32_t d, int32_t k, uint32_t seed, float *C0, int64_t *idx,
+            km_callback cb, void *cb_user, void *workspace, size_t workspace_bytes, void *stream) {
+    KM_TRY(check_shape(n, d, k));
+    if (n < 1 || !X || !C0) {
+        set_error("kmeans++ needs n >= 1 and non-NULL X, C0");
+        return KM_ERR_BAD_SHAPE;
+    }
+    KM_TRY(check_ws(workspace, workspace_bytes, kmpp_ws_size(n, d, k)));
+    return run_kmpp(X, n, d, k, seed, C0, idx, cb, cb_user, workspace, static_cast<cudaStream_t>(stream));
+}
+
+size_t km_lloyd_workspace_size(int64_t n, int32_t d, int32_t k, int32_t precision) {
+    if (check_shape(n, d, k) != KM_OK) return 0;
+    return lloyd_ws_bytes(n, d, k, resolve_precision(precision, d, k, false));
+}
+
+int km_lloyd(const float *X, int64_t n, int32_t d, int32_t k, float *C, int32_t max_iter,
+             double tolerance, int32_t precision, int32_t *labels, double *inertias,
+             int32_t *n_iter, int32_t *converged, km_callback cb, void *cb_user, void *workspace,
+             size_t workspace_bytes, void *stream) {
+    KM_TRY(check_shape(n, d, k));
+    if (n < 1 || !X || !C || !labels || !n_iter || !converged || max_iter < 0) {
+        set_error("km_lloyd needs n >= 1, max_iter >= 0 and non-NULL X, C, labels, n_iter, converged");
+        return KM_ERR_BAD_SHAPE;
+    }
+    *n_iter = 0;
+    *converged = 0;
+    int prec = resolve_precision(precision, d, k, true);
+    if (prec == KM_PREC_BF16 && !tc_supported(d, k)) {
+        set_error("no tensor-core kernel for d=%d, k=%d on this device", d, k);
+        return KM_ERR_UNSUPPORTED;
+    }
+    const size_t need = lloyd_ws_bytes(n, d, k, prec);
+    KM_TRY(check_ws(workspace, workspace_bytes, need));
+    if (max_iter == 0) return KM_OK;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+
+    Carver cv(workspace);
+    void *ws_update = cv.take<char>(update_ws_size(n, d, k));
+    float *C_new = cv.take<float>((size_t)k * d);
+    double *cost = cv.take<double>(1);
+    uint32_t *err = cv.take<uint32_t>(1);
+    void *ws_assign = cv.take<char>(assign_ws_bytes(n, d, k, prec));
+
+    TcBuffers b;
+    if (prec == KM_PREC_BF16) {
+        // The shift stays fixed for the whole run so that the BF16 frame copy
+        // is made once.
+        carve_assign(ws_assign, n, d, k, b);
+        KM_TRY(tc_prepare_shift_from_centers(C, d, k, b, s));
+        KM_TRY(tc_prepare_frames(X, n, d, b, s));
+    }
+    KM_CUDA(cudaMemsetAsync(err, 0, sizeof(uint32_t), s));
+
+    // One iteration: assign, update, C <- C_new.  The first iteration runs
+    // eagerly (it also performs every lazy one-time set-up); the following
+    // ones replay a CUDA graph captured from the same sequence.
+    ProfEvents prof;
+    KM_TRY(prof.open());
+    struct Closer {
+        ProfEvents &p;
+        ~Closer() { p.close(); }
+    } closer{prof};
+    auto enqueue = [&](cudaStream_t st) -> int {
+        if (prec == KM_PREC_BF16) {
+            KM_TRY(tc_prepare_centers(C, d, k, b, st));
+            KM_TRY(tc_assign(X, n, d, C, k, labels, b, st, &prof));
+        } else {
+            prof.begin(kProfFp32, st);
+            KM_TRY(launch_assign_fp32(X, nullptr, nullptr, n, d, C, k, labels, nullptr, nullptr, st));
+            prof.end(kProfFp32, st);
+        }
+        prof.begin(kProfUpdate, st);
+        KM_TRY(launch_update(X, n, d, labels, k, C, C_new, nullptr, cost, err, ws_update, st));
+        prof.end(kProfUpdate, st);
+        KM_CUDA(cudaMemcpyAsync(C, C_new, sizeof(float) * k * d, cudaMemcpyDeviceToDevice, st));
+        return KM_OK;
+    };
+
+    cudaGraphExec_t exec = nullptr;
+    int status = KM_OK;
+    double prev = 0.0;
+    for (int32_t it = 0; it < max_iter; ++it) {
+        if (it == 0) {
+            status = enqueue(s);
+        } else {
+            if (!exec) {
+                cudaStream_t cs;
+                KM_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+                cudaGraph_t graph = nullptr;
+                cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+                if (e == cudaSuccess) {
+                    status = enqueue(cs);
+                    cudaError_t e2 = cudaStreamEndCapture(cs, &graph);
+                    if (status == KM_OK && e2 != cudaSuccess) status = cuda_fail(e2, "cudaStreamEndCapture");
+                    if (status == KM_OK) {
+                        e2 = cudaGraphInstantiate(&exec, graph, 0);
+                        if (e2 != cudaSuccess) status = cuda_fail(e2, "cudaGraphInstantiate");
+                    }
+                    if (graph) cudaGraphDestroy(graph);
+                } else {
+                    status = cuda_fail(e, "cudaStreamBeginCapture");
+                }
+                cudaStreamDestroy(cs);
+                if (status != KM_OK) break;
+            }
+            cudaError_t e = cudaGraphLaunch(exec, s);
+            if (e != cudaSuccess) {
+                status = cuda_fail(e, "cudaGraphLaunch");
+                break;
+            }
+        }
+        if (status != KM_OK) break;
+        double h_cost = 0.0;
+        uint32_t h_err = 0, tc_err = 0;
+        cudaError_t e = cudaMemcpyAsync(&h_cost, cost, sizeof(double), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&h_err, err, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess && prec == KM_PREC_BF16)
+            e = cudaMemcpyAsync(&tc_err, b.err, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) {
+            status = cuda_fail(e, "Lloyd iteration");
+            break;
+        }
+        h_err |= tc_err;
+        prof.collect();
+        status = check_device_errors(h_err);
+        if (status != KM_OK) break;
+        if (inertias) inertias[it] = h_cost;
+        *n_iter = it + 1;
+        const double rel = h_cost != 0.0 ? fabs(h_cost - prev) / h_cost : 0.0;
+        prev = h_cost;
+        if (cb) cb(cb_user);
+        if (rel <= tolerance) {
+            *converged = 1;
+            break;
+        }
+    }
+    if (exec) cudaGraphExecDestroy(exec);
+    return status;
+}
+
+}  // extern "C"

@@ -1,0 +1,184 @@
+// km_common.cuh -- shared helpers of libkmgpu: status plumbing, workspace
+// carving, exact float32 distance, Philox4x32-10 and bounded device waits.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdarg>
+#include <cstdio>
+
+#include "../../include/kmgpu.h"
+
+namespace km {
+
+// ---------------------------------------------------------------------------
+// Error reporting (thread-local message, see km_last_error()).
+// ---------------------------------------------------------------------------
+void set_error(const char *fmt, ...);
+
+inline int cuda_fail(cudaError_t e, const char *what) {
+    set_error("%s: %s", what, cudaGetErrorString(e));
+    return KM_ERR_CUDA;
+}
+
+#define KM_CUDA(call)                                          \
+    do {                                                       \
+        cudaError_t _e = (call);                               \
+        if (_e != cudaSuccess) return ::km::cuda_fail(_e, #call); \
+    } while (0)
+
+#define KM_TRY(call)                \
+    do {                            \
+        int _s = (call);            \
+        if (_s != KM_OK) return _s; \
+    } while (0)
+
+// ---------------------------------------------------------------------------
+// Workspace carving: sub-buffers aligned to 256 bytes.  The same sequence of
+// take() calls is run once with base == nullptr to size the workspace.
+// ---------------------------------------------------------------------------
+struct Carver {
+    char *base;
+    size_t off = 0;
+    explicit Carver(void *b) : base(static_cast<char *>(b)) {}
+    template <typename T>
+    T *take(size_t count) {
+        off = (off + 255) & ~size_t(255);
+        T *p = base ? reinterpret_cast<T *>(base + off) : nullptr;
+        off += count * sizeof(T);
+        return p;
+    }
+    size_t bytes() const { return (off + 255) & ~size_t(255); }
+};
+
+constexpr int kMaxD = 4096;
+constexpr int kMaxK = 1 << 20;
+
+inline int check_shape(int64_t n, int32_t d, int32_t k) {
+    if (n < 0 || n >= (int64_t(1) << 31)) {
+        set_error("n=%lld out of range [0, 2^31)", (long long)n);
+        return KM_ERR_BAD_SHAPE;
+    }
+    if (d < 1 || d > kMaxD) {
+        set_error("d=%d out of range [1, %d]", d, kMaxD);
+        return KM_ERR_BAD_SHAPE;
+    }
+    if (k < 1 || k > kMaxK) {
+        set_error("k=%d out of range [1, %d]", k, kMaxK);
+        return KM_ERR_BAD_SHAPE;
+    }
+    return KM_OK;
+}
+
+inline int check_ws(void *ws, size_t have, size_t need) {
+    if (need == 0) return KM_OK;
+    if (!ws || have < need) {
+        set_error("workspace of %zu bytes given, %zu needed", have, need);
+        return KM_ERR_WORKSPACE;
+    }
+    return KM_OK;
+}
+
+inline int num_sms() {
+    static int cached = 0;
+    if (!cached) {
+        int dev = 0, v = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+        cached = v > 0 ? v : 1;
+    }
+    return cached;
+}
+
+// Device error word written by kernels whose waits ran out (bit set per site).
+enum DeviceError : uint32_t {
+    kDevTimeoutTma = 1u,
+    kDevTimeoutMma = 2u,
+    kDevTimeoutEpi = 4u,
+    kDevBadLabel = 8u,
+    kDevNonFinite = 16u,
+};
+
+// ---------------------------------------------------------------------------
+// Exact float32 squared distance in feature order, each operation rounded on
+// its own (no fused multiply-add), as the oracle and the reference's x86-64
+// build compute it.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float sq_term(float x, float c) {
+    float t = __fsub_rn(x, c);
+    return __fmul_rn(t, t);
+}
+
+__device__ __forceinline__ float sqdist_exact(const float *__restrict__ x, const float *__restrict__ c,
+                                              int d) {
+    float acc = 0.0f;
+    if ((d & 3) == 0 && ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(c)) & 15) == 0) {
+        const float4 *x4 = reinterpret_cast<const float4 *>(x);
+        const float4 *c4 = reinterpret_cast<const float4 *>(c);
+        for (int f = 0; f < (d >> 2); ++f) {
+            float4 a = __ldg(x4 + f);
+            float4 b = __ldg(c4 + f);
+            acc = __fadd_rn(acc, sq_term(a.x, b.x));
+            acc = __fadd_rn(acc, sq_term(a.y, b.y));
+            acc = __fadd_rn(acc, sq_term(a.z, b.z));
+            acc = __fadd_rn(acc, sq_term(a.w, b.w));
+        }
+    } else {
+        for (int f = 0; f < d; ++f) acc = __fadd_rn(acc, sq_term(__ldg(x + f), __ldg(c + f)));
+    }
+    return acc;
+}
+
+// Lexicographic (distance, index) minimum across a warp; NaN never wins.
+__device__ __forceinline__ void warp_argmin(float &bd, int &bj) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        float od = __shfl_xor_sync(0xffffffffu, bd, off);
+        int oj = __shfl_xor_sync(0xffffffffu, bj, off);
+        if (od < bd || (od == bd && oj < bj)) {
+            bd = od;
+            bj = oj;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Philox4x32-10 (Salmon et al., SC'11) and the kmeans++ draw of round r.
+// ---------------------------------------------------------------------------
+__host__ __device__ __forceinline__ void philox4x32_10(uint32_t c[4], uint32_t k0, uint32_t k1) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        if (r > 0) {
+            k0 += 0x9E3779B9u;
+            k1 += 0xBB67AE85u;
+        }
+        uint64_t p0 = uint64_t(0xD2511F53u) * c[0];
+        uint64_t p1 = uint64_t(0xCD9E8D57u) * c[2];
+        uint32_t n0 = uint32_t(p1 >> 32) ^ c[1] ^ k0;
+        uint32_t n2 = uint32_t(p0 >> 32) ^ c[3] ^ k1;
+        c[1] = uint32_t(p1);
+        c[3] = uint32_t(p0);
+        c[0] = n0;
+        c[2] = n2;
+    }
+}
+
+__host__ __device__ __forceinline__ uint64_t kmpp_draw(uint32_t seed, uint32_t round) {
+    uint32_t c[4] = {round, 0u, 0x6B6D7070u, 0u};
+    philox4x32_10(c, seed, 0x4B4D4750u);
+    return (uint64_t(c[0]) << 32) | uint64_t(c[1]);
+}
+
+// ---------------------------------------------------------------------------
+// Bounded waits: a spin gives up after kWaitLimitNs of wall time.
+// ---------------------------------------------------------------------------
+constexpr uint64_t kWaitLimitNs = 4000000000ull;  // 4 s
+
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+}  // namespace km

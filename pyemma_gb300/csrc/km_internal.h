@@ -1,0 +1,98 @@
+// km_internal.h -- host launchers shared between the translation units of
+// libkmgpu.  Not part of the public ABI (include/kmgpu.h is).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstddef>
+
+namespace km {
+
+// ---- profiling (capi.cu) ------------------------------------------------------
+// Event pairs recorded around the main kernels of one pass when profiling is
+// on (km_profile_enable).  Inside a captured graph the records become event
+// nodes, so every replay re-times the same launches.
+enum ProfKind { kProfTc = 0, kProfFp32 = 1, kProfRecheck = 2, kProfUpdate = 3, kProfKinds = 4 };
+
+struct ProfEvents {
+    cudaEvent_t ev[kProfKinds][2] = {};
+    bool used[kProfKinds] = {};
+    bool active = false;
+    int open();                 // creates the events when profiling is on
+    void close();
+    void begin(int kind, cudaStream_t s);
+    void end(int kind, cudaStream_t s);
+    void collect();             // after a synchronisation: adds elapsed times to the totals
+};
+
+// ---- assign_fp32.cu ------------------------------------------------------
+// Exact float32 argmin over all k centers.  With frame_idx the kernel visits
+// frames frame_idx[0..n) and writes labels[frame_idx[i]]; n_dev (nullable)
+// replaces n by a device-resident count capped at n.  flipped (nullable)
+// counts frames whose new label differs from the one already in labels.
+int launch_assign_fp32(const float *X, const int32_t *frame_idx, const int32_t *n_dev, int64_t n,
+                       int d, const float *C, int k, int32_t *labels, float *dist,
+                       unsigned long long *flipped, cudaStream_t s);
+
+// Exact float32 re-evaluation of candidate lists written by the tensor-core
+// kernel: entry e holds frame rc_frames[e] and L candidate indices
+// rc_cands[e*L .. e*L+L) (-1 = unused).  The entry count is *rc_count.
+int launch_recheck_candidates(const float *X, int d, const float *C, const int32_t *rc_frames,
+                              const int32_t *rc_cands, int L, const int32_t *rc_count,
+                              int64_t max_entries, int32_t *labels, unsigned long long *flipped,
+                              cudaStream_t s);
+
+// ---- update.cu -------------------------------------------------------------
+size_t update_ws_size(int64_t n, int d, int k);
+// Enqueues one centroid update (no host synchronisation).  err (device,
+// uint32) receives kDevBadLabel when a label is outside [0, k).
+int launch_update(const float *X, int64_t n, int d, const int32_t *labels, int k,
+                  const float *C_old, float *C_new, int64_t *counts_out, double *cost,
+                  uint32_t *err, void *ws, cudaStream_t s);
+
+// ---- kmpp.cu -----------------------------------------------------------------
+size_t kmpp_ws_size(int64_t n, int d, int k);
+int run_kmpp(const float *X, int64_t n, int d, int k, uint32_t seed, float *C0, int64_t *idx,
+             void (*cb)(void *), void *cb_user, void *ws, cudaStream_t s);
+
+// ---- assign_tc.cu ------------------------------------------------------------
+// Tensor-core (tcgen05, BF16) assignment with exact FP32 recheck.
+bool tc_supported(int d, int k);   // a plan exists and the device is sm_10x
+bool tc_plan_exists(int d, int k); // shape check only (no device query)
+size_t tc_frames_ws_size(int64_t n, int d);     // bf16 frame copy + norms
+size_t tc_centers_ws_size(int d, int k);        // bf16 centers + norms + shift
+size_t tc_assign_ws_size(int64_t n, int d, int k);  // candidate lists + counters
+
+struct TcBuffers {
+    // frames
+    void *xb = nullptr;          // n x kp bf16 (centered)
+    float2 *xnorm = nullptr;     // (||x_hat||^2, ||x'||) per frame
+    // centers
+    void *cb = nullptr;          // k x kp bf16 (centered)
+    float *cn2 = nullptr;        // ||c_hat||^2 per center
+    float *shift = nullptr;      // d floats
+    uint32_t *cmax = nullptr;    // max ||c'|| as float bits
+    // candidate lists
+    int32_t *rc_frames = nullptr;
+    int32_t *rc_cands = nullptr;
+    int32_t *full_frames = nullptr;
+    int32_t *counters = nullptr;  // [0] recheck entries, [1] full entries
+    unsigned long long *flipped = nullptr;
+    uint32_t *err = nullptr;
+    int kp = 0;
+};
+
+void tc_carve_frames(void *ws, int64_t n, int d, TcBuffers &b);
+void tc_carve_centers(void *ws, int d, int k, TcBuffers &b);
+void tc_carve_assign(void *ws, int64_t n, int d, int k, TcBuffers &b);
+
+// shift == nullptr: the shift is the mean of the centers (computed on device).
+int tc_prepare_shift_from_centers(const float *C, int d, int k, TcBuffers &b, cudaStream_t s);
+int tc_prepare_frames(const float *X, int64_t n, int d, TcBuffers &b, cudaStream_t s);
+int tc_prepare_centers(const float *C, int d, int k, TcBuffers &b, cudaStream_t s);
+// Runs the tensor-core pass, the candidate recheck and the full recheck.
+int tc_assign(const float *X, int64_t n, int d, const float *C, int k, int32_t *labels,
+              TcBuffers &b, cudaStream_t s, ProfEvents *prof = nullptr);
+
+}  // namespace km

@@ -1,0 +1,334 @@
+// update.cu -- kernel (c): centroid update and inertia in float64.
+//
+// Reference: the M-step of KMeans.fit, pyemma/coordinates/clustering/
+// kmeans.py:253-258 (new center = mean of its members; the cost function of
+// kmeans.py:71-75 evaluated for the new centers).  An empty cluster keeps its
+// previous center.
+//
+// Frames are grouped by label with a counting sort (histogram, exclusive
+// scan, warp-aggregated scatter of frame indices).  Warps then walk the
+// sorted index list in fixed-size pieces; inside a piece consecutive frames
+// mostly share a label, so per-lane float64 registers accumulate a run and
+// flush it with one atomic add per feature when the label changes.  The
+// number of global atomics is about (pieces + k) * d instead of n * d.
+//
+// Sums are taken relative to the previous center c_j of each cluster:
+//   S_j = sum (x_i - c_j),  Q_j = sum ||x_i - c_j||^2,
+//   mu_j = float(c_j + S_j / n_j),  delta_j = mu_j - c_j,
+//   inertia_j = Q_j - 2 delta_j . S_j + n_j ||delta_j||^2
+// which is sum_i ||x_i - mu_j||^2 without the cancellation of raw moments.
+#include "km_common.cuh"
+#include "km_internal.h"
+
+namespace km {
+
+namespace {
+
+constexpr int kPiece = 512;     // sorted positions per warp
+constexpr int kWideRegs = 8;    // float64 accumulators per lane in the wide pass (256 features)
+
+struct UpdateWs {
+    int32_t *counts;
+    int32_t *offsets;
+    int32_t *cursor;
+    int32_t *perm;
+    double *S;
+    double *Q;
+    double *ccost;
+};
+
+UpdateWs carve(void *ws, int64_t n, int d, int k, size_t *bytes) {
+    Carver c(ws);
+    UpdateWs u;
+    u.counts = c.take<int32_t>(k);
+    u.offsets = c.take<int32_t>((size_t)k + 1);
+    u.cursor = c.take<int32_t>(k);
+    u.perm = c.take<int32_t>(n > 0 ? n : 1);
+    u.S = c.take<double>((size_t)k * d);
+    u.Q = c.take<double>(k);
+    u.ccost = c.take<double>(k);
+    if (bytes) *bytes = c.bytes();
+    return u;
+}
+
+__global__ void count_labels_kernel(const int32_t *__restrict__ labels, int64_t n, int k,
+                                    int32_t *__restrict__ counts, uint32_t *err) {
+    const int lane = threadIdx.x & 31;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += stride) {
+        const int64_t i = base + threadIdx.x;
+        int l = i < n ? labels[i] : -1;
+        if (i < n && (l < 0 || l >= k)) {
+            atomicOr(err, (uint32_t)kDevBadLabel);
+            l = -1;
+        }
+        const unsigned peers = __match_any_sync(0xffffffffu, l);
+        if (l >= 0 && lane == __ffs(peers) - 1) atomicAdd(&counts[l], __popc(peers));
+    }
+}
+
+// Single CTA: exclusive scan of counts into offsets[0..k] and cursor.
+__global__ void __launch_bounds__(1024) scan_counts_kernel(const int32_t *__restrict__ counts, int k,
+                                                            int32_t *__restrict__ offsets,
+                                                            int32_t *__restrict__ cursor) {
+    __shared__ int32_t part[1024];
+    const int per = (k + blockDim.x - 1) / blockDim.x;
+    const int lo = threadIdx.x * per;
+    const int hi = min(lo + per, k);
+    int32_t s = 0;
+    for (int j = lo; j < hi; ++j) s += counts[j];
+    part[threadIdx.x] = s;
+    __syncthreads();
+    for (int off = 1; off < (int)blockDim.x; off <<= 1) {
+        int32_t v = threadIdx.x >= (unsigned)off ? part[threadIdx.x - off] : 0;
+        __syncthreads();
+        part[threadIdx.x] += v;
+        __syncthreads();
+    }
+    int32_t run = part[threadIdx.x] - s;
+    for (int j = lo; j < hi; ++j) {
+        offsets[j] = run;
+        cursor[j] = run;
+        run += counts[j];
+    }
+    if (threadIdx.x == blockDim.x - 1) offsets[k] = part[threadIdx.x];
+}
+
+__global__ void scatter_kernel(const int32_t *__restrict__ labels, int64_t n, int k,
+                               int32_t *__restrict__ cursor, int32_t *__restrict__ perm) {
+    const int lane = threadIdx.x & 31;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += stride) {
+        const int64_t i = base + threadIdx.x;
+        int l = i < n ? labels[i] : -1;
+        if (l >= k) l = -1;
+        const unsigned peers = __match_any_sync(0xffffffffu, l);
+        const int leader = __ffs(peers) - 1;
+        int pos = 0;
+        if (l >= 0 && lane == leader) pos = atomicAdd(&cursor[l], __popc(peers));
+        pos = __shfl_sync(0xffffffffu, pos, leader);
+        if (l >= 0) perm[pos + __popc(peers & ((1u << lane) - 1u))] = (int32_t)i;
+    }
+}
+
+// d >= 32: the whole warp walks one row at a time, lane covers features
+// f0 + lane + 32 m.  Label changes are warp-uniform.
+__global__ void seg_accumulate_wide_kernel(const float *__restrict__ X, int d,
+                                           const int32_t *__restrict__ perm,
+                                           const int32_t *__restrict__ labels, int64_t n,
+                                           const float *__restrict__ C_old, double *__restrict__ S,
+                                           double *__restrict__ Q) {
+    const int lane = threadIdx.x & 31;
+    const int64_t gwarp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int64_t npieces = (n + kPiece - 1) / kPiece;
+    for (int64_t piece = gwarp; piece < npieces; piece += nwarps) {
+        const int64_t p0 = piece * kPiece;
+        const int64_t p1 = min(p0 + kPiece, n);
+        for (int f0 = 0; f0 < d; f0 += 32 * kWideRegs) {
+            double acc[kWideRegs];
+            float cold[kWideRegs];
+            double q = 0.0;
+            int cur = -1;
+            for (int64_t p = p0; p < p1; ++p) {
+                const int64_t i = perm[p];
+                const int l = labels[i];
+                if (l != cur) {
+                    if (cur >= 0) {
+#pragma unroll
+                        for (int m = 0; m < kWideRegs; ++m) {
+                            const int f = f0 + lane + 32 * m;
+                            if (f < d) atomicAdd(&S[(int64_t)cur * d + f], acc[m]);
+                        }
+                        for (int off = 16; off > 0; off >>= 1) q += __shfl_xor_sync(0xffffffffu, q, off);
+                        if (lane == 0) atomicAdd(&Q[cur], q);
+                    }
+                    cur = l;
+                    q = 0.0;
+#pragma unroll
+                    for (int m = 0; m < kWideRegs; ++m) {
+                        const int f = f0 + lane + 32 * m;
+                        acc[m] = 0.0;
+                        cold[m] = f < d ? __ldg(C_old + (int64_t)l * d + f) : 0.0f;
+                    }
+                }
+                const float *x = X + i * d;
+#pragma unroll
+                for (int m = 0; m < kWideRegs; ++m) {
+                    const int f = f0 + lane + 32 * m;
+                    if (f < d) {
+                        const double t = (double)__ldg(x + f) - (double)cold[m];
+                        acc[m] += t;
+                        q += t * t;
+                    }
+                }
+            }
+            if (cur >= 0) {
+#pragma unroll
+                for (int m = 0; m < kWideRegs; ++m) {
+                    const int f = f0 + lane + 32 * m;
+                    if (f < d) atomicAdd(&S[(int64_t)cur * d + f], acc[m]);
+                }
+                for (int off = 16; off > 0; off >>= 1) q += __shfl_xor_sync(0xffffffffu, q, off);
+                if (lane == 0) atomicAdd(&Q[cur], q);
+            }
+        }
+    }
+}
+
+// d < 32: the warp is split into 32/DP row slots of DP lanes (DP = next
+// power of two >= d); slot s walks positions p0+s, p0+s+R, ...
+template <int DP>
+__global__ void seg_accumulate_narrow_kernel(const float *__restrict__ X, int d,
+                                             const int32_t *__restrict__ perm,
+                                             const int32_t *__restrict__ labels, int64_t n,
+                                             const float *__restrict__ C_old,
+                                             double *__restrict__ S, double *__restrict__ Q) {
+    constexpr int R = 32 / DP;
+    const int lane = threadIdx.x & 31;
+    const int slot = lane / DP;
+    const int f = lane % DP;
+    const bool fvalid = f < d;
+    const int64_t gwarp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int64_t npieces = (n + kPiece - 1) / kPiece;
+    for (int64_t piece = gwarp; piece < npieces; piece += nwarps) {
+        const int64_t p0 = piece * kPiece;
+        const int64_t p1 = min(p0 + kPiece, n);
+        double acc = 0.0, q = 0.0;
+        float cold = 0.0f;
+        int cur = -1;
+        for (int64_t p = p0 + slot; p < p1; p += R) {
+            const int64_t i = perm[p];
+            const int l = labels[i];
+            if (l != cur) {
+                if (cur >= 0 && fvalid) {
+                    atomicAdd(&S[(int64_t)cur * d + f], acc);
+                    atomicAdd(&Q[cur], q);
+                }
+                cur = l;
+                acc = 0.0;
+                q = 0.0;
+                cold = fvalid ? __ldg(C_old + (int64_t)l * d + f) : 0.0f;
+            }
+            if (fvalid) {
+                const double t = (double)__ldg(X + i * d + f) - (double)cold;
+                acc += t;
+                q += t * t;
+            }
+        }
+        if (cur >= 0 && fvalid) {
+            atomicAdd(&S[(int64_t)cur * d + f], acc);
+            atomicAdd(&Q[cur], q);
+        }
+    }
+}
+
+// One warp per cluster: new center, per-cluster inertia.
+__global__ void finalize_kernel(const double *__restrict__ S, const double *__restrict__ Q,
+                                const int32_t *__restrict__ counts, const float *__restrict__ C_old,
+                                float *__restrict__ C_new, int d, int k, double *__restrict__ ccost,
+                                int64_t *__restrict__ counts_out) {
+    const int lane = threadIdx.x & 31;
+    const int64_t j = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (j >= k) return;
+    const int cnt = counts[j];
+    const float *c = C_old + j * d;
+    float *m = C_new + j * d;
+    if (cnt == 0) {
+        for (int f = lane; f < d; f += 32) m[f] = c[f];
+        if (lane == 0) ccost[j] = 0.0;
+    } else {
+        const double dc = (double)cnt;
+        const double *s = S + j * d;
+        double cross = 0.0, sq = 0.0;
+        for (int f = lane; f < d; f += 32) {
+            const float mu = (float)((double)c[f] + s[f] / dc);
+            const double dl = (double)mu - (double)c[f];
+            cross += dl * s[f];
+            sq += dl * dl;
+            m[f] = mu;
+        }
+        for (int off = 16; off > 0; off >>= 1) {
+            cross += __shfl_xor_sync(0xffffffffu, cross, off);
+            sq += __shfl_xor_sync(0xffffffffu, sq, off);
+        }
+        if (lane == 0) ccost[j] = Q[j] - 2.0 * cross + dc * sq;
+    }
+    if (counts_out && lane == 0) counts_out[j] = cnt;
+}
+
+// Single CTA, fixed summation tree: the same inputs give the same cost.
+__global__ void __launch_bounds__(1024) reduce_cost_kernel(const double *__restrict__ ccost, int k,
+                                                            double *__restrict__ cost) {
+    __shared__ double part[1024];
+    double s = 0.0;
+    for (int j = threadIdx.x; j < k; j += blockDim.x) s += ccost[j];
+    part[threadIdx.x] = s;
+    __syncthreads();
+    for (int off = blockDim.x >> 1; off > 0; off >>= 1) {
+        if (threadIdx.x < (unsigned)off) part[threadIdx.x] += part[threadIdx.x + off];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *cost = part[0];
+}
+
+unsigned grid_for(int64_t work, int threads, int per_sm) {
+    int64_t g = (work + threads - 1) / threads;
+    int64_t cap = (int64_t)num_sms() * per_sm;
+    if (g > cap) g = cap;
+    return (unsigned)(g < 1 ? 1 : g);
+}
+
+}  // namespace
+
+size_t update_ws_size(int64_t n, int d, int k) {
+    size_t b = 0;
+    carve(nullptr, n, d, k, &b);
+    return b;
+}
+
+int launch_update(const float *X, int64_t n, int d, const int32_t *labels, int k,
+                  const float *C_old, float *C_new, int64_t *counts_out, double *cost,
+                  uint32_t *err, void *ws, cudaStream_t s) {
+    UpdateWs u = carve(ws, n, d, k, nullptr);
+    KM_CUDA(cudaMemsetAsync(u.counts, 0, sizeof(int32_t) * k, s));
+    KM_CUDA(cudaMemsetAsync(u.S, 0, sizeof(double) * (size_t)k * d, s));
+    KM_CUDA(cudaMemsetAsync(u.Q, 0, sizeof(double) * k, s));
+    if (n > 0) {
+        count_labels_kernel<<<grid_for(n, 256, 8), 256, 0, s>>>(labels, n, k, u.counts, err);
+        KM_CUDA(cudaGetLastError());
+    }
+    scan_counts_kernel<<<1, 1024, 0, s>>>(u.counts, k, u.offsets, u.cursor);
+    KM_CUDA(cudaGetLastError());
+    if (n > 0) {
+        scatter_kernel<<<grid_for(n, 256, 8), 256, 0, s>>>(labels, n, k, u.cursor, u.perm);
+        KM_CUDA(cudaGetLastError());
+        const int64_t npieces = (n + kPiece - 1) / kPiece;
+        const unsigned g = grid_for(npieces * 32, 256, 8);
+        if (d >= 32) {
+            seg_accumulate_wide_kernel<<<g, 256, 0, s>>>(X, d, u.perm, labels, n, C_old, u.S, u.Q);
+        } else if (d > 16) {
+            seg_accumulate_narrow_kernel<32><<<g, 256, 0, s>>>(X, d, u.perm, labels, n, C_old, u.S, u.Q);
+        } else if (d > 8) {
+            seg_accumulate_narrow_kernel<16><<<g, 256, 0, s>>>(X, d, u.perm, labels, n, C_old, u.S, u.Q);
+        } else if (d > 4) {
+            seg_accumulate_narrow_kernel<8><<<g, 256, 0, s>>>(X, d, u.perm, labels, n, C_old, u.S, u.Q);
+        } else if (d > 2) {
+            seg_accumulate_narrow_kernel<4><<<g, 256, 0, s>>>(X, d, u.perm, labels, n, C_old, u.S, u.Q);
+        } else if (d > 1) {
+            seg_accumulate_narrow_kernel<2><<<g, 256, 0, s>>>(X, d, u.perm, labels, n, C_old, u.S, u.Q);
+        } else {
+            seg_accumulate_narrow_kernel<1><<<g, 256, 0, s>>>(X, d, u.perm, labels, n, C_old, u.S, u.Q);
+        }
+        KM_CUDA(cudaGetLastError());
+    }
+    finalize_kernel<<<(unsigned)(((int64_t)k * 32 + 255) / 256), 256, 0, s>>>(
+        u.S, u.Q, u.counts, C_old, C_new, d, k, u.ccost, counts_out);
+    KM_CUDA(cudaGetLastError());
+    reduce_cost_kernel<<<1, 1024, 0, s>>>(u.ccost, k, cost);
+    KM_CUDA(cudaGetLastError());
+    return KM_OK;
+}
+
+}  // namespace km

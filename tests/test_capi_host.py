@@ -1,0 +1,194 @@
+"""CPU checks of the C ABI library and of the host layer (no GPU needed).
+
+libkmgpu.so must load, export every entry point include/kmgpu.h declares,
+size workspaces and reject bad arguments before touching a device.  The
+host layer must keep PyEMMA's conventions (input normalisation, lengths,
+seed and n_jobs rules) and fail loudly without a CUDA device.
+"""
+import ctypes
+import os
+import re
+from unittest import mock
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    names = []
+    for fn in os.listdir(os.path.join(ROOT, "include")):
+        if fn.endswith(".h"):
+            text = open(os.path.join(ROOT, "include", fn)).read()
+            names += re.findall(r"^\s*(?:int|size_t|const char \*)\s*(km_\w+)\s*\(", text, re.M)
+    return sorted(set(names))
+
+
+def test_header_declares_entry_points():
+    names = declared_symbols()
+    for required in ("km_assign", "km_batch_assign", "km_update", "km_kmpp", "km_lloyd"):
+        assert required in names
+
+
+def test_library_exports_every_declared_symbol(kmlib):
+    for name in declared_symbols():
+        assert hasattr(kmlib, name), name
+
+
+def test_binding_lists_every_declared_symbol():
+    from pyemma_gb300 import _lib
+    assert sorted(_lib.EXPORTED) == [n for n in declared_symbols() if n in _lib.EXPORTED]
+    assert set(declared_symbols()) <= set(_lib.EXPORTED) | {"km_assign_noalloc", "km_assign_noalloc_max"}
+
+
+def test_version_and_status_strings(kmlib):
+    assert kmlib.km_version() >= 1
+    for s in range(8):
+        assert len(kmlib.km_status_string(s)) > 0
+
+
+def test_workspace_sizes_are_host_only(kmlib):
+    assert kmlib.km_assign_workspace_size(1000, 2, 50, 0) == 0  # exact FP32 kernel needs none
+    bf16 = kmlib.km_assign_workspace_size(2_000_000, 528, 2000, 1)
+    assert bf16 >= 2_000_000 * 576 * 2  # the BF16 frame copy
+    assert kmlib.km_assign_workspace_size(2_000_000, 528, 2000, 2) == bf16  # auto picks BF16 for wide d
+    assert kmlib.km_assign_workspace_size(1000, 10, 50, 2) == 0  # auto picks FP32 for narrow d
+    assert kmlib.km_update_workspace_size(100, 3, 7) > 0
+    assert kmlib.km_kmpp_workspace_size(100, 3, 7) > 0
+    assert kmlib.km_lloyd_workspace_size(100, 3, 7, 0) >= kmlib.km_update_workspace_size(100, 3, 7)
+    # out-of-range shapes give 0
+    assert kmlib.km_assign_workspace_size(-1, 3, 7, 0) == 0
+    assert kmlib.km_assign_workspace_size(10, 0, 7, 0) == 0
+    assert kmlib.km_assign_workspace_size(10, 3, 0, 0) == 0
+
+
+def test_bad_arguments_rejected_before_device(kmlib):
+    from pyemma_gb300 import _lib
+    stats = _lib.AssignStats()
+    rc = kmlib.km_assign(None, -5, 3, None, 2, 0, None, None, 0, ctypes.byref(stats), None)
+    assert rc == _lib.KM_ERR_BAD_SHAPE
+    assert b"out of range" in kmlib.km_last_error()
+    rc = kmlib.km_assign(None, 10, 3, None, 2, 0, None, None, 0, ctypes.byref(stats), None)
+    assert rc == _lib.KM_ERR_BAD_SHAPE
+    offs = np.array([0, 5, 3], dtype=np.int64)
+    rc = kmlib.km_batch_assign(ctypes.c_void_p(16), offs.ctypes.data_as(ctypes.c_void_p), 2, 3,
+                               ctypes.c_void_p(16), 2, 0, ctypes.c_void_p(16), None, 0, None, None)
+    assert rc == _lib.KM_ERR_BAD_SHAPE
+    rc = kmlib.km_update(ctypes.c_void_p(16), 10, 3, ctypes.c_void_p(16), 2, ctypes.c_void_p(32),
+                         ctypes.c_void_p(32), None, ctypes.c_void_p(64), None, 0, None)
+    assert rc == _lib.KM_ERR_BAD_SHAPE  # C_new aliases C_old
+    rc = kmlib.km_update(ctypes.c_void_p(16), 10, 3, ctypes.c_void_p(16), 2, ctypes.c_void_p(32),
+                         ctypes.c_void_p(48), None, ctypes.c_void_p(64), None, 0, None)
+    assert rc == _lib.KM_ERR_WORKSPACE
+    n_iter, conv = ctypes.c_int32(), ctypes.c_int32()
+    rc = kmlib.km_lloyd(None, 10, 3, 2, None, 5, 1e-5, 0, None, None, ctypes.byref(n_iter), ctypes.byref(conv),
+                        _lib.CALLBACK(0), None, None, 0, None)
+    assert rc == _lib.KM_ERR_BAD_SHAPE
+
+
+# ---------------------------------------------------------------------------
+# host layer
+# ---------------------------------------------------------------------------
+def test_ensure_traj_list_conventions():
+    from pyemma_gb300.coordinates.data import InMemorySource, ensure_traj_list
+    assert ensure_traj_list(np.zeros(7))[0].shape == (7, 1)
+    assert ensure_traj_list([1.0, 2.0, 3.0])[0].shape == (3, 1)
+    assert [t.shape for t in ensure_traj_list([np.zeros((4, 2)), np.zeros((5, 2))])] == [(4, 2), (5, 2)]
+    assert ensure_traj_list(np.zeros((3, 2, 4)))[0].shape == (3, 8)
+    with pytest.raises(ValueError):
+        InMemorySource([np.zeros((4, 2)), np.zeros((4, 3))])
+    with pytest.raises(ValueError):
+        ensure_traj_list("not data")
+
+
+def test_strided_lengths():
+    from pyemma_gb300.coordinates.data import InMemorySource
+    src = InMemorySource([np.zeros((100, 3)), np.zeros((10, 3)), np.zeros((3, 3))])
+    for stride in (1, 2, 3, 7):
+        for skip in (0, 1, 5, 42):
+            want = [len(t[skip::stride]) for t in src.data]
+            assert list(src.trajectory_lengths(stride=stride, skip=skip)) == want
+            assert [len(f) for f in src.frames(stride=stride, skip=skip)] == want
+    with pytest.raises(IndexError):
+        src.trajectory_length(3)
+    assert src.default_chunksize == 256 * 1024 * 1024 // (8 * 3)
+
+
+def test_fixed_seed_rules():
+    from pyemma_gb300.coordinates import KmeansClustering
+    km = KmeansClustering(5, fixed_seed=True)
+    assert km.fixed_seed == 42
+    assert KmeansClustering(5, fixed_seed=463498).fixed_seed == 463498
+    for bad in (-1, 2 ** 32):
+        s = KmeansClustering(5, fixed_seed=bad).fixed_seed
+        assert 0 <= s <= 2 ** 32 - 1
+    assert 0 <= KmeansClustering(5, fixed_seed=False).fixed_seed <= 2 ** 32 - 1
+    with pytest.raises(ValueError):
+        KmeansClustering(5, fixed_seed="x")
+    with pytest.raises(ValueError):
+        KmeansClustering(5, init_strategy="random")
+
+
+def test_n_jobs_resolution():
+    from pyemma_gb300.coordinates import AssignCenters
+    C = np.zeros((3, 2))
+    with mock.patch.dict(os.environ, {"PYEMMA_NJOBS": "0"}):
+        assert AssignCenters(C, n_jobs=2).n_jobs == 2
+    with mock.patch.dict(os.environ, {"PYEMMA_NJOBS": "3"}):
+        assert AssignCenters(C, n_jobs=None).n_jobs == 3
+    env = {k: v for k, v in os.environ.items() if k not in ("PYEMMA_NJOBS", "SLURM_CPUS_ON_NODE")}
+    with mock.patch.dict(os.environ, env, clear=True), mock.patch("psutil.cpu_count", lambda *a, **k: 5):
+        assert AssignCenters(C).n_jobs == 5
+    env["PYEMMA_NJOBS"] = "this is not right"
+    with mock.patch.dict(os.environ, env, clear=True), mock.patch("psutil.cpu_count", lambda *a, **k: 3):
+        assert AssignCenters(C).n_jobs == 3
+    with pytest.raises(ValueError):
+        AssignCenters(C, n_jobs=0)
+
+
+def test_assign_centers_shape_errors():
+    from pyemma_gb300.coordinates import assign_to_centers
+    with pytest.raises(ValueError):
+        assign_to_centers(np.empty((100, 3)), np.empty((5, 4)))
+    with pytest.raises(ValueError):
+        assign_to_centers(np.empty((100, 3)), np.empty(1))
+    with pytest.raises(ValueError):
+        assign_to_centers(np.empty((100, 3)), None)
+
+
+def test_uniform_init_follows_reference_rule():
+    # kmeans.py:299-324: seeded random.sample per trajectory, frames taken in
+    # iteration order until n_clusters.
+    import math
+    import random
+    from pyemma_gb300.coordinates import KmeansClustering
+    trajs = [np.arange(40, dtype=np.float32)[:, None], 100 + np.arange(60, dtype=np.float32)[:, None]]
+    km = KmeansClustering(7, init_strategy="uniform", fixed_seed=11)
+    lengths = [40, 60]
+    idx = km._uniform_indices(lengths, 100)
+    state = random.getstate()
+    random.seed(11)
+    want = {i: random.sample(list(range(L)), int(math.ceil(L / 100.0 * 7))) for i, L in enumerate(lengths)}
+    random.setstate(state)
+    assert idx == want
+    centers = km._uniform_centers(trajs, idx)
+    expect = [trajs[0][t] for t in sorted(want[0])] + [trajs[1][t] for t in sorted(want[1])]
+    np.testing.assert_array_equal(centers, np.asarray(expect[:7]).reshape(-1, 1))
+
+
+def test_minrmsd_not_available():
+    from pyemma_gb300.coordinates import cluster_kmeans
+    with pytest.raises(NotImplementedError):
+        cluster_kmeans(None, k=3, metric="minRMSD")
+
+
+def test_gpu_path_fails_loudly_without_device():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a CUDA device is present")
+    from pyemma_gb300.coordinates import assign_to_centers, cluster_kmeans
+    with pytest.raises(RuntimeError):
+        assign_to_centers(np.zeros((10, 2)), np.zeros((3, 2)))
+    with pytest.raises(RuntimeError):
+        cluster_kmeans(np.zeros((10, 2)), k=2)

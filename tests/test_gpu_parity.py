@@ -1,0 +1,255 @@
+"""GPU parity: libkmgpu (through its C ABI) against the CPU oracle.
+
+Bars:
+  * labels (assign, batch assign, the tensor-core path after its recheck):
+    bit-exact against the oracle;
+  * kmeans++ chosen frames: identical;
+  * one centroid update: centers within 1e-6 relative (float64 sums in a
+    different order may move a center by one float32 ulp), counts exact,
+    inertia within 1e-9 relative;
+  * Lloyd runs: same number of iterations and convergence flag, centers
+    within 1e-5 relative, inertias within 1e-6 relative.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+RTOL_CENTER_STEP = 1e-6
+RTOL_CENTERS = 1e-5
+RTOL_INERTIA = 1e-6
+
+
+@pytest.fixture(scope="module")
+def torch():
+    import torch as _t
+    return _t
+
+
+@pytest.fixture(scope="module")
+def L():
+    from pyemma_gb300 import _lib
+    _lib.load()
+    return _lib
+
+
+def dev(torch, a):
+    return torch.from_numpy(np.ascontiguousarray(a, dtype=np.float32)).cuda()
+
+
+def gpu_assign(torch, L, X, C, precision):
+    lab, stats = L.assign(dev(torch, X), dev(torch, C), precision=precision)
+    return lab.cpu().numpy(), stats
+
+
+PRECS = ["fp32", "bf16"]
+
+
+@pytest.mark.parametrize("prec", PRECS)
+@pytest.mark.parametrize("case", ["assign", "wide", "tie", "blobs"])
+def test_golden_labels(torch, L, golden, case, prec):
+    X, C, want = golden[case + "_X"], golden[case + "_C"], golden[case + "_labels"]
+    got, stats = gpu_assign(torch, L, X, C, prec)
+    np.testing.assert_array_equal(got, want)
+    assert stats["precision"] == prec
+
+
+@pytest.mark.parametrize("prec", PRECS)
+@pytest.mark.parametrize("d", [1, 2, 3, 7, 10, 16, 31, 32, 33, 64, 100, 128, 200, 257, 528, 576])
+def test_random_shapes(torch, L, oracle, d, prec):
+    rng = np.random.default_rng(1000 + d)
+    for n, k in [(1, 1), (127, 5), (1000, 33), (4097, 257), (3000, 1000)]:
+        X = rng.normal(size=(n, d)).astype(np.float32)
+        C = (X[rng.integers(0, n, size=k)] + 0.1 * rng.normal(size=(k, d))).astype(np.float32)
+        got, _ = gpu_assign(torch, L, X, C, prec)
+        np.testing.assert_array_equal(got, oracle.assign(X, C), err_msg="n=%d k=%d d=%d" % (n, k, d))
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_duplicate_centers_ties(torch, L, oracle, prec):
+    rng = np.random.default_rng(7)
+    d = 64
+    base = rng.normal(size=(100, d)).astype(np.float32)
+    C = np.concatenate([base, base, base[::-1]])  # every center three times
+    X = np.concatenate([base, base + 0.01 * rng.normal(size=base.shape).astype(np.float32)])
+    got, stats = gpu_assign(torch, L, X, C, prec)
+    np.testing.assert_array_equal(got, oracle.assign(X, C))
+    assert got[:100].tolist() == list(range(100))  # exact hits go to the lowest duplicate
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_offset_data_bound(torch, L, oracle, prec):
+    # Large common offset with small spread: the stress case of the BF16 bound.
+    rng = np.random.default_rng(11)
+    X = (1.0e4 + 1e-2 * rng.normal(size=(5000, 128))).astype(np.float32)
+    C = X[rng.choice(5000, 300, replace=False)].copy()
+    got, stats = gpu_assign(torch, L, X, C, prec)
+    np.testing.assert_array_equal(got, oracle.assign(X, C))
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_non_finite_frames(torch, L, oracle, prec):
+    rng = np.random.default_rng(12)
+    X = rng.normal(size=(300, 96)).astype(np.float32)
+    X[5, 3] = np.nan
+    X[17, :] = np.nan
+    X[40, 0] = np.inf
+    X[41, 7] = -np.inf
+    C = rng.normal(size=(20, 96)).astype(np.float32)
+    got, _ = gpu_assign(torch, L, X, C, prec)
+    np.testing.assert_array_equal(got, oracle.assign(X, C))
+
+
+def test_empty_input(torch, L):
+    X = torch.empty((0, 8), dtype=torch.float32, device="cuda")
+    C = torch.ones((3, 8), dtype=torch.float32, device="cuda")
+    for prec in PRECS:
+        lab, stats = L.assign(X, C, precision=prec)
+        assert lab.numel() == 0 and stats["n_frames"] == 0
+
+
+def test_bad_shapes_raise(torch, L):
+    X = torch.ones((10, 4), dtype=torch.float32, device="cuda")
+    with pytest.raises(ValueError):
+        L.assign(X, torch.ones((3, 5), dtype=torch.float32, device="cuda"))
+    with pytest.raises(L.KmError):
+        L.assign(X, torch.ones((0, 4), dtype=torch.float32, device="cuda"))
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_batch_assign_uneven(torch, L, oracle, prec):
+    rng = np.random.default_rng(13)
+    lengths = [0, 1, 1000, 37, 5000, 0, 129]
+    trajs = [rng.normal(size=(t, 72)).astype(np.float32) for t in lengths]
+    C = rng.normal(size=(64, 72)).astype(np.float32)
+    Xp = np.concatenate(trajs)
+    offsets = np.concatenate([[0], np.cumsum(lengths)])
+    lab, stats = L.batch_assign(dev(torch, Xp), offsets, dev(torch, C), precision=prec)
+    np.testing.assert_array_equal(lab.cpu().numpy(), oracle.assign(Xp, C))
+
+
+def test_update_matches_oracle(torch, L, oracle, golden):
+    X, C, lab = golden["assign_X"], golden["assign_C"], golden["assign_labels"]
+    Cn, counts, cost = L.update(dev(torch, X), torch.from_numpy(lab).cuda(), dev(torch, C))
+    np.testing.assert_allclose(Cn.cpu().numpy(), golden["update_C"], rtol=RTOL_CENTER_STEP, atol=0)
+    np.testing.assert_array_equal(counts.cpu().numpy(), golden["update_counts"])
+    assert abs(cost - golden["update_cost"][0]) <= 1e-9 * golden["update_cost"][0]
+
+
+@pytest.mark.parametrize("d", [1, 2, 10, 31, 32, 100, 528])
+def test_update_shapes(torch, L, oracle, d):
+    rng = np.random.default_rng(50 + d)
+    n, k = 20000, 97
+    X = (5.0 + rng.normal(size=(n, d))).astype(np.float32)
+    C = X[:k].copy()
+    C[3] = 1e6  # an empty cluster keeps its center
+    lab = oracle.assign(X, C)
+    Cn_ref, cnt_ref, cost_ref, _ = oracle.update(X, lab, C)
+    Cn, counts, cost = L.update(dev(torch, X), torch.from_numpy(lab).cuda(), dev(torch, C))
+    np.testing.assert_allclose(Cn.cpu().numpy(), Cn_ref, rtol=RTOL_CENTER_STEP, atol=0)
+    np.testing.assert_array_equal(Cn.cpu().numpy()[3], C[3])
+    np.testing.assert_array_equal(counts.cpu().numpy(), cnt_ref)
+    assert abs(cost - cost_ref) <= 1e-9 * cost_ref
+
+
+def test_update_sorted_labels_long_runs(torch, L, oracle):
+    # Long runs of equal labels (time-correlated trajectories) stress the run flushes.
+    rng = np.random.default_rng(77)
+    n, d, k = 200000, 10, 50
+    lab = np.repeat(rng.integers(0, k, size=n // 5000), 5000).astype(np.int32)
+    X = rng.normal(size=(n, d)).astype(np.float32)
+    C = rng.normal(size=(k, d)).astype(np.float32)
+    Cn_ref, cnt_ref, cost_ref, _ = oracle.update(X, lab, C)
+    Cn, counts, cost = L.update(dev(torch, X), torch.from_numpy(lab).cuda(), dev(torch, C))
+    np.testing.assert_allclose(Cn.cpu().numpy(), Cn_ref, rtol=RTOL_CENTER_STEP, atol=1e-7)
+    np.testing.assert_array_equal(counts.cpu().numpy(), cnt_ref)
+    assert abs(cost - cost_ref) <= 1e-9 * cost_ref
+
+
+def test_update_bad_label_raises(torch, L):
+    X = torch.ones((10, 3), dtype=torch.float32, device="cuda")
+    C = torch.zeros((2, 3), dtype=torch.float32, device="cuda")
+    lab = torch.zeros(10, dtype=torch.int32, device="cuda")
+    lab[4] = 2
+    with pytest.raises(L.KmError) as e:
+        L.update(X, lab, C)
+    assert e.value.status == L.KM_ERR_BAD_LABEL
+
+
+def test_kmpp_golden(torch, L, golden):
+    X = golden["kmpp_X"]
+    C0, idx = L.kmpp(dev(torch, X), 20, int(golden["kmpp_seed"][0]))
+    np.testing.assert_array_equal(idx.cpu().numpy(), golden["kmpp_idx"])
+    np.testing.assert_array_equal(C0.cpu().numpy(), X[golden["kmpp_idx"]])
+
+
+@pytest.mark.parametrize("n,d,k,seed", [(1, 3, 1, 0), (5, 2, 5, 1), (3000, 2, 50, 42), (10000, 10, 200, 7),
+                                        (4100, 528, 30, 3), (2049, 7, 64, 2 ** 32 - 1)])
+def test_kmpp_matches_oracle(torch, L, oracle, n, d, k, seed):
+    rng = np.random.default_rng(seed % 1000)
+    X = rng.normal(size=(n, d)).astype(np.float32)
+    _, idx_ref = oracle.kmpp(X, k, seed)
+    calls = []
+    C0, idx = L.kmpp(dev(torch, X), k, seed, callback=lambda: calls.append(1))
+    np.testing.assert_array_equal(idx.cpu().numpy(), idx_ref)
+    assert len(calls) == k
+
+
+def test_kmpp_duplicates(torch, L, oracle):
+    X = np.ones((100, 4), dtype=np.float32)
+    X[50:] = 2.0
+    _, idx_ref = oracle.kmpp(X, 6, 5)
+    _, idx = L.kmpp(dev(torch, X), 6, 5)
+    np.testing.assert_array_equal(idx.cpu().numpy(), idx_ref)
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_lloyd_golden(torch, L, golden, prec):
+    X, C0 = golden["lloyd_X"], golden["lloyd_C0"]
+    C = dev(torch, C0)
+    calls = []
+    r = L.lloyd(dev(torch, X), C, 100, 1e-5, precision=prec if X.shape[1] >= 2 else "fp32",
+                callback=lambda: calls.append(1))
+    assert r["n_iter"] == golden["lloyd_n_iter"][0]
+    assert int(r["converged"]) == golden["lloyd_converged"][0]
+    assert len(calls) == r["n_iter"]
+    np.testing.assert_allclose(C.cpu().numpy(), golden["lloyd_C"], rtol=RTOL_CENTERS, atol=1e-6)
+    np.testing.assert_allclose(r["inertias"], golden["lloyd_inertias"], rtol=RTOL_INERTIA)
+
+
+@pytest.mark.parametrize("prec", PRECS)
+@pytest.mark.parametrize("d,k", [(10, 100), (64, 64), (528, 40)])
+def test_lloyd_matches_oracle(torch, L, oracle, prec, d, k):
+    from pyemma_gb300 import datasets
+    X = datasets.gaussian_mixture(20000, d, 2 * k, 0.3, 5.0, seed=d)
+    C0, _ = oracle.kmpp(X, k, 9)
+    ref = oracle.lloyd(X, C0, 30, 1e-5)
+    C = dev(torch, C0)
+    r = L.lloyd(dev(torch, X), C, 30, 1e-5, precision=prec)
+    assert r["n_iter"] == ref["n_iter"] and r["converged"] == ref["converged"]
+    np.testing.assert_allclose(C.cpu().numpy(), ref["centers"], rtol=RTOL_CENTERS, atol=1e-5)
+    np.testing.assert_allclose(r["inertias"], ref["inertias"], rtol=RTOL_INERTIA)
+    np.testing.assert_array_equal(r["labels"].cpu().numpy(), ref["labels"])
+
+
+def test_lloyd_zero_iterations(torch, L):
+    X = torch.ones((10, 3), dtype=torch.float32, device="cuda")
+    C = torch.zeros((2, 3), dtype=torch.float32, device="cuda")
+    r = L.lloyd(X, C, 0, 1e-5)
+    assert r["n_iter"] == 0 and not r["converged"]
+    assert float(C.abs().sum()) == 0.0
+
+
+def test_full_size_wide_bf16_equals_fp32(torch, L, oracle):
+    """2,000,000 x 528 Calpha distances, k=2000: tensor-core labels equal the exact kernel's."""
+    from pyemma_gb300 import datasets
+    X = datasets.calpha_distances(2_000_000, seed=3, device="cuda")
+    rng = np.random.default_rng(3)
+    C = X[torch.from_numpy(rng.choice(X.shape[0], 2000, replace=False)).cuda()].contiguous()
+    lab32, _ = L.assign(X, C, precision="fp32")
+    lab16, stats = L.assign(X, C, precision="bf16")
+    assert torch.equal(lab32, lab16)
+    assert stats["n_recheck"] + stats["n_full"] < X.shape[0]
+    sample = rng.choice(X.shape[0], 2000, replace=False)
+    Xs = X[torch.from_numpy(sample).cuda()].cpu().numpy()
+    np.testing.assert_array_equal(lab16.cpu().numpy()[sample], oracle.assign(Xs, C.cpu().numpy()))

@@ -1,0 +1,187 @@
+"""Pins the CPU oracle to the known answers of the reference's own tests.
+
+The reference's k-means arithmetic (deeptime) is absent, so the oracle is a
+restatement; these tests re-express the reference's known-answer tests with
+freshly generated inputs and run them against it.  Each test names the
+reference test it follows.
+"""
+import numpy as np
+import pytest
+
+
+def _kmeans(O, X, k, seed=42, max_iter=10, tol=1e-5, C0=None):
+    X = np.asarray(X, dtype=np.float32)
+    if X.ndim == 1:
+        X = X[:, None]
+    if C0 is None:
+        C0, _ = O.kmpp(X, k, seed)
+    return O.lloyd(X, np.asarray(C0, dtype=np.float32), max_iter, tol)
+
+
+def test_philox_known_answers(oracle, golden):
+    for c, k, o in zip(golden["philox_ctr"], golden["philox_key"], golden["philox_out"]):
+        assert oracle.philox4x32_10(list(c), list(k)) == list(o)
+
+
+def test_assign_five_blobs_exact(oracle):
+    # test_assign.py:50-78,102-109: dtraj[i] == i // 1000 for separated blobs.
+    rng = np.random.default_rng(1)
+    means = np.array([[-3, 0], [-1, 1], [0, 0], [1, -1], [4, 2]], dtype=float)
+    X = np.zeros((5000, 2))
+    for i in range(5):
+        X[i * 1000:(i + 1) * 1000] = 0.1 * rng.normal(size=(1000, 2)) + means[i]
+    labels = oracle.assign(X, means.astype(np.float32))
+    assert labels.dtype == np.int32
+    np.testing.assert_array_equal(labels, np.arange(5000) // 1000)
+
+
+def test_assign_thread_invariance(oracle):
+    # test_assign.py:232-239: multithreaded == single-threaded assignment.
+    rng = np.random.default_rng(2)
+    X = rng.normal(size=(5000, 2)).astype(np.float32)
+    C = X[rng.choice(5000, 100)]
+    np.testing.assert_array_equal(oracle.assign(X, C, n_threads=1), oracle.assign(X, C, n_threads=4))
+
+
+def test_kmeans_k1_cube_is_origin(oracle):
+    # test_kmeans.py:154-166: k=1 on the 8 cube corners gives exactly (0,0,0).
+    X = np.array([[1, 1, 1], [1, 1, -1], [1, -1, -1], [-1, -1, -1], [-1, 1, 1], [-1, -1, 1], [-1, 1, -1],
+                  [1, -1, 1]], dtype=np.float32)
+    r = _kmeans(oracle, X, 1)
+    np.testing.assert_equal(r["centers"].squeeze(), np.zeros(3))
+
+
+def test_kmeans_outlier_converges(oracle):
+    # test_kmeans.py:168-179: from (+-2,0,0), max_iter=500, all |centers| <= 1.
+    X = np.array([[1, 1.5, 1], [1, 1, -1], [1, -1, -1], [-1, -1, -1], [-1, 1, 1], [-1, -1, 1], [-1, 1, -1],
+                  [1, -1, 1]], dtype=np.float32)
+    r = _kmeans(oracle, X, 2, C0=[[2, 0, 0], [-2, 0, 0]], max_iter=500)
+    assert np.all(np.abs(r["centers"]) <= 1)
+
+
+def test_kmeans_convex_hull(oracle):
+    # test_kmeans.py:181-233: the k=1 center is the mean, inside the hull.
+    rng = np.random.default_rng(3)
+    P = rng.normal(size=(24, 3)).astype(np.float32)
+    r = _kmeans(oracle, P, 1)
+    np.testing.assert_allclose(r["centers"][0], P.astype(np.float64).mean(0), rtol=0, atol=1e-6)
+
+
+def test_kmeans_trivial_blocks_exact(oracle):
+    # test_kmeans.py:411-426: four constant blocks -> centers exactly 30/60/90/120.
+    X = np.zeros((40000, 4), dtype=np.float32)
+    for b, v in enumerate((30.0, 60.0, 90.0, 120.0)):
+        X[b * 10000:(b + 1) * 10000] = v
+    r = _kmeans(oracle, X, 4, seed=42)
+    found = sorted(float(c[0]) for c in r["centers"] if np.all(c == c[0]))
+    assert found == [30.0, 60.0, 90.0, 120.0]
+
+
+def test_kmeans_seeded_determinism(oracle):
+    # test_kmeans.py:64-102: same seed -> identical initial and final centers.
+    rng = np.random.default_rng(42)
+    X = np.hstack([rng.normal(size=200) - 2.0, rng.normal(size=200), rng.normal(size=200) + 2.0])[:, None]
+    X = X.astype(np.float32)
+    for seed in (42, 463498):
+        a, ia = oracle.kmpp(X, 50, seed)
+        b, ib = oracle.kmpp(X, 50, seed)
+        np.testing.assert_equal(a, b)
+        ra = _kmeans(oracle, X, 50, C0=a, max_iter=100)
+        rb = _kmeans(oracle, X, 50, C0=b, max_iter=100)
+        np.testing.assert_allclose(ra["centers"], rb["centers"], atol=1e-6)
+        cc = ra["centers"]
+        assert np.all(np.isfinite(cc)) and np.any((cc > -1.0) & (cc < 1.0))
+
+
+def test_kmeans_serial_equals_parallel(oracle):
+    # test_kmeans.py:104-128: n_jobs=1 and n_jobs=2 give the same centers.
+    rng = np.random.default_rng(45)
+    means = rng.uniform(-10, 10, size=(6, 2))
+    X = np.concatenate([m + 0.5 * rng.normal(size=(84, 2)) for m in means]).astype(np.float32)
+    C0, _ = oracle.kmpp(X, 6, 7)
+    a = oracle.lloyd(X, C0, 50, 1e-5, n_threads=1)
+    b = oracle.lloyd(X, C0, 50, 1e-5, n_threads=2)
+    np.testing.assert_allclose(a["centers"], b["centers"], atol=1e-4)
+
+
+def test_kmeans_resume_reduces_error(oracle):
+    # test_kmeans.py:357-374: resuming from 1-iteration centers moves them towards (-2, 0, 2).
+    rng = np.random.default_rng(32)
+    X = np.hstack([rng.normal(size=1000) - 2.0, rng.normal(size=1000), rng.normal(size=1000) + 2.0])
+    X = X[:, None].astype(np.float32)
+    r1 = oracle.lloyd(X, np.array([[20], [42], [-29]], dtype=np.float32), 1, 1e-5)
+    r2 = oracle.lloyd(X, r1["centers"], 50, 1e-5)
+    true = np.array([-2, 0, 2])
+    d0 = np.linalg.norm(true - np.sort(r1["centers"].ravel()))
+    d1 = np.linalg.norm(true - np.sort(r2["centers"].ravel()))
+    assert d1 < d0
+
+
+def test_stopping_rule_first_iteration(oracle):
+    # kmeans.py:432-436: prev starts at 0, so the first iteration never converges
+    # unless the inertia is 0.
+    X = np.array([[0.0], [0.0], [5.0], [5.0]], dtype=np.float32)
+    r = oracle.lloyd(X, np.array([[0.0], [5.0]], dtype=np.float32), 10, 1e-5)
+    assert r["n_iter"] == 1 and r["converged"] and r["inertias"][0] == 0.0
+    X2 = np.array([[0.0], [1.0], [5.0], [6.0]], dtype=np.float32)
+    r2 = oracle.lloyd(X2, np.array([[0.0], [5.0]], dtype=np.float32), 10, 1e-5)
+    assert r2["n_iter"] == 2 and r2["converged"]
+    np.testing.assert_allclose(r2["inertias"], [1.0, 1.0])
+
+
+def test_empty_cluster_keeps_center(oracle):
+    X = np.array([[0.0, 0.0], [0.1, 0.0]], dtype=np.float32)
+    C = np.array([[0.0, 0.0], [100.0, 100.0]], dtype=np.float32)
+    labels = oracle.assign(X, C)
+    Cn, counts, cost, _ = oracle.update(X, labels, C)
+    assert counts.tolist() == [2, 0]
+    np.testing.assert_array_equal(Cn[1], C[1])
+
+
+def test_update_matches_float64_reference(oracle):
+    rng = np.random.default_rng(5)
+    X = (1000.0 + rng.normal(size=(4000, 9))).astype(np.float32)
+    C = X[:30].copy()
+    lab = oracle.assign(X, C)
+    Cn, counts, cost, _ = oracle.update(X, lab, C)
+    C64, cnt = oracle.centers_fp64(X, lab, C)
+    np.testing.assert_allclose(Cn, C64, rtol=1e-7, atol=0)
+    np.testing.assert_array_equal(counts, cnt.astype(np.int64))
+    assert abs(cost - oracle.inertia_fp64(X, lab, Cn)) <= 1e-9 * cost
+
+
+def test_kmpp_spreads_centers(oracle):
+    # D^2 sampling on 4 far-apart tight blobs picks one center per blob.
+    rng = np.random.default_rng(9)
+    means = np.array([[0, 0], [100, 0], [0, 100], [100, 100]], dtype=float)
+    X = np.concatenate([m + 0.01 * rng.normal(size=(500, 2)) for m in means]).astype(np.float32)
+    for seed in range(5):
+        C, idx = oracle.kmpp(X, 4, seed)
+        assert sorted(set(int(i) // 500 for i in idx)) == [0, 1, 2, 3]
+
+
+def test_kmpp_duplicate_data_falls_back_to_uniform(oracle):
+    X = np.ones((50, 3), dtype=np.float32)
+    C, idx = oracle.kmpp(X, 5, 11)
+    assert C.shape == (5, 3) and np.all(C == 1.0)
+    assert np.all((idx >= 0) & (idx < 50))
+
+
+def test_quant_exponent_bounds(oracle):
+    for M, n in [(1.0, 1), (3.5, 1000), (1e-30, 2 ** 31 - 1), (1e30, 7), (1.4e-45, 100)]:
+        e = oracle.quant_exponent(M, n)
+        M = float(np.float32(M))
+        L = int(np.ceil(np.log2(n))) if n > 1 else 0
+        assert M * 2.0 ** e < 2.0 ** (62 - L)
+        assert M * 2.0 ** e >= 2.0 ** (61 - L)
+
+
+@pytest.mark.parametrize("d", [1, 2, 3, 8, 9, 33])
+def test_assign_matches_sequential_numpy(oracle, d):
+    rng = np.random.default_rng(d)
+    X = rng.normal(size=(500, d)).astype(np.float32)
+    C = rng.normal(size=(19, d)).astype(np.float32)
+    D = oracle.sqdist_fp32_sequential(X, C)
+    lab, dist = oracle.assign(X, C, return_dist=True)
+    np.testing.assert_array_equal(lab, np.argmin(D, axis=1))
+    np.testing.assert_array_equal(dist, D.min(axis=1))
