@@ -111,8 +111,11 @@ def get_n_jobs(logger=None):
     """n_jobs from SLURM_CPUS_ON_NODE, PYEMMA_NJOBS or the logical CPU count."""
 
     def _from_hardware():
-        import psutil
-        count = psutil.cpu_count(logical=True)
+        try:
+            import psutil
+            count = psutil.cpu_count(logical=True)
+        except ImportError:
+            count = os.cpu_count()
         return count if count is not None else 1
 
     def _from_env(var):

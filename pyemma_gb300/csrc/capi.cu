@@ -50,14 +50,16 @@ void ProfEvents::close() {
     active = false;
 }
 
+// cudaEventRecordExternal makes a capturing stream add an event-record node
+// to the graph (a plain record would only be a capture dependency).
 void ProfEvents::begin(int kind, cudaStream_t s) {
     if (!active) return;
-    cudaEventRecord(ev[kind][0], s);
+    cudaEventRecordWithFlags(ev[kind][0], s, cudaEventRecordExternal);
     used[kind] = true;
 }
 
 void ProfEvents::end(int kind, cudaStream_t s) {
-    if (active) cudaEventRecord(ev[kind][1], s);
+    if (active) cudaEventRecordWithFlags(ev[kind][1], s, cudaEventRecordExternal);
 }
 
 void ProfEvents::collect() {
@@ -69,6 +71,8 @@ void ProfEvents::collect() {
         if (cudaEventElapsedTime(&ms, ev[i][0], ev[i][1]) == cudaSuccess) {
             g_prof.ms[i] += ms;
             g_prof.n[i] += 1;
+        } else {
+            cudaGetLastError();  // a failed read must not surface at the next launch check
         }
     }
 }

@@ -253,3 +253,23 @@ def test_full_size_wide_bf16_equals_fp32(torch, L, oracle):
     sample = rng.choice(X.shape[0], 2000, replace=False)
     Xs = X[torch.from_numpy(sample).cuda()].cpu().numpy()
     np.testing.assert_array_equal(lab16.cpu().numpy()[sample], oracle.assign(Xs, C.cpu().numpy()))
+
+
+def test_profile_counts_graph_replays(torch, L):
+    rng = np.random.default_rng(21)
+    X = dev(torch, rng.normal(size=(20000, 96)))
+    C0 = X[:40].clone()
+    L.profile_enable(True)
+    try:
+        C = C0.clone()
+        L.lloyd(X, C, 6, -1.0, precision="bf16")
+        C = C0.clone()
+        L.lloyd(X, C, 4, -1.0, precision="fp32")
+        prof = L.profile_read()
+    finally:
+        L.profile_enable(False)
+    assert prof["tc"][1] == 6 and prof["tc"][0] > 0
+    assert prof["fp32"][1] == 4 and prof["fp32"][0] > 0
+    assert prof["update"][1] == 10
+    lab, _ = L.assign(X, C0, precision="bf16")  # no error left behind by the timing
+    assert lab.shape[0] == 20000
