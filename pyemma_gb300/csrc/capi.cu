@@ -50,16 +50,25 @@ void ProfEvents::close() {
     active = false;
 }
 
-// cudaEventRecordExternal makes a capturing stream add an event-record node
-// to the graph (a plain record would only be a capture dependency).
+// While a stream is being captured, cudaEventRecordExternal makes the record
+// an event-record node of the graph (a plain record would only be a capture
+// dependency); outside capture the flag is not allowed.
+static void record_event(cudaEvent_t ev, cudaStream_t s) {
+    cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &st) == cudaSuccess && st == cudaStreamCaptureStatusActive)
+        cudaEventRecordWithFlags(ev, s, cudaEventRecordExternal);
+    else
+        cudaEventRecord(ev, s);
+}
+
 void ProfEvents::begin(int kind, cudaStream_t s) {
     if (!active) return;
-    cudaEventRecordWithFlags(ev[kind][0], s, cudaEventRecordExternal);
+    record_event(ev[kind][0], s);
     used[kind] = true;
 }
 
 void ProfEvents::end(int kind, cudaStream_t s) {
-    if (active) cudaEventRecordWithFlags(ev[kind][1], s, cudaEventRecordExternal);
+    if (active) record_event(ev[kind][1], s);
 }
 
 void ProfEvents::collect() {
