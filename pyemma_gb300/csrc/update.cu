@@ -115,9 +115,12 @@ __global__ void scatter_kernel(const int32_t *__restrict__ labels, int64_t n, in
 // f0 + lane + 32 m.  Label changes are warp-uniform.
 __global__ void seg_accumulate_wide_kernel(const float *__restrict__ X, int d,
                                            const int32_t *__restrict__ perm,
-                                           const int32_t *__restrict__ labels, int64_t n,
+                                           const int32_t *__restrict__ labels, int64_t n_max,
+                                           const int32_t *__restrict__ n_sorted,
                                            const float *__restrict__ C_old, double *__restrict__ S,
                                            double *__restrict__ Q) {
+    // Only the frames the scatter placed (valid labels) are in perm.
+    const int64_t n = min(n_max, (int64_t)*n_sorted);
     const int lane = threadIdx.x & 31;
     const int64_t gwarp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -181,10 +184,12 @@ __global__ void seg_accumulate_wide_kernel(const float *__restrict__ X, int d,
 template <int DP>
 __global__ void seg_accumulate_narrow_kernel(const float *__restrict__ X, int d,
                                              const int32_t *__restrict__ perm,
-                                             const int32_t *__restrict__ labels, int64_t n,
+                                             const int32_t *__restrict__ labels, int64_t n_max,
+                                             const int32_t *__restrict__ n_sorted,
                                              const float *__restrict__ C_old,
                                              double *__restrict__ S, double *__restrict__ Q) {
     constexpr int R = 32 / DP;
+    const int64_t n = min(n_max, (int64_t)*n_sorted);
     const int lane = threadIdx.x & 31;
     const int slot = lane / DP;
     const int f = lane % DP;
@@ -307,19 +312,19 @@ int launch_update(const float *X, int64_t n, int d, const int32_t *labels, int k
         const int64_t npieces = (n + kPiece - 1) / kPiece;
         const unsigned g = grid_for(npieces * 32, 256, 8);
         if (d >= 32) {
-            seg_accumulate_wide_kernel<<<g, 256, 0, s>>>(X, d, u.perm, labels, n, C_old, u.S, u.Q);
+            seg_accumulate_wide_kernel<<<g, 256, 0, s>>>(X, d, u.perm, labels, n, u.offsets + k, C_old, u.S, u.Q);
         } else if (d > 16) {
-            seg_accumulate_narrow_kernel<32><<<g, 256, 0, s>>>(X, d, u.perm, labels, n, C_old, u.S, u.Q);
+            seg_accumulate_narrow_kernel<32><<<g, 256, 0, s>>>(X, d, u.perm, labels, n, u.offsets + k, C_old, u.S, u.Q);
         } else if (d > 8) {
-            seg_accumulate_narrow_kernel<16><<<g, 256, 0, s>>>(X, d, u.perm, labels, n, C_old, u.S, u.Q);
+            seg_accumulate_narrow_kernel<16><<<g, 256, 0, s>>>(X, d, u.perm, labels, n, u.offsets + k, C_old, u.S, u.Q);
         } else if (d > 4) {
-            seg_accumulate_narrow_kernel<8><<<g, 256, 0, s>>>(X, d, u.perm, labels, n, C_old, u.S, u.Q);
+            seg_accumulate_narrow_kernel<8><<<g, 256, 0, s>>>(X, d, u.perm, labels, n, u.offsets + k, C_old, u.S, u.Q);
         } else if (d > 2) {
-            seg_accumulate_narrow_kernel<4><<<g, 256, 0, s>>>(X, d, u.perm, labels, n, C_old, u.S, u.Q);
+            seg_accumulate_narrow_kernel<4><<<g, 256, 0, s>>>(X, d, u.perm, labels, n, u.offsets + k, C_old, u.S, u.Q);
         } else if (d > 1) {
-            seg_accumulate_narrow_kernel<2><<<g, 256, 0, s>>>(X, d, u.perm, labels, n, C_old, u.S, u.Q);
+            seg_accumulate_narrow_kernel<2><<<g, 256, 0, s>>>(X, d, u.perm, labels, n, u.offsets + k, C_old, u.S, u.Q);
         } else {
-            seg_accumulate_narrow_kernel<1><<<g, 256, 0, s>>>(X, d, u.perm, labels, n, C_old, u.S, u.Q);
+            seg_accumulate_narrow_kernel<1><<<g, 256, 0, s>>>(X, d, u.perm, labels, n, u.offsets + k, C_old, u.S, u.Q);
         }
         KM_CUDA(cudaGetLastError());
     }
