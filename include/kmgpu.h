@@ -112,6 +112,21 @@ int km_update(const float *X, int64_t n, int32_t d, const int32_t *labels, int32
               const float *C_old, float *C_new, int64_t *counts, double *cost, void *workspace,
               size_t workspace_bytes, void *stream);
 
+/* ---- centroid update without a workspace (no counterpart in the reference) --
+ * Same arithmetic and outputs as km_update, for callers that cannot provide
+ * device memory (a plugin inside a host program that owns all device
+ * allocations, or a loop that must not call cudaMalloc).  Its scratch is a
+ * fixed array inside the library of km_update_noalloc_max_bytes() bytes
+ * (32 MiB), held on every GPU that loads the library until the process
+ * exits; shapes whose scratch (about 4 n + 8 k d + 28 k bytes) does not fit
+ * return KM_ERR_WORKSPACE.  The first call on a device looks up the array's
+ * device address; make that first call before any stream capture.  All calls
+ * share the array, so calls whose work overlaps on the GPU (other streams,
+ * other host threads) race; serialise them.  The call synchronises `stream`. */
+size_t km_update_noalloc_max_bytes(void);
+int km_update_noalloc(const float *X, int64_t n, int32_t d, const int32_t *labels, int32_t k,
+                      const float *C_old, float *C_new, int64_t *counts, double *cost, void *stream);
+
 /* ---- kmeans++ initialisation: KMeans(init_strategy='kmeans++') -----------
  * kmeans.py:211-212,253; seed = fixed_seed (kmeans.py:146-164).  Writes k
  * centers into C0 (device, k*d floats) and, when idx is given (device, k

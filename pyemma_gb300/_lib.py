@@ -27,7 +27,7 @@ KM_ERR_BAD_LABEL = 7
 EXPORTED = (
     "km_version", "km_status_string", "km_last_error", "km_profile_enable", "km_profile_read",
     "km_assign_workspace_size", "km_assign", "km_batch_assign",
-    "km_update_workspace_size", "km_update",
+    "km_update_workspace_size", "km_update", "km_update_noalloc_max_bytes", "km_update_noalloc",
     "km_kmpp_workspace_size", "km_kmpp",
     "km_lloyd_workspace_size", "km_lloyd",
 )
@@ -89,6 +89,9 @@ def load(build_if_missing=False):
     L.km_update_workspace_size.argtypes = [i64, i32, i32]
     L.km_update_workspace_size.restype = sz
     L.km_update.argtypes = [P, i64, i32, P, i32, P, P, P, P, P, sz, P]
+    L.km_update_noalloc_max_bytes.restype = sz
+    L.km_update_noalloc.argtypes = [P, i64, i32, P, i32, P, P, P, P, P]
+    L.km_update_noalloc.restype = ctypes.c_int
     L.km_kmpp_workspace_size.argtypes = [i64, i32, i32]
     L.km_kmpp_workspace_size.restype = sz
     L.km_kmpp.argtypes = [P, i64, i32, i32, u32, P, P, CALLBACK, P, P, sz, P]

@@ -17,6 +17,8 @@
 //   mu_j = float(c_j + S_j / n_j),  delta_j = mu_j - c_j,
 //   inertia_j = Q_j - 2 delta_j . S_j + n_j ||delta_j||^2
 // which is sum_i ||x_i - mu_j||^2 without the cancellation of raw moments.
+#include <mutex>
+
 #include "km_common.cuh"
 #include "km_internal.h"
 
@@ -337,3 +339,91 @@ int launch_update(const float *X, int64_t n, int d, const int32_t *labels, int k
 }
 
 }  // namespace km
+
+// ---------------------------------------------------------------------------
+// km_update_noalloc: the centroid update without a caller workspace.
+//
+// Some callers cannot hand out device memory: a plugin running inside a host
+// program that owns every device allocation (an MD engine or a serving
+// framework with its own memory pool and budget), or code that must not call
+// cudaMalloc because that call can synchronise the whole device in the middle
+// of a latency-sensitive loop.  This entry point uses a fixed scratch array
+// that is part of the library image instead.  The array costs
+// kNoAllocScratchBytes of device memory on every GPU that loads the library,
+// for as long as the process runs.
+// ---------------------------------------------------------------------------
+namespace km {
+namespace {
+
+constexpr size_t kNoAllocScratchBytes = size_t(32) << 20;  // 32 MiB
+
+static __device__ __align__(256) unsigned char g_update_scratch[kNoAllocScratchBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_scratch_mutex;
+void *g_scratch_ptr[kMaxDevices] = {};
+
+// Device address of g_update_scratch on the current device.  In host code the
+// array's name is only a stand-in, so the address is looked up once per
+// device (with that device current) and cached.
+int scratch_address(void **out) {
+    int dev = 0;
+    KM_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) {
+        set_error("device ordinal %d is beyond the %d devices this library tracks", dev, kMaxDevices);
+        return KM_ERR_UNSUPPORTED;
+    }
+    std::lock_guard<std::mutex> lk(g_scratch_mutex);
+    if (!g_scratch_ptr[dev]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_update_scratch);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_update_scratch)");
+        g_scratch_ptr[dev] = p;
+    }
+    *out = g_scratch_ptr[dev];
+    return KM_OK;
+}
+
+}  // namespace
+}  // namespace km
+
+extern "C" size_t km_update_noalloc_max_bytes(void) { return km::kNoAllocScratchBytes; }
+
+extern "C" int km_update_noalloc(const float *X, int64_t n, int32_t d, const int32_t *labels, int32_t k,
+                                 const float *C_old, float *C_new, int64_t *counts, double *cost,
+                                 void *stream) {
+    using namespace km;
+    KM_TRY(check_shape(n, d, k));
+    if ((n > 0 && (!X || !labels)) || !C_old || !C_new || !cost) {
+        set_error("X, labels, C_old, C_new and cost must be non-NULL");
+        return KM_ERR_BAD_SHAPE;
+    }
+    if (C_old == C_new) {
+        set_error("C_new must not alias C_old");
+        return KM_ERR_BAD_SHAPE;
+    }
+    // Scratch layout: the workspace of the update followed by one error word.
+    const size_t need = update_ws_size(n, d, k) + 256;
+    if (need > kNoAllocScratchBytes) {
+        set_error("km_update_noalloc needs %zu bytes of scratch for n=%lld, d=%d, k=%d; its fixed array "
+                  "holds %zu (about 4 n + 8 k d + 28 k bytes must fit); use km_update with a workspace",
+                  need, (long long)n, d, k, kNoAllocScratchBytes);
+        return KM_ERR_WORKSPACE;
+    }
+    void *scratch = nullptr;
+    KM_TRY(scratch_address(&scratch));
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    uint32_t *err = reinterpret_cast<uint32_t *>(static_cast<char *>(scratch) + update_ws_size(n, d, k));
+    // The array keeps the previous call's contents: the error word is cleared
+    // here, and launch_update clears its own counters and sums.
+    KM_CUDA(cudaMemsetAsync(err, 0, sizeof(uint32_t), s));
+    KM_TRY(launch_update(X, n, d, labels, k, C_old, C_new, counts, cost, err, scratch, s));
+    uint32_t e = 0;
+    KM_CUDA(cudaMemcpyAsync(&e, err, sizeof(e), cudaMemcpyDeviceToHost, s));
+    KM_CUDA(cudaStreamSynchronize(s));
+    if (e & kDevBadLabel) {
+        set_error("a label is outside [0, k)");
+        return KM_ERR_BAD_LABEL;
+    }
+    return KM_OK;
+}
