@@ -48,12 +48,13 @@ typedef enum {
 /* Distance arithmetic of the assignment.
  *   KM_PREC_FP32: exact float32 difference of squares in feature order
  *                 (plain CUDA-core kernel).
- *   KM_PREC_BF16: tensor-core BF16 distances (tcgen05, FP32 accumulate) with
- *                 an exact FP32 recheck of every frame whose nearest centers
- *                 lie within the derived error bound; the labels equal the
- *                 KM_PREC_FP32 labels bit for bit.
+ *   KM_PREC_FP16: tensor-core distances (tcgen05, FP16 operands scaled by a
+ *                 power of two, FP32 accumulate) with an exact FP32 recheck
+ *                 of every frame whose nearest centers lie within the derived
+ *                 error bound; the labels equal the KM_PREC_FP32 labels bit
+ *                 for bit.
  *   KM_PREC_AUTO: the library picks by (d, k). */
-typedef enum { KM_PREC_FP32 = 0, KM_PREC_BF16 = 1, KM_PREC_AUTO = 2 } km_precision;
+typedef enum { KM_PREC_FP32 = 0, KM_PREC_FP16 = 1, KM_PREC_AUTO = 2 } km_precision;
 
 /* Progress hook, called on the calling host thread (kmeans.py:241-251
  * passes callback_init_centers / callback_loop into the native fit). */
@@ -91,6 +92,14 @@ size_t km_assign_workspace_size(int64_t n, int32_t d, int32_t k, int32_t precisi
 int km_assign(const float *X, int64_t n, int32_t d, const float *C, int32_t k, int32_t precision,
               int32_t *labels, void *workspace, size_t workspace_bytes, km_assign_stats *stats,
               void *stream);
+
+/* ---- diagnostics: tensor-core distances (no reference counterpart) --------
+ * Runs the KM_PREC_FP16 assignment (labels as km_assign) and also writes the
+ * tensor-core approximation of every squared distance to V (device, n*k
+ * floats, V[i*k + j]); the tests use it to check the error bound pair by
+ * pair.  Workspace as km_assign with KM_PREC_FP16. */
+int km_debug_tc_distances(const float *X, int64_t n, int32_t d, const float *C, int32_t k, float *V,
+                          int32_t *labels, void *workspace, size_t workspace_bytes, void *stream);
 
 /* ---- batched assignment of uneven trajectories --------------------------
  * The get_output loop of datasource.py:402-406 runs transform chunk by chunk

@@ -12,7 +12,7 @@ import numpy as np
 
 from . import _build
 
-PRECISIONS = {"fp32": 0, "bf16": 1, "auto": 2}
+PRECISIONS = {"fp32": 0, "fp16": 1, "auto": 2}
 PRECISION_NAMES = {v: k for k, v in PRECISIONS.items()}
 
 KM_OK = 0
@@ -26,7 +26,7 @@ KM_ERR_BAD_LABEL = 7
 
 EXPORTED = (
     "km_version", "km_status_string", "km_last_error", "km_profile_enable", "km_profile_read",
-    "km_assign_workspace_size", "km_assign", "km_batch_assign",
+    "km_assign_workspace_size", "km_assign", "km_batch_assign", "km_debug_tc_distances",
     "km_update_workspace_size", "km_update", "km_update_noalloc_max_bytes", "km_update_noalloc",
     "km_kmpp_workspace_size", "km_kmpp",
     "km_lloyd_workspace_size", "km_lloyd",
@@ -85,6 +85,8 @@ def load(build_if_missing=False):
     L.km_assign_workspace_size.argtypes = [i64, i32, i32, i32]
     L.km_assign_workspace_size.restype = sz
     L.km_assign.argtypes = [P, i64, i32, P, i32, i32, P, P, sz, ctypes.POINTER(AssignStats), P]
+    L.km_debug_tc_distances.argtypes = [P, i64, i32, P, i32, P, P, P, sz, P]
+    L.km_debug_tc_distances.restype = ctypes.c_int
     L.km_batch_assign.argtypes = [P, P, i32, i32, P, i32, i32, P, P, sz, ctypes.POINTER(AssignStats), P]
     L.km_update_workspace_size.argtypes = [i64, i32, i32]
     L.km_update_workspace_size.restype = sz
@@ -187,6 +189,23 @@ def assign(X, C, precision="auto", labels=None):
     check(L.km_assign(_ptr(X), n, d, _ptr(C), k, p, _ptr(labels), _ptr(ws), ws_bytes, ctypes.byref(stats),
                       _stream(torch, X.device)))
     return labels, stats.as_dict()
+
+
+def debug_tc_distances(X, C):
+    """(labels, V): the tensor-core assignment and its n x k approximate distances."""
+    torch = _torch()
+    L = load()
+    _check_frames(torch, X)
+    _check_frames(torch, C, "C")
+    n, d = X.shape
+    k = C.shape[0]
+    V = torch.empty((n, k), dtype=torch.float32, device=X.device)
+    labels = torch.empty(n, dtype=torch.int32, device=X.device)
+    ws_bytes = L.km_assign_workspace_size(n, d, k, PRECISIONS["fp16"])
+    ws = _workspace(torch, ws_bytes, X.device)
+    check(L.km_debug_tc_distances(_ptr(X), n, d, _ptr(C), k, _ptr(V), _ptr(labels), _ptr(ws), ws_bytes,
+                                  _stream(torch, X.device)))
+    return labels, V
 
 
 def batch_assign(X_packed, offsets, C, precision="auto", labels=None):

@@ -1,5 +1,5 @@
 // assign_tc.cu -- kernel (b): nearest-center assignment on the tcgen05
-// tensor cores in BF16 with FP32 accumulation, followed by an exact FP32
+// tensor cores (FP16 operands, FP32 accumulation), followed by an exact FP32
 // recheck (kernel (b'), assign_fp32.cu) of every frame whose nearest centers
 // are not separated by the derived error bound.  The resulting labels equal
 // those of the exact FP32 kernel bit for bit.
@@ -9,39 +9,46 @@
 // inside KMeans.fit, kmeans.py:253).
 //
 // Data flow
-//   prep: x' = x - s and c' = c - s in float32 (s = a fixed shift, the mean of
-//         the centers; squared distances are translation invariant), rounded
-//         to BF16, rows padded with zeros to kp = 64 * ceil(d/64).  Per frame
-//         (||x_hat||^2, ||x'||), per center ||c_hat||^2 and max ||c'||.
+//   prep: x' = x - m and c' = c - m in float32 (m = the mean of the centers;
+//         squared distances are translation invariant), multiplied by a power
+//         of two s (chosen so that s max ||c'|| lies in (2^6, 2^7]) and
+//         rounded to FP16.  Rows are padded with zeros to kp = 64 ceil((d+2)/64)
+//         columns; columns d and d+1 carry 1 for frames and the FP16 hi/lo
+//         split of -||c_hat||^2/2 for centers, so the accumulator holds
+//         a_j = x_hat.c_hat_j - ||c_hat_j||^2/2 and
+//         v_j = ||x_hat||^2 - 2 a_j = ||x_hat - c_hat_j||^2 (scaled by s^2).
 //   main: persistent CTA per SM.  A frame tile (128 frames x kp) stays in
 //         shared memory while center tiles (BN x kp) stream through a TMA
 //         ring; one thread issues tcgen05.mma (M=128, N=BN, K=16) into one of
-//         two TMEM accumulators; four epilogue warps read the accumulator
-//         with tcgen05.ld, form e_j = ||c_hat_j||^2 - 2 x_hat.c_hat_j and keep
-//         the L smallest e_j per frame.
-//   decision: with v = ||x_hat||^2 + e an approximation of the exact float32
-//         distance D, the bound below gives an interval [lo(v), hi(v)] that
-//         holds D.  Center j can be the exact argmin only if lo(v_j) <=
-//         hi(v_min).  One candidate: final label.  2..L candidates: exact
-//         recheck of those.  More than L, or a non-finite value: exact
-//         recheck over all centers.
+//         two TMEM accumulators; four epilogue warps read them with
+//         tcgen05.ld and keep the L largest a_j per frame (a branch-free max
+//         over each 32-column chunk gates the rare insertions).
+//   decision: the bound below gives, for each listed center, an interval
+//         [lo_j(v_j), hi_j(v_j)] holding the exact float32 distance D_j.  With
+//         H = min_j hi_j, center j can be the exact argmin only if lo_j <= H.
+//         One candidate: final label.  2..L candidates: exact recheck of
+//         those.  A full list whose last entry (with the largest center norm)
+//         still passes, or a non-finite value: exact recheck over all centers.
 //
-// Bound (u = 2^-24, ub = 2^-8, kp padded dimension, sx >= ||x'||, sc >=
-// max ||c'||):
-//   | ||x_hat - c_hat|| - ||x - c|| | <= R = (ub + 2^-23) (sx + sc)
-//   | v - ||x_hat - c_hat||^2 |       <= E = (3 kp + 8) u (sx + sc)^2
-//        (norm sums, an FP32 accumulation error of kp 2^-22 per step
-//         assumed for the tensor cores, and the epilogue roundings)
-//   | D - ||x - c||^2 |               <= g ||x - c||^2,  g = (d + 2) u / (1 - (d + 2) u)
-// so lo(v) = (1-g) max(sqrt(max(v-E, 0)) - R, 0)^2 and
-//    hi(v) = (1+g) (sqrt(v+E) + R)^2, each inflated for its own rounding.
+// Bound, in unscaled units (u = 2^-24, u16 = 2^-11, sx >= ||x'||, sc_j >=
+// ||c'_j||):
+//   | ||x_hat - c_hat||/s - ||x - c|| | <= R_j = (u16 + 2^-23)(sx + sc_j)
+//        + sqrt(kp) 2^-25 / s                       (FP16 rounding, subnormals)
+//   | v_j/s^2 - ||x_hat - c_hat||^2/s^2 | <= E_j = e (sx + sc_j)^2
+//        e covers the tensor-core accumulation (an error of 2^-21 per 16-term
+//        MMA block, four times one truncation to FP32), the hi/lo split of the
+//        center norm, the rounding of ||x_hat||^2 and of v.
+//   | D - ||x - c||^2 | <= g ||x - c||^2,  g = (d + 2) u / (1 - (d + 2) u)
+// so lo_j(v) = (1-g) max(sqrt(max(v-E_j, 0)) - R_j, 0)^2 and
+//    hi_j(v) = (1+g) (sqrt(v+E_j) + R_j)^2, evaluated with directed rounding.
 #include <cuda.h>
 
 #include "km_common.cuh"
 #include "km_internal.h"
 
-#include <cuda_bf16.h>
+#include <cuda_fp16.h>
 
+#include <cmath>
 #include <mutex>
 
 namespace km {
@@ -49,12 +56,16 @@ namespace km {
 namespace {
 
 constexpr int kBM = 128;          // frames per tile (UMMA M)
-constexpr int kKC = 64;           // bf16 elements per K chunk (128 B, one SW128 row)
-constexpr int kL = 4;             // candidates kept per frame
+constexpr int kKC = 64;           // fp16 elements per K chunk (128 B, one SW128 row)
+constexpr int kL = TC_CANDIDATES; // candidates kept per frame
 constexpr int kThreadsTC = 192;   // warp 0 TMA, warp 1 MMA, warps 2-5 epilogue
 constexpr int kMaxNkc = 9;        // resident A tile up to kp = 576
 constexpr int kSmemLimit = 232448;
 constexpr int kABytesPerChunk = kBM * kKC * 2;  // 16 KB
+constexpr float kFp16Max = 65504.0f;
+
+// Scalars shared by the prep kernels and the main kernel (uint32 words).
+enum ScalarSlot { kScale = 0, kInvScale2 = 1, kScaleMax = 2, kCmax = 3, kNumScalars = 8 };
 
 struct TcParams {
     int64_t n;
@@ -68,18 +79,20 @@ struct TcParams {
     int n_ctiles;
     uint32_t tmem_cols;
     float r_coef;
+    float r_abs_scaled;  // sqrt(kp) 2^-25, divided by s at run time
     float e_coef;
     float g_lo;   // 1 - g, deflated
     float g_hi;   // 1 + g, inflated
     const float2 *xnorm;
-    const float *cn2;
-    const uint32_t *cmax;
+    const float *cnorm;
+    const uint32_t *scal;
     int32_t *labels;
     int32_t *rc_frames;
     int32_t *rc_cands;
     int32_t *full_frames;
     int32_t *counters;
     uint32_t *err;
+    float *dump;  // optional n x k distances (diagnostics)
 };
 
 // ---------------------------------------------------------------------------
@@ -159,7 +172,7 @@ __device__ __forceinline__ void tc_fence_after() {
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 }
 
-__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+__device__ __forceinline__ void mma_f16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
                                          uint32_t accumulate) {
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
@@ -204,9 +217,9 @@ __device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
     return desc;
 }
 
-// Instruction descriptor of kind::f16: BF16 x BF16 -> F32, both K-major.
+// Instruction descriptor of kind::f16: FP16 x FP16 -> F32, both K-major.
 __host__ __device__ constexpr uint32_t make_idesc(int M, int N) {
-    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+    return (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
 // ---------------------------------------------------------------------------
@@ -220,63 +233,138 @@ __global__ void shift_mean_kernel(const float *__restrict__ C, int d, int k, flo
     shift[f] = (float)(s / k);
 }
 
-// One warp per row: centered BF16 copy padded to kp, and the row's norms.
-// out_norm.x = ||x_hat||^2, out_norm.y = upper bound of ||x - shift||.
-__device__ __forceinline__ void convert_row(const float *__restrict__ src, int d, int kp,
-                                            const float *__restrict__ shift, __nv_bfloat16 *__restrict__ dst,
-                                            float &h2, float &s2) {
+__device__ __forceinline__ double warp_sum_d(double v) {
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    return v;
+}
+
+// ||c_j - m|| of every center (one warp each) and their maximum: picks the scale.
+__global__ void center_norm_max_kernel(const float *__restrict__ C, int k, int d,
+                                       const float *__restrict__ shift, uint32_t *__restrict__ scal) {
+    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
     const int lane = threadIdx.x & 31;
-    h2 = 0.0f;
-    s2 = 0.0f;
-    __nv_bfloat162 *dst2 = reinterpret_cast<__nv_bfloat162 *>(dst);
-    for (int f = 2 * lane; f < kp; f += 64) {
-        float a = 0.0f, b = 0.0f;
-        if (f < d) a = __fsub_rn(src[f], shift[f]);
-        if (f + 1 < d) b = __fsub_rn(src[f + 1], shift[f + 1]);
-        const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
-        dst2[f >> 1] = h;
-        const float ha = __low2float(h), hb = __high2float(h);
-        h2 += ha * ha + hb * hb;
-        s2 += a * a + b * b;
-    }
-    for (int off = 16; off > 0; off >>= 1) {
-        h2 += __shfl_xor_sync(0xffffffffu, h2, off);
-        s2 += __shfl_xor_sync(0xffffffffu, s2, off);
-    }
-}
-
-__global__ void prep_frames_kernel(const float *__restrict__ X, int64_t n, int d, int kp,
-                                   const float *__restrict__ shift, __nv_bfloat16 *__restrict__ xb,
-                                   float2 *__restrict__ xnorm, float norm_inflate) {
-    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t i = w; i < n; i += nw) {
-        float h2, s2;
-        convert_row(X + i * d, d, kp, shift, xb + i * kp, h2, s2);
-        if ((threadIdx.x & 31) == 0) xnorm[i] = make_float2(h2, __fsqrt_ru(s2 * norm_inflate));
-    }
-}
-
-__global__ void prep_centers_kernel(const float *__restrict__ C, int k, int k_pad, int d, int kp,
-                                    const float *__restrict__ shift, __nv_bfloat16 *__restrict__ cb,
-                                    float *__restrict__ cn2, uint32_t *__restrict__ cmax,
-                                    float norm_inflate) {
-    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t j = w; j < k_pad; j += nw) {
-        if (j < k) {
-            float h2, s2;
-            convert_row(C + j * d, d, kp, shift, cb + j * kp, h2, s2);
-            if ((threadIdx.x & 31) == 0) {
-                cn2[j] = h2;
-                const float nrm = __fsqrt_ru(s2 * norm_inflate);
-                // NaN or inf norms poison the bound on purpose (full recheck).
-                atomicMax(cmax, nrm == nrm ? __float_as_uint(nrm) : 0x7f800000u);
-            }
-        } else if ((threadIdx.x & 31) == 0) {
-            cn2[j] = __int_as_float(0x7f800000);  // padding columns never win
+    for (int64_t j = w; j < k; j += nw) {
+        CSum s2;
+        for (int f = lane; f < d; f += 32) {
+            const float a = __fsub_rn(C[j * d + f], shift[f]);
+            s2.add(a * a);
+        }
+        const double tot = warp_sum_d(s2.value());
+        if (lane == 0) {
+            const float nrm = (float)sqrt(tot);
+            atomicMax(&scal[kScaleMax], nrm == nrm ? __float_as_uint(nrm) : 0x7f800000u);
         }
     }
+}
+
+// s = 2^sigma with s max||c'|| in (2^6, 2^7]; 1 when the centers coincide.
+__global__ void scale_finalize_kernel(uint32_t *__restrict__ scal) {
+    const float m = __uint_as_float(scal[kScaleMax]);
+    int sigma = 0;
+    if (m > 0.0f && m < __int_as_float(0x7f800000)) {
+        int e;
+        frexpf(m, &e);  // m = f 2^e, f in [0.5, 1): 2^(e-1) <= m < 2^e
+        sigma = 7 - e;
+        if (sigma > 60) sigma = 60;
+        if (sigma < -60) sigma = -60;
+    }
+    scal[kScale] = __float_as_uint(ldexpf(1.0f, sigma));
+    scal[kInvScale2] = __float_as_uint(ldexpf(1.0f, -2 * sigma));
+}
+
+// Frames: one warp per row.  xnorm = (||x_hat||^2 in scaled units, upper
+// bound of ||x'|| in unscaled units).
+__global__ void prep_frames_kernel(const float *__restrict__ X, int64_t n, int d, int kp,
+                                   const float *__restrict__ shift, const uint32_t *__restrict__ scal,
+                                   __half *__restrict__ xh, float2 *__restrict__ xnorm, float norm_inflate) {
+    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    const float sc = __uint_as_float(scal[kScale]);
+    for (int64_t i = w; i < n; i += nw) {
+        const float *src = X + i * d;
+        __half2 *dst = reinterpret_cast<__half2 *>(xh + i * kp);
+        CSum h2, s2;
+        for (int f = 2 * lane; f < kp; f += 64) {
+            // Columns < d: centered, scaled frame values; d and d+1: 1 (they
+            // meet the hi/lo norm columns of the centers); the rest: 0.
+            float a = 0.0f, b = 0.0f, ia, ib;
+            if (f < d) {
+                a = __fsub_rn(src[f], shift[f]);
+                ia = a * sc;
+            } else {
+                ia = (f == d || f == d + 1) ? 1.0f : 0.0f;
+            }
+            if (f + 1 < d) {
+                b = __fsub_rn(src[f + 1], shift[f + 1]);
+                ib = b * sc;
+            } else {
+                ib = (f + 1 == d || f + 1 == d + 1) ? 1.0f : 0.0f;
+            }
+            const __half2 h = __floats2half2_rn(ia, ib);
+            dst[f >> 1] = h;
+            if (f < d) {
+                const float ha = __low2float(h);
+                h2.add(ha * ha);
+                s2.add(a * a);
+            }
+            if (f + 1 < d) {
+                const float hb = __high2float(h);
+                h2.add(hb * hb);
+                s2.add(b * b);
+            }
+        }
+        const double th = warp_sum_d(h2.value());
+        const double ts = warp_sum_d(s2.value());
+        if (lane == 0) xnorm[i] = make_float2((float)th, __fsqrt_ru(__fmul_ru((float)ts, norm_inflate)));
+    }
+}
+
+// Centers: one warp per row of the k_pad-row block.  Columns d, d+1 hold the
+// hi/lo FP16 split of -||c_hat||^2/2; cnorm is an upper bound of ||c'||.
+// A norm that FP16 cannot encode poisons cmax (every frame then takes the
+// exact path).
+__global__ void prep_centers_kernel(const float *__restrict__ C, int k, int k_pad, int d, int kp,
+                                    const float *__restrict__ shift, uint32_t *__restrict__ scal,
+                                    __half *__restrict__ ch, float *__restrict__ cnorm, float norm_inflate) {
+    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    const float sc = __uint_as_float(scal[kScale]);
+    for (int64_t j = w; j < k; j += nw) {
+        const float *src = C + j * d;
+        __half2 *dst = reinterpret_cast<__half2 *>(ch + j * kp);
+        double h2 = 0.0;
+        CSum s2;
+        for (int f = 2 * lane; f < d; f += 64) {
+            const float a = __fsub_rn(src[f], shift[f]);
+            const float b = f + 1 < d ? __fsub_rn(src[f + 1], shift[f + 1]) : 0.0f;
+            const __half2 h = __floats2half2_rn(a * sc, b * sc);
+            const double ha = (double)__low2float(h), hb = (double)__high2float(h);
+            h2 += ha * ha + hb * hb;
+            s2.add(a * a);
+            if (f + 1 < d) s2.add(b * b);
+            dst[f >> 1] = h;
+        }
+        const double tot = warp_sum_d(h2);
+        const double ts = warp_sum_d(s2.value());
+        __syncwarp();  // the pair writes above land before lane 0 writes columns d, d+1
+        if (lane == 0) {
+            const double val = -0.5 * tot;
+            const __half hi = __float2half_rn((float)val);
+            const __half lo = __float2half_rn((float)(val - (double)__half2float(hi)));
+            __half *row = ch + j * kp;
+            row[d] = hi;
+            row[d + 1] = lo;
+            const float nrm = __fsqrt_ru(__fmul_ru((float)ts, norm_inflate));
+            cnorm[j] = nrm;
+            const bool encodable = fabs(val) < (double)kFp16Max && nrm == nrm;
+            atomicMax(&scal[kCmax], encodable ? __float_as_uint(nrm) : 0x7f800000u);
+        }
+    }
+    for (int64_t j = k + w; j < k_pad; j += nw)
+        if (lane == 0) cnorm[j] = 0.0f;
 }
 
 // ---------------------------------------------------------------------------
@@ -414,8 +502,8 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                     const uint32_t a0 = smem_u32(sA + kc * kABytesPerChunk);
                     const uint32_t b0 = smem_u32(sB + s * b_stage_bytes);
                     for (int kk = 0; kk < nks; ++kk) {
-                        mma_bf16(d_tmem, sw128_desc(a0 + kk * 32), sw128_desc(b0 + kk * 32), idesc,
-                                 (kc | kk) != 0);
+                        mma_f16(d_tmem, sw128_desc(a0 + kk * 32), sw128_desc(b0 + kk * 32), idesc,
+                                (kc | kk) != 0);
                     }
                     mma_commit(&b_empty[s]);
                     if (ct == p.n_ctiles - 1) mma_commit(&a_empty[kc]);
@@ -439,17 +527,21 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
         const int quarter = warp & 3;
         const int row = quarter * 32 + lane;
         const uint32_t lane_off = (uint32_t)(quarter * 32) << 16;
-        const float sc = __uint_as_float(*p.cmax);
+        const float inv_s2 = __uint_as_float(p.scal[kInvScale2]);
+        const float r_abs = p.r_abs_scaled / __uint_as_float(p.scal[kScale]);
+        const float sc_max = __uint_as_float(p.scal[kCmax]);
+        const float kNegInf = __int_as_float(0xff800000);
+        const float kInf = __int_as_float(0x7f800000);
         uint32_t accq = 0;
         bool ok = true;
         for (int64_t ft = blockIdx.x; ft < n_ftiles && ok; ft += gridDim.x) {
             const int64_t i = ft * kBM + row;
             const float2 xn = i < p.n ? p.xnorm[i] : make_float2(0.0f, 0.0f);
-            float v[kL];
+            float a[kL];
             int id[kL];
 #pragma unroll
             for (int m = 0; m < kL; ++m) {
-                v[m] = __int_as_float(0x7f800000);
+                a[m] = kNegInf;
                 id[m] = -1;
             }
             for (int ct = 0; ct < p.n_ctiles; ++ct) {
@@ -466,23 +558,34 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                     tmem_ld32(tbase + cc, r);
                     tmem_wait_ld();
                     const int j0 = ct * p.bn + cc;
-                    const float4 *c4 = reinterpret_cast<const float4 *>(p.cn2 + j0);
+                    float v[32];
 #pragma unroll
-                    for (int q = 0; q < 8; ++q) {
-                        const float4 cn = __ldg(c4 + q);
-                        const float cv[4] = {cn.x, cn.y, cn.z, cn.w};
+                    for (int c = 0; c < 32; ++c) v[c] = __uint_as_float(r[c]);
+                    if (j0 + 32 > p.k) {
 #pragma unroll
-                        for (int u = 0; u < 4; ++u) {
-                            const float e = fmaf(-2.0f, __uint_as_float(r[q * 4 + u]), cv[u]);
-                            if (e < v[kL - 1]) {
-                                float ev = e;
-                                int ej = j0 + q * 4 + u;
+                        for (int c = 0; c < 32; ++c)
+                            if (j0 + c >= p.k) v[c] = kNegInf;
+                    }
+                    if (p.dump && i < p.n) {
+#pragma unroll
+                        for (int c = 0; c < 32; ++c)
+                            if (j0 + c < p.k) p.dump[i * p.k + j0 + c] = fmaf(-2.0f, v[c], xn.x) * inv_s2;
+                    }
+                    float mx = v[0];
+#pragma unroll
+                    for (int c = 1; c < 32; ++c) mx = fmaxf(mx, v[c]);
+                    if (mx > a[kL - 1]) {
+#pragma unroll
+                        for (int c = 0; c < 32; ++c) {
+                            if (v[c] > a[kL - 1]) {
+                                float ev = v[c];
+                                int ej = j0 + c;
 #pragma unroll
                                 for (int m = 0; m < kL; ++m) {
-                                    if (ev < v[m]) {
-                                        const float tv = v[m];
+                                    if (ev > a[m]) {
+                                        const float tv = a[m];
                                         const int tj = id[m];
-                                        v[m] = ev;
+                                        a[m] = ev;
                                         id[m] = ej;
                                         ev = tv;
                                         ej = tj;
@@ -501,27 +604,47 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
 
             // ---- decision ----
             bool need_rc = false, need_full = false;
-            int ncand = 0;
+            unsigned cmask = 0;  // bit m: listed center m is a candidate
             if (i < p.n) {
-                const float ssum = xn.y + sc;
-                const float R = __fmul_ru(p.r_coef, ssum) + 1e-35f;
-                const float E = __fmul_ru(p.e_coef, __fmul_ru(ssum, ssum));
-                const float v0 = xn.x + v[0];
-                if (!(v0 < __int_as_float(0x7f800000)) || !(R < __int_as_float(0x7f800000)) ||
-                    !(E < __int_as_float(0x7f800000))) {
+                const float sx = xn.y;
+                float vv[kL], RR[kL], EE[kL];
+                float H = kInf;
+#pragma unroll
+                for (int m = 0; m < kL; ++m) {
+                    vv[m] = kInf;
+                    RR[m] = 0.0f;
+                    EE[m] = 0.0f;
+                    if (id[m] >= 0) {
+                        const float s = sx + p.cnorm[id[m]];
+                        RR[m] = __fadd_ru(__fmul_ru(p.r_coef, s), r_abs);
+                        EE[m] = __fmul_ru(p.e_coef, __fmul_ru(s, s));
+                        vv[m] = fmaf(-2.0f, a[m], xn.x) * inv_s2;
+                        H = fminf(H, hi_bound(vv[m], EE[m], RR[m], p.g_hi));
+                    }
+                }
+                const bool finite = vv[0] < kInf && H < kInf && sx < kInf && sc_max < kInf && vv[0] == vv[0];
+                if (!finite) {
                     need_full = true;
                 } else {
-                    const float H = hi_bound(__fadd_ru(xn.x, v[0]), E, R, p.g_hi);
 #pragma unroll
-                    for (int m = 0; m < kL; ++m) {
-                        if (v[m] < __int_as_float(0x7f800000) &&
-                            lo_bound(__fadd_rd(xn.x, v[m]), E, R, p.g_lo) <= H)
-                            ++ncand;
+                    for (int m = 0; m < kL; ++m)
+                        if (id[m] >= 0 && lo_bound(vv[m], EE[m], RR[m], p.g_lo) <= H) cmask |= 1u << m;
+                    if (p.k > kL && id[kL - 1] >= 0) {
+                        // Unlisted centers have v >= vv[L-1]; bound them with the largest norm.
+                        const float s = sx + sc_max;
+                        const float R = __fadd_ru(__fmul_ru(p.r_coef, s), r_abs);
+                        const float E = __fmul_ru(p.e_coef, __fmul_ru(s, s));
+                        if (lo_bound(vv[kL - 1], E, R, p.g_lo) <= H) need_full = true;
                     }
-                    if (ncand == kL) need_full = true;  // more candidates may lie beyond the list
-                    else if (ncand > 1) need_rc = true;
+                    if (!need_full && __popc(cmask) > 1) need_rc = true;
                 }
-                p.labels[i] = id[0] >= 0 ? id[0] : 0;
+                int lab = id[0] >= 0 ? id[0] : 0;
+                if (!need_full && !need_rc) {
+#pragma unroll
+                    for (int m = 0; m < kL; ++m)
+                        if (cmask == (1u << m)) lab = id[m];
+                }
+                p.labels[i] = lab;
             }
             const unsigned m_rc = __ballot_sync(0xffffffffu, need_rc);
             if (m_rc) {
@@ -532,8 +655,13 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                 if (need_rc) {
                     const int e = base + __popc(m_rc & ((1u << lane) - 1u));
                     p.rc_frames[e] = (int32_t)i;
+                    int32_t *dst = p.rc_cands + (int64_t)e * kL;
+                    const int ncand = __popc(cmask);
 #pragma unroll
-                    for (int m = 0; m < kL; ++m) p.rc_cands[(int64_t)e * kL + m] = m < ncand ? id[m] : -1;
+                    for (int m = 0; m < kL; ++m) {
+                        if ((cmask >> m) & 1u) dst[__popc(cmask & ((1u << m) - 1u))] = id[m];
+                        if (m >= ncand) dst[m] = -1;
+                    }
                 }
             }
             const unsigned m_full = __ballot_sync(0xffffffffu, need_full);
@@ -592,7 +720,7 @@ int make_map(CUtensorMap *tm, const void *base, int64_t rows, int kp, int box_ro
     cuuint64_t strides[1] = {(cuuint64_t)kp * 2};
     cuuint32_t box[2] = {(cuuint32_t)kKC, (cuuint32_t)box_rows};
     cuuint32_t estr[2] = {1, 1};
-    CUresult r = enc(tm, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(base), dims, strides, box, estr,
+    CUresult r = enc(tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, const_cast<void *>(base), dims, strides, box, estr,
                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                      CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) {
@@ -603,7 +731,7 @@ int make_map(CUtensorMap *tm, const void *base, int64_t rows, int kp, int box_ro
     return KM_OK;
 }
 
-int kp_of(int d) { return (d + kKC - 1) / kKC * kKC; }
+int kp_of(int d) { return (d + 2 + kKC - 1) / kKC * kKC; }
 
 int pick_bn(int k) {
     if (k >= 256) return 256;
@@ -646,6 +774,18 @@ bool device_is_sm10x() {
     return cc == 10;
 }
 
+float norm_inflate_of(int d) {
+    // A compensated float32 sum of d squares is within a few u of the true value.
+    return 1.0f + (float)(d + 8) * 5.9604645e-8f + 1e-6f;
+}
+
+int64_t prep_blocks(int64_t rows) {
+    int64_t blocks = (rows * 32 + 255) / 256;
+    const int64_t cap = (int64_t)num_sms() * 16;
+    if (blocks > cap) blocks = cap;
+    return blocks < 1 ? 1 : blocks;
+}
+
 }  // namespace
 
 bool tc_plan_exists(int d, int k) {
@@ -668,7 +808,7 @@ size_t tc_frames_ws_size(int64_t n, int d) {
 void tc_carve_frames(void *ws, int64_t n, int d, TcBuffers &b) {
     Carver c(ws);
     b.kp = kp_of(d);
-    b.xb = c.take<uint16_t>((size_t)(n > 0 ? n : 1) * b.kp);
+    b.xh = c.take<uint16_t>((size_t)(n > 0 ? n : 1) * b.kp);
     b.xnorm = c.take<float2>(n > 0 ? n : 1);
 }
 
@@ -677,17 +817,17 @@ size_t tc_centers_ws_size(int d, int k) {
     c.take<uint16_t>((size_t)k_pad_of(k) * kp_of(d));
     c.take<float>(k_pad_of(k));
     c.take<float>(d);
-    c.take<uint32_t>(1);
+    c.take<uint32_t>(kNumScalars);
     return c.bytes();
 }
 
 void tc_carve_centers(void *ws, int d, int k, TcBuffers &b) {
     Carver c(ws);
     b.kp = kp_of(d);
-    b.cb = c.take<uint16_t>((size_t)k_pad_of(k) * b.kp);
-    b.cn2 = c.take<float>(k_pad_of(k));
+    b.ch = c.take<uint16_t>((size_t)k_pad_of(k) * b.kp);
+    b.cnorm = c.take<float>(k_pad_of(k));
     b.shift = c.take<float>(d);
-    b.cmax = c.take<uint32_t>(1);
+    b.scal = c.take<uint32_t>(kNumScalars);
 }
 
 size_t tc_assign_ws_size(int64_t n, int d, int k) {
@@ -720,43 +860,36 @@ void tc_carve_assign(void *ws, int64_t n, int d, int k, TcBuffers &b) {
 int tc_prepare_shift_from_centers(const float *C, int d, int k, TcBuffers &b, cudaStream_t s) {
     shift_mean_kernel<<<(d + 127) / 128, 128, 0, s>>>(C, d, k, b.shift);
     KM_CUDA(cudaGetLastError());
+    KM_CUDA(cudaMemsetAsync(b.scal, 0, kNumScalars * sizeof(uint32_t), s));
+    center_norm_max_kernel<<<(unsigned)prep_blocks(k), 256, 0, s>>>(C, k, d, b.shift, b.scal);
+    KM_CUDA(cudaGetLastError());
+    scale_finalize_kernel<<<1, 1, 0, s>>>(b.scal);
+    KM_CUDA(cudaGetLastError());
     return KM_OK;
-}
-
-static float norm_inflate_of(int d) {
-    // The float32 sum of d squares is within (d+1) u of the true value.
-    return 1.0f + (float)(d + 4) * 5.9604645e-8f + 1e-6f;
 }
 
 int tc_prepare_frames(const float *X, int64_t n, int d, TcBuffers &b, cudaStream_t s) {
     if (n == 0) return KM_OK;
-    int64_t warps = n;
-    int64_t blocks = (warps * 32 + 255) / 256;
-    const int64_t cap = (int64_t)num_sms() * 16;
-    if (blocks > cap) blocks = cap;
-    prep_frames_kernel<<<(unsigned)blocks, 256, 0, s>>>(X, n, d, b.kp, b.shift,
-                                                       reinterpret_cast<__nv_bfloat16 *>(b.xb), b.xnorm,
-                                                       norm_inflate_of(d));
+    prep_frames_kernel<<<(unsigned)prep_blocks(n), 256, 0, s>>>(X, n, d, b.kp, b.shift, b.scal,
+                                                              reinterpret_cast<__half *>(b.xh), b.xnorm,
+                                                              norm_inflate_of(d));
     KM_CUDA(cudaGetLastError());
     return KM_OK;
 }
 
 int tc_prepare_centers(const float *C, int d, int k, TcBuffers &b, cudaStream_t s) {
     const int kpad = k_pad_of(k);
-    KM_CUDA(cudaMemsetAsync(b.cmax, 0, sizeof(uint32_t), s));
-    KM_CUDA(cudaMemsetAsync(b.cb, 0, (size_t)kpad * b.kp * 2, s));
-    int64_t blocks = ((int64_t)kpad * 32 + 255) / 256;
-    const int64_t cap = (int64_t)num_sms() * 16;
-    if (blocks > cap) blocks = cap;
-    prep_centers_kernel<<<(unsigned)blocks, 256, 0, s>>>(C, k, kpad, d, b.kp, b.shift,
-                                                        reinterpret_cast<__nv_bfloat16 *>(b.cb), b.cn2, b.cmax,
-                                                        norm_inflate_of(d));
+    KM_CUDA(cudaMemsetAsync(b.scal + kCmax, 0, sizeof(uint32_t), s));
+    KM_CUDA(cudaMemsetAsync(b.ch, 0, (size_t)kpad * b.kp * 2, s));
+    prep_centers_kernel<<<(unsigned)prep_blocks(kpad), 256, 0, s>>>(C, k, kpad, d, b.kp, b.shift, b.scal,
+                                                                   reinterpret_cast<__half *>(b.ch), b.cnorm,
+                                                                   norm_inflate_of(d));
     KM_CUDA(cudaGetLastError());
     return KM_OK;
 }
 
 int tc_assign(const float *X, int64_t n, int d, const float *C, int k, int32_t *labels, TcBuffers &b,
-              cudaStream_t s, ProfEvents *prof) {
+              cudaStream_t s, ProfEvents *prof, float *dump) {
     if (n == 0) return KM_OK;
     Plan pl;
     if (!make_plan(d, k, pl) || !device_is_sm10x()) {
@@ -771,8 +904,8 @@ int tc_assign(const float *X, int64_t n, int d, const float *C, int k, int32_t *
     KM_CUDA(attr_err);
 
     CUtensorMap tmA, tmB;
-    KM_TRY(make_map(&tmA, b.xb, n, b.kp, kBM));
-    KM_TRY(make_map(&tmB, b.cb, k_pad_of(k), b.kp, pl.bn));
+    KM_TRY(make_map(&tmA, b.xh, n, b.kp, kBM));
+    KM_TRY(make_map(&tmB, b.ch, k_pad_of(k), b.kp, pl.bn));
 
     KM_CUDA(cudaMemsetAsync(b.counters, 0, 4 * sizeof(int32_t), s));
     KM_CUDA(cudaMemsetAsync(b.flipped, 0, sizeof(unsigned long long), s));
@@ -785,26 +918,29 @@ int tc_assign(const float *X, int64_t n, int d, const float *C, int k, int32_t *
     p.d = d;
     p.kp = b.kp;
     p.nkc = pl.nkc;
-    const int rem = d - (pl.nkc - 1) * kKC;
+    const int rem = d + 2 - (pl.nkc - 1) * kKC;
     p.ksteps_last = (rem + 15) / 16;
     p.bn = pl.bn;
     p.stages = pl.stages;
     p.n_ctiles = (k + pl.bn - 1) / pl.bn;
     p.tmem_cols = pl.tmem_cols;
-    p.r_coef = (float)((1.0 / 256.0 + 2.0 * u) * 1.01);
-    p.e_coef = (float)((3.0 * b.kp + 8.0) * u * 1.02);
+    p.r_coef = (float)((1.0 / 2048.0 + 2.0 * u) * 1.01);
+    p.r_abs_scaled = (float)(std::sqrt((double)b.kp) * std::ldexp(1.0, -25) * 1.01);
+    const double gamma_acc = (b.kp / 16 + 1) * std::ldexp(1.0, -21);
+    p.e_coef = (float)((gamma_acc * 1.003 + std::ldexp(1.0, -21) + 4.0 * u) * 1.01);
     const double g = (d + 2) * u / (1.0 - (d + 2) * u) * 1.01;
     p.g_lo = (float)((1.0 - g) * (1.0 - 4.0 * u));
     p.g_hi = (float)((1.0 + g) * (1.0 + 4.0 * u));
     p.xnorm = b.xnorm;
-    p.cn2 = b.cn2;
-    p.cmax = b.cmax;
+    p.cnorm = b.cnorm;
+    p.scal = b.scal;
     p.labels = labels;
     p.rc_frames = b.rc_frames;
     p.rc_cands = b.rc_cands;
     p.full_frames = b.full_frames;
     p.counters = b.counters;
     p.err = b.err;
+    p.dump = dump;
 
     const int64_t n_ftiles = (n + kBM - 1) / kBM;
     int64_t grid = num_sms();

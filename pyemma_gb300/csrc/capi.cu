@@ -91,7 +91,7 @@ namespace {
 int resolve_precision(int precision, int d, int k, bool check_device) {
     if (precision == KM_PREC_AUTO) {
         if (d >= 64 && (check_device ? tc_supported(d, k) : tc_plan_exists(d, k)))
-            return KM_PREC_BF16;
+            return KM_PREC_FP16;
         return KM_PREC_FP32;
     }
     return precision;
@@ -102,7 +102,7 @@ struct AssignWs {
 };
 
 size_t assign_ws_bytes(int64_t n, int d, int k, int prec) {
-    if (prec != KM_PREC_BF16) return 0;
+    if (prec != KM_PREC_FP16) return 0;
     return tc_frames_ws_size(n, d) + tc_centers_ws_size(d, k) + tc_assign_ws_size(n, d, k) + 3 * 256;
 }
 
@@ -135,11 +135,11 @@ int assign_impl(const float *X, int64_t n, int32_t d, const float *C, int32_t k,
         return KM_ERR_BAD_SHAPE;
     }
     int prec = resolve_precision(precision, d, k, true);
-    if (prec != KM_PREC_FP32 && prec != KM_PREC_BF16) {
+    if (prec != KM_PREC_FP32 && prec != KM_PREC_FP16) {
         set_error("unknown precision %d", precision);
         return KM_ERR_BAD_SHAPE;
     }
-    if (prec == KM_PREC_BF16 && !tc_supported(d, k)) {
+    if (prec == KM_PREC_FP16 && !tc_supported(d, k)) {
         set_error("no tensor-core kernel for d=%d, k=%d on this device", d, k);
         return KM_ERR_UNSUPPORTED;
     }
@@ -280,6 +280,30 @@ int km_batch_assign(const float *X_packed, const int64_t *offsets, int32_t n_tra
                        static_cast<cudaStream_t>(stream));
 }
 
+int km_debug_tc_distances(const float *X, int64_t n, int32_t d, const float *C, int32_t k, float *V,
+                          int32_t *labels, void *workspace, size_t workspace_bytes, void *stream) {
+    KM_TRY(check_shape(n, d, k));
+    if (n > 0 && (!X || !V || !labels || !C)) {
+        set_error("X, C, V and labels must be non-NULL");
+        return KM_ERR_BAD_SHAPE;
+    }
+    if (!tc_supported(d, k)) {
+        set_error("no tensor-core kernel for d=%d, k=%d on this device", d, k);
+        return KM_ERR_UNSUPPORTED;
+    }
+    KM_TRY(check_ws(workspace, workspace_bytes, assign_ws_bytes(n, d, k, KM_PREC_FP16)));
+    if (n == 0) return KM_OK;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    TcBuffers b;
+    carve_assign(workspace, n, d, k, b);
+    KM_TRY(tc_prepare_shift_from_centers(C, d, k, b, s));
+    KM_TRY(tc_prepare_centers(C, d, k, b, s));
+    KM_TRY(tc_prepare_frames(X, n, d, b, s));
+    KM_TRY(tc_assign(X, n, d, C, k, labels, b, s, nullptr, V));
+    KM_CUDA(cudaStreamSynchronize(s));
+    return KM_OK;
+}
+
 size_t km_update_workspace_size(int64_t n, int32_t d, int32_t k) {
     if (check_shape(n, d, k) != KM_OK) return 0;
     return update_ws_size(n, d, k) + 256;
@@ -342,7 +366,7 @@ int km_lloyd(const float *X, int64_t n, int32_t d, int32_t k, float *C, int32_t 
     *n_iter = 0;
     *converged = 0;
     int prec = resolve_precision(precision, d, k, true);
-    if (prec == KM_PREC_BF16 && !tc_supported(d, k)) {
+    if (prec == KM_PREC_FP16 && !tc_supported(d, k)) {
         set_error("no tensor-core kernel for d=%d, k=%d on this device", d, k);
         return KM_ERR_UNSUPPORTED;
     }
@@ -359,8 +383,8 @@ int km_lloyd(const float *X, int64_t n, int32_t d, int32_t k, float *C, int32_t 
     void *ws_assign = cv.take<char>(assign_ws_bytes(n, d, k, prec));
 
     TcBuffers b;
-    if (prec == KM_PREC_BF16) {
-        // The shift stays fixed for the whole run so that the BF16 frame copy
+    if (prec == KM_PREC_FP16) {
+        // The shift and scale stay fixed for the whole run so that the FP16 frame copy
         // is made once.
         carve_assign(ws_assign, n, d, k, b);
         KM_TRY(tc_prepare_shift_from_centers(C, d, k, b, s));
@@ -378,7 +402,7 @@ int km_lloyd(const float *X, int64_t n, int32_t d, int32_t k, float *C, int32_t 
         ~Closer() { p.close(); }
     } closer{prof};
     auto enqueue = [&](cudaStream_t st) -> int {
-        if (prec == KM_PREC_BF16) {
+        if (prec == KM_PREC_FP16) {
             KM_TRY(tc_prepare_centers(C, d, k, b, st));
             KM_TRY(tc_assign(X, n, d, C, k, labels, b, st, &prof));
         } else {
@@ -431,7 +455,7 @@ int km_lloyd(const float *X, int64_t n, int32_t d, int32_t k, float *C, int32_t 
         uint32_t h_err = 0, tc_err = 0;
         cudaError_t e = cudaMemcpyAsync(&h_cost, cost, sizeof(double), cudaMemcpyDeviceToHost, s);
         if (e == cudaSuccess) e = cudaMemcpyAsync(&h_err, err, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
-        if (e == cudaSuccess && prec == KM_PREC_BF16)
+        if (e == cudaSuccess && prec == KM_PREC_FP16)
             e = cudaMemcpyAsync(&tc_err, b.err, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
         if (e == cudaSuccess) e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) {

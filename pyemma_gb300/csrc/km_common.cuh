@@ -130,6 +130,22 @@ __device__ __forceinline__ float sqdist_exact(const float *__restrict__ x, const
     return acc;
 }
 
+// Neumaier-compensated float32 sum: value() is within a few u of the exact
+// sum of the added terms (plus an O(n u^2) remainder).
+struct CSum {
+    float s = 0.0f, c = 0.0f;
+    __device__ __forceinline__ void add(float v) {
+        const float t = s + v;
+        c += fabsf(s) >= fabsf(v) ? (s - t) + v : (v - t) + s;
+        s = t;
+    }
+    __device__ __forceinline__ void reset() {
+        s = 0.0f;
+        c = 0.0f;
+    }
+    __device__ __forceinline__ double value() const { return (double)s + (double)c; }
+};
+
 // Lexicographic (distance, index) minimum across a warp; NaN never wins.
 __device__ __forceinline__ void warp_argmin(float &bd, int &bj) {
 #pragma unroll

@@ -57,22 +57,24 @@ int run_kmpp(const float *X, int64_t n, int d, int k, uint32_t seed, float *C0, 
              void (*cb)(void *), void *cb_user, void *ws, cudaStream_t s);
 
 // ---- assign_tc.cu ------------------------------------------------------------
-// Tensor-core (tcgen05, BF16) assignment with exact FP32 recheck.
+// Tensor-core (tcgen05, FP16 operands) assignment with exact FP32 recheck.
 bool tc_supported(int d, int k);   // a plan exists and the device is sm_10x
 bool tc_plan_exists(int d, int k); // shape check only (no device query)
-size_t tc_frames_ws_size(int64_t n, int d);     // bf16 frame copy + norms
-size_t tc_centers_ws_size(int d, int k);        // bf16 centers + norms + shift
+size_t tc_frames_ws_size(int64_t n, int d);     // fp16 frame copy + norms
+size_t tc_centers_ws_size(int d, int k);        // fp16 centers + norms + shift + scalars
 size_t tc_assign_ws_size(int64_t n, int d, int k);  // candidate lists + counters
+
+#define TC_CANDIDATES 8  // candidate centers kept per frame by the tensor-core pass
 
 struct TcBuffers {
     // frames
-    void *xb = nullptr;          // n x kp bf16 (centered)
-    float2 *xnorm = nullptr;     // (||x_hat||^2, ||x'||) per frame
+    void *xh = nullptr;          // n x kp fp16 (centered, scaled; columns d, d+1 = 1)
+    float2 *xnorm = nullptr;     // (||x_hat||^2 scaled, upper bound of ||x'||) per frame
     // centers
-    void *cb = nullptr;          // k x kp bf16 (centered)
-    float *cn2 = nullptr;        // ||c_hat||^2 per center
+    void *ch = nullptr;          // k_pad x kp fp16 (centered, scaled; columns d, d+1 = -||c_hat||^2/2 hi/lo)
+    float *cnorm = nullptr;      // upper bound of ||c'|| per center
     float *shift = nullptr;      // d floats
-    uint32_t *cmax = nullptr;    // max ||c'|| as float bits
+    uint32_t *scal = nullptr;    // scale, 1/scale^2, norm maxima (float bits)
     // candidate lists
     int32_t *rc_frames = nullptr;
     int32_t *rc_cands = nullptr;
@@ -92,7 +94,8 @@ int tc_prepare_shift_from_centers(const float *C, int d, int k, TcBuffers &b, cu
 int tc_prepare_frames(const float *X, int64_t n, int d, TcBuffers &b, cudaStream_t s);
 int tc_prepare_centers(const float *C, int d, int k, TcBuffers &b, cudaStream_t s);
 // Runs the tensor-core pass, the candidate recheck and the full recheck.
+// dump (nullable, n x k floats) receives every tensor-core distance (diagnostics).
 int tc_assign(const float *X, int64_t n, int d, const float *C, int k, int32_t *labels,
-              TcBuffers &b, cudaStream_t s, ProfEvents *prof = nullptr);
+              TcBuffers &b, cudaStream_t s, ProfEvents *prof = nullptr, float *dump = nullptr);
 
 }  // namespace km

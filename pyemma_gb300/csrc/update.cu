@@ -6,11 +6,13 @@
 // previous center.
 //
 // Frames are grouped by label with a counting sort (histogram, exclusive
-// scan, warp-aggregated scatter of frame indices).  Warps then walk the
-// sorted index list in fixed-size pieces; inside a piece consecutive frames
-// mostly share a label, so per-lane float64 registers accumulate a run and
-// flush it with one atomic add per feature when the label changes.  The
-// number of global atomics is about (pieces + k) * d instead of n * d.
+// scan, warp-aggregated scatter of frame indices and their labels).  Warps
+// then walk the sorted list in pieces of 256 positions; inside a piece
+// consecutive frames mostly share a label, so per-lane compensated float32
+// sums accumulate a run and flush it into the float64 totals with one atomic
+// add per feature when the label changes.  The number of global atomics is
+// about (pieces + k) * d instead of n * d, and no per-element float64
+// arithmetic is needed.  Each deviation x - c_j is rounded once to float32.
 //
 // Sums are taken relative to the previous center c_j of each cluster:
 //   S_j = sum (x_i - c_j),  Q_j = sum ||x_i - c_j||^2,
@@ -26,14 +28,15 @@ namespace km {
 
 namespace {
 
-constexpr int kPiece = 512;     // sorted positions per warp
-constexpr int kWideRegs = 8;    // float64 accumulators per lane in the wide pass (256 features)
+constexpr int kPiece = 256;     // sorted positions per warp (8 groups of 32)
+constexpr int kGroups = kPiece / 32;
 
 struct UpdateWs {
     int32_t *counts;
     int32_t *offsets;
     int32_t *cursor;
     int32_t *perm;
+    int32_t *slab;
     double *S;
     double *Q;
     double *ccost;
@@ -46,6 +49,7 @@ UpdateWs carve(void *ws, int64_t n, int d, int k, size_t *bytes) {
     u.offsets = c.take<int32_t>((size_t)k + 1);
     u.cursor = c.take<int32_t>(k);
     u.perm = c.take<int32_t>(n > 0 ? n : 1);
+    u.slab = c.take<int32_t>(n > 0 ? n : 1);
     u.S = c.take<double>((size_t)k * d);
     u.Q = c.take<double>(k);
     u.ccost = c.take<double>(k);
@@ -97,7 +101,8 @@ __global__ void __launch_bounds__(1024) scan_counts_kernel(const int32_t *__rest
 }
 
 __global__ void scatter_kernel(const int32_t *__restrict__ labels, int64_t n, int k,
-                               int32_t *__restrict__ cursor, int32_t *__restrict__ perm) {
+                               int32_t *__restrict__ cursor, int32_t *__restrict__ perm,
+                               int32_t *__restrict__ slab) {
     const int lane = threadIdx.x & 31;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += stride) {
@@ -109,18 +114,24 @@ __global__ void scatter_kernel(const int32_t *__restrict__ labels, int64_t n, in
         int pos = 0;
         if (l >= 0 && lane == leader) pos = atomicAdd(&cursor[l], __popc(peers));
         pos = __shfl_sync(0xffffffffu, pos, leader);
-        if (l >= 0) perm[pos + __popc(peers & ((1u << lane) - 1u))] = (int32_t)i;
+        if (l >= 0) {
+            const int at = pos + __popc(peers & ((1u << lane) - 1u));
+            perm[at] = (int32_t)i;
+            slab[at] = l;
+        }
     }
 }
 
-// d >= 32: the whole warp walks one row at a time, lane covers features
-// f0 + lane + 32 m.  Label changes are warp-uniform.
-__global__ void seg_accumulate_wide_kernel(const float *__restrict__ X, int d,
-                                           const int32_t *__restrict__ perm,
-                                           const int32_t *__restrict__ labels, int64_t n_max,
-                                           const int32_t *__restrict__ n_sorted,
-                                           const float *__restrict__ C_old, double *__restrict__ S,
-                                           double *__restrict__ Q) {
+// The whole warp walks one sorted row at a time; lane covers features
+// f_base + lane + 32 m (m < MW); frames wider than 1024 features take one
+// launch per 1024-feature slice.  Indices and labels of the piece
+// sit in registers (8 per lane) and are broadcast by shuffles; label changes
+// are warp-uniform.
+template <int MW>
+__global__ void __launch_bounds__(256) seg_accumulate_wide_kernel(
+    const float *__restrict__ X, int d, int f_base, const int32_t *__restrict__ perm,
+    const int32_t *__restrict__ slab, int64_t n_max, const int32_t *__restrict__ n_sorted,
+    const float *__restrict__ C_old, double *__restrict__ S, double *__restrict__ Q) {
     // Only the frames the scatter placed (valid labels) are in perm.
     const int64_t n = min(n_max, (int64_t)*n_sorted);
     const int lane = threadIdx.x & 31;
@@ -129,67 +140,72 @@ __global__ void seg_accumulate_wide_kernel(const float *__restrict__ X, int d,
     const int64_t npieces = (n + kPiece - 1) / kPiece;
     for (int64_t piece = gwarp; piece < npieces; piece += nwarps) {
         const int64_t p0 = piece * kPiece;
-        const int64_t p1 = min(p0 + kPiece, n);
-        for (int f0 = 0; f0 < d; f0 += 32 * kWideRegs) {
-            double acc[kWideRegs];
-            float cold[kWideRegs];
-            double q = 0.0;
-            int cur = -1;
-            for (int64_t p = p0; p < p1; ++p) {
-                const int64_t i = perm[p];
-                const int l = labels[i];
+        int my_i[kGroups], my_l[kGroups];
+#pragma unroll
+        for (int g = 0; g < kGroups; ++g) {
+            const int64_t p = p0 + 32 * g + lane;
+            my_i[g] = p < n ? perm[p] : 0;
+            my_l[g] = p < n ? slab[p] : -1;
+        }
+        CSum acc[MW], qacc;
+        float cold[MW];
+        int cur = -1;
+        auto flush = [&]() {
+#pragma unroll
+            for (int m = 0; m < MW; ++m) {
+                const int f = f_base + lane + 32 * m;
+                if (f < d) atomicAdd(&S[(int64_t)cur * d + f], acc[m].value());
+            }
+            double q = qacc.value();
+            for (int off = 16; off > 0; off >>= 1) q += __shfl_xor_sync(0xffffffffu, q, off);
+            if (lane == 0) atomicAdd(&Q[cur], q);
+        };
+#pragma unroll
+        for (int g = 0; g < kGroups; ++g) {
+            for (int r = 0; r < 32; ++r) {
+                const int l = __shfl_sync(0xffffffffu, my_l[g], r);
+                if (l < 0) break;
+                const int64_t i = __shfl_sync(0xffffffffu, my_i[g], r);
                 if (l != cur) {
-                    if (cur >= 0) {
-#pragma unroll
-                        for (int m = 0; m < kWideRegs; ++m) {
-                            const int f = f0 + lane + 32 * m;
-                            if (f < d) atomicAdd(&S[(int64_t)cur * d + f], acc[m]);
-                        }
-                        for (int off = 16; off > 0; off >>= 1) q += __shfl_xor_sync(0xffffffffu, q, off);
-                        if (lane == 0) atomicAdd(&Q[cur], q);
-                    }
+                    if (cur >= 0) flush();
                     cur = l;
-                    q = 0.0;
+                    qacc.reset();
 #pragma unroll
-                    for (int m = 0; m < kWideRegs; ++m) {
-                        const int f = f0 + lane + 32 * m;
-                        acc[m] = 0.0;
+                    for (int m = 0; m < MW; ++m) {
+                        const int f = f_base + lane + 32 * m;
+                        acc[m].reset();
                         cold[m] = f < d ? __ldg(C_old + (int64_t)l * d + f) : 0.0f;
                     }
                 }
                 const float *x = X + i * d;
+                float xv[MW];
 #pragma unroll
-                for (int m = 0; m < kWideRegs; ++m) {
-                    const int f = f0 + lane + 32 * m;
+                for (int m = 0; m < MW; ++m) {
+                    const int f = f_base + lane + 32 * m;
+                    xv[m] = f < d ? __ldg(x + f) : 0.0f;
+                }
+#pragma unroll
+                for (int m = 0; m < MW; ++m) {
+                    const int f = f_base + lane + 32 * m;
                     if (f < d) {
-                        const double t = (double)__ldg(x + f) - (double)cold[m];
-                        acc[m] += t;
-                        q += t * t;
+                        const float t = xv[m] - cold[m];
+                        acc[m].add(t);
+                        qacc.add(t * t);
                     }
                 }
             }
-            if (cur >= 0) {
-#pragma unroll
-                for (int m = 0; m < kWideRegs; ++m) {
-                    const int f = f0 + lane + 32 * m;
-                    if (f < d) atomicAdd(&S[(int64_t)cur * d + f], acc[m]);
-                }
-                for (int off = 16; off > 0; off >>= 1) q += __shfl_xor_sync(0xffffffffu, q, off);
-                if (lane == 0) atomicAdd(&Q[cur], q);
-            }
         }
+        if (cur >= 0) flush();
     }
 }
 
 // d < 32: the warp is split into 32/DP row slots of DP lanes (DP = next
 // power of two >= d); slot s walks positions p0+s, p0+s+R, ...
 template <int DP>
-__global__ void seg_accumulate_narrow_kernel(const float *__restrict__ X, int d,
-                                             const int32_t *__restrict__ perm,
-                                             const int32_t *__restrict__ labels, int64_t n_max,
-                                             const int32_t *__restrict__ n_sorted,
-                                             const float *__restrict__ C_old,
-                                             double *__restrict__ S, double *__restrict__ Q) {
+__global__ void __launch_bounds__(256) seg_accumulate_narrow_kernel(
+    const float *__restrict__ X, int d, const int32_t *__restrict__ perm, const int32_t *__restrict__ slab,
+    int64_t n_max, const int32_t *__restrict__ n_sorted, const float *__restrict__ C_old, double *__restrict__ S,
+    double *__restrict__ Q) {
     constexpr int R = 32 / DP;
     const int64_t n = min(n_max, (int64_t)*n_sorted);
     const int lane = threadIdx.x & 31;
@@ -202,31 +218,31 @@ __global__ void seg_accumulate_narrow_kernel(const float *__restrict__ X, int d,
     for (int64_t piece = gwarp; piece < npieces; piece += nwarps) {
         const int64_t p0 = piece * kPiece;
         const int64_t p1 = min(p0 + kPiece, n);
-        double acc = 0.0, q = 0.0;
+        CSum acc, qacc;
         float cold = 0.0f;
         int cur = -1;
         for (int64_t p = p0 + slot; p < p1; p += R) {
+            const int l = slab[p];
             const int64_t i = perm[p];
-            const int l = labels[i];
             if (l != cur) {
                 if (cur >= 0 && fvalid) {
-                    atomicAdd(&S[(int64_t)cur * d + f], acc);
-                    atomicAdd(&Q[cur], q);
+                    atomicAdd(&S[(int64_t)cur * d + f], acc.value());
+                    atomicAdd(&Q[cur], qacc.value());
                 }
                 cur = l;
-                acc = 0.0;
-                q = 0.0;
+                acc.reset();
+                qacc.reset();
                 cold = fvalid ? __ldg(C_old + (int64_t)l * d + f) : 0.0f;
             }
             if (fvalid) {
-                const double t = (double)__ldg(X + i * d + f) - (double)cold;
-                acc += t;
-                q += t * t;
+                const float t = __ldg(X + i * d + f) - cold;
+                acc.add(t);
+                qacc.add(t * t);
             }
         }
         if (cur >= 0 && fvalid) {
-            atomicAdd(&S[(int64_t)cur * d + f], acc);
-            atomicAdd(&Q[cur], q);
+            atomicAdd(&S[(int64_t)cur * d + f], acc.value());
+            atomicAdd(&Q[cur], qacc.value());
         }
     }
 }
@@ -287,6 +303,55 @@ unsigned grid_for(int64_t work, int threads, int per_sm) {
     return (unsigned)(g < 1 ? 1 : g);
 }
 
+template <int MW>
+void launch_wide(const float *X, int64_t n, int d, const UpdateWs &u, int k, const float *C_old, unsigned g,
+                 cudaStream_t s) {
+    for (int f_base = 0; f_base < d; f_base += 32 * MW)
+        seg_accumulate_wide_kernel<MW><<<g, 256, 0, s>>>(X, d, f_base, u.perm, u.slab, n, u.offsets + k, C_old,
+                                                         u.S, u.Q);
+}
+
+template <int DP>
+void launch_narrow(const float *X, int64_t n, int d, const UpdateWs &u, int k, const float *C_old, unsigned g,
+                   cudaStream_t s) {
+    seg_accumulate_narrow_kernel<DP><<<g, 256, 0, s>>>(X, d, u.perm, u.slab, n, u.offsets + k, C_old, u.S, u.Q);
+}
+
+template <int MW>
+bool try_wide(int mw, const float *X, int64_t n, int d, const UpdateWs &u, int k, const float *C_old, unsigned g,
+              cudaStream_t s) {
+    if (mw > MW) return false;
+    launch_wide<MW>(X, n, d, u, k, C_old, g, s);
+    return true;
+}
+
+int launch_segments(const float *X, int64_t n, int d, const UpdateWs &u, int k, const float *C_old, unsigned g,
+                    cudaStream_t s) {
+    if (d >= 32) {
+        const int mw = (d + 31) / 32;
+        const bool ok = try_wide<1>(mw, X, n, d, u, k, C_old, g, s) || try_wide<2>(mw, X, n, d, u, k, C_old, g, s) ||
+                        try_wide<3>(mw, X, n, d, u, k, C_old, g, s) || try_wide<4>(mw, X, n, d, u, k, C_old, g, s) ||
+                        try_wide<6>(mw, X, n, d, u, k, C_old, g, s) || try_wide<8>(mw, X, n, d, u, k, C_old, g, s) ||
+                        try_wide<12>(mw, X, n, d, u, k, C_old, g, s) || try_wide<17>(mw, X, n, d, u, k, C_old, g, s) ||
+                        try_wide<24>(mw, X, n, d, u, k, C_old, g, s) || try_wide<32>(mw, X, n, d, u, k, C_old, g, s);
+        if (!ok) launch_wide<32>(X, n, d, u, k, C_old, g, s);  // d > 1024: slices of 1024 features
+    } else if (d > 16) {
+        launch_narrow<32>(X, n, d, u, k, C_old, g, s);
+    } else if (d > 8) {
+        launch_narrow<16>(X, n, d, u, k, C_old, g, s);
+    } else if (d > 4) {
+        launch_narrow<8>(X, n, d, u, k, C_old, g, s);
+    } else if (d > 2) {
+        launch_narrow<4>(X, n, d, u, k, C_old, g, s);
+    } else if (d > 1) {
+        launch_narrow<2>(X, n, d, u, k, C_old, g, s);
+    } else {
+        launch_narrow<1>(X, n, d, u, k, C_old, g, s);
+    }
+    KM_CUDA(cudaGetLastError());
+    return KM_OK;
+}
+
 }  // namespace
 
 size_t update_ws_size(int64_t n, int d, int k) {
@@ -309,26 +374,11 @@ int launch_update(const float *X, int64_t n, int d, const int32_t *labels, int k
     scan_counts_kernel<<<1, 1024, 0, s>>>(u.counts, k, u.offsets, u.cursor);
     KM_CUDA(cudaGetLastError());
     if (n > 0) {
-        scatter_kernel<<<grid_for(n, 256, 8), 256, 0, s>>>(labels, n, k, u.cursor, u.perm);
+        scatter_kernel<<<grid_for(n, 256, 8), 256, 0, s>>>(labels, n, k, u.cursor, u.perm, u.slab);
         KM_CUDA(cudaGetLastError());
         const int64_t npieces = (n + kPiece - 1) / kPiece;
         const unsigned g = grid_for(npieces * 32, 256, 8);
-        if (d >= 32) {
-            seg_accumulate_wide_kernel<<<g, 256, 0, s>>>(X, d, u.perm, labels, n, u.offsets + k, C_old, u.S, u.Q);
-        } else if (d > 16) {
-            seg_accumulate_narrow_kernel<32><<<g, 256, 0, s>>>(X, d, u.perm, labels, n, u.offsets + k, C_old, u.S, u.Q);
-        } else if (d > 8) {
-            seg_accumulate_narrow_kernel<16><<<g, 256, 0, s>>>(X, d, u.perm, labels, n, u.offsets + k, C_old, u.S, u.Q);
-        } else if (d > 4) {
-            seg_accumulate_narrow_kernel<8><<<g, 256, 0, s>>>(X, d, u.perm, labels, n, u.offsets + k, C_old, u.S, u.Q);
-        } else if (d > 2) {
-            seg_accumulate_narrow_kernel<4><<<g, 256, 0, s>>>(X, d, u.perm, labels, n, u.offsets + k, C_old, u.S, u.Q);
-        } else if (d > 1) {
-            seg_accumulate_narrow_kernel<2><<<g, 256, 0, s>>>(X, d, u.perm, labels, n, u.offsets + k, C_old, u.S, u.Q);
-        } else {
-            seg_accumulate_narrow_kernel<1><<<g, 256, 0, s>>>(X, d, u.perm, labels, n, u.offsets + k, C_old, u.S, u.Q);
-        }
-        KM_CUDA(cudaGetLastError());
+        KM_TRY(launch_segments(X, n, d, u, k, C_old, g, s));
     }
     finalize_kernel<<<(unsigned)(((int64_t)k * 32 + 255) / 256), 256, 0, s>>>(
         u.S, u.Q, u.counts, C_old, C_new, d, k, u.ccost, counts_out);

@@ -50,9 +50,9 @@ def test_version_and_status_strings(kmlib):
 
 def test_workspace_sizes_are_host_only(kmlib):
     assert kmlib.km_assign_workspace_size(1000, 2, 50, 0) == 0  # exact FP32 kernel needs none
-    bf16 = kmlib.km_assign_workspace_size(2_000_000, 528, 2000, 1)
-    assert bf16 >= 2_000_000 * 576 * 2  # the BF16 frame copy
-    assert kmlib.km_assign_workspace_size(2_000_000, 528, 2000, 2) == bf16  # auto picks BF16 for wide d
+    tc = kmlib.km_assign_workspace_size(2_000_000, 528, 2000, 1)
+    assert tc >= 2_000_000 * 576 * 2  # the FP16 frame copy
+    assert kmlib.km_assign_workspace_size(2_000_000, 528, 2000, 2) == tc  # auto picks the tensor cores for wide d
     assert kmlib.km_assign_workspace_size(1000, 10, 50, 2) == 0  # auto picks FP32 for narrow d
     assert kmlib.km_update_workspace_size(100, 3, 7) > 0
     assert kmlib.km_kmpp_workspace_size(100, 3, 7) > 0

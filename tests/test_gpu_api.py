@@ -207,7 +207,7 @@ def test_kmeans_precisions_agree(coor):
     from pyemma_gb300 import datasets
     X = datasets.gaussian_mixture(30000, 128, 40, 0.3, 5.0, seed=8)
     a = coor.cluster_kmeans(X, k=20, max_iter=20, fixed_seed=3, precision="fp32")
-    b = coor.cluster_kmeans(X, k=20, max_iter=20, fixed_seed=3, precision="bf16")
+    b = coor.cluster_kmeans(X, k=20, max_iter=20, fixed_seed=3, precision="fp16")
     assert a.n_iter == b.n_iter
     np.testing.assert_allclose(a.clustercenters, b.clustercenters, rtol=1e-5, atol=1e-6)
     np.testing.assert_array_equal(a.dtrajs[0], b.dtrajs[0])

@@ -1,0 +1,82 @@
+"""The error bound of the tensor-core assignment, checked pair by pair.
+
+km_debug_tc_distances returns the tensor-core value v of every squared
+distance.  For every (frame, center) pair the exact float32 distance D of the
+oracle must lie in [lo(v), hi(v)] as the kernel computes them (formulas in
+pyemma_gb300/csrc/assign_tc.cu).  The test also measures how much of the
+accumulation allowance E the hardware uses: the exact distance of the
+FP16-rounded operands is evaluated here in float64 and compared with v.
+"""
+import math
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+U = 2.0 ** -24
+
+
+def bound_terms(X, C):
+    n, d = X.shape
+    k = C.shape[0]
+    kp = 64 * math.ceil((d + 2) / 64)
+    shift = (C.astype(np.float64).sum(0) / k).astype(np.float32)
+    xp = (X - shift).astype(np.float32)
+    cp = (C - shift).astype(np.float32)
+    sx = np.sqrt((xp.astype(np.float64) ** 2).sum(1)) * (1 + 1e-6)
+    sc = np.sqrt((cp.astype(np.float64) ** 2).sum(1)) * (1 + 1e-6)
+    e = math.frexp(float(sc.max()))[1] if sc.max() > 0 else 7
+    scale = 2.0 ** (7 - e)
+    r_coef = (2.0 ** -11 + 2 * U) * 1.01
+    r_abs = math.sqrt(kp) * 2.0 ** -25 * 1.01 / scale
+    e_coef = ((kp // 16 + 1) * 2.0 ** -21 * 1.003 + 2.0 ** -21 + 4 * U) * 1.01
+    g = (d + 2) * U / (1 - (d + 2) * U) * 1.01
+    S = sx[:, None] + sc[None, :]
+    return dict(R=r_coef * S + r_abs, E=e_coef * S ** 2, g=g, xp=xp, cp=cp, scale=scale)
+
+
+def check_pairs(L, torch, oracle, X, C):
+    Xd = torch.from_numpy(X).cuda()
+    Cd = torch.from_numpy(C).cuda()
+    labels, V = L.debug_tc_distances(Xd, Cd)
+    V = V.cpu().numpy().astype(np.float64)
+    t = bound_terms(X, C)
+    R, E, g = t["R"], t["E"], t["g"]
+    lo = (1 - g) * np.maximum(np.sqrt(np.maximum(V - E, 0)) - R, 0) ** 2
+    hi = (1 + g) * (np.sqrt(np.maximum(V + E, 0)) + R) ** 2
+    D = oracle.sqdist_fp32_sequential(X, C).astype(np.float64)
+    bad = (D < lo * (1 - 1e-6) - 1e-30) | (D > hi * (1 + 1e-6) + 1e-30)
+    assert not bad.any(), "bound violated for %d pairs" % bad.sum()
+    # Accumulation: v against the exact distance of the rounded operands.
+    s = t["scale"]
+    xh = (t["xp"] * s).astype(np.float16).astype(np.float64)
+    ch = (t["cp"] * s).astype(np.float16).astype(np.float64)
+    Dh = ((xh[:, None, :] - ch[None, :, :]) ** 2).sum(-1) / s ** 2
+    acc_use = float(np.max(np.abs(V - Dh) / E))
+    assert acc_use <= 1.0
+    np.testing.assert_array_equal(labels.cpu().numpy(), oracle.assign(X, C))
+    return acc_use
+
+
+def test_bound_holds_on_varied_data(oracle):
+    import torch
+    from pyemma_gb300 import _lib as L, datasets
+    L.load()
+    rng = np.random.default_rng(5)
+    cases = []
+    X = rng.normal(size=(1500, 528)).astype(np.float32)
+    cases.append((X, X[rng.choice(1500, 300, replace=False)] + 0.05 * rng.normal(size=(300, 528)).astype(np.float32)))
+    X = datasets.calpha_distances(n_frames=1500, seed=2)
+    cases.append((X, X[rng.choice(1500, 200, replace=False)]))
+    X = (1e3 + rng.normal(size=(1000, 200))).astype(np.float32)
+    cases.append((X, X[rng.choice(1000, 100, replace=False)]))
+    # cancellation: alternating large components with small differences
+    base = rng.choice([-50.0, 50.0], size=(1, 128)) * rng.uniform(0.5, 1.5, size=(1, 128))
+    X = (base + rng.normal(scale=0.1, size=(1200, 128))).astype(np.float32)
+    cases.append((X, X[rng.choice(1200, 64, replace=False)]))
+    uses = []
+    for X, C in cases:
+        uses.append(check_pairs(L, torch, oracle, np.ascontiguousarray(X, np.float32),
+                                np.ascontiguousarray(C, np.float32)))
+    print("largest share of the accumulation allowance used:", uses)
