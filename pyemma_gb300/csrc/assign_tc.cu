@@ -21,8 +21,11 @@
 //         shared memory while center tiles (BN x kp) stream through a TMA
 //         ring; one thread issues tcgen05.mma (M=128, N=BN, K=16) into one of
 //         two TMEM accumulators; four epilogue warps read them with
-//         tcgen05.ld and keep the L largest a_j per frame (a branch-free max
-//         over each 32-column chunk gates the rare insertions).
+//         tcgen05.ld.  Per frame the epilogue keeps the best a_j and, from the
+//         bound, the smallest a a center must reach to stay a possible
+//         argmin; a branch-free max over each 32-column chunk skips chunks
+//         below that threshold, and the few centers above it go into a list
+//         of L (overflow -> exact recheck over all centers).
 //   decision: the bound below gives, for each listed center, an interval
 //         [lo_j(v_j), hi_j(v_j)] holding the exact float32 distance D_j.  With
 //         H = min_j hi_j, center j can be the exact argmin only if lo_j <= H.
@@ -30,10 +33,10 @@
 //         those.  A full list whose last entry (with the largest center norm)
 //         still passes, or a non-finite value: exact recheck over all centers.
 //
-// Bound, in unscaled units (u = 2^-24, u16 = 2^-11, sx >= ||x'||, sc_j >=
-// ||c'_j||):
-//   | ||x_hat - c_hat||/s - ||x - c|| | <= R_j = (u16 + 2^-23)(sx + sc_j)
-//        + sqrt(kp) 2^-25 / s                       (FP16 rounding, subnormals)
+// Bound, in unscaled units (u = 2^-24, sx >= ||x'||, sc_j >= ||c'_j||, and
+// hx >= ||x_hat/s - x'||, hc_j >= ||c_hat_j/s - c'_j|| the exact norms of the
+// FP16 rounding errors, measured when the operands are made):
+//   | ||x_hat - c_hat||/s - ||x - c|| | <= R_j = hx + hc_j + 2^-23 (sx + sc_j)
 //   | v_j/s^2 - ||x_hat - c_hat||^2/s^2 | <= E_j = e (sx + sc_j)^2
 //        e covers the tensor-core accumulation (an error of 2^-21 per 16-term
 //        MMA block, four times one truncation to FP32), the hi/lo split of the
@@ -59,13 +62,13 @@ constexpr int kBM = 128;          // frames per tile (UMMA M)
 constexpr int kKC = 64;           // fp16 elements per K chunk (128 B, one SW128 row)
 constexpr int kL = TC_CANDIDATES; // candidates kept per frame
 constexpr int kThreadsTC = 192;   // warp 0 TMA, warp 1 MMA, warps 2-5 epilogue
-constexpr int kMaxNkc = 9;        // resident A tile up to kp = 576
+constexpr int kMaxNkc = 10;       // resident A tile up to kp = 640
 constexpr int kSmemLimit = 232448;
 constexpr int kABytesPerChunk = kBM * kKC * 2;  // 16 KB
 constexpr float kFp16Max = 65504.0f;
 
 // Scalars shared by the prep kernels and the main kernel (uint32 words).
-enum ScalarSlot { kScale = 0, kInvScale2 = 1, kScaleMax = 2, kCmax = 3, kNumScalars = 8 };
+enum ScalarSlot { kScale = 0, kInvScale2 = 1, kScaleMax = 2, kCmax = 3, kHcMax = 4, kNumScalars = 8 };
 
 struct TcParams {
     int64_t n;
@@ -78,13 +81,11 @@ struct TcParams {
     int stages;
     int n_ctiles;
     uint32_t tmem_cols;
-    float r_coef;
-    float r_abs_scaled;  // sqrt(kp) 2^-25, divided by s at run time
     float e_coef;
     float g_lo;   // 1 - g, deflated
     float g_hi;   // 1 + g, inflated
-    const float2 *xnorm;
-    const float *cnorm;
+    const float4 *xnorm;
+    const float2 *cnorm;
     const uint32_t *scal;
     int32_t *labels;
     int32_t *rc_frames;
@@ -274,18 +275,19 @@ __global__ void scale_finalize_kernel(uint32_t *__restrict__ scal) {
 }
 
 // Frames: one warp per row.  xnorm = (||x_hat||^2 in scaled units, upper
-// bound of ||x'|| in unscaled units).
+// bound of ||x'||, upper bound of ||x_hat/s - x'||, 0) in unscaled units.
 __global__ void prep_frames_kernel(const float *__restrict__ X, int64_t n, int d, int kp,
                                    const float *__restrict__ shift, const uint32_t *__restrict__ scal,
-                                   __half *__restrict__ xh, float2 *__restrict__ xnorm, float norm_inflate) {
+                                   __half *__restrict__ xh, float4 *__restrict__ xnorm, float norm_inflate) {
     const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
     const int lane = threadIdx.x & 31;
     const float sc = __uint_as_float(scal[kScale]);
+    const float inv_sc = 1.0f / sc;  // exact: a power of two
     for (int64_t i = w; i < n; i += nw) {
         const float *src = X + i * d;
         __half2 *dst = reinterpret_cast<__half2 *>(xh + i * kp);
-        CSum h2, s2;
+        CSum h2, s2, e2;
         for (int f = 2 * lane; f < kp; f += 64) {
             // Columns < d: centered, scaled frame values; d and d+1: 1 (they
             // meet the hi/lo norm columns of the centers); the rest: 0.
@@ -306,49 +308,66 @@ __global__ void prep_frames_kernel(const float *__restrict__ X, int64_t n, int d
             dst[f >> 1] = h;
             if (f < d) {
                 const float ha = __low2float(h);
+                const float ea = ha - ia;
                 h2.add(ha * ha);
                 s2.add(a * a);
+                e2.add(ea * ea);
             }
             if (f + 1 < d) {
                 const float hb = __high2float(h);
+                const float eb = hb - ib;
                 h2.add(hb * hb);
                 s2.add(b * b);
+                e2.add(eb * eb);
             }
         }
         const double th = warp_sum_d(h2.value());
         const double ts = warp_sum_d(s2.value());
-        if (lane == 0) xnorm[i] = make_float2((float)th, __fsqrt_ru(__fmul_ru((float)ts, norm_inflate)));
+        const double te = warp_sum_d(e2.value());
+        if (lane == 0) {
+            const float sx = __fsqrt_ru(__fmul_ru((float)ts, norm_inflate));
+            const float hx = __fmul_ru(__fadd_ru(__fsqrt_ru(__fmul_ru((float)te, norm_inflate)), 1e-30f), inv_sc);
+            xnorm[i] = make_float4((float)th, sx, hx, 0.0f);
+        }
     }
 }
 
 // Centers: one warp per row of the k_pad-row block.  Columns d, d+1 hold the
-// hi/lo FP16 split of -||c_hat||^2/2; cnorm is an upper bound of ||c'||.
-// A norm that FP16 cannot encode poisons cmax (every frame then takes the
-// exact path).
+// hi/lo FP16 split of -||c_hat||^2/2; cnorm = (upper bound of ||c'||, upper
+// bound of ||c_hat/s - c'||).  A norm that FP16 cannot encode poisons cmax
+// (every frame then takes the exact path).
 __global__ void prep_centers_kernel(const float *__restrict__ C, int k, int k_pad, int d, int kp,
                                     const float *__restrict__ shift, uint32_t *__restrict__ scal,
-                                    __half *__restrict__ ch, float *__restrict__ cnorm, float norm_inflate) {
+                                    __half *__restrict__ ch, float2 *__restrict__ cnorm, float norm_inflate) {
     const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
     const int lane = threadIdx.x & 31;
     const float sc = __uint_as_float(scal[kScale]);
+    const float inv_sc = 1.0f / sc;
     for (int64_t j = w; j < k; j += nw) {
         const float *src = C + j * d;
         __half2 *dst = reinterpret_cast<__half2 *>(ch + j * kp);
         double h2 = 0.0;
-        CSum s2;
+        CSum s2, e2;
         for (int f = 2 * lane; f < d; f += 64) {
             const float a = __fsub_rn(src[f], shift[f]);
             const float b = f + 1 < d ? __fsub_rn(src[f + 1], shift[f + 1]) : 0.0f;
             const __half2 h = __floats2half2_rn(a * sc, b * sc);
-            const double ha = (double)__low2float(h), hb = (double)__high2float(h);
-            h2 += ha * ha + hb * hb;
+            const float ha = __low2float(h), hb = __high2float(h);
+            h2 += (double)ha * ha + (double)hb * hb;
             s2.add(a * a);
-            if (f + 1 < d) s2.add(b * b);
+            const float ea = ha - a * sc;
+            e2.add(ea * ea);
+            if (f + 1 < d) {
+                s2.add(b * b);
+                const float eb = hb - b * sc;
+                e2.add(eb * eb);
+            }
             dst[f >> 1] = h;
         }
         const double tot = warp_sum_d(h2);
         const double ts = warp_sum_d(s2.value());
+        const double te = warp_sum_d(e2.value());
         __syncwarp();  // the pair writes above land before lane 0 writes columns d, d+1
         if (lane == 0) {
             const double val = -0.5 * tot;
@@ -358,13 +377,15 @@ __global__ void prep_centers_kernel(const float *__restrict__ C, int k, int k_pa
             row[d] = hi;
             row[d + 1] = lo;
             const float nrm = __fsqrt_ru(__fmul_ru((float)ts, norm_inflate));
-            cnorm[j] = nrm;
-            const bool encodable = fabs(val) < (double)kFp16Max && nrm == nrm;
+            const float hc = __fmul_ru(__fadd_ru(__fsqrt_ru(__fmul_ru((float)te, norm_inflate)), 1e-30f), inv_sc);
+            cnorm[j] = make_float2(nrm, hc);
+            const bool encodable = fabs(val) < (double)kFp16Max && nrm == nrm && hc == hc;
             atomicMax(&scal[kCmax], encodable ? __float_as_uint(nrm) : 0x7f800000u);
+            atomicMax(&scal[kHcMax], encodable ? __float_as_uint(hc) : 0x7f800000u);
         }
     }
     for (int64_t j = k + w; j < k_pad; j += nw)
-        if (lane == 0) cnorm[j] = 0.0f;
+        if (lane == 0) cnorm[j] = make_float2(0.0f, 0.0f);
 }
 
 // ---------------------------------------------------------------------------
@@ -379,6 +400,24 @@ __device__ __forceinline__ float lo_bound(float v, float E, float R, float g_lo)
 __device__ __forceinline__ float hi_bound(float v, float E, float R, float g_hi) {
     float a = __fadd_ru(__fsqrt_ru(fmaxf(__fadd_ru(v, E), 0.0f)), R);
     return __fadd_ru(__fmul_ru(__fmul_ru(a, a), g_hi), 1e-37f);
+}
+
+// Rounding of the float32 centering x' = fl(x - m): at most 2^-24 |x - m|
+// per component, so 2^-23 (sx + sc) covers both operands.
+constexpr float kCenterEps = 1.1920929e-07f;  // 2^-23
+
+// Smallest accumulator a' that can still belong to a possible argmin, given
+// the best accumulator so far: with H the upper end of the best distance,
+// lo(v') <= H needs v' <= V = (sqrt(H / (1-g)) + R)^2 + E (worst-case R, E),
+// and v' = (||x_hat||^2 - 2 a') / s^2.  Rounded towards admitting more.
+__device__ __forceinline__ float window_threshold(float best, float xn2, float inv_s2, float s2, float E,
+                                                  float R, float g_lo, float g_hi) {
+    const float vb = fmaf(-2.0f, best, xn2) * inv_s2;
+    const float H = hi_bound(vb, E, R, g_hi);
+    const float q = __fadd_ru(__fsqrt_ru(__fdiv_ru(H, g_lo)), R);
+    const float V = __fadd_ru(__fmul_ru(q, q), E);
+    const float t = __fmul_rd(__fsub_rd(xn2, __fmul_ru(V, s2)), 0.5f);
+    return __fsub_rd(t, __fmul_ru(fabsf(t), 1e-6f)) - 1e-30f;
 }
 
 __global__ void __launch_bounds__(kThreadsTC, 1)
@@ -528,21 +567,30 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
         const int row = quarter * 32 + lane;
         const uint32_t lane_off = (uint32_t)(quarter * 32) << 16;
         const float inv_s2 = __uint_as_float(p.scal[kInvScale2]);
-        const float r_abs = p.r_abs_scaled / __uint_as_float(p.scal[kScale]);
+        const float s2 = 1.0f / inv_s2;  // exact: a power of two
         const float sc_max = __uint_as_float(p.scal[kCmax]);
+        const float hc_max = __uint_as_float(p.scal[kHcMax]);
         const float kNegInf = __int_as_float(0xff800000);
         const float kInf = __int_as_float(0x7f800000);
         uint32_t accq = 0;
         bool ok = true;
         for (int64_t ft = blockIdx.x; ft < n_ftiles && ok; ft += gridDim.x) {
             const int64_t i = ft * kBM + row;
-            const float2 xn = i < p.n ? p.xnorm[i] : make_float2(0.0f, 0.0f);
-            float a[kL];
-            int id[kL];
+            const float4 xn = i < p.n ? p.xnorm[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            // Worst-case bound terms over all centers: the acceptance window
+            // and the overflow decision use them.
+            const float smax = xn.y + sc_max;
+            const float Rmax = __fadd_ru(__fadd_ru(xn.z, hc_max), __fmul_ru(kCenterEps, smax));
+            const float Emax = __fmul_ru(p.e_coef, __fmul_ru(smax, smax));
+            float best = kNegInf, thr = kNegInf;
+            int best_id = 0;
+            bool ovf = false;
+            float la[kL];
+            int lid[kL];
 #pragma unroll
             for (int m = 0; m < kL; ++m) {
-                a[m] = kNegInf;
-                id[m] = -1;
+                la[m] = kNegInf;
+                lid[m] = -1;
             }
             for (int ct = 0; ct < p.n_ctiles; ++ct) {
                 const uint32_t buf = accq & 1u;
@@ -574,23 +622,27 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                     float mx = v[0];
 #pragma unroll
                     for (int c = 1; c < 32; ++c) mx = fmaxf(mx, v[c]);
-                    if (mx > a[kL - 1]) {
+                    if (mx >= thr && mx > kNegInf) {
+                        if (mx > best) {
+                            int bc = 31;
+#pragma unroll
+                            for (int c = 31; c >= 0; --c)
+                                if (v[c] == mx) bc = c;
+                            best = mx;
+                            best_id = j0 + bc;
+                            thr = window_threshold(best, xn.x, inv_s2, s2, Emax, Rmax, p.g_lo, p.g_hi);
+                        }
 #pragma unroll
                         for (int c = 0; c < 32; ++c) {
-                            if (v[c] > a[kL - 1]) {
-                                float ev = v[c];
-                                int ej = j0 + c;
+                            if (v[c] >= thr) {
+                                if (lid[kL - 1] >= 0 && la[kL - 1] >= thr) ovf = true;
 #pragma unroll
-                                for (int m = 0; m < kL; ++m) {
-                                    if (ev > a[m]) {
-                                        const float tv = a[m];
-                                        const int tj = id[m];
-                                        a[m] = ev;
-                                        id[m] = ej;
-                                        ev = tv;
-                                        ej = tj;
-                                    }
+                                for (int m = kL - 1; m > 0; --m) {
+                                    la[m] = la[m - 1];
+                                    lid[m] = lid[m - 1];
                                 }
+                                la[0] = v[c];
+                                lid[0] = j0 + c;
                             }
                         }
                     }
@@ -604,9 +656,8 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
 
             // ---- decision ----
             bool need_rc = false, need_full = false;
-            unsigned cmask = 0;  // bit m: listed center m is a candidate
+            unsigned cmask = 0;  // bit m: list entry m is a candidate
             if (i < p.n) {
-                const float sx = xn.y;
                 float vv[kL], RR[kL], EE[kL];
                 float H = kInf;
 #pragma unroll
@@ -614,35 +665,31 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                     vv[m] = kInf;
                     RR[m] = 0.0f;
                     EE[m] = 0.0f;
-                    if (id[m] >= 0) {
-                        const float s = sx + p.cnorm[id[m]];
-                        RR[m] = __fadd_ru(__fmul_ru(p.r_coef, s), r_abs);
-                        EE[m] = __fmul_ru(p.e_coef, __fmul_ru(s, s));
-                        vv[m] = fmaf(-2.0f, a[m], xn.x) * inv_s2;
+                    if (lid[m] >= 0 && la[m] >= thr) {
+                        const float2 cn = p.cnorm[lid[m]];
+                        const float sj = xn.y + cn.x;
+                        RR[m] = __fadd_ru(__fadd_ru(xn.z, cn.y), __fmul_ru(kCenterEps, sj));
+                        EE[m] = __fmul_ru(p.e_coef, __fmul_ru(sj, sj));
+                        vv[m] = fmaf(-2.0f, la[m], xn.x) * inv_s2;
                         H = fminf(H, hi_bound(vv[m], EE[m], RR[m], p.g_hi));
                     }
                 }
-                const bool finite = vv[0] < kInf && H < kInf && sx < kInf && sc_max < kInf && vv[0] == vv[0];
-                if (!finite) {
+                const bool finite = best > kNegInf && H < kInf && Rmax < kInf && Emax < kInf;
+                if (!finite || ovf) {
                     need_full = true;
                 } else {
 #pragma unroll
                     for (int m = 0; m < kL; ++m)
-                        if (id[m] >= 0 && lo_bound(vv[m], EE[m], RR[m], p.g_lo) <= H) cmask |= 1u << m;
-                    if (p.k > kL && id[kL - 1] >= 0) {
-                        // Unlisted centers have v >= vv[L-1]; bound them with the largest norm.
-                        const float s = sx + sc_max;
-                        const float R = __fadd_ru(__fmul_ru(p.r_coef, s), r_abs);
-                        const float E = __fmul_ru(p.e_coef, __fmul_ru(s, s));
-                        if (lo_bound(vv[kL - 1], E, R, p.g_lo) <= H) need_full = true;
-                    }
-                    if (!need_full && __popc(cmask) > 1) need_rc = true;
+                        if (vv[m] < kInf && lo_bound(vv[m], EE[m], RR[m], p.g_lo) <= H) cmask |= 1u << m;
+                    const int nc = __popc(cmask);
+                    if (nc == 0) need_full = true;
+                    else if (nc > 1) need_rc = true;
                 }
-                int lab = id[0] >= 0 ? id[0] : 0;
+                int lab = best_id;
                 if (!need_full && !need_rc) {
 #pragma unroll
                     for (int m = 0; m < kL; ++m)
-                        if (cmask == (1u << m)) lab = id[m];
+                        if (cmask == (1u << m)) lab = lid[m];
                 }
                 p.labels[i] = lab;
             }
@@ -659,7 +706,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                     const int ncand = __popc(cmask);
 #pragma unroll
                     for (int m = 0; m < kL; ++m) {
-                        if ((cmask >> m) & 1u) dst[__popc(cmask & ((1u << m) - 1u))] = id[m];
+                        if ((cmask >> m) & 1u) dst[__popc(cmask & ((1u << m) - 1u))] = lid[m];
                         if (m >= ncand) dst[m] = -1;
                     }
                 }
@@ -801,7 +848,7 @@ bool tc_supported(int d, int k) {
 size_t tc_frames_ws_size(int64_t n, int d) {
     Carver c(nullptr);
     c.take<uint16_t>((size_t)(n > 0 ? n : 1) * kp_of(d));
-    c.take<float2>(n > 0 ? n : 1);
+    c.take<float4>(n > 0 ? n : 1);
     return c.bytes();
 }
 
@@ -809,13 +856,13 @@ void tc_carve_frames(void *ws, int64_t n, int d, TcBuffers &b) {
     Carver c(ws);
     b.kp = kp_of(d);
     b.xh = c.take<uint16_t>((size_t)(n > 0 ? n : 1) * b.kp);
-    b.xnorm = c.take<float2>(n > 0 ? n : 1);
+    b.xnorm = c.take<float4>(n > 0 ? n : 1);
 }
 
 size_t tc_centers_ws_size(int d, int k) {
     Carver c(nullptr);
     c.take<uint16_t>((size_t)k_pad_of(k) * kp_of(d));
-    c.take<float>(k_pad_of(k));
+    c.take<float2>(k_pad_of(k));
     c.take<float>(d);
     c.take<uint32_t>(kNumScalars);
     return c.bytes();
@@ -825,7 +872,7 @@ void tc_carve_centers(void *ws, int d, int k, TcBuffers &b) {
     Carver c(ws);
     b.kp = kp_of(d);
     b.ch = c.take<uint16_t>((size_t)k_pad_of(k) * b.kp);
-    b.cnorm = c.take<float>(k_pad_of(k));
+    b.cnorm = c.take<float2>(k_pad_of(k));
     b.shift = c.take<float>(d);
     b.scal = c.take<uint32_t>(kNumScalars);
 }
@@ -879,7 +926,7 @@ int tc_prepare_frames(const float *X, int64_t n, int d, TcBuffers &b, cudaStream
 
 int tc_prepare_centers(const float *C, int d, int k, TcBuffers &b, cudaStream_t s) {
     const int kpad = k_pad_of(k);
-    KM_CUDA(cudaMemsetAsync(b.scal + kCmax, 0, sizeof(uint32_t), s));
+    KM_CUDA(cudaMemsetAsync(b.scal + kCmax, 0, 2 * sizeof(uint32_t), s));  // kCmax, kHcMax
     KM_CUDA(cudaMemsetAsync(b.ch, 0, (size_t)kpad * b.kp * 2, s));
     prep_centers_kernel<<<(unsigned)prep_blocks(kpad), 256, 0, s>>>(C, k, kpad, d, b.kp, b.shift, b.scal,
                                                                    reinterpret_cast<__half *>(b.ch), b.cnorm,
@@ -924,8 +971,6 @@ int tc_assign(const float *X, int64_t n, int d, const float *C, int k, int32_t *
     p.stages = pl.stages;
     p.n_ctiles = (k + pl.bn - 1) / pl.bn;
     p.tmem_cols = pl.tmem_cols;
-    p.r_coef = (float)((1.0 / 2048.0 + 2.0 * u) * 1.01);
-    p.r_abs_scaled = (float)(std::sqrt((double)b.kp) * std::ldexp(1.0, -25) * 1.01);
     const double gamma_acc = (b.kp / 16 + 1) * std::ldexp(1.0, -21);
     p.e_coef = (float)((gamma_acc * 1.003 + std::ldexp(1.0, -21) + 4.0 * u) * 1.01);
     const double g = (d + 2) * u / (1.0 - (d + 2) * u) * 1.01;

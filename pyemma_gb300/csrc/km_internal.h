@@ -69,10 +69,10 @@ size_t tc_assign_ws_size(int64_t n, int d, int k);  // candidate lists + counter
 struct TcBuffers {
     // frames
     void *xh = nullptr;          // n x kp fp16 (centered, scaled; columns d, d+1 = 1)
-    float2 *xnorm = nullptr;     // (||x_hat||^2 scaled, upper bound of ||x'||) per frame
+    float4 *xnorm = nullptr;     // (||x_hat||^2 scaled, bounds of ||x'|| and of its FP16 rounding error, 0)
     // centers
     void *ch = nullptr;          // k_pad x kp fp16 (centered, scaled; columns d, d+1 = -||c_hat||^2/2 hi/lo)
-    float *cnorm = nullptr;      // upper bound of ||c'|| per center
+    float2 *cnorm = nullptr;     // bounds of ||c'|| and of its FP16 rounding error per center
     float *shift = nullptr;      // d floats
     uint32_t *scal = nullptr;    // scale, 1/scale^2, norm maxima (float bits)
     // candidate lists

@@ -26,14 +26,16 @@ def bound_terms(X, C):
     cp = (C - shift).astype(np.float32)
     sx = np.sqrt((xp.astype(np.float64) ** 2).sum(1)) * (1 + 1e-6)
     sc = np.sqrt((cp.astype(np.float64) ** 2).sum(1)) * (1 + 1e-6)
-    e = math.frexp(float(sc.max()))[1] if sc.max() > 0 else 7
+    e = math.frexp(float(np.sqrt((cp.astype(np.float64) ** 2).sum(1)).max()))[1] if sc.max() > 0 else 7
     scale = 2.0 ** (7 - e)
-    r_coef = (2.0 ** -11 + 2 * U) * 1.01
-    r_abs = math.sqrt(kp) * 2.0 ** -25 * 1.01 / scale
+    # exact norms of the FP16 rounding errors, as the prep kernels measure them
+    hx = np.sqrt(((((xp * scale).astype(np.float16).astype(np.float64)) / scale - xp) ** 2).sum(1)) * (1 + 1e-6)
+    hc = np.sqrt(((((cp * scale).astype(np.float16).astype(np.float64)) / scale - cp) ** 2).sum(1)) * (1 + 1e-6)
     e_coef = ((kp // 16 + 1) * 2.0 ** -21 * 1.003 + 2.0 ** -21 + 4 * U) * 1.01
     g = (d + 2) * U / (1 - (d + 2) * U) * 1.01
     S = sx[:, None] + sc[None, :]
-    return dict(R=r_coef * S + r_abs, E=e_coef * S ** 2, g=g, xp=xp, cp=cp, scale=scale)
+    R = hx[:, None] + hc[None, :] + 2.0 ** -23 * S
+    return dict(R=R, E=e_coef * S ** 2, g=g, xp=xp, cp=cp, scale=scale)
 
 
 def check_pairs(L, torch, oracle, X, C):
