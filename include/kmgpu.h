@@ -94,12 +94,17 @@ int km_assign(const float *X, int64_t n, int32_t d, const float *C, int32_t k, i
               void *stream);
 
 /* ---- diagnostics: tensor-core distances (no reference counterpart) --------
- * Runs the KM_PREC_FP16 assignment (labels as km_assign) and also writes the
- * tensor-core approximation of every squared distance to V (device, n*k
- * floats, V[i*k + j]); the tests use it to check the error bound pair by
- * pair.  Workspace as km_assign with KM_PREC_FP16. */
+ * Runs the KM_PREC_FP16 assignment (labels as km_assign).  V (device, n*k
+ * floats, nullable) receives the tensor-core approximation of every squared
+ * distance, V[i*k + j]; the tests use it to check the error bound pair by
+ * pair.  wait_cycles (host, 8 counters, nullable) receives the SM cycles the
+ * kernel's roles spent waiting: producer on free B / A buffers, MMA issuer on
+ * loaded B / A and on a drained accumulator, epilogue on a ready
+ * accumulator, then the epilogue's and the MMA issuer's total cycles.
+ * Workspace as km_assign with KM_PREC_FP16. */
 int km_debug_tc_distances(const float *X, int64_t n, int32_t d, const float *C, int32_t k, float *V,
-                          int32_t *labels, void *workspace, size_t workspace_bytes, void *stream);
+                          int32_t *labels, uint64_t *wait_cycles, void *workspace, size_t workspace_bytes,
+                          void *stream);
 
 /* ---- batched assignment of uneven trajectories --------------------------
  * The get_output loop of datasource.py:402-406 runs transform chunk by chunk

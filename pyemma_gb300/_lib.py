@@ -85,7 +85,7 @@ def load(build_if_missing=False):
     L.km_assign_workspace_size.argtypes = [i64, i32, i32, i32]
     L.km_assign_workspace_size.restype = sz
     L.km_assign.argtypes = [P, i64, i32, P, i32, i32, P, P, sz, ctypes.POINTER(AssignStats), P]
-    L.km_debug_tc_distances.argtypes = [P, i64, i32, P, i32, P, P, P, sz, P]
+    L.km_debug_tc_distances.argtypes = [P, i64, i32, P, i32, P, P, P, P, sz, P]
     L.km_debug_tc_distances.restype = ctypes.c_int
     L.km_batch_assign.argtypes = [P, P, i32, i32, P, i32, i32, P, P, sz, ctypes.POINTER(AssignStats), P]
     L.km_update_workspace_size.argtypes = [i64, i32, i32]
@@ -191,21 +191,27 @@ def assign(X, C, precision="auto", labels=None):
     return labels, stats.as_dict()
 
 
-def debug_tc_distances(X, C):
-    """(labels, V): the tensor-core assignment and its n x k approximate distances."""
+WAIT_SLOTS = ("producer_b", "producer_a", "mma_b", "mma_a", "mma_acc", "epilogue_acc", "epilogue_total",
+              "mma_total")
+
+
+def debug_tc_distances(X, C, distances=True):
+    """(labels, V or None, wait cycles): the tensor-core assignment, its n x k
+    approximate distances and the cycles each kernel role spent waiting."""
     torch = _torch()
     L = load()
     _check_frames(torch, X)
     _check_frames(torch, C, "C")
     n, d = X.shape
     k = C.shape[0]
-    V = torch.empty((n, k), dtype=torch.float32, device=X.device)
+    V = torch.empty((n, k), dtype=torch.float32, device=X.device) if distances else None
     labels = torch.empty(n, dtype=torch.int32, device=X.device)
     ws_bytes = L.km_assign_workspace_size(n, d, k, PRECISIONS["fp16"])
     ws = _workspace(torch, ws_bytes, X.device)
-    check(L.km_debug_tc_distances(_ptr(X), n, d, _ptr(C), k, _ptr(V), _ptr(labels), _ptr(ws), ws_bytes,
+    wait = (ctypes.c_uint64 * 8)()
+    check(L.km_debug_tc_distances(_ptr(X), n, d, _ptr(C), k, _ptr(V), _ptr(labels), wait, _ptr(ws), ws_bytes,
                                   _stream(torch, X.device)))
-    return labels, V
+    return labels, V, dict(zip(WAIT_SLOTS, list(wait)))
 
 
 def batch_assign(X_packed, offsets, C, precision="auto", labels=None):

@@ -94,6 +94,20 @@ struct TcParams {
     int32_t *counters;
     uint32_t *err;
     float *dump;  // optional n x k distances (diagnostics)
+    unsigned long long *wait_cycles;  // optional per-role wait counters (diagnostics), WaitSlot order
+};
+
+// Diagnostic counters: SM cycles each role spent waiting (summed over CTAs).
+enum WaitSlot {
+    kWaitProdB = 0,     // producer: B stage free
+    kWaitProdA = 1,     // producer: A chunk free
+    kWaitMmaB = 2,      // MMA: B stage loaded
+    kWaitMmaA = 3,      // MMA: A chunk loaded
+    kWaitMmaAcc = 4,    // MMA: accumulator drained by the epilogue
+    kWaitEpiAcc = 5,    // epilogue: accumulator ready
+    kEpiTotal = 6,      // epilogue: all cycles of its loop
+    kMmaTotal = 7,      // MMA: all cycles of its loop
+    kNumWaitSlots = 8
 };
 
 // ---------------------------------------------------------------------------
@@ -140,6 +154,15 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
         if (mbar_try_wait(bar, parity)) return true;
         if ((spin & 255u) == 0 && globaltimer_ns() - t0 > kWaitLimitNs) return false;
     }
+}
+
+// mbar_wait that adds the cycles it spent to *acc when acc is non-null.
+__device__ __forceinline__ bool mbar_wait_timed(uint64_t *bar, uint32_t parity, unsigned long long *acc) {
+    if (!acc) return mbar_wait(bar, parity);
+    const long long t0 = clock64();
+    const bool ok = mbar_wait(bar, parity);
+    *acc += (unsigned long long)(clock64() - t0);
+    return ok;
 }
 
 __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *tm, int x, int y,
@@ -475,11 +498,14 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
         uint32_t bq = 0;
         uint32_t t_local = 0;
         bool ok = true;
+        unsigned long long w_b = 0, w_a = 0;
+        unsigned long long *pw_b = p.wait_cycles ? &w_b : nullptr;
+        unsigned long long *pw_a = p.wait_cycles ? &w_a : nullptr;
         for (int64_t ft = blockIdx.x; ft < n_ftiles && ok; ft += gridDim.x, ++t_local) {
             for (int ct = 0; ct < p.n_ctiles && ok; ++ct) {
                 for (int kc = 0; kc < p.nkc; ++kc) {
                     if (ct == 0) {
-                        if (!mbar_wait(&a_empty[kc], (t_local & 1u) ^ 1u)) {
+                        if (!mbar_wait_timed(&a_empty[kc], (t_local & 1u) ^ 1u, pw_a)) {
                             ok = false;
                             break;
                         }
@@ -488,7 +514,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                     }
                     const uint32_t s = bq % p.stages;
                     const uint32_t ph = (bq / p.stages) & 1u;
-                    if (!mbar_wait(&b_empty[s], ph ^ 1u)) {
+                    if (!mbar_wait_timed(&b_empty[s], ph ^ 1u, pw_b)) {
                         ok = false;
                         break;
                     }
@@ -502,6 +528,10 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
         if (!ok) {
             atomicOr(p.err, (uint32_t)kDevTimeoutTma);
             *abort_flag = 1;
+        }
+        if (p.wait_cycles) {
+            atomicAdd(&p.wait_cycles[kWaitProdB], w_b);
+            atomicAdd(&p.wait_cycles[kWaitProdA], w_a);
         }
         // Drain: every load issued above has landed before the CTA exits.
         if (t_local > 0 || bq > 0) {
@@ -517,22 +547,27 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
         const uint32_t idesc = make_idesc(kBM, p.bn);
         uint32_t bq = 0, accq = 0, t_local = 0;
         bool ok = true;
+        unsigned long long w_b = 0, w_a = 0, w_acc = 0;
+        const long long t_start = clock64();
+        unsigned long long *pw_b = p.wait_cycles ? &w_b : nullptr;
+        unsigned long long *pw_a = p.wait_cycles ? &w_a : nullptr;
+        unsigned long long *pw_acc = p.wait_cycles ? &w_acc : nullptr;
         for (int64_t ft = blockIdx.x; ft < n_ftiles && ok; ft += gridDim.x, ++t_local) {
             for (int ct = 0; ct < p.n_ctiles && ok; ++ct) {
                 const uint32_t buf = accq & 1u;
-                if (!mbar_wait(&acc_empty[buf], ((accq >> 1) & 1u) ^ 1u)) {
+                if (!mbar_wait_timed(&acc_empty[buf], ((accq >> 1) & 1u) ^ 1u, pw_acc)) {
                     ok = false;
                     break;
                 }
                 tc_fence_after();
                 const uint32_t d_tmem = tmem_base + buf * (uint32_t)p.bn;
                 for (int kc = 0; kc < p.nkc; ++kc) {
-                    if (ct == 0 && !mbar_wait(&a_full[kc], t_local & 1u)) {
+                    if (ct == 0 && !mbar_wait_timed(&a_full[kc], t_local & 1u, pw_a)) {
                         ok = false;
                         break;
                     }
                     const uint32_t s = bq % p.stages;
-                    if (!mbar_wait(&b_full[s], (bq / p.stages) & 1u)) {
+                    if (!mbar_wait_timed(&b_full[s], (bq / p.stages) & 1u, pw_b)) {
                         ok = false;
                         break;
                     }
@@ -558,6 +593,12 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
             atomicOr(p.err, (uint32_t)kDevTimeoutMma);
             *abort_flag = 1;
         }
+        if (p.wait_cycles) {
+            atomicAdd(&p.wait_cycles[kWaitMmaB], w_b);
+            atomicAdd(&p.wait_cycles[kWaitMmaA], w_a);
+            atomicAdd(&p.wait_cycles[kWaitMmaAcc], w_acc);
+            atomicAdd(&p.wait_cycles[kMmaTotal], (unsigned long long)(clock64() - t_start));
+        }
         // Drain: all issued MMAs complete before TMEM is released.
         mma_commit(drain);
         mbar_wait(drain, 0);
@@ -574,6 +615,9 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
         const float kInf = __int_as_float(0x7f800000);
         uint32_t accq = 0;
         bool ok = true;
+        unsigned long long w_acc = 0;
+        const long long t_start = clock64();
+        unsigned long long *pw_acc = (p.wait_cycles && warp == 2 && lane == 0) ? &w_acc : nullptr;
         for (int64_t ft = blockIdx.x; ft < n_ftiles && ok; ft += gridDim.x) {
             const int64_t i = ft * kBM + row;
             const float4 xn = i < p.n ? p.xnorm[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -594,7 +638,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
             }
             for (int ct = 0; ct < p.n_ctiles; ++ct) {
                 const uint32_t buf = accq & 1u;
-                const bool got = __all_sync(0xffffffffu, mbar_wait(&acc_full[buf], (accq >> 1) & 1u));
+                const bool got = __all_sync(0xffffffffu, mbar_wait_timed(&acc_full[buf], (accq >> 1) & 1u, pw_acc));
                 if (!got) {
                     ok = false;
                     break;
@@ -724,6 +768,10 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
         if (!ok) {
             atomicOr(p.err, (uint32_t)kDevTimeoutEpi);
             *abort_flag = 1;
+        }
+        if (pw_acc) {
+            atomicAdd(&p.wait_cycles[kWaitEpiAcc], w_acc);
+            atomicAdd(&p.wait_cycles[kEpiTotal], (unsigned long long)(clock64() - t_start));
         }
     }
 
@@ -885,7 +933,7 @@ size_t tc_assign_ws_size(int64_t n, int d, int k) {
     c.take<int32_t>(nn);
     c.take<int32_t>(nn * kL);
     c.take<int32_t>(nn);
-    c.take<int32_t>(4);
+    c.take<int32_t>(20);
     c.take<unsigned long long>(1);
     c.take<uint32_t>(1);
     return c.bytes();
@@ -899,7 +947,7 @@ void tc_carve_assign(void *ws, int64_t n, int d, int k, TcBuffers &b) {
     b.rc_frames = c.take<int32_t>(nn);
     b.rc_cands = c.take<int32_t>(nn * kL);
     b.full_frames = c.take<int32_t>(nn);
-    b.counters = c.take<int32_t>(4);
+    b.counters = c.take<int32_t>(20);  // [0] recheck entries, [1] full entries, [4..20) diagnostics
     b.flipped = c.take<unsigned long long>(1);
     b.err = c.take<uint32_t>(1);
 }
@@ -936,7 +984,7 @@ int tc_prepare_centers(const float *C, int d, int k, TcBuffers &b, cudaStream_t 
 }
 
 int tc_assign(const float *X, int64_t n, int d, const float *C, int k, int32_t *labels, TcBuffers &b,
-              cudaStream_t s, ProfEvents *prof, float *dump) {
+              cudaStream_t s, ProfEvents *prof, float *dump, unsigned long long *wait_cycles) {
     if (n == 0) return KM_OK;
     Plan pl;
     if (!make_plan(d, k, pl) || !device_is_sm10x()) {
@@ -986,6 +1034,7 @@ int tc_assign(const float *X, int64_t n, int d, const float *C, int k, int32_t *
     p.counters = b.counters;
     p.err = b.err;
     p.dump = dump;
+    p.wait_cycles = wait_cycles;
 
     const int64_t n_ftiles = (n + kBM - 1) / kBM;
     int64_t grid = num_sms();

@@ -281,10 +281,11 @@ int km_batch_assign(const float *X_packed, const int64_t *offsets, int32_t n_tra
 }
 
 int km_debug_tc_distances(const float *X, int64_t n, int32_t d, const float *C, int32_t k, float *V,
-                          int32_t *labels, void *workspace, size_t workspace_bytes, void *stream) {
+                          int32_t *labels, uint64_t *wait_cycles, void *workspace, size_t workspace_bytes,
+                          void *stream) {
     KM_TRY(check_shape(n, d, k));
-    if (n > 0 && (!X || !V || !labels || !C)) {
-        set_error("X, C, V and labels must be non-NULL");
+    if (n > 0 && (!X || !labels || !C)) {
+        set_error("X, C and labels must be non-NULL");
         return KM_ERR_BAD_SHAPE;
     }
     if (!tc_supported(d, k)) {
@@ -299,7 +300,15 @@ int km_debug_tc_distances(const float *X, int64_t n, int32_t d, const float *C, 
     KM_TRY(tc_prepare_shift_from_centers(C, d, k, b, s));
     KM_TRY(tc_prepare_centers(C, d, k, b, s));
     KM_TRY(tc_prepare_frames(X, n, d, b, s));
-    KM_TRY(tc_assign(X, n, d, C, k, labels, b, s, nullptr, V));
+    // The 8 wait counters live in the unused tail of the candidate counters block.
+    unsigned long long *dev_wait = nullptr;
+    if (wait_cycles) {
+        dev_wait = reinterpret_cast<unsigned long long *>(b.counters + 4);
+        KM_CUDA(cudaMemsetAsync(dev_wait, 0, 8 * sizeof(unsigned long long), s));
+    }
+    KM_TRY(tc_assign(X, n, d, C, k, labels, b, s, nullptr, V, dev_wait));
+    if (wait_cycles)
+        KM_CUDA(cudaMemcpyAsync(wait_cycles, dev_wait, 8 * sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
     KM_CUDA(cudaStreamSynchronize(s));
     return KM_OK;
 }

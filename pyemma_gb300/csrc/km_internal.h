@@ -94,8 +94,11 @@ int tc_prepare_shift_from_centers(const float *C, int d, int k, TcBuffers &b, cu
 int tc_prepare_frames(const float *X, int64_t n, int d, TcBuffers &b, cudaStream_t s);
 int tc_prepare_centers(const float *C, int d, int k, TcBuffers &b, cudaStream_t s);
 // Runs the tensor-core pass, the candidate recheck and the full recheck.
-// dump (nullable, n x k floats) receives every tensor-core distance (diagnostics).
+// dump (nullable, n x k floats) receives every tensor-core distance;
+// wait_cycles (nullable, 8 device counters) the cycles each kernel role
+// spent waiting (diagnostics).
 int tc_assign(const float *X, int64_t n, int d, const float *C, int k, int32_t *labels,
-              TcBuffers &b, cudaStream_t s, ProfEvents *prof = nullptr, float *dump = nullptr);
+              TcBuffers &b, cudaStream_t s, ProfEvents *prof = nullptr, float *dump = nullptr,
+              unsigned long long *wait_cycles = nullptr);
 
 }  // namespace km

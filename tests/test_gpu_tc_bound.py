@@ -41,7 +41,7 @@ def bound_terms(X, C):
 def check_pairs(L, torch, oracle, X, C):
     Xd = torch.from_numpy(X).cuda()
     Cd = torch.from_numpy(C).cuda()
-    labels, V = L.debug_tc_distances(Xd, Cd)
+    labels, V, _ = L.debug_tc_distances(Xd, Cd)
     V = V.cpu().numpy().astype(np.float64)
     t = bound_terms(X, C)
     R, E, g = t["R"], t["E"], t["g"]
