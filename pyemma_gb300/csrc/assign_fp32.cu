@@ -138,50 +138,44 @@ int launch_cfg(const float *X, const int32_t *frame_idx, const int32_t *n_dev, i
     return KM_OK;
 }
 
-// Kernel (b'): one group of L threads per entry, one thread per candidate.
-__global__ void __launch_bounds__(256) recheck_candidates_kernel(
-    const float *__restrict__ X, int d, const float *__restrict__ C,
-    const int32_t *__restrict__ rc_frames, const int32_t *__restrict__ rc_cands, int L,
-    const int32_t *__restrict__ rc_count, int64_t max_entries, int32_t *__restrict__ labels,
+// Kernel (b'): exact float32 distance of every (entry, candidate) pair, one
+// thread per pair.  The key (distance bits << 32 | center) of a non-negative
+// float orders lexicographically as an unsigned integer, so atomicMin keeps
+// the smallest distance and, among equal distances, the lowest center.
+__global__ void __launch_bounds__(256) recheck_pairs_kernel(
+    const float *__restrict__ X, int d, const float *__restrict__ C, const int32_t *__restrict__ rc_frames,
+    const int32_t *__restrict__ pair_entry, const int32_t *__restrict__ pair_center,
+    const int32_t *__restrict__ pair_count, int64_t max_pairs, unsigned long long *__restrict__ keys) {
+    int64_t count = *pair_count;
+    if (count > max_pairs) count = max_pairs;
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < count;
+         q += (int64_t)gridDim.x * blockDim.x) {
+        const int e = pair_entry[q];
+        const int j = pair_center[q];
+        const int64_t frame = rc_frames[e];
+        const float dd = sqdist_exact(X + frame * d, C + (int64_t)j * d, d);
+        const unsigned long long key = ((unsigned long long)__float_as_uint(dd) << 32) | (unsigned)j;
+        atomicMin(&keys[e], key);
+    }
+}
+
+// One thread per entry: the winning key becomes the label (label 0 when no
+// candidate distance is finite, as in the exact kernel).
+__global__ void __launch_bounds__(256) recheck_finalize_kernel(
+    const int32_t *__restrict__ rc_frames, const unsigned long long *__restrict__ keys,
+    const int32_t *__restrict__ entry_count, int64_t max_entries, int32_t *__restrict__ labels,
     unsigned long long *flipped) {
-    int64_t count = *rc_count;
+    int64_t count = *entry_count;
     if (count > max_entries) count = max_entries;
-    const int per_block = blockDim.x / L;
-    const int sub = threadIdx.x % L;
-    const int grp = threadIdx.x / L;
     unsigned long long nflip = 0;
-    // Every thread runs the same number of iterations so that the shuffles
-    // below see full warps.
-    const int64_t rounds = (count + (int64_t)per_block * gridDim.x - 1) / ((int64_t)per_block * gridDim.x);
-    for (int64_t it = 0; it < rounds; ++it) {
-        const int64_t e = (it * gridDim.x + blockIdx.x) * per_block + grp;
-        float bd = __int_as_float(0x7f800000);
-        int bj = 0x7fffffff;
-        int64_t frame = -1;
-        if (e < count) {
-            frame = rc_frames[e];
-            const int j = rc_cands[e * L + sub];
-            if (j >= 0) {
-                const float dd = sqdist_exact(X + frame * d, C + (int64_t)j * d, d);
-                if (dd < __int_as_float(0x7f800000)) {  // inf and NaN never win
-                    bd = dd;
-                    bj = j;
-                }
-            }
-        }
-        for (int off = L >> 1; off > 0; off >>= 1) {
-            float od = __shfl_xor_sync(0xffffffffu, bd, off);
-            int oj = __shfl_xor_sync(0xffffffffu, bj, off);
-            if (od < bd || (od == bd && oj < bj)) {
-                bd = od;
-                bj = oj;
-            }
-        }
-        if (sub == 0 && e < count) {
-            const int lbl = bj == 0x7fffffff ? 0 : bj;  // no finite distance: label 0
-            if (labels[frame] != lbl) ++nflip;
-            labels[frame] = lbl;
-        }
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < count;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const unsigned long long key = keys[e];
+        const uint32_t dbits = (uint32_t)(key >> 32);
+        const int lbl = dbits < 0x7f800000u ? (int)(uint32_t)key : 0;
+        const int64_t frame = rc_frames[e];
+        if (labels[frame] != lbl) ++nflip;
+        labels[frame] = lbl;
     }
     if (flipped && nflip) atomicAdd(flipped, nflip);
 }
@@ -192,27 +186,30 @@ int launch_assign_fp32(const float *X, const int32_t *frame_idx, const int32_t *
                        int d, const float *C, int k, int32_t *labels, float *dist,
                        unsigned long long *flipped, cudaStream_t s) {
     if (n == 0) return KM_OK;
+    // Index lists (frames re-evaluated after the tensor-core pass) are short:
+    // 8-frame tiles spread them over all SMs.
+    if (frame_idx) return launch_cfg<1, 8>(X, frame_idx, n_dev, n, d, C, k, labels, dist, flipped, s);
     if (k <= 32) return launch_cfg<4, 1>(X, frame_idx, n_dev, n, d, C, k, labels, dist, flipped, s);
     if (k <= 64) return launch_cfg<4, 2>(X, frame_idx, n_dev, n, d, C, k, labels, dist, flipped, s);
     if (k <= 128) return launch_cfg<4, 4>(X, frame_idx, n_dev, n, d, C, k, labels, dist, flipped, s);
     return launch_cfg<4, 8>(X, frame_idx, n_dev, n, d, C, k, labels, dist, flipped, s);
 }
 
-int launch_recheck_candidates(const float *X, int d, const float *C, const int32_t *rc_frames,
-                              const int32_t *rc_cands, int L, const int32_t *rc_count,
-                              int64_t max_entries, int32_t *labels, unsigned long long *flipped,
-                              cudaStream_t s) {
+int launch_recheck_pairs(const float *X, int d, const float *C, const int32_t *rc_frames,
+                         const int32_t *pair_entry, const int32_t *pair_center, unsigned long long *keys,
+                         const int32_t *counters, int64_t max_entries, int64_t max_pairs, int32_t *labels,
+                         unsigned long long *flipped, cudaStream_t s) {
     if (max_entries == 0) return KM_OK;
-    if (L < 1 || L > 32 || (L & (L - 1))) {
-        set_error("candidate list length %d must be a power of two <= 32", L);
-        return KM_ERR_BAD_SHAPE;
-    }
-    int64_t per_block = 256 / L;
-    int64_t grid = (max_entries + per_block - 1) / per_block;
-    int64_t cap = (int64_t)num_sms() * 8;
-    if (grid > cap) grid = cap;
-    recheck_candidates_kernel<<<(unsigned)grid, 256, 0, s>>>(X, d, C, rc_frames, rc_cands, L, rc_count,
-                                                             max_entries, labels, flipped);
+    const int64_t cap = (int64_t)num_sms() * 8;
+    int64_t g1 = (max_pairs + 255) / 256;
+    if (g1 > cap) g1 = cap;
+    recheck_pairs_kernel<<<(unsigned)(g1 < 1 ? 1 : g1), 256, 0, s>>>(X, d, C, rc_frames, pair_entry, pair_center,
+                                                                    counters + 2, max_pairs, keys);
+    KM_CUDA(cudaGetLastError());
+    int64_t g2 = (max_entries + 255) / 256;
+    if (g2 > cap) g2 = cap;
+    recheck_finalize_kernel<<<(unsigned)(g2 < 1 ? 1 : g2), 256, 0, s>>>(rc_frames, keys, counters, max_entries,
+                                                                       labels, flipped);
     KM_CUDA(cudaGetLastError());
     return KM_OK;
 }

@@ -89,7 +89,9 @@ struct TcParams {
     const uint32_t *scal;
     int32_t *labels;
     int32_t *rc_frames;
-    int32_t *rc_cands;
+    int32_t *pair_entry;
+    int32_t *pair_center;
+    unsigned long long *rc_keys;
     int32_t *full_frames;
     int32_t *counters;
     uint32_t *err;
@@ -571,7 +573,8 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                         ok = false;
                         break;
                     }
-                    tc_fence_after();
+                    // TMA completion on the mbarrier orders the loaded tiles before
+                    // the MMAs; no tcgen05 fence is needed here.
                     const int nks = (kc == p.nkc - 1) ? p.ksteps_last : (kKC / 16);
                     const uint32_t a0 = smem_u32(sA + kc * kABytesPerChunk);
                     const uint32_t b0 = smem_u32(sB + s * b_stage_bytes);
@@ -739,19 +742,36 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
             }
             const unsigned m_rc = __ballot_sync(0xffffffffu, need_rc);
             if (m_rc) {
+                // One entry per re-checked frame and one pair per candidate,
+                // both appended with a single atomic per warp.
                 const int leader = __ffs(m_rc) - 1;
-                int base = 0;
-                if (lane == leader) base = atomicAdd(&p.counters[0], __popc(m_rc));
+                const int npairs = need_rc ? __popc(cmask) : 0;
+                int excl = npairs;
+#pragma unroll
+                for (int off = 1; off < 32; off <<= 1) {
+                    const int v = __shfl_up_sync(0xffffffffu, excl, off);
+                    if (lane >= off) excl += v;
+                }
+                const int total = __shfl_sync(0xffffffffu, excl, 31);
+                excl -= npairs;
+                int base = 0, pbase = 0;
+                if (lane == leader) {
+                    base = atomicAdd(&p.counters[0], __popc(m_rc));
+                    pbase = atomicAdd(&p.counters[2], total);
+                }
                 base = __shfl_sync(0xffffffffu, base, leader);
+                pbase = __shfl_sync(0xffffffffu, pbase, leader);
                 if (need_rc) {
                     const int e = base + __popc(m_rc & ((1u << lane) - 1u));
                     p.rc_frames[e] = (int32_t)i;
-                    int32_t *dst = p.rc_cands + (int64_t)e * kL;
-                    const int ncand = __popc(cmask);
+                    p.rc_keys[e] = ~0ull;
 #pragma unroll
                     for (int m = 0; m < kL; ++m) {
-                        if ((cmask >> m) & 1u) dst[__popc(cmask & ((1u << m) - 1u))] = lid[m];
-                        if (m >= ncand) dst[m] = -1;
+                        if ((cmask >> m) & 1u) {
+                            const int q = pbase + excl + __popc(cmask & ((1u << m) - 1u));
+                            p.pair_entry[q] = e;
+                            p.pair_center[q] = lid[m];
+                        }
                     }
                 }
             }
@@ -932,6 +952,8 @@ size_t tc_assign_ws_size(int64_t n, int d, int k) {
     const size_t nn = n > 0 ? n : 1;
     c.take<int32_t>(nn);
     c.take<int32_t>(nn * kL);
+    c.take<int32_t>(nn * kL);
+    c.take<unsigned long long>(nn);
     c.take<int32_t>(nn);
     c.take<int32_t>(20);
     c.take<unsigned long long>(1);
@@ -945,7 +967,9 @@ void tc_carve_assign(void *ws, int64_t n, int d, int k, TcBuffers &b) {
     Carver c(ws);
     const size_t nn = n > 0 ? n : 1;
     b.rc_frames = c.take<int32_t>(nn);
-    b.rc_cands = c.take<int32_t>(nn * kL);
+    b.pair_entry = c.take<int32_t>(nn * kL);
+    b.pair_center = c.take<int32_t>(nn * kL);
+    b.rc_keys = c.take<unsigned long long>(nn);
     b.full_frames = c.take<int32_t>(nn);
     b.counters = c.take<int32_t>(20);  // [0] recheck entries, [1] full entries, [4..20) diagnostics
     b.flipped = c.take<unsigned long long>(1);
@@ -1029,7 +1053,9 @@ int tc_assign(const float *X, int64_t n, int d, const float *C, int k, int32_t *
     p.scal = b.scal;
     p.labels = labels;
     p.rc_frames = b.rc_frames;
-    p.rc_cands = b.rc_cands;
+    p.pair_entry = b.pair_entry;
+    p.pair_center = b.pair_center;
+    p.rc_keys = b.rc_keys;
     p.full_frames = b.full_frames;
     p.counters = b.counters;
     p.err = b.err;
@@ -1045,7 +1071,8 @@ int tc_assign(const float *X, int64_t n, int d, const float *C, int k, int32_t *
     if (prof) prof->end(kProfTc, s);
 
     if (prof) prof->begin(kProfRecheck, s);
-    KM_TRY(launch_recheck_candidates(X, d, C, b.rc_frames, b.rc_cands, kL, b.counters, n, labels, b.flipped, s));
+    KM_TRY(launch_recheck_pairs(X, d, C, b.rc_frames, b.pair_entry, b.pair_center, b.rc_keys, b.counters, n,
+                                n * kL, labels, b.flipped, s));
     KM_TRY(launch_assign_fp32(X, b.full_frames, b.counters + 1, n, d, C, k, labels, nullptr, b.flipped, s));
     if (prof) prof->end(kProfRecheck, s);
     return KM_OK;

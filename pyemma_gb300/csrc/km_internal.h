@@ -35,13 +35,14 @@ int launch_assign_fp32(const float *X, const int32_t *frame_idx, const int32_t *
                        int d, const float *C, int k, int32_t *labels, float *dist,
                        unsigned long long *flipped, cudaStream_t s);
 
-// Exact float32 re-evaluation of candidate lists written by the tensor-core
-// kernel: entry e holds frame rc_frames[e] and L candidate indices
-// rc_cands[e*L .. e*L+L) (-1 = unused).  The entry count is *rc_count.
-int launch_recheck_candidates(const float *X, int d, const float *C, const int32_t *rc_frames,
-                              const int32_t *rc_cands, int L, const int32_t *rc_count,
-                              int64_t max_entries, int32_t *labels, unsigned long long *flipped,
-                              cudaStream_t s);
+// Exact float32 re-evaluation of the candidates the tensor-core kernel could
+// not separate: pair q = (entry pair_entry[q], center pair_center[q]); entry e
+// stands for frame rc_frames[e] and keys[e] (initialised to ~0) collects the
+// winner.  counters[0] = entries, counters[2] = pairs (device).
+int launch_recheck_pairs(const float *X, int d, const float *C, const int32_t *rc_frames,
+                         const int32_t *pair_entry, const int32_t *pair_center, unsigned long long *keys,
+                         const int32_t *counters, int64_t max_entries, int64_t max_pairs, int32_t *labels,
+                         unsigned long long *flipped, cudaStream_t s);
 
 // ---- update.cu -------------------------------------------------------------
 size_t update_ws_size(int64_t n, int d, int k);
@@ -76,10 +77,12 @@ struct TcBuffers {
     float *shift = nullptr;      // d floats
     uint32_t *scal = nullptr;    // scale, 1/scale^2, norm maxima (float bits)
     // candidate lists
-    int32_t *rc_frames = nullptr;
-    int32_t *rc_cands = nullptr;
+    int32_t *rc_frames = nullptr;           // entry -> frame
+    int32_t *pair_entry = nullptr;          // pair -> entry
+    int32_t *pair_center = nullptr;         // pair -> candidate center
+    unsigned long long *rc_keys = nullptr;  // entry -> (distance bits, center) minimum
     int32_t *full_frames = nullptr;
-    int32_t *counters = nullptr;  // [0] recheck entries, [1] full entries
+    int32_t *counters = nullptr;  // [0] recheck entries, [1] full entries, [2] pairs
     unsigned long long *flipped = nullptr;
     uint32_t *err = nullptr;
     int kp = 0;
