@@ -357,7 +357,7 @@ def run_ours(args):
         dist.destroy_process_group()
     if rank != 0:
         return
-    launches_per_step = 10  # prep_centers, tc, 2 rechecks, 6 update kernels
+    launches_per_step = 11  # prep_centers, tc, 2 pair-recheck kernels, full recheck, 6 update kernels
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "fp16 distances (fp32 accumulate), fp32 recheck, f64 sums",

@@ -79,7 +79,8 @@ const char *km_last_error(void);
  * km_lloyd calls record an event pair around their main kernels, including
  * inside CUDA-graph replays; the pair is read at the synchronisation points
  * these calls already have.  kind: 0 tensor-core distance kernel, 1 exact
- * FP32 assignment kernel, 2 exact recheck kernels, 3 centroid update.
+ * FP32 assignment kernel, 2 exact recheck of candidate pairs, 3 centroid
+ * update, 4 exact recheck of frames over all centers.
  * km_profile_read returns the summed milliseconds and the launch count. */
 int km_profile_enable(int on);
 int km_profile_read(int32_t kind, double *ms_total, int64_t *launches);

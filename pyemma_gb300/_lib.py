@@ -106,7 +106,7 @@ def load(build_if_missing=False):
     return L
 
 
-PROFILE_KINDS = {"tc": 0, "fp32": 1, "recheck": 2, "update": 3}
+PROFILE_KINDS = {"tc": 0, "fp32": 1, "recheck": 2, "update": 3, "full_recheck": 4}
 
 
 def profile_enable(on=True):

@@ -1073,8 +1073,10 @@ int tc_assign(const float *X, int64_t n, int d, const float *C, int k, int32_t *
     if (prof) prof->begin(kProfRecheck, s);
     KM_TRY(launch_recheck_pairs(X, d, C, b.rc_frames, b.pair_entry, b.pair_center, b.rc_keys, b.counters, n,
                                 n * kL, labels, b.flipped, s));
-    KM_TRY(launch_assign_fp32(X, b.full_frames, b.counters + 1, n, d, C, k, labels, nullptr, b.flipped, s));
     if (prof) prof->end(kProfRecheck, s);
+    if (prof) prof->begin(kProfFull, s);
+    KM_TRY(launch_assign_fp32(X, b.full_frames, b.counters + 1, n, d, C, k, labels, nullptr, b.flipped, s));
+    if (prof) prof->end(kProfFull, s);
     return KM_OK;
 }
 

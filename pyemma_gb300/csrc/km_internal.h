@@ -13,7 +13,7 @@ namespace km {
 // Event pairs recorded around the main kernels of one pass when profiling is
 // on (km_profile_enable).  Inside a captured graph the records become event
 // nodes, so every replay re-times the same launches.
-enum ProfKind { kProfTc = 0, kProfFp32 = 1, kProfRecheck = 2, kProfUpdate = 3, kProfKinds = 4 };
+enum ProfKind { kProfTc = 0, kProfFp32 = 1, kProfRecheck = 2, kProfUpdate = 3, kProfFull = 4, kProfKinds = 5 };
 
 struct ProfEvents {
     cudaEvent_t ev[kProfKinds][2] = {};
@@ -65,7 +65,7 @@ size_t tc_frames_ws_size(int64_t n, int d);     // fp16 frame copy + norms
 size_t tc_centers_ws_size(int d, int k);        // fp16 centers + norms + shift + scalars
 size_t tc_assign_ws_size(int64_t n, int d, int k);  // candidate lists + counters
 
-#define TC_CANDIDATES 8  // candidate centers kept per frame by the tensor-core pass
+#define TC_CANDIDATES 16  // candidate centers kept per frame by the tensor-core pass
 
 struct TcBuffers {
     // frames
