@@ -60,7 +60,8 @@ namespace {
 
 constexpr int kBM = 128;          // frames per tile (UMMA M)
 constexpr int kKC = 64;           // fp16 elements per K chunk (128 B, one SW128 row)
-constexpr int kL = TC_CANDIDATES; // candidates kept per frame
+constexpr int kL = TC_CANDIDATES; // candidate slots per frame (shared memory)
+constexpr int kCandBytes = kL * kBM * 8;  // per CTA: kL x 128 (float, int) slots
 constexpr int kThreadsTC = 192;   // warp 0 TMA, warp 1 MMA, warps 2-5 epilogue
 constexpr int kMaxNkc = 10;       // resident A tile up to kp = 640
 constexpr int kSmemLimit = 232448;
@@ -427,6 +428,22 @@ __device__ __forceinline__ float hi_bound(float v, float E, float R, float g_hi)
     return __fadd_ru(__fmul_ru(__fmul_ru(a, a), g_hi), 1e-37f);
 }
 
+// Drops the slots of one frame whose value fell below the threshold (the
+// threshold only rises); returns the new count.  Kept out of line: it runs
+// rarely and the callers are unrolled.
+__device__ __noinline__ int compact_slots(float *a, int *j, int cnt, float thr) {
+    int w = 0;
+    for (int s = 0; s < cnt; ++s) {
+        const float v = a[s * kBM];
+        if (v >= thr) {
+            a[w * kBM] = v;
+            j[w * kBM] = j[s * kBM];
+            ++w;
+        }
+    }
+    return w;
+}
+
 // Rounding of the float32 centering x' = fl(x - m): at most 2^-24 |x - m|
 // per component, so 2^-23 (sx + sc) covers both operands.
 constexpr float kCenterEps = 1.1920929e-07f;  // 2^-23
@@ -453,7 +470,9 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
     uint8_t *sA = smem;
     uint8_t *sB = sA + p.nkc * kABytesPerChunk;
     const int b_stage_bytes = p.bn * 128;
-    uint64_t *bars = reinterpret_cast<uint64_t *>(sB + p.stages * b_stage_bytes);
+    float *cand_a = reinterpret_cast<float *>(sB + p.stages * b_stage_bytes);  // [kL][128]
+    int *cand_j = reinterpret_cast<int *>(cand_a + kL * kBM);                   // [kL][128]
+    uint64_t *bars = reinterpret_cast<uint64_t *>(reinterpret_cast<uint8_t *>(cand_a) + kCandBytes);
     uint64_t *a_full = bars;
     uint64_t *a_empty = a_full + p.nkc;
     uint64_t *b_full = a_empty + p.nkc;
@@ -616,6 +635,8 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
         const float hc_max = __uint_as_float(p.scal[kHcMax]);
         const float kNegInf = __int_as_float(0xff800000);
         const float kInf = __int_as_float(0x7f800000);
+        float *my_a = cand_a + row;  // slot s at my_a[s * kBM]
+        int *my_j = cand_j + row;
         uint32_t accq = 0;
         bool ok = true;
         unsigned long long w_acc = 0;
@@ -630,15 +651,55 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
             const float Rmax = __fadd_ru(__fadd_ru(xn.z, hc_max), __fmul_ru(kCenterEps, smax));
             const float Emax = __fmul_ru(p.e_coef, __fmul_ru(smax, smax));
             float best = kNegInf, thr = kNegInf;
-            int best_id = 0;
+            int best_id = 0, cnt = 0;
             bool ovf = false;
-            float la[kL];
-            int lid[kL];
+
+            // One 32-column chunk: skipped unless some lane of the warp has a
+            // value at or above its threshold; then appends those values to the
+            // lane's slots (predicated stores).
+            auto chunk = [&](const uint32_t (&r)[32], int j0) {
+                float v[32];
 #pragma unroll
-            for (int m = 0; m < kL; ++m) {
-                la[m] = kNegInf;
-                lid[m] = -1;
-            }
+                for (int c = 0; c < 32; ++c) v[c] = __uint_as_float(r[c]);
+                if (j0 + 32 > p.k) {
+#pragma unroll
+                    for (int c = 0; c < 32; ++c)
+                        if (j0 + c >= p.k) v[c] = kNegInf;
+                }
+                if (p.dump && i < p.n) {
+#pragma unroll
+                    for (int c = 0; c < 32; ++c)
+                        if (j0 + c < p.k) p.dump[i * p.k + j0 + c] = fmaf(-2.0f, v[c], xn.x) * inv_s2;
+                }
+                float mx = v[0];
+#pragma unroll
+                for (int c = 1; c < 32; ++c) mx = fmaxf(mx, v[c]);
+                const bool hit = mx >= thr && mx > kNegInf;
+                if (!__any_sync(0xffffffffu, hit)) return;
+                if (hit && mx > best) {
+                    int bc = 31;
+#pragma unroll
+                    for (int c = 31; c >= 0; --c)
+                        if (v[c] == mx) bc = c;
+                    best = mx;
+                    best_id = j0 + bc;
+                    thr = window_threshold(best, xn.x, inv_s2, s2, Emax, Rmax, p.g_lo, p.g_hi);
+                }
+#pragma unroll
+                for (int c = 0; c < 32; ++c) {
+                    if (v[c] >= thr) {
+                        if (cnt == kL) cnt = compact_slots(my_a, my_j, cnt, thr);
+                        if (cnt < kL) {
+                            my_a[cnt * kBM] = v[c];
+                            my_j[cnt * kBM] = j0 + c;
+                            ++cnt;
+                        } else {
+                            ovf = true;
+                        }
+                    }
+                }
+            };
+
             for (int ct = 0; ct < p.n_ctiles; ++ct) {
                 const uint32_t buf = accq & 1u;
                 const bool got = __all_sync(0xffffffffu, mbar_wait_timed(&acc_full[buf], (accq >> 1) & 1u, pw_acc));
@@ -648,51 +709,15 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                 }
                 tc_fence_after();
                 const uint32_t tbase = tmem_base + lane_off + buf * (uint32_t)p.bn;
-                for (int cc = 0; cc < p.bn; cc += 32) {
-                    uint32_t r[32];
-                    tmem_ld32(tbase + cc, r);
+                for (int cc = 0; cc < p.bn; cc += 64) {
+                    // Two TMEM loads in flight before one wait.
+                    uint32_t r0[32], r1[32];
+                    const bool two = cc + 32 < p.bn;
+                    tmem_ld32(tbase + cc, r0);
+                    if (two) tmem_ld32(tbase + cc + 32, r1);
                     tmem_wait_ld();
-                    const int j0 = ct * p.bn + cc;
-                    float v[32];
-#pragma unroll
-                    for (int c = 0; c < 32; ++c) v[c] = __uint_as_float(r[c]);
-                    if (j0 + 32 > p.k) {
-#pragma unroll
-                        for (int c = 0; c < 32; ++c)
-                            if (j0 + c >= p.k) v[c] = kNegInf;
-                    }
-                    if (p.dump && i < p.n) {
-#pragma unroll
-                        for (int c = 0; c < 32; ++c)
-                            if (j0 + c < p.k) p.dump[i * p.k + j0 + c] = fmaf(-2.0f, v[c], xn.x) * inv_s2;
-                    }
-                    float mx = v[0];
-#pragma unroll
-                    for (int c = 1; c < 32; ++c) mx = fmaxf(mx, v[c]);
-                    if (mx >= thr && mx > kNegInf) {
-                        if (mx > best) {
-                            int bc = 31;
-#pragma unroll
-                            for (int c = 31; c >= 0; --c)
-                                if (v[c] == mx) bc = c;
-                            best = mx;
-                            best_id = j0 + bc;
-                            thr = window_threshold(best, xn.x, inv_s2, s2, Emax, Rmax, p.g_lo, p.g_hi);
-                        }
-#pragma unroll
-                        for (int c = 0; c < 32; ++c) {
-                            if (v[c] >= thr) {
-                                if (lid[kL - 1] >= 0 && la[kL - 1] >= thr) ovf = true;
-#pragma unroll
-                                for (int m = kL - 1; m > 0; --m) {
-                                    la[m] = la[m - 1];
-                                    lid[m] = lid[m - 1];
-                                }
-                                la[0] = v[c];
-                                lid[0] = j0 + c;
-                            }
-                        }
-                    }
+                    chunk(r0, ct * p.bn + cc);
+                    if (two) chunk(r1, ct * p.bn + cc + 32);
                 }
                 tc_fence_before();
                 __syncwarp();
@@ -703,49 +728,49 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
 
             // ---- decision ----
             bool need_rc = false, need_full = false;
-            unsigned cmask = 0;  // bit m: list entry m is a candidate
+            int ncand = 0, first = -1;
+            float H = kInf;
             if (i < p.n) {
-                float vv[kL], RR[kL], EE[kL];
-                float H = kInf;
-#pragma unroll
-                for (int m = 0; m < kL; ++m) {
-                    vv[m] = kInf;
-                    RR[m] = 0.0f;
-                    EE[m] = 0.0f;
-                    if (lid[m] >= 0 && la[m] >= thr) {
-                        const float2 cn = p.cnorm[lid[m]];
+                // Entries still above the final threshold; H = min of their upper ends.
+                for (int s = 0; s < cnt; ++s) {
+                    const float a = my_a[s * kBM];
+                    if (a >= thr) {
+                        const float2 cn = p.cnorm[my_j[s * kBM]];
                         const float sj = xn.y + cn.x;
-                        RR[m] = __fadd_ru(__fadd_ru(xn.z, cn.y), __fmul_ru(kCenterEps, sj));
-                        EE[m] = __fmul_ru(p.e_coef, __fmul_ru(sj, sj));
-                        vv[m] = fmaf(-2.0f, la[m], xn.x) * inv_s2;
-                        H = fminf(H, hi_bound(vv[m], EE[m], RR[m], p.g_hi));
+                        const float R = __fadd_ru(__fadd_ru(xn.z, cn.y), __fmul_ru(kCenterEps, sj));
+                        const float E = __fmul_ru(p.e_coef, __fmul_ru(sj, sj));
+                        H = fminf(H, hi_bound(fmaf(-2.0f, a, xn.x) * inv_s2, E, R, p.g_hi));
                     }
                 }
                 const bool finite = best > kNegInf && H < kInf && Rmax < kInf && Emax < kInf;
                 if (!finite || ovf) {
                     need_full = true;
                 } else {
-#pragma unroll
-                    for (int m = 0; m < kL; ++m)
-                        if (vv[m] < kInf && lo_bound(vv[m], EE[m], RR[m], p.g_lo) <= H) cmask |= 1u << m;
-                    const int nc = __popc(cmask);
-                    if (nc == 0) need_full = true;
-                    else if (nc > 1) need_rc = true;
+                    for (int s = 0; s < cnt; ++s) {
+                        const float a = my_a[s * kBM];
+                        if (a >= thr) {
+                            const int j = my_j[s * kBM];
+                            const float2 cn = p.cnorm[j];
+                            const float sj = xn.y + cn.x;
+                            const float R = __fadd_ru(__fadd_ru(xn.z, cn.y), __fmul_ru(kCenterEps, sj));
+                            const float E = __fmul_ru(p.e_coef, __fmul_ru(sj, sj));
+                            if (lo_bound(fmaf(-2.0f, a, xn.x) * inv_s2, E, R, p.g_lo) <= H) {
+                                if (first < 0) first = j;
+                                ++ncand;
+                            }
+                        }
+                    }
+                    if (ncand == 0) need_full = true;
+                    else if (ncand > 1) need_rc = true;
                 }
-                int lab = best_id;
-                if (!need_full && !need_rc) {
-#pragma unroll
-                    for (int m = 0; m < kL; ++m)
-                        if (cmask == (1u << m)) lab = lid[m];
-                }
-                p.labels[i] = lab;
+                p.labels[i] = (!need_full && ncand == 1) ? first : best_id;
             }
             const unsigned m_rc = __ballot_sync(0xffffffffu, need_rc);
             if (m_rc) {
                 // One entry per re-checked frame and one pair per candidate,
                 // both appended with a single atomic per warp.
                 const int leader = __ffs(m_rc) - 1;
-                const int npairs = need_rc ? __popc(cmask) : 0;
+                const int npairs = need_rc ? ncand : 0;
                 int excl = npairs;
 #pragma unroll
                 for (int off = 1; off < 32; off <<= 1) {
@@ -765,12 +790,20 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                     const int e = base + __popc(m_rc & ((1u << lane) - 1u));
                     p.rc_frames[e] = (int32_t)i;
                     p.rc_keys[e] = ~0ull;
-#pragma unroll
-                    for (int m = 0; m < kL; ++m) {
-                        if ((cmask >> m) & 1u) {
-                            const int q = pbase + excl + __popc(cmask & ((1u << m) - 1u));
-                            p.pair_entry[q] = e;
-                            p.pair_center[q] = lid[m];
+                    int q = pbase + excl;
+                    for (int s = 0; s < cnt; ++s) {
+                        const float a = my_a[s * kBM];
+                        if (a >= thr) {
+                            const int j = my_j[s * kBM];
+                            const float2 cn = p.cnorm[j];
+                            const float sj = xn.y + cn.x;
+                            const float R = __fadd_ru(__fadd_ru(xn.z, cn.y), __fmul_ru(kCenterEps, sj));
+                            const float E = __fmul_ru(p.e_coef, __fmul_ru(sj, sj));
+                            if (lo_bound(fmaf(-2.0f, a, xn.x) * inv_s2, E, R, p.g_lo) <= H) {
+                                p.pair_entry[q] = e;
+                                p.pair_center[q] = j;
+                                ++q;
+                            }
                         }
                     }
                 }
@@ -865,8 +898,12 @@ bool make_plan(int d, int k, Plan &pl) {
     pl.nkc = kp_of(d) / kKC;
     if (pl.nkc > kMaxNkc) return false;
     pl.bn = pick_bn(k);
-    const int fixed = 1024 + 512 + pl.nkc * kABytesPerChunk;
+    const int fixed = 1024 + 512 + kCandBytes + pl.nkc * kABytesPerChunk;
     int stages = (kSmemLimit - fixed) / (pl.bn * 128);
+    if (stages < 2 && pl.bn > 128) {
+        pl.bn = 128;
+        stages = (kSmemLimit - fixed) / (pl.bn * 128);
+    }
     if (stages > 6) stages = 6;
     if (stages < 2) return false;
     pl.stages = stages;

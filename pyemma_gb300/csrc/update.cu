@@ -160,48 +160,39 @@ __global__ void __launch_bounds__(256) seg_accumulate_wide_kernel(
             for (int off = 16; off > 0; off >>= 1) q += __shfl_xor_sync(0xffffffffu, q, off);
             if (lane == 0) atomicAdd(&Q[cur], q);
         };
-        // Rows go two at a time: both rows' loads are issued before either is
-        // accumulated, doubling the loads in flight per warp.
-        auto accumulate = [&](int l, const float (&xv)[MW]) {
-            if (l != cur) {
-                if (cur >= 0) flush();
-                cur = l;
-                qacc.reset();
-#pragma unroll
-                for (int m = 0; m < MW; ++m) {
-                    const int f = f_base + lane + 32 * m;
-                    acc[m].reset();
-                    cold[m] = f < d ? __ldg(C_old + (int64_t)l * d + f) : 0.0f;
-                }
-            }
-#pragma unroll
-            for (int m = 0; m < MW; ++m) {
-                const int f = f_base + lane + 32 * m;
-                if (f < d) {
-                    const float t = xv[m] - cold[m];
-                    acc[m].add(t);
-                    qacc.add(t * t);
-                }
-            }
-        };
 #pragma unroll
         for (int g = 0; g < kGroups; ++g) {
-            for (int r = 0; r < 32; r += 2) {
-                const int l0 = __shfl_sync(0xffffffffu, my_l[g], r);
-                const int l1 = __shfl_sync(0xffffffffu, my_l[g], r + 1);
-                if (l0 < 0) break;
-                const int64_t i0 = __shfl_sync(0xffffffffu, my_i[g], r);
-                const int64_t i1 = __shfl_sync(0xffffffffu, my_i[g], r + 1);
-                float x0[MW], x1[MW];
+            for (int r = 0; r < 32; ++r) {
+                const int l = __shfl_sync(0xffffffffu, my_l[g], r);
+                if (l < 0) break;
+                const int64_t i = __shfl_sync(0xffffffffu, my_i[g], r);
+                if (l != cur) {
+                    if (cur >= 0) flush();
+                    cur = l;
+                    qacc.reset();
+#pragma unroll
+                    for (int m = 0; m < MW; ++m) {
+                        const int f = f_base + lane + 32 * m;
+                        acc[m].reset();
+                        cold[m] = f < d ? __ldg(C_old + (int64_t)l * d + f) : 0.0f;
+                    }
+                }
+                const float *x = X + i * d;
+                float xv[MW];
 #pragma unroll
                 for (int m = 0; m < MW; ++m) {
                     const int f = f_base + lane + 32 * m;
-                    x0[m] = f < d ? __ldg(X + i0 * d + f) : 0.0f;
-                    x1[m] = (f < d && l1 >= 0) ? __ldg(X + i1 * d + f) : 0.0f;
+                    xv[m] = f < d ? __ldg(x + f) : 0.0f;
                 }
-                accumulate(l0, x0);
-                if (l1 < 0) break;
-                accumulate(l1, x1);
+#pragma unroll
+                for (int m = 0; m < MW; ++m) {
+                    const int f = f_base + lane + 32 * m;
+                    if (f < d) {
+                        const float t = xv[m] - cold[m];
+                        acc[m].add(t);
+                        qacc.add(t * t);
+                    }
+                }
             }
         }
         if (cur >= 0) flush();
