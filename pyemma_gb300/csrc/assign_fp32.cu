@@ -24,11 +24,15 @@ constexpr int kWarps = 8;
 constexpr int kThreads = kWarps * 32;
 constexpr int kFC = 32;  // features per shared-memory chunk
 
-template <int FT, int G>
+// SPLIT: blockIdx.y selects one block of 32*G centers and the result of the
+// block goes to keys[entry] by atomicMin of (distance bits << 32 | center),
+// which recheck_finalize_kernel turns into labels.
+template <int FT, int G, bool SPLIT>
 __global__ void __launch_bounds__(kThreads) assign_fp32_kernel(
     const float *__restrict__ X, const int32_t *__restrict__ frame_idx,
     const int32_t *__restrict__ n_dev, int64_t n_max, int d, const float *__restrict__ C, int k,
-    int32_t *__restrict__ labels, float *__restrict__ dist, unsigned long long *flipped) {
+    int32_t *__restrict__ labels, float *__restrict__ dist, unsigned long long *flipped,
+    unsigned long long *__restrict__ keys) {
     constexpr int BM = kWarps * FT;
     constexpr int BN = 32 * G;
     __shared__ float Xs[BM][kFC];
@@ -53,7 +57,9 @@ __global__ void __launch_bounds__(kThreads) assign_fp32_kernel(
             bd[t] = __int_as_float(0x7f800000);  // +inf
             bj[t] = 0;
         }
-        for (int cb = 0; cb < k; cb += BN) {
+        const int cb_begin = SPLIT ? (int)blockIdx.y * BN : 0;
+        const int cb_end = SPLIT ? min(k, cb_begin + BN) : k;
+        for (int cb = cb_begin; cb < cb_end; cb += BN) {
             float acc[FT][G];
 #pragma unroll
             for (int t = 0; t < FT; ++t)
@@ -106,6 +112,11 @@ __global__ void __launch_bounds__(kThreads) assign_fp32_kernel(
         for (int t = 0; t < FT; ++t) {
             warp_argmin(bd[t], bj[t]);
             const int64_t i = t0 + warp * FT + t;
+            if (SPLIT) {
+                if (lane == 0 && i < n)
+                    atomicMin(&keys[i], ((unsigned long long)__float_as_uint(bd[t]) << 32) | (unsigned)bj[t]);
+                continue;
+            }
             if (lane == 0 && i < n) {
                 const int64_t out = frame_idx ? (int64_t)frame_idx[i] : i;
                 if (flipped && labels[out] != bj[t]) ++nflip;
@@ -125,15 +136,15 @@ int launch_cfg(const float *X, const int32_t *frame_idx, const int32_t *n_dev, i
     static int per_sm = -1;  // cached: no queries while a stream is being captured
     if (per_sm < 0) {
         int v = 0;
-        KM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, assign_fp32_kernel<FT, G>, kThreads, 0));
+        KM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, assign_fp32_kernel<FT, G, false>, kThreads, 0));
         per_sm = v;
     }
     int64_t ntiles = (n + BM - 1) / BM;
     int64_t grid = (int64_t)num_sms() * (per_sm > 0 ? per_sm : 1);
     if (grid > ntiles) grid = ntiles;
     if (grid < 1) grid = 1;
-    assign_fp32_kernel<FT, G><<<(unsigned)grid, kThreads, 0, s>>>(X, frame_idx, n_dev, n, d, C, k,
-                                                                 labels, dist, flipped);
+    assign_fp32_kernel<FT, G, false><<<(unsigned)grid, kThreads, 0, s>>>(X, frame_idx, n_dev, n, d, C, k,
+                                                                        labels, dist, flipped, nullptr);
     KM_CUDA(cudaGetLastError());
     return KM_OK;
 }
@@ -186,9 +197,6 @@ int launch_assign_fp32(const float *X, const int32_t *frame_idx, const int32_t *
                        int d, const float *C, int k, int32_t *labels, float *dist,
                        unsigned long long *flipped, cudaStream_t s) {
     if (n == 0) return KM_OK;
-    // Index lists (frames re-evaluated after the tensor-core pass) are short:
-    // 8-frame tiles spread them over all SMs.
-    if (frame_idx) return launch_cfg<1, 8>(X, frame_idx, n_dev, n, d, C, k, labels, dist, flipped, s);
     if (k <= 32) return launch_cfg<4, 1>(X, frame_idx, n_dev, n, d, C, k, labels, dist, flipped, s);
     if (k <= 64) return launch_cfg<4, 2>(X, frame_idx, n_dev, n, d, C, k, labels, dist, flipped, s);
     if (k <= 128) return launch_cfg<4, 4>(X, frame_idx, n_dev, n, d, C, k, labels, dist, flipped, s);
@@ -210,6 +218,40 @@ int launch_recheck_pairs(const float *X, int d, const float *C, const int32_t *r
     if (g2 > cap) g2 = cap;
     recheck_finalize_kernel<<<(unsigned)(g2 < 1 ? 1 : g2), 256, 0, s>>>(rc_frames, keys, counters, max_entries,
                                                                        labels, flipped);
+    KM_CUDA(cudaGetLastError());
+    return KM_OK;
+}
+
+int launch_full_recheck(const float *X, const int32_t *frames, const int32_t *n_dev, int64_t n_max, int d,
+                        const float *C, int k, unsigned long long *keys, int32_t *labels,
+                        unsigned long long *flipped, cudaStream_t s) {
+    if (n_max == 0) return KM_OK;
+    // The list is short next to n_max: tiles of 32 frames x 256 centers,
+    // one CTA per (frame tile, center block), so that a few thousand frames
+    // still occupy every SM.
+    constexpr int FT = 4, G = 8, BM = kWarps * FT, BN = 32 * G;
+    static int per_sm = -1;
+    if (per_sm < 0) {
+        int v = 0;
+        KM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, assign_fp32_kernel<FT, G, true>, kThreads, 0));
+        per_sm = v > 0 ? v : 1;
+    }
+    const int64_t gy = (k + BN - 1) / BN;
+    int64_t gx = (n_max + BM - 1) / BM;
+    int64_t cap = (int64_t)num_sms() * per_sm * 2;
+    cap = cap / gy > 0 ? cap / gy : 1;
+    if (gx > cap) gx = cap;
+    if (gy > 65535) {
+        set_error("k=%d: too many center blocks for the full re-check", k);
+        return KM_ERR_BAD_SHAPE;
+    }
+    assign_fp32_kernel<FT, G, true><<<dim3((unsigned)gx, (unsigned)gy), kThreads, 0, s>>>(
+        X, frames, n_dev, n_max, d, C, k, nullptr, nullptr, nullptr, keys);
+    KM_CUDA(cudaGetLastError());
+    int64_t g2 = (n_max + 255) / 256;
+    const int64_t cap2 = (int64_t)num_sms() * 8;
+    if (g2 > cap2) g2 = cap2;
+    recheck_finalize_kernel<<<(unsigned)g2, 256, 0, s>>>(frames, keys, n_dev, n_max, labels, flipped);
     KM_CUDA(cudaGetLastError());
     return KM_OK;
 }

@@ -60,8 +60,7 @@ namespace {
 
 constexpr int kBM = 128;          // frames per tile (UMMA M)
 constexpr int kKC = 64;           // fp16 elements per K chunk (128 B, one SW128 row)
-constexpr int kL = TC_CANDIDATES; // candidate slots per frame (shared memory)
-constexpr int kCandBytes = kL * kBM * 8;  // per CTA: kL x 128 (float, int) slots
+constexpr int kL = TC_CANDIDATES; // candidates kept per frame (registers)
 constexpr int kThreadsTC = 192;   // warp 0 TMA, warp 1 MMA, warps 2-5 epilogue
 constexpr int kMaxNkc = 10;       // resident A tile up to kp = 640
 constexpr int kSmemLimit = 232448;
@@ -77,7 +76,9 @@ struct TcParams {
     int d;
     int kp;
     int nkc;
-    int ksteps_last;
+    int ksteps_total;  // 16-wide K steps holding data (ceil((d+2)/16))
+    int bk;            // K columns per B stage: 64 (128-byte swizzle) or 32 (64-byte swizzle)
+    int nbst;          // B stages per center tile (ceil(ksteps_total * 16 / bk))
     int bn;
     int stages;
     int n_ctiles;
@@ -94,6 +95,7 @@ struct TcParams {
     int32_t *pair_center;
     unsigned long long *rc_keys;
     int32_t *full_frames;
+    unsigned long long *full_keys;
     int32_t *counters;
     uint32_t *err;
     float *dump;  // optional n x k distances (diagnostics)
@@ -147,6 +149,17 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
         : "r"(smem_u32(bar)), "r"(parity)
         : "memory");
     return ok != 0;
+}
+
+// One lane of the converged warp (the same lane every time).
+__device__ __forceinline__ bool elect_one() {
+    uint32_t pred = 0;
+    asm volatile(
+        "{\n\t.reg .pred P;\n\t"
+        "elect.sync _|P, 0xffffffff;\n\t"
+        "selp.u32 %0, 1, 0, P;\n\t}"
+        : "=r"(pred));
+    return pred != 0;
 }
 
 // Waits for the phase of the given parity; false after kWaitLimitNs.
@@ -234,6 +247,8 @@ __device__ __forceinline__ void tmem_wait_ld() {
 
 // Shared-memory matrix descriptor: K-major operand in the 128-byte swizzle
 // layout written by TMA (8-row atoms of 128 B, atoms 1024 B apart).
+__device__ __forceinline__ uint64_t sw64_desc(uint32_t saddr);
+
 __device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
     uint64_t desc = 0;
     desc |= (uint64_t)((saddr & 0x3FFFFu) >> 4);  // start address
@@ -241,6 +256,17 @@ __device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
     desc |= (uint64_t)(1024 >> 4) << 32;          // stride byte offset: 8 rows x 128 B
     desc |= (uint64_t)1 << 46;                    // descriptor version
     desc |= (uint64_t)2 << 61;                    // 128-byte swizzle
+    return desc;
+}
+
+// Same for the 64-byte swizzle (8-row atoms of 64 B, atoms 512 B apart).
+__device__ __forceinline__ uint64_t sw64_desc(uint32_t saddr) {
+    uint64_t desc = 0;
+    desc |= (uint64_t)((saddr & 0x3FFFFu) >> 4);  // start address
+    desc |= (uint64_t)1 << 16;                    // leading byte offset (unused for swizzled K-major)
+    desc |= (uint64_t)(512 >> 4) << 32;           // stride byte offset: 8 rows x 64 B
+    desc |= (uint64_t)1 << 46;                    // descriptor version
+    desc |= (uint64_t)4 << 61;                    // 64-byte swizzle
     return desc;
 }
 
@@ -428,22 +454,6 @@ __device__ __forceinline__ float hi_bound(float v, float E, float R, float g_hi)
     return __fadd_ru(__fmul_ru(__fmul_ru(a, a), g_hi), 1e-37f);
 }
 
-// Drops the slots of one frame whose value fell below the threshold (the
-// threshold only rises); returns the new count.  Kept out of line: it runs
-// rarely and the callers are unrolled.
-__device__ __noinline__ int compact_slots(float *a, int *j, int cnt, float thr) {
-    int w = 0;
-    for (int s = 0; s < cnt; ++s) {
-        const float v = a[s * kBM];
-        if (v >= thr) {
-            a[w * kBM] = v;
-            j[w * kBM] = j[s * kBM];
-            ++w;
-        }
-    }
-    return w;
-}
-
 // Rounding of the float32 centering x' = fl(x - m): at most 2^-24 |x - m|
 // per component, so 2^-23 (sx + sc) covers both operands.
 constexpr float kCenterEps = 1.1920929e-07f;  // 2^-23
@@ -469,10 +479,9 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
     uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     uint8_t *sA = smem;
     uint8_t *sB = sA + p.nkc * kABytesPerChunk;
-    const int b_stage_bytes = p.bn * 128;
-    float *cand_a = reinterpret_cast<float *>(sB + p.stages * b_stage_bytes);  // [kL][128]
-    int *cand_j = reinterpret_cast<int *>(cand_a + kL * kBM);                   // [kL][128]
-    uint64_t *bars = reinterpret_cast<uint64_t *>(reinterpret_cast<uint8_t *>(cand_a) + kCandBytes);
+    const int b_stage_bytes = p.bn * p.bk * 2;
+    const int spc = kKC / p.bk;  // B stages per A chunk (1 or 2)
+    uint64_t *bars = reinterpret_cast<uint64_t *>(sB + p.stages * b_stage_bytes);
     uint64_t *a_full = bars;
     uint64_t *a_empty = a_full + p.nkc;
     uint64_t *b_full = a_empty + p.nkc;
@@ -514,43 +523,54 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
 
     const int64_t n_ftiles = (p.n + kBM - 1) / kBM;
 
-    if (warp == 0 && lane == 0) {
+    if (warp == 0) {
         // ---------------- TMA producer ----------------
+        // The whole warp runs the loop (waits by all lanes, agreed by vote);
+        // one elected lane issues the copies.  Per center tile: B stages
+        // t = 0..nbst-1 (bk K-columns each); the A chunk kc = t/spc (64
+        // K-columns) is loaded with its first stage on the first center tile.
         uint32_t bq = 0;
         uint32_t t_local = 0;
         bool ok = true;
         unsigned long long w_b = 0, w_a = 0;
-        unsigned long long *pw_b = p.wait_cycles ? &w_b : nullptr;
-        unsigned long long *pw_a = p.wait_cycles ? &w_a : nullptr;
+        unsigned long long *pw_b = (p.wait_cycles && lane == 0) ? &w_b : nullptr;
+        unsigned long long *pw_a = (p.wait_cycles && lane == 0) ? &w_a : nullptr;
         for (int64_t ft = blockIdx.x; ft < n_ftiles && ok; ft += gridDim.x, ++t_local) {
             for (int ct = 0; ct < p.n_ctiles && ok; ++ct) {
-                for (int kc = 0; kc < p.nkc; ++kc) {
-                    if (ct == 0) {
-                        if (!mbar_wait_timed(&a_empty[kc], (t_local & 1u) ^ 1u, pw_a)) {
+                for (int t = 0; t < p.nbst; ++t) {
+                    const int kc = t / spc;
+                    if (ct == 0 && t % spc == 0) {
+                        if (!__all_sync(0xffffffffu, mbar_wait_timed(&a_empty[kc], (t_local & 1u) ^ 1u, pw_a))) {
                             ok = false;
                             break;
                         }
-                        mbar_arrive_expect_tx(&a_full[kc], kABytesPerChunk);
-                        tma_load_2d(sA + kc * kABytesPerChunk, &tmA, kc * kKC, (int)(ft * kBM), &a_full[kc]);
+                        if (elect_one()) {
+                            mbar_arrive_expect_tx(&a_full[kc], kABytesPerChunk);
+                            tma_load_2d(sA + kc * kABytesPerChunk, &tmA, kc * kKC, (int)(ft * kBM), &a_full[kc]);
+                        }
+                        __syncwarp();
                     }
                     const uint32_t s = bq % p.stages;
                     const uint32_t ph = (bq / p.stages) & 1u;
-                    if (!mbar_wait_timed(&b_empty[s], ph ^ 1u, pw_b)) {
+                    if (!__all_sync(0xffffffffu, mbar_wait_timed(&b_empty[s], ph ^ 1u, pw_b))) {
                         ok = false;
                         break;
                     }
-                    mbar_arrive_expect_tx(&b_full[s], b_stage_bytes);
-                    tma_load_2d(sB + s * b_stage_bytes, &tmB, kc * kKC, ct * p.bn, &b_full[s]);
+                    if (elect_one()) {
+                        mbar_arrive_expect_tx(&b_full[s], b_stage_bytes);
+                        tma_load_2d(sB + s * b_stage_bytes, &tmB, t * p.bk, ct * p.bn, &b_full[s]);
+                    }
+                    __syncwarp();
                     ++bq;
                 }
-                if (*abort_flag) ok = false;
+                if (__any_sync(0xffffffffu, *abort_flag != 0)) ok = false;
             }
         }
-        if (!ok) {
+        if (!ok && lane == 0) {
             atomicOr(p.err, (uint32_t)kDevTimeoutTma);
             *abort_flag = 1;
         }
-        if (p.wait_cycles) {
+        if (pw_b) {
             atomicAdd(&p.wait_cycles[kWaitProdB], w_b);
             atomicAdd(&p.wait_cycles[kWaitProdA], w_a);
         }
@@ -563,67 +583,81 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                 mbar_wait(&b_full[s], (last_q / p.stages) & 1u);
             }
         }
-    } else if (warp == 1 && lane == 0) {
+        __syncwarp();
+    } else if (warp == 1) {
         // ---------------- MMA issuer ----------------
+        // Converged warp; one elected lane issues the MMAs and commits.
         const uint32_t idesc = make_idesc(kBM, p.bn);
+        const uint64_t adesc0 = sw128_desc(smem_u32(sA));
+        const uint32_t sb0 = smem_u32(sB);
+        const int spt = p.bk >> 4;  // K steps per full stage
         uint32_t bq = 0, accq = 0, t_local = 0;
         bool ok = true;
         unsigned long long w_b = 0, w_a = 0, w_acc = 0;
         const long long t_start = clock64();
-        unsigned long long *pw_b = p.wait_cycles ? &w_b : nullptr;
-        unsigned long long *pw_a = p.wait_cycles ? &w_a : nullptr;
-        unsigned long long *pw_acc = p.wait_cycles ? &w_acc : nullptr;
+        unsigned long long *pw_b = (p.wait_cycles && lane == 0) ? &w_b : nullptr;
+        unsigned long long *pw_a = (p.wait_cycles && lane == 0) ? &w_a : nullptr;
+        unsigned long long *pw_acc = (p.wait_cycles && lane == 0) ? &w_acc : nullptr;
         for (int64_t ft = blockIdx.x; ft < n_ftiles && ok; ft += gridDim.x, ++t_local) {
             for (int ct = 0; ct < p.n_ctiles && ok; ++ct) {
                 const uint32_t buf = accq & 1u;
-                if (!mbar_wait_timed(&acc_empty[buf], ((accq >> 1) & 1u) ^ 1u, pw_acc)) {
+                if (!__all_sync(0xffffffffu, mbar_wait_timed(&acc_empty[buf], ((accq >> 1) & 1u) ^ 1u, pw_acc))) {
                     ok = false;
                     break;
                 }
                 tc_fence_after();
                 const uint32_t d_tmem = tmem_base + buf * (uint32_t)p.bn;
-                for (int kc = 0; kc < p.nkc; ++kc) {
-                    if (ct == 0 && !mbar_wait_timed(&a_full[kc], t_local & 1u, pw_a)) {
+                for (int t = 0; t < p.nbst; ++t) {
+                    const int kc = t / spc;
+                    const int half = t % spc;
+                    if (ct == 0 && half == 0 &&
+                        !__all_sync(0xffffffffu, mbar_wait_timed(&a_full[kc], t_local & 1u, pw_a))) {
                         ok = false;
                         break;
                     }
                     const uint32_t s = bq % p.stages;
-                    if (!mbar_wait_timed(&b_full[s], (bq / p.stages) & 1u, pw_b)) {
+                    if (!__all_sync(0xffffffffu, mbar_wait_timed(&b_full[s], (bq / p.stages) & 1u, pw_b))) {
                         ok = false;
                         break;
                     }
                     // TMA completion on the mbarrier orders the loaded tiles before
                     // the MMAs; no tcgen05 fence is needed here.
-                    const int nks = (kc == p.nkc - 1) ? p.ksteps_last : (kKC / 16);
-                    const uint32_t a0 = smem_u32(sA + kc * kABytesPerChunk);
-                    const uint32_t b0 = smem_u32(sB + s * b_stage_bytes);
-                    for (int kk = 0; kk < nks; ++kk) {
-                        mma_f16(d_tmem, sw128_desc(a0 + kk * 32), sw128_desc(b0 + kk * 32), idesc,
-                                (kc | kk) != 0);
+                    const int steps = min(spt, p.ksteps_total - spt * t);
+                    const uint64_t ad = adesc0 + (uint64_t)((kc * kABytesPerChunk + half * p.bk * 2) >> 4);
+                    const uint32_t b0 = sb0 + s * b_stage_bytes;
+                    const uint64_t bd = p.bk == kKC ? sw128_desc(b0) : sw64_desc(b0);
+                    if (elect_one()) {
+#pragma unroll
+                        for (int kk = 0; kk < 4; ++kk)  // 32-byte K steps: +2 in the start-address field
+                            if (kk < steps) mma_f16(d_tmem, ad + 2 * kk, bd + 2 * kk, idesc, (t | kk) != 0);
+                        mma_commit(&b_empty[s]);
+                        if (ct == p.n_ctiles - 1 && (half == spc - 1 || t == p.nbst - 1)) mma_commit(&a_empty[kc]);
                     }
-                    mma_commit(&b_empty[s]);
-                    if (ct == p.n_ctiles - 1) mma_commit(&a_empty[kc]);
+                    __syncwarp();
                     ++bq;
                 }
                 if (!ok) break;
-                mma_commit(&acc_full[buf]);
+                if (elect_one()) mma_commit(&acc_full[buf]);
+                __syncwarp();
                 ++accq;
-                if (*abort_flag) ok = false;
+                if (__any_sync(0xffffffffu, *abort_flag != 0)) ok = false;
             }
         }
-        if (!ok) {
+        if (!ok && lane == 0) {
             atomicOr(p.err, (uint32_t)kDevTimeoutMma);
             *abort_flag = 1;
         }
-        if (p.wait_cycles) {
+        if (pw_b) {
             atomicAdd(&p.wait_cycles[kWaitMmaB], w_b);
             atomicAdd(&p.wait_cycles[kWaitMmaA], w_a);
             atomicAdd(&p.wait_cycles[kWaitMmaAcc], w_acc);
             atomicAdd(&p.wait_cycles[kMmaTotal], (unsigned long long)(clock64() - t_start));
         }
         // Drain: all issued MMAs complete before TMEM is released.
-        mma_commit(drain);
+        if (elect_one()) mma_commit(drain);
+        __syncwarp();
         mbar_wait(drain, 0);
+        __syncwarp();
     } else if (warp >= 2) {
         // ---------------- epilogue ----------------
         const int quarter = warp & 3;
@@ -635,8 +669,6 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
         const float hc_max = __uint_as_float(p.scal[kHcMax]);
         const float kNegInf = __int_as_float(0xff800000);
         const float kInf = __int_as_float(0x7f800000);
-        float *my_a = cand_a + row;  // slot s at my_a[s * kBM]
-        int *my_j = cand_j + row;
         uint32_t accq = 0;
         bool ok = true;
         unsigned long long w_acc = 0;
@@ -651,55 +683,15 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
             const float Rmax = __fadd_ru(__fadd_ru(xn.z, hc_max), __fmul_ru(kCenterEps, smax));
             const float Emax = __fmul_ru(p.e_coef, __fmul_ru(smax, smax));
             float best = kNegInf, thr = kNegInf;
-            int best_id = 0, cnt = 0;
+            int best_id = 0;
             bool ovf = false;
-
-            // One 32-column chunk: skipped unless some lane of the warp has a
-            // value at or above its threshold; then appends those values to the
-            // lane's slots (predicated stores).
-            auto chunk = [&](const uint32_t (&r)[32], int j0) {
-                float v[32];
+            float la[kL];
+            int lid[kL];
 #pragma unroll
-                for (int c = 0; c < 32; ++c) v[c] = __uint_as_float(r[c]);
-                if (j0 + 32 > p.k) {
-#pragma unroll
-                    for (int c = 0; c < 32; ++c)
-                        if (j0 + c >= p.k) v[c] = kNegInf;
-                }
-                if (p.dump && i < p.n) {
-#pragma unroll
-                    for (int c = 0; c < 32; ++c)
-                        if (j0 + c < p.k) p.dump[i * p.k + j0 + c] = fmaf(-2.0f, v[c], xn.x) * inv_s2;
-                }
-                float mx = v[0];
-#pragma unroll
-                for (int c = 1; c < 32; ++c) mx = fmaxf(mx, v[c]);
-                const bool hit = mx >= thr && mx > kNegInf;
-                if (!__any_sync(0xffffffffu, hit)) return;
-                if (hit && mx > best) {
-                    int bc = 31;
-#pragma unroll
-                    for (int c = 31; c >= 0; --c)
-                        if (v[c] == mx) bc = c;
-                    best = mx;
-                    best_id = j0 + bc;
-                    thr = window_threshold(best, xn.x, inv_s2, s2, Emax, Rmax, p.g_lo, p.g_hi);
-                }
-#pragma unroll
-                for (int c = 0; c < 32; ++c) {
-                    if (v[c] >= thr) {
-                        if (cnt == kL) cnt = compact_slots(my_a, my_j, cnt, thr);
-                        if (cnt < kL) {
-                            my_a[cnt * kBM] = v[c];
-                            my_j[cnt * kBM] = j0 + c;
-                            ++cnt;
-                        } else {
-                            ovf = true;
-                        }
-                    }
-                }
-            };
-
+            for (int m = 0; m < kL; ++m) {
+                la[m] = kNegInf;
+                lid[m] = -1;
+            }
             for (int ct = 0; ct < p.n_ctiles; ++ct) {
                 const uint32_t buf = accq & 1u;
                 const bool got = __all_sync(0xffffffffu, mbar_wait_timed(&acc_full[buf], (accq >> 1) & 1u, pw_acc));
@@ -709,15 +701,51 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                 }
                 tc_fence_after();
                 const uint32_t tbase = tmem_base + lane_off + buf * (uint32_t)p.bn;
-                for (int cc = 0; cc < p.bn; cc += 64) {
-                    // Two TMEM loads in flight before one wait.
-                    uint32_t r0[32], r1[32];
-                    const bool two = cc + 32 < p.bn;
-                    tmem_ld32(tbase + cc, r0);
-                    if (two) tmem_ld32(tbase + cc + 32, r1);
+                for (int cc = 0; cc < p.bn; cc += 32) {
+                    uint32_t r[32];
+                    tmem_ld32(tbase + cc, r);
                     tmem_wait_ld();
-                    chunk(r0, ct * p.bn + cc);
-                    if (two) chunk(r1, ct * p.bn + cc + 32);
+                    const int j0 = ct * p.bn + cc;
+                    float v[32];
+#pragma unroll
+                    for (int c = 0; c < 32; ++c) v[c] = __uint_as_float(r[c]);
+                    if (j0 + 32 > p.k) {
+#pragma unroll
+                        for (int c = 0; c < 32; ++c)
+                            if (j0 + c >= p.k) v[c] = kNegInf;
+                    }
+                    if (p.dump && i < p.n) {
+#pragma unroll
+                        for (int c = 0; c < 32; ++c)
+                            if (j0 + c < p.k) p.dump[i * p.k + j0 + c] = fmaf(-2.0f, v[c], xn.x) * inv_s2;
+                    }
+                    float mx = v[0];
+#pragma unroll
+                    for (int c = 1; c < 32; ++c) mx = fmaxf(mx, v[c]);
+                    if (mx >= thr && mx > kNegInf) {
+                        if (mx > best) {
+                            int bc = 31;
+#pragma unroll
+                            for (int c = 31; c >= 0; --c)
+                                if (v[c] == mx) bc = c;
+                            best = mx;
+                            best_id = j0 + bc;
+                            thr = window_threshold(best, xn.x, inv_s2, s2, Emax, Rmax, p.g_lo, p.g_hi);
+                        }
+#pragma unroll
+                        for (int c = 0; c < 32; ++c) {
+                            if (v[c] >= thr) {
+                                if (lid[kL - 1] >= 0 && la[kL - 1] >= thr) ovf = true;
+#pragma unroll
+                                for (int m = kL - 1; m > 0; --m) {
+                                    la[m] = la[m - 1];
+                                    lid[m] = lid[m - 1];
+                                }
+                                la[0] = v[c];
+                                lid[0] = j0 + c;
+                            }
+                        }
+                    }
                 }
                 tc_fence_before();
                 __syncwarp();
@@ -728,49 +756,49 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
 
             // ---- decision ----
             bool need_rc = false, need_full = false;
-            int ncand = 0, first = -1;
-            float H = kInf;
+            unsigned cmask = 0;  // bit m: list entry m is a candidate
             if (i < p.n) {
-                // Entries still above the final threshold; H = min of their upper ends.
-                for (int s = 0; s < cnt; ++s) {
-                    const float a = my_a[s * kBM];
-                    if (a >= thr) {
-                        const float2 cn = p.cnorm[my_j[s * kBM]];
+                float vv[kL], RR[kL], EE[kL];
+                float H = kInf;
+#pragma unroll
+                for (int m = 0; m < kL; ++m) {
+                    vv[m] = kInf;
+                    RR[m] = 0.0f;
+                    EE[m] = 0.0f;
+                    if (lid[m] >= 0 && la[m] >= thr) {
+                        const float2 cn = p.cnorm[lid[m]];
                         const float sj = xn.y + cn.x;
-                        const float R = __fadd_ru(__fadd_ru(xn.z, cn.y), __fmul_ru(kCenterEps, sj));
-                        const float E = __fmul_ru(p.e_coef, __fmul_ru(sj, sj));
-                        H = fminf(H, hi_bound(fmaf(-2.0f, a, xn.x) * inv_s2, E, R, p.g_hi));
+                        RR[m] = __fadd_ru(__fadd_ru(xn.z, cn.y), __fmul_ru(kCenterEps, sj));
+                        EE[m] = __fmul_ru(p.e_coef, __fmul_ru(sj, sj));
+                        vv[m] = fmaf(-2.0f, la[m], xn.x) * inv_s2;
+                        H = fminf(H, hi_bound(vv[m], EE[m], RR[m], p.g_hi));
                     }
                 }
                 const bool finite = best > kNegInf && H < kInf && Rmax < kInf && Emax < kInf;
                 if (!finite || ovf) {
                     need_full = true;
                 } else {
-                    for (int s = 0; s < cnt; ++s) {
-                        const float a = my_a[s * kBM];
-                        if (a >= thr) {
-                            const int j = my_j[s * kBM];
-                            const float2 cn = p.cnorm[j];
-                            const float sj = xn.y + cn.x;
-                            const float R = __fadd_ru(__fadd_ru(xn.z, cn.y), __fmul_ru(kCenterEps, sj));
-                            const float E = __fmul_ru(p.e_coef, __fmul_ru(sj, sj));
-                            if (lo_bound(fmaf(-2.0f, a, xn.x) * inv_s2, E, R, p.g_lo) <= H) {
-                                if (first < 0) first = j;
-                                ++ncand;
-                            }
-                        }
-                    }
-                    if (ncand == 0) need_full = true;
-                    else if (ncand > 1) need_rc = true;
+#pragma unroll
+                    for (int m = 0; m < kL; ++m)
+                        if (vv[m] < kInf && lo_bound(vv[m], EE[m], RR[m], p.g_lo) <= H) cmask |= 1u << m;
+                    const int nc = __popc(cmask);
+                    if (nc == 0) need_full = true;
+                    else if (nc > 1) need_rc = true;
                 }
-                p.labels[i] = (!need_full && ncand == 1) ? first : best_id;
+                int lab = best_id;
+                if (!need_full && !need_rc) {
+#pragma unroll
+                    for (int m = 0; m < kL; ++m)
+                        if (cmask == (1u << m)) lab = lid[m];
+                }
+                p.labels[i] = lab;
             }
             const unsigned m_rc = __ballot_sync(0xffffffffu, need_rc);
             if (m_rc) {
                 // One entry per re-checked frame and one pair per candidate,
                 // both appended with a single atomic per warp.
                 const int leader = __ffs(m_rc) - 1;
-                const int npairs = need_rc ? ncand : 0;
+                const int npairs = need_rc ? __popc(cmask) : 0;
                 int excl = npairs;
 #pragma unroll
                 for (int off = 1; off < 32; off <<= 1) {
@@ -790,20 +818,12 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                     const int e = base + __popc(m_rc & ((1u << lane) - 1u));
                     p.rc_frames[e] = (int32_t)i;
                     p.rc_keys[e] = ~0ull;
-                    int q = pbase + excl;
-                    for (int s = 0; s < cnt; ++s) {
-                        const float a = my_a[s * kBM];
-                        if (a >= thr) {
-                            const int j = my_j[s * kBM];
-                            const float2 cn = p.cnorm[j];
-                            const float sj = xn.y + cn.x;
-                            const float R = __fadd_ru(__fadd_ru(xn.z, cn.y), __fmul_ru(kCenterEps, sj));
-                            const float E = __fmul_ru(p.e_coef, __fmul_ru(sj, sj));
-                            if (lo_bound(fmaf(-2.0f, a, xn.x) * inv_s2, E, R, p.g_lo) <= H) {
-                                p.pair_entry[q] = e;
-                                p.pair_center[q] = j;
-                                ++q;
-                            }
+#pragma unroll
+                    for (int m = 0; m < kL; ++m) {
+                        if ((cmask >> m) & 1u) {
+                            const int q = pbase + excl + __popc(cmask & ((1u << m) - 1u));
+                            p.pair_entry[q] = e;
+                            p.pair_center[q] = lid[m];
                         }
                     }
                 }
@@ -814,7 +834,11 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                 int base = 0;
                 if (lane == leader) base = atomicAdd(&p.counters[1], __popc(m_full));
                 base = __shfl_sync(0xffffffffu, base, leader);
-                if (need_full) p.full_frames[base + __popc(m_full & ((1u << lane) - 1u))] = (int32_t)i;
+                if (need_full) {
+                    const int e = base + __popc(m_full & ((1u << lane) - 1u));
+                    p.full_frames[e] = (int32_t)i;
+                    p.full_keys[e] = ~0ull;
+                }
             }
             if (__any_sync(0xffffffffu, *abort_flag != 0)) ok = false;
         }
@@ -858,7 +882,8 @@ EncodeTiledFn get_encode() {
     return fn;
 }
 
-int make_map(CUtensorMap *tm, const void *base, int64_t rows, int kp, int box_rows) {
+int make_map(CUtensorMap *tm, const void *base, int64_t rows, int kp, int box_rows, int box_k,
+             CUtensorMapSwizzle swizzle) {
     EncodeTiledFn enc = get_encode();
     if (!enc) {
         set_error("cuTensorMapEncodeTiled is not available from the driver");
@@ -866,10 +891,10 @@ int make_map(CUtensorMap *tm, const void *base, int64_t rows, int kp, int box_ro
     }
     cuuint64_t dims[2] = {(cuuint64_t)kp, (cuuint64_t)rows};
     cuuint64_t strides[1] = {(cuuint64_t)kp * 2};
-    cuuint32_t box[2] = {(cuuint32_t)kKC, (cuuint32_t)box_rows};
+    cuuint32_t box[2] = {(cuuint32_t)box_k, (cuuint32_t)box_rows};
     cuuint32_t estr[2] = {1, 1};
     CUresult r = enc(tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, const_cast<void *>(base), dims, strides, box, estr,
-                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, swizzle,
                      CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) {
         set_error("cuTensorMapEncodeTiled failed (%d) for %lld x %d rows/box %d", (int)r, (long long)rows, kp,
@@ -889,8 +914,15 @@ int pick_bn(int k) {
 
 int k_pad_of(int k) { return (k + 255) / 256 * 256; }
 
+// K columns per B stage: 64 (one 128-byte swizzle row) by default.
+int pick_bk(int d, int k) {
+    (void)d;
+    (void)k;
+    return 64;
+}
+
 struct Plan {
-    int bn, stages, nkc, smem;
+    int bn, bk, stages, nkc, smem;
     uint32_t tmem_cols;
 };
 
@@ -898,16 +930,17 @@ bool make_plan(int d, int k, Plan &pl) {
     pl.nkc = kp_of(d) / kKC;
     if (pl.nkc > kMaxNkc) return false;
     pl.bn = pick_bn(k);
-    const int fixed = 1024 + 512 + kCandBytes + pl.nkc * kABytesPerChunk;
-    int stages = (kSmemLimit - fixed) / (pl.bn * 128);
-    if (stages < 2 && pl.bn > 128) {
-        pl.bn = 128;
-        stages = (kSmemLimit - fixed) / (pl.bn * 128);
+    pl.bk = pick_bk(d, k);
+    const int fixed = 1024 + 512 + pl.nkc * kABytesPerChunk;
+    int stages = (kSmemLimit - fixed) / (pl.bn * pl.bk * 2);
+    if (stages > 8) stages = 8;
+    if (stages < 2 && pl.bk == kKC) {
+        pl.bk = kKC / 2;  // narrower stages when two wide ones do not fit
+        stages = (kSmemLimit - fixed) / (pl.bn * pl.bk * 2);
     }
-    if (stages > 6) stages = 6;
     if (stages < 2) return false;
     pl.stages = stages;
-    pl.smem = fixed + stages * pl.bn * 128;
+    pl.smem = fixed + stages * pl.bn * pl.bk * 2;
     if (pl.smem < 120 * 1024) pl.smem = 120 * 1024;  // one CTA per SM: TMEM is sized for one
     uint32_t cols = 32;
     while (cols < (uint32_t)(2 * pl.bn)) cols <<= 1;
@@ -982,25 +1015,9 @@ void tc_carve_centers(void *ws, int d, int k, TcBuffers &b) {
     b.scal = c.take<uint32_t>(kNumScalars);
 }
 
-size_t tc_assign_ws_size(int64_t n, int d, int k) {
-    (void)d;
-    (void)k;
-    Carver c(nullptr);
-    const size_t nn = n > 0 ? n : 1;
-    c.take<int32_t>(nn);
-    c.take<int32_t>(nn * kL);
-    c.take<int32_t>(nn * kL);
-    c.take<unsigned long long>(nn);
-    c.take<int32_t>(nn);
-    c.take<int32_t>(20);
-    c.take<unsigned long long>(1);
-    c.take<uint32_t>(1);
-    return c.bytes();
-}
-
-void tc_carve_assign(void *ws, int64_t n, int d, int k, TcBuffers &b) {
-    (void)d;
-    (void)k;
+namespace {
+// One carving sequence for sizing (ws == nullptr) and for carving.
+size_t carve_assign(void *ws, int64_t n, TcBuffers &b) {
     Carver c(ws);
     const size_t nn = n > 0 ? n : 1;
     b.rc_frames = c.take<int32_t>(nn);
@@ -1008,9 +1025,25 @@ void tc_carve_assign(void *ws, int64_t n, int d, int k, TcBuffers &b) {
     b.pair_center = c.take<int32_t>(nn * kL);
     b.rc_keys = c.take<unsigned long long>(nn);
     b.full_frames = c.take<int32_t>(nn);
-    b.counters = c.take<int32_t>(20);  // [0] recheck entries, [1] full entries, [4..20) diagnostics
+    b.full_keys = c.take<unsigned long long>(nn);
+    b.counters = c.take<int32_t>(20);  // [0] recheck entries, [1] full entries, [2] pairs, [4..20) diagnostics
     b.flipped = c.take<unsigned long long>(1);
     b.err = c.take<uint32_t>(1);
+    return c.bytes();
+}
+}  // namespace
+
+size_t tc_assign_ws_size(int64_t n, int d, int k) {
+    (void)d;
+    (void)k;
+    TcBuffers b;
+    return carve_assign(nullptr, n, b);
+}
+
+void tc_carve_assign(void *ws, int64_t n, int d, int k, TcBuffers &b) {
+    (void)d;
+    (void)k;
+    carve_assign(ws, n, b);
 }
 
 int tc_prepare_shift_from_centers(const float *C, int d, int k, TcBuffers &b, cudaStream_t s) {
@@ -1060,8 +1093,9 @@ int tc_assign(const float *X, int64_t n, int d, const float *C, int k, int32_t *
     KM_CUDA(attr_err);
 
     CUtensorMap tmA, tmB;
-    KM_TRY(make_map(&tmA, b.xh, n, b.kp, kBM));
-    KM_TRY(make_map(&tmB, b.ch, k_pad_of(k), b.kp, pl.bn));
+    KM_TRY(make_map(&tmA, b.xh, n, b.kp, kBM, kKC, CU_TENSOR_MAP_SWIZZLE_128B));
+    KM_TRY(make_map(&tmB, b.ch, k_pad_of(k), b.kp, pl.bn, pl.bk,
+                    pl.bk == kKC ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B));
 
     KM_CUDA(cudaMemsetAsync(b.counters, 0, 4 * sizeof(int32_t), s));
     KM_CUDA(cudaMemsetAsync(b.flipped, 0, sizeof(unsigned long long), s));
@@ -1074,8 +1108,9 @@ int tc_assign(const float *X, int64_t n, int d, const float *C, int k, int32_t *
     p.d = d;
     p.kp = b.kp;
     p.nkc = pl.nkc;
-    const int rem = d + 2 - (pl.nkc - 1) * kKC;
-    p.ksteps_last = (rem + 15) / 16;
+    p.ksteps_total = (d + 2 + 15) / 16;
+    p.bk = pl.bk;
+    p.nbst = (p.ksteps_total * 16 + pl.bk - 1) / pl.bk;
     p.bn = pl.bn;
     p.stages = pl.stages;
     p.n_ctiles = (k + pl.bn - 1) / pl.bn;
@@ -1094,6 +1129,7 @@ int tc_assign(const float *X, int64_t n, int d, const float *C, int k, int32_t *
     p.pair_center = b.pair_center;
     p.rc_keys = b.rc_keys;
     p.full_frames = b.full_frames;
+    p.full_keys = b.full_keys;
     p.counters = b.counters;
     p.err = b.err;
     p.dump = dump;
@@ -1112,7 +1148,7 @@ int tc_assign(const float *X, int64_t n, int d, const float *C, int k, int32_t *
                                 n * kL, labels, b.flipped, s));
     if (prof) prof->end(kProfRecheck, s);
     if (prof) prof->begin(kProfFull, s);
-    KM_TRY(launch_assign_fp32(X, b.full_frames, b.counters + 1, n, d, C, k, labels, nullptr, b.flipped, s));
+    KM_TRY(launch_full_recheck(X, b.full_frames, b.counters + 1, n, d, C, k, b.full_keys, labels, b.flipped, s));
     if (prof) prof->end(kProfFull, s);
     return KM_OK;
 }

@@ -39,6 +39,12 @@ int launch_assign_fp32(const float *X, const int32_t *frame_idx, const int32_t *
 // not separate: pair q = (entry pair_entry[q], center pair_center[q]); entry e
 // stands for frame rc_frames[e] and keys[e] (initialised to ~0) collects the
 // winner.  counters[0] = entries, counters[2] = pairs (device).
+// Exact re-evaluation of the frames frames[0..*n_dev) against all centers,
+// split over (frame tile, center block) CTAs; keys[e] must hold ~0 on entry.
+int launch_full_recheck(const float *X, const int32_t *frames, const int32_t *n_dev, int64_t n_max, int d,
+                        const float *C, int k, unsigned long long *keys, int32_t *labels,
+                        unsigned long long *flipped, cudaStream_t s);
+
 int launch_recheck_pairs(const float *X, int d, const float *C, const int32_t *rc_frames,
                          const int32_t *pair_entry, const int32_t *pair_center, unsigned long long *keys,
                          const int32_t *counters, int64_t max_entries, int64_t max_pairs, int32_t *labels,
@@ -65,7 +71,7 @@ size_t tc_frames_ws_size(int64_t n, int d);     // fp16 frame copy + norms
 size_t tc_centers_ws_size(int d, int k);        // fp16 centers + norms + shift + scalars
 size_t tc_assign_ws_size(int64_t n, int d, int k);  // candidate lists + counters
 
-#define TC_CANDIDATES 16  // candidate slots per frame (shared memory) of the tensor-core pass
+#define TC_CANDIDATES 8  // candidate centers kept per frame by the tensor-core pass
 
 struct TcBuffers {
     // frames
@@ -82,6 +88,7 @@ struct TcBuffers {
     int32_t *pair_center = nullptr;         // pair -> candidate center
     unsigned long long *rc_keys = nullptr;  // entry -> (distance bits, center) minimum
     int32_t *full_frames = nullptr;
+    unsigned long long *full_keys = nullptr;
     int32_t *counters = nullptr;  // [0] recheck entries, [1] full entries, [2] pairs
     unsigned long long *flipped = nullptr;
     uint32_t *err = nullptr;

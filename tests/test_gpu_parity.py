@@ -80,6 +80,23 @@ def test_duplicate_centers_ties(torch, L, oracle, prec):
     assert got[:100].tolist() == list(range(100))  # exact hits go to the lowest duplicate
 
 
+def test_full_recheck_across_center_blocks(torch, L, oracle):
+    # Groups of 12 nearly equal centers overflow the candidate list of the
+    # tensor-core pass; the exact copies of each group sit 256+ indexes apart,
+    # so the exact re-check must pick the lowest index across center blocks.
+    rng = np.random.default_rng(21)
+    d, groups = 96, 90
+    base = rng.normal(size=(groups, d)).astype(np.float32)
+    near = [base + 1e-4 * rng.normal(size=base.shape).astype(np.float32) for _ in range(11)]
+    C = np.concatenate([base] + near + [base]).astype(np.float32)  # k = 13 * 90 = 1170
+    X = np.concatenate([base + 1e-3 * rng.normal(size=base.shape).astype(np.float32) for _ in range(30)])
+    X = np.concatenate([X, base]).astype(np.float32)
+    got, stats = gpu_assign(torch, L, X, C, "fp16")
+    assert stats["n_full"] > 0
+    np.testing.assert_array_equal(got, oracle.assign(X, C))
+    assert got[-groups:].tolist() == list(range(groups))
+
+
 @pytest.mark.parametrize("prec", PRECS)
 def test_offset_data_bound(torch, L, oracle, prec):
     # Large common offset with small spread: the stress case of the tensor-core bound.
