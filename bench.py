@@ -21,6 +21,13 @@ near ties (labels equal the plain FP32 kernel's bit for bit).  A "step" is one L
 --impl reference times the CPU restatement of the reference's
 implementation on the host cores (bounded sample) with the same metric.
 
+--config selects the other measured workloads (each prints its own line):
+  c1  100,000 x 2 mixture, k=50: kmeans++ + Lloyd to convergence + dtrajs
+  c2  20 uneven AR(1) trajectories (~3.9M frames), d=10, k=1000, packed
+  c4  precision sweep, 1M frames, d in {16,64,256,1024}, k in {100,1000,5000}
+  c5  serving: Poisson arrivals (200 req/s) of trajectories of 1k-1M frames
+      against 8 resident center sets, 40 GB admission budget, p50/p99
+
 Multi-GPU (torchrun): each rank discretizes its own 2,000,000 frames (weak
 scaling, no collective on the data path); value = all frames / max rank time.
 """
@@ -56,6 +63,8 @@ def parse_args():
     p.add_argument("--no-fp32", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--config", default="c3", choices=["c1", "c2", "c3", "c4", "c5"])
+    p.add_argument("--serve-seconds", type=float, default=10.0)
     return p.parse_args()
 
 
@@ -357,7 +366,7 @@ def run_ours(args):
         dist.destroy_process_group()
     if rank != 0:
         return
-    launches_per_step = 11  # prep_centers, tc, 2 pair-recheck kernels, full recheck, 6 update kernels
+    launches_per_step = 12  # prep_centers, tc, 2 pair-recheck kernels, 2 full-recheck kernels, 6 update kernels
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "fp16 distances (fp32 accumulate), fp32 recheck, f64 sums",
@@ -368,10 +377,291 @@ def run_ours(args):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------------------
+# other workloads (--config)
+# ---------------------------------------------------------------------------
+def _emit(line):
+    print(json.dumps(line), flush=True)
+
+
+def _fp32_sgemm_tflops(torch):
+    """Measured FP32 (no TF32) GEMM rate of this GPU: the CUDA-core FMA peak proxy."""
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    try:
+        a = torch.randn(8192, 8192, device="cuda")
+        b = torch.randn(8192, 8192, device="cuda")
+        for _ in range(2):
+            a @ b
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(5):
+            a @ b
+        e1.record()
+        torch.cuda.synchronize()
+        return 5 * 2 * 8192.0 ** 3 / (e0.elapsed_time(e1) / 1e3) / 1e12
+    finally:
+        torch.backends.cuda.matmul.allow_tf32 = prev
+
+
+def _lloyd_rate(torch, _lib, X, C0, steps, precision):
+    """(ms per Lloyd iteration, profile) over `steps` graph-launched iterations."""
+    C = C0.clone()
+    _lib.lloyd(X, C, 3, -1.0, precision=precision)
+    C = C0.clone()
+    _lib.profile_enable(True)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    _lib.lloyd(X, C, steps, -1.0, precision=precision)
+    e1.record()
+    torch.cuda.synchronize()
+    prof = _lib.profile_read()
+    _lib.profile_enable(False)
+    return e0.elapsed_time(e1) / steps, prof
+
+
+def run_c1(args):
+    """100,000 x 2, k=50, kmeans++ (fixed_seed=42), max_iter=100, tol 1e-5, then dtrajs."""
+    import torch
+    from oracle import oracle
+    from pyemma_gb300 import _lib, datasets
+    from pyemma_gb300.coordinates import cluster_kmeans
+    _lib.load()
+    X = datasets.small_mixture(seed=SEED)
+    cluster_kmeans(X, k=50, max_iter=100, tolerance=1e-5, fixed_seed=42).dtrajs  # warm-up
+    times, its = [], []
+    for _ in range(max(3, args.steps // 10)):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        km = cluster_kmeans(X, k=50, max_iter=100, tolerance=1e-5, fixed_seed=42)
+        dtrajs = km.dtrajs
+        times.append(time.perf_counter() - t)
+        its.append(int(len(km.inertias)))
+    ms = 1e3 * statistics.median(times)
+    threads = len(os.sched_getaffinity(0))
+    t = time.perf_counter()
+    C0, _ = oracle.kmpp(X, 50, 42, n_threads=threads)
+    res = oracle.lloyd(X, C0, 100, 1e-5, n_threads=threads)
+    oracle.assign(X, res["centers"], n_threads=threads)
+    cpu_ms = 1e3 * (time.perf_counter() - t)
+    _emit({"metric": "k-means wall time (kmeans++ + Lloyd to convergence + dtrajs)", "value": ms, "unit": "ms",
+           "higher_is_better": False, "n_gpus": 1, "frames": len(X), "lloyd_iterations": its[-1],
+           "frames_per_s_end_to_end": len(X) / (ms / 1e3),
+           "config": {"workload": "c1: 100000 x 2 mixture of 10 Gaussians (sigma 0.5, means U[-5,5]^2), k=50, "
+                                  "kmeans++ fixed_seed=42, max_iter=100, tol=1e-5, public API from host numpy"},
+           "cpu_oracle_ms": cpu_ms, "cpu_cores": threads, "dtrajs_len": int(sum(len(d) for d in dtrajs)),
+           "bound": "launch/latency (1.2 MB per pass); no roofline fraction"})
+
+
+def run_c2(args):
+    """20 uneven AR(1) trajectories, d=10, k=1000: packed Lloyd iterations."""
+    import torch
+    from pyemma_gb300 import _lib, datasets
+    from pyemma_gb300.coordinates import KmeansClustering
+    _lib.load()
+    trajs = datasets.metastable_trajectories(n_traj=20, d=10, seed=SEED)
+    n = sum(len(t) for t in trajs)
+    X = torch.from_numpy(np.concatenate(trajs)).cuda()
+    rng = np.random.default_rng(SEED)
+    C0 = X[torch.from_numpy(rng.choice(n, 1000, replace=False)).cuda()].contiguous()
+    ms, prof = _lloyd_rate(torch, _lib, X, C0, args.steps, "fp32")
+    flops = 2.0 * n * 1000 * 10
+    fp32_ms = prof["fp32"][0] / max(1, prof["fp32"][1])
+    peak = _fp32_sgemm_tflops(torch)
+    achieved = flops / (fp32_ms / 1e3) / 1e12
+    # e2e: the public estimator on the 20 host trajectories (pinned), one iteration
+    pinned = []
+    for t in trajs:
+        p = torch.empty(t.shape, dtype=torch.float32, pin_memory=True)
+        p.numpy()[...] = t
+        pinned.append(p.numpy())
+    Ch = C0.cpu().numpy()
+    km = KmeansClustering(n_clusters=1000, max_iter=1, tolerance=-1.0, clustercenters=Ch, precision="fp32")
+    km.estimate(pinned)
+    reps = 3
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        km = KmeansClustering(n_clusters=1000, max_iter=1, tolerance=-1.0, clustercenters=Ch, precision="fp32")
+        km.estimate(pinned)
+        dtrajs = km.dtrajs
+    e2e_s = (time.perf_counter() - t0) / reps
+    _emit({"metric": "k-means frames/s (Lloyd iteration, packed uneven trajectories)", "value": n / (ms / 1e3),
+           "unit": "frames/s", "n_gpus": 1, "steps": args.steps, "ms_per_step": ms, "higher_is_better": True,
+           "dtype": "f32 exact distances, f64 sums",
+           "config": {"workload": "c2: 20 AR(1) metastable trajectories, lengths log-uniform [50k, 500k] "
+                                  "(%d frames), d=10, k=1000, one CUDA graph per Lloyd iteration" % n,
+                      "lengths": [len(t) for t in trajs]},
+           "roofline": {"bound": "fp32 pipe", "kernel": "assign_fp32_kernel", "achieved": achieved,
+                        "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                        "peak_source": "measured FP32 SGEMM (TF32 off) on this GPU",
+                        "note": "exact distances take 3 instructions (sub, mul, add; no FMA) per 2 flops",
+                        "step_breakdown_ms": {k: (v[0] / v[1] if v[1] else None) for k, v in prof.items()}},
+           "e2e": {"value": n / e2e_s, "unit": "frames/s", "h2d_bytes_per_step": n * 40,
+                   "d2h_bytes_per_step": n * 4 + 1000 * 40,
+                   "api": "KmeansClustering(max_iter=1, clustercenters=C).estimate(20 pinned trajectories); dtrajs"},
+           "dtrajs": len(dtrajs)})
+
+
+def run_c4(args):
+    """Precision sweep: 1M frames, d x k grid, fp32 vs fp16 tensor cores."""
+    import torch
+    from pyemma_gb300 import _lib
+    _lib.load()
+    n = 1_000_000
+    rows = []
+    for d in (16, 64, 256, 1024):
+        for k in (100, 1000, 5000):
+            g = torch.Generator(device="cuda")
+            g.manual_seed(SEED + 31 * d + k)
+            means = (torch.rand((4 * k, d), device="cuda", generator=g) * 10.0 - 5.0)
+            comp = torch.randint(0, 4 * k, (n,), device="cuda", generator=g)
+            X = (means[comp] + 0.3 * torch.randn((n, d), device="cuda", generator=g)).contiguous()
+            del means, comp
+            C0 = X[torch.randperm(n, device="cuda", generator=g)[:k]].contiguous()
+            row = {"d": d, "k": k}
+            steps = 2
+            for prec in ("fp32", "fp16"):
+                try:
+                    ms, prof = _lloyd_rate(torch, _lib, X, C0, steps, prec)
+                    row[prec + "_ms_per_iter"] = ms
+                except _lib.KmError as e:
+                    row[prec + "_ms_per_iter"] = None
+                    row[prec + "_error"] = str(e)
+            if row.get("fp16_ms_per_iter") and row.get("fp32_ms_per_iter"):
+                row["speedup"] = row["fp32_ms_per_iter"] / row["fp16_ms_per_iter"]
+                lab16, st = _lib.assign(X, C0, precision="fp16")
+                lab32, _ = _lib.assign(X, C0, precision="fp32")
+                row["recheck_fraction"] = (st["n_recheck"] + st["n_full"]) / float(n)
+                row["full_recheck_fraction"] = st["n_full"] / float(n)
+                row["labels_identical"] = bool(torch.equal(lab16, lab32))
+                row["tflops_fp16_iter"] = 2.0 * n * k * d / (row["fp16_ms_per_iter"] / 1e3) / 1e12
+            rows.append(row)
+            del X, C0
+            torch.cuda.empty_cache()
+    _emit({"metric": "Lloyd iteration time per precision (precision sweep)", "unit": "ms", "n_gpus": 1,
+           "higher_is_better": False,
+           "config": {"workload": "c4: 1,000,000 frames, 4k Gaussian clusters (sigma 0.3, means U[-5,5]^d), "
+                                  "d in {16,64,256,1024}, k in {100,1000,5000}; fp32 exact vs fp16 tensor cores "
+                                  "with exact recheck"},
+           "rows": rows})
+
+
+def run_c5(args):
+    """Serving: Poisson arrivals against 8 resident center sets."""
+    import torch
+    from pyemma_gb300 import _lib, datasets
+    _lib.load()
+    rng = np.random.default_rng(SEED)
+    specs = [(2, 100), (2, 500), (10, 1000), (10, 5000), (528, 500), (528, 1000), (528, 2000), (528, 5000)]
+    pool_n = {2: 2_000_000, 10: 2_000_000, 528: 1_000_000}
+    pools = {}
+    src = {2: datasets.gaussian_mixture(pool_n[2], 2, 10, 0.5, 5.0, SEED),
+           10: np.concatenate(datasets.metastable_trajectories(n_traj=12, d=10, lmin=150_000, lmax=300_000,
+                                                               seed=SEED))[:pool_n[10]]}
+    for d, a in src.items():
+        pool_n[d] = len(a)
+        t = torch.empty(a.shape, dtype=torch.float32, pin_memory=True)
+        t.numpy()[...] = a
+        pools[d] = t
+    Xd528 = datasets.calpha_distances(n_frames=pool_n[528], seed=SEED, device="cuda")
+    pools[528] = torch.empty(tuple(Xd528.shape), dtype=torch.float32, pin_memory=True)
+    pools[528].copy_(Xd528)
+    srv = _lib.Server(hbm_budget_bytes=40 << 30)
+    sets = []
+    for d, k in specs:
+        if d == 528:
+            C = Xd528[torch.from_numpy(rng.choice(pool_n[d], k, replace=False)).cuda()].contiguous()
+        else:
+            C = torch.from_numpy(pools[d].numpy()[rng.choice(pool_n[d], k, replace=False)]).cuda()
+        cs = _lib.Centers(C, precision="auto")
+        sets.append((srv.add_centers(cs), cs, d, k))
+    del Xd528
+    torch.cuda.empty_cache()
+    # schedule
+    rate, dur = 200.0, float(args.serve_seconds)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, size=int(rate * dur * 2)))
+    arrivals = arrivals[arrivals < dur]
+    m = len(arrivals)
+    lengths = np.exp(rng.uniform(np.log(1e3), np.log(1e6), size=m)).astype(np.int64)
+    which = rng.integers(0, len(specs), size=m)
+    starts = [int(rng.integers(0, pool_n[specs[w][0]] - L + 1)) for w, L in zip(which, lengths)]
+    total = int(lengths.sum())
+    arena = torch.empty(total, dtype=torch.int32, pin_memory=True).numpy()
+    offs = np.concatenate([[0], np.cumsum(lengths)])
+    # warm-up: one small request per set
+    for sid, cs, d, k in sets:
+        t, _ = srv.submit(sid, pools[d].numpy()[:4096])
+        srv.poll(t)
+    infos = [None] * m
+    tickets = [None] * m
+
+    def poller():
+        for i in range(m):
+            while tickets[i] is None:
+                time.sleep(0.0002)
+            infos[i] = srv.poll(tickets[i])
+
+    th = threading.Thread(target=poller)
+    th.start()
+    t0 = time.perf_counter()
+    for i in range(m):
+        now = time.perf_counter() - t0
+        if arrivals[i] > now:
+            time.sleep(arrivals[i] - now)
+        sid, cs, d, k = sets[which[i]]
+        Xr = pools[d].numpy()[starts[i]:starts[i] + lengths[i]]
+        tickets[i] = srv.submit(sid, Xr, arena[offs[i]:offs[i + 1]])[0]
+    th.join()
+    t_end = time.perf_counter() - t0
+    lat = np.array([x["total_ms"] for x in infos])
+    qlat = np.array([x["queue_ms"] for x in infos])
+    st = srv.stats()
+    # the same requests alone (one per set, first occurrence) against the mixed results
+    same = True
+    checked = 0
+    for w in range(len(specs)):
+        idx = np.nonzero(which == w)[0]
+        if len(idx) == 0:
+            continue
+        i = int(idx[0])
+        sid, cs, d, k = sets[w]
+        Xr = pools[d].numpy()[starts[i]:starts[i] + lengths[i]]
+        alone, _ = cs.assign(torch.from_numpy(np.ascontiguousarray(Xr)).cuda())
+        same &= bool(np.array_equal(alone.cpu().numpy(), arena[offs[i]:offs[i + 1]]))
+        checked += 1
+    srv.shutdown()
+    flops = sum(2.0 * L * specs[w][1] * specs[w][0] for w, L in zip(which, lengths))
+    per_d = {}
+    for dd in (2, 10, 528):
+        sel = np.array([specs[w][0] == dd for w in which])
+        if sel.any():
+            per_d[str(dd)] = {"requests": int(sel.sum()), "p50_ms": float(np.percentile(lat[sel], 50)),
+                              "p99_ms": float(np.percentile(lat[sel], 99))}
+    _emit({"metric": "serving frames/s with p50/p99 request latency", "value": total / t_end, "unit": "frames/s",
+           "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+           "max_ms": float(lat.max()), "queue_p99_ms": float(np.percentile(qlat, 99)), "n_gpus": 1,
+           "requests": m, "frames": total, "offered_frames_per_s": total / dur,
+           "offered_tflops": flops / dur / 1e12, "wall_s": t_end, "server": st,
+           "labels_same_alone_and_mixed": same, "checked_requests": checked, "per_d": per_d,
+           "config": {"workload": "c5: Poisson arrivals at %.0f req/s for %.0f s, lengths log-uniform [1k, 1M], "
+                                  "8 resident center sets (d, k) = %s, 40 GB admission budget, pinned host "
+                                  "buffers, copies included" % (rate, dur, specs)}})
+
+
 def main():
     args = parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.config == "c1":
+        run_c1(args)
+    elif args.config == "c2":
+        run_c2(args)
+    elif args.config == "c4":
+        run_c4(args)
+    elif args.config == "c5":
+        run_c5(args)
     else:
         run_ours(args)
 

@@ -17,7 +17,9 @@
  *     centers are row-major float32 (k, d); labels are int32.
  *   - Scratch memory is a caller-owned device workspace whose size the
  *     matching *_workspace_size() function returns; pass NULL/0 when it
- *     returns 0.  Entry points allocate no device memory of their own.
+ *     returns 0.  Entry points allocate no device memory of their own,
+ *     except the two object constructors: km_centers_create (a resident
+ *     center set) and km_serve_create (the serving loop's batch slots).
  *   - `stream` is a cudaStream_t (NULL = legacy default stream).  Work is
  *     enqueued on it; calls that return host results synchronise it.
  *   - Every call returns a km_status; km_last_error() gives a message for
@@ -42,7 +44,8 @@ typedef enum {
     KM_ERR_TIMEOUT = 4,         /* a bounded device-side wait expired; the context stays usable */
     KM_ERR_CUDA = 5,            /* a CUDA runtime call failed */
     KM_ERR_UNSUPPORTED = 6,     /* the requested precision or shape has no kernel on this device */
-    KM_ERR_BAD_LABEL = 7        /* a label is outside [0, k) */
+    KM_ERR_BAD_LABEL = 7,       /* a label is outside [0, k) */
+    KM_PENDING = 8              /* km_serve_poll: the request has not completed yet (not an error) */
 } km_status;
 
 /* Distance arithmetic of the assignment.
@@ -161,6 +164,78 @@ int km_lloyd(const float *X, int64_t n, int32_t d, int32_t k, float *C, int32_t 
              double tolerance, int32_t precision, int32_t *labels, double *inertias,
              int32_t *n_iter, int32_t *converged, km_callback cb, void *cb_user, void *workspace,
              size_t workspace_bytes, void *stream);
+
+/* ---- resident center sets: ClusterModel(centers, metric) built once -------
+ * interface.py:164-165 constructs ClusterModel(cluster_centers, metric) for
+ * every chunk it transforms.  A km_centers handle holds a device copy of
+ * the centers and, for KM_PREC_FP16, their scaled FP16 copy, norms and
+ * centering shift, prepared once; any number of km_assign_centers calls on
+ * any streams may share it.  km_centers_create copies C (device), resolves
+ * KM_PREC_AUTO, allocates the device memory that km_centers_info reports
+ * and synchronises `stream`.  km_centers_destroy frees it; no call using
+ * the handle may still be running. */
+typedef struct km_centers km_centers;
+int km_centers_create(const float *C, int32_t k, int32_t d, int32_t precision, void *stream, km_centers **out);
+int km_centers_destroy(km_centers *centers);
+int km_centers_info(const km_centers *centers, int32_t *k, int32_t *d, int32_t *precision,
+                    int64_t *device_bytes);
+
+/* Assignment against a resident set: labels as km_assign with the set's
+ * precision.  The workspace holds only the per-frame buffers. */
+size_t km_assign_centers_workspace_size(int64_t n, const km_centers *centers);
+int km_assign_centers(const float *X, int64_t n, int32_t d, const km_centers *centers, int32_t *labels,
+                      void *workspace, size_t workspace_bytes, km_assign_stats *stats, void *stream);
+
+/* ---- serving loop (no counterpart in the reference) ------------------------
+ * A native worker thread assigns trajectories submitted from any host
+ * thread against resident center sets.  Requests for the same center set
+ * are packed into one batch (continuous batching, FIFO by the oldest
+ * request); a request longer than a batch is split across batches.  Two
+ * batch slots alternate so that the copies of one batch overlap the
+ * kernels of the other.  The slots (frames, labels, assignment workspace)
+ * are the device memory held for requests in flight; their total stays
+ * within hbm_budget_bytes, which sets the batch size.
+ *   km_serve_submit: X_host (host, n*d float32) and labels_host (host, n
+ *     int32) must stay valid until the request completes; page-locked
+ *     buffers let the copies run asynchronously.  d must match the set.
+ *   km_serve_poll: waits up to timeout_ms (-1: no limit) for the request;
+ *     returns KM_PENDING if it has not completed, else its final status,
+ *     after which the ticket is released.  info (host, nullable) receives
+ *     its timings.
+ *   km_serve_shutdown: completes every submitted request, stops the worker
+ *     and frees the slots.  The center sets stay owned by the caller. */
+typedef struct {
+    int64_t hbm_budget_bytes;  /* device bytes for requests in flight; 0 = 40 GiB */
+    int64_t max_batch_frames;  /* frames per batch at most; 0 = as many as the budget allows */
+    int32_t device;            /* CUDA device of the server */
+    int32_t reserved;
+} km_serve_config;
+
+typedef struct {
+    int32_t status;       /* km_status of the request (KM_PENDING while running) */
+    int32_t set_id;
+    int64_t n_frames;
+    int64_t batch_frames; /* frames of the largest batch the request ran in */
+    double queue_ms;      /* submit -> launch of its first batch */
+    double total_ms;      /* submit -> its labels in host memory */
+} km_request_info;
+
+typedef struct {
+    int64_t batches;          /* batches launched */
+    int64_t frames;           /* frames assigned */
+    int64_t requests;         /* requests completed */
+    int64_t batch_cap_frames; /* frames per batch allowed by the budget */
+    int64_t device_bytes;     /* device memory held by the batch slots */
+} km_serve_stats;
+
+typedef struct km_server km_server;
+int km_serve_create(const km_serve_config *config, km_server **out);
+int km_serve_add_centers(km_server *server, const km_centers *centers, int32_t *set_id);
+int km_serve_submit(km_server *server, int32_t set_id, const float *X_host, int64_t n, int32_t d,
+                    int32_t *labels_host, uint64_t *ticket);
+int km_serve_poll(km_server *server, uint64_t ticket, int32_t timeout_ms, km_request_info *info);
+int km_serve_stats_read(km_server *server, km_serve_stats *stats);
+int km_serve_shutdown(km_server *server);
 
 #ifdef __cplusplus
 }

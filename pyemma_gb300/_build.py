@@ -17,7 +17,7 @@ LIB_DIR = os.path.join(HERE, "_lib")
 LIB_PATH = os.path.join(LIB_DIR, "libkmgpu.so")
 INCLUDE_DIR = os.path.join(os.path.dirname(HERE), "include")
 
-SOURCES = ["capi.cu", "assign_fp32.cu", "assign_tc.cu", "update.cu", "kmpp.cu"]
+SOURCES = ["capi.cu", "assign_fp32.cu", "assign_tc.cu", "update.cu", "kmpp.cu", "serve.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O3", "--expt-relaxed-constexpr",
               "-I" + INCLUDE_DIR]
@@ -71,7 +71,7 @@ def build(verbose=False, extra_flags=None):
     with ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(compile_one, SOURCES))
     if _stale(LIB_PATH, objs):
-        cmd = [nvcc] + ARCH + ["-shared", "-o", LIB_PATH] + objs
+        cmd = [nvcc] + ARCH + ["-shared", "-o", LIB_PATH] + objs + ["-lpthread"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n%s%s" % (r.stdout, r.stderr))

@@ -23,6 +23,7 @@ KM_ERR_TIMEOUT = 4
 KM_ERR_CUDA = 5
 KM_ERR_UNSUPPORTED = 6
 KM_ERR_BAD_LABEL = 7
+KM_PENDING = 8
 
 EXPORTED = (
     "km_version", "km_status_string", "km_last_error", "km_profile_enable", "km_profile_read",
@@ -30,6 +31,10 @@ EXPORTED = (
     "km_update_workspace_size", "km_update", "km_update_noalloc_max_bytes", "km_update_noalloc",
     "km_kmpp_workspace_size", "km_kmpp",
     "km_lloyd_workspace_size", "km_lloyd",
+    "km_centers_create", "km_centers_destroy", "km_centers_info", "km_assign_centers_workspace_size",
+    "km_assign_centers",
+    "km_serve_create", "km_serve_add_centers", "km_serve_submit", "km_serve_poll", "km_serve_stats_read",
+    "km_serve_shutdown",
 )
 
 
@@ -52,6 +57,28 @@ class AssignStats(ctypes.Structure):
 
 
 CALLBACK = ctypes.CFUNCTYPE(None, ctypes.c_void_p)
+
+
+class ServeConfig(ctypes.Structure):
+    _fields_ = [("hbm_budget_bytes", ctypes.c_int64), ("max_batch_frames", ctypes.c_int64),
+                ("device", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
+class RequestInfo(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int32), ("set_id", ctypes.c_int32), ("n_frames", ctypes.c_int64),
+                ("batch_frames", ctypes.c_int64), ("queue_ms", ctypes.c_double), ("total_ms", ctypes.c_double)]
+
+    def as_dict(self):
+        return dict(status=self.status, set_id=self.set_id, n_frames=self.n_frames,
+                    batch_frames=self.batch_frames, queue_ms=self.queue_ms, total_ms=self.total_ms)
+
+
+class ServeStats(ctypes.Structure):
+    _fields_ = [("batches", ctypes.c_int64), ("frames", ctypes.c_int64), ("requests", ctypes.c_int64),
+                ("batch_cap_frames", ctypes.c_int64), ("device_bytes", ctypes.c_int64)]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
 
 _lib = None
 
@@ -100,7 +127,24 @@ def load(build_if_missing=False):
     L.km_lloyd_workspace_size.argtypes = [i64, i32, i32, i32]
     L.km_lloyd_workspace_size.restype = sz
     L.km_lloyd.argtypes = [P, i64, i32, i32, P, i32, f64, i32, P, P, P, P, CALLBACK, P, P, sz, P]
-    for name in ("km_assign", "km_batch_assign", "km_update", "km_kmpp", "km_lloyd"):
+    pp = ctypes.POINTER(ctypes.c_void_p)
+    L.km_centers_create.argtypes = [P, i32, i32, i32, P, pp]
+    L.km_centers_destroy.argtypes = [P]
+    L.km_centers_info.argtypes = [P, ctypes.POINTER(i32), ctypes.POINTER(i32), ctypes.POINTER(i32),
+                                  ctypes.POINTER(i64)]
+    L.km_assign_centers_workspace_size.argtypes = [i64, P]
+    L.km_assign_centers_workspace_size.restype = sz
+    L.km_assign_centers.argtypes = [P, i64, i32, P, P, P, sz, ctypes.POINTER(AssignStats), P]
+    L.km_serve_create.argtypes = [ctypes.POINTER(ServeConfig), pp]
+    L.km_serve_add_centers.argtypes = [P, P, ctypes.POINTER(i32)]
+    L.km_serve_submit.argtypes = [P, i32, P, i64, i32, P, ctypes.POINTER(ctypes.c_uint64)]
+    L.km_serve_poll.argtypes = [P, ctypes.c_uint64, i32, ctypes.POINTER(RequestInfo)]
+    L.km_serve_stats_read.argtypes = [P, ctypes.POINTER(ServeStats)]
+    L.km_serve_shutdown.argtypes = [P]
+    for name in ("km_assign", "km_batch_assign", "km_update", "km_kmpp", "km_lloyd", "km_centers_create",
+                 "km_centers_destroy", "km_centers_info", "km_assign_centers", "km_serve_create",
+                 "km_serve_add_centers", "km_serve_submit", "km_serve_poll", "km_serve_stats_read",
+                 "km_serve_shutdown"):
         getattr(L, name).restype = ctypes.c_int
     _lib = L
     return L
@@ -302,3 +346,123 @@ def lloyd(X, C, max_iter, tolerance, precision="auto", callback=None, labels=Non
     del keep
     return dict(labels=labels, inertias=inertias[:n_iter.value].copy(), n_iter=n_iter.value,
                 converged=bool(conv.value))
+
+
+class Centers(object):
+    """A resident center set (km_centers): centers copied to the device and,
+    for the tensor-core path, prepared once for every later assignment."""
+
+    def __init__(self, C, precision="auto"):
+        torch = _torch()
+        L = load()
+        _check_frames(torch, C, "C")
+        self._L = L
+        self._h = ctypes.c_void_p()
+        self.device = C.device
+        check(L.km_centers_create(_ptr(C), C.shape[0], C.shape[1], precision_code(precision),
+                                  _stream(torch, C.device), ctypes.byref(self._h)))
+        k, d, p, nb = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int64()
+        check(L.km_centers_info(self._h, ctypes.byref(k), ctypes.byref(d), ctypes.byref(p), ctypes.byref(nb)))
+        self.k, self.d, self.precision, self.device_bytes = k.value, d.value, PRECISION_NAMES[p.value], nb.value
+
+    @property
+    def handle(self):
+        if not self._h:
+            raise ValueError("the center set was released")
+        return self._h
+
+    def assign(self, X, labels=None):
+        """Labels (int32 CUDA tensor) of the nearest resident center for every row of X."""
+        torch = _torch()
+        _check_frames(torch, X)
+        n, d = X.shape
+        if labels is None:
+            labels = torch.empty(n, dtype=torch.int32, device=X.device)
+        ws_bytes = self._L.km_assign_centers_workspace_size(n, self.handle)
+        ws = _workspace(torch, ws_bytes, X.device)
+        stats = AssignStats()
+        check(self._L.km_assign_centers(_ptr(X), n, d, self.handle, _ptr(labels), _ptr(ws), ws_bytes,
+                                        ctypes.byref(stats), _stream(torch, X.device)))
+        return labels, stats.as_dict()
+
+    def close(self):
+        if self._h:
+            torch = _torch()
+            torch.cuda.synchronize(self.device)
+            check(self._L.km_centers_destroy(self._h))
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server(object):
+    """The native serving loop (km_serve_*): trajectories submitted from host
+    memory are batched per resident center set and assigned on the GPU."""
+
+    def __init__(self, hbm_budget_bytes=40 << 30, max_batch_frames=0, device=0):
+        L = load()
+        self._L = L
+        cfg = ServeConfig(int(hbm_budget_bytes), int(max_batch_frames), int(device), 0)
+        self._h = ctypes.c_void_p()
+        check(L.km_serve_create(ctypes.byref(cfg), ctypes.byref(self._h)))
+        self._sets = []
+        self._inflight = {}
+
+    def add_centers(self, centers):
+        """Registers a Centers object; returns its set id."""
+        sid = ctypes.c_int32()
+        check(self._L.km_serve_add_centers(self._h, centers.handle, ctypes.byref(sid)))
+        self._sets.append(centers)
+        return sid.value
+
+    def submit(self, set_id, X_host, labels_host=None):
+        """Queues X_host (C-contiguous float32 (n, d) numpy array or CPU tensor,
+        page-locked for asynchronous copies); returns (ticket, labels array)."""
+        if hasattr(X_host, "numpy"):
+            X_np = X_host.numpy()
+        else:
+            X_np = X_host
+        if X_np.dtype != np.float32 or X_np.ndim != 2 or not X_np.flags["C_CONTIGUOUS"]:
+            raise ValueError("X_host must be a C-contiguous float32 (n, d) host array")
+        n, d = X_np.shape
+        if labels_host is None:
+            labels_host = np.empty(n, dtype=np.int32)
+        lab_np = labels_host.numpy() if hasattr(labels_host, "numpy") else labels_host
+        if lab_np.dtype != np.int32 or lab_np.shape != (n,) or not lab_np.flags["C_CONTIGUOUS"]:
+            raise ValueError("labels_host must be a contiguous int32 array of n entries")
+        t = ctypes.c_uint64()
+        check(self._L.km_serve_submit(self._h, int(set_id), X_np.ctypes.data_as(ctypes.c_void_p), n, d,
+                                      lab_np.ctypes.data_as(ctypes.c_void_p), ctypes.byref(t)))
+        self._inflight[t.value] = (X_host, labels_host)  # keep the buffers alive
+        return t.value, labels_host
+
+    def poll(self, ticket, timeout_ms=-1):
+        """Request info dict once the request completed, None while pending."""
+        info = RequestInfo()
+        rc = self._L.km_serve_poll(self._h, ctypes.c_uint64(ticket), int(timeout_ms), ctypes.byref(info))
+        if rc == KM_PENDING:
+            return None
+        self._inflight.pop(ticket, None)
+        check(rc)
+        return info.as_dict()
+
+    def stats(self):
+        st = ServeStats()
+        check(self._L.km_serve_stats_read(self._h, ctypes.byref(st)))
+        return st.as_dict()
+
+    def shutdown(self):
+        if self._h:
+            check(self._L.km_serve_shutdown(self._h))
+            self._h = ctypes.c_void_p()
+            self._inflight.clear()
+
+    def __del__(self):
+        try:
+            self.shutdown()
+        except Exception:
+            pass

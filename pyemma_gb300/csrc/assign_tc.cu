@@ -46,6 +46,8 @@
 //    hi_j(v) = (1+g) (sqrt(v+E_j) + R_j)^2, evaluated with directed rounding.
 #include <cuda.h>
 
+#include <algorithm>
+
 #include "km_common.cuh"
 #include "km_internal.h"
 
@@ -81,6 +83,7 @@ struct TcParams {
     int nbst;          // B stages per center tile (ceil(ksteps_total * 16 / bk))
     int bn;
     int stages;
+    int stream_a;  // 1: A chunks travel with the B stages instead of staying resident (large d)
     int n_ctiles;
     uint32_t tmem_cols;
     float e_coef;
@@ -477,14 +480,21 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                      const TcParams p) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    // Resident mode: sA holds the frame tile's nkc A chunks, the ring of
+    // stages holds B.  Streaming mode (d too large for a resident tile):
+    // every stage holds one A chunk followed by the matching B chunk.
+    const bool stream = p.stream_a != 0;
+    const int nab = stream ? 0 : p.nkc;  // resident A chunks (and their barrier pairs)
     uint8_t *sA = smem;
-    uint8_t *sB = sA + p.nkc * kABytesPerChunk;
+    uint8_t *sB = sA + nab * kABytesPerChunk;
     const int b_stage_bytes = p.bn * p.bk * 2;
-    const int spc = kKC / p.bk;  // B stages per A chunk (1 or 2)
-    uint64_t *bars = reinterpret_cast<uint64_t *>(sB + p.stages * b_stage_bytes);
+    const int stage_bytes = b_stage_bytes + (stream ? kABytesPerChunk : 0);
+    const int b_off = stream ? kABytesPerChunk : 0;  // B within a stage
+    const int spc = kKC / p.bk;  // B stages per A chunk (1 or 2; 1 when streaming)
+    uint64_t *bars = reinterpret_cast<uint64_t *>(sB + p.stages * stage_bytes);
     uint64_t *a_full = bars;
-    uint64_t *a_empty = a_full + p.nkc;
-    uint64_t *b_full = a_empty + p.nkc;
+    uint64_t *a_empty = a_full + nab;
+    uint64_t *b_full = a_empty + nab;
     uint64_t *b_empty = b_full + p.stages;
     uint64_t *acc_full = b_empty + p.stages;
     uint64_t *acc_empty = acc_full + 2;
@@ -496,7 +506,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
     const int lane = threadIdx.x & 31;
 
     if (threadIdx.x == 0) {
-        for (int c = 0; c < p.nkc; ++c) {
+        for (int c = 0; c < nab; ++c) {
             mbar_init(&a_full[c], 1);
             mbar_init(&a_empty[c], 1);
         }
@@ -539,7 +549,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
             for (int ct = 0; ct < p.n_ctiles && ok; ++ct) {
                 for (int t = 0; t < p.nbst; ++t) {
                     const int kc = t / spc;
-                    if (ct == 0 && t % spc == 0) {
+                    if (!stream && ct == 0 && t % spc == 0) {
                         if (!__all_sync(0xffffffffu, mbar_wait_timed(&a_empty[kc], (t_local & 1u) ^ 1u, pw_a))) {
                             ok = false;
                             break;
@@ -557,8 +567,10 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                         break;
                     }
                     if (elect_one()) {
-                        mbar_arrive_expect_tx(&b_full[s], b_stage_bytes);
-                        tma_load_2d(sB + s * b_stage_bytes, &tmB, t * p.bk, ct * p.bn, &b_full[s]);
+                        uint8_t *st = sB + s * stage_bytes;
+                        mbar_arrive_expect_tx(&b_full[s], stage_bytes);
+                        if (stream) tma_load_2d(st, &tmA, t * kKC, (int)(ft * kBM), &b_full[s]);
+                        tma_load_2d(st + b_off, &tmB, t * p.bk, ct * p.bn, &b_full[s]);
                     }
                     __syncwarp();
                     ++bq;
@@ -577,7 +589,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
         // Drain: every load issued above has landed before the CTA exits.
         if (t_local > 0 || bq > 0) {
             const uint32_t last_a = (t_local - 1u) & 1u;
-            for (int kc = 0; kc < p.nkc && t_local > 0; ++kc) mbar_wait(&a_full[kc], last_a);
+            for (int kc = 0; kc < nab && t_local > 0; ++kc) mbar_wait(&a_full[kc], last_a);
             for (uint32_t s = 0; s < (uint32_t)p.stages && s < bq; ++s) {
                 const uint32_t last_q = bq - 1u - ((bq - 1u - s) % p.stages);
                 mbar_wait(&b_full[s], (last_q / p.stages) & 1u);
@@ -610,7 +622,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                 for (int t = 0; t < p.nbst; ++t) {
                     const int kc = t / spc;
                     const int half = t % spc;
-                    if (ct == 0 && half == 0 &&
+                    if (!stream && ct == 0 && half == 0 &&
                         !__all_sync(0xffffffffu, mbar_wait_timed(&a_full[kc], t_local & 1u, pw_a))) {
                         ok = false;
                         break;
@@ -623,15 +635,18 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                     // TMA completion on the mbarrier orders the loaded tiles before
                     // the MMAs; no tcgen05 fence is needed here.
                     const int steps = min(spt, p.ksteps_total - spt * t);
-                    const uint64_t ad = adesc0 + (uint64_t)((kc * kABytesPerChunk + half * p.bk * 2) >> 4);
-                    const uint32_t b0 = sb0 + s * b_stage_bytes;
+                    const uint32_t st0 = sb0 + s * stage_bytes;
+                    const uint64_t ad = stream ? sw128_desc(st0)
+                                               : adesc0 + (uint64_t)((kc * kABytesPerChunk + half * p.bk * 2) >> 4);
+                    const uint32_t b0 = st0 + b_off;
                     const uint64_t bd = p.bk == kKC ? sw128_desc(b0) : sw64_desc(b0);
                     if (elect_one()) {
 #pragma unroll
                         for (int kk = 0; kk < 4; ++kk)  // 32-byte K steps: +2 in the start-address field
                             if (kk < steps) mma_f16(d_tmem, ad + 2 * kk, bd + 2 * kk, idesc, (t | kk) != 0);
                         mma_commit(&b_empty[s]);
-                        if (ct == p.n_ctiles - 1 && (half == spc - 1 || t == p.nbst - 1)) mma_commit(&a_empty[kc]);
+                        if (!stream && ct == p.n_ctiles - 1 && (half == spc - 1 || t == p.nbst - 1))
+                            mma_commit(&a_empty[kc]);
                     }
                     __syncwarp();
                     ++bq;
@@ -922,25 +937,35 @@ int pick_bk(int d, int k) {
 }
 
 struct Plan {
-    int bn, bk, stages, nkc, smem;
+    int bn, bk, stages, nkc, smem, stream_a;
     uint32_t tmem_cols;
 };
 
 bool make_plan(int d, int k, Plan &pl) {
     pl.nkc = kp_of(d) / kKC;
-    if (pl.nkc > kMaxNkc) return false;
     pl.bn = pick_bn(k);
     pl.bk = pick_bk(d, k);
-    const int fixed = 1024 + 512 + pl.nkc * kABytesPerChunk;
-    int stages = (kSmemLimit - fixed) / (pl.bn * pl.bk * 2);
-    if (stages > 8) stages = 8;
-    if (stages < 2 && pl.bk == kKC) {
-        pl.bk = kKC / 2;  // narrower stages when two wide ones do not fit
-        stages = (kSmemLimit - fixed) / (pl.bn * pl.bk * 2);
+    pl.stream_a = 0;
+    const int fixed = 1024 + 512;
+    int stages = 0;
+    if (pl.nkc <= kMaxNkc) {
+        const int res = fixed + pl.nkc * kABytesPerChunk;
+        stages = std::min(8, (kSmemLimit - res) / (pl.bn * pl.bk * 2));
+        if (stages < 2 && pl.bk == kKC) {
+            pl.bk = kKC / 2;  // narrower stages when two wide ones do not fit
+            stages = std::min(8, (kSmemLimit - res) / (pl.bn * pl.bk * 2));
+        }
+        if (stages >= 2) pl.smem = res + stages * pl.bn * pl.bk * 2;
     }
-    if (stages < 2) return false;
+    if (stages < 2) {
+        // Streaming: each stage carries an A chunk and a full-width B chunk.
+        pl.stream_a = 1;
+        pl.bk = kKC;
+        stages = std::min(8, (kSmemLimit - fixed) / (kABytesPerChunk + pl.bn * kKC * 2));
+        if (stages < 2) return false;
+        pl.smem = fixed + stages * (kABytesPerChunk + pl.bn * kKC * 2);
+    }
     pl.stages = stages;
-    pl.smem = fixed + stages * pl.bn * pl.bk * 2;
     if (pl.smem < 120 * 1024) pl.smem = 120 * 1024;  // one CTA per SM: TMEM is sized for one
     uint32_t cols = 32;
     while (cols < (uint32_t)(2 * pl.bn)) cols <<= 1;
@@ -1110,6 +1135,7 @@ int tc_assign(const float *X, int64_t n, int d, const float *C, int k, int32_t *
     p.nkc = pl.nkc;
     p.ksteps_total = (d + 2 + 15) / 16;
     p.bk = pl.bk;
+    p.stream_a = pl.stream_a;
     p.nbst = (p.ksteps_total * 16 + pl.bk - 1) / pl.bk;
     p.bn = pl.bn;
     p.stages = pl.stages;

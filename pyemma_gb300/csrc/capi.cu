@@ -127,23 +127,11 @@ int check_device_errors(uint32_t e) {
     return KM_OK;
 }
 
-int assign_impl(const float *X, int64_t n, int32_t d, const float *C, int32_t k, int32_t precision,
-                int32_t *labels, void *ws, size_t ws_bytes, km_assign_stats *stats, cudaStream_t s) {
-    KM_TRY(check_shape(n, d, k));
-    if ((n > 0 && (!X || !labels)) || !C) {
-        set_error("X, C and labels must be non-NULL");
-        return KM_ERR_BAD_SHAPE;
-    }
-    int prec = resolve_precision(precision, d, k, true);
-    if (prec != KM_PREC_FP32 && prec != KM_PREC_FP16) {
-        set_error("unknown precision %d", precision);
-        return KM_ERR_BAD_SHAPE;
-    }
-    if (prec == KM_PREC_FP16 && !tc_supported(d, k)) {
-        set_error("no tensor-core kernel for d=%d, k=%d on this device", d, k);
-        return KM_ERR_UNSUPPORTED;
-    }
-    KM_TRY(check_ws(ws, ws_bytes, assign_ws_bytes(n, d, k, prec)));
+// The assignment once the precision is resolved and the workspace checked.
+// For KM_PREC_FP16, b holds the carved buffers; centers_ready means the
+// center half (FP16 copy, norms, shift, scale) is already prepared.
+int assign_core(const float *X, int64_t n, int32_t d, const float *C, int32_t k, int prec, int32_t *labels,
+                TcBuffers &b, bool centers_ready, km_assign_stats *stats, cudaStream_t s) {
     if (stats) {
         std::memset(stats, 0, sizeof(*stats));
         stats->n_frames = n;
@@ -164,10 +152,10 @@ int assign_impl(const float *X, int64_t n, int32_t d, const float *C, int32_t k,
         prof.collect();
         return KM_OK;
     }
-    TcBuffers b;
-    carve_assign(ws, n, d, k, b);
-    KM_TRY(tc_prepare_shift_from_centers(C, d, k, b, s));
-    KM_TRY(tc_prepare_centers(C, d, k, b, s));
+    if (!centers_ready) {
+        KM_TRY(tc_prepare_shift_from_centers(C, d, k, b, s));
+        KM_TRY(tc_prepare_centers(C, d, k, b, s));
+    }
     KM_TRY(tc_prepare_frames(X, n, d, b, s));
     KM_TRY(tc_assign(X, n, d, C, k, labels, b, s, &prof));
     if (prof.active) {
@@ -190,6 +178,34 @@ int assign_impl(const float *X, int64_t n, int32_t d, const float *C, int32_t k,
     return KM_OK;
 }
 
+int assign_impl(const float *X, int64_t n, int32_t d, const float *C, int32_t k, int32_t precision,
+                int32_t *labels, void *ws, size_t ws_bytes, km_assign_stats *stats, cudaStream_t s) {
+    KM_TRY(check_shape(n, d, k));
+    if ((n > 0 && (!X || !labels)) || !C) {
+        set_error("X, C and labels must be non-NULL");
+        return KM_ERR_BAD_SHAPE;
+    }
+    int prec = resolve_precision(precision, d, k, true);
+    if (prec != KM_PREC_FP32 && prec != KM_PREC_FP16) {
+        set_error("unknown precision %d", precision);
+        return KM_ERR_BAD_SHAPE;
+    }
+    if (prec == KM_PREC_FP16 && !tc_supported(d, k)) {
+        set_error("no tensor-core kernel for d=%d, k=%d on this device", d, k);
+        return KM_ERR_UNSUPPORTED;
+    }
+    KM_TRY(check_ws(ws, ws_bytes, assign_ws_bytes(n, d, k, prec)));
+    TcBuffers b;
+    if (prec == KM_PREC_FP16 && n > 0) carve_assign(ws, n, d, k, b);
+    return assign_core(X, n, d, C, k, prec, labels, b, false, stats, s);
+}
+
+// Workspace of an assignment whose centers are prepared: frames + lists.
+size_t resident_ws_bytes(int64_t n, int d, int k, int prec) {
+    if (prec != KM_PREC_FP16) return 0;
+    return tc_frames_ws_size(n, d) + tc_assign_ws_size(n, d, k) + 2 * 256;
+}
+
 size_t lloyd_ws_bytes(int64_t n, int d, int k, int prec) {
     Carver c(nullptr);
     c.take<char>(update_ws_size(n, d, k));
@@ -204,6 +220,44 @@ size_t lloyd_ws_bytes(int64_t n, int d, int k, int prec) {
 }  // namespace km
 
 using namespace km;
+
+// A resident center set (include/kmgpu.h).
+struct km_centers {
+    int32_t k = 0, d = 0, prec = KM_PREC_FP32;
+    int device = 0;
+    void *mem = nullptr;
+    size_t bytes = 0;
+    float *C = nullptr;
+    TcBuffers tc;  // center half: ch, cnorm, shift, scal (KM_PREC_FP16)
+};
+
+namespace km {
+// Enqueues the assignment of n frames against a resident center set without
+// synchronising: the device error word (tensor-core waits) is copied to
+// err_host (host, ideally pinned) on the same stream, 0 for KM_PREC_FP32.
+int assign_centers_enqueue(const float *X, int64_t n, const km_centers *h, int32_t *labels, void *ws,
+                           size_t ws_bytes, uint32_t *err_host, cudaStream_t s) {
+    *err_host = 0;
+    KM_TRY(check_ws(ws, ws_bytes, resident_ws_bytes(n, h->d, h->k, h->prec)));
+    if (n == 0) return KM_OK;
+    if (h->prec == KM_PREC_FP32)
+        return launch_assign_fp32(X, nullptr, nullptr, n, h->d, h->C, h->k, labels, nullptr, nullptr, s);
+    TcBuffers b = h->tc;
+    char *p = static_cast<char *>(ws);
+    tc_carve_frames(p, n, h->d, b);
+    p += (tc_frames_ws_size(n, h->d) + 255) / 256 * 256;
+    tc_carve_assign(p, n, h->d, h->k, b);
+    KM_TRY(tc_prepare_frames(X, n, h->d, b, s));
+    KM_TRY(tc_assign(X, n, h->d, h->C, h->k, labels, b, s, nullptr));
+    KM_CUDA(cudaMemcpyAsync(err_host, b.err, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    return KM_OK;
+}
+
+size_t assign_centers_ws_bytes(int64_t n, const km_centers *h) { return resident_ws_bytes(n, h->d, h->k, h->prec); }
+int centers_d(const km_centers *h) { return h->d; }
+int centers_device(const km_centers *h) { return h->device; }
+int device_error_status(uint32_t e) { return check_device_errors(e); }
+}  // namespace km
 
 extern "C" {
 
@@ -487,6 +541,119 @@ int km_lloyd(const float *X, int64_t n, int32_t d, int32_t k, float *C, int32_t 
     }
     if (exec) cudaGraphExecDestroy(exec);
     return status;
+}
+
+// ---- resident center sets --------------------------------------------------
+
+int km_centers_create(const float *C, int32_t k, int32_t d, int32_t precision, void *stream, km_centers **out) {
+    if (!out) {
+        set_error("out must be non-NULL");
+        return KM_ERR_BAD_SHAPE;
+    }
+    *out = nullptr;
+    KM_TRY(check_shape(0, d, k));
+    if (!C) {
+        set_error("C must be non-NULL");
+        return KM_ERR_BAD_SHAPE;
+    }
+    const int prec = resolve_precision(precision, d, k, true);
+    if (prec != KM_PREC_FP32 && prec != KM_PREC_FP16) {
+        set_error("unknown precision %d", precision);
+        return KM_ERR_BAD_SHAPE;
+    }
+    if (prec == KM_PREC_FP16 && !tc_supported(d, k)) {
+        set_error("no tensor-core kernel for d=%d, k=%d on this device", d, k);
+        return KM_ERR_UNSUPPORTED;
+    }
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    km_centers *h = new km_centers();
+    h->k = k;
+    h->d = d;
+    h->prec = prec;
+    cudaGetDevice(&h->device);
+    const size_t c_bytes = ((size_t)k * d * sizeof(float) + 255) / 256 * 256;
+    h->bytes = c_bytes + (prec == KM_PREC_FP16 ? tc_centers_ws_size(d, k) : 0);
+    cudaError_t e = cudaMalloc(&h->mem, h->bytes);
+    if (e != cudaSuccess) {
+        delete h;
+        return cuda_fail(e, "cudaMalloc (resident centers)");
+    }
+    h->C = static_cast<float *>(h->mem);
+    int st = KM_OK;
+    e = cudaMemcpyAsync(h->C, C, (size_t)k * d * sizeof(float), cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) st = cuda_fail(e, "cudaMemcpyAsync (resident centers)");
+    if (st == KM_OK && prec == KM_PREC_FP16) {
+        tc_carve_centers(static_cast<char *>(h->mem) + c_bytes, d, k, h->tc);
+        st = tc_prepare_shift_from_centers(h->C, d, k, h->tc, s);
+        if (st == KM_OK) st = tc_prepare_centers(h->C, d, k, h->tc, s);
+    }
+    if (st == KM_OK) {
+        e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) st = cuda_fail(e, "cudaStreamSynchronize (resident centers)");
+    }
+    if (st != KM_OK) {
+        cudaFree(h->mem);
+        delete h;
+        return st;
+    }
+    *out = h;
+    return KM_OK;
+}
+
+int km_centers_destroy(km_centers *h) {
+    if (!h) return KM_OK;
+    int prev = 0;
+    cudaGetDevice(&prev);
+    if (prev != h->device) cudaSetDevice(h->device);
+    cudaError_t e = cudaFree(h->mem);
+    if (prev != h->device) cudaSetDevice(prev);
+    delete h;
+    if (e != cudaSuccess) return cuda_fail(e, "cudaFree (resident centers)");
+    return KM_OK;
+}
+
+int km_centers_info(const km_centers *h, int32_t *k, int32_t *d, int32_t *precision, int64_t *device_bytes) {
+    if (!h) {
+        set_error("centers must be non-NULL");
+        return KM_ERR_BAD_SHAPE;
+    }
+    if (k) *k = h->k;
+    if (d) *d = h->d;
+    if (precision) *precision = h->prec;
+    if (device_bytes) *device_bytes = (int64_t)h->bytes;
+    return KM_OK;
+}
+
+size_t km_assign_centers_workspace_size(int64_t n, const km_centers *h) {
+    if (!h || check_shape(n, h->d, h->k) != KM_OK) return 0;
+    return resident_ws_bytes(n, h->d, h->k, h->prec);
+}
+
+int km_assign_centers(const float *X, int64_t n, int32_t d, const km_centers *h, int32_t *labels, void *workspace,
+                      size_t workspace_bytes, km_assign_stats *stats, void *stream) {
+    if (!h) {
+        set_error("centers must be non-NULL");
+        return KM_ERR_BAD_SHAPE;
+    }
+    KM_TRY(check_shape(n, d, h->k));
+    if (d != h->d) {
+        set_error("frames have d=%d, the center set d=%d", d, h->d);
+        return KM_ERR_BAD_SHAPE;
+    }
+    if (n > 0 && (!X || !labels)) {
+        set_error("X and labels must be non-NULL");
+        return KM_ERR_BAD_SHAPE;
+    }
+    KM_TRY(check_ws(workspace, workspace_bytes, resident_ws_bytes(n, d, h->k, h->prec)));
+    TcBuffers b;
+    if (h->prec == KM_PREC_FP16 && n > 0) {
+        b = h->tc;  // prepared center half; the carves below fill the frame and list fields
+        char *p = static_cast<char *>(workspace);
+        tc_carve_frames(p, n, d, b);
+        p += (tc_frames_ws_size(n, d) + 255) / 256 * 256;
+        tc_carve_assign(p, n, d, h->k, b);
+    }
+    return assign_core(X, n, d, h->C, h->k, h->prec, labels, b, true, stats, static_cast<cudaStream_t>(stream));
 }
 
 }  // extern "C"

@@ -7,6 +7,8 @@
 
 #include <cstddef>
 
+#include "../../include/kmgpu.h"
+
 namespace km {
 
 // ---- profiling (capi.cu) ------------------------------------------------------
@@ -110,5 +112,13 @@ int tc_prepare_centers(const float *C, int d, int k, TcBuffers &b, cudaStream_t 
 int tc_assign(const float *X, int64_t n, int d, const float *C, int k, int32_t *labels,
               TcBuffers &b, cudaStream_t s, ProfEvents *prof = nullptr, float *dump = nullptr,
               unsigned long long *wait_cycles = nullptr);
+
+// Resident center sets (capi.cu), used by the serving loop (serve.cu).
+int assign_centers_enqueue(const float *X, int64_t n, const km_centers *h, int32_t *labels, void *ws,
+                           size_t ws_bytes, uint32_t *err_host, cudaStream_t s);
+size_t assign_centers_ws_bytes(int64_t n, const km_centers *h);
+int centers_d(const km_centers *h);
+int centers_device(const km_centers *h);
+int device_error_status(uint32_t e);
 
 }  // namespace km

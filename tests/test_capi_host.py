@@ -192,3 +192,23 @@ def test_gpu_path_fails_loudly_without_device():
         assign_to_centers(np.zeros((10, 2)), np.zeros((3, 2)))
     with pytest.raises(RuntimeError):
         cluster_kmeans(np.zeros((10, 2)), k=2)
+
+
+def test_serving_and_resident_sets_need_a_device():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a CUDA device is present")
+    from pyemma_gb300 import _lib
+    with pytest.raises(_lib.KmError) as e:
+        _lib.Server()
+    assert e.value.status == _lib.KM_ERR_CUDA
+    L = _lib.load()
+    import ctypes
+    # argument checks run before any device call
+    assert L.km_serve_submit(None, 0, None, 0, 1, None, None) == _lib.KM_ERR_BAD_SHAPE
+    assert L.km_serve_poll(None, 1, 0, None) == _lib.KM_ERR_BAD_SHAPE
+    assert L.km_serve_shutdown(None) == _lib.KM_OK
+    assert L.km_centers_destroy(None) == _lib.KM_OK
+    out = ctypes.c_void_p()
+    assert L.km_centers_create(None, 4, 2, 0, None, ctypes.byref(out)) == _lib.KM_ERR_BAD_SHAPE
+    assert L.km_assign_centers_workspace_size(100, None) == 0

@@ -58,7 +58,7 @@ def test_golden_labels(torch, L, golden, case, prec):
 
 
 @pytest.mark.parametrize("prec", PRECS)
-@pytest.mark.parametrize("d", [1, 2, 3, 7, 10, 16, 31, 32, 33, 64, 100, 128, 200, 257, 528, 576])
+@pytest.mark.parametrize("d", [1, 2, 3, 7, 10, 16, 31, 32, 33, 64, 100, 128, 200, 257, 528, 576, 640, 1024, 2050])
 def test_random_shapes(torch, L, oracle, d, prec):
     rng = np.random.default_rng(1000 + d)
     for n, k in [(1, 1), (127, 5), (1000, 33), (4097, 257), (3000, 1000)]:
