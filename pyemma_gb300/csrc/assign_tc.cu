@@ -539,45 +539,52 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
         // one elected lane issues the copies.  Per center tile: B stages
         // t = 0..nbst-1 (bk K-columns each); the A chunk kc = t/spc (64
         // K-columns) is loaded with its first stage on the first center tile.
-        uint32_t bq = 0;
+        // Stage index and phase advance incrementally; a failed wait clears
+        // ok and stops the issues, and the warp agrees on ok once per center
+        // tile.  `issued` counts the B stages actually loaded (for the drain).
+        uint32_t issued = 0, a_issued_tiles = 0;
         uint32_t t_local = 0;
         bool ok = true;
         unsigned long long w_b = 0, w_a = 0;
         unsigned long long *pw_b = (p.wait_cycles && lane == 0) ? &w_b : nullptr;
         unsigned long long *pw_a = (p.wait_cycles && lane == 0) ? &w_a : nullptr;
+        uint32_t s = 0, sph = 0;
         for (int64_t ft = blockIdx.x; ft < n_ftiles && ok; ft += gridDim.x, ++t_local) {
+            const int frame_row = (int)(ft * kBM);
             for (int ct = 0; ct < p.n_ctiles && ok; ++ct) {
+                int kc = 0, half = 0;
                 for (int t = 0; t < p.nbst; ++t) {
-                    const int kc = t / spc;
-                    if (!stream && ct == 0 && t % spc == 0) {
-                        if (!__all_sync(0xffffffffu, mbar_wait_timed(&a_empty[kc], (t_local & 1u) ^ 1u, pw_a))) {
-                            ok = false;
-                            break;
-                        }
-                        if (elect_one()) {
+                    if (!stream && ct == 0 && half == 0) {
+                        if (ok) ok = mbar_wait_timed(&a_empty[kc], (t_local & 1u) ^ 1u, pw_a);
+                        if (elect_one() && ok) {
                             mbar_arrive_expect_tx(&a_full[kc], kABytesPerChunk);
-                            tma_load_2d(sA + kc * kABytesPerChunk, &tmA, kc * kKC, (int)(ft * kBM), &a_full[kc]);
+                            tma_load_2d(sA + kc * kABytesPerChunk, &tmA, kc * kKC, frame_row, &a_full[kc]);
                         }
                         __syncwarp();
                     }
-                    const uint32_t s = bq % p.stages;
-                    const uint32_t ph = (bq / p.stages) & 1u;
-                    if (!__all_sync(0xffffffffu, mbar_wait_timed(&b_empty[s], ph ^ 1u, pw_b))) {
-                        ok = false;
-                        break;
-                    }
-                    if (elect_one()) {
+                    if (ok) ok = mbar_wait_timed(&b_empty[s], sph ^ 1u, pw_b);
+                    if (elect_one() && ok) {
                         uint8_t *st = sB + s * stage_bytes;
                         mbar_arrive_expect_tx(&b_full[s], stage_bytes);
-                        if (stream) tma_load_2d(st, &tmA, t * kKC, (int)(ft * kBM), &b_full[s]);
+                        if (stream) tma_load_2d(st, &tmA, t * kKC, frame_row, &b_full[s]);
                         tma_load_2d(st + b_off, &tmB, t * p.bk, ct * p.bn, &b_full[s]);
+                        ++issued;
                     }
                     __syncwarp();
-                    ++bq;
+                    if (++s == (uint32_t)p.stages) {
+                        s = 0;
+                        sph ^= 1u;
+                    }
+                    if (++half == spc) {
+                        half = 0;
+                        ++kc;
+                    }
                 }
-                if (__any_sync(0xffffffffu, *abort_flag != 0)) ok = false;
+                if (ct == 0) a_issued_tiles += 1;
+                ok = __all_sync(0xffffffffu, ok) && !__any_sync(0xffffffffu, *abort_flag != 0);
             }
         }
+        issued = __shfl_sync(0xffffffffu, issued, 0);  // lane 0 is the elected lane of a full warp
         if (!ok && lane == 0) {
             atomicOr(p.err, (uint32_t)kDevTimeoutTma);
             *abort_flag = 1;
@@ -586,14 +593,16 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
             atomicAdd(&p.wait_cycles[kWaitProdB], w_b);
             atomicAdd(&p.wait_cycles[kWaitProdA], w_a);
         }
-        // Drain: every load issued above has landed before the CTA exits.
-        if (t_local > 0 || bq > 0) {
-            const uint32_t last_a = (t_local - 1u) & 1u;
-            for (int kc = 0; kc < nab && t_local > 0; ++kc) mbar_wait(&a_full[kc], last_a);
-            for (uint32_t s = 0; s < (uint32_t)p.stages && s < bq; ++s) {
-                const uint32_t last_q = bq - 1u - ((bq - 1u - s) % p.stages);
-                mbar_wait(&b_full[s], (last_q / p.stages) & 1u);
-            }
+        // Drain: every load issued above has landed before the CTA exits
+        // (the A chunks of the last frame tile whose loads were issued, and
+        // the last issued load of every B stage).
+        if (a_issued_tiles > 0) {
+            const uint32_t last_a = (a_issued_tiles - 1u) & 1u;
+            for (int kc = 0; kc < nab; ++kc) mbar_wait(&a_full[kc], last_a);
+        }
+        for (uint32_t st = 0; st < (uint32_t)p.stages && st < issued; ++st) {
+            const uint32_t last_q = issued - 1u - ((issued - 1u - st) % p.stages);
+            mbar_wait(&b_full[st], (last_q / p.stages) & 1u);
         }
         __syncwarp();
     } else if (warp == 1) {
@@ -610,47 +619,48 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
         unsigned long long *pw_b = (p.wait_cycles && lane == 0) ? &w_b : nullptr;
         unsigned long long *pw_a = (p.wait_cycles && lane == 0) ? &w_a : nullptr;
         unsigned long long *pw_acc = (p.wait_cycles && lane == 0) ? &w_acc : nullptr;
+        // Stage index and phase advance incrementally (no divisions in the
+        // loop); a failed wait clears ok and stops the issues (the elected
+        // lane, lane 0 of the converged warp, decides by its own wait), and
+        // the warp agrees on ok once per center tile.
+        const bool wide_b = p.bk == kKC;
+        uint32_t s = 0, sph = 0;  // B stage and its phase
         for (int64_t ft = blockIdx.x; ft < n_ftiles && ok; ft += gridDim.x, ++t_local) {
             for (int ct = 0; ct < p.n_ctiles && ok; ++ct) {
                 const uint32_t buf = accq & 1u;
-                if (!__all_sync(0xffffffffu, mbar_wait_timed(&acc_empty[buf], ((accq >> 1) & 1u) ^ 1u, pw_acc))) {
-                    ok = false;
-                    break;
-                }
+                ok = mbar_wait_timed(&acc_empty[buf], ((accq >> 1) & 1u) ^ 1u, pw_acc);
                 tc_fence_after();
                 const uint32_t d_tmem = tmem_base + buf * (uint32_t)p.bn;
+                int kc = 0, half = 0;
                 for (int t = 0; t < p.nbst; ++t) {
-                    const int kc = t / spc;
-                    const int half = t % spc;
-                    if (!stream && ct == 0 && half == 0 &&
-                        !__all_sync(0xffffffffu, mbar_wait_timed(&a_full[kc], t_local & 1u, pw_a))) {
-                        ok = false;
-                        break;
-                    }
-                    const uint32_t s = bq % p.stages;
-                    if (!__all_sync(0xffffffffu, mbar_wait_timed(&b_full[s], (bq / p.stages) & 1u, pw_b))) {
-                        ok = false;
-                        break;
-                    }
+                    if (!stream && ct == 0 && half == 0 && ok) ok = mbar_wait_timed(&a_full[kc], t_local & 1u, pw_a);
+                    if (ok) ok = mbar_wait_timed(&b_full[s], sph, pw_b);
                     // TMA completion on the mbarrier orders the loaded tiles before
                     // the MMAs; no tcgen05 fence is needed here.
                     const int steps = min(spt, p.ksteps_total - spt * t);
                     const uint32_t st0 = sb0 + s * stage_bytes;
-                    const uint64_t ad = stream ? sw128_desc(st0)
-                                               : adesc0 + (uint64_t)((kc * kABytesPerChunk + half * p.bk * 2) >> 4);
-                    const uint32_t b0 = st0 + b_off;
-                    const uint64_t bd = p.bk == kKC ? sw128_desc(b0) : sw64_desc(b0);
-                    if (elect_one()) {
+                    const uint64_t a_d =
+                        stream ? sw128_desc(st0) : adesc0 + (uint64_t)((kc * kABytesPerChunk + half * p.bk * 2) >> 4);
+                    const uint64_t bd = wide_b ? sw128_desc(st0 + b_off) : sw64_desc(st0 + b_off);
+                    if (elect_one() && ok) {
 #pragma unroll
                         for (int kk = 0; kk < 4; ++kk)  // 32-byte K steps: +2 in the start-address field
-                            if (kk < steps) mma_f16(d_tmem, ad + 2 * kk, bd + 2 * kk, idesc, (t | kk) != 0);
+                            if (kk < steps) mma_f16(d_tmem, a_d + 2 * kk, bd + 2 * kk, idesc, (t | kk) != 0);
                         mma_commit(&b_empty[s]);
                         if (!stream && ct == p.n_ctiles - 1 && (half == spc - 1 || t == p.nbst - 1))
                             mma_commit(&a_empty[kc]);
                     }
                     __syncwarp();
-                    ++bq;
+                    if (++s == (uint32_t)p.stages) {
+                        s = 0;
+                        sph ^= 1u;
+                    }
+                    if (++half == spc) {
+                        half = 0;
+                        ++kc;
+                    }
                 }
+                ok = __all_sync(0xffffffffu, ok);
                 if (!ok) break;
                 if (elect_one()) mma_commit(&acc_full[buf]);
                 __syncwarp();
@@ -747,18 +757,35 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                             best_id = j0 + bc;
                             thr = window_threshold(best, xn.x, inv_s2, s2, Emax, Rmax, p.g_lo, p.g_hi);
                         }
+                        // Columns at or above the threshold as a bit mask; each
+                        // one is then picked out of the registers by a select
+                        // tree over the bits of its index and pushed on the list.
+                        unsigned msk = 0;
 #pragma unroll
-                        for (int c = 0; c < 32; ++c) {
-                            if (v[c] >= thr) {
-                                if (lid[kL - 1] >= 0 && la[kL - 1] >= thr) ovf = true;
+                        for (int c = 0; c < 32; ++c) msk |= (v[c] >= thr ? 1u : 0u) << c;
+                        const int nv = p.k - j0;
+                        if (nv < 32) msk &= nv > 0 ? (1u << nv) - 1u : 0u;
+                        while (msk) {
+                            const int c = __ffs(msk) - 1;
+                            msk &= msk - 1u;
+                            float t16[16], t8[8], t4[4], t2[2];
 #pragma unroll
-                                for (int m = kL - 1; m > 0; --m) {
-                                    la[m] = la[m - 1];
-                                    lid[m] = lid[m - 1];
-                                }
-                                la[0] = v[c];
-                                lid[0] = j0 + c;
+                            for (int q = 0; q < 16; ++q) t16[q] = (c & 16) ? v[q + 16] : v[q];
+#pragma unroll
+                            for (int q = 0; q < 8; ++q) t8[q] = (c & 8) ? t16[q + 8] : t16[q];
+#pragma unroll
+                            for (int q = 0; q < 4; ++q) t4[q] = (c & 4) ? t8[q + 4] : t8[q];
+#pragma unroll
+                            for (int q = 0; q < 2; ++q) t2[q] = (c & 2) ? t4[q + 2] : t4[q];
+                            const float vc = (c & 1) ? t2[1] : t2[0];
+                            if (lid[kL - 1] >= 0 && la[kL - 1] >= thr) ovf = true;
+#pragma unroll
+                            for (int m = kL - 1; m > 0; --m) {
+                                la[m] = la[m - 1];
+                                lid[m] = lid[m - 1];
                             }
+                            la[0] = vc;
+                            lid[0] = j0 + c;
                         }
                     }
                 }
