@@ -199,6 +199,177 @@ __global__ void __launch_bounds__(256) seg_accumulate_wide_kernel(
     }
 }
 
+// ---------------------------------------------------------------------------
+// Row gathers through 1-D bulk copies (TMA).  The random row reads of the
+// sorted walk are latency bound: a warp that loads a row into registers has
+// one row in flight.  Here each warp keeps kRing rows in flight in a ring of
+// shared-memory row buffers filled by cp.async.bulk (no registers held), and
+// reads the features from shared memory.  Needs rows of 16-byte multiples
+// (d % 4 == 0) and a 16-byte aligned X.
+// ---------------------------------------------------------------------------
+constexpr int kRing = 4;
+constexpr int kBulkWarps = 8;
+
+__device__ __forceinline__ uint32_t sh_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void ring_bar_init(uint64_t *b) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(sh_addr(b)) : "memory");
+}
+
+__device__ __forceinline__ bool ring_bar_try(uint64_t *b, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(sh_addr(b)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait (kWaitLimitNs); false when it gave up.
+__device__ __forceinline__ bool ring_bar_wait(uint64_t *b, uint32_t parity) {
+    if (ring_bar_try(b, parity)) return true;
+    const uint64_t t0 = globaltimer_ns();
+    for (uint32_t spin = 1;; ++spin) {
+        if (ring_bar_try(b, parity)) return true;
+        if ((spin & 255u) == 0 && globaltimer_ns() - t0 > kWaitLimitNs) return false;
+    }
+}
+
+// One row into a ring slot; the slot's barrier completes when it has landed.
+__device__ __forceinline__ void ring_fetch(void *dst, const void *src, uint32_t bytes, uint64_t *b) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(sh_addr(b)), "r"(bytes) : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     sh_addr(dst)),
+                 "l"(src), "r"(bytes), "r"(sh_addr(b))
+                 : "memory");
+}
+
+// Ring rows hold MW*32 floats (zero beyond d), so the inner loop needs no
+// bounds test.
+size_t bulk_smem_bytes(int mw) { return (size_t)kBulkWarps * ((size_t)kRing * mw * 128 + 2 * kPiece * 4 + kRing * 8); }
+
+template <int MW>
+__global__ void __launch_bounds__(kBulkWarps * 32, (MW > 17 ? 1 : 2)) seg_accumulate_bulk_kernel(
+    const float *__restrict__ X, int d, const int32_t *__restrict__ perm, const int32_t *__restrict__ slab,
+    int64_t n_max, const int32_t *__restrict__ n_sorted, const float *__restrict__ C_old, double *__restrict__ S,
+    double *__restrict__ Q, uint32_t *err) {
+    extern __shared__ __align__(16) unsigned char smem_bulk[];
+    constexpr int RS = MW * 32;  // ring row stride (floats)
+    const int warp = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+    const uint32_t row_bytes = (uint32_t)d * 4u;
+    unsigned char *wbase = smem_bulk + (size_t)warp * ((size_t)kRing * RS * 4 + 2 * kPiece * 4 + kRing * 8);
+    float *ring = reinterpret_cast<float *>(wbase);
+    int32_t *pidx = reinterpret_cast<int32_t *>(wbase + (size_t)kRing * RS * 4);
+    int32_t *plab = pidx + kPiece;
+    uint64_t *bars = reinterpret_cast<uint64_t *>(plab + kPiece);
+    for (int e = lane; e < kRing * RS; e += 32) ring[e] = 0.0f;  // the tails beyond d stay zero
+    if (lane == 0) {
+        for (int r = 0; r < kRing; ++r) ring_bar_init(&bars[r]);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncwarp();
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    uint32_t phase = 0;  // bit r: parity of the next completion of bars[r]
+    bool ok = true;
+
+    const int64_t n = min(n_max, (int64_t)*n_sorted);
+    const int64_t gwarp = (int64_t)blockIdx.x * kBulkWarps + warp;
+    const int64_t nwarps = (int64_t)gridDim.x * kBulkWarps;
+    const int64_t npieces = (n + kPiece - 1) / kPiece;
+    for (int64_t piece = gwarp; piece < npieces && ok; piece += nwarps) {
+        const int64_t p0 = piece * kPiece;
+        const int cnt = (int)min((int64_t)kPiece, n - p0);
+        for (int q = lane; q < cnt; q += 32) {
+            pidx[q] = perm[p0 + q];
+            plab[q] = slab[p0 + q];
+        }
+        __syncwarp();
+        int issued = 0;
+        auto issue = [&](int q) {  // the whole warp calls; lane 0 issues
+            if (lane == 0) {
+                const int slot = q & (kRing - 1);
+                ring_fetch(ring + (size_t)slot * RS, X + (int64_t)pidx[q] * d, row_bytes, &bars[slot]);
+            }
+            ++issued;
+        };
+        for (int q = 0; q < cnt && q < kRing; ++q) issue(q);
+
+        // Per feature a Kahan sum (ks, kc: the sum is ks - kc); per row the
+        // squared deviations of the lane's features in two FMA chains, added
+        // to a compensated row total.
+        float ks[MW], kc[MW], cold[MW];
+        CSum qacc;
+        int cur = -1;
+        auto flush = [&]() {
+#pragma unroll
+            for (int m = 0; m < MW; ++m) {
+                const int f = lane + 32 * m;
+                if (f < d) atomicAdd(&S[(int64_t)cur * d + f], (double)ks[m] - (double)kc[m]);
+            }
+            double qq = qacc.value();
+            for (int off = 16; off > 0; off >>= 1) qq += __shfl_xor_sync(0xffffffffu, qq, off);
+            if (lane == 0) atomicAdd(&Q[cur], qq);
+        };
+        int q = 0;
+        for (; q < cnt; ++q) {
+            const int slot = q & (kRing - 1);
+            ok = __all_sync(0xffffffffu, ring_bar_wait(&bars[slot], (phase >> slot) & 1u));
+            if (!ok) break;
+            phase ^= 1u << slot;
+            const int l = plab[q];
+            if (l != cur) {
+                if (cur >= 0) flush();
+                cur = l;
+                qacc.reset();
+#pragma unroll
+                for (int m = 0; m < MW; ++m) {
+                    const int f = lane + 32 * m;
+                    ks[m] = 0.0f;
+                    kc[m] = 0.0f;
+                    cold[m] = f < d ? __ldg(C_old + (int64_t)l * d + f) : 0.0f;
+                }
+            }
+            const float *row = ring + (size_t)slot * RS;
+            float q0 = 0.0f, q1 = 0.0f;
+#pragma unroll
+            for (int m = 0; m < MW; ++m) {
+                const float t = __fsub_rn(row[lane + 32 * m], cold[m]);  // zero beyond d
+                const float y = __fsub_rn(t, kc[m]);
+                const float sn = __fadd_rn(ks[m], y);
+                kc[m] = __fsub_rn(__fsub_rn(sn, ks[m]), y);
+                ks[m] = sn;
+                if (m & 1)
+                    q1 = __fmaf_rn(t, t, q1);
+                else
+                    q0 = __fmaf_rn(t, t, q0);
+            }
+            qacc.add(q0 + q1);
+            __syncwarp();
+            if (q + kRing < cnt) {
+                // The slot's shared-memory reads above come before the copy
+                // that overwrites it.
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                issue(q + kRing);
+            }
+        }
+        if (cur >= 0 && ok) flush();
+        if (!ok) {
+            // Let the copies still in flight land before the CTA exits.
+            for (int r = q; r < issued; ++r) {
+                const int slot = r & (kRing - 1);
+                ring_bar_wait(&bars[slot], (phase >> slot) & 1u);
+                phase ^= 1u << slot;
+            }
+            if (lane == 0) atomicOr(err, (uint32_t)kDevTimeoutTma);
+        }
+        __syncwarp();
+    }
+}
+
 // d < 32: the warp is split into 32/DP row slots of DP lanes (DP = next
 // power of two >= d); slot s walks positions p0+s, p0+s+R, ...
 template <int DP>
@@ -325,6 +496,50 @@ bool try_wide(int mw, const float *X, int64_t n, int d, const UpdateWs &u, int k
     return true;
 }
 
+template <int MW>
+int launch_bulk(const float *X, int64_t n, int d, const UpdateWs &u, int k, const float *C_old, uint32_t *err,
+                cudaStream_t s) {
+    const size_t smem = bulk_smem_bytes(MW);
+    static int per_sm = -1;  // cached: no attribute calls while a stream is being captured
+    if (per_sm < 0) {
+        KM_CUDA(cudaFuncSetAttribute(seg_accumulate_bulk_kernel<MW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)(232448)));
+        int v = 0;
+        KM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, seg_accumulate_bulk_kernel<MW>, kBulkWarps * 32,
+                                                              smem));
+        per_sm = v > 0 ? v : 1;
+    }
+    const int64_t npieces = (n + kPiece - 1) / kPiece;
+    int64_t g = (npieces + kBulkWarps - 1) / kBulkWarps;
+    const int64_t cap = (int64_t)num_sms() * per_sm;
+    if (g > cap) g = cap;
+    seg_accumulate_bulk_kernel<MW><<<(unsigned)(g < 1 ? 1 : g), kBulkWarps * 32, smem, s>>>(
+        X, d, u.perm, u.slab, n, u.offsets + k, C_old, u.S, u.Q, err);
+    KM_CUDA(cudaGetLastError());
+    return KM_OK;
+}
+
+int launch_segments_bulk(const float *X, int64_t n, int d, const UpdateWs &u, int k, const float *C_old,
+                         uint32_t *err, cudaStream_t s) {
+    const int mw = (d + 31) / 32;
+    switch (mw) {
+        case 1: return launch_bulk<1>(X, n, d, u, k, C_old, err, s);
+        case 2: return launch_bulk<2>(X, n, d, u, k, C_old, err, s);
+        case 3: return launch_bulk<3>(X, n, d, u, k, C_old, err, s);
+        case 4: return launch_bulk<4>(X, n, d, u, k, C_old, err, s);
+        case 5: case 6: return launch_bulk<6>(X, n, d, u, k, C_old, err, s);
+        case 7: case 8: return launch_bulk<8>(X, n, d, u, k, C_old, err, s);
+        case 9: case 10: case 11: case 12: return launch_bulk<12>(X, n, d, u, k, C_old, err, s);
+        case 13: case 14: case 15: case 16: case 17: return launch_bulk<17>(X, n, d, u, k, C_old, err, s);
+        case 18: case 19: case 20: case 21: case 22: case 23: case 24: return launch_bulk<24>(X, n, d, u, k, C_old, err, s);
+        default: return launch_bulk<32>(X, n, d, u, k, C_old, err, s);
+    }
+}
+
+bool bulk_ok(const float *X, int d) {
+    return d >= 32 && d <= 1024 && (d % 4) == 0 && (reinterpret_cast<uintptr_t>(X) % 16) == 0;
+}
+
 int launch_segments(const float *X, int64_t n, int d, const UpdateWs &u, int k, const float *C_old, unsigned g,
                     cudaStream_t s) {
     if (d >= 32) {
@@ -376,9 +591,13 @@ int launch_update(const float *X, int64_t n, int d, const int32_t *labels, int k
     if (n > 0) {
         scatter_kernel<<<grid_for(n, 256, 8), 256, 0, s>>>(labels, n, k, u.cursor, u.perm, u.slab);
         KM_CUDA(cudaGetLastError());
-        const int64_t npieces = (n + kPiece - 1) / kPiece;
-        const unsigned g = grid_for(npieces * 32, 256, 8);
-        KM_TRY(launch_segments(X, n, d, u, k, C_old, g, s));
+        if (bulk_ok(X, d)) {
+            KM_TRY(launch_segments_bulk(X, n, d, u, k, C_old, err, s));
+        } else {
+            const int64_t npieces = (n + kPiece - 1) / kPiece;
+            const unsigned g = grid_for(npieces * 32, 256, 8);
+            KM_TRY(launch_segments(X, n, d, u, k, C_old, g, s));
+        }
     }
     finalize_kernel<<<(unsigned)(((int64_t)k * 32 + 255) / 256), 256, 0, s>>>(
         u.S, u.Q, u.counts, C_old, C_new, d, k, u.ccost, counts_out);
