@@ -73,7 +73,7 @@ size_t tc_frames_ws_size(int64_t n, int d);     // fp16 frame copy + norms
 size_t tc_centers_ws_size(int d, int k);        // fp16 centers + norms + shift + scalars
 size_t tc_assign_ws_size(int64_t n, int d, int k);  // candidate lists + counters
 
-#define TC_CANDIDATES 8  // candidate centers kept per frame by the tensor-core pass
+#define TC_CANDIDATES 16  // candidate centers kept per frame by the tensor-core pass
 
 struct TcBuffers {
     // frames

@@ -81,14 +81,15 @@ def test_duplicate_centers_ties(torch, L, oracle, prec):
 
 
 def test_full_recheck_across_center_blocks(torch, L, oracle):
-    # Groups of 12 nearly equal centers overflow the candidate list of the
-    # tensor-core pass; the exact copies of each group sit 256+ indexes apart,
-    # so the exact re-check must pick the lowest index across center blocks.
+    # Groups of 26 nearly equal centers overflow the candidate list of the
+    # tensor-core pass (at most 16 entries); the exact copies of each group sit
+    # 256+ indexes apart, so the exact re-check must pick the lowest index
+    # across center blocks.
     rng = np.random.default_rng(21)
     d, groups = 96, 90
     base = rng.normal(size=(groups, d)).astype(np.float32)
-    near = [base + 1e-4 * rng.normal(size=base.shape).astype(np.float32) for _ in range(11)]
-    C = np.concatenate([base] + near + [base]).astype(np.float32)  # k = 13 * 90 = 1170
+    near = [base + 1e-4 * rng.normal(size=base.shape).astype(np.float32) for _ in range(24)]
+    C = np.concatenate([base] + near + [base]).astype(np.float32)  # k = 26 * 90 = 2340
     X = np.concatenate([base + 1e-3 * rng.normal(size=base.shape).astype(np.float32) for _ in range(30)])
     X = np.concatenate([X, base]).astype(np.float32)
     got, stats = gpu_assign(torch, L, X, C, "fp16")
