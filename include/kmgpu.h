@@ -71,6 +71,7 @@ typedef struct {
     int64_t n_flipped;  /* frames whose exact label differs from the tensor-core argmin */
     int32_t precision;  /* precision actually used (km_precision) */
     int32_t reserved;
+    int64_t n_pairs;    /* (frame, candidate center) pairs listed for the exact re-check */
 } km_assign_stats;
 
 int km_version(void);

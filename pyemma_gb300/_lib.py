@@ -49,11 +49,12 @@ class KmError(RuntimeError):
 class AssignStats(ctypes.Structure):
     _fields_ = [("n_frames", ctypes.c_int64), ("n_recheck", ctypes.c_int64),
                 ("n_full", ctypes.c_int64), ("n_flipped", ctypes.c_int64),
-                ("precision", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+                ("precision", ctypes.c_int32), ("reserved", ctypes.c_int32), ("n_pairs", ctypes.c_int64)]
 
     def as_dict(self):
         return dict(n_frames=self.n_frames, n_recheck=self.n_recheck, n_full=self.n_full,
-                    n_flipped=self.n_flipped, precision=PRECISION_NAMES.get(self.precision, "?"))
+                    n_flipped=self.n_flipped, n_pairs=self.n_pairs,
+                    precision=PRECISION_NAMES.get(self.precision, "?"))
 
 
 CALLBACK = ctypes.CFUNCTYPE(None, ctypes.c_void_p)

@@ -149,13 +149,34 @@ int launch_cfg(const float *X, const int32_t *frame_idx, const int32_t *n_dev, i
     return KM_OK;
 }
 
-// Kernel (b'): exact float32 distance of every (entry, candidate) pair, one
-// thread per pair.  The key (distance bits << 32 | center) of a non-negative
-// float orders lexicographically as an unsigned integer, so atomicMin keeps
-// the smallest distance and, among equal distances, the lowest center.
-__global__ void __launch_bounds__(256) recheck_pairs_kernel(
+// Kernel (b'): exact float32 distances of the candidates of re-checked frames.
+// A key (distance bits << 32 | center) of a non-negative float orders
+// lexicographically as an unsigned integer, so atomicMin keeps the smallest
+// distance and, among equal distances, the lowest center.
+//
+// Phase 1 evaluates, for every entry, the candidate with the smallest
+// tensor-core distance.  Phase 2 evaluates the other candidates whose lower
+// bound does not exceed that exact distance (the rest can neither win nor
+// tie).  One thread per evaluation, sqdist_exact over the two rows: the many
+// independent 16-byte loads of each thread keep the memory system busy.
+__global__ void __launch_bounds__(256) recheck_best_kernel(
     const float *__restrict__ X, int d, const float *__restrict__ C, const int32_t *__restrict__ rc_frames,
-    const int32_t *__restrict__ pair_entry, const int32_t *__restrict__ pair_center,
+    const int32_t *__restrict__ rc_best, const int32_t *__restrict__ entry_count, int64_t max_entries,
+    unsigned long long *__restrict__ keys) {
+    int64_t count = *entry_count;
+    if (count > max_entries) count = max_entries;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < count;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int j = rc_best[e];
+        const float dd = sqdist_exact(X + (int64_t)rc_frames[e] * d, C + (int64_t)j * d, d);
+        keys[e] = ((unsigned long long)__float_as_uint(dd) << 32) | (unsigned)j;
+    }
+}
+
+__global__ void __launch_bounds__(256) recheck_rest_kernel(
+    const float *__restrict__ X, int d, const float *__restrict__ C, const int32_t *__restrict__ rc_frames,
+    const int32_t *__restrict__ rc_best, const int32_t *__restrict__ pair_entry,
+    const int32_t *__restrict__ pair_center, const float *__restrict__ pair_lo,
     const int32_t *__restrict__ pair_count, int64_t max_pairs, unsigned long long *__restrict__ keys) {
     int64_t count = *pair_count;
     if (count > max_pairs) count = max_pairs;
@@ -163,10 +184,11 @@ __global__ void __launch_bounds__(256) recheck_pairs_kernel(
          q += (int64_t)gridDim.x * blockDim.x) {
         const int e = pair_entry[q];
         const int j = pair_center[q];
-        const int64_t frame = rc_frames[e];
-        const float dd = sqdist_exact(X + frame * d, C + (int64_t)j * d, d);
-        const unsigned long long key = ((unsigned long long)__float_as_uint(dd) << 32) | (unsigned)j;
-        atomicMin(&keys[e], key);
+        if (j == rc_best[e]) continue;
+        const float dstar = __uint_as_float((uint32_t)(keys[e] >> 32));
+        if (pair_lo[q] > dstar) continue;  // false for NaN: evaluated
+        const float dd = sqdist_exact(X + (int64_t)rc_frames[e] * d, C + (int64_t)j * d, d);
+        atomicMin(&keys[e], ((unsigned long long)__float_as_uint(dd) << 32) | (unsigned)j);
     }
 }
 
@@ -203,16 +225,21 @@ int launch_assign_fp32(const float *X, const int32_t *frame_idx, const int32_t *
     return launch_cfg<4, 8>(X, frame_idx, n_dev, n, d, C, k, labels, dist, flipped, s);
 }
 
-int launch_recheck_pairs(const float *X, int d, const float *C, const int32_t *rc_frames,
-                         const int32_t *pair_entry, const int32_t *pair_center, unsigned long long *keys,
-                         const int32_t *counters, int64_t max_entries, int64_t max_pairs, int32_t *labels,
-                         unsigned long long *flipped, cudaStream_t s) {
+int launch_recheck_pairs(const float *X, int d, const float *C, const int32_t *rc_frames, const int32_t *rc_best,
+                         const int32_t *pair_entry, const int32_t *pair_center, const float *pair_lo,
+                         unsigned long long *keys, const int32_t *counters, int64_t max_entries, int64_t max_pairs,
+                         int32_t *labels, unsigned long long *flipped, cudaStream_t s) {
     if (max_entries == 0) return KM_OK;
     const int64_t cap = (int64_t)num_sms() * 8;
+    int64_t g0 = (max_entries + 255) / 256;
+    if (g0 > cap) g0 = cap;
+    recheck_best_kernel<<<(unsigned)(g0 < 1 ? 1 : g0), 256, 0, s>>>(X, d, C, rc_frames, rc_best, counters,
+                                                                  max_entries, keys);
+    KM_CUDA(cudaGetLastError());
     int64_t g1 = (max_pairs + 255) / 256;
     if (g1 > cap) g1 = cap;
-    recheck_pairs_kernel<<<(unsigned)(g1 < 1 ? 1 : g1), 256, 0, s>>>(X, d, C, rc_frames, pair_entry, pair_center,
-                                                                    counters + 2, max_pairs, keys);
+    recheck_rest_kernel<<<(unsigned)(g1 < 1 ? 1 : g1), 256, 0, s>>>(X, d, C, rc_frames, rc_best, pair_entry,
+                                                                  pair_center, pair_lo, counters + 2, max_pairs, keys);
     KM_CUDA(cudaGetLastError());
     int64_t g2 = (max_entries + 255) / 256;
     if (g2 > cap) g2 = cap;

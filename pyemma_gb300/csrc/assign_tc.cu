@@ -97,6 +97,8 @@ struct TcParams {
     int32_t *pair_entry;
     int32_t *pair_center;
     unsigned long long *rc_keys;
+    int32_t *rc_best;
+    float *pair_lo;
     int32_t *full_frames;
     unsigned long long *full_keys;
     int32_t *counters;
@@ -799,6 +801,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
             // ---- decision ----
             bool need_rc = false, need_full = false;
             unsigned cmask = 0;  // bit m: list entry m is a candidate
+            float lo[kL];        // lower bounds of the candidates' exact distances
             if (i < p.n) {
                 float vv[kL], RR[kL], EE[kL];
                 float H = kInf;
@@ -821,8 +824,10 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                     need_full = true;
                 } else {
 #pragma unroll
-                    for (int m = 0; m < kL; ++m)
-                        if (vv[m] < kInf && lo_bound(vv[m], EE[m], RR[m], p.g_lo) <= H) cmask |= 1u << m;
+                    for (int m = 0; m < kL; ++m) {
+                        lo[m] = vv[m] < kInf ? lo_bound(vv[m], EE[m], RR[m], p.g_lo) : kInf;
+                        if (lo[m] <= H) cmask |= 1u << m;
+                    }
                     const int nc = __popc(cmask);
                     if (nc == 0) need_full = true;
                     else if (nc > 1) need_rc = true;
@@ -858,7 +863,20 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                 pbase = __shfl_sync(0xffffffffu, pbase, leader);
                 if (need_rc) {
                     const int e = base + __popc(m_rc & ((1u << lane) - 1u));
+                    // The candidate with the largest accumulator (smallest
+                    // approximate distance) is evaluated first; the others are
+                    // evaluated only if their lower bound does not exceed it.
+                    float vb = kNegInf;
+                    int jb = 0;
+#pragma unroll
+                    for (int m = 0; m < kL; ++m) {
+                        if (((cmask >> m) & 1u) && la[m] > vb) {
+                            vb = la[m];
+                            jb = lid[m];
+                        }
+                    }
                     p.rc_frames[e] = (int32_t)i;
+                    p.rc_best[e] = jb;
                     p.rc_keys[e] = ~0ull;
 #pragma unroll
                     for (int m = 0; m < kL; ++m) {
@@ -866,6 +884,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                             const int q = pbase + excl + __popc(cmask & ((1u << m) - 1u));
                             p.pair_entry[q] = e;
                             p.pair_center[q] = lid[m];
+                            p.pair_lo[q] = lo[m];
                         }
                     }
                 }
@@ -1076,6 +1095,8 @@ size_t carve_assign(void *ws, int64_t n, TcBuffers &b) {
     b.pair_entry = c.take<int32_t>(nn * kL);
     b.pair_center = c.take<int32_t>(nn * kL);
     b.rc_keys = c.take<unsigned long long>(nn);
+    b.rc_best = c.take<int32_t>(nn);
+    b.pair_lo = c.take<float>(nn * kL);
     b.full_frames = c.take<int32_t>(nn);
     b.full_keys = c.take<unsigned long long>(nn);
     b.counters = c.take<int32_t>(20);  // [0] recheck entries, [1] full entries, [2] pairs, [4..20) diagnostics
@@ -1181,6 +1202,8 @@ int tc_assign(const float *X, int64_t n, int d, const float *C, int k, int32_t *
     p.pair_entry = b.pair_entry;
     p.pair_center = b.pair_center;
     p.rc_keys = b.rc_keys;
+    p.rc_best = b.rc_best;
+    p.pair_lo = b.pair_lo;
     p.full_frames = b.full_frames;
     p.full_keys = b.full_keys;
     p.counters = b.counters;
@@ -1197,8 +1220,8 @@ int tc_assign(const float *X, int64_t n, int d, const float *C, int k, int32_t *
     if (prof) prof->end(kProfTc, s);
 
     if (prof) prof->begin(kProfRecheck, s);
-    KM_TRY(launch_recheck_pairs(X, d, C, b.rc_frames, b.pair_entry, b.pair_center, b.rc_keys, b.counters, n,
-                                n * kL, labels, b.flipped, s));
+    KM_TRY(launch_recheck_pairs(X, d, C, b.rc_frames, b.rc_best, b.pair_entry, b.pair_center, b.pair_lo, b.rc_keys,
+                                b.counters, n, n * kL, labels, b.flipped, s));
     if (prof) prof->end(kProfRecheck, s);
     if (prof) prof->begin(kProfFull, s);
     KM_TRY(launch_full_recheck(X, b.full_frames, b.counters + 1, n, d, C, k, b.full_keys, labels, b.flipped, s));

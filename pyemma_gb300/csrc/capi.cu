@@ -163,7 +163,7 @@ int assign_core(const float *X, int64_t n, int32_t d, const float *C, int32_t k,
         prof.collect();
     }
     if (stats) {
-        int32_t cnt[2];
+        int32_t cnt[3];
         unsigned long long flips = 0;
         uint32_t err = 0;
         KM_CUDA(cudaMemcpyAsync(cnt, b.counters, sizeof(cnt), cudaMemcpyDeviceToHost, s));
@@ -172,6 +172,7 @@ int assign_core(const float *X, int64_t n, int32_t d, const float *C, int32_t k,
         KM_CUDA(cudaStreamSynchronize(s));
         stats->n_recheck = cnt[0];
         stats->n_full = cnt[1];
+        stats->n_pairs = cnt[2];
         stats->n_flipped = (int64_t)flips;
         KM_TRY(check_device_errors(err));
     }

@@ -47,10 +47,10 @@ int launch_full_recheck(const float *X, const int32_t *frames, const int32_t *n_
                         const float *C, int k, unsigned long long *keys, int32_t *labels,
                         unsigned long long *flipped, cudaStream_t s);
 
-int launch_recheck_pairs(const float *X, int d, const float *C, const int32_t *rc_frames,
-                         const int32_t *pair_entry, const int32_t *pair_center, unsigned long long *keys,
-                         const int32_t *counters, int64_t max_entries, int64_t max_pairs, int32_t *labels,
-                         unsigned long long *flipped, cudaStream_t s);
+int launch_recheck_pairs(const float *X, int d, const float *C, const int32_t *rc_frames, const int32_t *rc_best,
+                         const int32_t *pair_entry, const int32_t *pair_center, const float *pair_lo,
+                         unsigned long long *keys, const int32_t *counters, int64_t max_entries, int64_t max_pairs,
+                         int32_t *labels, unsigned long long *flipped, cudaStream_t s);
 
 // ---- update.cu -------------------------------------------------------------
 size_t update_ws_size(int64_t n, int d, int k);
@@ -89,6 +89,8 @@ struct TcBuffers {
     int32_t *pair_entry = nullptr;          // pair -> entry
     int32_t *pair_center = nullptr;         // pair -> candidate center
     unsigned long long *rc_keys = nullptr;  // entry -> (distance bits, center) minimum
+    int32_t *rc_best = nullptr;             // entry -> candidate with the smallest tensor-core distance
+    float *pair_lo = nullptr;               // pair -> lower bound of the candidate's exact distance
     int32_t *full_frames = nullptr;
     unsigned long long *full_keys = nullptr;
     int32_t *counters = nullptr;  // [0] recheck entries, [1] full entries, [2] pairs
