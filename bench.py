@@ -366,7 +366,9 @@ def run_ours(args):
         dist.destroy_process_group()
     if rank != 0:
         return
-    launches_per_step = 12  # prep_centers, tc, 2 pair-recheck kernels, 2 full-recheck kernels, 6 update kernels
+    # prep_centers, tc_assign, 3 candidate re-check kernels, 2 full re-check
+    # kernels, 6 centroid-update kernels
+    launches_per_step = 13
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "fp16 distances (fp32 accumulate), fp32 recheck, f64 sums",

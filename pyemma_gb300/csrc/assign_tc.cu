@@ -291,6 +291,23 @@ __global__ void shift_mean_kernel(const float *__restrict__ C, int d, int k, flo
     shift[f] = (float)(s / k);
 }
 
+// Warp sum of per-lane compensated sums (s + c) in float32 (double-float
+// style: TwoSum of the leading parts, errors carried in c): no float64 work,
+// which is slow on this part.  Relative error a few units of float32.
+__device__ __forceinline__ float warp_sum_ff(float s, float c) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        const float s2 = __shfl_xor_sync(0xffffffffu, s, off);
+        const float c2 = __shfl_xor_sync(0xffffffffu, c, off);
+        const float t = __fadd_rn(s, s2);
+        const float bp = __fsub_rn(t, s);
+        const float e = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(s2, bp));
+        s = t;
+        c = __fadd_rn(__fadd_rn(c, c2), e);
+    }
+    return __fadd_rn(s, c);
+}
+
 __device__ __forceinline__ double warp_sum_d(double v) {
     for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
     return v;
@@ -378,14 +395,98 @@ __global__ void prep_frames_kernel(const float *__restrict__ X, int64_t n, int d
                 e2.add(eb * eb);
             }
         }
-        const double th = warp_sum_d(h2.value());
-        const double ts = warp_sum_d(s2.value());
-        const double te = warp_sum_d(e2.value());
+        const float th = warp_sum_ff(h2.s, h2.c);
+        const float ts = warp_sum_ff(s2.s, s2.c);
+        const float te = warp_sum_ff(e2.s, e2.c);
         if (lane == 0) {
-            const float sx = __fsqrt_ru(__fmul_ru((float)ts, norm_inflate));
-            const float hx = __fmul_ru(__fadd_ru(__fsqrt_ru(__fmul_ru((float)te, norm_inflate)), 1e-30f), inv_sc);
-            xnorm[i] = make_float4((float)th, sx, hx, 0.0f);
+            const float sx = __fsqrt_ru(__fmul_ru(ts, norm_inflate));
+            const float hx = __fmul_ru(__fadd_ru(__fsqrt_ru(__fmul_ru(te, norm_inflate)), 1e-30f), inv_sc);
+            xnorm[i] = make_float4(th, sx, hx, 0.0f);
         }
+    }
+}
+
+// The same conversion with 16-byte loads (d % 4 == 0, 16-byte aligned X and
+// shift): each lane owns 4 consecutive columns of every 128-column slice, and
+// all of a row's loads are issued before any of its arithmetic, so a warp
+// keeps the whole row in flight instead of one slice at a time.
+template <int IT>  // 128-column slices per row: IT * 128 >= kp
+__global__ void __launch_bounds__(256, 2) prep_frames_v4_kernel(const float *__restrict__ X, int64_t n, int d,
+                                                                int kp, const float *__restrict__ shift,
+                                                                const uint32_t *__restrict__ scal,
+                                                                __half *__restrict__ xh, float4 *__restrict__ xnorm,
+                                                                float norm_inflate) {
+    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    const float sc = __uint_as_float(scal[kScale]);
+    const float inv_sc = 1.0f / sc;  // exact: a power of two
+    auto load_row = [&](int64_t i, float4 (&v)[IT]) {
+        const float *src = X + i * d;
+#pragma unroll
+        for (int it = 0; it < IT; ++it) {
+            const int f = 4 * lane + 128 * it;
+            v[it] = (i < n && f < d) ? __ldg(reinterpret_cast<const float4 *>(src + f)) : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+    };
+    float4 xv[IT];
+    load_row(w, xv);
+    for (int64_t i = w; i < n; i += nw) {
+        // The next row's loads are in flight while this row is converted.
+        float4 nx[IT];
+        load_row(i + nw, nx);
+        // ||x_hat||^2 enters the distance itself: a Kahan sum per lane (within
+        // about 2u of the lane's terms; the distance bound allows 8u for this
+        // norm).  The other two are bounds inflated by norm_inflate (far above
+        // the few units of rounding of a plain per-lane sum): plain float32.
+        float hs = 0.0f, hc = 0.0f;
+        float s2 = 0.0f, e2 = 0.0f;
+#pragma unroll
+        for (int it = 0; it < IT; ++it) {
+            const int f = 4 * lane + 128 * it;
+            if (f >= kp) continue;
+            const float4 s4 = f < d ? __ldg(reinterpret_cast<const float4 *>(shift + f)) : make_float4(0.f, 0.f, 0.f, 0.f);
+            const float xa[4] = {xv[it].x, xv[it].y, xv[it].z, xv[it].w};
+            const float sa[4] = {s4.x, s4.y, s4.z, s4.w};
+            float a[4], ia[4];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                // Columns < d: centered, scaled frame values; d and d+1: 1
+                // (they meet the hi/lo norm columns of the centers); the rest: 0.
+                const int c = f + e;
+                a[e] = c < d ? __fsub_rn(xa[e], sa[e]) : 0.0f;
+                ia[e] = c < d ? a[e] * sc : ((c == d || c == d + 1) ? 1.0f : 0.0f);
+            }
+            const __half2 h01 = __floats2half2_rn(ia[0], ia[1]);
+            const __half2 h23 = __floats2half2_rn(ia[2], ia[3]);
+            uint2 packed;
+            packed.x = *reinterpret_cast<const uint32_t *>(&h01);
+            packed.y = *reinterpret_cast<const uint32_t *>(&h23);
+            *reinterpret_cast<uint2 *>(xh + i * kp + f) = packed;
+            const float hv[4] = {__low2float(h01), __high2float(h01), __low2float(h23), __high2float(h23)};
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                if (f + e < d) {
+                    const float ee = hv[e] - ia[e];
+                    const float y = __fsub_rn(__fmul_rn(hv[e], hv[e]), hc);
+                    const float t = __fadd_rn(hs, y);
+                    hc = __fsub_rn(__fsub_rn(t, hs), y);
+                    hs = t;
+                    s2 = __fmaf_rn(a[e], a[e], s2);
+                    e2 = __fmaf_rn(ee, ee, e2);
+                }
+            }
+        }
+        const float th = warp_sum_ff(hs, -hc);
+        const float ts = warp_sum_ff(s2, 0.0f);
+        const float te = warp_sum_ff(e2, 0.0f);
+        if (lane == 0) {
+            const float sx = __fsqrt_ru(__fmul_ru(ts, norm_inflate));
+            const float hx = __fmul_ru(__fadd_ru(__fsqrt_ru(__fmul_ru(te, norm_inflate)), 1e-30f), inv_sc);
+            xnorm[i] = make_float4(th, sx, hx, 0.0f);
+        }
+#pragma unroll
+        for (int it = 0; it < IT; ++it) xv[it] = nx[it];
     }
 }
 
@@ -1130,11 +1231,34 @@ int tc_prepare_shift_from_centers(const float *C, int d, int k, TcBuffers &b, cu
     return KM_OK;
 }
 
+template <int IT>
+void launch_prep_v4(const float *X, int64_t n, int d, TcBuffers &b, cudaStream_t s) {
+    prep_frames_v4_kernel<IT><<<(unsigned)prep_blocks(n), 256, 0, s>>>(X, n, d, b.kp, b.shift, b.scal,
+                                                                     reinterpret_cast<__half *>(b.xh), b.xnorm,
+                                                                     norm_inflate_of(d));
+}
+
 int tc_prepare_frames(const float *X, int64_t n, int d, TcBuffers &b, cudaStream_t s) {
     if (n == 0) return KM_OK;
-    prep_frames_kernel<<<(unsigned)prep_blocks(n), 256, 0, s>>>(X, n, d, b.kp, b.shift, b.scal,
-                                                              reinterpret_cast<__half *>(b.xh), b.xnorm,
-                                                              norm_inflate_of(d));
+    const int it = (b.kp + 127) / 128;
+    const bool v4 = d % 4 == 0 && it <= 9 && ((reinterpret_cast<uintptr_t>(X) | reinterpret_cast<uintptr_t>(b.shift)) & 15) == 0;
+    if (v4) {
+        switch (it) {
+            case 1: launch_prep_v4<1>(X, n, d, b, s); break;
+            case 2: launch_prep_v4<2>(X, n, d, b, s); break;
+            case 3: launch_prep_v4<3>(X, n, d, b, s); break;
+            case 4: launch_prep_v4<4>(X, n, d, b, s); break;
+            case 5: launch_prep_v4<5>(X, n, d, b, s); break;
+            case 6: launch_prep_v4<6>(X, n, d, b, s); break;
+            case 7: launch_prep_v4<7>(X, n, d, b, s); break;
+            case 8: launch_prep_v4<8>(X, n, d, b, s); break;
+            default: launch_prep_v4<9>(X, n, d, b, s); break;
+        }
+    } else {
+        prep_frames_kernel<<<(unsigned)prep_blocks(n), 256, 0, s>>>(X, n, d, b.kp, b.shift, b.scal,
+                                                                  reinterpret_cast<__half *>(b.xh), b.xnorm,
+                                                                  norm_inflate_of(d));
+    }
     KM_CUDA(cudaGetLastError());
     return KM_OK;
 }
@@ -1190,7 +1314,7 @@ int tc_assign(const float *X, int64_t n, int d, const float *C, int k, int32_t *
     p.n_ctiles = (k + pl.bn - 1) / pl.bn;
     p.tmem_cols = pl.tmem_cols;
     const double gamma_acc = (b.kp / 16 + 1) * std::ldexp(1.0, -21);
-    p.e_coef = (float)((gamma_acc * 1.003 + std::ldexp(1.0, -21) + 4.0 * u) * 1.01);
+    p.e_coef = (float)((gamma_acc * 1.003 + std::ldexp(1.0, -21) + 8.0 * u) * 1.01);
     const double g = (d + 2) * u / (1.0 - (d + 2) * u) * 1.01;
     p.g_lo = (float)((1.0 - g) * (1.0 - 4.0 * u));
     p.g_hi = (float)((1.0 + g) * (1.0 + 4.0 * u));

@@ -31,7 +31,7 @@ def bound_terms(X, C):
     # exact norms of the FP16 rounding errors, as the prep kernels measure them
     hx = np.sqrt(((((xp * scale).astype(np.float16).astype(np.float64)) / scale - xp) ** 2).sum(1)) * (1 + 1e-6)
     hc = np.sqrt(((((cp * scale).astype(np.float16).astype(np.float64)) / scale - cp) ** 2).sum(1)) * (1 + 1e-6)
-    e_coef = ((kp // 16 + 1) * 2.0 ** -21 * 1.003 + 2.0 ** -21 + 4 * U) * 1.01
+    e_coef = ((kp // 16 + 1) * 2.0 ** -21 * 1.003 + 2.0 ** -21 + 8 * U) * 1.01
     g = (d + 2) * U / (1 - (d + 2) * U) * 1.01
     S = sx[:, None] + sc[None, :]
     R = hx[:, None] + hc[None, :] + 2.0 ** -23 * S
