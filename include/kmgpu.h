@@ -166,6 +166,22 @@ int km_lloyd(const float *X, int64_t n, int32_t d, int32_t k, float *C, int32_t 
              int32_t *n_iter, int32_t *converged, km_callback cb, void *cb_user, void *workspace,
              size_t workspace_bytes, void *stream);
 
+/* ---- precision autotuning (no counterpart in the reference) ---------------
+ * KM_PREC_AUTO picks the faster of the exact FP32 kernel and the tensor-core
+ * path by a rule measured on a d x k sweep.  km_tune measures instead: it
+ * times both on the given frames and centers (one warm-up and three timed
+ * km_assign calls each; the caller passes a representative sample) and
+ * stores the faster for this (d, k) in a process-wide table behind a mutex,
+ * which KM_PREC_AUTO consults first.  chosen, ms_fp32 and ms_fp16 (host,
+ * nullable) receive the choice and the per-call times (ms_fp16 = -1 when the
+ * tensor-core path has no kernel for the shape).  Synchronises `stream`;
+ * refuses to run while the stream is being captured.  km_tune_clear empties
+ * the table. */
+size_t km_tune_workspace_size(int64_t n, int32_t d, int32_t k);
+int km_tune(const float *X, int64_t n, int32_t d, const float *C, int32_t k, void *workspace,
+            size_t workspace_bytes, int32_t *chosen, double *ms_fp32, double *ms_fp16, void *stream);
+int km_tune_clear(void);
+
 /* ---- resident center sets: ClusterModel(centers, metric) built once -------
  * interface.py:164-165 constructs ClusterModel(cluster_centers, metric) for
  * every chunk it transforms.  A km_centers handle holds a device copy of

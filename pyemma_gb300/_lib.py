@@ -34,7 +34,7 @@ EXPORTED = (
     "km_centers_create", "km_centers_destroy", "km_centers_info", "km_assign_centers_workspace_size",
     "km_assign_centers",
     "km_serve_create", "km_serve_add_centers", "km_serve_submit", "km_serve_poll", "km_serve_stats_read",
-    "km_serve_shutdown",
+    "km_serve_shutdown", "km_tune_workspace_size", "km_tune", "km_tune_clear",
 )
 
 
@@ -142,6 +142,12 @@ def load(build_if_missing=False):
     L.km_serve_poll.argtypes = [P, ctypes.c_uint64, i32, ctypes.POINTER(RequestInfo)]
     L.km_serve_stats_read.argtypes = [P, ctypes.POINTER(ServeStats)]
     L.km_serve_shutdown.argtypes = [P]
+    L.km_tune_workspace_size.argtypes = [i64, i32, i32]
+    L.km_tune_workspace_size.restype = sz
+    L.km_tune.argtypes = [P, i64, i32, P, i32, P, sz, ctypes.POINTER(i32), ctypes.POINTER(f64),
+                          ctypes.POINTER(f64), P]
+    L.km_tune.restype = ctypes.c_int
+    L.km_tune_clear.restype = ctypes.c_int
     for name in ("km_assign", "km_batch_assign", "km_update", "km_kmpp", "km_lloyd", "km_centers_create",
                  "km_centers_destroy", "km_centers_info", "km_assign_centers", "km_serve_create",
                  "km_serve_add_centers", "km_serve_submit", "km_serve_poll", "km_serve_stats_read",
@@ -467,3 +473,26 @@ class Server(object):
             self.shutdown()
         except Exception:
             pass
+
+
+def tune(X, C):
+    """Times both precisions on X (a representative sample) against C and
+    stores the faster for (d, k); 'auto' then uses it.  Returns
+    dict(chosen, ms_fp32, ms_fp16)."""
+    torch = _torch()
+    L = load()
+    _check_frames(torch, X)
+    _check_frames(torch, C, "C")
+    n, d = X.shape
+    k = C.shape[0]
+    ws_bytes = L.km_tune_workspace_size(n, d, k)
+    ws = _workspace(torch, ws_bytes, X.device)
+    chosen, t32, t16 = ctypes.c_int32(), ctypes.c_double(), ctypes.c_double()
+    check(L.km_tune(_ptr(X), n, d, _ptr(C), k, _ptr(ws), ws_bytes, ctypes.byref(chosen), ctypes.byref(t32),
+                    ctypes.byref(t16), _stream(torch, X.device)))
+    return dict(chosen=PRECISION_NAMES[chosen.value], ms_fp32=t32.value,
+                ms_fp16=t16.value if t16.value >= 0 else None)
+
+
+def tune_clear():
+    check(load().km_tune_clear())

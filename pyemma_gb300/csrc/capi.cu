@@ -2,7 +2,9 @@
 // include/kmgpu.h).  Each one validates its arguments, carves the caller's
 // workspace and enqueues kernels on the caller's stream.
 #include <cstring>
+#include <map>
 #include <mutex>
+#include <utility>
 
 #include "km_common.cuh"
 #include "km_internal.h"
@@ -88,13 +90,26 @@ void ProfEvents::collect() {
 
 namespace {
 
+// Precisions chosen by km_tune, per (d, k).
+struct TuneCache {
+    std::mutex m;
+    std::map<std::pair<int, int>, int> choice;
+} g_tune;
+
+// KM_PREC_AUTO: a km_tune result for (d, k) if there is one, else the rule
+// measured on the precision sweep (1M frames, d 16..1024, k 100..5000): the
+// tensor-core path wins from d >= 64 at every k, and for d >= 16 once
+// k >= 1000; below that the exact FP32 kernel is as fast or faster.
 int resolve_precision(int precision, int d, int k, bool check_device) {
-    if (precision == KM_PREC_AUTO) {
-        if (d >= 64 && (check_device ? tc_supported(d, k) : tc_plan_exists(d, k)))
-            return KM_PREC_FP16;
-        return KM_PREC_FP32;
+    if (precision != KM_PREC_AUTO) return precision;
+    {
+        std::lock_guard<std::mutex> lk(g_tune.m);
+        auto it = g_tune.choice.find(std::make_pair(d, k));
+        if (it != g_tune.choice.end()) return it->second;
     }
-    return precision;
+    const bool tc_ok = check_device ? tc_supported(d, k) : tc_plan_exists(d, k);
+    if (tc_ok && (d >= 64 || (d >= 16 && k >= 1000))) return KM_PREC_FP16;
+    return KM_PREC_FP32;
 }
 
 struct AssignWs {
@@ -655,6 +670,77 @@ int km_assign_centers(const float *X, int64_t n, int32_t d, const km_centers *h,
         tc_carve_assign(p, n, d, h->k, b);
     }
     return assign_core(X, n, d, h->C, h->k, h->prec, labels, b, true, stats, static_cast<cudaStream_t>(stream));
+}
+
+// ---- precision autotuning ----------------------------------------------------
+
+size_t km_tune_workspace_size(int64_t n, int32_t d, int32_t k) {
+    if (check_shape(n, d, k) != KM_OK) return 0;
+    Carver c(nullptr);
+    c.take<int32_t>(n > 0 ? n : 1);
+    c.take<char>(assign_ws_bytes(n, d, k, KM_PREC_FP16));
+    return c.bytes();
+}
+
+int km_tune(const float *X, int64_t n, int32_t d, const float *C, int32_t k, void *workspace,
+            size_t workspace_bytes, int32_t *chosen, double *ms_fp32, double *ms_fp16, void *stream) {
+    KM_TRY(check_shape(n, d, k));
+    if (n < 1 || !X || !C) {
+        set_error("km_tune needs n >= 1 and non-NULL X, C");
+        return KM_ERR_BAD_SHAPE;
+    }
+    KM_TRY(check_ws(workspace, workspace_bytes, km_tune_workspace_size(n, d, k)));
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cap) == cudaSuccess && cap != cudaStreamCaptureStatusNone) {
+        set_error("km_tune synchronises and cannot run while the stream is captured");
+        return KM_ERR_BAD_SHAPE;
+    }
+    Carver cv(workspace);
+    int32_t *labels = cv.take<int32_t>(n);
+    void *ws = cv.take<char>(assign_ws_bytes(n, d, k, KM_PREC_FP16));
+    const size_t ws_bytes = assign_ws_bytes(n, d, k, KM_PREC_FP16);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    KM_CUDA(cudaEventCreate(&e0));
+    cudaError_t ce = cudaEventCreate(&e1);
+    if (ce != cudaSuccess) {
+        cudaEventDestroy(e0);
+        return cuda_fail(ce, "cudaEventCreate");
+    }
+    // Median-free timing: one warm-up call, then the mean of three.
+    auto time_prec = [&](int prec, double *ms) -> int {
+        KM_TRY(assign_impl(X, n, d, C, k, prec, labels, ws, ws_bytes, nullptr, s));
+        KM_CUDA(cudaEventRecord(e0, s));
+        for (int r = 0; r < 3; ++r) KM_TRY(assign_impl(X, n, d, C, k, prec, labels, ws, ws_bytes, nullptr, s));
+        KM_CUDA(cudaEventRecord(e1, s));
+        KM_CUDA(cudaEventSynchronize(e1));
+        float t = 0.0f;
+        KM_CUDA(cudaEventElapsedTime(&t, e0, e1));
+        *ms = t / 3.0;
+        return KM_OK;
+    };
+    double t32 = 0.0, t16 = -1.0;
+    int st = time_prec(KM_PREC_FP32, &t32);
+    const bool tc_ok = tc_supported(d, k);
+    if (st == KM_OK && tc_ok) st = time_prec(KM_PREC_FP16, &t16);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (st != KM_OK) return st;
+    const int best = (tc_ok && t16 < t32) ? KM_PREC_FP16 : KM_PREC_FP32;
+    {
+        std::lock_guard<std::mutex> lk(g_tune.m);
+        g_tune.choice[std::make_pair((int)d, (int)k)] = best;
+    }
+    if (chosen) *chosen = best;
+    if (ms_fp32) *ms_fp32 = t32;
+    if (ms_fp16) *ms_fp16 = t16;
+    return KM_OK;
+}
+
+int km_tune_clear(void) {
+    std::lock_guard<std::mutex> lk(g_tune.m);
+    g_tune.choice.clear();
+    return KM_OK;
 }
 
 }  // extern "C"
