@@ -182,6 +182,20 @@ int km_tune(const float *X, int64_t n, int32_t d, const float *C, int32_t k, voi
             size_t workspace_bytes, int32_t *chosen, double *ms_fp32, double *ms_fp16, void *stream);
 int km_tune_clear(void);
 
+/* ---- regular space clustering, first pass ----------------------------------
+ * RegularSpaceClustering._estimate, pyemma/coordinates/clustering/
+ * regspace.py:140-152 (deeptime RegularSpace.partial_fit).  Walks the n
+ * frames of X in order: the first becomes a center, a later one becomes a
+ * center when its distance (sqrt of the float32 squared distance in feature
+ * order, correctly rounded) to every center so far is >= dmin.  centers
+ * (device, max_centers*d floats) receives them, *n_centers (host) their
+ * number.  When a (max_centers+1)-th center would be added the walk stops
+ * and *converged (host) is 0 (the reference's MaxCentersReached case).
+ * Synchronises `stream` once per 65,536 frames. */
+size_t km_regspace_workspace_size(int32_t d);
+int km_regspace(const float *X, int64_t n, int32_t d, double dmin, int32_t max_centers, float *centers,
+                int32_t *n_centers, int32_t *converged, void *workspace, size_t workspace_bytes, void *stream);
+
 /* ---- resident center sets: ClusterModel(centers, metric) built once -------
  * interface.py:164-165 constructs ClusterModel(cluster_centers, metric) for
  * every chunk it transforms.  A km_centers handle holds a device copy of

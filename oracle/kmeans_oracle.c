@@ -370,3 +370,39 @@ int kmo_kmpp(const float *X, int64_t n, int32_t d, int32_t k, uint32_t seed, flo
     free(mind);
     return KMO_OK;
 }
+
+/* Regular space clustering, first pass (pyemma/coordinates/clustering/
+ * regspace.py:140-152, deeptime RegularSpace.partial_fit over the chunks in
+ * iteration order): the first frame becomes a center; every later frame
+ * becomes one when its distance to every center so far is at least dmin.
+ * Distance: sqrtf of the float32 sequential squared distance (kmo_sqdist),
+ * compared in double with dmin (assumption: deeptime's exact comparison
+ * could not be checked; pyemma's comment reads ">= dmin").  Stops when a
+ * (max_centers+1)-th center would be added.  Returns the number of centers
+ * in *n_centers and 1 in *converged unless max_centers was hit. */
+int kmo_regspace(const float *X, int64_t n, int32_t d, double dmin, int32_t max_centers, float *centers,
+                 int32_t *n_centers, int32_t *converged) {
+    int32_t nc = 0;
+    *converged = 1;
+    for (int64_t i = 0; i < n; ++i) {
+        const float *x = X + i * d;
+        int is_new = 1;
+        for (int32_t j = 0; j < nc; ++j) {
+            const float dist = sqrtf(kmo_sqdist(x, centers + (int64_t)j * d, d));
+            if (!((double)dist >= dmin)) {
+                is_new = 0;
+                break;
+            }
+        }
+        if (is_new) {
+            if (nc == max_centers) {
+                *converged = 0;
+                break;
+            }
+            memcpy(centers + (int64_t)nc * d, x, sizeof(float) * (size_t)d);
+            ++nc;
+        }
+    }
+    *n_centers = nc;
+    return 0;
+}

@@ -43,6 +43,7 @@ def lib():
         L.kmo_update.argtypes = [P, i64, i32, P, i32, P, P, P, P, P]
         L.kmo_lloyd.argtypes = [P, i64, i32, i32, P, i32, f64, P, P, P, P, i32]
         L.kmo_kmpp.argtypes = [P, i64, i32, i32, u32, P, P, i32]
+        L.kmo_regspace.argtypes = [P, i64, i32, f64, i32, P, P, P]
         for name in ("kmo_assign", "kmo_update", "kmo_lloyd", "kmo_kmpp"):
             getattr(L, name).restype = ctypes.c_int
         _lib = L
@@ -141,6 +142,18 @@ def kmpp(X, k, seed, n_threads=None):
                         n_threads or default_threads())
     _check(rc, "kmpp")
     return C0, idx
+
+
+def regspace(X, dmin, max_centers):
+    """Regular space centers in frame order; returns (centers, converged)."""
+    X = _f32(X)
+    n, d = X.shape
+    C = np.empty((max(1, max_centers), d), dtype=np.float32)
+    nc = np.zeros(1, dtype=np.int32)
+    conv = np.zeros(1, dtype=np.int32)
+    rc = lib().kmo_regspace(_ptr(X), n, d, float(dmin), int(max_centers), _ptr(C), _ptr(nc), _ptr(conv))
+    _check(rc, "regspace")
+    return C[:int(nc[0])].copy(), bool(conv[0])
 
 
 # ---------------------------------------------------------------------------

@@ -35,6 +35,7 @@ EXPORTED = (
     "km_assign_centers",
     "km_serve_create", "km_serve_add_centers", "km_serve_submit", "km_serve_poll", "km_serve_stats_read",
     "km_serve_shutdown", "km_tune_workspace_size", "km_tune", "km_tune_clear",
+    "km_regspace_workspace_size", "km_regspace",
 )
 
 
@@ -148,6 +149,10 @@ def load(build_if_missing=False):
                           ctypes.POINTER(f64), P]
     L.km_tune.restype = ctypes.c_int
     L.km_tune_clear.restype = ctypes.c_int
+    L.km_regspace_workspace_size.argtypes = [i32]
+    L.km_regspace_workspace_size.restype = sz
+    L.km_regspace.argtypes = [P, i64, i32, f64, i32, P, ctypes.POINTER(i32), ctypes.POINTER(i32), P, sz, P]
+    L.km_regspace.restype = ctypes.c_int
     for name in ("km_assign", "km_batch_assign", "km_update", "km_kmpp", "km_lloyd", "km_centers_create",
                  "km_centers_destroy", "km_centers_info", "km_assign_centers", "km_serve_create",
                  "km_serve_add_centers", "km_serve_submit", "km_serve_poll", "km_serve_stats_read",
@@ -496,3 +501,18 @@ def tune(X, C):
 
 def tune_clear():
     check(load().km_tune_clear())
+
+
+def regspace(X, dmin, max_centers):
+    """Regular space centers of X in frame order: (centers (m, d) CUDA tensor, converged)."""
+    torch = _torch()
+    L = load()
+    _check_frames(torch, X)
+    n, d = X.shape
+    C = torch.empty((max(1, int(max_centers)), d), dtype=torch.float32, device=X.device)
+    ws_bytes = L.km_regspace_workspace_size(d)
+    ws = _workspace(torch, ws_bytes, X.device)
+    nc, conv = ctypes.c_int32(), ctypes.c_int32()
+    check(L.km_regspace(_ptr(X), n, d, float(dmin), int(max_centers), _ptr(C), ctypes.byref(nc), ctypes.byref(conv),
+                        _ptr(ws), ws_bytes, _stream(torch, X.device)))
+    return C[:nc.value].clone(), bool(conv.value)

@@ -1,13 +1,18 @@
-"""User API: cluster_kmeans and assign_to_centers.
+"""User API: cluster_kmeans, assign_to_centers and the sibling estimators.
 
 Same signatures and outputs as pyemma.coordinates.cluster_kmeans
-(pyemma/coordinates/api.py:1727-1867) and assign_to_centers
-(api.py:2060-2156), plus an optional ``precision`` keyword.
+(pyemma/coordinates/api.py:1727-1867), assign_to_centers (api.py:2060-2156),
+cluster_mini_batch_kmeans (api.py:1671-1725), cluster_uniform_time
+(api.py:1870-1951) and cluster_regspace (api.py:1953-2057), plus an optional
+``precision`` keyword.
 """
 from .clustering.assign import AssignCenters
-from .clustering.kmeans import KmeansClustering
+from .clustering.kmeans import KmeansClustering, MiniBatchKmeansClustering
+from .clustering.regspace import RegularSpaceClustering
+from .clustering.uniform_time import UniformTimeClustering
 
-__all__ = ["cluster_kmeans", "assign_to_centers"]
+__all__ = ["cluster_kmeans", "assign_to_centers", "cluster_mini_batch_kmeans", "cluster_uniform_time",
+           "cluster_regspace"]
 
 
 def _chunksize(chunksize, kwargs):
@@ -61,6 +66,48 @@ def assign_to_centers(data=None, centers=None, stride=1, return_dtrajs=True, met
         res.estimate(data, chunksize=cs)
         if return_dtrajs:
             return res.dtrajs
+    else:
+        res.chunksize = cs
+    return res
+
+
+def cluster_mini_batch_kmeans(data=None, k=100, max_iter=10, batch_size=0.2, metric="euclidean",
+                              init_strategy="kmeans++", n_jobs=None, chunksize=None, skip=0, clustercenters=None,
+                              precision="auto", **kwargs):
+    r"""k-means with mini-batches (api.py:1671); returns a MiniBatchKmeansClustering object."""
+    res = MiniBatchKmeansClustering(n_clusters=k, max_iter=max_iter, metric=metric, init_strategy=init_strategy,
+                                    batch_size=batch_size, n_jobs=n_jobs, skip=skip, clustercenters=clustercenters,
+                                    precision=precision)
+    cs = _chunksize(chunksize, kwargs)
+    if data is not None:
+        res.estimate(data, chunksize=cs)
+    else:
+        res.chunksize = cs
+    return res
+
+
+def cluster_uniform_time(data=None, k=None, stride=1, metric="euclidean", n_jobs=None, chunksize=None, skip=0,
+                         precision="auto", **kwargs):
+    r"""Uniform time clustering (api.py:1870); returns a UniformTimeClustering object."""
+    res = UniformTimeClustering(k, metric=metric, n_jobs=n_jobs, skip=skip, stride=stride, precision=precision)
+    cs = _chunksize(chunksize, kwargs)
+    if data is not None:
+        res.estimate(data, chunksize=cs)
+    else:
+        res.chunksize = cs
+    return res
+
+
+def cluster_regspace(data=None, dmin=-1, max_centers=1000, stride=1, metric="euclidean", n_jobs=None,
+                     chunksize=None, skip=0, precision="auto", **kwargs):
+    r"""Regular space clustering (api.py:1953); returns a RegularSpaceClustering object."""
+    if dmin == -1:
+        raise ValueError("provide a minimum distance for clustering, e.g. 2.0")
+    res = RegularSpaceClustering(dmin, max_centers=max_centers, metric=metric, n_jobs=n_jobs, stride=stride,
+                                 skip=skip, precision=precision)
+    cs = _chunksize(chunksize, kwargs)
+    if data is not None:
+        res.estimate(data, chunksize=cs)
     else:
         res.chunksize = cs
     return res

@@ -1,6 +1,9 @@
 """Clustering estimators (pyemma.coordinates.clustering)."""
 from .assign import AssignCenters
 from .interface import AbstractClustering
-from .kmeans import KmeansClustering
+from .kmeans import KmeansClustering, MiniBatchKmeansClustering
+from .regspace import NotConvergedWarning, RegularSpaceClustering
+from .uniform_time import UniformTimeClustering
 
-__all__ = ["AbstractClustering", "AssignCenters", "KmeansClustering"]
+__all__ = ["AbstractClustering", "AssignCenters", "KmeansClustering", "MiniBatchKmeansClustering",
+           "RegularSpaceClustering", "UniformTimeClustering", "NotConvergedWarning"]

@@ -16,7 +16,7 @@ from ... import _lib
 from .. import _device
 from .interface import AbstractClustering
 
-__all__ = ["KmeansClustering"]
+__all__ = ["KmeansClustering", "MiniBatchKmeansClustering"]
 
 
 class KmeansClustering(AbstractClustering):
@@ -196,4 +196,95 @@ class KmeansClustering(AbstractClustering):
         else:
             self.logger.warning("Algorithm did not reach convergence criterion of %g in %i iterations. "
                                 "Consider increasing max_iter.", self.tolerance, self.max_iter)
+        return self
+
+
+class MiniBatchKmeansClustering(KmeansClustering):
+    r"""Mini-batch k-means clustering (kmeans.py:340-447).
+
+    Every pass draws a random sample of ``batch_size`` of the frames (per
+    trajectory in proportion to its length, without replacement, in time
+    order; kmeans.py:363-398) and performs one Lloyd step (assignment, mean
+    of the members, inertia of the sample) on it from the current centers.
+    The first pass starts from kmeans++ (or uniform) centers of its sample.
+    Passes stop when the relative change of the sample inertia is at most
+    ``tolerance`` or after ``max_iter`` passes.
+    """
+
+    def __init__(self, n_clusters, max_iter=5, metric="euclidean", tolerance=1e-5, init_strategy="kmeans++",
+                 batch_size=0.2, oom_strategy="memmap", fixed_seed=False, stride=None, n_jobs=None, skip=0,
+                 clustercenters=None, keep_data=False, precision="auto"):
+        if stride is not None:
+            raise ValueError("stride is a dummy value in MiniBatch Kmeans")
+        if batch_size > 1:
+            raise ValueError("batch_size should be less or equal to 1, but was %s" % batch_size)
+        if keep_data:
+            raise ValueError("keep_data is a dummy value in MiniBatch Kmeans")
+        super(MiniBatchKmeansClustering, self).__init__(n_clusters, max_iter, metric, tolerance, init_strategy,
+                                                        False, oom_strategy, stride=stride, n_jobs=n_jobs,
+                                                        skip=skip, clustercenters=clustercenters, keep_data=False,
+                                                        precision=precision)
+        self.batch_size = batch_size
+
+    def _param_names(self):
+        return KmeansClustering._param_names(self) + ("batch_size",)
+
+    def _sample_sizes(self, traj_lengths):
+        total = int(sum(traj_lengths))
+        samples = int(math.ceil(total * self.batch_size))
+        return [int(math.floor(L / float(total) * samples)) for L in traj_lengths]
+
+    def _draw_sample(self, frames, sizes):
+        parts = []
+        for X, m in zip(frames, sizes):
+            if m == 0:
+                continue
+            choice = np.sort(np.random.choice(len(X), m, replace=False))
+            parts.append(np.asarray(X[choice], dtype=np.float32))
+        return parts
+
+    def _estimate(self, source):
+        self.stride = None
+        frames = source.frames(stride=1, skip=self.skip)
+        traj_lengths = [len(X) for X in frames]
+        if sum(traj_lengths) == 0:
+            raise ValueError("no frames to cluster (skip=%s)" % self.skip)
+        if not self.n_clusters:
+            self.n_clusters = min(int(math.sqrt(sum(traj_lengths))), 5000)
+        sizes = self._sample_sizes(traj_lengths)
+        if sum(sizes) == 0:
+            raise ValueError("batch_size %s selects no frames" % self.batch_size)
+        dim = source.dimension()
+        C = None
+        if self._check_resume_iteration():
+            C = _device.centers_to_device(self.clustercenters)
+        self._converged = False
+        prev_cost = 0.0
+        i_pass = 0
+        inertias = []
+        while not (self._converged or i_pass + 1 > self.max_iter):
+            Xb = _device.pack_to_device(self._draw_sample(frames, sizes), dim)
+            if C is None:
+                if self.init_strategy == "uniform":
+                    idx = np.random.choice(Xb.shape[0], int(self.n_clusters), replace=False)
+                    C = Xb[_device.torch_module().from_numpy(np.sort(idx)).to(Xb.device)].contiguous()
+                else:
+                    C, _ = _lib.kmpp(Xb, int(self.n_clusters), int(np.random.randint(0, 2 ** 32 - 1, dtype=np.int64)))
+                self.initial_centers_ = C.cpu().numpy()
+            res = _lib.lloyd(Xb, C, 1, -1.0, precision=self.precision)
+            cost = float(res["inertias"][0])
+            inertias.append(cost)
+            rel_change = abs(cost - prev_cost) / cost if cost != 0.0 else 0.0
+            prev_cost = cost
+            if rel_change <= self.tolerance:
+                self._converged = True
+                self.logger.info("Cluster centers converged after %i steps.", i_pass + 1)
+            i_pass += 1
+            del Xb
+        self.clustercenters = C.cpu().numpy()
+        self.inertias = np.asarray(inertias)
+        self.n_iter = i_pass
+        if not self._converged:
+            self.logger.info("Algorithm did not reach convergence criterion of %g in %i iterations. "
+                             "Consider increasing max_iter.", self.tolerance, self.max_iter)
         return self

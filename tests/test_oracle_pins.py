@@ -185,3 +185,22 @@ def test_assign_matches_sequential_numpy(oracle, d):
     lab, dist = oracle.assign(X, C, return_dist=True)
     np.testing.assert_array_equal(lab, np.argmin(D, axis=1))
     np.testing.assert_array_equal(dist, D.min(axis=1))
+
+
+def test_regspace_oracle_properties(oracle):
+    # regspace.py docstring and reference test_regspace.py: centers at least
+    # dmin apart, the first frame is the first center, max_centers stops the walk.
+    import itertools
+    rng = np.random.default_rng(11)
+    X = rng.random((1000, 3)).astype(np.float32)
+    C, conv = oracle.regspace(X, 0.3, 1000)
+    assert conv and len(C) > 1
+    np.testing.assert_array_equal(C[0], X[0])
+    for a, b in itertools.combinations(C, 2):
+        assert np.linalg.norm(a - b) >= 0.3
+    # every frame is within dmin of some center (else it would be one)
+    d = np.sqrt(((X[:, None, :].astype(np.float64) - C[None].astype(np.float64)) ** 2).sum(-1)).min(1)
+    assert (d < 0.3 + 1e-6).all()
+    C2, conv2 = oracle.regspace(X, 1e-8, 50)
+    assert not conv2 and len(C2) == 50
+    np.testing.assert_array_equal(C2, X[:50])
