@@ -196,6 +196,19 @@ size_t km_regspace_workspace_size(int32_t d);
 int km_regspace(const float *X, int64_t n, int32_t d, double dmin, int32_t max_centers, float *centers,
                 int32_t *n_centers, int32_t *converged, void *workspace, size_t workspace_bytes, void *stream);
 
+/* ---- lag-tau transition counts of discrete trajectories ---------------------
+ * The step after discretization: pyemma/msm/estimators/_dtraj_stats.py:139-145
+ * (deeptime count_matrix / TransitionCountEstimator).  dtrajs (device int32)
+ * holds the trajectories back to back, delimited by offsets (host, n_traj+1
+ * entries, offsets[0] = 0).  counts (device, nstates*nstates int64,
+ * row-major from -> to) receives, per trajectory, the pairs
+ * (dtraj[t], dtraj[t+lag]) for t = 0 .. T-lag-1 (sliding != 0) or
+ * t = 0, lag, 2 lag, ... < T-lag (sliding == 0); pairs with a state outside
+ * [0, nstates) (e.g. -1, unassigned) are left out. */
+size_t km_count_matrix_workspace_size(int32_t n_traj);
+int km_count_matrix(const int32_t *dtrajs, const int64_t *offsets, int32_t n_traj, int32_t lag, int32_t sliding,
+                    int32_t nstates, int64_t *counts, void *workspace, size_t workspace_bytes, void *stream);
+
 /* ---- resident center sets: ClusterModel(centers, metric) built once -------
  * interface.py:164-165 constructs ClusterModel(cluster_centers, metric) for
  * every chunk it transforms.  A km_centers handle holds a device copy of

@@ -156,6 +156,26 @@ def regspace(X, dmin, max_centers):
     return C[:int(nc[0])].copy(), bool(conv[0])
 
 
+def count_matrix(dtrajs, lag, sliding=True, nstates=None):
+    """Dense lag-`lag` transition counts, as deeptime's count_matrix builds
+    them (rows dtraj[0:-lag] or dtraj[0:-lag:lag], columns dtraj[lag:] or
+    dtraj[lag::lag]; pairs with a negative state dropped)."""
+    dtrajs = [np.asarray(d, dtype=np.int64) for d in dtrajs]
+    if nstates is None:
+        nstates = max((int(d.max()) for d in dtrajs if len(d)), default=-1) + 1
+    C = np.zeros((nstates, nstates), dtype=np.int64)
+    for d in dtrajs:
+        if len(d) <= lag:
+            continue
+        if sliding:
+            row, col = d[:-lag], d[lag:]
+        else:
+            row, col = d[0:-lag:lag], d[lag::lag]
+        keep = (row >= 0) & (col >= 0) & (row < nstates) & (col < nstates)
+        np.add.at(C, (row[keep], col[keep]), 1)
+    return C
+
+
 # ---------------------------------------------------------------------------
 # float64 NumPy reference (independent of the C code)
 # ---------------------------------------------------------------------------

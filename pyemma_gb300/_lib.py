@@ -35,7 +35,7 @@ EXPORTED = (
     "km_assign_centers",
     "km_serve_create", "km_serve_add_centers", "km_serve_submit", "km_serve_poll", "km_serve_stats_read",
     "km_serve_shutdown", "km_tune_workspace_size", "km_tune", "km_tune_clear",
-    "km_regspace_workspace_size", "km_regspace",
+    "km_regspace_workspace_size", "km_regspace", "km_count_matrix_workspace_size", "km_count_matrix",
 )
 
 
@@ -153,6 +153,10 @@ def load(build_if_missing=False):
     L.km_regspace_workspace_size.restype = sz
     L.km_regspace.argtypes = [P, i64, i32, f64, i32, P, ctypes.POINTER(i32), ctypes.POINTER(i32), P, sz, P]
     L.km_regspace.restype = ctypes.c_int
+    L.km_count_matrix_workspace_size.argtypes = [i32]
+    L.km_count_matrix_workspace_size.restype = sz
+    L.km_count_matrix.argtypes = [P, P, i32, i32, i32, i32, P, P, sz, P]
+    L.km_count_matrix.restype = ctypes.c_int
     for name in ("km_assign", "km_batch_assign", "km_update", "km_kmpp", "km_lloyd", "km_centers_create",
                  "km_centers_destroy", "km_centers_info", "km_assign_centers", "km_serve_create",
                  "km_serve_add_centers", "km_serve_submit", "km_serve_poll", "km_serve_stats_read",
@@ -516,3 +520,20 @@ def regspace(X, dmin, max_centers):
     check(L.km_regspace(_ptr(X), n, d, float(dmin), int(max_centers), _ptr(C), ctypes.byref(nc), ctypes.byref(conv),
                         _ptr(ws), ws_bytes, _stream(torch, X.device)))
     return C[:nc.value].clone(), bool(conv.value)
+
+
+def count_matrix(dtrajs_packed, offsets, lag, nstates, sliding=True):
+    """Dense (nstates, nstates) int64 CUDA tensor of lag-`lag` transition counts."""
+    torch = _torch()
+    L = load()
+    if dtrajs_packed.device.type != "cuda" or dtrajs_packed.dtype != torch.int32 or not dtrajs_packed.is_contiguous():
+        raise ValueError("dtrajs_packed must be a contiguous int32 CUDA tensor")
+    offs = np.ascontiguousarray(offsets, dtype=np.int64)
+    n_traj = len(offs) - 1
+    counts = torch.empty((int(nstates), int(nstates)), dtype=torch.int64, device=dtrajs_packed.device)
+    ws_bytes = L.km_count_matrix_workspace_size(n_traj)
+    ws = _workspace(torch, ws_bytes, dtrajs_packed.device)
+    check(L.km_count_matrix(_ptr(dtrajs_packed), offs.ctypes.data_as(ctypes.c_void_p), n_traj, int(lag),
+                            1 if sliding else 0, int(nstates), _ptr(counts), _ptr(ws), ws_bytes,
+                            _stream(torch, dtrajs_packed.device)))
+    return counts

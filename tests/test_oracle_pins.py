@@ -204,3 +204,15 @@ def test_regspace_oracle_properties(oracle):
     C2, conv2 = oracle.regspace(X, 1e-8, 50)
     assert not conv2 and len(C2) == 50
     np.testing.assert_array_equal(C2, X[:50])
+
+
+def test_count_matrix_oracle_known_answers(oracle):
+    # sliding: T - lag pairs (t, t+lag); sample: pairs at multiples of lag
+    # (the count modes documented at pyemma/msm/estimators/_dtraj_stats.py:103-117)
+    d = np.array([0, 0, 1, 1, 0])
+    C = oracle.count_matrix([d], 1)
+    np.testing.assert_array_equal(C, [[1, 1], [1, 1]])
+    C = oracle.count_matrix([d], 2, sliding=False)
+    np.testing.assert_array_equal(C, [[0, 1], [1, 0]])
+    C = oracle.count_matrix([np.array([0, -1, 1, 1]), np.array([2])], 1)
+    np.testing.assert_array_equal(C, [[0, 0, 0], [0, 1, 0], [0, 0, 0]])
