@@ -209,6 +209,17 @@ size_t km_count_matrix_workspace_size(int32_t n_traj);
 int km_count_matrix(const int32_t *dtrajs, const int64_t *offsets, int32_t n_traj, int32_t lag, int32_t sliding,
                     int32_t nstates, int64_t *counts, void *workspace, size_t workspace_bytes, void *stream);
 
+/* ---- atom-pair distance features --------------------------------------------
+ * The featurization that feeds the discretization:
+ * pyemma/coordinates/data/featurization/featurizer.py:305-372 (add_distances,
+ * add_distances_ca) and distances.py:53-54 (mdtraj.compute_distances, no
+ * unit cell).  xyz (device, n * n_atoms * 3 float32, frame-major), pairs
+ * (device, npairs * 2 int32 atom indices), out (device, n * npairs float32):
+ * out[t*npairs + p] = sqrt((dx*dx + dy*dy) + dz*dz) in float32 with
+ * d = xyz[t, pairs[p][1]] - xyz[t, pairs[p][0]]. */
+int km_pair_distances(const float *xyz, int64_t n, int32_t n_atoms, const int32_t *pairs, int32_t npairs,
+                      float *out, void *stream);
+
 /* ---- resident center sets: ClusterModel(centers, metric) built once -------
  * interface.py:164-165 constructs ClusterModel(cluster_centers, metric) for
  * every chunk it transforms.  A km_centers handle holds a device copy of

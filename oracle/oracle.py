@@ -176,6 +176,18 @@ def count_matrix(dtrajs, lag, sliding=True, nstates=None):
     return C
 
 
+def pair_distances(xyz, pairs):
+    """Atom-pair distances in float32 with each operation rounded on its own:
+    sqrt((dx*dx + dy*dy) + dz*dz), d = xyz[:, j] - xyz[:, i]
+    (mdtraj.compute_distances without a unit cell, as called from
+    pyemma/coordinates/data/featurization/distances.py:53-54)."""
+    xyz = np.asarray(xyz, dtype=np.float32)
+    pairs = np.asarray(pairs, dtype=np.int64).reshape(-1, 2)
+    d = xyz[:, pairs[:, 1], :] - xyz[:, pairs[:, 0], :]
+    r2 = (d[..., 0] * d[..., 0] + d[..., 1] * d[..., 1]) + d[..., 2] * d[..., 2]
+    return np.sqrt(r2).astype(np.float32)
+
+
 # ---------------------------------------------------------------------------
 # float64 NumPy reference (independent of the C code)
 # ---------------------------------------------------------------------------

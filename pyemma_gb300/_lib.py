@@ -36,6 +36,7 @@ EXPORTED = (
     "km_serve_create", "km_serve_add_centers", "km_serve_submit", "km_serve_poll", "km_serve_stats_read",
     "km_serve_shutdown", "km_tune_workspace_size", "km_tune", "km_tune_clear",
     "km_regspace_workspace_size", "km_regspace", "km_count_matrix_workspace_size", "km_count_matrix",
+    "km_pair_distances",
 )
 
 
@@ -157,6 +158,8 @@ def load(build_if_missing=False):
     L.km_count_matrix_workspace_size.restype = sz
     L.km_count_matrix.argtypes = [P, P, i32, i32, i32, i32, P, P, sz, P]
     L.km_count_matrix.restype = ctypes.c_int
+    L.km_pair_distances.argtypes = [P, i64, i32, P, i32, P, P]
+    L.km_pair_distances.restype = ctypes.c_int
     for name in ("km_assign", "km_batch_assign", "km_update", "km_kmpp", "km_lloyd", "km_centers_create",
                  "km_centers_destroy", "km_centers_info", "km_assign_centers", "km_serve_create",
                  "km_serve_add_centers", "km_serve_submit", "km_serve_poll", "km_serve_stats_read",
@@ -537,3 +540,23 @@ def count_matrix(dtrajs_packed, offsets, lag, nstates, sliding=True):
                             1 if sliding else 0, int(nstates), _ptr(counts), _ptr(ws), ws_bytes,
                             _stream(torch, dtrajs_packed.device)))
     return counts
+
+
+def pair_distances(xyz, pairs, out=None):
+    """(n, npairs) float32 CUDA tensor of atom-pair distances of xyz (n, n_atoms, 3) CUDA float32."""
+    torch = _torch()
+    L = load()
+    if xyz.device.type != "cuda" or xyz.dtype != torch.float32 or xyz.dim() != 3 or xyz.shape[2] != 3 \
+            or not xyz.is_contiguous():
+        raise ValueError("xyz must be a contiguous float32 (n, n_atoms, 3) CUDA tensor")
+    n, n_atoms, _ = xyz.shape
+    if pairs.device.type != "cuda" or pairs.dtype != torch.int32 or pairs.dim() != 2 or pairs.shape[1] != 2 \
+            or not pairs.is_contiguous():
+        raise ValueError("pairs must be a contiguous int32 (npairs, 2) CUDA tensor")
+    if pairs.numel() and (int(pairs.min()) < 0 or int(pairs.max()) >= n_atoms):
+        raise ValueError("pair indices out of range [0, %d)" % n_atoms)
+    npairs = pairs.shape[0]
+    if out is None:
+        out = torch.empty((n, npairs), dtype=torch.float32, device=xyz.device)
+    check(L.km_pair_distances(_ptr(xyz), n, n_atoms, _ptr(pairs), npairs, _ptr(out), _stream(torch, xyz.device)))
+    return out

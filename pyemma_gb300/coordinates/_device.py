@@ -35,6 +35,15 @@ def pack_to_device(trajs, dim):
     directly.
     """
     torch = torch_module()
+    if len(trajs) > 0 and all(isinstance(t, torch.Tensor) and t.device.type == "cuda" for t in trajs):
+        # frames already on the device: used as they are when they form one
+        # contiguous float32 block, else gathered on the device
+        ts = [t for t in trajs if len(t)]
+        if len(ts) == 1 and ts[0].dtype == torch.float32 and ts[0].is_contiguous():
+            return ts[0]
+        if not ts:
+            return torch.empty((0, dim), dtype=torch.float32, device=device())
+        return torch.cat([t.float() for t in ts]).contiguous()
     n = int(sum(len(t) for t in trajs))
     dev = torch.empty((n, dim), dtype=torch.float32, device=device())
     pos = 0

@@ -10,7 +10,7 @@ import os
 import numpy as np
 
 from .. import _device
-from ..data import InMemorySource, default_chunksize, get_n_jobs, make_logger
+from ..data import DeviceSource, InMemorySource, default_chunksize, get_n_jobs, is_device_data, make_logger
 
 _METRICS = ("euclidean", "minRMSD")
 
@@ -130,6 +130,8 @@ class AbstractClustering(object):
     def _source(self, X, chunksize=None):
         if isinstance(X, InMemorySource):
             return X
+        if is_device_data(X):
+            return DeviceSource(X, chunksize=chunksize)
         return InMemorySource(X, chunksize=chunksize)
 
     # ---- estimation ------------------------------------------------------
@@ -188,17 +190,18 @@ class AbstractClustering(object):
 
     def _transform_array(self, X):
         """get closest index of point in clustercenters to x (column vector)."""
-        X = np.asarray(X)
+        if not is_device_data(X):
+            X = np.asarray(X)
         if X.ndim == 1:
             X = X[:, None]
         return self._assign_arrays([X])[0][:, None]
 
     def transform(self, X):
-        """Maps X (ndarray or list of ndarrays) to (T, 1) int32 column vector(s)."""
+        """Maps X (ndarray, CUDA tensor or a list of them) to (T, 1) int32 column vector(s)."""
+        source = DeviceSource(X) if is_device_data(X) else InMemorySource(X)
         if isinstance(X, (list, tuple)):
-            trajs = InMemorySource(X).data
-            return [lab[:, None] for lab in self._assign_arrays(trajs)]
-        return self._transform_array(InMemorySource(X).data[0])
+            return [lab[:, None] for lab in self._assign_arrays(source.data)]
+        return self._transform_array(source.data[0])
 
     def get_output(self, dimensions=slice(0, None), stride=1, skip=0, chunk=None):
         """Assigns all frames of the data producer; list of (T_i, 1) int32 arrays."""

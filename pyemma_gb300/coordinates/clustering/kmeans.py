@@ -142,7 +142,8 @@ class KmeansClustering(AbstractClustering):
                 if len(picked) >= self.n_clusters:
                     break
                 if t in chosen:
-                    picked.append(X[t])
+                    row = X[t]
+                    picked.append(row.cpu().numpy() if hasattr(row, "cpu") else row)
         dim = trajs[0].shape[1]
         return np.asarray(picked).reshape(-1, dim)
 
@@ -240,7 +241,11 @@ class MiniBatchKmeansClustering(KmeansClustering):
             if m == 0:
                 continue
             choice = np.sort(np.random.choice(len(X), m, replace=False))
-            parts.append(np.asarray(X[choice], dtype=np.float32))
+            if hasattr(X, "device"):  # frames on the GPU
+                import torch
+                parts.append(X[torch.from_numpy(choice).to(X.device)].float())
+            else:
+                parts.append(np.asarray(X[choice], dtype=np.float32))
         return parts
 
     def _estimate(self, source):

@@ -67,6 +67,8 @@ class UniformTimeClustering(AbstractClustering):
         linspace = stride * np.arange(next_t, T - next_t + 1, (T - 2 * next_t + 1) // self.n_clusters)[:self.n_clusters]
         picks = [self._idx_to_traj_idx(x, cumsum) for x in linspace]
         frames = source.frames(stride=1, skip=self.skip)
-        self.clustercenters = np.asarray([frames[i][t] for i, t in picks], dtype=np.float32)
+        rows = [frames[i][t] for i, t in picks]
+        self.clustercenters = np.asarray([r.cpu().numpy() if hasattr(r, "cpu") else r for r in rows],
+                                         dtype=np.float32)
         assert len(self.clustercenters) == self.n_clusters
         return self

@@ -107,6 +107,48 @@ class InMemorySource(object):
         return default_chunksize(self._dim, itemsize)
 
 
+def is_device_data(data):
+    """True for a CUDA torch tensor or a list/tuple of them (frames already on the GPU)."""
+    try:
+        import torch
+    except ImportError:
+        return False
+    if isinstance(data, torch.Tensor):
+        return data.device.type == "cuda"
+    if isinstance(data, (list, tuple)) and len(data) > 0:
+        return all(isinstance(t, torch.Tensor) and t.device.type == "cuda" for t in data)
+    return False
+
+
+class DeviceSource(InMemorySource):
+    """Trajectories that already live in device memory (CUDA torch tensors),
+    e.g. features computed on the GPU; they are used without a host copy."""
+
+    def __init__(self, data, chunksize=None):
+        import torch
+        if isinstance(data, torch.Tensor):
+            data = [data]
+        out = []
+        for t in data:
+            if t.dim() == 1:
+                t = t[:, None]
+            elif t.dim() > 2:
+                t = t.reshape(t.shape[0], -1)
+            out.append(t)
+        if len(out) == 0:
+            raise ValueError("no trajectories given")
+        dims = {int(t.shape[1]) for t in out}
+        if len(dims) != 1:
+            raise ValueError("trajectories have different dimensions: %s" % sorted(dims))
+        self._data = out
+        self._dim = dims.pop()
+        self.chunksize = chunksize
+
+    @property
+    def default_chunksize(self):
+        return default_chunksize(self._dim, 4)
+
+
 def get_n_jobs(logger=None):
     """n_jobs from SLURM_CPUS_ON_NODE, PYEMMA_NJOBS or the logical CPU count."""
 
