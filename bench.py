@@ -348,6 +348,33 @@ def run_ours(args):
         e2e = {"value": n / dt, "unit": UNIT, "h2d_bytes_per_step": n * D * 4, "d2h_bytes_per_step": K * D * 4 + 8,
                "api": "KmeansClustering(n_clusters=2000, max_iter=1, clustercenters=C).estimate(pinned host X)",
                "steps": e2e_steps}
+        del Xh, Xh_np
+        # The same iteration from pinned host C-alpha coordinates: the
+        # 528 distance features are computed on the device (featurize.ca_distances)
+        # and clustered there, so 396 bytes per frame cross the host link.
+        from pyemma_gb300 import featurize
+        xyz_d = datasets.calpha_coordinates(n_frames=n, seed=SEED + rank)
+        xyz_h = torch.empty(tuple(xyz_d.shape), dtype=torch.float32, pin_memory=True)
+        xyz_h.copy_(xyz_d)
+        del xyz_d
+        torch.cuda.empty_cache()
+        F = featurize.ca_distances(xyz_h, excluded_neighbors=0)
+        KmeansClustering(n_clusters=K, max_iter=1, tolerance=-1.0, clustercenters=C0h, precision="fp16").estimate(F)
+        del F
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            F = featurize.ca_distances(xyz_h, excluded_neighbors=0)
+            km = KmeansClustering(n_clusters=K, max_iter=1, tolerance=-1.0, clustercenters=C0h, precision="fp16")
+            km.estimate(F)
+            _ = km.clustercenters
+            del F
+        dtc = (time.perf_counter() - t0) / e2e_steps
+        e2e["from_coordinates"] = {
+            "value": n / dtc, "unit": UNIT, "h2d_bytes_per_step": n * 33 * 3 * 4, "d2h_bytes_per_step": K * D * 4 + 8,
+            "api": "featurize.ca_distances(pinned host xyz (n, 33, 3)) -> KmeansClustering(max_iter=1).estimate",
+            "workload": "same chain model, coordinates instead of precomputed distances"}
+        del xyz_h
 
     # ---- CPU baseline (rank 0, N=1) ----
     cpu = None
@@ -489,6 +516,17 @@ def run_c2(args):
         km.estimate(pinned)
         dtrajs = km.dtrajs
     e2e_s = (time.perf_counter() - t0) / reps
+    # the next step of the pipeline: lag-10 transition counts of the 20 dtrajs
+    packed = torch.from_numpy(np.concatenate(dtrajs).astype(np.int32)).cuda()
+    offsets = np.concatenate([[0], np.cumsum([len(d) for d in dtrajs])]).astype(np.int64)
+    _lib.count_matrix(packed, offsets, 10, 1000)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(10):
+        counts = _lib.count_matrix(packed, offsets, 10, 1000)
+    e1.record()
+    torch.cuda.synchronize()
+    cm_ms = e0.elapsed_time(e1) / 10
     _emit({"metric": "k-means frames/s (Lloyd iteration, packed uneven trajectories)", "value": n / (ms / 1e3),
            "unit": "frames/s", "n_gpus": 1, "steps": args.steps, "ms_per_step": ms, "higher_is_better": True,
            "dtype": "f32 exact distances, f64 sums",
@@ -503,7 +541,9 @@ def run_c2(args):
            "e2e": {"value": n / e2e_s, "unit": "frames/s", "h2d_bytes_per_step": n * 40,
                    "d2h_bytes_per_step": n * 4 + 1000 * 40,
                    "api": "KmeansClustering(max_iter=1, clustercenters=C).estimate(20 pinned trajectories); dtrajs"},
-           "dtrajs": len(dtrajs)})
+           "dtrajs": len(dtrajs),
+           "count_matrix": {"lag": 10, "ms": cm_ms, "frames_per_s": n / (cm_ms / 1e3), "counts": int(counts.sum()),
+                            "note": "km_count_matrix on the 20 dtrajs, dense 1000 x 1000 int64 (memset included)"}})
 
 
 def run_c4(args):

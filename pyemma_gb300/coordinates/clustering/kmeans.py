@@ -143,7 +143,7 @@ class KmeansClustering(AbstractClustering):
                     break
                 if t in chosen:
                     row = X[t]
-                    picked.append(row.cpu().numpy() if hasattr(row, "cpu") else row)
+                    picked.append(row if isinstance(row, np.ndarray) else row.cpu().numpy())
         dim = trajs[0].shape[1]
         return np.asarray(picked).reshape(-1, dim)
 
@@ -241,7 +241,7 @@ class MiniBatchKmeansClustering(KmeansClustering):
             if m == 0:
                 continue
             choice = np.sort(np.random.choice(len(X), m, replace=False))
-            if hasattr(X, "device"):  # frames on the GPU
+            if not isinstance(X, np.ndarray):  # frames on the GPU (torch tensor)
                 import torch
                 parts.append(X[torch.from_numpy(choice).to(X.device)].float())
             else:

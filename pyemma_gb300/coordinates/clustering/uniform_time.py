@@ -68,7 +68,7 @@ class UniformTimeClustering(AbstractClustering):
         picks = [self._idx_to_traj_idx(x, cumsum) for x in linspace]
         frames = source.frames(stride=1, skip=self.skip)
         rows = [frames[i][t] for i, t in picks]
-        self.clustercenters = np.asarray([r.cpu().numpy() if hasattr(r, "cpu") else r for r in rows],
+        self.clustercenters = np.asarray([r if isinstance(r, np.ndarray) else r.cpu().numpy() for r in rows],
                                          dtype=np.float32)
         assert len(self.clustercenters) == self.n_clusters
         return self

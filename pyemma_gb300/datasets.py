@@ -110,6 +110,31 @@ def _calpha_distances_torch(n_frames, n_beads, bond, jitter, n_conf, dwell, seed
     return out
 
 
+def calpha_coordinates(n_frames=2_000_000, n_beads=33, bond=0.38, jitter=0.05, n_conf=64, dwell=2000, seed=0,
+                       device="cuda"):
+    """(n_frames, n_beads, 3) float32 C-alpha coordinates of the same jittered
+    chain model as calpha_distances (generated on `device`; a CUDA tensor)."""
+    import torch
+    rng = np.random.default_rng(seed)
+    steps = rng.standard_normal((n_conf, n_beads - 1, 3))
+    steps *= bond / np.linalg.norm(steps, axis=2, keepdims=True)
+    base = np.concatenate([np.zeros((n_conf, 1, 3)), np.cumsum(steps, axis=1)], axis=1)
+    waits = rng.geometric(1.0 / dwell, size=n_frames // dwell * 2 + 2)
+    starts = np.concatenate([[0], np.cumsum(waits)])
+    conf = rng.integers(0, n_conf, size=len(starts))
+    seg = np.searchsorted(starts, np.arange(n_frames), side="right") - 1
+    frame_conf = torch.from_numpy(conf[seg]).to(device)
+    base_t = torch.from_numpy(base).to(device=device, dtype=torch.float32)
+    gen = torch.Generator(device=device)
+    gen.manual_seed(seed)
+    out = torch.empty((n_frames, n_beads, 3), dtype=torch.float32, device=device)
+    step = 1 << 17
+    for a in range(0, n_frames, step):
+        b = min(n_frames, a + step)
+        out[a:b] = base_t[frame_conf[a:b]] + jitter * torch.randn((b - a, n_beads, 3), generator=gen, device=device)
+    return out
+
+
 def sweep_mixture(n, d, k, seed=0):
     """Precision-sweep data: 4k true clusters, sigma 0.3, means U[-5, 5]^d."""
     return gaussian_mixture(n, d, 4 * k, 0.3, 5.0, seed)
