@@ -564,7 +564,7 @@ def run_c4(args):
             C0 = X[torch.randperm(n, device="cuda", generator=g)[:k]].contiguous()
             row = {"d": d, "k": k}
             steps = 2
-            for prec in ("fp32", "fp16"):
+            for prec in ("fp32", "fp16", "bf16"):
                 try:
                     ms, prof = _lloyd_rate(torch, _lib, X, C0, steps, prec)
                     row[prec + "_ms_per_iter"] = ms
@@ -579,14 +579,19 @@ def run_c4(args):
                 row["full_recheck_fraction"] = st["n_full"] / float(n)
                 row["labels_identical"] = bool(torch.equal(lab16, lab32))
                 row["tflops_fp16_iter"] = 2.0 * n * k * d / (row["fp16_ms_per_iter"] / 1e3) / 1e12
+                if row.get("bf16_ms_per_iter"):
+                    labb, stb = _lib.assign(X, C0, precision="bf16")
+                    row["bf16_recheck_fraction"] = (stb["n_recheck"] + stb["n_full"]) / float(n)
+                    row["bf16_labels_identical"] = bool(torch.equal(labb, lab32))
+                    del labb
             rows.append(row)
             del X, C0
             torch.cuda.empty_cache()
     _emit({"metric": "Lloyd iteration time per precision (precision sweep)", "unit": "ms", "n_gpus": 1,
            "higher_is_better": False,
            "config": {"workload": "c4: 1,000,000 frames, 4k Gaussian clusters (sigma 0.3, means U[-5,5]^d), "
-                                  "d in {16,64,256,1024}, k in {100,1000,5000}; fp32 exact vs fp16 tensor cores "
-                                  "with exact recheck"},
+                                  "d in {16,64,256,1024}, k in {100,1000,5000}; fp32 exact vs fp16 and bf16 tensor "
+                                  "cores with exact recheck"},
            "rows": rows})
 
 

@@ -56,8 +56,10 @@ typedef enum {
  *                 of every frame whose nearest centers lie within the derived
  *                 error bound; the labels equal the KM_PREC_FP32 labels bit
  *                 for bit.
- *   KM_PREC_AUTO: the library picks by (d, k). */
-typedef enum { KM_PREC_FP32 = 0, KM_PREC_FP16 = 1, KM_PREC_AUTO = 2 } km_precision;
+ *   KM_PREC_BF16: the same with BF16 operands (8-bit mantissa: a wider bound,
+ *                 so more frames are re-checked; same labels).
+ *   KM_PREC_AUTO: the library picks by (d, k) (km_tune can measure it). */
+typedef enum { KM_PREC_FP32 = 0, KM_PREC_FP16 = 1, KM_PREC_AUTO = 2, KM_PREC_BF16 = 3 } km_precision;
 
 /* Progress hook, called on the calling host thread (kmeans.py:241-251
  * passes callback_init_centers / callback_loop into the native fit). */

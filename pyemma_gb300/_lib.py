@@ -12,7 +12,7 @@ import numpy as np
 
 from . import _build
 
-PRECISIONS = {"fp32": 0, "fp16": 1, "auto": 2}
+PRECISIONS = {"fp32": 0, "fp16": 1, "auto": 2, "bf16": 3}
 PRECISION_NAMES = {v: k for k, v in PRECISIONS.items()}
 
 KM_OK = 0

@@ -35,7 +35,7 @@ def cluster_kmeans(data=None, k=None, max_iter=10, tolerance=1e-5, stride=1, met
     iterations run on the GPU; the object then holds ``clustercenters`` and
     the int32 ``dtrajs`` of the data.  Parameters as in PyEMMA
     (api.py:1727); ``precision`` selects the distance arithmetic of the
-    assignment step ('auto', 'fp32', 'fp16'; the labels are exact in all
+    assignment step ('auto', 'fp32', 'fp16', 'bf16'; the labels are exact in all
     cases).
     """
     res = KmeansClustering(n_clusters=k, max_iter=max_iter, metric=metric, tolerance=tolerance,

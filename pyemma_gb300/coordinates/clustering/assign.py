@@ -25,7 +25,7 @@ class AssignCenters(AbstractClustering):
         Accepted for compatibility.
     skip : int
         Skip the first n frames of each trajectory.
-    precision : {'auto', 'fp32', 'fp16'}
+    precision : {'auto', 'fp32', 'fp16', 'bf16'}
     """
 
     def __init__(self, clustercenters, metric="euclidean", stride=1, n_jobs=None, skip=0, precision="auto"):

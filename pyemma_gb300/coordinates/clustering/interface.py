@@ -25,7 +25,7 @@ class AbstractClustering(object):
     n_jobs : int or None
         Accepted for compatibility (thread count of the reference's OpenMP
         backend); resolved as the reference does and otherwise unused.
-    precision : {'auto', 'fp32', 'fp16'}
+    precision : {'auto', 'fp32', 'fp16', 'bf16'}
         Arithmetic of the distance kernel.  Every choice gives the labels of
         the exact float32 evaluation; 'fp16' uses the tensor cores with an
         exact recheck of near ties.

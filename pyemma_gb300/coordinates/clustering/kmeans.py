@@ -47,7 +47,7 @@ class KmeansClustering(AbstractClustering):
         Resume from these centers (init_strategy is ignored).
     keep_data : bool
         Keep the device copy of the frames for a later resume.
-    precision : {'auto', 'fp32', 'fp16'}
+    precision : {'auto', 'fp32', 'fp16', 'bf16'}
         Distance arithmetic of the assignment step (labels are exact in all
         cases).
     """

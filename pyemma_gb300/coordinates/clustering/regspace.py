@@ -37,7 +37,7 @@ class RegularSpaceClustering(AbstractClustering):
         Frames used for the center search: traj[skip::stride].
     n_jobs : int or None
         Accepted for compatibility.
-    precision : {'auto', 'fp32', 'fp16'}
+    precision : {'auto', 'fp32', 'fp16', 'bf16'}
         Arithmetic of the assignment pass (labels are exact in all cases).
     """
 

@@ -26,7 +26,7 @@ class UniformTimeClustering(AbstractClustering):
     stride, skip : int
     n_jobs : int or None
         Accepted for compatibility.
-    precision : {'auto', 'fp32', 'fp16'}
+    precision : {'auto', 'fp32', 'fp16', 'bf16'}
     """
 
     def __init__(self, n_clusters=2, metric="euclidean", stride=1, n_jobs=None, skip=0, precision="auto"):

@@ -51,6 +51,7 @@
 #include "km_common.cuh"
 #include "km_internal.h"
 
+#include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
 #include <cmath>
@@ -84,6 +85,7 @@ struct TcParams {
     int bn;
     int stages;
     int stream_a;  // 1: A chunks travel with the B stages instead of staying resident (large d)
+    int bf16;      // 1: BF16 operands instead of FP16
     int n_ctiles;
     uint32_t tmem_cols;
     float e_coef;
@@ -275,10 +277,36 @@ __device__ __forceinline__ uint64_t sw64_desc(uint32_t saddr) {
     return desc;
 }
 
-// Instruction descriptor of kind::f16: FP16 x FP16 -> F32, both K-major.
-__host__ __device__ constexpr uint32_t make_idesc(int M, int N) {
-    return (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+// Instruction descriptor of kind::f16: FP16 x FP16 (or BF16 x BF16) -> F32,
+// both K-major.
+__host__ __device__ constexpr uint32_t make_idesc(int M, int N, bool bf16 = false) {
+    return (1u << 4) | (bf16 ? ((1u << 7) | (1u << 10)) : 0u) | ((uint32_t)(N >> 3) << 17) |
+           ((uint32_t)(M >> 4) << 24);
 }
+
+// The 16-bit operand type of the tensor-core pass.
+template <typename T>
+struct Op16;
+template <>
+struct Op16<__half> {
+    using T2 = __half2;
+    static __device__ __forceinline__ T2 pack(float a, float b) { return __floats2half2_rn(a, b); }
+    static __device__ __forceinline__ float lo(T2 v) { return __low2float(v); }
+    static __device__ __forceinline__ float hi(T2 v) { return __high2float(v); }
+    static __device__ __forceinline__ __half one(float v) { return __float2half_rn(v); }
+    static __device__ __forceinline__ float to_float(__half v) { return __half2float(v); }
+    static constexpr double kMax = 65504.0;
+};
+template <>
+struct Op16<__nv_bfloat16> {
+    using T2 = __nv_bfloat162;
+    static __device__ __forceinline__ T2 pack(float a, float b) { return __floats2bfloat162_rn(a, b); }
+    static __device__ __forceinline__ float lo(T2 v) { return __low2float(v); }
+    static __device__ __forceinline__ float hi(T2 v) { return __high2float(v); }
+    static __device__ __forceinline__ __nv_bfloat16 one(float v) { return __float2bfloat16_rn(v); }
+    static __device__ __forceinline__ float to_float(__nv_bfloat16 v) { return __bfloat162float(v); }
+    static constexpr double kMax = 3.3895313892515355e38;
+};
 
 // ---------------------------------------------------------------------------
 // Prep kernels
@@ -350,9 +378,11 @@ __global__ void scale_finalize_kernel(uint32_t *__restrict__ scal) {
 
 // Frames: one warp per row.  xnorm = (||x_hat||^2 in scaled units, upper
 // bound of ||x'||, upper bound of ||x_hat/s - x'||, 0) in unscaled units.
+template <typename T>
 __global__ void prep_frames_kernel(const float *__restrict__ X, int64_t n, int d, int kp,
                                    const float *__restrict__ shift, const uint32_t *__restrict__ scal,
-                                   __half *__restrict__ xh, float4 *__restrict__ xnorm, float norm_inflate) {
+                                   T *__restrict__ xh, float4 *__restrict__ xnorm, float norm_inflate) {
+    using O = Op16<T>;
     const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
     const int lane = threadIdx.x & 31;
@@ -360,7 +390,7 @@ __global__ void prep_frames_kernel(const float *__restrict__ X, int64_t n, int d
     const float inv_sc = 1.0f / sc;  // exact: a power of two
     for (int64_t i = w; i < n; i += nw) {
         const float *src = X + i * d;
-        __half2 *dst = reinterpret_cast<__half2 *>(xh + i * kp);
+        typename O::T2 *dst = reinterpret_cast<typename O::T2 *>(xh + i * kp);
         CSum h2, s2, e2;
         for (int f = 2 * lane; f < kp; f += 64) {
             // Columns < d: centered, scaled frame values; d and d+1: 1 (they
@@ -378,17 +408,17 @@ __global__ void prep_frames_kernel(const float *__restrict__ X, int64_t n, int d
             } else {
                 ib = (f + 1 == d || f + 1 == d + 1) ? 1.0f : 0.0f;
             }
-            const __half2 h = __floats2half2_rn(ia, ib);
+            const typename O::T2 h = O::pack(ia, ib);
             dst[f >> 1] = h;
             if (f < d) {
-                const float ha = __low2float(h);
+                const float ha = O::lo(h);
                 const float ea = ha - ia;
                 h2.add(ha * ha);
                 s2.add(a * a);
                 e2.add(ea * ea);
             }
             if (f + 1 < d) {
-                const float hb = __high2float(h);
+                const float hb = O::hi(h);
                 const float eb = hb - ib;
                 h2.add(hb * hb);
                 s2.add(b * b);
@@ -410,12 +440,13 @@ __global__ void prep_frames_kernel(const float *__restrict__ X, int64_t n, int d
 // shift): each lane owns 4 consecutive columns of every 128-column slice, and
 // all of a row's loads are issued before any of its arithmetic, so a warp
 // keeps the whole row in flight instead of one slice at a time.
-template <int IT>  // 128-column slices per row: IT * 128 >= kp
+template <typename T, int IT>  // 128-column slices per row: IT * 128 >= kp
 __global__ void __launch_bounds__(256, 2) prep_frames_v4_kernel(const float *__restrict__ X, int64_t n, int d,
                                                                 int kp, const float *__restrict__ shift,
                                                                 const uint32_t *__restrict__ scal,
-                                                                __half *__restrict__ xh, float4 *__restrict__ xnorm,
+                                                                T *__restrict__ xh, float4 *__restrict__ xnorm,
                                                                 float norm_inflate) {
+    using O = Op16<T>;
     const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
     const int lane = threadIdx.x & 31;
@@ -457,13 +488,13 @@ __global__ void __launch_bounds__(256, 2) prep_frames_v4_kernel(const float *__r
                 a[e] = c < d ? __fsub_rn(xa[e], sa[e]) : 0.0f;
                 ia[e] = c < d ? a[e] * sc : ((c == d || c == d + 1) ? 1.0f : 0.0f);
             }
-            const __half2 h01 = __floats2half2_rn(ia[0], ia[1]);
-            const __half2 h23 = __floats2half2_rn(ia[2], ia[3]);
+            const typename O::T2 h01 = O::pack(ia[0], ia[1]);
+            const typename O::T2 h23 = O::pack(ia[2], ia[3]);
             uint2 packed;
             packed.x = *reinterpret_cast<const uint32_t *>(&h01);
             packed.y = *reinterpret_cast<const uint32_t *>(&h23);
             *reinterpret_cast<uint2 *>(xh + i * kp + f) = packed;
-            const float hv[4] = {__low2float(h01), __high2float(h01), __low2float(h23), __high2float(h23)};
+            const float hv[4] = {O::lo(h01), O::hi(h01), O::lo(h23), O::hi(h23)};
 #pragma unroll
             for (int e = 0; e < 4; ++e) {
                 if (f + e < d) {
@@ -494,9 +525,11 @@ __global__ void __launch_bounds__(256, 2) prep_frames_v4_kernel(const float *__r
 // hi/lo FP16 split of -||c_hat||^2/2; cnorm = (upper bound of ||c'||, upper
 // bound of ||c_hat/s - c'||).  A norm that FP16 cannot encode poisons cmax
 // (every frame then takes the exact path).
+template <typename T>
 __global__ void prep_centers_kernel(const float *__restrict__ C, int k, int k_pad, int d, int kp,
                                     const float *__restrict__ shift, uint32_t *__restrict__ scal,
-                                    __half *__restrict__ ch, float2 *__restrict__ cnorm, float norm_inflate) {
+                                    T *__restrict__ ch, float2 *__restrict__ cnorm, float norm_inflate) {
+    using O = Op16<T>;
     const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
     const int lane = threadIdx.x & 31;
@@ -504,14 +537,14 @@ __global__ void prep_centers_kernel(const float *__restrict__ C, int k, int k_pa
     const float inv_sc = 1.0f / sc;
     for (int64_t j = w; j < k; j += nw) {
         const float *src = C + j * d;
-        __half2 *dst = reinterpret_cast<__half2 *>(ch + j * kp);
+        typename O::T2 *dst = reinterpret_cast<typename O::T2 *>(ch + j * kp);
         double h2 = 0.0;
         CSum s2, e2;
         for (int f = 2 * lane; f < d; f += 64) {
             const float a = __fsub_rn(src[f], shift[f]);
             const float b = f + 1 < d ? __fsub_rn(src[f + 1], shift[f + 1]) : 0.0f;
-            const __half2 h = __floats2half2_rn(a * sc, b * sc);
-            const float ha = __low2float(h), hb = __high2float(h);
+            const typename O::T2 h = O::pack(a * sc, b * sc);
+            const float ha = O::lo(h), hb = O::hi(h);
             h2 += (double)ha * ha + (double)hb * hb;
             s2.add(a * a);
             const float ea = ha - a * sc;
@@ -529,15 +562,15 @@ __global__ void prep_centers_kernel(const float *__restrict__ C, int k, int k_pa
         __syncwarp();  // the pair writes above land before lane 0 writes columns d, d+1
         if (lane == 0) {
             const double val = -0.5 * tot;
-            const __half hi = __float2half_rn((float)val);
-            const __half lo = __float2half_rn((float)(val - (double)__half2float(hi)));
-            __half *row = ch + j * kp;
+            const T hi = O::one((float)val);
+            const T lo = O::one((float)(val - (double)O::to_float(hi)));
+            T *row = ch + j * kp;
             row[d] = hi;
             row[d + 1] = lo;
             const float nrm = __fsqrt_ru(__fmul_ru((float)ts, norm_inflate));
             const float hc = __fmul_ru(__fadd_ru(__fsqrt_ru(__fmul_ru((float)te, norm_inflate)), 1e-30f), inv_sc);
             cnorm[j] = make_float2(nrm, hc);
-            const bool encodable = fabs(val) < (double)kFp16Max && nrm == nrm && hc == hc;
+            const bool encodable = fabs(val) < O::kMax && nrm == nrm && hc == hc;
             atomicMax(&scal[kCmax], encodable ? __float_as_uint(nrm) : 0x7f800000u);
             atomicMax(&scal[kHcMax], encodable ? __float_as_uint(hc) : 0x7f800000u);
         }
@@ -711,7 +744,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
     } else if (warp == 1) {
         // ---------------- MMA issuer ----------------
         // Converged warp; one elected lane issues the MMAs and commits.
-        const uint32_t idesc = make_idesc(kBM, p.bn);
+        const uint32_t idesc = make_idesc(kBM, p.bn, p.bf16 != 0);
         const uint64_t adesc0 = sw128_desc(smem_u32(sA));
         const uint32_t sb0 = smem_u32(sB);
         const int spt = p.bk >> 4;  // K steps per full stage
@@ -1045,7 +1078,7 @@ EncodeTiledFn get_encode() {
 }
 
 int make_map(CUtensorMap *tm, const void *base, int64_t rows, int kp, int box_rows, int box_k,
-             CUtensorMapSwizzle swizzle) {
+             CUtensorMapSwizzle swizzle, bool bf16) {
     EncodeTiledFn enc = get_encode();
     if (!enc) {
         set_error("cuTensorMapEncodeTiled is not available from the driver");
@@ -1055,7 +1088,8 @@ int make_map(CUtensorMap *tm, const void *base, int64_t rows, int kp, int box_ro
     cuuint64_t strides[1] = {(cuuint64_t)kp * 2};
     cuuint32_t box[2] = {(cuuint32_t)box_k, (cuuint32_t)box_rows};
     cuuint32_t estr[2] = {1, 1};
-    CUresult r = enc(tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, const_cast<void *>(base), dims, strides, box, estr,
+    CUresult r = enc(tm, bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2,
+                     const_cast<void *>(base), dims, strides, box, estr,
                      CU_TENSOR_MAP_INTERLEAVE_NONE, swizzle,
                      CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) {
@@ -1231,34 +1265,43 @@ int tc_prepare_shift_from_centers(const float *C, int d, int k, TcBuffers &b, cu
     return KM_OK;
 }
 
-template <int IT>
+template <typename T, int IT>
 void launch_prep_v4(const float *X, int64_t n, int d, TcBuffers &b, cudaStream_t s) {
-    prep_frames_v4_kernel<IT><<<(unsigned)prep_blocks(n), 256, 0, s>>>(X, n, d, b.kp, b.shift, b.scal,
-                                                                     reinterpret_cast<__half *>(b.xh), b.xnorm,
+    prep_frames_v4_kernel<T, IT><<<(unsigned)prep_blocks(n), 256, 0, s>>>(X, n, d, b.kp, b.shift, b.scal,
+                                                                        reinterpret_cast<T *>(b.xh), b.xnorm,
+                                                                        norm_inflate_of(d));
+}
+
+template <typename T>
+void prepare_frames_t(const float *X, int64_t n, int d, TcBuffers &b, cudaStream_t s) {
+    const int it = (b.kp + 127) / 128;
+    const bool v4 = d % 4 == 0 && it <= 9 &&
+                    ((reinterpret_cast<uintptr_t>(X) | reinterpret_cast<uintptr_t>(b.shift)) & 15) == 0;
+    if (v4) {
+        switch (it) {
+            case 1: launch_prep_v4<T, 1>(X, n, d, b, s); break;
+            case 2: launch_prep_v4<T, 2>(X, n, d, b, s); break;
+            case 3: launch_prep_v4<T, 3>(X, n, d, b, s); break;
+            case 4: launch_prep_v4<T, 4>(X, n, d, b, s); break;
+            case 5: launch_prep_v4<T, 5>(X, n, d, b, s); break;
+            case 6: launch_prep_v4<T, 6>(X, n, d, b, s); break;
+            case 7: launch_prep_v4<T, 7>(X, n, d, b, s); break;
+            case 8: launch_prep_v4<T, 8>(X, n, d, b, s); break;
+            default: launch_prep_v4<T, 9>(X, n, d, b, s); break;
+        }
+    } else {
+        prep_frames_kernel<T><<<(unsigned)prep_blocks(n), 256, 0, s>>>(X, n, d, b.kp, b.shift, b.scal,
+                                                                     reinterpret_cast<T *>(b.xh), b.xnorm,
                                                                      norm_inflate_of(d));
+    }
 }
 
 int tc_prepare_frames(const float *X, int64_t n, int d, TcBuffers &b, cudaStream_t s) {
     if (n == 0) return KM_OK;
-    const int it = (b.kp + 127) / 128;
-    const bool v4 = d % 4 == 0 && it <= 9 && ((reinterpret_cast<uintptr_t>(X) | reinterpret_cast<uintptr_t>(b.shift)) & 15) == 0;
-    if (v4) {
-        switch (it) {
-            case 1: launch_prep_v4<1>(X, n, d, b, s); break;
-            case 2: launch_prep_v4<2>(X, n, d, b, s); break;
-            case 3: launch_prep_v4<3>(X, n, d, b, s); break;
-            case 4: launch_prep_v4<4>(X, n, d, b, s); break;
-            case 5: launch_prep_v4<5>(X, n, d, b, s); break;
-            case 6: launch_prep_v4<6>(X, n, d, b, s); break;
-            case 7: launch_prep_v4<7>(X, n, d, b, s); break;
-            case 8: launch_prep_v4<8>(X, n, d, b, s); break;
-            default: launch_prep_v4<9>(X, n, d, b, s); break;
-        }
-    } else {
-        prep_frames_kernel<<<(unsigned)prep_blocks(n), 256, 0, s>>>(X, n, d, b.kp, b.shift, b.scal,
-                                                                  reinterpret_cast<__half *>(b.xh), b.xnorm,
-                                                                  norm_inflate_of(d));
-    }
+    if (b.bf16)
+        prepare_frames_t<__nv_bfloat16>(X, n, d, b, s);
+    else
+        prepare_frames_t<__half>(X, n, d, b, s);
     KM_CUDA(cudaGetLastError());
     return KM_OK;
 }
@@ -1267,9 +1310,13 @@ int tc_prepare_centers(const float *C, int d, int k, TcBuffers &b, cudaStream_t 
     const int kpad = k_pad_of(k);
     KM_CUDA(cudaMemsetAsync(b.scal + kCmax, 0, 2 * sizeof(uint32_t), s));  // kCmax, kHcMax
     KM_CUDA(cudaMemsetAsync(b.ch, 0, (size_t)kpad * b.kp * 2, s));
-    prep_centers_kernel<<<(unsigned)prep_blocks(kpad), 256, 0, s>>>(C, k, kpad, d, b.kp, b.shift, b.scal,
-                                                                   reinterpret_cast<__half *>(b.ch), b.cnorm,
-                                                                   norm_inflate_of(d));
+    if (b.bf16)
+        prep_centers_kernel<__nv_bfloat16><<<(unsigned)prep_blocks(kpad), 256, 0, s>>>(
+            C, k, kpad, d, b.kp, b.shift, b.scal, reinterpret_cast<__nv_bfloat16 *>(b.ch), b.cnorm,
+            norm_inflate_of(d));
+    else
+        prep_centers_kernel<__half><<<(unsigned)prep_blocks(kpad), 256, 0, s>>>(
+            C, k, kpad, d, b.kp, b.shift, b.scal, reinterpret_cast<__half *>(b.ch), b.cnorm, norm_inflate_of(d));
     KM_CUDA(cudaGetLastError());
     return KM_OK;
 }
@@ -1290,9 +1337,9 @@ int tc_assign(const float *X, int64_t n, int d, const float *C, int k, int32_t *
     KM_CUDA(attr_err);
 
     CUtensorMap tmA, tmB;
-    KM_TRY(make_map(&tmA, b.xh, n, b.kp, kBM, kKC, CU_TENSOR_MAP_SWIZZLE_128B));
+    KM_TRY(make_map(&tmA, b.xh, n, b.kp, kBM, kKC, CU_TENSOR_MAP_SWIZZLE_128B, b.bf16 != 0));
     KM_TRY(make_map(&tmB, b.ch, k_pad_of(k), b.kp, pl.bn, pl.bk,
-                    pl.bk == kKC ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B));
+                    pl.bk == kKC ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B, b.bf16 != 0));
 
     KM_CUDA(cudaMemsetAsync(b.counters, 0, 4 * sizeof(int32_t), s));
     KM_CUDA(cudaMemsetAsync(b.flipped, 0, sizeof(unsigned long long), s));
@@ -1314,7 +1361,10 @@ int tc_assign(const float *X, int64_t n, int d, const float *C, int k, int32_t *
     p.n_ctiles = (k + pl.bn - 1) / pl.bn;
     p.tmem_cols = pl.tmem_cols;
     const double gamma_acc = (b.kp / 16 + 1) * std::ldexp(1.0, -21);
-    p.e_coef = (float)((gamma_acc * 1.003 + std::ldexp(1.0, -21) + 8.0 * u) * 1.01);
+    // The hi/lo split of -||c_hat||^2/2 leaves at most 2^-24 (FP16) or 2^-18
+    // (BF16) of it; the bound allows 2^-21 and 2^-17.
+    p.bf16 = b.bf16;
+    p.e_coef = (float)((gamma_acc * 1.003 + std::ldexp(1.0, b.bf16 ? -17 : -21) + 8.0 * u) * 1.01);
     const double g = (d + 2) * u / (1.0 - (d + 2) * u) * 1.01;
     p.g_lo = (float)((1.0 - g) * (1.0 - 4.0 * u));
     p.g_hi = (float)((1.0 + g) * (1.0 + 4.0 * u));

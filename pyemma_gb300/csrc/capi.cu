@@ -90,6 +90,9 @@ void ProfEvents::collect() {
 
 namespace {
 
+// The tensor-core precisions (FP16 or BF16 operands, exact re-check).
+inline bool is_tc(int prec) { return prec == KM_PREC_FP16 || prec == KM_PREC_BF16; }
+
 // Precisions chosen by km_tune, per (d, k).
 struct TuneCache {
     std::mutex m;
@@ -117,7 +120,7 @@ struct AssignWs {
 };
 
 size_t assign_ws_bytes(int64_t n, int d, int k, int prec) {
-    if (prec != KM_PREC_FP16) return 0;
+    if (!is_tc(prec)) return 0;
     return tc_frames_ws_size(n, d) + tc_centers_ws_size(d, k) + tc_assign_ws_size(n, d, k) + 3 * 256;
 }
 
@@ -143,7 +146,8 @@ int check_device_errors(uint32_t e) {
 }
 
 // The assignment once the precision is resolved and the workspace checked.
-// For KM_PREC_FP16, b holds the carved buffers; centers_ready means the
+// For the tensor-core precisions, b holds the carved buffers (b.bf16 set);
+// centers_ready means the
 // center half (FP16 copy, norms, shift, scale) is already prepared.
 int assign_core(const float *X, int64_t n, int32_t d, const float *C, int32_t k, int prec, int32_t *labels,
                 TcBuffers &b, bool centers_ready, km_assign_stats *stats, cudaStream_t s) {
@@ -202,23 +206,26 @@ int assign_impl(const float *X, int64_t n, int32_t d, const float *C, int32_t k,
         return KM_ERR_BAD_SHAPE;
     }
     int prec = resolve_precision(precision, d, k, true);
-    if (prec != KM_PREC_FP32 && prec != KM_PREC_FP16) {
+    if (prec != KM_PREC_FP32 && !is_tc(prec)) {
         set_error("unknown precision %d", precision);
         return KM_ERR_BAD_SHAPE;
     }
-    if (prec == KM_PREC_FP16 && !tc_supported(d, k)) {
+    if (is_tc(prec) && !tc_supported(d, k)) {
         set_error("no tensor-core kernel for d=%d, k=%d on this device", d, k);
         return KM_ERR_UNSUPPORTED;
     }
     KM_TRY(check_ws(ws, ws_bytes, assign_ws_bytes(n, d, k, prec)));
     TcBuffers b;
-    if (prec == KM_PREC_FP16 && n > 0) carve_assign(ws, n, d, k, b);
+    if (is_tc(prec) && n > 0) {
+        carve_assign(ws, n, d, k, b);
+        b.bf16 = prec == KM_PREC_BF16;
+    }
     return assign_core(X, n, d, C, k, prec, labels, b, false, stats, s);
 }
 
 // Workspace of an assignment whose centers are prepared: frames + lists.
 size_t resident_ws_bytes(int64_t n, int d, int k, int prec) {
-    if (prec != KM_PREC_FP16) return 0;
+    if (!is_tc(prec)) return 0;
     return tc_frames_ws_size(n, d) + tc_assign_ws_size(n, d, k) + 2 * 256;
 }
 
@@ -244,7 +251,7 @@ struct km_centers {
     void *mem = nullptr;
     size_t bytes = 0;
     float *C = nullptr;
-    TcBuffers tc;  // center half: ch, cnorm, shift, scal (KM_PREC_FP16)
+    TcBuffers tc;  // center half: ch, cnorm, shift, scal (tensor-core precisions)
 };
 
 namespace km {
@@ -445,7 +452,7 @@ int km_lloyd(const float *X, int64_t n, int32_t d, int32_t k, float *C, int32_t 
     *n_iter = 0;
     *converged = 0;
     int prec = resolve_precision(precision, d, k, true);
-    if (prec == KM_PREC_FP16 && !tc_supported(d, k)) {
+    if (is_tc(prec) && !tc_supported(d, k)) {
         set_error("no tensor-core kernel for d=%d, k=%d on this device", d, k);
         return KM_ERR_UNSUPPORTED;
     }
@@ -462,10 +469,11 @@ int km_lloyd(const float *X, int64_t n, int32_t d, int32_t k, float *C, int32_t 
     void *ws_assign = cv.take<char>(assign_ws_bytes(n, d, k, prec));
 
     TcBuffers b;
-    if (prec == KM_PREC_FP16) {
-        // The shift and scale stay fixed for the whole run so that the FP16 frame copy
-        // is made once.
+    if (is_tc(prec)) {
+        // The shift and scale stay fixed for the whole run so that the 16-bit
+        // frame copy is made once.
         carve_assign(ws_assign, n, d, k, b);
+        b.bf16 = prec == KM_PREC_BF16;
         KM_TRY(tc_prepare_shift_from_centers(C, d, k, b, s));
         KM_TRY(tc_prepare_frames(X, n, d, b, s));
     }
@@ -481,7 +489,7 @@ int km_lloyd(const float *X, int64_t n, int32_t d, int32_t k, float *C, int32_t 
         ~Closer() { p.close(); }
     } closer{prof};
     auto enqueue = [&](cudaStream_t st) -> int {
-        if (prec == KM_PREC_FP16) {
+        if (is_tc(prec)) {
             KM_TRY(tc_prepare_centers(C, d, k, b, st));
             KM_TRY(tc_assign(X, n, d, C, k, labels, b, st, &prof));
         } else {
@@ -534,7 +542,7 @@ int km_lloyd(const float *X, int64_t n, int32_t d, int32_t k, float *C, int32_t 
         uint32_t h_err = 0, tc_err = 0;
         cudaError_t e = cudaMemcpyAsync(&h_cost, cost, sizeof(double), cudaMemcpyDeviceToHost, s);
         if (e == cudaSuccess) e = cudaMemcpyAsync(&h_err, err, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
-        if (e == cudaSuccess && prec == KM_PREC_FP16)
+        if (e == cudaSuccess && is_tc(prec))
             e = cudaMemcpyAsync(&tc_err, b.err, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
         if (e == cudaSuccess) e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) {
@@ -573,11 +581,11 @@ int km_centers_create(const float *C, int32_t k, int32_t d, int32_t precision, v
         return KM_ERR_BAD_SHAPE;
     }
     const int prec = resolve_precision(precision, d, k, true);
-    if (prec != KM_PREC_FP32 && prec != KM_PREC_FP16) {
+    if (prec != KM_PREC_FP32 && !is_tc(prec)) {
         set_error("unknown precision %d", precision);
         return KM_ERR_BAD_SHAPE;
     }
-    if (prec == KM_PREC_FP16 && !tc_supported(d, k)) {
+    if (is_tc(prec) && !tc_supported(d, k)) {
         set_error("no tensor-core kernel for d=%d, k=%d on this device", d, k);
         return KM_ERR_UNSUPPORTED;
     }
@@ -588,7 +596,7 @@ int km_centers_create(const float *C, int32_t k, int32_t d, int32_t precision, v
     h->prec = prec;
     cudaGetDevice(&h->device);
     const size_t c_bytes = ((size_t)k * d * sizeof(float) + 255) / 256 * 256;
-    h->bytes = c_bytes + (prec == KM_PREC_FP16 ? tc_centers_ws_size(d, k) : 0);
+    h->bytes = c_bytes + (is_tc(prec) ? tc_centers_ws_size(d, k) : 0);
     cudaError_t e = cudaMalloc(&h->mem, h->bytes);
     if (e != cudaSuccess) {
         delete h;
@@ -598,8 +606,9 @@ int km_centers_create(const float *C, int32_t k, int32_t d, int32_t precision, v
     int st = KM_OK;
     e = cudaMemcpyAsync(h->C, C, (size_t)k * d * sizeof(float), cudaMemcpyDeviceToDevice, s);
     if (e != cudaSuccess) st = cuda_fail(e, "cudaMemcpyAsync (resident centers)");
-    if (st == KM_OK && prec == KM_PREC_FP16) {
+    if (st == KM_OK && is_tc(prec)) {
         tc_carve_centers(static_cast<char *>(h->mem) + c_bytes, d, k, h->tc);
+        h->tc.bf16 = prec == KM_PREC_BF16;
         st = tc_prepare_shift_from_centers(h->C, d, k, h->tc, s);
         if (st == KM_OK) st = tc_prepare_centers(h->C, d, k, h->tc, s);
     }
@@ -662,7 +671,7 @@ int km_assign_centers(const float *X, int64_t n, int32_t d, const km_centers *h,
     }
     KM_TRY(check_ws(workspace, workspace_bytes, resident_ws_bytes(n, d, h->k, h->prec)));
     TcBuffers b;
-    if (h->prec == KM_PREC_FP16 && n > 0) {
+    if (is_tc(h->prec) && n > 0) {
         b = h->tc;  // prepared center half; the carves below fill the frame and list fields
         char *p = static_cast<char *>(workspace);
         tc_carve_frames(p, n, d, b);

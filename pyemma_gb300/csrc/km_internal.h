@@ -97,6 +97,7 @@ struct TcBuffers {
     unsigned long long *flipped = nullptr;
     uint32_t *err = nullptr;
     int kp = 0;
+    int bf16 = 0;  // operand type of xh / ch: 0 FP16, 1 BF16
 };
 
 void tc_carve_frames(void *ws, int64_t n, int d, TcBuffers &b);
