@@ -222,6 +222,9 @@ int launch_assign_fp32(const float *X, const int32_t *frame_idx, const int32_t *
     if (k <= 32) return launch_cfg<4, 1>(X, frame_idx, n_dev, n, d, C, k, labels, dist, flipped, s);
     if (k <= 64) return launch_cfg<4, 2>(X, frame_idx, n_dev, n, d, C, k, labels, dist, flipped, s);
     if (k <= 128) return launch_cfg<4, 4>(X, frame_idx, n_dev, n, d, C, k, labels, dist, flipped, s);
+    // Narrow frames: more frames per thread, so each shared-memory center
+    // value feeds more distances (the chunk loop is short at small d).
+    if (d <= 32) return launch_cfg<8, 8>(X, frame_idx, n_dev, n, d, C, k, labels, dist, flipped, s);
     return launch_cfg<4, 8>(X, frame_idx, n_dev, n, d, C, k, labels, dist, flipped, s);
 }
 
