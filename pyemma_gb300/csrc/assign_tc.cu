@@ -80,8 +80,7 @@ struct TcParams {
     int kp;
     int nkc;
     int ksteps_total;  // 16-wide K steps holding data (ceil((d+2)/16))
-    int bk;            // K columns per B stage: 64 (128-byte swizzle) or 32 (64-byte swizzle)
-    int nbst;          // B stages per center tile (ceil(ksteps_total * 16 / bk))
+    int nbst;          // B stages per center tile (64 K columns each): ceil(ksteps_total / 4)
     int bn;
     int stages;
     int stream_a;  // 1: A chunks travel with the B stages instead of staying resident (large d)
@@ -254,8 +253,6 @@ __device__ __forceinline__ void tmem_wait_ld() {
 
 // Shared-memory matrix descriptor: K-major operand in the 128-byte swizzle
 // layout written by TMA (8-row atoms of 128 B, atoms 1024 B apart).
-__device__ __forceinline__ uint64_t sw64_desc(uint32_t saddr);
-
 __device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
     uint64_t desc = 0;
     desc |= (uint64_t)((saddr & 0x3FFFFu) >> 4);  // start address
@@ -263,17 +260,6 @@ __device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
     desc |= (uint64_t)(1024 >> 4) << 32;          // stride byte offset: 8 rows x 128 B
     desc |= (uint64_t)1 << 46;                    // descriptor version
     desc |= (uint64_t)2 << 61;                    // 128-byte swizzle
-    return desc;
-}
-
-// Same for the 64-byte swizzle (8-row atoms of 64 B, atoms 512 B apart).
-__device__ __forceinline__ uint64_t sw64_desc(uint32_t saddr) {
-    uint64_t desc = 0;
-    desc |= (uint64_t)((saddr & 0x3FFFFu) >> 4);  // start address
-    desc |= (uint64_t)1 << 16;                    // leading byte offset (unused for swizzled K-major)
-    desc |= (uint64_t)(512 >> 4) << 32;           // stride byte offset: 8 rows x 64 B
-    desc |= (uint64_t)1 << 46;                    // descriptor version
-    desc |= (uint64_t)4 << 61;                    // 64-byte swizzle
     return desc;
 }
 
@@ -623,10 +609,9 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
     const int nab = stream ? 0 : p.nkc;  // resident A chunks (and their barrier pairs)
     uint8_t *sA = smem;
     uint8_t *sB = sA + nab * kABytesPerChunk;
-    const int b_stage_bytes = p.bn * p.bk * 2;
+    const int b_stage_bytes = p.bn * kKC * 2;
     const int stage_bytes = b_stage_bytes + (stream ? kABytesPerChunk : 0);
     const int b_off = stream ? kABytesPerChunk : 0;  // B within a stage
-    const int spc = kKC / p.bk;  // B stages per A chunk (1 or 2; 1 when streaming)
     uint64_t *bars = reinterpret_cast<uint64_t *>(sB + p.stages * stage_bytes);
     uint64_t *a_full = bars;
     uint64_t *a_empty = a_full + nab;
@@ -673,8 +658,9 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
         // ---------------- TMA producer ----------------
         // The whole warp runs the loop (waits by all lanes, agreed by vote);
         // one elected lane issues the copies.  Per center tile: B stages
-        // t = 0..nbst-1 (bk K-columns each); the A chunk kc = t/spc (64
-        // K-columns) is loaded with its first stage on the first center tile.
+        // t = 0..nbst-1 of 64 K-columns each; in the resident form the A
+        // chunk t (the same 64 columns) is loaded with stage t of the first
+        // center tile, in the streaming form it travels inside every stage.
         // Stage index and phase advance incrementally; a failed wait clears
         // ok and stops the issues, and the warp agrees on ok once per center
         // tile.  `issued` counts the B stages actually loaded (for the drain).
@@ -688,13 +674,12 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
         for (int64_t ft = blockIdx.x; ft < n_ftiles && ok; ft += gridDim.x, ++t_local) {
             const int frame_row = (int)(ft * kBM);
             for (int ct = 0; ct < p.n_ctiles && ok; ++ct) {
-                int kc = 0, half = 0;
                 for (int t = 0; t < p.nbst; ++t) {
-                    if (!stream && ct == 0 && half == 0) {
-                        if (ok) ok = mbar_wait_timed(&a_empty[kc], (t_local & 1u) ^ 1u, pw_a);
+                    if (!stream && ct == 0) {
+                        if (ok) ok = mbar_wait_timed(&a_empty[t], (t_local & 1u) ^ 1u, pw_a);
                         if (elect_one() && ok) {
-                            mbar_arrive_expect_tx(&a_full[kc], kABytesPerChunk);
-                            tma_load_2d(sA + kc * kABytesPerChunk, &tmA, kc * kKC, frame_row, &a_full[kc]);
+                            mbar_arrive_expect_tx(&a_full[t], kABytesPerChunk);
+                            tma_load_2d(sA + t * kABytesPerChunk, &tmA, t * kKC, frame_row, &a_full[t]);
                         }
                         __syncwarp();
                     }
@@ -703,17 +688,13 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                         uint8_t *st = sB + s * stage_bytes;
                         mbar_arrive_expect_tx(&b_full[s], stage_bytes);
                         if (stream) tma_load_2d(st, &tmA, t * kKC, frame_row, &b_full[s]);
-                        tma_load_2d(st + b_off, &tmB, t * p.bk, ct * p.bn, &b_full[s]);
+                        tma_load_2d(st + b_off, &tmB, t * kKC, ct * p.bn, &b_full[s]);
                         ++issued;
                     }
                     __syncwarp();
                     if (++s == (uint32_t)p.stages) {
                         s = 0;
                         sph ^= 1u;
-                    }
-                    if (++half == spc) {
-                        half = 0;
-                        ++kc;
                     }
                 }
                 if (ct == 0) a_issued_tiles += 1;
@@ -743,57 +724,60 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
         __syncwarp();
     } else if (warp == 1) {
         // ---------------- MMA issuer ----------------
-        // Converged warp; one elected lane issues the MMAs and commits.
+        // Converged warp; one elected lane issues the MMAs and commits.  The
+        // shared-memory descriptors advance by adding to their start-address
+        // field (addresses stay below 256 KB); a failed wait clears ok and
+        // stops the issues (the elected lane, lane 0 of the converged warp,
+        // decides by its own wait), and the warp agrees on ok once per
+        // center tile.
         const uint32_t idesc = make_idesc(kBM, p.bn, p.bf16 != 0);
         const uint64_t adesc0 = sw128_desc(smem_u32(sA));
-        const uint32_t sb0 = smem_u32(sB);
-        const int spt = p.bk >> 4;  // K steps per full stage
-        uint32_t bq = 0, accq = 0, t_local = 0;
+        const uint64_t sdesc0 = sw128_desc(smem_u32(sB));
+        const uint64_t sstep = (uint64_t)(stage_bytes >> 4);
+        const uint64_t boff = (uint64_t)(b_off >> 4);
+        const uint64_t astep = (uint64_t)(kABytesPerChunk >> 4);
+        const int last_steps = p.ksteps_total - 4 * (p.nbst - 1);  // 1..4
+        uint32_t accq = 0, t_local = 0;
         bool ok = true;
         unsigned long long w_b = 0, w_a = 0, w_acc = 0;
         const long long t_start = clock64();
         unsigned long long *pw_b = (p.wait_cycles && lane == 0) ? &w_b : nullptr;
         unsigned long long *pw_a = (p.wait_cycles && lane == 0) ? &w_a : nullptr;
         unsigned long long *pw_acc = (p.wait_cycles && lane == 0) ? &w_acc : nullptr;
-        // Stage index and phase advance incrementally (no divisions in the
-        // loop); a failed wait clears ok and stops the issues (the elected
-        // lane, lane 0 of the converged warp, decides by its own wait), and
-        // the warp agrees on ok once per center tile.
-        const bool wide_b = p.bk == kKC;
         uint32_t s = 0, sph = 0;  // B stage and its phase
+        uint64_t sdesc = sdesc0;  // descriptor of stage s
         for (int64_t ft = blockIdx.x; ft < n_ftiles && ok; ft += gridDim.x, ++t_local) {
             for (int ct = 0; ct < p.n_ctiles && ok; ++ct) {
                 const uint32_t buf = accq & 1u;
                 ok = mbar_wait_timed(&acc_empty[buf], ((accq >> 1) & 1u) ^ 1u, pw_acc);
                 tc_fence_after();
                 const uint32_t d_tmem = tmem_base + buf * (uint32_t)p.bn;
-                int kc = 0, half = 0;
+                const bool first = ct == 0, last = ct == p.n_ctiles - 1;
+                uint64_t ad = adesc0;
                 for (int t = 0; t < p.nbst; ++t) {
-                    if (!stream && ct == 0 && half == 0 && ok) ok = mbar_wait_timed(&a_full[kc], t_local & 1u, pw_a);
+                    if (!stream && first && ok) ok = mbar_wait_timed(&a_full[t], t_local & 1u, pw_a);
                     if (ok) ok = mbar_wait_timed(&b_full[s], sph, pw_b);
                     // TMA completion on the mbarrier orders the loaded tiles before
                     // the MMAs; no tcgen05 fence is needed here.
-                    const int steps = min(spt, p.ksteps_total - spt * t);
-                    const uint32_t st0 = sb0 + s * stage_bytes;
-                    const uint64_t a_d =
-                        stream ? sw128_desc(st0) : adesc0 + (uint64_t)((kc * kABytesPerChunk + half * p.bk * 2) >> 4);
-                    const uint64_t bd = wide_b ? sw128_desc(st0 + b_off) : sw64_desc(st0 + b_off);
+                    const uint64_t a_d = stream ? sdesc : ad;
+                    const uint64_t b_d = sdesc + boff;
+                    const int steps = t == p.nbst - 1 ? last_steps : 4;
                     if (elect_one() && ok) {
+                        mma_f16(d_tmem, a_d, b_d, idesc, t != 0);
 #pragma unroll
-                        for (int kk = 0; kk < 4; ++kk)  // 32-byte K steps: +2 in the start-address field
-                            if (kk < steps) mma_f16(d_tmem, a_d + 2 * kk, bd + 2 * kk, idesc, (t | kk) != 0);
+                        for (int kk = 1; kk < 4; ++kk)  // 32-byte K steps: +2 in the start-address field
+                            if (kk < steps) mma_f16(d_tmem, a_d + 2 * kk, b_d + 2 * kk, idesc, 1u);
                         mma_commit(&b_empty[s]);
-                        if (!stream && ct == p.n_ctiles - 1 && (half == spc - 1 || t == p.nbst - 1))
-                            mma_commit(&a_empty[kc]);
+                        if (!stream && last) mma_commit(&a_empty[t]);
                     }
                     __syncwarp();
+                    ad += astep;
                     if (++s == (uint32_t)p.stages) {
                         s = 0;
                         sph ^= 1u;
-                    }
-                    if (++half == spc) {
-                        half = 0;
-                        ++kc;
+                        sdesc = sdesc0;
+                    } else {
+                        sdesc += sstep;
                     }
                 }
                 ok = __all_sync(0xffffffffu, ok);
@@ -1110,38 +1094,25 @@ int pick_bn(int k) {
 
 int k_pad_of(int k) { return (k + 255) / 256 * 256; }
 
-// K columns per B stage: 64 (one 128-byte swizzle row) by default.
-int pick_bk(int d, int k) {
-    (void)d;
-    (void)k;
-    return 64;
-}
-
 struct Plan {
-    int bn, bk, stages, nkc, smem, stream_a;
+    int bn, stages, nkc, smem, stream_a;
     uint32_t tmem_cols;
 };
 
 bool make_plan(int d, int k, Plan &pl) {
     pl.nkc = kp_of(d) / kKC;
     pl.bn = pick_bn(k);
-    pl.bk = pick_bk(d, k);
     pl.stream_a = 0;
     const int fixed = 1024 + 512;
     int stages = 0;
     if (pl.nkc <= kMaxNkc) {
         const int res = fixed + pl.nkc * kABytesPerChunk;
-        stages = std::min(8, (kSmemLimit - res) / (pl.bn * pl.bk * 2));
-        if (stages < 2 && pl.bk == kKC) {
-            pl.bk = kKC / 2;  // narrower stages when two wide ones do not fit
-            stages = std::min(8, (kSmemLimit - res) / (pl.bn * pl.bk * 2));
-        }
-        if (stages >= 2) pl.smem = res + stages * pl.bn * pl.bk * 2;
+        stages = std::min(8, (kSmemLimit - res) / (pl.bn * kKC * 2));
+        if (stages >= 2) pl.smem = res + stages * pl.bn * kKC * 2;
     }
     if (stages < 2) {
         // Streaming: each stage carries an A chunk and a full-width B chunk.
         pl.stream_a = 1;
-        pl.bk = kKC;
         stages = std::min(8, (kSmemLimit - fixed) / (kABytesPerChunk + pl.bn * kKC * 2));
         if (stages < 2) return false;
         pl.smem = fixed + stages * (kABytesPerChunk + pl.bn * kKC * 2);
@@ -1338,8 +1309,7 @@ int tc_assign(const float *X, int64_t n, int d, const float *C, int k, int32_t *
 
     CUtensorMap tmA, tmB;
     KM_TRY(make_map(&tmA, b.xh, n, b.kp, kBM, kKC, CU_TENSOR_MAP_SWIZZLE_128B, b.bf16 != 0));
-    KM_TRY(make_map(&tmB, b.ch, k_pad_of(k), b.kp, pl.bn, pl.bk,
-                    pl.bk == kKC ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B, b.bf16 != 0));
+    KM_TRY(make_map(&tmB, b.ch, k_pad_of(k), b.kp, pl.bn, kKC, CU_TENSOR_MAP_SWIZZLE_128B, b.bf16 != 0));
 
     KM_CUDA(cudaMemsetAsync(b.counters, 0, 4 * sizeof(int32_t), s));
     KM_CUDA(cudaMemsetAsync(b.flipped, 0, sizeof(unsigned long long), s));
@@ -1353,9 +1323,8 @@ int tc_assign(const float *X, int64_t n, int d, const float *C, int k, int32_t *
     p.kp = b.kp;
     p.nkc = pl.nkc;
     p.ksteps_total = (d + 2 + 15) / 16;
-    p.bk = pl.bk;
     p.stream_a = pl.stream_a;
-    p.nbst = (p.ksteps_total * 16 + pl.bk - 1) / pl.bk;
+    p.nbst = (p.ksteps_total + 3) / 4;
     p.bn = pl.bn;
     p.stages = pl.stages;
     p.n_ctiles = (k + pl.bn - 1) / pl.bn;
