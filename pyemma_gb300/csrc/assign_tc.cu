@@ -55,6 +55,7 @@
 #include <cuda_fp16.h>
 
 #include <cmath>
+#include <cstdlib>
 #include <mutex>
 
 namespace km {
@@ -232,6 +233,108 @@ __device__ __forceinline__ void mma_commit(uint64_t *bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                      smem_u32(bar))
                  : "memory");
+}
+
+// ---- CTA pairs (cluster of 2, tcgen05 cta_group::2) ----
+__device__ __forceinline__ uint32_t cluster_ctarank() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+
+// Address of the same shared-memory offset in CTA `rank` of the cluster.
+__device__ __forceinline__ uint32_t mapa_shared(uint32_t addr, uint32_t rank) {
+    uint32_t r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(addr), "r"(rank));
+    return r;
+}
+
+// Every thread of both CTAs.
+__device__ __forceinline__ void cluster_sync_all() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+// Arrive on a barrier of either CTA of the pair.  The default (CTA-scope)
+// release: the arrive only has to follow the thread's completed tcgen05.ld of
+// the accumulator (ordered by tcgen05.fence::before_thread_sync), not its
+// global stores, which a cluster-scope release would wait for.
+__device__ __forceinline__ void mbar_arrive_cluster(uint32_t cluster_addr) {
+    asm volatile("mbarrier.arrive.shared::cluster.b64 _, [%0];" ::"r"(cluster_addr) : "memory");
+}
+
+// Wait on a local barrier that threads of the peer CTA arrive on.
+__device__ __forceinline__ bool mbar_try_wait_cluster(uint64_t *bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+__device__ __forceinline__ bool mbar_wait_cluster(uint64_t *bar, uint32_t parity) {
+    if (mbar_try_wait_cluster(bar, parity)) return true;
+    const uint64_t t0 = globaltimer_ns();
+    for (uint32_t spin = 1;; ++spin) {
+        if (mbar_try_wait_cluster(bar, parity)) return true;
+        if ((spin & 255u) == 0 && globaltimer_ns() - t0 > kWaitLimitNs) return false;
+    }
+}
+
+__device__ __forceinline__ bool mbar_wait_cluster_timed(uint64_t *bar, uint32_t parity, unsigned long long *acc) {
+    if (!acc) return mbar_wait_cluster(bar, parity);
+    const long long t0 = clock64();
+    const bool ok = mbar_wait_cluster(bar, parity);
+    *acc += (unsigned long long)(clock64() - t0);
+    return ok;
+}
+
+// TMA load into this CTA's shared memory whose completion is counted on the
+// barrier at `bar_cluster_addr` (the leader CTA's).
+__device__ __forceinline__ void tma_load_2d_pair(void *dst, const CUtensorMap *tm, int x, int y,
+                                                 uint32_t bar_cluster_addr) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.cta_group::2.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, "
+        "%3}], [%4];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(tm)), "r"(x), "r"(y), "r"(bar_cluster_addr)
+        : "memory");
+}
+
+__device__ __forceinline__ void tmem_alloc_pair(uint32_t *holder, uint32_t ncols) {
+    asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(holder)),
+                 "r"(ncols)
+                 : "memory");
+}
+
+__device__ __forceinline__ void tmem_relinquish_pair() {
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_dealloc_pair(uint32_t taddr, uint32_t ncols) {
+    asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+
+__device__ __forceinline__ void mma_f16_pair(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                              uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::2.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+// Arrive on the barrier at this offset in both CTAs of the pair once the
+// issuing thread's earlier MMAs are complete.
+__device__ __forceinline__ void mma_commit_pair(uint64_t *bar) {
+    asm volatile(
+        "tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(
+            smem_u32(bar)),
+        "h"((unsigned short)3)
+        : "memory");
 }
 
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
@@ -597,6 +700,14 @@ __device__ __forceinline__ float window_threshold(float best, float xn2, float i
     return __fsub_rd(t, __fmul_ru(fabsf(t), 1e-6f)) - 1e-30f;
 }
 
+// PAIR: a cluster of two CTAs on two SMs computes M = 256 tiles with
+// tcgen05 cta_group::2.  Each CTA keeps its own 128 frames (A) resident and
+// loads half of every 256-center B stage; the leader CTA (rank 0) issues the
+// MMAs, which read A and B from both CTAs' shared memory and write each CTA's
+// own accumulator rows.  All barriers the MMAs wait on live in the leader
+// (the peer's copies and accumulator releases arrive there); the MMA commits
+// arrive in both CTAs.
+template <bool PAIR>
 __global__ void __launch_bounds__(kThreadsTC, 1)
     tc_assign_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                      const TcParams p) {
@@ -609,7 +720,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
     const int nab = stream ? 0 : p.nkc;  // resident A chunks (and their barrier pairs)
     uint8_t *sA = smem;
     uint8_t *sB = sA + nab * kABytesPerChunk;
-    const int b_stage_bytes = p.bn * kKC * 2;
+    const int b_stage_bytes = (PAIR ? p.bn / 2 : p.bn) * kKC * 2;
     const int stage_bytes = b_stage_bytes + (stream ? kABytesPerChunk : 0);
     const int b_off = stream ? kABytesPerChunk : 0;  // B within a stage
     uint64_t *bars = reinterpret_cast<uint64_t *>(sB + p.stages * stage_bytes);
@@ -625,6 +736,14 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
 
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
+    const uint32_t rank = PAIR ? cluster_ctarank() : 0u;
+    const bool leader = rank == 0;
+    // Frame units: 128 frames per CTA; a pair takes 256 consecutive frames,
+    // its rank-r CTA the r-th half.
+    const int64_t unit = PAIR ? 2 * kBM : kBM;
+    const int64_t n_units = (p.n + unit - 1) / unit;
+    const int64_t unit0 = PAIR ? blockIdx.x / 2 : blockIdx.x;
+    const int64_t unit_stride = PAIR ? gridDim.x / 2 : gridDim.x;
 
     if (threadIdx.x == 0) {
         for (int c = 0; c < nab; ++c) {
@@ -637,22 +756,26 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
         }
         for (int b = 0; b < 2; ++b) {
             mbar_init(&acc_full[b], 1);
-            mbar_init(&acc_empty[b], 4);
+            mbar_init(&acc_empty[b], PAIR ? 8 : 4);  // the epilogue warps of one or both CTAs
         }
         mbar_init(drain, 1);
         *abort_flag = 0;
         fence_mbar_init();
     }
     if (warp == 1) {
-        tmem_alloc(tmem_holder, p.tmem_cols);
-        tmem_relinquish();
+        if (PAIR) {  // one warp of each CTA of the pair
+            tmem_alloc_pair(tmem_holder, p.tmem_cols);
+            tmem_relinquish_pair();
+        } else {
+            tmem_alloc(tmem_holder, p.tmem_cols);
+            tmem_relinquish();
+        }
     }
     tc_fence_before();
     __syncthreads();
+    if (PAIR) cluster_sync_all();  // both CTAs' barriers are initialised before any remote arrive
     tc_fence_after();
     const uint32_t tmem_base = *tmem_holder;
-
-    const int64_t n_ftiles = (p.n + kBM - 1) / kBM;
 
     if (warp == 0) {
         // ---------------- TMA producer ----------------
@@ -671,24 +794,36 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
         unsigned long long *pw_b = (p.wait_cycles && lane == 0) ? &w_b : nullptr;
         unsigned long long *pw_a = (p.wait_cycles && lane == 0) ? &w_a : nullptr;
         uint32_t s = 0, sph = 0;
-        for (int64_t ft = blockIdx.x; ft < n_ftiles && ok; ft += gridDim.x, ++t_local) {
-            const int frame_row = (int)(ft * kBM);
+        for (int64_t ft = unit0; ft < n_units && ok; ft += unit_stride, ++t_local) {
+            const int frame_row = (int)(ft * unit + rank * kBM);
             for (int ct = 0; ct < p.n_ctiles && ok; ++ct) {
                 for (int t = 0; t < p.nbst; ++t) {
                     if (!stream && ct == 0) {
                         if (ok) ok = mbar_wait_timed(&a_empty[t], (t_local & 1u) ^ 1u, pw_a);
                         if (elect_one() && ok) {
-                            mbar_arrive_expect_tx(&a_full[t], kABytesPerChunk);
-                            tma_load_2d(sA + t * kABytesPerChunk, &tmA, t * kKC, frame_row, &a_full[t]);
+                            if (PAIR) {
+                                if (leader) mbar_arrive_expect_tx(&a_full[t], 2 * kABytesPerChunk);
+                                tma_load_2d_pair(sA + t * kABytesPerChunk, &tmA, t * kKC, frame_row,
+                                                 mapa_shared(smem_u32(&a_full[t]), 0));
+                            } else {
+                                mbar_arrive_expect_tx(&a_full[t], kABytesPerChunk);
+                                tma_load_2d(sA + t * kABytesPerChunk, &tmA, t * kKC, frame_row, &a_full[t]);
+                            }
                         }
                         __syncwarp();
                     }
                     if (ok) ok = mbar_wait_timed(&b_empty[s], sph ^ 1u, pw_b);
                     if (elect_one() && ok) {
                         uint8_t *st = sB + s * stage_bytes;
-                        mbar_arrive_expect_tx(&b_full[s], stage_bytes);
-                        if (stream) tma_load_2d(st, &tmA, t * kKC, frame_row, &b_full[s]);
-                        tma_load_2d(st + b_off, &tmB, t * kKC, ct * p.bn, &b_full[s]);
+                        if (PAIR) {
+                            if (leader) mbar_arrive_expect_tx(&b_full[s], 2 * stage_bytes);
+                            tma_load_2d_pair(st, &tmB, t * kKC, ct * p.bn + (int)rank * (p.bn / 2),
+                                             mapa_shared(smem_u32(&b_full[s]), 0));
+                        } else {
+                            mbar_arrive_expect_tx(&b_full[s], stage_bytes);
+                            if (stream) tma_load_2d(st, &tmA, t * kKC, frame_row, &b_full[s]);
+                            tma_load_2d(st + b_off, &tmB, t * kKC, ct * p.bn, &b_full[s]);
+                        }
                         ++issued;
                     }
                     __syncwarp();
@@ -712,12 +847,14 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
         }
         // Drain: every load issued above has landed before the CTA exits
         // (the A chunks of the last frame tile whose loads were issued, and
-        // the last issued load of every B stage).
-        if (a_issued_tiles > 0) {
+        // the last issued load of every B stage).  In a pair the barriers are
+        // the leader's and count both CTAs' copies; the peer is held by the
+        // closing cluster barrier until the leader has drained.
+        if ((!PAIR || leader) && a_issued_tiles > 0) {
             const uint32_t last_a = (a_issued_tiles - 1u) & 1u;
             for (int kc = 0; kc < nab; ++kc) mbar_wait(&a_full[kc], last_a);
         }
-        for (uint32_t st = 0; st < (uint32_t)p.stages && st < issued; ++st) {
+        for (uint32_t st = 0; (!PAIR || leader) && st < (uint32_t)p.stages && st < issued; ++st) {
             const uint32_t last_q = issued - 1u - ((issued - 1u - st) % p.stages);
             mbar_wait(&b_full[st], (last_q / p.stages) & 1u);
         }
@@ -730,7 +867,9 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
         // stops the issues (the elected lane, lane 0 of the converged warp,
         // decides by its own wait), and the warp agrees on ok once per
         // center tile.
-        const uint32_t idesc = make_idesc(kBM, p.bn, p.bf16 != 0);
+        // In a pair only the leader issues; the peer's MMA warp waits for
+        // the drain commit below.
+        const uint32_t idesc = make_idesc(PAIR ? 2 * kBM : kBM, p.bn, p.bf16 != 0);
         const uint64_t adesc0 = sw128_desc(smem_u32(sA));
         const uint64_t sdesc0 = sw128_desc(smem_u32(sB));
         const uint64_t sstep = (uint64_t)(stage_bytes >> 4);
@@ -741,15 +880,18 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
         bool ok = true;
         unsigned long long w_b = 0, w_a = 0, w_acc = 0;
         const long long t_start = clock64();
-        unsigned long long *pw_b = (p.wait_cycles && lane == 0) ? &w_b : nullptr;
-        unsigned long long *pw_a = (p.wait_cycles && lane == 0) ? &w_a : nullptr;
-        unsigned long long *pw_acc = (p.wait_cycles && lane == 0) ? &w_acc : nullptr;
+        const bool diag = p.wait_cycles && lane == 0 && (!PAIR || leader);
+        unsigned long long *pw_b = diag ? &w_b : nullptr;
+        unsigned long long *pw_a = diag ? &w_a : nullptr;
+        unsigned long long *pw_acc = diag ? &w_acc : nullptr;
         uint32_t s = 0, sph = 0;  // B stage and its phase
         uint64_t sdesc = sdesc0;  // descriptor of stage s
-        for (int64_t ft = blockIdx.x; ft < n_ftiles && ok; ft += gridDim.x, ++t_local) {
+        for (int64_t ft = unit0; (!PAIR || leader) && ft < n_units && ok; ft += unit_stride, ++t_local) {
             for (int ct = 0; ct < p.n_ctiles && ok; ++ct) {
                 const uint32_t buf = accq & 1u;
-                ok = mbar_wait_timed(&acc_empty[buf], ((accq >> 1) & 1u) ^ 1u, pw_acc);
+                // The peer CTA's epilogue warps arrive here too (cluster scope).
+                ok = PAIR ? mbar_wait_cluster_timed(&acc_empty[buf], ((accq >> 1) & 1u) ^ 1u, pw_acc)
+                          : mbar_wait_timed(&acc_empty[buf], ((accq >> 1) & 1u) ^ 1u, pw_acc);
                 tc_fence_after();
                 const uint32_t d_tmem = tmem_base + buf * (uint32_t)p.bn;
                 const bool first = ct == 0, last = ct == p.n_ctiles - 1;
@@ -763,12 +905,21 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                     const uint64_t b_d = sdesc + boff;
                     const int steps = t == p.nbst - 1 ? last_steps : 4;
                     if (elect_one() && ok) {
-                        mma_f16(d_tmem, a_d, b_d, idesc, t != 0);
+                        if (PAIR) {
+                            mma_f16_pair(d_tmem, a_d, b_d, idesc, t != 0);
 #pragma unroll
-                        for (int kk = 1; kk < 4; ++kk)  // 32-byte K steps: +2 in the start-address field
-                            if (kk < steps) mma_f16(d_tmem, a_d + 2 * kk, b_d + 2 * kk, idesc, 1u);
-                        mma_commit(&b_empty[s]);
-                        if (!stream && last) mma_commit(&a_empty[t]);
+                            for (int kk = 1; kk < 4; ++kk)
+                                if (kk < steps) mma_f16_pair(d_tmem, a_d + 2 * kk, b_d + 2 * kk, idesc, 1u);
+                            mma_commit_pair(&b_empty[s]);
+                            if (last) mma_commit_pair(&a_empty[t]);
+                        } else {
+                            mma_f16(d_tmem, a_d, b_d, idesc, t != 0);
+#pragma unroll
+                            for (int kk = 1; kk < 4; ++kk)  // 32-byte K steps: +2 in the start-address field
+                                if (kk < steps) mma_f16(d_tmem, a_d + 2 * kk, b_d + 2 * kk, idesc, 1u);
+                            mma_commit(&b_empty[s]);
+                            if (!stream && last) mma_commit(&a_empty[t]);
+                        }
                     }
                     __syncwarp();
                     ad += astep;
@@ -782,7 +933,12 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                 }
                 ok = __all_sync(0xffffffffu, ok);
                 if (!ok) break;
-                if (elect_one()) mma_commit(&acc_full[buf]);
+                if (elect_one()) {
+                    if (PAIR)
+                        mma_commit_pair(&acc_full[buf]);
+                    else
+                        mma_commit(&acc_full[buf]);
+                }
                 __syncwarp();
                 ++accq;
                 if (__any_sync(0xffffffffu, *abort_flag != 0)) ok = false;
@@ -798,8 +954,14 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
             atomicAdd(&p.wait_cycles[kWaitMmaAcc], w_acc);
             atomicAdd(&p.wait_cycles[kMmaTotal], (unsigned long long)(clock64() - t_start));
         }
-        // Drain: all issued MMAs complete before TMEM is released.
-        if (elect_one()) mma_commit(drain);
+        // Drain: all issued MMAs complete before TMEM is released (in a pair
+        // the leader's commit arrives on both CTAs' drain barriers).
+        if (elect_one()) {
+            if (!PAIR)
+                mma_commit(drain);
+            else if (leader)
+                mma_commit_pair(drain);
+        }
         __syncwarp();
         mbar_wait(drain, 0);
         __syncwarp();
@@ -819,8 +981,8 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
         unsigned long long w_acc = 0;
         const long long t_start = clock64();
         unsigned long long *pw_acc = (p.wait_cycles && warp == 2 && lane == 0) ? &w_acc : nullptr;
-        for (int64_t ft = blockIdx.x; ft < n_ftiles && ok; ft += gridDim.x) {
-            const int64_t i = ft * kBM + row;
+        for (int64_t ft = unit0; ft < n_units && ok; ft += unit_stride) {
+            const int64_t i = ft * unit + (int64_t)rank * kBM + row;
             const float4 xn = i < p.n ? p.xnorm[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
             // Worst-case bound terms over all centers: the acceptance window
             // and the overflow decision use them.
@@ -911,7 +1073,12 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                 }
                 tc_fence_before();
                 __syncwarp();
-                if (lane == 0) mbar_arrive(&acc_empty[buf]);
+                if (lane == 0) {
+                    if (PAIR)
+                        mbar_arrive_cluster(mapa_shared(smem_u32(&acc_empty[buf]), 0));
+                    else
+                        mbar_arrive(&acc_empty[buf]);
+                }
                 ++accq;
             }
             if (!ok) break;
@@ -1033,9 +1200,15 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
 
     tc_fence_before();
     __syncthreads();
+    // A pair leaves together: no remote arrive or copy may target a CTA that
+    // has exited, and the pair's TMEM is released by both CTAs at once.
+    if (PAIR) cluster_sync_all();
     if (warp == 1) {
         tc_fence_after();
-        tmem_dealloc(tmem_base, p.tmem_cols);
+        if (PAIR)
+            tmem_dealloc_pair(tmem_base, p.tmem_cols);
+        else
+            tmem_dealloc(tmem_base, p.tmem_cols);
     }
 }
 
@@ -1096,8 +1269,18 @@ int k_pad_of(int k) { return (k + 255) / 256 * 256; }
 
 struct Plan {
     int bn, stages, nkc, smem, stream_a;
+    int pair;  // CTA-pair form (cta_group::2, M = 256)
     uint32_t tmem_cols;
 };
+
+// The CTA-pair form is used for full-width center tiles with a resident frame
+// tile; KM_TC_PAIR=0 or 1 in the environment forces the choice (both forms
+// give the same labels).
+bool pair_wanted() {
+    const char *e = std::getenv("KM_TC_PAIR");
+    if (e && e[0] == '0') return false;
+    return true;
+}
 
 bool make_plan(int d, int k, Plan &pl) {
     pl.nkc = kp_of(d) / kKC;
@@ -1118,6 +1301,18 @@ bool make_plan(int d, int k, Plan &pl) {
         pl.smem = fixed + stages * (kABytesPerChunk + pl.bn * kKC * 2);
     }
     pl.stages = stages;
+    pl.pair = 0;
+    if (!pl.stream_a && pl.bn == 256 && pair_wanted()) {
+        // Each CTA of the pair stages half of the B tile: 16 KB per stage.
+        const int res = fixed + pl.nkc * kABytesPerChunk;
+        const int half = pl.bn / 2 * kKC * 2;
+        const int pst = std::min(8, (kSmemLimit - res) / half);
+        if (pst >= 3) {
+            pl.pair = 1;
+            pl.stages = pst;
+            pl.smem = res + pst * half;
+        }
+    }
     if (pl.smem < 120 * 1024) pl.smem = 120 * 1024;  // one CTA per SM: TMEM is sized for one
     uint32_t cols = 32;
     while (cols < (uint32_t)(2 * pl.bn)) cols <<= 1;
@@ -1303,13 +1498,18 @@ int tc_assign(const float *X, int64_t n, int d, const float *C, int k, int32_t *
     static std::once_flag attr_once;
     static cudaError_t attr_err = cudaSuccess;
     std::call_once(attr_once, [] {
-        attr_err = cudaFuncSetAttribute(tc_assign_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemLimit);
+        attr_err = cudaFuncSetAttribute(tc_assign_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        kSmemLimit);
+        if (attr_err == cudaSuccess)
+            attr_err = cudaFuncSetAttribute(tc_assign_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            kSmemLimit);
     });
     KM_CUDA(attr_err);
 
     CUtensorMap tmA, tmB;
     KM_TRY(make_map(&tmA, b.xh, n, b.kp, kBM, kKC, CU_TENSOR_MAP_SWIZZLE_128B, b.bf16 != 0));
-    KM_TRY(make_map(&tmB, b.ch, k_pad_of(k), b.kp, pl.bn, kKC, CU_TENSOR_MAP_SWIZZLE_128B, b.bf16 != 0));
+    KM_TRY(make_map(&tmB, b.ch, k_pad_of(k), b.kp, pl.pair ? pl.bn / 2 : pl.bn, kKC, CU_TENSOR_MAP_SWIZZLE_128B,
+                    b.bf16 != 0));
 
     KM_CUDA(cudaMemsetAsync(b.counters, 0, 4 * sizeof(int32_t), s));
     KM_CUDA(cudaMemsetAsync(b.flipped, 0, sizeof(unsigned long long), s));
@@ -1354,11 +1554,50 @@ int tc_assign(const float *X, int64_t n, int d, const float *C, int k, int32_t *
     p.dump = dump;
     p.wait_cycles = wait_cycles;
 
-    const int64_t n_ftiles = (n + kBM - 1) / kBM;
-    int64_t grid = num_sms();
-    if (grid > n_ftiles) grid = n_ftiles;
     if (prof) prof->begin(kProfTc, s);
-    tc_assign_kernel<<<(unsigned)grid, kThreadsTC, pl.smem, s>>>(tmA, tmB, p);
+    if (pl.pair) {
+        // Clusters of two CTAs, as many as fit at once (one CTA per SM),
+        // each walking 256-frame units.
+        cudaLaunchConfig_t cfg = {};
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = 2;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.blockDim = dim3(kThreadsTC, 1, 1);
+        cfg.dynamicSmemBytes = (size_t)pl.smem;
+        cfg.stream = s;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        static std::mutex cl_mu;
+        static int cached_smem = -1, cached_clusters = 0;
+        int clusters_fit = 0;
+        {
+            std::lock_guard<std::mutex> lk(cl_mu);
+            if (cached_smem != pl.smem) {
+                cfg.gridDim = dim3((unsigned)(2 * (num_sms() / 2)), 1, 1);
+                int nc = 0;
+                KM_CUDA(cudaOccupancyMaxActiveClusters(&nc, tc_assign_kernel<true>, &cfg));
+                cached_clusters = nc;
+                cached_smem = pl.smem;
+            }
+            clusters_fit = cached_clusters;
+        }
+        if (clusters_fit < 1) {
+            set_error("no CTA pair of the tensor-core kernel fits on this device");
+            return KM_ERR_UNSUPPORTED;
+        }
+        const int64_t n_units = (n + 2 * kBM - 1) / (2 * kBM);
+        int64_t clusters = clusters_fit;
+        if (clusters > n_units) clusters = n_units;
+        cfg.gridDim = dim3((unsigned)(2 * clusters), 1, 1);
+        KM_CUDA(cudaLaunchKernelEx(&cfg, tc_assign_kernel<true>, tmA, tmB, p));
+    } else {
+        const int64_t n_ftiles = (n + kBM - 1) / kBM;
+        int64_t grid = num_sms();
+        if (grid > n_ftiles) grid = n_ftiles;
+        tc_assign_kernel<false><<<(unsigned)grid, kThreadsTC, pl.smem, s>>>(tmA, tmB, p);
+    }
     KM_CUDA(cudaGetLastError());
     if (prof) prof->end(kProfTc, s);
 
