@@ -91,6 +91,7 @@ struct TcParams {
     float e_coef;
     float g_lo;   // 1 - g, deflated
     float g_hi;   // 1 + g, inflated
+    float g_ratio;  // sqrt(g_hi / g_lo), inflated
     const float4 *xnorm;
     const float2 *cnorm;
     const uint32_t *scal;
@@ -687,14 +688,18 @@ __device__ __forceinline__ float hi_bound(float v, float E, float R, float g_hi)
 constexpr float kCenterEps = 1.1920929e-07f;  // 2^-23
 
 // Smallest accumulator a' that can still belong to a possible argmin, given
-// the best accumulator so far: with H the upper end of the best distance,
-// lo(v') <= H needs v' <= V = (sqrt(H / (1-g)) + R)^2 + E (worst-case R, E),
-// and v' = (||x_hat||^2 - 2 a') / s^2.  Rounded towards admitting more.
+// the best accumulator so far: with H = (sqrt(vb + E) + R)^2 g_hi the upper
+// end of the best distance, lo(v') <= H needs v' <= V = (sqrt(H / g_lo) + R)^2
+// + E (worst-case R, E), and v' = (||x_hat||^2 - 2 a') / s^2.  The root of
+// H / g_lo is (sqrt(vb + E) + R) sqrt(g_hi / g_lo): g_ratio is that factor
+// inflated by 2^-19 (more than the roundings of the literal form), and
+// R_pad = R + 1e-18 covers the root of hi_bound's 1e-37 term.  Rounded
+// towards admitting more throughout; one root, no division.
 __device__ __forceinline__ float window_threshold(float best, float xn2, float inv_s2, float s2, float E,
-                                                  float R, float g_lo, float g_hi) {
+                                                  float R, float R_pad, float g_ratio) {
     const float vb = fmaf(-2.0f, best, xn2) * inv_s2;
-    const float H = hi_bound(vb, E, R, g_hi);
-    const float q = __fadd_ru(__fsqrt_ru(__fdiv_ru(H, g_lo)), R);
+    const float a = __fadd_ru(__fsqrt_ru(fmaxf(__fadd_ru(vb, E), 0.0f)), R);
+    const float q = __fadd_ru(__fmul_ru(g_ratio, a), R_pad);
     const float V = __fadd_ru(__fmul_ru(q, q), E);
     const float t = __fmul_rd(__fsub_rd(xn2, __fmul_ru(V, s2)), 0.5f);
     return __fsub_rd(t, __fmul_ru(fabsf(t), 1e-6f)) - 1e-30f;
@@ -989,8 +994,8 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
             const float smax = xn.y + sc_max;
             const float Rmax = __fadd_ru(__fadd_ru(xn.z, hc_max), __fmul_ru(kCenterEps, smax));
             const float Emax = __fmul_ru(p.e_coef, __fmul_ru(smax, smax));
+            const float Rpad = __fadd_ru(Rmax, 1e-18f);
             float best = kNegInf, thr = kNegInf;
-            int best_id = 0;
             bool ovf = false;
             float la[kL];
             int lid[kL];
@@ -1026,40 +1031,48 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                         for (int c = 0; c < 32; ++c)
                             if (j0 + c < p.k) p.dump[i * p.k + j0 + c] = fmaf(-2.0f, v[c], xn.x) * inv_s2;
                     }
-                    float mx = v[0];
+                    // Chunk maximum by a tree (five dependent steps, not 31).
+                    float m16[16];
 #pragma unroll
-                    for (int c = 1; c < 32; ++c) mx = fmaxf(mx, v[c]);
+                    for (int q = 0; q < 16; ++q) m16[q] = fmaxf(v[q], v[q + 16]);
+#pragma unroll
+                    for (int w = 8; w >= 1; w >>= 1)
+#pragma unroll
+                        for (int q = 0; q < w; ++q) m16[q] = fmaxf(m16[q], m16[q + w]);
+                    const float mx = m16[0];
                     if (mx >= thr && mx > kNegInf) {
                         if (mx > best) {
-                            int bc = 31;
-#pragma unroll
-                            for (int c = 31; c >= 0; --c)
-                                if (v[c] == mx) bc = c;
                             best = mx;
-                            best_id = j0 + bc;
-                            thr = window_threshold(best, xn.x, inv_s2, s2, Emax, Rmax, p.g_lo, p.g_hi);
+                            thr = window_threshold(best, xn.x, inv_s2, s2, Emax, Rmax, Rpad, p.g_ratio);
                         }
                         // Columns at or above the threshold as a bit mask; each
-                        // one is then picked out of the registers by a select
-                        // tree over the bits of its index and pushed on the list.
-                        unsigned msk = 0;
+                        // one is pushed on the list.  A lone column is the
+                        // chunk's maximum; otherwise each value is picked out
+                        // of the registers by a select tree over the bits of
+                        // its index.
+                        unsigned mk[4] = {0u, 0u, 0u, 0u};  // four independent chains
 #pragma unroll
-                        for (int c = 0; c < 32; ++c) msk |= (v[c] >= thr ? 1u : 0u) << c;
+                        for (int c = 0; c < 32; ++c) mk[c & 3] |= (v[c] >= thr ? 1u : 0u) << c;
+                        unsigned msk = (mk[0] | mk[1]) | (mk[2] | mk[3]);
                         const int nv = p.k - j0;
                         if (nv < 32) msk &= nv > 0 ? (1u << nv) - 1u : 0u;
+                        const bool lone = (msk & (msk - 1u)) == 0u;
                         while (msk) {
                             const int c = __ffs(msk) - 1;
                             msk &= msk - 1u;
-                            float t16[16], t8[8], t4[4], t2[2];
+                            float vc = mx;
+                            if (!lone) {
+                                float t16[16], t8[8], t4[4], t2[2];
 #pragma unroll
-                            for (int q = 0; q < 16; ++q) t16[q] = (c & 16) ? v[q + 16] : v[q];
+                                for (int q = 0; q < 16; ++q) t16[q] = (c & 16) ? v[q + 16] : v[q];
 #pragma unroll
-                            for (int q = 0; q < 8; ++q) t8[q] = (c & 8) ? t16[q + 8] : t16[q];
+                                for (int q = 0; q < 8; ++q) t8[q] = (c & 8) ? t16[q + 8] : t16[q];
 #pragma unroll
-                            for (int q = 0; q < 4; ++q) t4[q] = (c & 4) ? t8[q + 4] : t8[q];
+                                for (int q = 0; q < 4; ++q) t4[q] = (c & 4) ? t8[q + 4] : t8[q];
 #pragma unroll
-                            for (int q = 0; q < 2; ++q) t2[q] = (c & 2) ? t4[q + 2] : t4[q];
-                            const float vc = (c & 1) ? t2[1] : t2[0];
+                                for (int q = 0; q < 2; ++q) t2[q] = (c & 2) ? t4[q + 2] : t4[q];
+                                vc = (c & 1) ? t2[1] : t2[0];
+                            }
                             if (lid[kL - 1] >= 0 && la[kL - 1] >= thr) ovf = true;
 #pragma unroll
                             for (int m = kL - 1; m > 0; --m) {
@@ -1086,6 +1099,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
             // ---- decision ----
             bool need_rc = false, need_full = false;
             unsigned cmask = 0;  // bit m: list entry m is a candidate
+            int jb = 0;          // candidate with the largest accumulator
             float lo[kL];        // lower bounds of the candidates' exact distances
             if (i < p.n) {
                 float vv[kL], RR[kL], EE[kL];
@@ -1117,13 +1131,18 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                     if (nc == 0) need_full = true;
                     else if (nc > 1) need_rc = true;
                 }
-                int lab = best_id;
-                if (!need_full && !need_rc) {
+                // Provisional label: the candidate with the largest
+                // accumulator (the final one when it is the only candidate;
+                // the re-checks overwrite the others).
+                float vb = kNegInf;
 #pragma unroll
-                    for (int m = 0; m < kL; ++m)
-                        if (cmask == (1u << m)) lab = lid[m];
+                for (int m = 0; m < kL; ++m) {
+                    if (((cmask >> m) & 1u) && la[m] > vb) {
+                        vb = la[m];
+                        jb = lid[m];
+                    }
                 }
-                p.labels[i] = lab;
+                p.labels[i] = jb;
             }
             const unsigned m_rc = __ballot_sync(0xffffffffu, need_rc);
             if (m_rc) {
@@ -1151,15 +1170,6 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                     // The candidate with the largest accumulator (smallest
                     // approximate distance) is evaluated first; the others are
                     // evaluated only if their lower bound does not exceed it.
-                    float vb = kNegInf;
-                    int jb = 0;
-#pragma unroll
-                    for (int m = 0; m < kL; ++m) {
-                        if (((cmask >> m) & 1u) && la[m] > vb) {
-                            vb = la[m];
-                            jb = lid[m];
-                        }
-                    }
                     p.rc_frames[e] = (int32_t)i;
                     p.rc_best[e] = jb;
                     p.rc_keys[e] = ~0ull;
@@ -1537,6 +1547,9 @@ int tc_assign(const float *X, int64_t n, int d, const float *C, int k, int32_t *
     const double g = (d + 2) * u / (1.0 - (d + 2) * u) * 1.01;
     p.g_lo = (float)((1.0 - g) * (1.0 - 4.0 * u));
     p.g_hi = (float)((1.0 + g) * (1.0 + 4.0 * u));
+    // sqrt(g_hi / g_lo) of the float factors, inflated by 2^-19 and rounded up.
+    p.g_ratio = std::nextafter((float)(std::sqrt((double)p.g_hi / (double)p.g_lo) * (1.0 + std::ldexp(1.0, -19))),
+                               INFINITY);
     p.xnorm = b.xnorm;
     p.cnorm = b.cnorm;
     p.scal = b.scal;
