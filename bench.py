@@ -333,6 +333,14 @@ def run_ours(args):
         Xh.copy_(X)
         Xh_np = Xh.numpy()
         C0h = C0.cpu().numpy()
+        # the bare pinned host-to-device rate of this machine, for reading e2e
+        ec0, ec1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        X.copy_(Xh, non_blocking=True)
+        ec0.record()
+        X.copy_(Xh, non_blocking=True)
+        ec1.record()
+        torch.cuda.synchronize()
+        link_gbs = n * D * 4 / (ec0.elapsed_time(ec1) / 1e3) / 1e9
         del X  # the API makes its own device copy
         torch.cuda.empty_cache()
         km = KmeansClustering(n_clusters=K, max_iter=1, tolerance=-1.0, clustercenters=C0h, precision="fp16")
@@ -347,7 +355,10 @@ def run_ours(args):
         dt = (time.perf_counter() - t0) / e2e_steps
         e2e = {"value": n / dt, "unit": UNIT, "h2d_bytes_per_step": n * D * 4, "d2h_bytes_per_step": K * D * 4 + 8,
                "api": "KmeansClustering(n_clusters=2000, max_iter=1, clustercenters=C).estimate(pinned host X)",
-               "steps": e2e_steps}
+               "steps": e2e_steps, "h2d_link_gbs": link_gbs,
+               "copy_bound_frames_per_s": link_gbs * 1e9 / (D * 4),
+               "overlap": "frames copied in chunks on a side stream while the first iteration assigns "
+                          "the chunks already copied (km_lloyd_host)"}
         del Xh, Xh_np
         # The same iteration from pinned host C-alpha coordinates: the
         # 528 distance features are computed on the device (featurize.ca_distances)

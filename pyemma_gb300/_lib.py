@@ -30,7 +30,7 @@ EXPORTED = (
     "km_assign_workspace_size", "km_assign", "km_batch_assign", "km_debug_tc_distances",
     "km_update_workspace_size", "km_update", "km_update_noalloc_max_bytes", "km_update_noalloc",
     "km_kmpp_workspace_size", "km_kmpp",
-    "km_lloyd_workspace_size", "km_lloyd",
+    "km_lloyd_workspace_size", "km_lloyd", "km_lloyd_host",
     "km_centers_create", "km_centers_destroy", "km_centers_info", "km_assign_centers_workspace_size",
     "km_assign_centers",
     "km_serve_create", "km_serve_add_centers", "km_serve_submit", "km_serve_poll", "km_serve_stats_read",
@@ -130,6 +130,7 @@ def load(build_if_missing=False):
     L.km_lloyd_workspace_size.argtypes = [i64, i32, i32, i32]
     L.km_lloyd_workspace_size.restype = sz
     L.km_lloyd.argtypes = [P, i64, i32, i32, P, i32, f64, i32, P, P, P, P, CALLBACK, P, P, sz, P]
+    L.km_lloyd_host.argtypes = [P, P, i32, P, i64, i32, i32, P, i32, f64, i32, P, P, P, P, CALLBACK, P, P, sz, P]
     pp = ctypes.POINTER(ctypes.c_void_p)
     L.km_centers_create.argtypes = [P, i32, i32, i32, P, pp]
     L.km_centers_destroy.argtypes = [P]
@@ -160,7 +161,8 @@ def load(build_if_missing=False):
     L.km_count_matrix.restype = ctypes.c_int
     L.km_pair_distances.argtypes = [P, i64, i32, P, i32, P, P]
     L.km_pair_distances.restype = ctypes.c_int
-    for name in ("km_assign", "km_batch_assign", "km_update", "km_kmpp", "km_lloyd", "km_centers_create",
+    for name in ("km_assign", "km_batch_assign", "km_update", "km_kmpp", "km_lloyd", "km_lloyd_host",
+                 "km_centers_create",
                  "km_centers_destroy", "km_centers_info", "km_assign_centers", "km_serve_create",
                  "km_serve_add_centers", "km_serve_submit", "km_serve_poll", "km_serve_stats_read",
                  "km_serve_shutdown"):
@@ -364,6 +366,52 @@ def lloyd(X, C, max_iter, tolerance, precision="auto", callback=None, labels=Non
                      None, _ptr(ws), ws_bytes, _stream(torch, X.device)))
     del keep
     return dict(labels=labels, inertias=inertias[:n_iter.value].copy(), n_iter=n_iter.value,
+                converged=bool(conv.value))
+
+
+def lloyd_host(parts, C, max_iter, tolerance, precision="auto", callback=None, X=None, labels=None):
+    """Lloyd iterations on frames in host memory, in place on C.
+
+    ``parts`` is a list of (T_i, d) float32 C-contiguous numpy arrays (pinned
+    memory gives an overlapped copy).  They are copied into the device tensor
+    ``X`` (allocated when None) while the first iteration assigns the frames
+    already copied.  Returns dict(X, labels, inertias, n_iter, converged).
+    """
+    torch = _torch()
+    L = load()
+    _check_frames(torch, C, "C")
+    d = C.shape[1]
+    k = C.shape[0]
+    arrs = []
+    for a in parts:
+        if not (isinstance(a, np.ndarray) and a.dtype == np.float32 and a.flags["C_CONTIGUOUS"] and a.ndim == 2
+                and a.shape[1] == d):
+            raise ValueError("host parts must be C-contiguous float32 arrays of shape (T, %d)" % d)
+        if len(a):
+            arrs.append(a)
+    n = int(sum(len(a) for a in arrs))
+    if X is None:
+        X = torch.empty((n, d), dtype=torch.float32, device=C.device)
+    _check_frames(torch, X)
+    if X.shape[0] != n or X.shape[1] != d:
+        raise ValueError("X must have shape (%d, %d)" % (n, d))
+    p = precision_code(precision)
+    if labels is None:
+        labels = torch.empty(n, dtype=torch.int32, device=C.device)
+    ptrs = (ctypes.c_void_p * max(1, len(arrs)))(*[a.ctypes.data for a in arrs])
+    rows = np.array([len(a) for a in arrs] or [0], dtype=np.int64)
+    inertias = np.zeros(max(1, max_iter), dtype=np.float64)
+    n_iter = ctypes.c_int32(0)
+    conv = ctypes.c_int32(0)
+    ws_bytes = L.km_lloyd_workspace_size(n, d, k, p)
+    ws = _workspace(torch, ws_bytes, C.device)
+    cb, keep = _callback(callback)
+    check(L.km_lloyd_host(ptrs, rows.ctypes.data_as(ctypes.c_void_p), len(arrs), _ptr(X), n, d, k, _ptr(C),
+                          int(max_iter), float(tolerance), p, _ptr(labels),
+                          inertias.ctypes.data_as(ctypes.c_void_p), ctypes.byref(n_iter), ctypes.byref(conv), cb,
+                          None, _ptr(ws), ws_bytes, _stream(torch, C.device)))
+    del keep
+    return dict(X=X, labels=labels, inertias=inertias[:n_iter.value].copy(), n_iter=n_iter.value,
                 converged=bool(conv.value))
 
 

@@ -57,6 +57,21 @@ def pack_to_device(trajs, dim):
     return dev
 
 
+def host_parts(trajs):
+    """The trajectories as float32 C-contiguous host arrays (cast where
+    needed, as np.require in interface.py:159), or None when any of them is
+    already on the device."""
+    torch = torch_module()
+    out = []
+    for t in trajs:
+        if isinstance(t, torch.Tensor):
+            if t.device.type != "cpu":
+                return None
+            t = t.numpy()
+        out.append(np.require(t, dtype=np.float32, requirements="C"))
+    return out
+
+
 def centers_to_device(centers):
     torch = torch_module()
     c = np.ascontiguousarray(centers, dtype=np.float32)

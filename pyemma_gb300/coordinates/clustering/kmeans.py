@@ -160,12 +160,19 @@ class KmeansClustering(AbstractClustering):
         dim = source.dimension()
         reuse = self._init_in_memory_chunks(total_length, dim)
 
+        host_parts = None
         if not self._check_resume_iteration() or not self._in_memory_chunks_set or not reuse:
             trajs = source.frames(stride=stride, skip=self.skip)
             if not self._check_resume_iteration() and self.init_strategy == "uniform":
                 indices = self._uniform_indices(traj_lengths, total_length)
                 self.clustercenters = self._uniform_centers(trajs, indices)
-            self._in_memory_chunks = _device.pack_to_device(trajs, dim)
+            if self._check_resume_iteration():
+                # Centers known (given, or drawn uniformly above) before the
+                # frames reach the device: the copy overlaps the first
+                # assignment (km_lloyd_host).
+                host_parts = _device.host_parts(trajs)
+            if host_parts is None:
+                self._in_memory_chunks = _device.pack_to_device(trajs, dim)
             self.initial_centers_ = self.clustercenters[:]
             self._in_memory_chunks_set = True
         else:
@@ -173,7 +180,6 @@ class KmeansClustering(AbstractClustering):
                 raise RuntimeError("Passed clustercenters do not match n_clusters: {} vs. {}".format(
                     len(self.clustercenters), self.n_clusters))
 
-        X = self._in_memory_chunks
         try:
             if self._check_resume_iteration():
                 if self.clustercenters.ndim != 2 or self.clustercenters.shape[1] != dim:
@@ -181,15 +187,22 @@ class KmeansClustering(AbstractClustering):
                                      % (self.clustercenters.shape, dim))
                 C = _device.centers_to_device(self.clustercenters)
             else:
-                C, _ = _lib.kmpp(X, int(self.n_clusters), self.fixed_seed)
-            res = _lib.lloyd(X, C, int(self.max_iter), float(self.tolerance), precision=self.precision)
+                C, _ = _lib.kmpp(self._in_memory_chunks, int(self.n_clusters), self.fixed_seed)
+            if host_parts is not None:
+                res = _lib.lloyd_host(host_parts, C, int(self.max_iter), float(self.tolerance),
+                                      precision=self.precision)
+                self._in_memory_chunks = res["X"]
+            else:
+                res = _lib.lloyd(self._in_memory_chunks, C, int(self.max_iter), float(self.tolerance),
+                                 precision=self.precision)
             self.clustercenters = C.cpu().numpy()
             self._converged = res["converged"]
             self.inertias = res["inertias"]
             self.n_iter = res["n_iter"]
         finally:
-            if not self.keep_data or self._converged:
-                del self._in_memory_chunks
+            if not self.keep_data or self._converged or not hasattr(self, "_in_memory_chunks"):
+                if hasattr(self, "_in_memory_chunks"):
+                    del self._in_memory_chunks
                 self._in_memory_chunks_set = False
 
         if self.converged:

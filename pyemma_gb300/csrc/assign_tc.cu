@@ -1523,7 +1523,7 @@ int tc_assign(const float *X, int64_t n, int d, const float *C, int k, int32_t *
 
     KM_CUDA(cudaMemsetAsync(b.counters, 0, 4 * sizeof(int32_t), s));
     KM_CUDA(cudaMemsetAsync(b.flipped, 0, sizeof(unsigned long long), s));
-    KM_CUDA(cudaMemsetAsync(b.err, 0, sizeof(uint32_t), s));
+    if (!b.keep_err) KM_CUDA(cudaMemsetAsync(b.err, 0, sizeof(uint32_t), s));
 
     const double u = 5.9604644775390625e-08;  // 2^-24
     TcParams p;

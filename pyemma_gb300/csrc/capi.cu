@@ -1,10 +1,12 @@
 // capi.cu -- the extern "C" entry points of libkmgpu (declared in
 // include/kmgpu.h).  Each one validates its arguments, carves the caller's
 // workspace and enqueues kernels on the caller's stream.
+#include <algorithm>
 #include <cstring>
 #include <map>
 #include <mutex>
 #include <utility>
+#include <vector>
 
 #include "km_common.cuh"
 #include "km_internal.h"
@@ -440,13 +442,33 @@ size_t km_lloyd_workspace_size(int64_t n, int32_t d, int32_t k, int32_t precisio
     return lloyd_ws_bytes(n, d, k, resolve_precision(precision, d, k, false));
 }
 
-int km_lloyd(const float *X, int64_t n, int32_t d, int32_t k, float *C, int32_t max_iter,
-             double tolerance, int32_t precision, int32_t *labels, double *inertias,
-             int32_t *n_iter, int32_t *converged, km_callback cb, void *cb_user, void *workspace,
-             size_t workspace_bytes, void *stream) {
+}  // extern "C"
+
+namespace {
+
+// Host frames of km_lloyd_host: n_parts row-major float32 blocks, copied one
+// after the other into the device frame buffer.
+struct HostFrames {
+    const float *const *parts;
+    const int64_t *rows;
+    int32_t n_parts;
+};
+
+// Rows per streamed chunk of the first iteration: about 1/24 of the run,
+// at least 16384 frames, a multiple of 256.
+int64_t stream_chunk_rows(int64_t n) {
+    int64_t c = (n + 23) / 24;
+    if (c < 16384) c = 16384;
+    return (c + 255) / 256 * 256;
+}
+
+int lloyd_run(const float *X_in, const HostFrames *hf, int64_t n, int32_t d, int32_t k, float *C, int32_t max_iter,
+              double tolerance, int32_t precision, int32_t *labels, double *inertias, int32_t *n_iter,
+              int32_t *converged, km_callback cb, void *cb_user, void *workspace, size_t workspace_bytes,
+              void *stream) {
     KM_TRY(check_shape(n, d, k));
-    if (n < 1 || !X || !C || !labels || !n_iter || !converged || max_iter < 0) {
-        set_error("km_lloyd needs n >= 1, max_iter >= 0 and non-NULL X, C, labels, n_iter, converged");
+    if (n < 1 || !X_in || !C || !labels || !n_iter || !converged || max_iter < 0) {
+        set_error("Lloyd needs n >= 1, max_iter >= 0 and non-NULL X, C, labels, n_iter, converged");
         return KM_ERR_BAD_SHAPE;
     }
     *n_iter = 0;
@@ -458,8 +480,66 @@ int km_lloyd(const float *X, int64_t n, int32_t d, int32_t k, float *C, int32_t 
     }
     const size_t need = lloyd_ws_bytes(n, d, k, prec);
     KM_TRY(check_ws(workspace, workspace_bytes, need));
-    if (max_iter == 0) return KM_OK;
+    if (max_iter == 0 && !hf) return KM_OK;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
+    float *X = const_cast<float *>(X_in);  // written only by the host-frame copies
+
+    // Host frames: one chunked copy on a side stream, an event per chunk.
+    struct Streamed {
+        cudaStream_t cs = nullptr;
+        std::vector<cudaEvent_t> ev;
+        std::vector<int64_t> begin;  // first row of each chunk (plus n at the end)
+        ~Streamed() {
+            for (cudaEvent_t e : ev)
+                if (e) cudaEventDestroy(e);
+            if (cs) cudaStreamDestroy(cs);
+        }
+    } sm;
+    if (hf) {
+        int64_t total = 0;
+        for (int32_t q = 0; q < hf->n_parts; ++q) {
+            if (hf->rows[q] < 0 || (hf->rows[q] > 0 && !hf->parts[q])) {
+                set_error("host part %d: negative rows or NULL pointer", q);
+                return KM_ERR_BAD_SHAPE;
+            }
+            total += hf->rows[q];
+        }
+        if (total != n) {
+            set_error("host parts hold %lld rows, n = %lld", (long long)total, (long long)n);
+            return KM_ERR_BAD_SHAPE;
+        }
+        const int64_t chunk = stream_chunk_rows(n);
+        for (int64_t a = 0; a < n; a += chunk) sm.begin.push_back(a);
+        sm.begin.push_back(n);
+        KM_CUDA(cudaStreamCreateWithFlags(&sm.cs, cudaStreamNonBlocking));
+        sm.ev.assign(sm.begin.size(), nullptr);  // [0]: the caller's stream reached this call
+        for (cudaEvent_t &e : sm.ev) KM_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        KM_CUDA(cudaEventRecord(sm.ev[0], s));
+        KM_CUDA(cudaStreamWaitEvent(sm.cs, sm.ev[0], 0));
+        int32_t q = 0;
+        int64_t q_off = 0;  // rows of part q already copied
+        for (size_t c = 0; c + 1 < sm.begin.size(); ++c) {
+            int64_t row = sm.begin[c];
+            const int64_t stop = sm.begin[c + 1];
+            while (row < stop) {
+                while (q < hf->n_parts && q_off == hf->rows[q]) {
+                    ++q;
+                    q_off = 0;
+                }
+                const int64_t take = std::min(stop - row, hf->rows[q] - q_off);
+                KM_CUDA(cudaMemcpyAsync(X + row * d, hf->parts[q] + q_off * d, sizeof(float) * (size_t)take * d,
+                                        cudaMemcpyHostToDevice, sm.cs));
+                row += take;
+                q_off += take;
+            }
+            KM_CUDA(cudaEventRecord(sm.ev[c + 1], sm.cs));
+        }
+        if (max_iter == 0) {
+            KM_CUDA(cudaStreamWaitEvent(s, sm.ev.back(), 0));
+            KM_CUDA(cudaStreamSynchronize(s));
+            return KM_OK;
+        }
+    }
 
     Carver cv(workspace);
     void *ws_update = cv.take<char>(update_ws_size(n, d, k));
@@ -475,19 +555,28 @@ int km_lloyd(const float *X, int64_t n, int32_t d, int32_t k, float *C, int32_t 
         carve_assign(ws_assign, n, d, k, b);
         b.bf16 = prec == KM_PREC_BF16;
         KM_TRY(tc_prepare_shift_from_centers(C, d, k, b, s));
-        KM_TRY(tc_prepare_frames(X, n, d, b, s));
+        if (!hf) KM_TRY(tc_prepare_frames(X, n, d, b, s));
     }
     KM_CUDA(cudaMemsetAsync(err, 0, sizeof(uint32_t), s));
 
     // One iteration: assign, update, C <- C_new.  The first iteration runs
     // eagerly (it also performs every lazy one-time set-up); the following
-    // ones replay a CUDA graph captured from the same sequence.
+    // ones replay a CUDA graph captured from the same sequence.  With host
+    // frames the first iteration assigns each chunk as soon as its copy has
+    // landed (and makes its 16-bit copy first), overlapping the transfer.
     ProfEvents prof;
     KM_TRY(prof.open());
     struct Closer {
         ProfEvents &p;
         ~Closer() { p.close(); }
     } closer{prof};
+    auto enqueue_update = [&](cudaStream_t st) -> int {
+        prof.begin(kProfUpdate, st);
+        KM_TRY(launch_update(X, n, d, labels, k, C, C_new, nullptr, cost, err, ws_update, st));
+        prof.end(kProfUpdate, st);
+        KM_CUDA(cudaMemcpyAsync(C, C_new, sizeof(float) * k * d, cudaMemcpyDeviceToDevice, st));
+        return KM_OK;
+    };
     auto enqueue = [&](cudaStream_t st) -> int {
         if (is_tc(prec)) {
             KM_TRY(tc_prepare_centers(C, d, k, b, st));
@@ -497,11 +586,29 @@ int km_lloyd(const float *X, int64_t n, int32_t d, int32_t k, float *C, int32_t 
             KM_TRY(launch_assign_fp32(X, nullptr, nullptr, n, d, C, k, labels, nullptr, nullptr, st));
             prof.end(kProfFp32, st);
         }
-        prof.begin(kProfUpdate, st);
-        KM_TRY(launch_update(X, n, d, labels, k, C, C_new, nullptr, cost, err, ws_update, st));
-        prof.end(kProfUpdate, st);
-        KM_CUDA(cudaMemcpyAsync(C, C_new, sizeof(float) * k * d, cudaMemcpyDeviceToDevice, st));
-        return KM_OK;
+        return enqueue_update(st);
+    };
+    auto enqueue_streamed = [&](cudaStream_t st) -> int {
+        if (is_tc(prec)) {
+            KM_TRY(tc_prepare_centers(C, d, k, b, st));
+            KM_CUDA(cudaMemsetAsync(b.err, 0, sizeof(uint32_t), st));
+        }
+        for (size_t c = 0; c + 1 < sm.begin.size(); ++c) {
+            const int64_t a = sm.begin[c], rows = sm.begin[c + 1] - a;
+            KM_CUDA(cudaStreamWaitEvent(st, sm.ev[c + 1], 0));
+            if (is_tc(prec)) {
+                TcBuffers v = tc_rows_from(b, a);
+                v.keep_err = 1;
+                KM_TRY(tc_prepare_frames(X + a * d, rows, d, v, st));
+                KM_TRY(tc_assign(X + a * d, rows, d, C, k, labels + a, v, st, &prof));
+            } else {
+                prof.begin(kProfFp32, st);
+                KM_TRY(launch_assign_fp32(X + a * d, nullptr, nullptr, rows, d, C, k, labels + a, nullptr, nullptr,
+                                          st));
+                prof.end(kProfFp32, st);
+            }
+        }
+        return enqueue_update(st);
     };
 
     cudaGraphExec_t exec = nullptr;
@@ -509,7 +616,7 @@ int km_lloyd(const float *X, int64_t n, int32_t d, int32_t k, float *C, int32_t 
     double prev = 0.0;
     for (int32_t it = 0; it < max_iter; ++it) {
         if (it == 0) {
-            status = enqueue(s);
+            status = hf ? enqueue_streamed(s) : enqueue(s);
         } else {
             if (!exec) {
                 cudaStream_t cs;
@@ -564,7 +671,36 @@ int km_lloyd(const float *X, int64_t n, int32_t d, int32_t k, float *C, int32_t 
         }
     }
     if (exec) cudaGraphExecDestroy(exec);
+    if (hf && status != KM_OK) {
+        // The copies may still be running into X: wait for them before
+        // returning the caller's buffer.
+        cudaStreamSynchronize(sm.cs);
+    }
     return status;
+}
+
+}  // namespace
+
+extern "C" {
+
+int km_lloyd(const float *X, int64_t n, int32_t d, int32_t k, float *C, int32_t max_iter, double tolerance,
+             int32_t precision, int32_t *labels, double *inertias, int32_t *n_iter, int32_t *converged,
+             km_callback cb, void *cb_user, void *workspace, size_t workspace_bytes, void *stream) {
+    return lloyd_run(X, nullptr, n, d, k, C, max_iter, tolerance, precision, labels, inertias, n_iter, converged, cb,
+                     cb_user, workspace, workspace_bytes, stream);
+}
+
+int km_lloyd_host(const float *const *X_parts, const int64_t *part_rows, int32_t n_parts, float *X, int64_t n,
+                  int32_t d, int32_t k, float *C, int32_t max_iter, double tolerance, int32_t precision,
+                  int32_t *labels, double *inertias, int32_t *n_iter, int32_t *converged, km_callback cb,
+                  void *cb_user, void *workspace, size_t workspace_bytes, void *stream) {
+    if (n_parts < 0 || (n_parts > 0 && (!X_parts || !part_rows))) {
+        set_error("km_lloyd_host needs n_parts >= 0 with X_parts and part_rows");
+        return KM_ERR_BAD_SHAPE;
+    }
+    HostFrames hf{X_parts, part_rows, n_parts};
+    return lloyd_run(X, &hf, n, d, k, C, max_iter, tolerance, precision, labels, inertias, n_iter, converged, cb,
+                     cb_user, workspace, workspace_bytes, stream);
 }
 
 // ---- resident center sets --------------------------------------------------

@@ -97,8 +97,17 @@ struct TcBuffers {
     unsigned long long *flipped = nullptr;
     uint32_t *err = nullptr;
     int kp = 0;
-    int bf16 = 0;  // operand type of xh / ch: 0 FP16, 1 BF16
+    int bf16 = 0;      // operand type of xh / ch: 0 FP16, 1 BF16
+    int keep_err = 0;  // 1: tc_assign leaves err as it is (the caller clears it once for several calls)
 };
+
+// The same buffers for frames [a, ...): the per-frame arrays start at row a.
+inline TcBuffers tc_rows_from(const TcBuffers &b, int64_t a) {
+    TcBuffers v = b;
+    v.xh = static_cast<char *>(b.xh) + (size_t)a * b.kp * 2;
+    v.xnorm = b.xnorm + a;
+    return v;
+}
 
 void tc_carve_frames(void *ws, int64_t n, int d, TcBuffers &b);
 void tc_carve_centers(void *ws, int d, int k, TcBuffers &b);

@@ -85,6 +85,19 @@ def test_bad_arguments_rejected_before_device(kmlib):
     rc = kmlib.km_lloyd(None, 10, 3, 2, None, 5, 1e-5, 0, None, None, ctypes.byref(n_iter), ctypes.byref(conv),
                         _lib.CALLBACK(0), None, None, 0, None)
     assert rc == _lib.KM_ERR_BAD_SHAPE
+    rc = kmlib.km_lloyd_host(None, None, -1, ctypes.c_void_p(16), 10, 3, 2, ctypes.c_void_p(32), 5, 1e-5, 0,
+                             ctypes.c_void_p(48), None, ctypes.byref(n_iter), ctypes.byref(conv), _lib.CALLBACK(0),
+                             None, None, 0, None)
+    assert rc == _lib.KM_ERR_BAD_SHAPE
+    # parts that do not add up to n are refused before any device work
+    rows = np.array([4, 5], dtype=np.int64)
+    ptrs = (ctypes.c_void_p * 2)(16, 32)
+    need = kmlib.km_lloyd_workspace_size(10, 3, 2, 0)
+    rc = kmlib.km_lloyd_host(ptrs, rows.ctypes.data_as(ctypes.c_void_p), 2, ctypes.c_void_p(16), 10, 3, 2,
+                             ctypes.c_void_p(32), 5, 1e-5, 0, ctypes.c_void_p(48), None, ctypes.byref(n_iter),
+                             ctypes.byref(conv), _lib.CALLBACK(0), None, ctypes.c_void_p(64), need, None)
+    assert rc == _lib.KM_ERR_BAD_SHAPE
+    assert b"host parts" in kmlib.km_last_error()
 
 
 # ---------------------------------------------------------------------------
