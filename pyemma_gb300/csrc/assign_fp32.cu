@@ -13,6 +13,8 @@
 // loads; every (frame, center) sum stays in one register in feature order,
 // and a lexicographic warp-shuffle (distance, index) reduction finishes the
 // argmin.
+#include <algorithm>
+
 #include "km_common.cuh"
 #include "km_internal.h"
 
@@ -23,6 +25,12 @@ namespace {
 constexpr int kWarps = 8;
 constexpr int kThreads = kWarps * 32;
 constexpr int kFC = 32;  // features per shared-memory chunk
+
+// Full re-check lists of at most this many frames go to full_few_kernel (one
+// distance per thread, all in one short wave); longer lists to the tiled
+// kernel, which reuses each staged center row for 32 frames.  The choice is
+// made on the device from the list's length.
+constexpr int64_t kFullFew = 64;
 
 // SPLIT: blockIdx.y selects one block of 32*G centers and the result of the
 // block goes to keys[entry] by atomicMin of (distance bits << 32 | center),
@@ -43,6 +51,7 @@ __global__ void __launch_bounds__(kThreads) assign_fp32_kernel(
         int64_t nd = *n_dev;
         n = nd < n_max ? nd : n_max;
     }
+    if (SPLIT && n <= kFullFew) return;  // full_few_kernel takes short lists
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
     const int64_t ntiles = (n + BM - 1) / BM;
@@ -192,6 +201,36 @@ __global__ void __launch_bounds__(256) recheck_rest_kernel(
     }
 }
 
+// Full re-check of a short list: one warp per (frame, 32 consecutive
+// centers), one exact distance per lane (sqdist_exact: the assignment's
+// arithmetic and order), the warp's smallest key, one atomicMin per warp.
+__global__ void __launch_bounds__(256) full_few_kernel(const float *__restrict__ X, const int32_t *__restrict__ frames,
+                                                       const int32_t *__restrict__ n_dev, int64_t n_max, int d,
+                                                       const float *__restrict__ C, int k,
+                                                       unsigned long long *__restrict__ keys) {
+    int64_t n = *n_dev;
+    if (n > n_max) n = n_max;
+    if (n > kFullFew) return;  // the tiled kernel takes long lists
+    const int lane = threadIdx.x & 31;
+    const int64_t groups = (k + 31) / 32;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < n * groups; w += nw) {
+        const int64_t e = w / groups;
+        const int j = (int)((w - e * groups) * 32) + lane;
+        unsigned long long key = ~0ull;
+        if (j < k) {
+            const float dd = sqdist_exact(X + (int64_t)frames[e] * d, C + (int64_t)j * d, d);
+            key = ((unsigned long long)__float_as_uint(dd) << 32) | (unsigned)j;
+        }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            const unsigned long long o = __shfl_xor_sync(0xffffffffu, key, off);
+            key = o < key ? o : key;
+        }
+        if (lane == 0) atomicMin(&keys[e], key);
+    }
+}
+
 // One thread per entry: the winning key becomes the label (label 0 when no
 // candidate distance is finite, as in the exact kernel).
 __global__ void __launch_bounds__(256) recheck_finalize_kernel(
@@ -275,6 +314,11 @@ int launch_full_recheck(const float *X, const int32_t *frames, const int32_t *n_
         set_error("k=%d: too many center blocks for the full re-check", k);
         return KM_ERR_BAD_SHAPE;
     }
+    int64_t gf = (std::min(n_max, kFullFew) * ((k + 31) / 32) + 7) / 8;  // 8 warps per block
+    const int64_t capf = (int64_t)num_sms() * 8;
+    if (gf > capf) gf = capf;
+    full_few_kernel<<<(unsigned)(gf < 1 ? 1 : gf), 256, 0, s>>>(X, frames, n_dev, n_max, d, C, k, keys);
+    KM_CUDA(cudaGetLastError());
     assign_fp32_kernel<FT, G, true><<<dim3((unsigned)gx, (unsigned)gy), kThreads, 0, s>>>(
         X, frames, n_dev, n_max, d, C, k, nullptr, nullptr, nullptr, keys);
     KM_CUDA(cudaGetLastError());

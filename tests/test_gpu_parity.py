@@ -80,20 +80,22 @@ def test_duplicate_centers_ties(torch, L, oracle, prec):
     assert got[:100].tolist() == list(range(100))  # exact hits go to the lowest duplicate
 
 
-def test_full_recheck_across_center_blocks(torch, L, oracle):
+@pytest.mark.parametrize("groups,reps", [(90, 30), (40, 0), (90, 0)])
+def test_full_recheck_across_center_blocks(torch, L, oracle, groups, reps):
     # Groups of 26 nearly equal centers overflow the candidate list of the
     # tensor-core pass (at most 16 entries); the exact copies of each group sit
-    # 256+ indexes apart, so the exact re-check must pick the lowest index
-    # across center blocks.
+    # 26 * groups apart, so the exact re-check must pick the lowest index
+    # across center blocks.  40 listed frames take the short-list kernel, the
+    # longer lists the tiled one.
     rng = np.random.default_rng(21)
-    d, groups = 96, 90
+    d = 96
     base = rng.normal(size=(groups, d)).astype(np.float32)
     near = [base + 1e-4 * rng.normal(size=base.shape).astype(np.float32) for _ in range(24)]
-    C = np.concatenate([base] + near + [base]).astype(np.float32)  # k = 26 * 90 = 2340
-    X = np.concatenate([base + 1e-3 * rng.normal(size=base.shape).astype(np.float32) for _ in range(30)])
-    X = np.concatenate([X, base]).astype(np.float32)
+    C = np.concatenate([base] + near + [base]).astype(np.float32)  # k = 26 * groups
+    X = [base + 1e-3 * rng.normal(size=base.shape).astype(np.float32) for _ in range(reps)]
+    X = np.concatenate(X + [base]).astype(np.float32)
     got, stats = gpu_assign(torch, L, X, C, "fp16")
-    assert stats["n_full"] > 0
+    assert stats["n_full"] >= groups
     np.testing.assert_array_equal(got, oracle.assign(X, C))
     assert got[-groups:].tolist() == list(range(groups))
 
