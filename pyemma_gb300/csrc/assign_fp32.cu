@@ -232,11 +232,12 @@ __global__ void __launch_bounds__(256) full_few_kernel(const float *__restrict__
 }
 
 // One thread per entry: the winning key becomes the label (label 0 when no
-// candidate distance is finite, as in the exact kernel).
+// candidate distance is finite, as in the exact kernel).  With a flip list
+// (flips non-null) a changed label is listed instead of written.
 __global__ void __launch_bounds__(256) recheck_finalize_kernel(
     const int32_t *__restrict__ rc_frames, const unsigned long long *__restrict__ keys,
     const int32_t *__restrict__ entry_count, int64_t max_entries, int32_t *__restrict__ labels,
-    unsigned long long *flipped) {
+    unsigned long long *flipped, int32_t *__restrict__ flips, int32_t *__restrict__ n_flips, int64_t max_flips) {
     int64_t count = *entry_count;
     if (count > max_entries) count = max_entries;
     unsigned long long nflip = 0;
@@ -246,8 +247,20 @@ __global__ void __launch_bounds__(256) recheck_finalize_kernel(
         const uint32_t dbits = (uint32_t)(key >> 32);
         const int lbl = dbits < 0x7f800000u ? (int)(uint32_t)key : 0;
         const int64_t frame = rc_frames[e];
-        if (labels[frame] != lbl) ++nflip;
-        labels[frame] = lbl;
+        const int before = labels[frame];
+        if (before != lbl) {
+            ++nflip;
+            if (flips) {
+                const int slot = atomicAdd(n_flips, 1);
+                if (slot < max_flips) {
+                    flips[3 * (int64_t)slot] = (int32_t)frame;
+                    flips[3 * (int64_t)slot + 1] = before;
+                    flips[3 * (int64_t)slot + 2] = lbl;
+                }
+            } else {
+                labels[frame] = lbl;
+            }
+        }
     }
     if (flipped && nflip) atomicAdd(flipped, nflip);
 }
@@ -270,9 +283,10 @@ int launch_assign_fp32(const float *X, const int32_t *frame_idx, const int32_t *
 int launch_recheck_pairs(const float *X, int d, const float *C, const int32_t *rc_frames, const int32_t *rc_best,
                          const int32_t *pair_entry, const int32_t *pair_center, const float *pair_lo,
                          unsigned long long *keys, const int32_t *counters, int64_t max_entries, int64_t max_pairs,
-                         int32_t *labels, unsigned long long *flipped, cudaStream_t s) {
+                         int32_t *labels, unsigned long long *flipped, cudaStream_t s, const FlipList *fl,
+                         int blocks_per_sm) {
     if (max_entries == 0) return KM_OK;
-    const int64_t cap = (int64_t)num_sms() * 8;
+    const int64_t cap = (int64_t)num_sms() * blocks_per_sm;
     int64_t g0 = (max_entries + 255) / 256;
     if (g0 > cap) g0 = cap;
     recheck_best_kernel<<<(unsigned)(g0 < 1 ? 1 : g0), 256, 0, s>>>(X, d, C, rc_frames, rc_best, counters,
@@ -285,15 +299,16 @@ int launch_recheck_pairs(const float *X, int d, const float *C, const int32_t *r
     KM_CUDA(cudaGetLastError());
     int64_t g2 = (max_entries + 255) / 256;
     if (g2 > cap) g2 = cap;
-    recheck_finalize_kernel<<<(unsigned)(g2 < 1 ? 1 : g2), 256, 0, s>>>(rc_frames, keys, counters, max_entries,
-                                                                       labels, flipped);
+    recheck_finalize_kernel<<<(unsigned)(g2 < 1 ? 1 : g2), 256, 0, s>>>(
+        rc_frames, keys, counters, max_entries, labels, flipped, fl ? fl->rows : nullptr, fl ? fl->count : nullptr,
+        fl ? fl->cap : 0);
     KM_CUDA(cudaGetLastError());
     return KM_OK;
 }
 
 int launch_full_recheck(const float *X, const int32_t *frames, const int32_t *n_dev, int64_t n_max, int d,
                         const float *C, int k, unsigned long long *keys, int32_t *labels,
-                        unsigned long long *flipped, cudaStream_t s) {
+                        unsigned long long *flipped, cudaStream_t s, const FlipList *fl) {
     if (n_max == 0) return KM_OK;
     // The list is short next to n_max: tiles of 32 frames x 256 centers,
     // one CTA per (frame tile, center block), so that a few thousand frames
@@ -325,7 +340,9 @@ int launch_full_recheck(const float *X, const int32_t *frames, const int32_t *n_
     int64_t g2 = (n_max + 255) / 256;
     const int64_t cap2 = (int64_t)num_sms() * 8;
     if (g2 > cap2) g2 = cap2;
-    recheck_finalize_kernel<<<(unsigned)g2, 256, 0, s>>>(frames, keys, n_dev, n_max, labels, flipped);
+    recheck_finalize_kernel<<<(unsigned)g2, 256, 0, s>>>(frames, keys, n_dev, n_max, labels, flipped,
+                                                          fl ? fl->rows : nullptr, fl ? fl->count : nullptr,
+                                                          fl ? fl->cap : 0);
     KM_CUDA(cudaGetLastError());
     return KM_OK;
 }

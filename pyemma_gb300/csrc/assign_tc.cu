@@ -1497,8 +1497,13 @@ int tc_prepare_centers(const float *C, int d, int k, TcBuffers &b, cudaStream_t 
     return KM_OK;
 }
 
-int tc_assign(const float *X, int64_t n, int d, const float *C, int k, int32_t *labels, TcBuffers &b,
-              cudaStream_t s, ProfEvents *prof, float *dump, unsigned long long *wait_cycles) {
+namespace {
+
+constexpr int kRecheckBesidePerSm = 4;
+
+int tc_assign_impl(const float *X, int64_t n, int d, const float *C, int k, int32_t *labels, TcBuffers &b,
+                   cudaStream_t s, ProfEvents *prof, float *dump, unsigned long long *wait_cycles, cudaStream_t side,
+                   cudaEvent_t ev_fork, const FlipList *fl) {
     if (n == 0) return KM_OK;
     Plan pl;
     if (!make_plan(d, k, pl) || !device_is_sm10x()) {
@@ -1614,14 +1619,36 @@ int tc_assign(const float *X, int64_t n, int d, const float *C, int k, int32_t *
     KM_CUDA(cudaGetLastError());
     if (prof) prof->end(kProfTc, s);
 
-    if (prof) prof->begin(kProfRecheck, s);
+    // The exact re-checks: on s, or on `side` beside the caller's next work.
+    cudaStream_t r = s;
+    if (side) {
+        KM_CUDA(cudaEventRecord(ev_fork, s));
+        KM_CUDA(cudaStreamWaitEvent(side, ev_fork, 0));
+        r = side;
+    }
+    if (prof) prof->begin(kProfRecheck, r);
+    // Beside the centroid update the re-check keeps to half of each SM's
+    // threads, so that both stay resident.
     KM_TRY(launch_recheck_pairs(X, d, C, b.rc_frames, b.rc_best, b.pair_entry, b.pair_center, b.pair_lo, b.rc_keys,
-                                b.counters, n, n * kL, labels, b.flipped, s));
-    if (prof) prof->end(kProfRecheck, s);
-    if (prof) prof->begin(kProfFull, s);
-    KM_TRY(launch_full_recheck(X, b.full_frames, b.counters + 1, n, d, C, k, b.full_keys, labels, b.flipped, s));
-    if (prof) prof->end(kProfFull, s);
+                                b.counters, n, n * kL, labels, b.flipped, r, fl, side ? kRecheckBesidePerSm : 8));
+    if (prof) prof->end(kProfRecheck, r);
+    if (prof) prof->begin(kProfFull, r);
+    KM_TRY(launch_full_recheck(X, b.full_frames, b.counters + 1, n, d, C, k, b.full_keys, labels, b.flipped, r, fl));
+    if (prof) prof->end(kProfFull, r);
     return KM_OK;
+}
+
+}  // namespace
+
+int tc_assign(const float *X, int64_t n, int d, const float *C, int k, int32_t *labels, TcBuffers &b,
+              cudaStream_t s, ProfEvents *prof, float *dump, unsigned long long *wait_cycles) {
+    return tc_assign_impl(X, n, d, C, k, labels, b, s, prof, dump, wait_cycles, nullptr, nullptr, nullptr);
+}
+
+int tc_assign_deferred(const float *X, int64_t n, int d, const float *C, int k, int32_t *labels, TcBuffers &b,
+                       cudaStream_t s, cudaStream_t side, cudaEvent_t ev_fork, const FlipList &fl,
+                       ProfEvents *prof) {
+    return tc_assign_impl(X, n, d, C, k, labels, b, s, prof, nullptr, nullptr, side, ev_fork, &fl);
 }
 
 }  // namespace km

@@ -238,6 +238,10 @@ size_t lloyd_ws_bytes(int64_t n, int d, int k, int prec) {
     c.take<double>(1);             // cost
     c.take<uint32_t>(1);           // error word
     c.take<char>(assign_ws_bytes(n, d, k, prec));
+    if (is_tc(prec)) {
+        c.take<int32_t>(3 * (size_t)n);  // flip list
+        c.take<int32_t>(1);              // its count
+    }
     return c.bytes();
 }
 
@@ -548,6 +552,29 @@ int lloyd_run(const float *X_in, const HostFrames *hf, int64_t n, int32_t d, int
     uint32_t *err = cv.take<uint32_t>(1);
     void *ws_assign = cv.take<char>(assign_ws_bytes(n, d, k, prec));
 
+    // Tensor-core iterations run the exact re-check on a side stream beside
+    // the centroid update, which sums by the tensor-core labels; the frames
+    // whose exact label differs then move between clusters before the new
+    // centers are formed.
+    FlipList fl;
+    struct Side {
+        cudaStream_t st = nullptr;
+        cudaEvent_t fork = nullptr, join = nullptr;
+        ~Side() {
+            if (fork) cudaEventDestroy(fork);
+            if (join) cudaEventDestroy(join);
+            if (st) cudaStreamDestroy(st);
+        }
+    } side;
+    if (is_tc(prec)) {
+        fl.rows = cv.take<int32_t>(3 * (size_t)n);
+        fl.count = cv.take<int32_t>(1);
+        fl.cap = n;
+        KM_CUDA(cudaStreamCreateWithFlags(&side.st, cudaStreamNonBlocking));
+        KM_CUDA(cudaEventCreateWithFlags(&side.fork, cudaEventDisableTiming));
+        KM_CUDA(cudaEventCreateWithFlags(&side.join, cudaEventDisableTiming));
+    }
+
     TcBuffers b;
     if (is_tc(prec)) {
         // The shift and scale stay fixed for the whole run so that the 16-bit
@@ -580,7 +607,18 @@ int lloyd_run(const float *X_in, const HostFrames *hf, int64_t n, int32_t d, int
     auto enqueue = [&](cudaStream_t st) -> int {
         if (is_tc(prec)) {
             KM_TRY(tc_prepare_centers(C, d, k, b, st));
-            KM_TRY(tc_assign(X, n, d, C, k, labels, b, st, &prof));
+            KM_CUDA(cudaMemsetAsync(fl.count, 0, sizeof(int32_t), st));
+            KM_TRY(tc_assign_deferred(X, n, d, C, k, labels, b, st, side.st, side.fork, fl, &prof));
+            prof.begin(kProfUpdate, st);
+            // one segment-sum CTA per SM: room for the re-check beside it
+            KM_TRY(launch_update_accumulate(X, n, d, labels, k, C, err, ws_update, st, 1));
+            KM_CUDA(cudaEventRecord(side.join, side.st));
+            KM_CUDA(cudaStreamWaitEvent(st, side.join, 0));
+            KM_TRY(launch_apply_flips(X, n, d, k, C, fl, labels, ws_update, st));
+            KM_TRY(launch_update_finish(n, d, k, C, C_new, nullptr, cost, ws_update, st));
+            prof.end(kProfUpdate, st);
+            KM_CUDA(cudaMemcpyAsync(C, C_new, sizeof(float) * k * d, cudaMemcpyDeviceToDevice, st));
+            return KM_OK;
         } else {
             prof.begin(kProfFp32, st);
             KM_TRY(launch_assign_fp32(X, nullptr, nullptr, n, d, C, k, labels, nullptr, nullptr, st));

@@ -37,20 +37,34 @@ int launch_assign_fp32(const float *X, const int32_t *frame_idx, const int32_t *
                        int d, const float *C, int k, int32_t *labels, float *dist,
                        unsigned long long *flipped, cudaStream_t s);
 
+// Labels that an exact re-check changes, listed instead of written: entry i
+// is (frame, label before, exact label) at rows[3i..3i+2]; *count (device)
+// counts them (at most cap).  A Lloyd iteration lets the centroid update run
+// on the tensor-core labels while the re-check runs beside it, then moves the
+// listed frames between clusters (launch_apply_flips).
+struct FlipList {
+    int32_t *rows = nullptr;
+    int32_t *count = nullptr;
+    int64_t cap = 0;
+};
+
+// Exact re-evaluation of the frames frames[0..*n_dev) against all centers,
+// split over (frame tile, center block) CTAs; keys[e] must hold ~0 on entry.
+// With fl the changed labels go to the list and labels stays as it is.
+int launch_full_recheck(const float *X, const int32_t *frames, const int32_t *n_dev, int64_t n_max, int d,
+                        const float *C, int k, unsigned long long *keys, int32_t *labels,
+                        unsigned long long *flipped, cudaStream_t s, const FlipList *fl = nullptr);
+
 // Exact float32 re-evaluation of the candidates the tensor-core kernel could
 // not separate: pair q = (entry pair_entry[q], center pair_center[q]); entry e
 // stands for frame rc_frames[e] and keys[e] (initialised to ~0) collects the
-// winner.  counters[0] = entries, counters[2] = pairs (device).
-// Exact re-evaluation of the frames frames[0..*n_dev) against all centers,
-// split over (frame tile, center block) CTAs; keys[e] must hold ~0 on entry.
-int launch_full_recheck(const float *X, const int32_t *frames, const int32_t *n_dev, int64_t n_max, int d,
-                        const float *C, int k, unsigned long long *keys, int32_t *labels,
-                        unsigned long long *flipped, cudaStream_t s);
-
+// winner.  counters[0] = entries, counters[2] = pairs (device).  With fl the
+// changed labels go to the list and labels stays as it is.
 int launch_recheck_pairs(const float *X, int d, const float *C, const int32_t *rc_frames, const int32_t *rc_best,
                          const int32_t *pair_entry, const int32_t *pair_center, const float *pair_lo,
                          unsigned long long *keys, const int32_t *counters, int64_t max_entries, int64_t max_pairs,
-                         int32_t *labels, unsigned long long *flipped, cudaStream_t s);
+                         int32_t *labels, unsigned long long *flipped, cudaStream_t s, const FlipList *fl = nullptr,
+                         int blocks_per_sm = 8);
 
 // ---- update.cu -------------------------------------------------------------
 size_t update_ws_size(int64_t n, int d, int k);
@@ -59,6 +73,18 @@ size_t update_ws_size(int64_t n, int d, int k);
 int launch_update(const float *X, int64_t n, int d, const int32_t *labels, int k,
                   const float *C_old, float *C_new, int64_t *counts_out, double *cost,
                   uint32_t *err, void *ws, cudaStream_t s);
+// launch_update in two halves: the sums over the members (counting sort and
+// segment sums) and the new centers and inertia from those sums.
+// seg_per_sm > 0 caps the segment-sum CTAs per SM (room for a kernel beside it).
+int launch_update_accumulate(const float *X, int64_t n, int d, const int32_t *labels, int k, const float *C_old,
+                             uint32_t *err, void *ws, cudaStream_t s, int seg_per_sm = 0);
+int launch_update_finish(int64_t n, int d, int k, const float *C_old, float *C_new, int64_t *counts_out,
+                         double *cost, void *ws, cudaStream_t s);
+// Between the halves: moves the frames of a flip list from the cluster of
+// their first label to that of their exact label (sums, squared sums, counts,
+// with the accumulation's float32 deviations) and writes the exact labels.
+int launch_apply_flips(const float *X, int64_t n, int d, int k, const float *C_old, const FlipList &fl,
+                       int32_t *labels, void *ws, cudaStream_t s);
 
 // ---- kmpp.cu -----------------------------------------------------------------
 size_t kmpp_ws_size(int64_t n, int d, int k);
@@ -124,6 +150,13 @@ int tc_prepare_centers(const float *C, int d, int k, TcBuffers &b, cudaStream_t 
 int tc_assign(const float *X, int64_t n, int d, const float *C, int k, int32_t *labels,
               TcBuffers &b, cudaStream_t s, ProfEvents *prof = nullptr, float *dump = nullptr,
               unsigned long long *wait_cycles = nullptr);
+// The tensor-core pass on s, then the exact re-checks on `side` (after
+// ev_fork, recorded on s) with their changed labels in fl (whose count must
+// be zero when the re-checks start).  labels holds the tensor-core labels;
+// the caller joins `side` back into s before it applies fl.
+int tc_assign_deferred(const float *X, int64_t n, int d, const float *C, int k, int32_t *labels, TcBuffers &b,
+                       cudaStream_t s, cudaStream_t side, cudaEvent_t ev_fork, const FlipList &fl,
+                       ProfEvents *prof = nullptr);
 
 // Resident center sets (capi.cu), used by the serving loop (serve.cu).
 int assign_centers_enqueue(const float *X, int64_t n, const km_centers *h, int32_t *labels, void *ws,

@@ -249,9 +249,11 @@ __device__ __forceinline__ void ring_fetch(void *dst, const void *src, uint32_t 
 
 // Ring rows hold MW*32 floats (zero beyond d), so the inner loop needs no
 // bounds test.
-size_t bulk_smem_bytes(int mw) { return (size_t)kBulkWarps * ((size_t)kRing * mw * 128 + 2 * kPiece * 4 + kRing * 8); }
+size_t bulk_smem_bytes(int mw, int ring) {
+    return (size_t)kBulkWarps * ((size_t)ring * mw * 128 + 2 * kPiece * 4 + ring * 8);
+}
 
-template <int MW>
+template <int MW, int RING>
 __global__ void __launch_bounds__(kBulkWarps * 32, (MW > 17 ? 1 : 2)) seg_accumulate_bulk_kernel(
     const float *__restrict__ X, int d, const int32_t *__restrict__ perm, const int32_t *__restrict__ slab,
     int64_t n_max, const int32_t *__restrict__ n_sorted, const float *__restrict__ C_old, double *__restrict__ S,
@@ -261,14 +263,14 @@ __global__ void __launch_bounds__(kBulkWarps * 32, (MW > 17 ? 1 : 2)) seg_accumu
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
     const uint32_t row_bytes = (uint32_t)d * 4u;
-    unsigned char *wbase = smem_bulk + (size_t)warp * ((size_t)kRing * RS * 4 + 2 * kPiece * 4 + kRing * 8);
+    unsigned char *wbase = smem_bulk + (size_t)warp * ((size_t)RING * RS * 4 + 2 * kPiece * 4 + RING * 8);
     float *ring = reinterpret_cast<float *>(wbase);
-    int32_t *pidx = reinterpret_cast<int32_t *>(wbase + (size_t)kRing * RS * 4);
+    int32_t *pidx = reinterpret_cast<int32_t *>(wbase + (size_t)RING * RS * 4);
     int32_t *plab = pidx + kPiece;
     uint64_t *bars = reinterpret_cast<uint64_t *>(plab + kPiece);
-    for (int e = lane; e < kRing * RS; e += 32) ring[e] = 0.0f;  // the tails beyond d stay zero
+    for (int e = lane; e < RING * RS; e += 32) ring[e] = 0.0f;  // the tails beyond d stay zero
     if (lane == 0) {
-        for (int r = 0; r < kRing; ++r) ring_bar_init(&bars[r]);
+        for (int r = 0; r < RING; ++r) ring_bar_init(&bars[r]);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncwarp();
@@ -291,12 +293,12 @@ __global__ void __launch_bounds__(kBulkWarps * 32, (MW > 17 ? 1 : 2)) seg_accumu
         int issued = 0;
         auto issue = [&](int q) {  // the whole warp calls; lane 0 issues
             if (lane == 0) {
-                const int slot = q & (kRing - 1);
+                const int slot = q & (RING - 1);
                 ring_fetch(ring + (size_t)slot * RS, X + (int64_t)pidx[q] * d, row_bytes, &bars[slot]);
             }
             ++issued;
         };
-        for (int q = 0; q < cnt && q < kRing; ++q) issue(q);
+        for (int q = 0; q < cnt && q < RING; ++q) issue(q);
 
         // Per feature a Kahan sum (ks, kc: the sum is ks - kc); per row the
         // squared deviations of the lane's features in two FMA chains, added
@@ -316,7 +318,7 @@ __global__ void __launch_bounds__(kBulkWarps * 32, (MW > 17 ? 1 : 2)) seg_accumu
         };
         int q = 0;
         for (; q < cnt; ++q) {
-            const int slot = q & (kRing - 1);
+            const int slot = q & (RING - 1);
             ok = __all_sync(0xffffffffu, ring_bar_wait(&bars[slot], (phase >> slot) & 1u));
             if (!ok) break;
             phase ^= 1u << slot;
@@ -349,18 +351,18 @@ __global__ void __launch_bounds__(kBulkWarps * 32, (MW > 17 ? 1 : 2)) seg_accumu
             }
             qacc.add(q0 + q1);
             __syncwarp();
-            if (q + kRing < cnt) {
+            if (q + RING < cnt) {
                 // The slot's shared-memory reads above come before the copy
                 // that overwrites it.
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                issue(q + kRing);
+                issue(q + RING);
             }
         }
         if (cur >= 0 && ok) flush();
         if (!ok) {
             // Let the copies still in flight land before the CTA exits.
             for (int r = q; r < issued; ++r) {
-                const int slot = r & (kRing - 1);
+                const int slot = r & (RING - 1);
                 ring_bar_wait(&bars[slot], (phase >> slot) & 1u);
                 phase ^= 1u << slot;
             }
@@ -452,6 +454,47 @@ __global__ void finalize_kernel(const double *__restrict__ S, const double *__re
     if (counts_out && lane == 0) counts_out[j] = cnt;
 }
 
+// One warp per listed frame: its contribution (float32 deviations from the
+// previous centers, as the segment sums take them) leaves the cluster of its
+// first label and joins that of its exact label.
+__global__ void apply_flips_kernel(const float *__restrict__ X, int d, const float *__restrict__ C_old,
+                                   const int32_t *__restrict__ flips, const int32_t *__restrict__ n_flips,
+                                   int64_t max_flips, int32_t *__restrict__ labels, int32_t *__restrict__ counts,
+                                   double *__restrict__ S, double *__restrict__ Q) {
+    int64_t nf = *n_flips;
+    if (nf > max_flips) nf = max_flips;
+    const int lane = threadIdx.x & 31;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nf; w += nw) {
+        const int64_t frame = flips[3 * w];
+        const int from = flips[3 * w + 1];
+        const int to = flips[3 * w + 2];
+        const float *x = X + frame * d;
+        const float *cf = C_old + (int64_t)from * d;
+        const float *ct = C_old + (int64_t)to * d;
+        double qf = 0.0, qt = 0.0;
+        for (int f = lane; f < d; f += 32) {
+            const float tf = __fsub_rn(x[f], cf[f]);
+            const float tt = __fsub_rn(x[f], ct[f]);
+            atomicAdd(&S[(int64_t)from * d + f], -(double)tf);
+            atomicAdd(&S[(int64_t)to * d + f], (double)tt);
+            qf += (double)__fmul_rn(tf, tf);
+            qt += (double)__fmul_rn(tt, tt);
+        }
+        for (int off = 16; off > 0; off >>= 1) {
+            qf += __shfl_xor_sync(0xffffffffu, qf, off);
+            qt += __shfl_xor_sync(0xffffffffu, qt, off);
+        }
+        if (lane == 0) {
+            atomicAdd(&Q[from], -qf);
+            atomicAdd(&Q[to], qt);
+            atomicSub(&counts[from], 1);
+            atomicAdd(&counts[to], 1);
+            labels[frame] = to;
+        }
+    }
+}
+
 // Single CTA, fixed summation tree: the same inputs give the same cost.
 __global__ void __launch_bounds__(1024) reduce_cost_kernel(const double *__restrict__ ccost, int k,
                                                             double *__restrict__ cost) {
@@ -496,43 +539,53 @@ bool try_wide(int mw, const float *X, int64_t n, int d, const UpdateWs &u, int k
     return true;
 }
 
-template <int MW>
-int launch_bulk(const float *X, int64_t n, int d, const UpdateWs &u, int k, const float *C_old, uint32_t *err,
-                cudaStream_t s) {
-    const size_t smem = bulk_smem_bytes(MW);
+template <int MW, int RING>
+int launch_bulk_ring(const float *X, int64_t n, int d, const UpdateWs &u, int k, const float *C_old, uint32_t *err,
+                     cudaStream_t s, int seg_per_sm) {
+    const size_t smem = bulk_smem_bytes(MW, RING);
     static int per_sm = -1;  // cached: no attribute calls while a stream is being captured
     if (per_sm < 0) {
-        KM_CUDA(cudaFuncSetAttribute(seg_accumulate_bulk_kernel<MW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)(232448)));
+        KM_CUDA(cudaFuncSetAttribute(seg_accumulate_bulk_kernel<MW, RING>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(232448)));
         int v = 0;
-        KM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, seg_accumulate_bulk_kernel<MW>, kBulkWarps * 32,
-                                                              smem));
+        KM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, seg_accumulate_bulk_kernel<MW, RING>,
+                                                              kBulkWarps * 32, smem));
         per_sm = v > 0 ? v : 1;
     }
     const int64_t npieces = (n + kPiece - 1) / kPiece;
     int64_t g = (npieces + kBulkWarps - 1) / kBulkWarps;
-    const int64_t cap = (int64_t)num_sms() * per_sm;
+    const int64_t cap = (int64_t)num_sms() * (seg_per_sm > 0 && seg_per_sm < per_sm ? seg_per_sm : per_sm);
     if (g > cap) g = cap;
-    seg_accumulate_bulk_kernel<MW><<<(unsigned)(g < 1 ? 1 : g), kBulkWarps * 32, smem, s>>>(
+    seg_accumulate_bulk_kernel<MW, RING><<<(unsigned)(g < 1 ? 1 : g), kBulkWarps * 32, smem, s>>>(
         X, d, u.perm, u.slab, n, u.offsets + k, C_old, u.S, u.Q, err);
     KM_CUDA(cudaGetLastError());
     return KM_OK;
 }
 
+// One CTA per SM (room for another kernel beside it) keeps twice the rows in
+// flight per warp when they fit in shared memory.
+template <int MW>
+int launch_bulk(const float *X, int64_t n, int d, const UpdateWs &u, int k, const float *C_old, uint32_t *err,
+                cudaStream_t s, int seg_per_sm) {
+    if (seg_per_sm == 1 && bulk_smem_bytes(MW, 2 * kRing) <= 227 * 1024)
+        return launch_bulk_ring<MW, 2 * kRing>(X, n, d, u, k, C_old, err, s, seg_per_sm);
+    return launch_bulk_ring<MW, kRing>(X, n, d, u, k, C_old, err, s, seg_per_sm);
+}
+
 int launch_segments_bulk(const float *X, int64_t n, int d, const UpdateWs &u, int k, const float *C_old,
-                         uint32_t *err, cudaStream_t s) {
+                         uint32_t *err, cudaStream_t s, int seg_per_sm) {
     const int mw = (d + 31) / 32;
     switch (mw) {
-        case 1: return launch_bulk<1>(X, n, d, u, k, C_old, err, s);
-        case 2: return launch_bulk<2>(X, n, d, u, k, C_old, err, s);
-        case 3: return launch_bulk<3>(X, n, d, u, k, C_old, err, s);
-        case 4: return launch_bulk<4>(X, n, d, u, k, C_old, err, s);
-        case 5: case 6: return launch_bulk<6>(X, n, d, u, k, C_old, err, s);
-        case 7: case 8: return launch_bulk<8>(X, n, d, u, k, C_old, err, s);
-        case 9: case 10: case 11: case 12: return launch_bulk<12>(X, n, d, u, k, C_old, err, s);
-        case 13: case 14: case 15: case 16: case 17: return launch_bulk<17>(X, n, d, u, k, C_old, err, s);
-        case 18: case 19: case 20: case 21: case 22: case 23: case 24: return launch_bulk<24>(X, n, d, u, k, C_old, err, s);
-        default: return launch_bulk<32>(X, n, d, u, k, C_old, err, s);
+        case 1: return launch_bulk<1>(X, n, d, u, k, C_old, err, s, seg_per_sm);
+        case 2: return launch_bulk<2>(X, n, d, u, k, C_old, err, s, seg_per_sm);
+        case 3: return launch_bulk<3>(X, n, d, u, k, C_old, err, s, seg_per_sm);
+        case 4: return launch_bulk<4>(X, n, d, u, k, C_old, err, s, seg_per_sm);
+        case 5: case 6: return launch_bulk<6>(X, n, d, u, k, C_old, err, s, seg_per_sm);
+        case 7: case 8: return launch_bulk<8>(X, n, d, u, k, C_old, err, s, seg_per_sm);
+        case 9: case 10: case 11: case 12: return launch_bulk<12>(X, n, d, u, k, C_old, err, s, seg_per_sm);
+        case 13: case 14: case 15: case 16: case 17: return launch_bulk<17>(X, n, d, u, k, C_old, err, s, seg_per_sm);
+        case 18: case 19: case 20: case 21: case 22: case 23: case 24: return launch_bulk<24>(X, n, d, u, k, C_old, err, s, seg_per_sm);
+        default: return launch_bulk<32>(X, n, d, u, k, C_old, err, s, seg_per_sm);
     }
 }
 
@@ -575,9 +628,8 @@ size_t update_ws_size(int64_t n, int d, int k) {
     return b;
 }
 
-int launch_update(const float *X, int64_t n, int d, const int32_t *labels, int k,
-                  const float *C_old, float *C_new, int64_t *counts_out, double *cost,
-                  uint32_t *err, void *ws, cudaStream_t s) {
+int launch_update_accumulate(const float *X, int64_t n, int d, const int32_t *labels, int k, const float *C_old,
+                             uint32_t *err, void *ws, cudaStream_t s, int seg_per_sm) {
     UpdateWs u = carve(ws, n, d, k, nullptr);
     KM_CUDA(cudaMemsetAsync(u.counts, 0, sizeof(int32_t) * k, s));
     KM_CUDA(cudaMemsetAsync(u.S, 0, sizeof(double) * (size_t)k * d, s));
@@ -592,19 +644,42 @@ int launch_update(const float *X, int64_t n, int d, const int32_t *labels, int k
         scatter_kernel<<<grid_for(n, 256, 8), 256, 0, s>>>(labels, n, k, u.cursor, u.perm, u.slab);
         KM_CUDA(cudaGetLastError());
         if (bulk_ok(X, d)) {
-            KM_TRY(launch_segments_bulk(X, n, d, u, k, C_old, err, s));
+            KM_TRY(launch_segments_bulk(X, n, d, u, k, C_old, err, s, seg_per_sm));
         } else {
             const int64_t npieces = (n + kPiece - 1) / kPiece;
             const unsigned g = grid_for(npieces * 32, 256, 8);
             KM_TRY(launch_segments(X, n, d, u, k, C_old, g, s));
         }
     }
+    return KM_OK;
+}
+
+int launch_update_finish(int64_t n, int d, int k, const float *C_old, float *C_new, int64_t *counts_out,
+                         double *cost, void *ws, cudaStream_t s) {
+    UpdateWs u = carve(ws, n, d, k, nullptr);
     finalize_kernel<<<(unsigned)(((int64_t)k * 32 + 255) / 256), 256, 0, s>>>(
         u.S, u.Q, u.counts, C_old, C_new, d, k, u.ccost, counts_out);
     KM_CUDA(cudaGetLastError());
     reduce_cost_kernel<<<1, 1024, 0, s>>>(u.ccost, k, cost);
     KM_CUDA(cudaGetLastError());
     return KM_OK;
+}
+
+int launch_apply_flips(const float *X, int64_t n, int d, int k, const float *C_old, const FlipList &fl,
+                       int32_t *labels, void *ws, cudaStream_t s) {
+    if (fl.cap == 0) return KM_OK;
+    UpdateWs u = carve(ws, n, d, k, nullptr);
+    apply_flips_kernel<<<grid_for(fl.cap * 32, 256, 4), 256, 0, s>>>(X, d, C_old, fl.rows, fl.count, fl.cap, labels,
+                                                                     u.counts, u.S, u.Q);
+    KM_CUDA(cudaGetLastError());
+    return KM_OK;
+}
+
+int launch_update(const float *X, int64_t n, int d, const int32_t *labels, int k,
+                  const float *C_old, float *C_new, int64_t *counts_out, double *cost,
+                  uint32_t *err, void *ws, cudaStream_t s) {
+    KM_TRY(launch_update_accumulate(X, n, d, labels, k, C_old, err, ws, s));
+    return launch_update_finish(n, d, k, C_old, C_new, counts_out, cost, ws, s);
 }
 
 }  // namespace km
