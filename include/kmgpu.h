@@ -183,6 +183,39 @@ int km_lloyd_host(const float *const *X_parts, const int64_t *part_rows, int32_t
                   int32_t *labels, double *inertias, int32_t *n_iter, int32_t *converged, km_callback cb,
                   void *cb_user, void *workspace, size_t workspace_bytes, void *stream);
 
+/* ---- the minRMSD metric ----------------------------------------------------
+ * Stands in for the minRMSD metric plug-in of
+ * pyemma/coordinates/clustering/src/clustering_module.cpp:9-36 (RMSDMetric,
+ * registered into deeptime's clustering; reached by cluster_kmeans(...,
+ * metric='minRMSD') and assign_to_centers(..., metric='minRMSD')).  Rows are
+ * atom-major (x0 y0 z0 x1 ...), d = 3 n_atoms; other d give
+ * KM_ERR_BAD_SHAPE, as the reference raises.  The squared metric is the mean
+ * square deviation after optimal translation and rotation (Theobald's
+ * quaternion characteristic polynomial).
+ *
+ * km_assign_minrmsd: labels (device, n) of the lowest-index center with the
+ *   smallest msd; rmsd (device, n, nullable) receives sqrt(msd) as float.
+ * km_minrmsd_rows: rmsd[i] = the metric of the row pair (X[i], Y[i])
+ *   (compute_metric, clustering_module.cpp:41-43).
+ * km_kmpp_minrmsd: kmeans++ with D^2 = msd (km_kmpp's draws); C0 receives
+ *   the chosen frames (uncentered), idx (device, nullable) their indexes.
+ * km_lloyd_minrmsd: Lloyd iterations as km_lloyd, assigning by the metric;
+ *   the new center is the mean of its members, the inertia the sum of the
+ *   members' msd to the new centers. */
+size_t km_assign_minrmsd_workspace_size(int64_t n, int32_t d, int32_t k);
+int km_assign_minrmsd(const float *X, int64_t n, int32_t d, const float *C, int32_t k, int32_t *labels, float *rmsd,
+                      void *workspace, size_t workspace_bytes, void *stream);
+size_t km_minrmsd_rows_workspace_size(int64_t n, int32_t d);
+int km_minrmsd_rows(const float *X, const float *Y, int64_t n, int32_t d, float *rmsd, void *workspace,
+                    size_t workspace_bytes, void *stream);
+size_t km_kmpp_minrmsd_workspace_size(int64_t n, int32_t d, int32_t k);
+int km_kmpp_minrmsd(const float *X, int64_t n, int32_t d, int32_t k, uint32_t seed, float *C0, int64_t *idx,
+                    km_callback cb, void *cb_user, void *workspace, size_t workspace_bytes, void *stream);
+size_t km_lloyd_minrmsd_workspace_size(int64_t n, int32_t d, int32_t k);
+int km_lloyd_minrmsd(const float *X, int64_t n, int32_t d, int32_t k, float *C, int32_t max_iter, double tolerance,
+                     int32_t *labels, double *inertias, int32_t *n_iter, int32_t *converged, km_callback cb,
+                     void *cb_user, void *workspace, size_t workspace_bytes, void *stream);
+
 /* ---- precision autotuning (no counterpart in the reference) ---------------
  * KM_PREC_AUTO picks the faster of the exact FP32 kernel and the tensor-core
  * path by a rule measured on a d x k sweep.  km_tune measures instead: it

@@ -406,3 +406,296 @@ int kmo_regspace(const float *X, int64_t n, int32_t d, double dmin, int32_t max_
     *n_centers = nc;
     return 0;
 }
+
+/* ------------------------------------------------------------------ */
+/* minRMSD metric                                                     */
+/* ------------------------------------------------------------------ */
+/* The minRMSD metric of pyemma/coordinates/clustering/src/
+ * clustering_module.cpp:9-36 (RMSDMetric, registered into deeptime's
+ * clustering): frames are atom-major (x0 y0 z0 x1 ...), d = 3 n_atoms; the
+ * squared metric is the mean square deviation after optimal translation and
+ * rotation, found with the quaternion characteristic polynomial method
+ * (Theobald, Acta Cryst. A61:478-480, 2005; mdtraj's libtheobald, which the
+ * reference links).  mdtraj is absent, so its float order is unpinned; this
+ * restatement fixes one order, which the CUDA kernels follow operation for
+ * operation:
+ *
+ *   centering  per row, the per-axis sum over atoms in double in the order of
+ *              a 32-lane warp: lane l sums atoms l, l+32, ... in turn, then an
+ *              xor butterfly (offsets 16, 8, 4, 2, 1) adds the lanes; the mean
+ *              is that sum / n_atoms; a = (float)(x - mean).  G = sum of a^2
+ *              (double products, double sums) in the same lane order.
+ *   pair       S[p][q] = sum_i a_i[p] b_i[q], float fused multiply-adds in atom
+ *              order; then in double: C2 = -2 sum S^2, C1 = -8 det S,
+ *              C0 = det K (the 4x4 key matrix, Laplace expansion on row 0);
+ *              Newton on lambda^4 + C2 lambda^2 + C1 lambda + C0 from
+ *              (Ga + Gb) / 2, at most 50 steps, until |step| < 1e-11 |lambda|;
+ *              msd = max(0, (Ga + Gb - 2 lambda) / n_atoms).
+ *   assign     the lowest-index minimum of msd (NaN never wins; label 0 when
+ *              no msd is a number).
+ *   update     the mean of the members (kmo_update: deeptime's center update
+ *              does not depend on the metric); inertia = sum_i msd(x_i,
+ *              new center of its label) (assumption: deeptime's cost for a
+ *              custom metric could not be checked).
+ *   kmeans++   D^2 sampling with D^2 = (float)msd, the draws of kmo_kmpp. */
+
+static double butterfly32(double s[32]) {
+    double t[32];
+    for (int off = 16; off > 0; off >>= 1) {
+        for (int l = 0; l < 32; ++l) t[l] = s[l] + s[l ^ off];
+        memcpy(s, t, sizeof(t));
+    }
+    return s[0];
+}
+
+/* Centers one atom-major row (n_atoms = d / 3) into a; returns G. */
+double kmo_rmsd_center(const float *x, int32_t n_atoms, float *a) {
+    double mean[3];
+    for (int c = 0; c < 3; ++c) {
+        double s[32];
+        for (int l = 0; l < 32; ++l) {
+            double acc = 0.0;
+            for (int32_t i = l; i < n_atoms; i += 32) acc += (double)x[3 * i + c];
+            s[l] = acc;
+        }
+        mean[c] = butterfly32(s) / (double)n_atoms;
+    }
+    double g[32];
+    for (int l = 0; l < 32; ++l) {
+        double acc = 0.0;
+        for (int32_t i = l; i < n_atoms; i += 32)
+            for (int c = 0; c < 3; ++c) {
+                const float v = (float)((double)x[3 * i + c] - mean[c]);
+                acc += (double)v * (double)v;
+            }
+        g[l] = acc;
+    }
+    for (int32_t i = 0; i < n_atoms; ++i)
+        for (int c = 0; c < 3; ++c) a[3 * i + c] = (float)((double)x[3 * i + c] - mean[c]);
+    return butterfly32(g);
+}
+
+static double det3(double a, double b, double c, double d, double e, double f, double g, double h, double i) {
+    return a * (e * i - f * h) - b * (d * i - f * g) + c * (d * h - e * g);
+}
+
+/* msd of two centered rows a, b with traces ga, gb. */
+double kmo_rmsd_msd(const float *a, const float *b, double ga, double gb, int32_t n_atoms) {
+    float S[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int32_t i = 0; i < n_atoms; ++i)
+        for (int p = 0; p < 3; ++p)
+            for (int q = 0; q < 3; ++q) S[3 * p + q] = fmaf(a[3 * i + p], b[3 * i + q], S[3 * p + q]);
+    const double xx = S[0], xy = S[1], xz = S[2], yx = S[3], yy = S[4], yz = S[5], zx = S[6], zy = S[7], zz = S[8];
+    double ss = 0.0;
+    for (int e = 0; e < 9; ++e) ss += (double)S[e] * (double)S[e];
+    const double C2 = -2.0 * ss;
+    const double C1 = -8.0 * det3(xx, xy, xz, yx, yy, yz, zx, zy, zz);
+    const double K[4][4] = {{xx + yy + zz, yz - zy, zx - xz, xy - yx},
+                            {yz - zy, xx - yy - zz, xy + yx, zx + xz},
+                            {zx - xz, xy + yx, -xx + yy - zz, yz + zy},
+                            {xy - yx, zx + xz, yz + zy, -xx - yy + zz}};
+    const double m0 = det3(K[1][1], K[1][2], K[1][3], K[2][1], K[2][2], K[2][3], K[3][1], K[3][2], K[3][3]);
+    const double m1 = det3(K[1][0], K[1][2], K[1][3], K[2][0], K[2][2], K[2][3], K[3][0], K[3][2], K[3][3]);
+    const double m2 = det3(K[1][0], K[1][1], K[1][3], K[2][0], K[2][1], K[2][3], K[3][0], K[3][1], K[3][3]);
+    const double m3 = det3(K[1][0], K[1][1], K[1][2], K[2][0], K[2][1], K[2][2], K[3][0], K[3][1], K[3][2]);
+    const double C0 = K[0][0] * m0 - K[0][1] * m1 + K[0][2] * m2 - K[0][3] * m3;
+    double lam = 0.5 * (ga + gb);
+    for (int it = 0; it < 50; ++it) {
+        const double l2 = lam * lam;
+        const double a2 = l2 + C2;
+        const double P = (a2 * l2 + C1 * lam) + C0;
+        const double D = (2.0 * lam) * (l2 + a2) + C1;
+        if (D == 0.0) break;
+        const double step = P / D;
+        const double next = lam - step;
+        lam = next;
+        if (fabs(step) < 1e-11 * fabs(next)) break;
+    }
+    const double msd = ((ga + gb) - 2.0 * lam) / (double)n_atoms;
+    return msd > 0.0 ? msd : 0.0;
+}
+
+/* Centers every row of an (n, d) array (d = 3 n_atoms). */
+static int rmsd_center_all(const float *X, int64_t n, int32_t d, float **Xc, double **G, int32_t n_threads) {
+    *Xc = (float *)malloc((size_t)n * d * sizeof(float));
+    *G = (double *)malloc((size_t)n * sizeof(double));
+    if (!*Xc || !*G) {
+        free(*Xc);
+        free(*G);
+        return KMO_NOMEM;
+    }
+#pragma omp parallel for num_threads(n_threads) schedule(static)
+    for (int64_t i = 0; i < n; ++i) (*G)[i] = kmo_rmsd_center(X + (size_t)i * d, d / 3, *Xc + (size_t)i * d);
+    return KMO_OK;
+}
+
+int kmo_assign_minrmsd(const float *X, int64_t n, int32_t d, const float *C, int32_t k, int32_t *labels,
+                       double *msd_out, int32_t n_threads) {
+    if (n < 0 || d <= 0 || d % 3 || k <= 0 || !C || !labels) return KMO_BAD_ARG;
+    if (n == 0) return KMO_OK;
+    if (n_threads <= 0) n_threads = 1;
+    float *Xc, *Cc;
+    double *G, *H;
+    int rc = rmsd_center_all(X, n, d, &Xc, &G, n_threads);
+    if (rc) return rc;
+    rc = rmsd_center_all(C, k, d, &Cc, &H, n_threads);
+    if (rc) {
+        free(Xc);
+        free(G);
+        return rc;
+    }
+#pragma omp parallel for num_threads(n_threads) schedule(static)
+    for (int64_t i = 0; i < n; ++i) {
+        double best = 0.0;
+        int32_t bj = -1;
+        for (int32_t j = 0; j < k; ++j) {
+            const double m = kmo_rmsd_msd(Xc + (size_t)i * d, Cc + (size_t)j * d, G[i], H[j], d / 3);
+            if (m == m && (bj < 0 || m < best)) {
+                best = m;
+                bj = j;
+            }
+        }
+        labels[i] = bj < 0 ? 0 : bj;
+        if (msd_out) msd_out[i] = bj < 0 ? NAN : best;
+    }
+    free(Xc);
+    free(G);
+    free(Cc);
+    free(H);
+    return KMO_OK;
+}
+
+/* rmsd = sqrt(msd) of row pairs (X[i], Y[i]), as compute_metric returns it. */
+int kmo_minrmsd_rows(const float *X, const float *Y, int64_t n, int32_t d, float *out) {
+    if (n < 0 || d <= 0 || d % 3) return KMO_BAD_ARG;
+    float *a = (float *)malloc((size_t)d * sizeof(float));
+    float *b = (float *)malloc((size_t)d * sizeof(float));
+    if (!a || !b) {
+        free(a);
+        free(b);
+        return KMO_NOMEM;
+    }
+    for (int64_t i = 0; i < n; ++i) {
+        const double ga = kmo_rmsd_center(X + (size_t)i * d, d / 3, a);
+        const double gb = kmo_rmsd_center(Y + (size_t)i * d, d / 3, b);
+        out[i] = (float)sqrt(kmo_rmsd_msd(a, b, ga, gb, d / 3));
+    }
+    free(a);
+    free(b);
+    return KMO_OK;
+}
+
+/* inertia of an assignment under the metric: sum_i msd(x_i, C[labels[i]]). */
+static double minrmsd_cost(const float *X, int64_t n, int32_t d, const float *C, int32_t k, const int32_t *labels,
+                           int32_t n_threads) {
+    float *Cc;
+    double *H;
+    if (rmsd_center_all(C, k, d, &Cc, &H, n_threads)) return NAN;
+    double cost = 0.0;
+    float *a = (float *)malloc((size_t)d * sizeof(float));
+    for (int64_t i = 0; i < n; ++i) {
+        const double g = kmo_rmsd_center(X + (size_t)i * d, d / 3, a);
+        const int32_t j = labels[i];
+        cost += kmo_rmsd_msd(a, Cc + (size_t)j * d, g, H[j], d / 3);
+    }
+    free(a);
+    free(Cc);
+    free(H);
+    return cost;
+}
+
+int kmo_lloyd_minrmsd(const float *X, int64_t n, int32_t d, int32_t k, float *C, int32_t max_iter, double tol,
+                      int32_t *labels, double *inertias, int32_t *n_iter, int32_t *converged, int32_t n_threads) {
+    if (n <= 0 || d <= 0 || d % 3 || k <= 0 || !C || !labels || max_iter < 0) return KMO_BAD_ARG;
+    float *Cn = (float *)malloc((size_t)k * d * sizeof(float));
+    int64_t *cnt = (int64_t *)malloc((size_t)k * sizeof(int64_t));
+    if (!Cn || !cnt) {
+        free(Cn);
+        free(cnt);
+        return KMO_NOMEM;
+    }
+    double prev = 0.0;
+    int32_t it = 0, conv = 0;
+    int rc = KMO_OK;
+    while (it < max_iter) {
+        rc = kmo_assign_minrmsd(X, n, d, C, k, labels, NULL, n_threads);
+        if (rc) break;
+        double unused;
+        rc = kmo_update(X, n, d, labels, k, C, Cn, cnt, &unused, NULL);
+        if (rc) break;
+        memcpy(C, Cn, (size_t)k * d * sizeof(float));
+        const double cost = minrmsd_cost(X, n, d, C, k, labels, n_threads);
+        if (inertias) inertias[it] = cost;
+        double rel = cost != 0.0 ? fabs(cost - prev) / cost : 0.0;
+        prev = cost;
+        ++it;
+        if (rel <= tol) {
+            conv = 1;
+            break;
+        }
+    }
+    free(Cn);
+    free(cnt);
+    if (n_iter) *n_iter = it;
+    if (converged) *converged = conv;
+    return rc;
+}
+
+int kmo_kmpp_minrmsd(const float *X, int64_t n, int32_t d, int32_t k, uint32_t seed, float *C0, int64_t *idx_out,
+                     int32_t n_threads) {
+    if (n <= 0 || d <= 0 || d % 3 || k <= 0 || !X || !C0) return KMO_BAD_ARG;
+    if (n_threads <= 0) n_threads = 1;
+    float *Xc;
+    double *G;
+    int rc = rmsd_center_all(X, n, d, &Xc, &G, n_threads);
+    if (rc) return rc;
+    int64_t p = (int64_t)mulhi64(kmo_kmpp_draw(seed, 0), (uint64_t)n);
+    memcpy(C0, X + (size_t)p * d, (size_t)d * sizeof(float));
+    if (idx_out) idx_out[0] = p;
+    float *mind = (float *)malloc((size_t)n * sizeof(float));
+    if (!mind) {
+        free(Xc);
+        free(G);
+        return KMO_NOMEM;
+    }
+    int64_t last = p;
+    double scale = 0.0;
+    for (int32_t r = 1; r < k; ++r) {
+#pragma omp parallel for num_threads(n_threads) schedule(static)
+        for (int64_t i = 0; i < n; ++i) {
+            const float dd = (float)kmo_rmsd_msd(Xc + (size_t)i * d, Xc + (size_t)last * d, G[i], G[last], d / 3);
+            if (r == 1 || dd < mind[i]) mind[i] = dd;
+        }
+        if (r == 1) {
+            float M = 0.0f;
+            for (int64_t i = 0; i < n; ++i)
+                if (isfinite(mind[i]) && mind[i] > M) M = mind[i];
+            int e = kmo_quant_exponent(M, n);
+            scale = (e == INT32_MIN) ? 0.0 : ldexp(1.0, e);
+        }
+        uint64_t total = 0;
+        for (int64_t i = 0; i < n; ++i) total += quant_weight(mind[i], scale);
+        uint64_t r64 = kmo_kmpp_draw(seed, (uint32_t)r);
+        if (total == 0) {
+            p = (int64_t)mulhi64(r64, (uint64_t)n);
+        } else {
+            uint64_t t = mulhi64(r64, total);
+            uint64_t acc = 0;
+            p = n - 1;
+            for (int64_t i = 0; i < n; ++i) {
+                acc += quant_weight(mind[i], scale);
+                if (acc > t) {
+                    p = i;
+                    break;
+                }
+            }
+        }
+        memcpy(C0 + (size_t)r * d, X + (size_t)p * d, (size_t)d * sizeof(float));
+        if (idx_out) idx_out[r] = p;
+        last = p;
+    }
+    free(mind);
+    free(Xc);
+    free(G);
+    return KMO_OK;
+}

@@ -44,7 +44,16 @@ def lib():
         L.kmo_lloyd.argtypes = [P, i64, i32, i32, P, i32, f64, P, P, P, P, i32]
         L.kmo_kmpp.argtypes = [P, i64, i32, i32, u32, P, P, i32]
         L.kmo_regspace.argtypes = [P, i64, i32, f64, i32, P, P, P]
-        for name in ("kmo_assign", "kmo_update", "kmo_lloyd", "kmo_kmpp"):
+        L.kmo_rmsd_center.argtypes = [P, i32, P]
+        L.kmo_rmsd_center.restype = f64
+        L.kmo_rmsd_msd.argtypes = [P, P, f64, f64, i32]
+        L.kmo_rmsd_msd.restype = f64
+        L.kmo_assign_minrmsd.argtypes = [P, i64, i32, P, i32, P, P, i32]
+        L.kmo_minrmsd_rows.argtypes = [P, P, i64, i32, P]
+        L.kmo_lloyd_minrmsd.argtypes = [P, i64, i32, i32, P, i32, f64, P, P, P, P, i32]
+        L.kmo_kmpp_minrmsd.argtypes = [P, i64, i32, i32, u32, P, P, i32]
+        for name in ("kmo_assign", "kmo_update", "kmo_lloyd", "kmo_kmpp", "kmo_assign_minrmsd", "kmo_minrmsd_rows",
+                     "kmo_lloyd_minrmsd", "kmo_kmpp_minrmsd"):
             getattr(L, name).restype = ctypes.c_int
         _lib = L
     return _lib
@@ -174,6 +183,75 @@ def count_matrix(dtrajs, lag, sliding=True, nstates=None):
         keep = (row >= 0) & (col >= 0) & (row < nstates) & (col < nstates)
         np.add.at(C, (row[keep], col[keep]), 1)
     return C
+
+
+def assign_minrmsd(X, C, n_threads=None, return_msd=False):
+    """int32 labels of the nearest center under the minRMSD metric (d = 3 n_atoms, atom-major)."""
+    X = _f32(X)
+    C = _f32(C)
+    n, d = X.shape
+    labels = np.empty(n, dtype=np.int32)
+    msd = np.empty(n, dtype=np.float64) if return_msd else None
+    _check(lib().kmo_assign_minrmsd(_ptr(X), n, d, _ptr(C), C.shape[0], _ptr(labels), _ptr(msd),
+                                    n_threads or default_threads()), "assign_minrmsd")
+    return (labels, msd) if return_msd else labels
+
+
+def minrmsd_rows(X, Y):
+    """float32 minRMSD of the row pairs (X[i], Y[i]) (compute_metric)."""
+    X = _f32(np.atleast_2d(X))
+    Y = _f32(np.atleast_2d(Y))
+    out = np.empty(X.shape[0], dtype=np.float32)
+    _check(lib().kmo_minrmsd_rows(_ptr(X), _ptr(Y), X.shape[0], X.shape[1], _ptr(out)), "minrmsd_rows")
+    return out
+
+
+def rmsd_center(x):
+    """(centered float32 row, trace G) of one atom-major row."""
+    x = _f32(x).ravel()
+    a = np.empty_like(x)
+    g = lib().kmo_rmsd_center(_ptr(x), x.size // 3, _ptr(a))
+    return a, g
+
+
+def lloyd_minrmsd(X, C0, max_iter, tol, n_threads=None):
+    """Lloyd iterations under the minRMSD metric (mean update); as lloyd()."""
+    X = _f32(X)
+    C = _f32(C0).copy()
+    n, d = X.shape
+    k = C.shape[0]
+    labels = np.zeros(n, dtype=np.int32)
+    inertias = np.zeros(max(1, max_iter), dtype=np.float64)
+    n_iter = np.zeros(1, dtype=np.int32)
+    conv = np.zeros(1, dtype=np.int32)
+    _check(lib().kmo_lloyd_minrmsd(_ptr(X), n, d, k, _ptr(C), max_iter, float(tol), _ptr(labels), _ptr(inertias),
+                                   _ptr(n_iter), _ptr(conv), n_threads or default_threads()), "lloyd_minrmsd")
+    it = int(n_iter[0])
+    return dict(centers=C, labels=labels, inertias=inertias[:it].copy(), n_iter=it, converged=bool(conv[0]))
+
+
+def kmpp_minrmsd(X, k, seed, n_threads=None):
+    """kmeans++ under the minRMSD metric; returns (centers, frame indices)."""
+    X = _f32(X)
+    n, d = X.shape
+    C0 = np.empty((k, d), dtype=np.float32)
+    idx = np.empty(k, dtype=np.int64)
+    _check(lib().kmo_kmpp_minrmsd(_ptr(X), n, d, k, int(seed) & 0xFFFFFFFF, _ptr(C0), _ptr(idx),
+                                  n_threads or default_threads()), "kmpp_minrmsd")
+    return C0, idx
+
+
+def kabsch_rmsd_fp64(x, y):
+    """Independent float64 check of minRMSD: optimal rotation by SVD (Kabsch)."""
+    a = np.asarray(x, dtype=np.float64).reshape(-1, 3)
+    b = np.asarray(y, dtype=np.float64).reshape(-1, 3)
+    a = a - a.mean(axis=0)
+    b = b - b.mean(axis=0)
+    u, s, vt = np.linalg.svd(a.T @ b)
+    sign = np.sign(np.linalg.det(u @ vt))
+    s[-1] *= sign
+    msd = (np.sum(a * a) + np.sum(b * b) - 2.0 * np.sum(s)) / a.shape[0]
+    return float(np.sqrt(max(msd, 0.0)))
 
 
 def pair_distances(xyz, pairs):

@@ -17,7 +17,7 @@ LIB_DIR = os.path.join(HERE, "_lib")
 LIB_PATH = os.path.join(LIB_DIR, "libkmgpu.so")
 INCLUDE_DIR = os.path.join(os.path.dirname(HERE), "include")
 
-SOURCES = ["capi.cu", "assign_fp32.cu", "assign_tc.cu", "update.cu", "kmpp.cu", "serve.cu", "regspace.cu", "counts.cu", "featurize.cu"]
+SOURCES = ["capi.cu", "assign_fp32.cu", "assign_tc.cu", "update.cu", "kmpp.cu", "serve.cu", "regspace.cu", "counts.cu", "featurize.cu", "minrmsd.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O3", "--expt-relaxed-constexpr",
               "-I" + INCLUDE_DIR]

@@ -36,7 +36,9 @@ EXPORTED = (
     "km_serve_create", "km_serve_add_centers", "km_serve_submit", "km_serve_poll", "km_serve_stats_read",
     "km_serve_shutdown", "km_tune_workspace_size", "km_tune", "km_tune_clear",
     "km_regspace_workspace_size", "km_regspace", "km_count_matrix_workspace_size", "km_count_matrix",
-    "km_pair_distances",
+    "km_pair_distances", "km_assign_minrmsd_workspace_size", "km_assign_minrmsd", "km_minrmsd_rows_workspace_size",
+    "km_minrmsd_rows", "km_kmpp_minrmsd_workspace_size", "km_kmpp_minrmsd", "km_lloyd_minrmsd_workspace_size",
+    "km_lloyd_minrmsd",
 )
 
 
@@ -131,6 +133,16 @@ def load(build_if_missing=False):
     L.km_lloyd_workspace_size.restype = sz
     L.km_lloyd.argtypes = [P, i64, i32, i32, P, i32, f64, i32, P, P, P, P, CALLBACK, P, P, sz, P]
     L.km_lloyd_host.argtypes = [P, P, i32, P, i64, i32, i32, P, i32, f64, i32, P, P, P, P, CALLBACK, P, P, sz, P]
+    for name, args in (("km_assign_minrmsd_workspace_size", [i64, i32, i32]),
+                       ("km_minrmsd_rows_workspace_size", [i64, i32]),
+                       ("km_kmpp_minrmsd_workspace_size", [i64, i32, i32]),
+                       ("km_lloyd_minrmsd_workspace_size", [i64, i32, i32])):
+        getattr(L, name).argtypes = args
+        getattr(L, name).restype = sz
+    L.km_assign_minrmsd.argtypes = [P, i64, i32, P, i32, P, P, P, sz, P]
+    L.km_minrmsd_rows.argtypes = [P, P, i64, i32, P, P, sz, P]
+    L.km_kmpp_minrmsd.argtypes = [P, i64, i32, i32, u32, P, P, CALLBACK, P, P, sz, P]
+    L.km_lloyd_minrmsd.argtypes = [P, i64, i32, i32, P, i32, f64, P, P, P, P, CALLBACK, P, P, sz, P]
     pp = ctypes.POINTER(ctypes.c_void_p)
     L.km_centers_create.argtypes = [P, i32, i32, i32, P, pp]
     L.km_centers_destroy.argtypes = [P]
@@ -162,6 +174,7 @@ def load(build_if_missing=False):
     L.km_pair_distances.argtypes = [P, i64, i32, P, i32, P, P]
     L.km_pair_distances.restype = ctypes.c_int
     for name in ("km_assign", "km_batch_assign", "km_update", "km_kmpp", "km_lloyd", "km_lloyd_host",
+                 "km_assign_minrmsd", "km_minrmsd_rows", "km_kmpp_minrmsd", "km_lloyd_minrmsd",
                  "km_centers_create",
                  "km_centers_destroy", "km_centers_info", "km_assign_centers", "km_serve_create",
                  "km_serve_add_centers", "km_serve_submit", "km_serve_poll", "km_serve_stats_read",
@@ -412,6 +425,85 @@ def lloyd_host(parts, C, max_iter, tolerance, precision="auto", callback=None, X
                           None, _ptr(ws), ws_bytes, _stream(torch, C.device)))
     del keep
     return dict(X=X, labels=labels, inertias=inertias[:n_iter.value].copy(), n_iter=n_iter.value,
+                converged=bool(conv.value))
+
+
+# ---------------------------------------------------------------------------
+# the minRMSD metric (atom-major rows, d = 3 n_atoms)
+# ---------------------------------------------------------------------------
+def assign_minrmsd(X, C, labels=None, return_rmsd=False):
+    """Labels of the nearest center under the minRMSD metric (and, when asked,
+    the metric value to it)."""
+    torch = _torch()
+    L = load()
+    _check_frames(torch, X)
+    _check_frames(torch, C, "C")
+    n, d = X.shape
+    k = C.shape[0]
+    if labels is None:
+        labels = torch.empty(n, dtype=torch.int32, device=X.device)
+    rmsd = torch.empty(n, dtype=torch.float32, device=X.device) if return_rmsd else None
+    ws_bytes = L.km_assign_minrmsd_workspace_size(n, d, k)
+    ws = _workspace(torch, ws_bytes, X.device)
+    check(L.km_assign_minrmsd(_ptr(X), n, d, _ptr(C), k, _ptr(labels), _ptr(rmsd), _ptr(ws), ws_bytes,
+                              _stream(torch, X.device)))
+    return (labels, rmsd) if return_rmsd else labels
+
+
+def minrmsd_rows(X, Y):
+    """float32 minRMSD of the row pairs (X[i], Y[i])."""
+    torch = _torch()
+    L = load()
+    _check_frames(torch, X)
+    _check_frames(torch, Y, "Y")
+    n, d = X.shape
+    if tuple(Y.shape) != (n, d):
+        raise ValueError("X and Y must have the same shape")
+    out = torch.empty(n, dtype=torch.float32, device=X.device)
+    ws_bytes = L.km_minrmsd_rows_workspace_size(n, d)
+    ws = _workspace(torch, ws_bytes, X.device)
+    check(L.km_minrmsd_rows(_ptr(X), _ptr(Y), n, d, _ptr(out), _ptr(ws), ws_bytes, _stream(torch, X.device)))
+    return out
+
+
+def kmpp_minrmsd(X, k, seed, callback=None):
+    """kmeans++ initial centers under the minRMSD metric and the chosen frame indices."""
+    torch = _torch()
+    L = load()
+    _check_frames(torch, X)
+    n, d = X.shape
+    C0 = torch.empty((k, d), dtype=torch.float32, device=X.device)
+    idx = torch.empty(k, dtype=torch.int64, device=X.device)
+    ws_bytes = L.km_kmpp_minrmsd_workspace_size(n, d, k)
+    ws = _workspace(torch, ws_bytes, X.device)
+    cb, keep = _callback(callback)
+    check(L.km_kmpp_minrmsd(_ptr(X), n, d, k, int(seed) & 0xFFFFFFFF, _ptr(C0), _ptr(idx), cb, None, _ptr(ws),
+                            ws_bytes, _stream(torch, X.device)))
+    del keep
+    return C0, idx
+
+
+def lloyd_minrmsd(X, C, max_iter, tolerance, callback=None, labels=None):
+    """Lloyd iterations under the minRMSD metric, in place on C."""
+    torch = _torch()
+    L = load()
+    _check_frames(torch, X)
+    _check_frames(torch, C, "C")
+    n, d = X.shape
+    k = C.shape[0]
+    if labels is None:
+        labels = torch.empty(n, dtype=torch.int32, device=X.device)
+    inertias = np.zeros(max(1, max_iter), dtype=np.float64)
+    n_iter = ctypes.c_int32(0)
+    conv = ctypes.c_int32(0)
+    ws_bytes = L.km_lloyd_minrmsd_workspace_size(n, d, k)
+    ws = _workspace(torch, ws_bytes, X.device)
+    cb, keep = _callback(callback)
+    check(L.km_lloyd_minrmsd(_ptr(X), n, d, k, _ptr(C), int(max_iter), float(tolerance), _ptr(labels),
+                             inertias.ctypes.data_as(ctypes.c_void_p), ctypes.byref(n_iter), ctypes.byref(conv),
+                             cb, None, _ptr(ws), ws_bytes, _stream(torch, X.device)))
+    del keep
+    return dict(labels=labels, inertias=inertias[:n_iter.value].copy(), n_iter=n_iter.value,
                 converged=bool(conv.value))
 
 

@@ -78,7 +78,13 @@ def centers_to_device(centers):
     return torch.from_numpy(c).to(device())
 
 
-def assign_trajs(trajs, centers, precision="auto", batch_bytes=None):
+def check_minrmsd_dim(dim):
+    if dim % 3 != 0:
+        # clustering_module.cpp:13-15 raises the same condition
+        raise ValueError("RMSDMetric is only implemented for input data with a dimension divisible by 3.")
+
+
+def assign_trajs(trajs, centers, precision="auto", batch_bytes=None, metric="euclidean"):
     """int32 labels for every frame of every trajectory; returns (list, stats)."""
     torch = torch_module()
     centers = np.ascontiguousarray(centers, dtype=np.float32)
@@ -89,6 +95,8 @@ def assign_trajs(trajs, centers, precision="auto", batch_bytes=None):
         if t.ndim != 2 or t.shape[1] != dim:
             raise ValueError("cluster centers have wrong dimension. Have dim=%i, but input has %i"
                              % (dim, t.shape[1] if t.ndim == 2 else 1))
+    if metric == "minRMSD":
+        check_minrmsd_dim(dim)
     C = centers_to_device(centers)
     budget = max(1, int((batch_bytes or BATCH_BYTES) // (4 * dim)))
     outs = [np.empty(len(t), dtype=np.int32) for t in trajs]
@@ -112,7 +120,11 @@ def assign_trajs(trajs, centers, precision="auto", batch_bytes=None):
         X = pack_to_device(arrays, dim)
         offsets = np.zeros(len(arrays) + 1, dtype=np.int64)
         offsets[1:] = np.cumsum([len(a) for a in arrays])
-        labels, st = _lib.batch_assign(X, offsets, C, precision=precision)
+        if metric == "minRMSD":
+            labels = _lib.assign_minrmsd(X, C)
+            st = dict(n_frames=int(X.shape[0]), n_recheck=0, n_full=0, n_flipped=0, precision="fp32")
+        else:
+            labels, st = _lib.batch_assign(X, offsets, C, precision=precision)
         host = labels.cpu().numpy()
         for (i, a, b), o0, o1 in zip(batch, offsets[:-1], offsets[1:]):
             outs[i][a:b] = host[o0:o1]

@@ -21,7 +21,9 @@ class AbstractClustering(object):
     Parameters
     ----------
     metric : str, default='euclidean'
-        Distance of the assignment.  Only 'euclidean' has a kernel here.
+        Distance of the assignment: 'euclidean', or 'minRMSD' (atom-major
+        coordinates, d = 3 n_atoms: the RMSD after optimal superposition,
+        clustering_module.cpp:9-36).
     n_jobs : int or None
         Accepted for compatibility (thread count of the reference's OpenMP
         backend); resolved as the reference does and otherwise unused.
@@ -55,8 +57,6 @@ class AbstractClustering(object):
     def metric(self, value):
         if value not in _METRICS:
             raise ValueError("metric must be one of %s, was %r" % (_METRICS, value))
-        if value == "minRMSD":
-            raise NotImplementedError("the minRMSD metric has no GPU kernel in this build; use 'euclidean'")
         self._metric = value
 
     @property
@@ -184,7 +184,8 @@ class AbstractClustering(object):
     def _assign_arrays(self, arrays):
         if self.clustercenters is None or len(self.clustercenters) == 0:
             raise ValueError("no cluster centers to assign to")
-        labels, stats = _device.assign_trajs(arrays, self.clustercenters, precision=self.precision)
+        labels, stats = _device.assign_trajs(arrays, self.clustercenters, precision=self.precision,
+                                             metric=self.metric)
         self.last_assign_stats = stats
         return labels
 

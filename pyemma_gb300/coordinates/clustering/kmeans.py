@@ -29,7 +29,8 @@ class KmeansClustering(AbstractClustering):
     max_iter : int
         Maximum number of Lloyd iterations.
     metric : str
-        'euclidean' (minRMSD has no kernel in this build).
+        'euclidean' or 'minRMSD' (atom-major coordinates; assignment by the
+        RMSD after optimal superposition, centers as member means).
     tolerance : float
         Stop when the relative change of the inertia
         C(S) = sum_i sum_{x in S_i} ||x - mu_i||^2 is <= tolerance.
@@ -158,6 +159,9 @@ class KmeansClustering(AbstractClustering):
             self.logger.info("The number of cluster centers was not specified, "
                              "using min(sqrt(N), 5000)=%s as n_clusters." % self.n_clusters)
         dim = source.dimension()
+        minrmsd = self.metric == "minRMSD"
+        if minrmsd:
+            _device.check_minrmsd_dim(dim)
         reuse = self._init_in_memory_chunks(total_length, dim)
 
         host_parts = None
@@ -166,7 +170,7 @@ class KmeansClustering(AbstractClustering):
             if not self._check_resume_iteration() and self.init_strategy == "uniform":
                 indices = self._uniform_indices(traj_lengths, total_length)
                 self.clustercenters = self._uniform_centers(trajs, indices)
-            if self._check_resume_iteration():
+            if self._check_resume_iteration() and not minrmsd:
                 # Centers known (given, or drawn uniformly above) before the
                 # frames reach the device: the copy overlaps the first
                 # assignment (km_lloyd_host).
@@ -186,9 +190,13 @@ class KmeansClustering(AbstractClustering):
                     raise ValueError("initial centers have shape %s, data has dimension %d"
                                      % (self.clustercenters.shape, dim))
                 C = _device.centers_to_device(self.clustercenters)
+            elif minrmsd:
+                C, _ = _lib.kmpp_minrmsd(self._in_memory_chunks, int(self.n_clusters), self.fixed_seed)
             else:
                 C, _ = _lib.kmpp(self._in_memory_chunks, int(self.n_clusters), self.fixed_seed)
-            if host_parts is not None:
+            if minrmsd:
+                res = _lib.lloyd_minrmsd(self._in_memory_chunks, C, int(self.max_iter), float(self.tolerance))
+            elif host_parts is not None:
                 res = _lib.lloyd_host(host_parts, C, int(self.max_iter), float(self.tolerance),
                                       precision=self.precision)
                 self._in_memory_chunks = res["X"]
@@ -273,6 +281,9 @@ class MiniBatchKmeansClustering(KmeansClustering):
         if sum(sizes) == 0:
             raise ValueError("batch_size %s selects no frames" % self.batch_size)
         dim = source.dimension()
+        minrmsd = self.metric == "minRMSD"
+        if minrmsd:
+            _device.check_minrmsd_dim(dim)
         C = None
         if self._check_resume_iteration():
             C = _device.centers_to_device(self.clustercenters)
@@ -287,9 +298,13 @@ class MiniBatchKmeansClustering(KmeansClustering):
                     idx = np.random.choice(Xb.shape[0], int(self.n_clusters), replace=False)
                     C = Xb[_device.torch_module().from_numpy(np.sort(idx)).to(Xb.device)].contiguous()
                 else:
-                    C, _ = _lib.kmpp(Xb, int(self.n_clusters), int(np.random.randint(0, 2 ** 32 - 1, dtype=np.int64)))
+                    seed = int(np.random.randint(0, 2 ** 32 - 1, dtype=np.int64))
+                    C, _ = (_lib.kmpp_minrmsd if minrmsd else _lib.kmpp)(Xb, int(self.n_clusters), seed)
                 self.initial_centers_ = C.cpu().numpy()
-            res = _lib.lloyd(Xb, C, 1, -1.0, precision=self.precision)
+            if minrmsd:
+                res = _lib.lloyd_minrmsd(Xb, C, 1, -1.0)
+            else:
+                res = _lib.lloyd(Xb, C, 1, -1.0, precision=self.precision)
             cost = float(res["inertias"][0])
             inertias.append(cost)
             rel_change = abs(cost - prev_cost) / cost if cost != 0.0 else 0.0

@@ -88,8 +88,17 @@ int launch_apply_flips(const float *X, int64_t n, int d, int k, const float *C_o
 
 // ---- kmpp.cu -----------------------------------------------------------------
 size_t kmpp_ws_size(int64_t n, int d, int k);
+// D^2 of kmeans++ under the minRMSD metric: the centered frames Xc with
+// their traces G; idx (device, k) receives the chosen frames and names the
+// newest center of each round.
+struct KmppMetric {
+    const float *Xc;
+    const double *G;
+    const int64_t *idx;
+};
 int run_kmpp(const float *X, int64_t n, int d, int k, uint32_t seed, float *C0, int64_t *idx,
-             void (*cb)(void *), void *cb_user, void *ws, cudaStream_t s);
+             void (*cb)(void *), void *cb_user, void *ws, cudaStream_t s, const KmppMetric *metric = nullptr);
+
 
 // ---- assign_tc.cu ------------------------------------------------------------
 // Tensor-core (tcgen05, FP16 operands) assignment with exact FP32 recheck.

@@ -19,6 +19,7 @@
 // per-tile weight sums; HBM-bound) and one single-CTA pick kernel.
 #include "km_common.cuh"
 #include "km_internal.h"
+#include "km_rmsd.cuh"
 
 namespace km {
 
@@ -63,16 +64,25 @@ __device__ __forceinline__ unsigned long long block_sum_u64(unsigned long long v
     return s;  // valid in thread 0
 }
 
+// D^2 of frame i to center c (round r's newest center, frame idx[r] under
+// the minRMSD metric).
+__device__ __forceinline__ float kmpp_d2(const float *__restrict__ X, int64_t i, int d, const float *__restrict__ c,
+                                         const KmppMetric &m, int r) {
+    if (!m.Xc) return sqdist_exact(X + i * d, c, d);
+    const int64_t p = m.idx[r];
+    return __double2float_rn(rmsd_msd_rows(m.Xc + i * d, m.Xc + p * d, m.G[i], m.G[p], d / 3));
+}
+
 // Round 1 pass: mind = D^2 to center 0; max of the finite values.
 __global__ void __launch_bounds__(kTileThreads) kmpp_first_kernel(
     const float *__restrict__ X, int64_t n, int d, const float *__restrict__ c0,
-    float *__restrict__ mind, uint32_t *__restrict__ maxbits) {
+    float *__restrict__ mind, uint32_t *__restrict__ maxbits, KmppMetric m) {
     float mx = 0.0f;
     const int64_t t0 = (int64_t)blockIdx.x * kTile;
     for (int u = 0; u < kTile / kTileThreads; ++u) {
         const int64_t i = t0 + u * kTileThreads + threadIdx.x;
         if (i < n) {
-            const float dd = sqdist_exact(X + i * d, c0, d);
+            const float dd = kmpp_d2(X, i, d, c0, m, 0);
             mind[i] = dd;
             if (dd < __int_as_float(0x7f800000) && dd > mx) mx = dd;
         }
@@ -125,7 +135,7 @@ __global__ void __launch_bounds__(kTileThreads) kmpp_weights_kernel(
 __global__ void __launch_bounds__(kTileThreads) kmpp_round_kernel(
     const float *__restrict__ X, int64_t n, int d, const float *__restrict__ c,
     float *__restrict__ mind, const double *__restrict__ scale_p,
-    unsigned long long *__restrict__ tile_sum) {
+    unsigned long long *__restrict__ tile_sum, KmppMetric m, int r_center) {
     __shared__ unsigned long long red[kTileThreads / 32];
     const double scale = *scale_p;
     const int64_t t0 = (int64_t)blockIdx.x * kTile;
@@ -133,13 +143,13 @@ __global__ void __launch_bounds__(kTileThreads) kmpp_round_kernel(
     for (int u = 0; u < kTile / kTileThreads; ++u) {
         const int64_t i = t0 + u * kTileThreads + threadIdx.x;
         if (i < n) {
-            const float dd = sqdist_exact(X + i * d, c, d);
-            float m = mind[i];
-            if (dd < m) {
-                m = dd;
-                mind[i] = m;
+            const float dd = kmpp_d2(X, i, d, c, m, r_center);
+            float mi = mind[i];
+            if (dd < mi) {
+                mi = dd;
+                mind[i] = mi;
             }
-            s += quant_weight(m, scale);
+            s += quant_weight(mi, scale);
         }
     }
     s = block_sum_u64(s, red);
@@ -233,7 +243,8 @@ size_t kmpp_ws_size(int64_t n, int d, int k) {
 }
 
 int run_kmpp(const float *X, int64_t n, int d, int k, uint32_t seed, float *C0, int64_t *idx,
-             void (*cb)(void *), void *cb_user, void *ws, cudaStream_t s) {
+             void (*cb)(void *), void *cb_user, void *ws, cudaStream_t s, const KmppMetric *metric) {
+    const KmppMetric m = metric ? *metric : KmppMetric{nullptr, nullptr, nullptr};
     if (n <= 0) {
         set_error("kmeans++ needs at least one frame");
         return KM_ERR_BAD_SHAPE;
@@ -246,7 +257,7 @@ int run_kmpp(const float *X, int64_t n, int d, int k, uint32_t seed, float *C0, 
     if (cb) cb(cb_user);
     if (k == 1) return KM_OK;
     KM_CUDA(cudaMemsetAsync(w.maxbits, 0, sizeof(uint32_t), s));
-    kmpp_first_kernel<<<(unsigned)ntiles, kTileThreads, 0, s>>>(X, n, d, C0, w.mind, w.maxbits);
+    kmpp_first_kernel<<<(unsigned)ntiles, kTileThreads, 0, s>>>(X, n, d, C0, w.mind, w.maxbits, m);
     KM_CUDA(cudaGetLastError());
     kmpp_scale_kernel<<<1, 1, 0, s>>>(w.maxbits, n, w.scale);
     KM_CUDA(cudaGetLastError());
@@ -255,7 +266,7 @@ int run_kmpp(const float *X, int64_t n, int d, int k, uint32_t seed, float *C0, 
     for (int r = 1; r < k; ++r) {
         if (r >= 2) {
             kmpp_round_kernel<<<(unsigned)ntiles, kTileThreads, 0, s>>>(
-                X, n, d, C0 + (int64_t)(r - 1) * d, w.mind, w.scale, w.tile_sum);
+                X, n, d, C0 + (int64_t)(r - 1) * d, w.mind, w.scale, w.tile_sum, m, r - 1);
             KM_CUDA(cudaGetLastError());
         }
         kmpp_pick_kernel<<<1, 1024, 0, s>>>(X, n, d, C0, idx, r, seed, 0, w.mind, w.scale, w.tile_sum,

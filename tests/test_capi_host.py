@@ -190,10 +190,18 @@ def test_uniform_init_follows_reference_rule():
     np.testing.assert_array_equal(centers, np.asarray(expect[:7]).reshape(-1, 1))
 
 
-def test_minrmsd_not_available():
-    from pyemma_gb300.coordinates import cluster_kmeans
+def test_minrmsd_dimension_rule():
+    # clustering_module.cpp:13-15: the metric needs d divisible by 3
+    from pyemma_gb300.coordinates.clustering.kmeans import KmeansClustering
+    from pyemma_gb300.coordinates.clustering.regspace import RegularSpaceClustering
+    km = KmeansClustering(n_clusters=3, metric="minRMSD")
+    assert km.metric == "minRMSD"
+    with pytest.raises(ValueError):
+        km.estimate(np.zeros((10, 4), dtype=np.float32))
     with pytest.raises(NotImplementedError):
-        cluster_kmeans(None, k=3, metric="minRMSD")
+        RegularSpaceClustering(dmin=1.0, metric="minRMSD").estimate(np.zeros((10, 6), dtype=np.float32))
+    with pytest.raises(ValueError):
+        KmeansClustering(n_clusters=3, metric="manhattan")
 
 
 def test_gpu_path_fails_loudly_without_device():

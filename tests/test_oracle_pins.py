@@ -216,3 +216,88 @@ def test_count_matrix_oracle_known_answers(oracle):
     np.testing.assert_array_equal(C, [[0, 1], [1, 0]])
     C = oracle.count_matrix([np.array([0, -1, 1, 1]), np.array([2])], 1)
     np.testing.assert_array_equal(C, [[0, 0, 0], [0, 1, 0], [0, 0, 0]])
+
+
+# ---------------------------------------------------------------------------
+# minRMSD metric (clustering_module.cpp:9-36); the reference's tests are
+# test_kmeans.py:235-316 and test_assign.py:241-274
+# ---------------------------------------------------------------------------
+def _rotation(axis, theta):
+    axis = np.asarray(axis, dtype=np.float64)
+    axis = axis / np.linalg.norm(axis)
+    a = np.cos(theta / 2.0)
+    b, c, d = -axis * np.sin(theta / 2.0)
+    return np.array([[a * a + b * b - c * c - d * d, 2 * (b * c + a * d), 2 * (b * d - a * c)],
+                     [2 * (b * c - a * d), a * a + c * c - b * b - d * d, 2 * (c * d + a * b)],
+                     [2 * (b * d + a * c), 2 * (c * d - a * b), a * a + d * d - b * b - c * c]])
+
+
+def rotated_clusters(rng, n_clusters=5, n_particles=3, per_cluster=25):
+    """Clusters of one noisy structure each, every frame randomly rotated about
+    y and translated (the data of test_kmeans.py:272-299)."""
+    out = np.zeros((n_clusters * per_cluster, 3 * n_particles))
+    for i in range(n_clusters):
+        base = rng.choice(np.arange(3 * n_particles), size=3 * n_particles).astype(float)
+        pos = np.repeat(base[None], per_cluster, axis=0) + rng.normal(size=(per_cluster, 3 * n_particles), scale=.1)
+        for n, p in enumerate(pos):
+            r = _rotation([0, 1, 0], np.pi * rng.random())
+            t = rng.normal(size=3)
+            for m in range(n_particles):
+                out[per_cluster * i + n, 3 * m:3 * (m + 1)] = r @ p[3 * m:3 * (m + 1)] - t
+    return out.astype(np.float32)
+
+
+@pytest.mark.parametrize("n_atoms", [1, 2, 3, 15, 58, 100])
+def test_minrmsd_metric_matches_kabsch(oracle, n_atoms):
+    # test_kmeans.py:254-265 compares the metric with mdtraj.rmsd (absent
+    # here); the float64 Kabsch superposition is the independent check.
+    rng = np.random.default_rng(n_atoms)
+    X = rng.uniform(size=(20, 3 * n_atoms)).astype(np.float32)
+    Y = rng.uniform(size=(20, 3 * n_atoms)).astype(np.float32)
+    got = oracle.minrmsd_rows(X, Y)
+    ref = np.array([oracle.kabsch_rmsd_fp64(x, y) for x, y in zip(X, Y)])
+    np.testing.assert_allclose(got, ref, rtol=2e-5, atol=1e-6)
+
+
+def test_minrmsd_invariant_under_rigid_motion(oracle):
+    rng = np.random.default_rng(4)
+    x = rng.normal(size=(40, 3))
+    y = x + 0.3 * rng.normal(size=x.shape)
+    r = _rotation([0.3, -1.0, 0.5], 1.1)
+    y2 = y @ r.T + np.array([4.0, -2.0, 7.0])
+    a = oracle.minrmsd_rows(x.astype(np.float32).ravel(), y.astype(np.float32).ravel())[0]
+    b = oracle.minrmsd_rows(x.astype(np.float32).ravel(), y2.astype(np.float32).ravel())[0]
+    assert abs(a - b) <= 1e-5 * a
+    assert abs(a - oracle.kabsch_rmsd_fp64(x, y)) <= 1e-5 * a
+
+
+def test_minrmsd_assignment_is_argmin_of_metric(oracle):
+    # test_kmeans.py:235-252: kmeans++ (seeded) is deterministic and the
+    # assignment is the argmin of the metric to the centers.
+    rng = np.random.RandomState(123)
+    data = rng.uniform(-50, 50, size=(500, 3 * 15)).astype(np.float32)
+    C1, i1 = oracle.kmpp_minrmsd(data, 15, 32)
+    C2, i2 = oracle.kmpp_minrmsd(data, 15, 32)
+    np.testing.assert_array_equal(i1, i2)
+    labels = oracle.assign_minrmsd(data, C1)
+    manual = [int(np.argmin(oracle.minrmsd_rows(np.repeat(f[None], 15, axis=0), C1))) for f in data]
+    np.testing.assert_array_equal(labels, manual)
+
+
+def test_minrmsd_rotated_clusters_assigned(oracle):
+    # test_kmeans.py:267-316: every cluster of rotated copies gets one label.
+    rng = np.random.default_rng(7)
+    out = rotated_clusters(rng)
+    C, idx = oracle.kmpp_minrmsd(out, 5, 11)
+    labels = oracle.assign_minrmsd(out, C)
+    for i in range(5):
+        assert len(np.unique(labels[25 * i:25 * (i + 1)])) == 1
+
+
+def test_minrmsd_lloyd_inertia_decreases(oracle):
+    rng = np.random.default_rng(9)
+    out = rotated_clusters(rng, n_clusters=6, n_particles=4, per_cluster=40)
+    C0, _ = oracle.kmpp_minrmsd(out, 6, 3)
+    r = oracle.lloyd_minrmsd(out, C0, 20, 1e-9)
+    assert r["n_iter"] >= 1
+    assert np.all(np.diff(r["inertias"]) <= 1e-6 * r["inertias"][0])
