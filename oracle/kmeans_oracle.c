@@ -428,8 +428,13 @@ int kmo_regspace(const float *X, int64_t n, int32_t d, double dmin, int32_t max_
  *   pair       S[p][q] = sum_i a_i[p] b_i[q], float fused multiply-adds in atom
  *              order; then in double: C2 = -2 sum S^2, C1 = -8 det S,
  *              C0 = det K (the 4x4 key matrix, Laplace expansion on row 0);
- *              Newton on lambda^4 + C2 lambda^2 + C1 lambda + C0 from
- *              (Ga + Gb) / 2, at most 50 steps, until |step| < 1e-11 |lambda|;
+ *              Newton on P = lambda^4 + C2 lambda^2 + C1 lambda + C0 from
+ *              (Ga + Gb) / 2, at most 50 steps, until |step| < 1e-11 |lambda|,
+ *              with P and P' in double and the step P * r, r the float
+ *              reciprocal of (float)P', or P / P' when that is outside float's
+ *              range (the root is P's; the derivative only
+ *              scales the step, and a double division costs too much on the
+ *              GPU's FP64 pipe);
  *              msd = max(0, (Ga + Gb - 2 lambda) / n_atoms).
  *   assign     the lowest-index minimum of msd (NaN never wins; label 0 when
  *              no msd is a number).
@@ -505,8 +510,10 @@ double kmo_rmsd_msd(const float *a, const float *b, double ga, double gb, int32_
         const double a2 = l2 + C2;
         const double P = (a2 * l2 + C1 * lam) + C0;
         const double D = (2.0 * lam) * (l2 + a2) + C1;
-        if (D == 0.0) break;
-        const double step = P / D;
+        const float Df = (float)D;
+        if (Df == 0.0f) break;
+        /* outside float's range (coordinates of order 1e5 and more): the double quotient */
+        const double step = isinf(Df) ? P / D : P * (double)(1.0f / Df);
         const double next = lam - step;
         lam = next;
         if (fabs(step) < 1e-11 * fabs(next)) break;

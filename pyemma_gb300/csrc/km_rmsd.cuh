@@ -14,8 +14,13 @@
 //   * S[p][q] = sum_i a_i[p] b_i[q] as float fused multiply-adds in atom
 //     order;
 //   * in double, without contraction: C2 = -2 sum S^2, C1 = -8 det S,
-//     C0 = det K, Newton on the quartic from (Ga + Gb) / 2 (at most 50 steps,
-//     until |step| < 1e-11 |lambda|), msd = max(0, (Ga + Gb - 2 lambda) / n).
+//     C0 = det K, Newton on the quartic P from (Ga + Gb) / 2 (at most 50
+//     steps, until |step| < 1e-11 |lambda|), msd = max(0, (Ga + Gb -
+//     2 lambda) / n).  P and P' are evaluated in double; the step is P times
+//     the float reciprocal of (float)P' (P / P' when that is outside float's
+//     range).  The root is P's, and the derivative
+//     only scales the step: this keeps the double divisions off the FP64
+//     pipe, which runs at a small fraction of the FP32 rate here.
 #pragma once
 
 #include <cstdint>
@@ -88,8 +93,10 @@ __device__ __forceinline__ double qcp_msd(const float (&S)[9], double ga, double
         const double a2 = __dadd_rn(l2, C2);
         const double P = __dadd_rn(__dadd_rn(__dmul_rn(a2, l2), __dmul_rn(C1, lam)), C0);
         const double D = __dadd_rn(__dmul_rn(__dmul_rn(2.0, lam), __dadd_rn(l2, a2)), C1);
-        if (D == 0.0) break;
-        const double step = __ddiv_rn(P, D);
+        const float Df = __double2float_rn(D);
+        if (Df == 0.0f) break;
+        // outside float's range (coordinates of order 1e5 and more): the double quotient
+        const double step = isinf(Df) ? __ddiv_rn(P, D) : __dmul_rn(P, (double)__frcp_rn(Df));
         const double next = __dsub_rn(lam, step);
         lam = next;
         if (fabs(step) < __dmul_rn(1e-11, fabs(next))) break;
