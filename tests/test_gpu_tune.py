@@ -38,6 +38,12 @@ def test_auto_rule_small_d():
         C = X[:k].contiguous()
         _, st = L.assign(X, C, precision="auto")
         assert st["precision"] == want, (k, st)
+    # d = 8..15 picks the tensor cores once k >= 1000, the exact kernel below
     X10 = torch.from_numpy(rng.normal(size=(5000, 10)).astype(np.float32)).cuda()
     _, st = L.assign(X10, X10[:2000].contiguous(), precision="auto")
+    assert st["precision"] == "fp16"
+    _, st = L.assign(X10, X10[:500].contiguous(), precision="auto")
+    assert st["precision"] == "fp32"
+    X4 = torch.from_numpy(rng.normal(size=(5000, 4)).astype(np.float32)).cuda()
+    _, st = L.assign(X4, X4[:2000].contiguous(), precision="auto")
     assert st["precision"] == "fp32"
