@@ -634,6 +634,10 @@ int lloyd_run(const float *X_in, const HostFrames *hf, int64_t n, int32_t d, int
             KM_TRY(tc_prepare_centers(C, d, k, b, st));
             KM_CUDA(cudaMemsetAsync(b.err, 0, sizeof(uint32_t), st));
         }
+        // Each chunk's members join the update's sums as soon as the chunk
+        // is assigned, so only the division remains after the last copy.
+        prof.begin(kProfUpdate, st);
+        KM_TRY(launch_update_parts_begin(n, d, k, ws_update, st));
         for (size_t c = 0; c + 1 < sm.begin.size(); ++c) {
             const int64_t a = sm.begin[c], rows = sm.begin[c + 1] - a;
             KM_CUDA(cudaStreamWaitEvent(st, sm.ev[c + 1], 0));
@@ -648,8 +652,12 @@ int lloyd_run(const float *X_in, const HostFrames *hf, int64_t n, int32_t d, int
                                           st));
                 prof.end(kProfFp32, st);
             }
+            KM_TRY(launch_update_part(X + a * d, n, d, labels + a, rows, k, C, err, ws_update, st));
         }
-        return enqueue_update(st);
+        KM_TRY(launch_update_parts_finish(n, d, k, C, C_new, cost, ws_update, st));
+        prof.end(kProfUpdate, st);
+        KM_CUDA(cudaMemcpyAsync(C, C_new, sizeof(float) * k * d, cudaMemcpyDeviceToDevice, st));
+        return KM_OK;
     };
 
     cudaGraphExec_t exec = nullptr;

@@ -80,6 +80,16 @@ int launch_update_accumulate(const float *X, int64_t n, int d, const int32_t *la
                              uint32_t *err, void *ws, cudaStream_t s, int seg_per_sm = 0);
 int launch_update_finish(int64_t n, int d, int k, const float *C_old, float *C_new, int64_t *counts_out,
                          double *cost, void *ws, cudaStream_t s);
+// The update of frames that arrive in parts: begin clears the totals, each
+// part adds its rows (X, labels already offset to the part; n is the full
+// count the workspace was sized for), finish forms the new centers and the
+// inertia.  The result equals launch_update over all rows up to the order
+// of the float64 sums.
+int launch_update_parts_begin(int64_t n, int d, int k, void *ws, cudaStream_t s);
+int launch_update_part(const float *X, int64_t n, int d, const int32_t *labels, int64_t rows, int k,
+                       const float *C_old, uint32_t *err, void *ws, cudaStream_t s);
+int launch_update_parts_finish(int64_t n, int d, int k, const float *C_old, float *C_new, double *cost, void *ws,
+                               cudaStream_t s);
 // Between the halves: moves the frames of a flip list from the cluster of
 // their first label to that of their exact label (sums, squared sums, counts,
 // with the accumulation's float32 deviations) and writes the exact labels.

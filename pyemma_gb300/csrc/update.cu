@@ -33,6 +33,7 @@ constexpr int kGroups = kPiece / 32;
 
 struct UpdateWs {
     int32_t *counts;
+    int32_t *total;  // members over several parts (launch_update_part)
     int32_t *offsets;
     int32_t *cursor;
     int32_t *perm;
@@ -46,6 +47,7 @@ UpdateWs carve(void *ws, int64_t n, int d, int k, size_t *bytes) {
     Carver c(ws);
     UpdateWs u;
     u.counts = c.take<int32_t>(k);
+    u.total = c.take<int32_t>(k);
     u.offsets = c.take<int32_t>((size_t)k + 1);
     u.cursor = c.take<int32_t>(k);
     u.perm = c.take<int32_t>(n > 0 ? n : 1);
@@ -495,6 +497,10 @@ __global__ void apply_flips_kernel(const float *__restrict__ X, int d, const flo
     }
 }
 
+__global__ void add_counts_kernel(const int32_t *__restrict__ counts, int k, int32_t *__restrict__ total) {
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < k; j += gridDim.x * blockDim.x) total[j] += counts[j];
+}
+
 // Single CTA, fixed summation tree: the same inputs give the same cost.
 __global__ void __launch_bounds__(1024) reduce_cost_kernel(const double *__restrict__ ccost, int k,
                                                             double *__restrict__ cost) {
@@ -680,6 +686,45 @@ int launch_update(const float *X, int64_t n, int d, const int32_t *labels, int k
                   uint32_t *err, void *ws, cudaStream_t s) {
     KM_TRY(launch_update_accumulate(X, n, d, labels, k, C_old, err, ws, s));
     return launch_update_finish(n, d, k, C_old, C_new, counts_out, cost, ws, s);
+}
+
+int launch_update_parts_begin(int64_t n, int d, int k, void *ws, cudaStream_t s) {
+    UpdateWs u = carve(ws, n, d, k, nullptr);
+    KM_CUDA(cudaMemsetAsync(u.total, 0, sizeof(int32_t) * k, s));
+    KM_CUDA(cudaMemsetAsync(u.S, 0, sizeof(double) * (size_t)k * d, s));
+    KM_CUDA(cudaMemsetAsync(u.Q, 0, sizeof(double) * k, s));
+    return KM_OK;
+}
+
+int launch_update_part(const float *X, int64_t n, int d, const int32_t *labels, int64_t rows, int k,
+                       const float *C_old, uint32_t *err, void *ws, cudaStream_t s) {
+    if (rows == 0) return KM_OK;
+    UpdateWs u = carve(ws, n, d, k, nullptr);
+    // The counting sort and the segment sums of these rows, into the totals;
+    // launch_update_accumulate without its clearing of the sums.
+    KM_CUDA(cudaMemsetAsync(u.counts, 0, sizeof(int32_t) * k, s));
+    count_labels_kernel<<<grid_for(rows, 256, 8), 256, 0, s>>>(labels, rows, k, u.counts, err);
+    KM_CUDA(cudaGetLastError());
+    scan_counts_kernel<<<1, 1024, 0, s>>>(u.counts, k, u.offsets, u.cursor);
+    KM_CUDA(cudaGetLastError());
+    scatter_kernel<<<grid_for(rows, 256, 8), 256, 0, s>>>(labels, rows, k, u.cursor, u.perm, u.slab);
+    KM_CUDA(cudaGetLastError());
+    if (bulk_ok(X, d)) {
+        KM_TRY(launch_segments_bulk(X, rows, d, u, k, C_old, err, s, 0));
+    } else {
+        const int64_t npieces = (rows + kPiece - 1) / kPiece;
+        KM_TRY(launch_segments(X, rows, d, u, k, C_old, grid_for(npieces * 32, 256, 8), s));
+    }
+    add_counts_kernel<<<(unsigned)((k + 255) / 256), 256, 0, s>>>(u.counts, k, u.total);
+    KM_CUDA(cudaGetLastError());
+    return KM_OK;
+}
+
+int launch_update_parts_finish(int64_t n, int d, int k, const float *C_old, float *C_new, double *cost, void *ws,
+                               cudaStream_t s) {
+    UpdateWs u = carve(ws, n, d, k, nullptr);
+    KM_CUDA(cudaMemcpyAsync(u.counts, u.total, sizeof(int32_t) * k, cudaMemcpyDeviceToDevice, s));
+    return launch_update_finish(n, d, k, C_old, C_new, nullptr, cost, ws, s);
 }
 
 }  // namespace km
