@@ -429,7 +429,10 @@ int kmo_regspace(const float *X, int64_t n, int32_t d, double dmin, int32_t max_
  *              order; then in double: C2 = -2 sum S^2, C1 = -8 det S,
  *              C0 = det K (the 4x4 key matrix, Laplace expansion on row 0);
  *              Newton on P = lambda^4 + C2 lambda^2 + C1 lambda + C0 from
- *              (Ga + Gb) / 2, at most 50 steps, until |step| < 1e-11 |lambda|,
+ *              the smaller of two upper bounds of the largest root,
+ *              (Ga + Gb) / 2 and sqrt(3) ||S||_F = sqrt(-1.5 C2) (a float
+ *              root inflated by 1e-6), at most 50 steps, until
+ *              |step| < 1e-11 |lambda|,
  *              with P and P' in double and the step P * r, r the float
  *              reciprocal of (float)P', or P / P' when that is outside float's
  *              range (the root is P's; the derivative only
@@ -505,6 +508,8 @@ double kmo_rmsd_msd(const float *a, const float *b, double ga, double gb, int32_
     const double m3 = det3(K[1][0], K[1][1], K[1][2], K[2][0], K[2][1], K[2][2], K[3][0], K[3][1], K[3][2]);
     const double C0 = K[0][0] * m0 - K[0][1] * m1 + K[0][2] * m2 - K[0][3] * m3;
     double lam = 0.5 * (ga + gb);
+    const double ub = (double)sqrtf((float)(-1.5 * C2)) * (1.0 + 1e-6);
+    if (ub < lam) lam = ub;
     for (int it = 0; it < 50; ++it) {
         const double l2 = lam * lam;
         const double a2 = l2 + C2;

@@ -14,8 +14,11 @@
 //   * S[p][q] = sum_i a_i[p] b_i[q] as float fused multiply-adds in atom
 //     order;
 //   * in double, without contraction: C2 = -2 sum S^2, C1 = -8 det S,
-//     C0 = det K, Newton on the quartic P from (Ga + Gb) / 2 (at most 50
-//     steps, until |step| < 1e-11 |lambda|), msd = max(0, (Ga + Gb -
+//     C0 = det K, Newton on the quartic P from the smaller of two upper
+//     bounds of its largest root, (Ga + Gb) / 2 and sqrt(3) ||S||_F =
+//     sqrt(-1.5 C2) (float root, inflated by 1e-6; the largest eigenvalue of
+//     the key matrix is at most the sum of the singular values of S), at most
+//     50 steps until |step| < 1e-11 |lambda|, msd = max(0, (Ga + Gb -
 //     2 lambda) / n).  P and P' are evaluated in double; the step is P times
 //     the float reciprocal of (float)P' (P / P' when that is outside float's
 //     range).  The root is P's, and the derivative
@@ -88,6 +91,8 @@ __device__ __forceinline__ double qcp_msd(const float (&S)[9], double ga, double
     const double C0 = __dsub_rn(__dadd_rn(__dsub_rn(__dmul_rn(k00, m0), __dmul_rn(k01, m1)), __dmul_rn(k02, m2)),
                                 __dmul_rn(k03, m3));
     double lam = __dmul_rn(0.5, __dadd_rn(ga, gb));
+    const double ub = __dmul_rn((double)__fsqrt_rn(__double2float_rn(__dmul_rn(-1.5, C2))), 1.0 + 1e-6);
+    if (ub < lam) lam = ub;
     for (int it = 0; it < 50; ++it) {
         const double l2 = __dmul_rn(lam, lam);
         const double a2 = __dadd_rn(l2, C2);
