@@ -234,8 +234,42 @@ size_t resident_ws_bytes(int64_t n, int d, int k, int prec) {
     return tc_frames_ws_size(n, d) + tc_assign_ws_size(n, d, k) + 2 * 256;
 }
 
+// Iterations after the first one can run as a CUDA graph WHILE loop: its
+// body is one iteration plus lloyd_loop_step_kernel, which records the
+// inertia, applies the stopping rule on the device and sets the loop's
+// condition, so a run of iterations costs one launch and one read-back.
+// A launch runs at most kLoopBatch iterations (the size of the inertia
+// buffer in the workspace).
+struct LoopState {
+    double prev;
+    double tol;
+    int32_t it;      // iterations run by this launch
+    int32_t max_it;  // bound for this launch
+    int32_t converged;
+    uint32_t err;
+};
+constexpr int kLoopBatch = 64;
+
+__global__ void lloyd_loop_step_kernel(LoopState *st, const double *cost, const uint32_t *err_update,
+                                       const uint32_t *err_tc, double *inertias, cudaGraphConditionalHandle h) {
+    const double c = *cost;
+    const uint32_t e = *err_update | (err_tc ? *err_tc : 0u);
+    const int it = st->it;
+    inertias[it] = c;
+    // the host loop's rule: rel = |cost - prev| / cost (0 when cost is 0)
+    const double rel = c != 0.0 ? fabs(c - st->prev) / c : 0.0;
+    st->prev = c;
+    st->it = it + 1;
+    st->err |= e;
+    const int conv = rel <= st->tol ? 1 : 0;
+    st->converged = conv;
+    cudaGraphSetConditional(h, (conv || e != 0u || it + 1 >= st->max_it) ? 0u : 1u);
+}
+
 size_t lloyd_ws_bytes(int64_t n, int d, int k, int prec) {
     Carver c(nullptr);
+    c.take<LoopState>(1);
+    c.take<double>(kLoopBatch);
     c.take<char>(update_ws_size(n, d, k));
     c.take<float>((size_t)k * d);  // C_new
     c.take<double>(1);             // cost
@@ -549,6 +583,8 @@ int lloyd_run(const float *X_in, const HostFrames *hf, int64_t n, int32_t d, int
     }
 
     Carver cv(workspace);
+    LoopState *loop_st = cv.take<LoopState>(1);
+    double *loop_inertias = cv.take<double>(kLoopBatch);
     void *ws_update = cv.take<char>(update_ws_size(n, d, k));
     float *C_new = cv.take<float>((size_t)k * d);
     double *cost = cv.take<double>(1);
@@ -660,10 +696,91 @@ int lloyd_run(const float *X_in, const HostFrames *hf, int64_t n, int32_t d, int
         return KM_OK;
     };
 
+    // The iterations it0, it0+1, ... as device-side WHILE loops.  handled = 0
+    // when the graph could not be built (then the host loop runs them).
+    auto device_loop = [&](int32_t it0, double prev0, int &handled) -> int {
+        handled = 0;
+        cudaStream_t cs = nullptr;
+        cudaGraph_t g = nullptr;
+        cudaGraphExec_t gx = nullptr;
+        auto cleanup = [&]() {
+            if (gx) cudaGraphExecDestroy(gx);
+            if (g) cudaGraphDestroy(g);
+            if (cs) cudaStreamDestroy(cs);
+        };
+        bool ok = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) == cudaSuccess;
+        if (ok) ok = cudaGraphCreate(&g, 0) == cudaSuccess;
+        cudaGraphConditionalHandle h = 0;
+        if (ok) ok = cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault) == cudaSuccess;
+        cudaGraphNodeParams np = {};
+        np.type = cudaGraphNodeTypeConditional;
+        np.conditional.handle = h;
+        np.conditional.type = cudaGraphCondTypeWhile;
+        np.conditional.size = 1;
+        cudaGraphNode_t node;
+        if (ok) ok = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &np) == cudaSuccess;
+        if (ok) {
+            cudaGraph_t body = np.conditional.phGraph_out[0];
+            ok = cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) ==
+                 cudaSuccess;
+            if (ok) {
+                const int st = enqueue(cs);
+                lloyd_loop_step_kernel<<<1, 1, 0, cs>>>(loop_st, cost, err, is_tc(prec) ? b.err : nullptr,
+                                                        loop_inertias, h);
+                cudaGraph_t out = nullptr;
+                const cudaError_t e2 = cudaStreamEndCapture(cs, &out);
+                ok = st == KM_OK && e2 == cudaSuccess;
+            }
+        }
+        if (ok) ok = cudaGraphInstantiate(&gx, g, 0) == cudaSuccess;
+        if (!ok) {
+            cudaGetLastError();  // not fatal: the host loop takes over
+            cleanup();
+            return KM_OK;
+        }
+        handled = 1;
+        int status = KM_OK;
+        int32_t it = it0;
+        double prev = prev0;
+        while (it < max_iter) {
+            LoopState hs{prev, tolerance, 0, std::min(kLoopBatch, max_iter - it), 0, 0u};
+            double hin[kLoopBatch];
+            cudaError_t e = cudaMemcpyAsync(loop_st, &hs, sizeof(hs), cudaMemcpyHostToDevice, s);
+            if (e == cudaSuccess) e = cudaGraphLaunch(gx, s);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(&hs, loop_st, sizeof(hs), cudaMemcpyDeviceToHost, s);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(hin, loop_inertias, sizeof(double) * kLoopBatch, cudaMemcpyDeviceToHost, s);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+            if (e != cudaSuccess) {
+                status = cuda_fail(e, "Lloyd iterations");
+                break;
+            }
+            for (int32_t j = 0; j < hs.it; ++j)
+                if (inertias) inertias[it + j] = hin[j];
+            it += hs.it;
+            *n_iter = it;
+            if (hs.it > 0) prev = hin[hs.it - 1];
+            status = check_device_errors(hs.err);
+            if (status != KM_OK) break;
+            if (hs.converged) {
+                *converged = 1;
+                break;
+            }
+            if (hs.it == 0) break;
+        }
+        cleanup();
+        return status;
+    };
+
     cudaGraphExec_t exec = nullptr;
     int status = KM_OK;
     double prev = 0.0;
     for (int32_t it = 0; it < max_iter; ++it) {
+        if (it == 1 && !cb && !prof.active) {
+            int handled = 0;
+            status = device_loop(it, prev, handled);
+            if (handled || status != KM_OK) break;
+        }
         if (it == 0) {
             status = hf ? enqueue_streamed(s) : enqueue(s);
         } else {

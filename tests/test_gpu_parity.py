@@ -296,3 +296,25 @@ def test_profile_counts_graph_replays(torch, L):
     assert prof["update"][1] == 10
     lab, _ = L.assign(X, C0, precision="fp16")  # no error left behind by the timing
     assert lab.shape[0] == 20000
+
+
+@pytest.mark.parametrize("prec", ["fp32", "fp16"])
+def test_lloyd_device_loop_equals_host_loop(torch, L, prec):
+    # Without a callback (and without profiling) the iterations after the first
+    # run as a device-side CUDA graph WHILE loop; with a callback the host loop
+    # runs them.  Both apply the same stopping rule.
+    rng = np.random.default_rng(77)
+    X = dev(torch, rng.normal(size=(30000, 64)))
+    C0 = X[:40].clone()
+    calls = []
+    for max_iter, tol in ((100, 1e-5), (150, -1.0)):
+        Ca, Cb = C0.clone(), C0.clone()
+        ra = L.lloyd(X, Ca, max_iter, tol, precision=prec)
+        rb = L.lloyd(X, Cb, max_iter, tol, precision=prec, callback=lambda: calls.append(1))
+        assert ra["n_iter"] == rb["n_iter"] and ra["converged"] == rb["converged"]
+        assert len(calls) == rb["n_iter"]
+        calls.clear()
+        if tol < 0:
+            assert ra["n_iter"] == max_iter  # crosses the 64-iteration launches
+        np.testing.assert_allclose(ra["inertias"], rb["inertias"], rtol=1e-6)
+        torch.testing.assert_close(Ca, Cb, rtol=1e-5, atol=1e-5)
