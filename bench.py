@@ -404,15 +404,17 @@ def run_ours(args):
         dist.destroy_process_group()
     if rank != 0:
         return
-    # prep_centers, tc_assign, 3 candidate re-check kernels, 2 full re-check
-    # kernels, 6 centroid-update kernels
-    launches_per_step = 13
+    # Per iteration: prep_centers, tc_assign, 3 candidate re-check kernels,
+    # 3 full re-check kernels (short list, tiled, finalize), 7 centroid-update
+    # kernels (count, scan, scatter, segment sums, flips, finalize, cost).
+    # Once per km_lloyd call: shift, center norms, scale, FP16 frame copy.
+    launches_per_step = 15
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "fp16 distances (fp32 accumulate), fp32 recheck, f64 sums",
             "data": "synthetic (seeded C-alpha distances, generated on device)",
             "config": config(args), "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
-            "gpu_launches": launches_per_step * args.steps + 2}
+            "gpu_launches": launches_per_step * args.steps + 4}
     line.update(extra)
     print(json.dumps(line), flush=True)
 
