@@ -298,14 +298,15 @@ def test_profile_counts_graph_replays(torch, L):
     assert lab.shape[0] == 20000
 
 
-@pytest.mark.parametrize("prec", ["fp32", "fp16"])
-def test_lloyd_device_loop_equals_host_loop(torch, L, prec):
+@pytest.mark.parametrize("prec,k", [("fp32", 40), ("fp16", 40), ("fp16", 300)])
+def test_lloyd_device_loop_equals_host_loop(torch, L, prec, k):
     # Without a callback (and without profiling) the iterations after the first
     # run as a device-side CUDA graph WHILE loop; with a callback the host loop
-    # runs them.  Both apply the same stopping rule.
+    # runs them.  Both apply the same stopping rule.  k = 300 runs the CTA-pair
+    # (cluster) launch inside the loop's body.
     rng = np.random.default_rng(77)
     X = dev(torch, rng.normal(size=(30000, 64)))
-    C0 = X[:40].clone()
+    C0 = X[:k].clone()
     calls = []
     for max_iter, tol in ((100, 1e-5), (150, -1.0)):
         Ca, Cb = C0.clone(), C0.clone()
