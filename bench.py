@@ -286,6 +286,11 @@ def run_ours(args):
     value = world * n * args.steps / (ms_max / 1e3)
 
     clocks = sampler.summary(t_wall0, t_wall1) if sampler else None
+    if sampler:
+        # nvidia-smi's queries take driver locks: keep them out of the
+        # end-to-end copies measured below
+        sampler.stop()
+        sampler = None
 
     # ---- roofline of the tensor-core distance kernel ----
     peaks, peak_kind = measured_peaks()
