@@ -338,7 +338,7 @@ def run_ours(args):
         Xh.copy_(X)
         Xh_np = Xh.numpy()
         C0h = C0.cpu().numpy()
-        # the bare pinned host-to-device rate of this box, for reading e2e
+        # the bare pinned host-to-device rate of this machine, for reading e2e
         ec0, ec1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         X.copy_(Xh, non_blocking=True)
         ec0.record()

@@ -3,7 +3,7 @@
 The oracle restates PyEMMA's k-means discretization path on the CPU
 (``oracle/kmeans_oracle.c``; semantics and reference citations are in that
 file's header).  Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU legs
-of ``bench.py`` import this module: it is the checker, never the product.
+of ``bench.py`` import this module: it checks the product and is never part of it.
 
 Besides the ctypes bindings this module holds a float64 NumPy reference for
 centers and inertia, which is independent of the C code.

@@ -91,7 +91,7 @@ class RegularSpaceClustering(AbstractClustering):
 
     def _estimate(self, source):
         if self.metric == "minRMSD":
-            raise NotImplementedError("regular space clustering has no minRMSD center search in this build; "
+            raise NotImplementedError("regular space clustering has no minRMSD center search; "
                                       "the minRMSD metric is available for k-means and assignment")
         stride = self.stride if self.stride else 1
         trajs = source.frames(stride=stride, skip=self.skip)
