@@ -185,6 +185,27 @@ def cpu_lloyd_rate(X, C, target_s, threads):
     return S / dt, S, dt
 
 
+def max_over_ranks(ms, dist, device):
+    """The slowest rank's time (every rank gets it); ms itself on one rank."""
+    if dist is None:
+        return float(ms)
+    import torch
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(world, frames_per_rank, steps, ms_max):
+    """Frames of all ranks per second over the slowest rank's time.  Every
+    rank owns its own frames (weak scaling; no data-path collective)."""
+    return world * frames_per_rank * steps / (ms_max / 1e3)
+
+
+def rank_seed(rank):
+    """Each rank's frames are drawn from their own seed."""
+    return SEED + rank
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -248,8 +269,8 @@ def run_ours(args):
 
     _lib.load()
     n = args.frames
-    X = datasets.calpha_distances(n_frames=n, seed=SEED + rank, device="cuda")
-    rng = np.random.default_rng(SEED + rank)
+    X = datasets.calpha_distances(n_frames=n, seed=rank_seed(rank), device="cuda")
+    rng = np.random.default_rng(rank_seed(rank))
     C0 = X[torch.from_numpy(rng.choice(n, K, replace=False)).cuda()].contiguous()
     torch.cuda.synchronize()
 
@@ -277,13 +298,9 @@ def run_ours(args):
     prof = _lib.profile_read()
     _lib.profile_enable(False)
     assert res["n_iter"] == args.steps
-    ms_max = ms
-    if dist is not None:
-        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_max = float(t.item())
+    ms_max = max_over_ranks(ms, dist, "cuda")
     ms_per_step = ms_max / args.steps
-    value = world * n * args.steps / (ms_max / 1e3)
+    value = whole_job_rate(world, n, args.steps, ms_max)
 
     clocks = sampler.summary(t_wall0, t_wall1) if sampler else None
     if sampler:
