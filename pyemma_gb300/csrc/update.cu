@@ -497,6 +497,57 @@ __global__ void apply_flips_kernel(const float *__restrict__ X, int d, const flo
     }
 }
 
+// Few centers and features (the sums of every center fit in shared memory,
+// d <= 32): each CTA sums its frames in shared memory with float64 atomics and
+// adds its partial sums to the totals once, instead of the counting sort and
+// segment pass.  The deviations x - c_old are rounded to float32 once, as in
+// the segment kernels; only the order of the float64 additions differs.
+constexpr size_t kSmallSumsBytes = 48 * 1024;
+
+bool small_ok(int d, int k) {
+    return d <= 32 && ((size_t)k * d + k) * sizeof(double) + (size_t)k * sizeof(int32_t) <= kSmallSumsBytes;
+}
+
+__global__ void __launch_bounds__(256) small_accumulate_kernel(const float *__restrict__ X, int64_t n, int d,
+                                                               const int32_t *__restrict__ labels, int k,
+                                                               const float *__restrict__ C_old,
+                                                               int32_t *__restrict__ counts, double *__restrict__ S,
+                                                               double *__restrict__ Q, uint32_t *err) {
+    extern __shared__ double small_sums[];
+    double *S_s = small_sums;
+    double *Q_s = S_s + (size_t)k * d;
+    int32_t *c_s = reinterpret_cast<int32_t *>(Q_s + k);
+    for (int e = threadIdx.x; e < k * d + k; e += blockDim.x) small_sums[e] = 0.0;
+    for (int e = threadIdx.x; e < k; e += blockDim.x) c_s[e] = 0;
+    __syncthreads();
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int j = labels[i];
+        if (j < 0 || j >= k) {
+            atomicOr(err, (uint32_t)kDevBadLabel);
+            continue;
+        }
+        const float *x = X + i * d;
+        const float *c = C_old + (int64_t)j * d;
+        double q = 0.0;
+        for (int f = 0; f < d; ++f) {
+            const float t = __fsub_rn(x[f], c[f]);
+            atomicAdd(&S_s[j * d + f], (double)t);
+            q += (double)t * (double)t;
+        }
+        atomicAdd(&Q_s[j], q);
+        atomicAdd(&c_s[j], 1);
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < k * d; e += blockDim.x)
+        if (S_s[e] != 0.0) atomicAdd(&S[e], S_s[e]);
+    for (int e = threadIdx.x; e < k; e += blockDim.x) {
+        if (c_s[e]) {
+            atomicAdd(&Q[e], Q_s[e]);
+            atomicAdd(&counts[e], c_s[e]);
+        }
+    }
+}
+
 __global__ void add_counts_kernel(const int32_t *__restrict__ counts, int k, int32_t *__restrict__ total) {
     for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < k; j += gridDim.x * blockDim.x) total[j] += counts[j];
 }
@@ -640,6 +691,13 @@ int launch_update_accumulate(const float *X, int64_t n, int d, const int32_t *la
     KM_CUDA(cudaMemsetAsync(u.counts, 0, sizeof(int32_t) * k, s));
     KM_CUDA(cudaMemsetAsync(u.S, 0, sizeof(double) * (size_t)k * d, s));
     KM_CUDA(cudaMemsetAsync(u.Q, 0, sizeof(double) * k, s));
+    if (n > 0 && small_ok(d, k)) {
+        const size_t smem = ((size_t)k * d + k) * sizeof(double) + (size_t)k * sizeof(int32_t);
+        small_accumulate_kernel<<<grid_for(n, 256, 2), 256, smem, s>>>(X, n, d, labels, k, C_old, u.counts, u.S, u.Q,
+                                                                        err);
+        KM_CUDA(cudaGetLastError());
+        return KM_OK;
+    }
     if (n > 0) {
         count_labels_kernel<<<grid_for(n, 256, 8), 256, 0, s>>>(labels, n, k, u.counts, err);
         KM_CUDA(cudaGetLastError());
