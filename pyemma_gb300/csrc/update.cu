@@ -19,6 +19,7 @@
 //   mu_j = float(c_j + S_j / n_j),  delta_j = mu_j - c_j,
 //   inertia_j = Q_j - 2 delta_j . S_j + n_j ||delta_j||^2
 // which is sum_i ||x_i - mu_j||^2 without the cancellation of raw moments.
+#include <algorithm>
 #include <mutex>
 
 #include "km_common.cuh"
@@ -497,22 +498,29 @@ __global__ void apply_flips_kernel(const float *__restrict__ X, int d, const flo
     }
 }
 
-// Few centers and features (the sums of every center fit in shared memory,
-// d <= 32): each CTA sums its frames in shared memory with float64 atomics and
-// adds its partial sums to the totals once, instead of the counting sort and
-// segment pass.  The deviations x - c_old are rounded to float32 once, as in
-// the segment kernels; only the order of the float64 additions differs.
+// Few centers and features (d <= 16 and every center's sums fit in 48 KB of
+// shared memory): one pass instead of the counting sort and segment pass.
+// Each thread walks a run of consecutive frames (time-ordered frames often
+// share a label), sums the deviations x - c_old of each feature with a
+// compensated float sum and the frame's squared deviations (one fused
+// multiply-add chain) into a compensated total, as the segment kernels do,
+// and adds the run's partial sums to the CTA's float64 sums in shared memory
+// whenever the label changes.  The CTA adds each of its totals to global
+// memory once.  Only the order of the float64 additions differs from the
+// segment path.
 constexpr size_t kSmallSumsBytes = 48 * 1024;
+constexpr int kSmallThreads = 256;
+constexpr int kSmallMaxRun = 16;
 
-bool small_ok(int d, int k) {
-    return d <= 32 && ((size_t)k * d + k) * sizeof(double) + (size_t)k * sizeof(int32_t) <= kSmallSumsBytes;
-}
+size_t small_sums_bytes(int d, int k) { return ((size_t)k * d + k) * sizeof(double) + (size_t)k * sizeof(int32_t); }
 
-__global__ void __launch_bounds__(256) small_accumulate_kernel(const float *__restrict__ X, int64_t n, int d,
-                                                               const int32_t *__restrict__ labels, int k,
-                                                               const float *__restrict__ C_old,
-                                                               int32_t *__restrict__ counts, double *__restrict__ S,
-                                                               double *__restrict__ Q, uint32_t *err) {
+bool small_ok(int d, int k) { return d <= 16 && small_sums_bytes(d, k) <= kSmallSumsBytes; }
+
+template <int DP>
+__global__ void __launch_bounds__(kSmallThreads) small_accumulate_kernel(
+    const float *__restrict__ X, int64_t n, int d, const int32_t *__restrict__ labels, int k,
+    const float *__restrict__ C_old, int run, int32_t *__restrict__ counts, double *__restrict__ S,
+    double *__restrict__ Q, uint32_t *err) {
     extern __shared__ double small_sums[];
     double *S_s = small_sums;
     double *Q_s = S_s + (size_t)k * d;
@@ -520,22 +528,50 @@ __global__ void __launch_bounds__(256) small_accumulate_kernel(const float *__re
     for (int e = threadIdx.x; e < k * d + k; e += blockDim.x) small_sums[e] = 0.0;
     for (int e = threadIdx.x; e < k; e += blockDim.x) c_s[e] = 0;
     __syncthreads();
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const int j = labels[i];
-        if (j < 0 || j >= k) {
-            atomicOr(err, (uint32_t)kDevBadLabel);
-            continue;
+    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t nt = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t r0 = tid * run; r0 < n; r0 += nt * run) {
+        const int64_t r1 = min(r0 + (int64_t)run, n);
+        CSum acc[DP], qacc;
+        float cold[DP];
+        int cur = -1, cnt = 0;
+        auto flush = [&]() {
+#pragma unroll
+            for (int f = 0; f < DP; ++f)
+                if (f < d) atomicAdd(&S_s[cur * d + f], acc[f].value());
+            atomicAdd(&Q_s[cur], qacc.value());
+            atomicAdd(&c_s[cur], cnt);
+        };
+        for (int64_t i = r0; i < r1; ++i) {
+            const int j = labels[i];
+            if (j < 0 || j >= k) {
+                atomicOr(err, (uint32_t)kDevBadLabel);
+                continue;
+            }
+            if (j != cur) {
+                if (cur >= 0) flush();
+                cur = j;
+                cnt = 0;
+                qacc.reset();
+#pragma unroll
+                for (int f = 0; f < DP; ++f) {
+                    acc[f].reset();
+                    cold[f] = f < d ? __ldg(C_old + (int64_t)j * d + f) : 0.0f;
+                }
+            }
+            float q = 0.0f;
+#pragma unroll
+            for (int f = 0; f < DP; ++f) {
+                if (f < d) {
+                    const float t = __fsub_rn(__ldg(X + i * d + f), cold[f]);
+                    acc[f].add(t);
+                    q = __fmaf_rn(t, t, q);
+                }
+            }
+            qacc.add(q);
+            ++cnt;
         }
-        const float *x = X + i * d;
-        const float *c = C_old + (int64_t)j * d;
-        double q = 0.0;
-        for (int f = 0; f < d; ++f) {
-            const float t = __fsub_rn(x[f], c[f]);
-            atomicAdd(&S_s[j * d + f], (double)t);
-            q += (double)t * (double)t;
-        }
-        atomicAdd(&Q_s[j], q);
-        atomicAdd(&c_s[j], 1);
+        if (cur >= 0) flush();
     }
     __syncthreads();
     for (int e = threadIdx.x; e < k * d; e += blockDim.x)
@@ -692,9 +728,22 @@ int launch_update_accumulate(const float *X, int64_t n, int d, const int32_t *la
     KM_CUDA(cudaMemsetAsync(u.S, 0, sizeof(double) * (size_t)k * d, s));
     KM_CUDA(cudaMemsetAsync(u.Q, 0, sizeof(double) * k, s));
     if (n > 0 && small_ok(d, k)) {
-        const size_t smem = ((size_t)k * d + k) * sizeof(double) + (size_t)k * sizeof(int32_t);
-        small_accumulate_kernel<<<grid_for(n, 256, 2), 256, smem, s>>>(X, n, d, labels, k, C_old, u.counts, u.S, u.Q,
-                                                                        err);
+        const int dp = d <= 1 ? 1 : d <= 2 ? 2 : d <= 4 ? 4 : d <= 8 ? 8 : 16;
+        // one frame per thread while the frames fill 8 CTAs of every SM, runs
+        // of up to kSmallMaxRun frames beyond that
+        const int64_t slots = (int64_t)num_sms() * 8 * kSmallThreads;
+        const int run = (int)std::min<int64_t>(kSmallMaxRun, std::max<int64_t>(1, (n + slots - 1) / slots));
+        const unsigned g = grid_for((n + run - 1) / run, kSmallThreads, 8);
+        const size_t smem = small_sums_bytes(d, k);
+        switch (dp) {
+#define KM_SMALL(DP)                                                                                          \
+    case DP:                                                                                                  \
+        small_accumulate_kernel<DP><<<g, kSmallThreads, smem, s>>>(X, n, d, labels, k, C_old, run, u.counts, \
+                                                                   u.S, u.Q, err);                           \
+        break;
+            KM_SMALL(1) KM_SMALL(2) KM_SMALL(4) KM_SMALL(8) KM_SMALL(16)
+#undef KM_SMALL
+        }
         KM_CUDA(cudaGetLastError());
         return KM_OK;
     }

@@ -175,6 +175,34 @@ def test_update_shapes(torch, L, oracle, d):
     assert abs(cost - cost_ref) <= RTOL_COST_STEP * cost_ref
 
 
+@pytest.mark.parametrize("d", [1, 2, 3, 4, 5, 8, 9, 16, 17])
+@pytest.mark.parametrize("k_kind", ["one", "max"])
+@pytest.mark.parametrize("n", [30011, 1000003])
+def test_update_one_pass_shapes(torch, L, oracle, d, k_kind, n):
+    # d <= 16 and few centers take the one-pass shared-memory sums: "max" is
+    # the largest k whose sums (k x (d + 1) doubles and k counts) fit in
+    # 48 KB, "one" puts every frame in one cluster; the larger n gives each
+    # thread a run of several frames.  d = 17 is the segment path.
+    k = 1 if k_kind == "one" else 49152 // (8 * (d + 1) + 4)
+    if n > 100000 and d not in (2, 16):
+        pytest.skip("runs of frames: two widths suffice")
+    rng = np.random.default_rng(300 + d)
+    X = (3.0 + rng.normal(size=(n, d))).astype(np.float32)
+    C = (3.0 + rng.normal(size=(k, d))).astype(np.float32)
+    lab = rng.integers(0, k, size=n).astype(np.int32)
+    if n > 100000:
+        lab[: n // 2] = np.repeat(lab[: n // 2: 7], 7)[: n // 2]  # runs of equal labels
+    if k > 2:
+        lab[lab == 1] = 0  # an empty cluster keeps its center
+    Cn_ref, cnt_ref, cost_ref, _ = oracle.update(X, lab, C)
+    Cn, counts, cost = L.update(dev(torch, X), torch.from_numpy(lab).cuda(), dev(torch, C))
+    np.testing.assert_allclose(Cn.cpu().numpy(), Cn_ref, rtol=RTOL_CENTER_STEP, atol=0)
+    np.testing.assert_array_equal(counts.cpu().numpy(), cnt_ref)
+    if k > 2:
+        np.testing.assert_array_equal(Cn.cpu().numpy()[1], C[1])
+    assert abs(cost - cost_ref) <= RTOL_COST_STEP * cost_ref
+
+
 def test_update_sorted_labels_long_runs(torch, L, oracle):
     # Long runs of equal labels (time-correlated trajectories) stress the run flushes.
     rng = np.random.default_rng(77)
