@@ -15,8 +15,10 @@
 // t = floor(u * W / 2^64) for the weight total W and picks the first frame
 // whose inclusive prefix weight exceeds t.
 //
-// Per round: one pass over X (distance to the newest center, running minimum,
-// per-tile weight sums; HBM-bound) and one single-CTA pick kernel.
+// Per round one launch: a pass over X (distance to the newest center,
+// running minimum, per-tile weight sums; HBM-bound), after which the CTA that
+// finishes last (a fenced atomic count, no waiting) draws the round's frame
+// and copies it into the centers.
 #include "km_common.cuh"
 #include "km_internal.h"
 #include "km_rmsd.cuh"
@@ -33,6 +35,7 @@ struct KmppWs {
     unsigned long long *tile_sum;
     uint32_t *maxbits;
     double *scale;
+    unsigned int *done;  // CTAs of the current round that have finished
 };
 
 KmppWs carve(void *ws, int64_t n, size_t *bytes) {
@@ -43,6 +46,7 @@ KmppWs carve(void *ws, int64_t n, size_t *bytes) {
     w.tile_sum = c.take<unsigned long long>(ntiles > 0 ? ntiles : 1);
     w.maxbits = c.take<uint32_t>(1);
     w.scale = c.take<double>(1);
+    w.done = c.take<unsigned int>(1);
     if (bytes) *bytes = c.bytes();
     return w;
 }
@@ -114,122 +118,148 @@ __global__ void kmpp_scale_kernel(const uint32_t *__restrict__ maxbits, int64_t 
     *scale = __longlong_as_double((long long)(e + 1023) << 52);
 }
 
-// Weight tile sums from mind (round 1).
-__global__ void __launch_bounds__(kTileThreads) kmpp_weights_kernel(
-    const float *__restrict__ mind, int64_t n, const double *__restrict__ scale_p,
-    unsigned long long *__restrict__ tile_sum) {
-    __shared__ unsigned long long red[kTileThreads / 32];
-    const double scale = *scale_p;
-    const int64_t t0 = (int64_t)blockIdx.x * kTile;
-    unsigned long long s = 0;
-    for (int u = 0; u < kTile / kTileThreads; ++u) {
-        const int64_t i = t0 + u * kTileThreads + threadIdx.x;
-        if (i < n) s += quant_weight(mind[i], scale);
+// Exclusive prefix sum of v over the CTA (kTileThreads threads, warp
+// shuffles and one pass over the warp totals); *total gets the sum.
+__device__ __forceinline__ unsigned long long cta_exclusive_scan_u64(unsigned long long v,
+                                                                     unsigned long long *warp_tot,
+                                                                     unsigned long long *total) {
+    constexpr int kWarps = kTileThreads / 32;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned long long x = v;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const unsigned long long y = __shfl_up_sync(0xffffffffu, x, off);
+        if (lane >= off) x += y;
     }
-    s = block_sum_u64(s, red);
-    if (threadIdx.x == 0) tile_sum[blockIdx.x] = s;
+    __syncthreads();  // warp_tot of an earlier scan has been read
+    if (lane == 31) warp_tot[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        unsigned long long w = lane < kWarps ? warp_tot[lane] : 0ull;
+#pragma unroll
+        for (int off = 1; off < kWarps; off <<= 1) {
+            const unsigned long long y = __shfl_up_sync(0xffffffffu, w, off);
+            if (lane >= off) w += y;
+        }
+        if (lane < kWarps) warp_tot[lane] = w;
+    }
+    __syncthreads();
+    *total = warp_tot[kWarps - 1];
+    return (warp > 0 ? warp_tot[warp - 1] : 0ull) + x - v;
 }
 
-// Rounds >= 2: update the running minimum with the newest center, then
-// weight tile sums.
+// Round r >= 1, one CTA per tile of kTile frames.  With r_center >= 0 the
+// running minimum first takes the distance to center r_center (rounds >= 2;
+// round 1 uses the minimum of kmpp_first_kernel as it is).  Then the tile's
+// weight sum; the CTA that finishes last draws frame r: t = floor(u W / 2^64)
+// for the weight total W, the first frame whose inclusive prefix weight
+// exceeds t (a uniform frame when W = 0), copied into C0[r].
 __global__ void __launch_bounds__(kTileThreads) kmpp_round_kernel(
-    const float *__restrict__ X, int64_t n, int d, const float *__restrict__ c,
-    float *__restrict__ mind, const double *__restrict__ scale_p,
-    unsigned long long *__restrict__ tile_sum, KmppMetric m, int r_center) {
+    const float *__restrict__ X, int64_t n, int d, float *__restrict__ C0, int64_t *__restrict__ idx_out,
+    float *__restrict__ mind, const double *__restrict__ scale_p, unsigned long long *__restrict__ tile_sum,
+    unsigned int *__restrict__ done, KmppMetric m, int r_center, int r, uint32_t seed) {
+    constexpr int kPer = kTile / kTileThreads;  // frames per thread in the draw's tile
     __shared__ unsigned long long red[kTileThreads / 32];
+    __shared__ bool last;
+    __shared__ long long tile_hit, pick;
+    __shared__ unsigned long long target;
     const double scale = *scale_p;
     const int64_t t0 = (int64_t)blockIdx.x * kTile;
     unsigned long long s = 0;
-    for (int u = 0; u < kTile / kTileThreads; ++u) {
+    for (int u = 0; u < kPer; ++u) {
         const int64_t i = t0 + u * kTileThreads + threadIdx.x;
         if (i < n) {
-            const float dd = kmpp_d2(X, i, d, c, m, r_center);
             float mi = mind[i];
-            if (dd < mi) {
-                mi = dd;
-                mind[i] = mi;
+            if (r_center >= 0) {
+                const float dd = kmpp_d2(X, i, d, C0 + (int64_t)r_center * d, m, r_center);
+                if (dd < mi) {
+                    mi = dd;
+                    mind[i] = mi;
+                }
             }
             s += quant_weight(mi, scale);
         }
     }
     s = block_sum_u64(s, red);
-    if (threadIdx.x == 0) tile_sum[blockIdx.x] = s;
-}
-
-// Single CTA of 1024 threads: draw round r and copy the chosen frame into
-// C0[r].  uniform != 0 draws a frame uniformly (round 0).
-__global__ void __launch_bounds__(1024) kmpp_pick_kernel(
-    const float *__restrict__ X, int64_t n, int d, float *__restrict__ C0,
-    int64_t *__restrict__ idx_out, int r, uint32_t seed, int uniform,
-    const float *__restrict__ mind, const double *__restrict__ scale_p,
-    const unsigned long long *__restrict__ tile_sum, int64_t ntiles) {
-    __shared__ unsigned long long part[1024];
-    __shared__ long long pick;
-    __shared__ unsigned long long target;
-    __shared__ long long tile_hit;
-    const int tid = threadIdx.x;
-    const uint64_t u = kmpp_draw(seed, (uint32_t)r);
-    if (tid == 0) {
-        pick = -1;
+    __threadfence();  // this thread's running minimum before the count
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        tile_sum[blockIdx.x] = s;
+        __threadfence();
+        last = atomicAdd(done, 1u) == gridDim.x - 1;
         tile_hit = -1;
+        pick = -1;
     }
-    if (!uniform) {
-        // Total weight and the tile holding the target.
-        const int64_t per = (ntiles + 1023) / 1024;
-        const int64_t lo = tid * per, hi = min(lo + per, ntiles);
-        unsigned long long s = 0;
-        for (int64_t b = lo; b < hi; ++b) s += tile_sum[b];
-        part[tid] = s;
-        __syncthreads();
-        for (int off = 1; off < 1024; off <<= 1) {
-            unsigned long long v = tid >= off ? part[tid - off] : 0ull;
-            __syncthreads();
-            part[tid] += v;
-            __syncthreads();
-        }
-        const unsigned long long total = part[1023];
-        if (total > 0) {
-            const unsigned long long t = __umul64hi(u, total);
-            unsigned long long run = part[tid] - s;  // exclusive prefix of this thread's range
-            if (run <= t && t < part[tid]) {
-                for (int64_t b = lo; b < hi; ++b) {
-                    if (t < run + tile_sum[b]) {
-                        tile_hit = b;
-                        target = t - run;
-                        break;
-                    }
-                    run += tile_sum[b];
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+
+    // The draw (the other CTAs' sums and minima are read past L1).
+    const int64_t ntiles = gridDim.x;
+    const uint64_t u = kmpp_draw(seed, (uint32_t)r);
+    const int64_t per = (ntiles + kTileThreads - 1) / kTileThreads;
+    const int64_t lo = min((int64_t)threadIdx.x * per, ntiles), hi = min(lo + per, ntiles);
+    unsigned long long ts = 0;
+    for (int64_t b = lo; b < hi; ++b) ts += __ldcg(tile_sum + b);
+    unsigned long long total;
+    const unsigned long long excl = cta_exclusive_scan_u64(ts, red, &total);
+    if (total > 0) {
+        const unsigned long long t = __umul64hi(u, total);
+        if (excl <= t && t < excl + ts) {
+            unsigned long long run = excl;
+            for (int64_t b = lo; b < hi; ++b) {
+                const unsigned long long w = __ldcg(tile_sum + b);
+                if (t < run + w) {
+                    tile_hit = b;
+                    target = t - run;
+                    break;
                 }
+                run += w;
             }
-        }
-        __syncthreads();
-        if (tile_hit >= 0) {
-            // Inside the tile: two frames per thread, inclusive scan.
-            const double scale = *scale_p;
-            const int64_t f0 = tile_hit * kTile + 2 * tid;
-            const unsigned long long w0 = f0 < n ? quant_weight(mind[f0], scale) : 0ull;
-            const unsigned long long w1 = f0 + 1 < n ? quant_weight(mind[f0 + 1], scale) : 0ull;
-            __syncthreads();
-            part[tid] = w0 + w1;
-            __syncthreads();
-            for (int off = 1; off < 1024; off <<= 1) {
-                unsigned long long v = tid >= off ? part[tid - off] : 0ull;
-                __syncthreads();
-                part[tid] += v;
-                __syncthreads();
-            }
-            const unsigned long long incl = part[tid];
-            const unsigned long long excl = incl - w0 - w1;
-            const unsigned long long tt = target;
-            if (excl <= tt && tt < incl) pick = (tt < excl + w0) ? f0 : f0 + 1;
         }
     }
     __syncthreads();
-    if (pick < 0 && tid == 0) pick = (long long)__umul64hi(u, (unsigned long long)n);
+    if (tile_hit >= 0) {
+        // Inside the tile: kPer consecutive frames per thread.
+        const int64_t f0 = tile_hit * kTile + (int64_t)threadIdx.x * kPer;
+        unsigned long long w[kPer], ws = 0;
+#pragma unroll
+        for (int q = 0; q < kPer; ++q) {
+            w[q] = f0 + q < n ? quant_weight(__ldcg(mind + f0 + q), scale) : 0ull;
+            ws += w[q];
+        }
+        unsigned long long tile_total;
+        unsigned long long run = cta_exclusive_scan_u64(ws, red, &tile_total);
+        const unsigned long long tt = target;
+        if (run <= tt && tt < run + ws) {
+#pragma unroll
+            for (int q = 0; q < kPer; ++q) {
+                if (tt < run + w[q]) {
+                    pick = f0 + q;
+                    break;
+                }
+                run += w[q];
+            }
+        }
+    }
+    __syncthreads();
+    if (pick < 0 && threadIdx.x == 0) pick = (long long)__umul64hi(u, (unsigned long long)n);
     __syncthreads();
     const int64_t p = pick;
-    for (int f = tid; f < d; f += 1024) C0[(int64_t)r * d + f] = X[p * d + f];
-    if (idx_out && tid == 0) idx_out[r] = p;
+    for (int f = threadIdx.x; f < d; f += kTileThreads) C0[(int64_t)r * d + f] = X[p * d + f];
+    if (threadIdx.x == 0) {
+        if (idx_out) idx_out[r] = p;
+        *done = 0u;  // for the next round's launch
+    }
+}
+
+// Round 0: a uniformly drawn frame, copied into C0[0].
+__global__ void __launch_bounds__(kTileThreads) kmpp_uniform_kernel(const float *__restrict__ X, int64_t n, int d,
+                                                                    float *__restrict__ C0,
+                                                                    int64_t *__restrict__ idx_out, uint32_t seed) {
+    const int64_t p = (int64_t)__umul64hi(kmpp_draw(seed, 0u), (unsigned long long)n);
+    for (int f = threadIdx.x; f < d; f += blockDim.x) C0[f] = X[p * d + f];
+    if (idx_out && threadIdx.x == 0) idx_out[0] = p;
 }
 
 }  // namespace
@@ -251,26 +281,19 @@ int run_kmpp(const float *X, int64_t n, int d, int k, uint32_t seed, float *C0, 
     }
     KmppWs w = carve(ws, n, nullptr);
     const int64_t ntiles = (n + kTile - 1) / kTile;
-    kmpp_pick_kernel<<<1, 1024, 0, s>>>(X, n, d, C0, idx, 0, seed, 1, w.mind, w.scale, w.tile_sum,
-                                        ntiles);
+    kmpp_uniform_kernel<<<1, kTileThreads, 0, s>>>(X, n, d, C0, idx, seed);
     KM_CUDA(cudaGetLastError());
     if (cb) cb(cb_user);
     if (k == 1) return KM_OK;
     KM_CUDA(cudaMemsetAsync(w.maxbits, 0, sizeof(uint32_t), s));
+    KM_CUDA(cudaMemsetAsync(w.done, 0, sizeof(unsigned int), s));
     kmpp_first_kernel<<<(unsigned)ntiles, kTileThreads, 0, s>>>(X, n, d, C0, w.mind, w.maxbits, m);
     KM_CUDA(cudaGetLastError());
     kmpp_scale_kernel<<<1, 1, 0, s>>>(w.maxbits, n, w.scale);
     KM_CUDA(cudaGetLastError());
-    kmpp_weights_kernel<<<(unsigned)ntiles, kTileThreads, 0, s>>>(w.mind, n, w.scale, w.tile_sum);
-    KM_CUDA(cudaGetLastError());
     for (int r = 1; r < k; ++r) {
-        if (r >= 2) {
-            kmpp_round_kernel<<<(unsigned)ntiles, kTileThreads, 0, s>>>(
-                X, n, d, C0 + (int64_t)(r - 1) * d, w.mind, w.scale, w.tile_sum, m, r - 1);
-            KM_CUDA(cudaGetLastError());
-        }
-        kmpp_pick_kernel<<<1, 1024, 0, s>>>(X, n, d, C0, idx, r, seed, 0, w.mind, w.scale, w.tile_sum,
-                                            ntiles);
+        kmpp_round_kernel<<<(unsigned)ntiles, kTileThreads, 0, s>>>(X, n, d, C0, idx, w.mind, w.scale, w.tile_sum,
+                                                                    w.done, m, r >= 2 ? r - 1 : -1, r, seed);
         KM_CUDA(cudaGetLastError());
         if (cb) cb(cb_user);
     }

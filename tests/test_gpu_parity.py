@@ -175,17 +175,14 @@ def test_update_shapes(torch, L, oracle, d):
     assert abs(cost - cost_ref) <= RTOL_COST_STEP * cost_ref
 
 
-@pytest.mark.parametrize("d", [1, 2, 3, 4, 5, 8, 9, 16, 17])
+@pytest.mark.parametrize("d,n", [(d, 30011) for d in (1, 2, 3, 4, 5, 8, 9, 16, 17)] + [(2, 1000003), (16, 1000003)])
 @pytest.mark.parametrize("k_kind", ["one", "max"])
-@pytest.mark.parametrize("n", [30011, 1000003])
-def test_update_one_pass_shapes(torch, L, oracle, d, k_kind, n):
+def test_update_one_pass_shapes(torch, L, oracle, d, n, k_kind):
     # d <= 16 and few centers take the one-pass shared-memory sums: "max" is
     # the largest k whose sums (k x (d + 1) doubles and k counts) fit in
     # 48 KB, "one" puts every frame in one cluster; the larger n gives each
     # thread a run of several frames.  d = 17 is the segment path.
     k = 1 if k_kind == "one" else 49152 // (8 * (d + 1) + 4)
-    if n > 100000 and d not in (2, 16):
-        pytest.skip("runs of frames: two widths suffice")
     rng = np.random.default_rng(300 + d)
     X = (3.0 + rng.normal(size=(n, d))).astype(np.float32)
     C = (3.0 + rng.normal(size=(k, d))).astype(np.float32)
@@ -235,7 +232,8 @@ def test_kmpp_golden(torch, L, golden):
 
 
 @pytest.mark.parametrize("n,d,k,seed", [(1, 3, 1, 0), (5, 2, 5, 1), (3000, 2, 50, 42), (10000, 10, 200, 7),
-                                        (4100, 528, 30, 3), (2049, 7, 64, 2 ** 32 - 1)])
+                                        (4100, 528, 30, 3), (2049, 7, 64, 2 ** 32 - 1), (600000, 2, 20, 11),
+                                        (1100001, 3, 8, 5)])
 def test_kmpp_matches_oracle(torch, L, oracle, n, d, k, seed):
     rng = np.random.default_rng(seed % 1000)
     X = rng.normal(size=(n, d)).astype(np.float32)
@@ -244,6 +242,18 @@ def test_kmpp_matches_oracle(torch, L, oracle, n, d, k, seed):
     C0, idx = L.kmpp(dev(torch, X), k, seed, callback=lambda: calls.append(1))
     np.testing.assert_array_equal(idx.cpu().numpy(), idx_ref)
     assert len(calls) == k
+
+
+def test_kmpp_sparse_weights_many_tiles(torch, L, oracle):
+    # 700,000 frames (342 weight tiles, more than one per thread of the draw):
+    # all but 30 frames equal, so after a few rounds most tiles weigh 0 and
+    # the last rounds find no weight at all (uniform fallback).
+    rng = np.random.default_rng(4)
+    X = np.zeros((700000, 2), dtype=np.float32)
+    X[rng.choice(700000, 30, replace=False)] = rng.normal(size=(30, 2)).astype(np.float32) * 10
+    _, idx_ref = oracle.kmpp(X, 40, 17)
+    _, idx = L.kmpp(dev(torch, X), 40, 17)
+    np.testing.assert_array_equal(idx.cpu().numpy(), idx_ref)
 
 
 def test_kmpp_duplicates(torch, L, oracle):
