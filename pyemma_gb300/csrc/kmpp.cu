@@ -118,12 +118,13 @@ __global__ void kmpp_scale_kernel(const uint32_t *__restrict__ maxbits, int64_t 
     *scale = __longlong_as_double((long long)(e + 1023) << 52);
 }
 
-// Exclusive prefix sum of v over the CTA (kTileThreads threads, warp
-// shuffles and one pass over the warp totals); *total gets the sum.
+// Exclusive prefix sum of v over the CTA (THREADS threads, warp shuffles
+// and one pass over the warp totals); *total gets the sum.
+template <int THREADS>
 __device__ __forceinline__ unsigned long long cta_exclusive_scan_u64(unsigned long long v,
                                                                      unsigned long long *warp_tot,
                                                                      unsigned long long *total) {
-    constexpr int kWarps = kTileThreads / 32;
+    constexpr int kWarps = THREADS / 32;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     unsigned long long x = v;
 #pragma unroll
@@ -153,13 +154,16 @@ __device__ __forceinline__ unsigned long long cta_exclusive_scan_u64(unsigned lo
 // round 1 uses the minimum of kmpp_first_kernel as it is).  Then the tile's
 // weight sum; the CTA that finishes last draws frame r: t = floor(u W / 2^64)
 // for the weight total W, the first frame whose inclusive prefix weight
-// exceeds t (a uniform frame when W = 0), copied into C0[r].
-__global__ void __launch_bounds__(kTileThreads) kmpp_round_kernel(
+// exceeds t (a uniform frame when W = 0), copied into C0[r].  THREADS = 1024
+// for the Euclidean metric (two frames per thread: the pass is latency-bound
+// at small n), 256 for minRMSD (the QCP solve needs the registers).
+template <int THREADS, bool RMSD>
+__global__ void __launch_bounds__(THREADS) kmpp_round_kernel(
     const float *__restrict__ X, int64_t n, int d, float *__restrict__ C0, int64_t *__restrict__ idx_out,
     float *__restrict__ mind, const double *__restrict__ scale_p, unsigned long long *__restrict__ tile_sum,
     unsigned int *__restrict__ done, KmppMetric m, int r_center, int r, uint32_t seed) {
-    constexpr int kPer = kTile / kTileThreads;  // frames per thread in the draw's tile
-    __shared__ unsigned long long red[kTileThreads / 32];
+    constexpr int kPer = kTile / THREADS;  // frames per thread in the pass and in the draw's tile
+    __shared__ unsigned long long red[THREADS / 32];
     __shared__ bool last;
     __shared__ long long tile_hit, pick;
     __shared__ unsigned long long target;
@@ -167,11 +171,12 @@ __global__ void __launch_bounds__(kTileThreads) kmpp_round_kernel(
     const int64_t t0 = (int64_t)blockIdx.x * kTile;
     unsigned long long s = 0;
     for (int u = 0; u < kPer; ++u) {
-        const int64_t i = t0 + u * kTileThreads + threadIdx.x;
+        const int64_t i = t0 + u * THREADS + threadIdx.x;
         if (i < n) {
             float mi = mind[i];
             if (r_center >= 0) {
-                const float dd = kmpp_d2(X, i, d, C0 + (int64_t)r_center * d, m, r_center);
+                const float *c = C0 + (int64_t)r_center * d;
+                const float dd = RMSD ? kmpp_d2(X, i, d, c, m, r_center) : sqdist_exact(X + i * d, c, d);
                 if (dd < mi) {
                     mi = dd;
                     mind[i] = mi;
@@ -197,12 +202,12 @@ __global__ void __launch_bounds__(kTileThreads) kmpp_round_kernel(
     // The draw (the other CTAs' sums and minima are read past L1).
     const int64_t ntiles = gridDim.x;
     const uint64_t u = kmpp_draw(seed, (uint32_t)r);
-    const int64_t per = (ntiles + kTileThreads - 1) / kTileThreads;
+    const int64_t per = (ntiles + THREADS - 1) / THREADS;
     const int64_t lo = min((int64_t)threadIdx.x * per, ntiles), hi = min(lo + per, ntiles);
     unsigned long long ts = 0;
     for (int64_t b = lo; b < hi; ++b) ts += __ldcg(tile_sum + b);
     unsigned long long total;
-    const unsigned long long excl = cta_exclusive_scan_u64(ts, red, &total);
+    const unsigned long long excl = cta_exclusive_scan_u64<THREADS>(ts, red, &total);
     if (total > 0) {
         const unsigned long long t = __umul64hi(u, total);
         if (excl <= t && t < excl + ts) {
@@ -229,7 +234,7 @@ __global__ void __launch_bounds__(kTileThreads) kmpp_round_kernel(
             ws += w[q];
         }
         unsigned long long tile_total;
-        unsigned long long run = cta_exclusive_scan_u64(ws, red, &tile_total);
+        unsigned long long run = cta_exclusive_scan_u64<THREADS>(ws, red, &tile_total);
         const unsigned long long tt = target;
         if (run <= tt && tt < run + ws) {
 #pragma unroll
@@ -246,7 +251,7 @@ __global__ void __launch_bounds__(kTileThreads) kmpp_round_kernel(
     if (pick < 0 && threadIdx.x == 0) pick = (long long)__umul64hi(u, (unsigned long long)n);
     __syncthreads();
     const int64_t p = pick;
-    for (int f = threadIdx.x; f < d; f += kTileThreads) C0[(int64_t)r * d + f] = X[p * d + f];
+    for (int f = threadIdx.x; f < d; f += THREADS) C0[(int64_t)r * d + f] = X[p * d + f];
     if (threadIdx.x == 0) {
         if (idx_out) idx_out[r] = p;
         *done = 0u;  // for the next round's launch
@@ -292,8 +297,13 @@ int run_kmpp(const float *X, int64_t n, int d, int k, uint32_t seed, float *C0, 
     kmpp_scale_kernel<<<1, 1, 0, s>>>(w.maxbits, n, w.scale);
     KM_CUDA(cudaGetLastError());
     for (int r = 1; r < k; ++r) {
-        kmpp_round_kernel<<<(unsigned)ntiles, kTileThreads, 0, s>>>(X, n, d, C0, idx, w.mind, w.scale, w.tile_sum,
-                                                                    w.done, m, r >= 2 ? r - 1 : -1, r, seed);
+        const int rc = r >= 2 ? r - 1 : -1;
+        if (m.Xc)
+            kmpp_round_kernel<256, true><<<(unsigned)ntiles, 256, 0, s>>>(X, n, d, C0, idx, w.mind, w.scale,
+                                                                          w.tile_sum, w.done, m, rc, r, seed);
+        else
+            kmpp_round_kernel<1024, false><<<(unsigned)ntiles, 1024, 0, s>>>(X, n, d, C0, idx, w.mind, w.scale,
+                                                                             w.tile_sum, w.done, m, rc, r, seed);
         KM_CUDA(cudaGetLastError());
         if (cb) cb(cb_user);
     }
