@@ -84,6 +84,28 @@ def check_minrmsd_dim(dim):
         raise ValueError("RMSDMetric is only implemented for input data with a dimension divisible by 3.")
 
 
+def plan_batches(lengths, budget):
+    """Batches of (traj, start, stop) pieces covering trajectories of the
+    given lengths in order, at most ``budget`` frames per batch; every batch
+    but the last is full, so a trajectory may be split across batches."""
+    if budget < 1:
+        raise ValueError("a batch must hold at least one frame")
+    pieces, batch, size = [], [], 0
+    for i, length in enumerate(lengths):
+        start = 0
+        while start < length:
+            take = min(length - start, budget - size)
+            batch.append((i, start, start + take))
+            size += take
+            start += take
+            if size == budget:
+                pieces.append(batch)
+                batch, size = [], 0
+    if batch:
+        pieces.append(batch)
+    return pieces
+
+
 def assign_trajs(trajs, centers, precision="auto", batch_bytes=None, metric="euclidean"):
     """int32 labels for every frame of every trajectory; returns (list, stats)."""
     torch = torch_module()
@@ -101,21 +123,7 @@ def assign_trajs(trajs, centers, precision="auto", batch_bytes=None, metric="euc
     budget = max(1, int((batch_bytes or BATCH_BYTES) // (4 * dim)))
     outs = [np.empty(len(t), dtype=np.int32) for t in trajs]
     stats = dict(n_frames=0, n_recheck=0, n_full=0, n_flipped=0, precision=None)
-    # Work list of (traj, start, stop) pieces grouped into batches.
-    pieces, batch, size = [], [], 0
-    for i, t in enumerate(trajs):
-        start = 0
-        while start < len(t):
-            take = min(len(t) - start, budget - size)
-            batch.append((i, start, start + take))
-            size += take
-            start += take
-            if size == budget:
-                pieces.append(batch)
-                batch, size = [], 0
-    if batch:
-        pieces.append(batch)
-    for batch in pieces:
+    for batch in plan_batches([len(t) for t in trajs], budget):
         arrays = [trajs[i][a:b] for i, a, b in batch]
         X = pack_to_device(arrays, dim)
         offsets = np.zeros(len(arrays) + 1, dtype=np.int64)

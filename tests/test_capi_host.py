@@ -233,3 +233,26 @@ def test_serving_and_resident_sets_need_a_device():
     out = ctypes.c_void_p()
     assert L.km_centers_create(None, 4, 2, 0, None, ctypes.byref(out)) == _lib.KM_ERR_BAD_SHAPE
     assert L.km_assign_centers_workspace_size(100, None) == 0
+
+
+def test_plan_batches_covers_every_frame_in_order():
+    from pyemma_gb300.coordinates._device import plan_batches
+    rng = np.random.default_rng(0)
+    for lengths in ([0], [5], [0, 3, 0, 7, 1], list(rng.integers(0, 50, size=30))):
+        for budget in (1, 4, 7, 1000):
+            batches = plan_batches(lengths, budget)
+            sizes = [sum(b - a for _, a, b in batch) for batch in batches]
+            assert all(0 < s <= budget for s in sizes)
+            assert all(s == budget for s in sizes[:-1])
+            seen = {i: [] for i in range(len(lengths))}
+            for batch in batches:
+                for i, a, b in batch:
+                    assert 0 <= a < b <= lengths[i]
+                    seen[i].append((a, b))
+            for i, length in enumerate(lengths):
+                spans = seen[i]
+                assert (spans[0][0] if spans else 0) == 0
+                assert all(spans[j][1] == spans[j + 1][0] for j in range(len(spans) - 1))
+                assert (spans[-1][1] if spans else 0) == length
+    with pytest.raises(ValueError):
+        plan_batches([3], 0)

@@ -75,6 +75,22 @@ def test_assign_list_and_skip_stride(coor, oracle):
         np.testing.assert_array_equal(x, oracle.assign(t[3::2], C))
 
 
+@pytest.mark.parametrize("metric", ["euclidean", "minRMSD"])
+def test_assign_split_across_batches(oracle, metric):
+    # a 1,000-frame batch budget splits trajectories across batches
+    from pyemma_gb300.coordinates import _device
+    rng = np.random.default_rng(9)
+    d = 12
+    trajs = [rng.normal(size=(n, d)).astype(np.float32) for n in (0, 1, 2500, 999, 1001, 3)]
+    C = rng.normal(size=(17, d)).astype(np.float32)
+    for prec in (["fp32", "fp16"] if metric == "euclidean" else ["fp32"]):
+        labels, stats = _device.assign_trajs(trajs, C, precision=prec, batch_bytes=4 * d * 1000, metric=metric)
+        assert stats["n_frames"] == sum(len(t) for t in trajs)
+        for got, t in zip(labels, trajs):
+            want = oracle.assign_minrmsd(t, C) if metric == "minRMSD" else oracle.assign(t, C)
+            np.testing.assert_array_equal(got, want)
+
+
 def test_centers_from_file(coor, tmp_path, oracle):
     rng = np.random.default_rng(3)
     C = rng.normal(size=(6, 4)).astype(np.float32)
