@@ -142,8 +142,9 @@ int km_update(const float *X, int64_t n, int32_t d, const int32_t *labels, int32
  * exits; shapes whose scratch (about 4 n + 8 k d + 28 k bytes) does not fit
  * return KM_ERR_WORKSPACE.  The first call on a device looks up the array's
  * device address; make that first call before any stream capture.  All calls
- * share the array, so calls whose work overlaps on the GPU (other streams,
- * other host threads) race; serialise them.  The call synchronises `stream`. */
+ * share the array, so the library runs them one at a time: a call holds a
+ * process-wide lock from its first launch until `stream` has drained (the
+ * call synchronises `stream`). */
 size_t km_update_noalloc_max_bytes(void);
 int km_update_noalloc(const float *X, int64_t n, int32_t d, const int32_t *labels, int32_t k,
                       const float *C_old, float *C_new, int64_t *counts, double *cost, void *stream);

@@ -858,6 +858,9 @@ static __device__ __align__(256) unsigned char g_update_scratch[kNoAllocScratchB
 constexpr int kMaxDevices = 64;
 std::mutex g_scratch_mutex;
 void *g_scratch_ptr[kMaxDevices] = {};
+// Held by km_update_noalloc from its first launch until its stream has
+// drained: the calls share the scratch array, so they run one at a time.
+std::mutex g_noalloc_call_mutex;
 
 // Device address of g_update_scratch on the current device.  In host code the
 // array's name is only a stand-in, so the address is looked up once per
@@ -910,13 +913,21 @@ extern "C" int km_update_noalloc(const float *X, int64_t n, int32_t d, const int
     KM_TRY(scratch_address(&scratch));
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     uint32_t *err = reinterpret_cast<uint32_t *>(static_cast<char *>(scratch) + update_ws_size(n, d, k));
+    std::lock_guard<std::mutex> call_lock(g_noalloc_call_mutex);
     // The array keeps the previous call's contents: the error word is cleared
     // here, and launch_update clears its own counters and sums.
-    KM_CUDA(cudaMemsetAsync(err, 0, sizeof(uint32_t), s));
-    KM_TRY(launch_update(X, n, d, labels, k, C_old, C_new, counts, cost, err, scratch, s));
+    cudaError_t ce = cudaMemsetAsync(err, 0, sizeof(uint32_t), s);
+    if (ce != cudaSuccess) return cuda_fail(ce, "cudaMemsetAsync(error word)");
+    int rc = launch_update(X, n, d, labels, k, C_old, C_new, counts, cost, err, scratch, s);
     uint32_t e = 0;
-    KM_CUDA(cudaMemcpyAsync(&e, err, sizeof(e), cudaMemcpyDeviceToHost, s));
-    KM_CUDA(cudaStreamSynchronize(s));
+    if (rc == KM_OK) {
+        ce = cudaMemcpyAsync(&e, err, sizeof(e), cudaMemcpyDeviceToHost, s);
+        if (ce != cudaSuccess) rc = cuda_fail(ce, "cudaMemcpyAsync(error word)");
+    }
+    // drained before the lock is released, also after a failed launch
+    ce = cudaStreamSynchronize(s);
+    if (rc != KM_OK) return rc;
+    if (ce != cudaSuccess) return cuda_fail(ce, "cudaStreamSynchronize");
     if (e & kDevBadLabel) {
         set_error("a label is outside [0, k)");
         return KM_ERR_BAD_LABEL;

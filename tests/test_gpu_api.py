@@ -60,9 +60,9 @@ def test_assign_return_dtrajs_and_chunksize(coor, blobs, oracle):
 
 def test_assign_wrong_centers(coor):
     with pytest.raises(ValueError):
-        coor.assign_to_centers(np.empty((100, 3)), np.empty((5, 4)))
+        coor.assign_to_centers(np.zeros((100, 3)), np.zeros((5, 4)))
     with pytest.raises(ValueError):
-        coor.assign_to_centers(np.empty((100, 3)), np.empty(1))
+        coor.assign_to_centers(np.zeros((100, 3)), np.zeros(1))
 
 
 def test_assign_list_and_skip_stride(coor, oracle):

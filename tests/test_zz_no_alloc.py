@@ -47,7 +47,7 @@ def _case(torch, seed, n, d, k):
 def test_noalloc_matches_workspace_update_twice():
     import torch
     from pyemma_gb300 import _lib as L
-    for seed, (n, d, k) in enumerate([(50000, 528, 300), (7000, 10, 1000)]):
+    for seed, (n, d, k) in enumerate([(50000, 528, 300), (7000, 10, 1000), (30000, 3, 20)]):
         X, labels, C = _case(torch, seed, n, d, k)
         rc, C_na, cnt_na, cost_na = _call_noalloc(L, torch, X, labels, C)
         assert rc == L.KM_OK, L.load().km_last_error()
@@ -77,3 +77,40 @@ def test_noalloc_rejects_oversized_shapes_and_bad_labels():
     labels[17] = 0
     rc, C_na, _, _ = _call_noalloc(L, torch, X, labels, C)  # the error word does not stick
     assert rc == L.KM_OK
+
+
+def test_noalloc_concurrent_threads_and_streams():
+    # Two host threads, each on its own stream, call km_update_noalloc with
+    # different shapes; the library runs the calls one at a time, so every
+    # result equals the workspace update's.
+    import threading
+    import torch
+    from pyemma_gb300 import _lib as L
+    cases = [_case(torch, 10 + i, n, d, k) for i, (n, d, k) in enumerate([(40000, 64, 200), (25000, 5, 30)])]
+    want = [L.update(X, labels, C) for X, labels, C in cases]
+    torch.cuda.synchronize()
+    failures = []
+
+    def worker(i):
+        X, labels, C = cases[i]
+        C_ws, cnt_ws, cost_ws = want[i]
+        with torch.cuda.stream(torch.cuda.Stream()):
+            for _ in range(15):
+                rc, C_na, cnt_na, cost_na = _call_noalloc(L, torch, X, labels, C)
+                if rc != L.KM_OK:
+                    failures.append((i, "rc", rc))
+                    return
+                if not np.allclose(C_na.cpu().numpy(), C_ws.cpu().numpy(), rtol=RTOL_CENTER_STEP, atol=0):
+                    failures.append((i, "centers"))
+                if not np.array_equal(cnt_na.cpu().numpy(), cnt_ws.cpu().numpy()):
+                    failures.append((i, "counts"))
+                if abs(cost_na - cost_ws) > RTOL_INERTIA * abs(cost_ws):
+                    failures.append((i, "cost"))
+
+    threads = [threading.Thread(target=worker, args=(i,)) for i in range(2)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join(timeout=120)
+    assert not any(t.is_alive() for t in threads)
+    assert not failures, failures
