@@ -20,7 +20,8 @@ def declared_symbols():
     names = []
     for fn in os.listdir(os.path.join(ROOT, "include")):
         if fn.endswith(".h"):
-            text = open(os.path.join(ROOT, "include", fn)).read()
+            with open(os.path.join(ROOT, "include", fn)) as fh:
+                text = fh.read()
             names += re.findall(r"^\s*(?:int|size_t|const char \*)\s*(km_\w+)\s*\(", text, re.M)
     return sorted(set(names))
 
