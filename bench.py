@@ -159,9 +159,10 @@ def profiled_traffic():
     """Per-launch DRAM bytes of the tensor-core kernel from the committed ncu summary."""
     path = os.path.join(ROOT, "profiles", "tc_assign_kernel_c3.md")
     try:
-        for line in open(path):
-            if line.startswith("traffic_bytes_per_launch_full_size:"):
-                return float(line.split(":", 1)[1].strip())
+        with open(path) as fh:
+            for line in fh:
+                if line.startswith("traffic_bytes_per_launch_full_size:"):
+                    return float(line.split(":", 1)[1].strip())
     except OSError:
         pass
     return None
