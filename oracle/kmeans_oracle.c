@@ -616,6 +616,56 @@ static double minrmsd_cost(const float *X, int64_t n, int32_t d, const float *C,
     return cost;
 }
 
+/* Regular space clustering under the minRMSD metric (regspace.py:89
+ * registers the metric, regspace.py:144-152 walks the frames;
+ * test_regspace.py:107-115,137-141 run it): kmo_regspace's walk with the
+ * distance rmsd = (float)sqrt(msd(frame, center)) (the frame's centered row
+ * first in the correlation sums, as in kmo_assign_minrmsd), compared in
+ * double with dmin.  Centers are the frames' own (uncentered) rows. */
+int kmo_regspace_minrmsd(const float *X, int64_t n, int32_t d, double dmin, int32_t max_centers, float *centers,
+                         int32_t *n_centers, int32_t *converged) {
+    if (n < 0 || d <= 0 || d % 3 || max_centers < 1 || !n_centers || !converged) return KMO_BAD_ARG;
+    *n_centers = 0;
+    *converged = 1;
+    if (n == 0) return KMO_OK;
+    float *Xc;
+    double *G;
+    int rc = rmsd_center_all(X, n, d, &Xc, &G, 1);
+    if (rc) return rc;
+    int64_t *idx = (int64_t *)malloc((size_t)max_centers * sizeof(int64_t));
+    if (!idx) {
+        free(Xc);
+        free(G);
+        return KMO_NOMEM;
+    }
+    int32_t nc = 0;
+    for (int64_t i = 0; i < n; ++i) {
+        int is_new = 1;
+        for (int32_t j = 0; j < nc; ++j) {
+            const int64_t c = idx[j];
+            const float dist = (float)sqrt(kmo_rmsd_msd(Xc + (size_t)i * d, Xc + (size_t)c * d, G[i], G[c], d / 3));
+            if (!((double)dist >= dmin)) {
+                is_new = 0;
+                break;
+            }
+        }
+        if (is_new) {
+            if (nc == max_centers) {
+                *converged = 0;
+                break;
+            }
+            idx[nc] = i;
+            memcpy(centers + (size_t)nc * d, X + (size_t)i * d, sizeof(float) * (size_t)d);
+            ++nc;
+        }
+    }
+    *n_centers = nc;
+    free(idx);
+    free(Xc);
+    free(G);
+    return KMO_OK;
+}
+
 int kmo_lloyd_minrmsd(const float *X, int64_t n, int32_t d, int32_t k, float *C, int32_t max_iter, double tol,
                       int32_t *labels, double *inertias, int32_t *n_iter, int32_t *converged, int32_t n_threads) {
     if (n <= 0 || d <= 0 || d % 3 || k <= 0 || !C || !labels || max_iter < 0) return KMO_BAD_ARG;

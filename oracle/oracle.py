@@ -52,8 +52,9 @@ def lib():
         L.kmo_minrmsd_rows.argtypes = [P, P, i64, i32, P]
         L.kmo_lloyd_minrmsd.argtypes = [P, i64, i32, i32, P, i32, f64, P, P, P, P, i32]
         L.kmo_kmpp_minrmsd.argtypes = [P, i64, i32, i32, u32, P, P, i32]
+        L.kmo_regspace_minrmsd.argtypes = [P, i64, i32, f64, i32, P, P, P]
         for name in ("kmo_assign", "kmo_update", "kmo_lloyd", "kmo_kmpp", "kmo_assign_minrmsd", "kmo_minrmsd_rows",
-                     "kmo_lloyd_minrmsd", "kmo_kmpp_minrmsd"):
+                     "kmo_lloyd_minrmsd", "kmo_kmpp_minrmsd", "kmo_regspace_minrmsd"):
             getattr(L, name).restype = ctypes.c_int
         _lib = L
     return _lib
@@ -162,6 +163,18 @@ def regspace(X, dmin, max_centers):
     conv = np.zeros(1, dtype=np.int32)
     rc = lib().kmo_regspace(_ptr(X), n, d, float(dmin), int(max_centers), _ptr(C), _ptr(nc), _ptr(conv))
     _check(rc, "regspace")
+    return C[:int(nc[0])].copy(), bool(conv[0])
+
+
+def regspace_minrmsd(X, dmin, max_centers):
+    """Regular space centers under the minRMSD metric; returns (centers, converged)."""
+    X = _f32(X)
+    n, d = X.shape
+    C = np.empty((max(1, max_centers), d), dtype=np.float32)
+    nc = np.zeros(1, dtype=np.int32)
+    conv = np.zeros(1, dtype=np.int32)
+    rc = lib().kmo_regspace_minrmsd(_ptr(X), n, d, float(dmin), int(max_centers), _ptr(C), _ptr(nc), _ptr(conv))
+    _check(rc, "regspace_minrmsd")
     return C[:int(nc[0])].copy(), bool(conv[0])
 
 

@@ -3,7 +3,9 @@
 Mirrors RegularSpaceClustering of pyemma/coordinates/clustering/
 regspace.py:36-185.  The first pass (the leader walk over the frames in
 iteration order, deeptime RegularSpace.partial_fit at regspace.py:140-152)
-runs as km_regspace; the second pass (Voronoi assignment) is the same
+runs as km_regspace for the Euclidean metric and as
+:func:`minrmsd_leader_walk` over km_assign_minrmsd for minRMSD (the metric
+regspace.py:89 registers); the second pass (Voronoi assignment) is the same
 assignment path as every other estimator here.
 """
 import warnings
@@ -15,6 +17,53 @@ from .. import _device
 from .interface import AbstractClustering
 
 __all__ = ["RegularSpaceClustering", "NotConvergedWarning"]
+
+
+MINRMSD_WALK_BLOCK = 8192
+
+
+def minrmsd_leader_walk(X, dmin, max_centers, block=MINRMSD_WALK_BLOCK):
+    """The regular space walk under the minRMSD metric.
+
+    X is a contiguous float32 (n, 3 n_atoms) CUDA tensor.  Returns the frame
+    indices of the centers in frame order and whether the walk finished
+    (False when a (max_centers + 1)-th center would be added).
+
+    The walk is the sequential one (a frame becomes a center when its float32
+    rmsd to every center before it, compared in double, is at least dmin),
+    batched: for a block of frames one km_assign_minrmsd call gives every
+    frame's smallest rmsd to the centers found before the block, which
+    settles the frames below dmin.  The others are resolved in frame order:
+    the first is a center (no center of the block precedes it), the later
+    ones stay candidates only if at least dmin from it (one more call), and
+    so on.  A frame's rmsd to a center is the same value in both forms, so
+    the result equals the sequential walk's.
+    """
+    import torch
+    n = int(X.shape[0])
+    idx = []
+    C = None
+    for pos in range(0, n, block):
+        blk = X[pos:pos + block]
+        if C is None:
+            cand = np.arange(int(blk.shape[0]))
+        else:
+            _, r = _lib.assign_minrmsd(blk, C, return_rmsd=True)
+            cand = np.nonzero(r.cpu().numpy().astype(np.float64) >= dmin)[0]
+        while len(cand):
+            if len(idx) == max_centers:
+                return idx, False
+            first = int(cand[0])
+            idx.append(pos + first)
+            c1 = blk[first:first + 1].contiguous()
+            C = c1 if C is None else torch.cat([C, c1]).contiguous()
+            rest = cand[1:]
+            if not len(rest):
+                break
+            rows = blk[torch.from_numpy(rest).to(blk.device)].contiguous()
+            _, r = _lib.assign_minrmsd(rows, c1, return_rmsd=True)
+            cand = rest[r.cpu().numpy().astype(np.float64) >= dmin]
+    return idx, True
 
 
 class NotConvergedWarning(RuntimeWarning):
@@ -32,7 +81,7 @@ class RegularSpaceClustering(AbstractClustering):
         When this many centers are found and another frame qualifies, the
         walk stops with a warning and the centers found so far are kept.
     metric : str
-        'euclidean'.
+        'euclidean' or 'minRMSD'.
     stride, skip : int
         Frames used for the center search: traj[skip::stride].
     n_jobs : int or None
@@ -90,15 +139,19 @@ class RegularSpaceClustering(AbstractClustering):
         return self._converged
 
     def _estimate(self, source):
-        if self.metric == "minRMSD":
-            raise NotImplementedError("regular space clustering has no minRMSD center search; "
-                                      "the minRMSD metric is available for k-means and assignment")
         stride = self.stride if self.stride else 1
         trajs = source.frames(stride=stride, skip=self.skip)
         dim = source.dimension()
+        if self.metric == "minRMSD":
+            _device.check_minrmsd_dim(dim)
         used = int(sum(len(t) for t in trajs))
         X = _device.pack_to_device(trajs, dim)
-        C, converged = _lib.regspace(X, self.dmin, max(1, self.max_centers))
+        if self.metric == "minRMSD":
+            import torch
+            idx, converged = minrmsd_leader_walk(X, self.dmin, max(1, self.max_centers))
+            C = X[torch.tensor(idx, dtype=torch.int64, device=X.device)]
+        else:
+            C, converged = _lib.regspace(X, self.dmin, max(1, self.max_centers))
         del X
         self.clustercenters = C.cpu().numpy()
         self._converged = converged

@@ -26,6 +26,7 @@ import numpy as np
 
 from . import _lib
 from .coordinates import _device
+from .coordinates.clustering.regspace import minrmsd_leader_walk
 
 __all__ = ["KMeans", "KMeansModel", "MiniBatchKMeans", "ClusterModel", "RegularSpace", "metrics",
            "MaxCentersReachedException", "install", "uninstall"]
@@ -237,12 +238,9 @@ class RegularSpace(object):
             raise ValueError("dmin has to be positive, got %s" % dmin)
         if int(max_centers) < 1:
             raise ValueError("max_centers has to be at least 1, got %s" % max_centers)
-        if _check_metric(metric) == "minRMSD":
-            raise NotImplementedError("regular space clustering has no minRMSD center search; "
-                                      "the minRMSD metric is available for k-means and assignment")
         self.dmin = float(dmin)
         self.max_centers = int(max_centers)
-        self.metric = metric
+        self.metric = _check_metric(metric)
         self.n_jobs = n_jobs
         self._centers = None
 
@@ -260,7 +258,12 @@ class RegularSpace(object):
                 raise ValueError("data has dimension %d, the centers %d" % (X.shape[1], self._centers.shape[1]))
             torch = _device.torch_module()
             X = torch.cat([_device.centers_to_device(self._centers), X]).contiguous()
-        C, converged = _lib.regspace(X, self.dmin, self.max_centers)
+        if self.metric == "minRMSD":
+            torch = _device.torch_module()
+            idx, converged = minrmsd_leader_walk(X, self.dmin, self.max_centers)
+            C = X[torch.tensor(idx, dtype=torch.int64, device=X.device)]
+        else:
+            C, converged = _lib.regspace(X, self.dmin, self.max_centers)
         self._centers = C.cpu().numpy()
         if not converged:
             raise MaxCentersReachedException("Maximum number of cluster centers (%d) reached" % self.max_centers)

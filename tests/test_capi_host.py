@@ -199,8 +199,8 @@ def test_minrmsd_dimension_rule():
     assert km.metric == "minRMSD"
     with pytest.raises(ValueError):
         km.estimate(np.zeros((10, 4), dtype=np.float32))
-    with pytest.raises(NotImplementedError):
-        RegularSpaceClustering(dmin=1.0, metric="minRMSD").estimate(np.zeros((10, 6), dtype=np.float32))
+    with pytest.raises(ValueError):
+        RegularSpaceClustering(dmin=1.0, metric="minRMSD").estimate(np.zeros((10, 4), dtype=np.float32))
     with pytest.raises(ValueError):
         KmeansClustering(n_clusters=3, metric="manhattan")
 
@@ -257,3 +257,37 @@ def test_plan_batches_covers_every_frame_in_order():
                 assert (spans[-1][1] if spans else 0) == length
     with pytest.raises(ValueError):
         plan_batches([3], 0)
+
+
+
+def test_minrmsd_leader_walk_equals_sequential_walk(oracle, monkeypatch):
+    # The batched walk over km_assign_minrmsd, driven here by a stand-in that
+    # returns the oracle's labels and float32 rmsd (the values the kernel
+    # returns bit for bit), equals the oracle's sequential walk for any block
+    # size, including the max_centers stop and a frame that is not finite.
+    import torch
+    from pyemma_gb300 import _lib
+    from pyemma_gb300.coordinates.clustering import regspace
+
+    def fake_assign_minrmsd(X, C, labels=None, return_rmsd=False):
+        lab, msd = oracle.assign_minrmsd(X.numpy(), C.numpy(), return_msd=True)
+        return torch.from_numpy(lab), torch.from_numpy(np.sqrt(msd).astype(np.float32))
+
+    monkeypatch.setattr(_lib, "assign_minrmsd", fake_assign_minrmsd)
+    from test_oracle_pins import rotated_clusters
+    rng = np.random.default_rng(22)
+    X = np.concatenate([rotated_clusters(rng, n_clusters=4, n_particles=4, per_cluster=30),
+                        rng.uniform(-2, 2, size=(60, 12)).astype(np.float32)])
+    X[7, 2] = np.nan
+    Xt = torch.from_numpy(X)
+    for dmin, max_centers in ((0.9, 1000), (0.5, 1000), (0.5, 7), (0.5, 1)):
+        want, conv = oracle.regspace_minrmsd(X, dmin, max_centers)
+        for block in (1, 5, 64, 8192):
+            idx, done = regspace.minrmsd_leader_walk(Xt, dmin, max_centers, block=block)
+            np.testing.assert_array_equal(X[idx], want)
+            assert done == conv
+    Xn = X.copy()
+    Xn[0, 0] = np.nan  # a first frame that is not finite is the only center
+    want, conv = oracle.regspace_minrmsd(Xn, 0.5, 1000)
+    idx, done = regspace.minrmsd_leader_walk(torch.from_numpy(Xn), 0.5, 1000, block=16)
+    assert idx == [0] and len(want) == 1 and done == conv

@@ -58,8 +58,9 @@ def test_argument_checks():
         dc.ClusterModel(np.zeros(3, dtype=np.float32))
     with pytest.raises(ValueError):
         dc.RegularSpace(-1.0)
-    with pytest.raises(NotImplementedError):
-        dc.RegularSpace(1.0, metric="minRMSD")
+    with pytest.raises(ValueError):
+        dc.RegularSpace(1.0, metric="hamming")
+    assert dc.RegularSpace(1.0, metric="minRMSD").metric == "minRMSD"
     with pytest.raises(NotImplementedError):
         dc.MiniBatchKMeans(3).fit(np.zeros((10, 2), dtype=np.float32))
     km = dc.KMeans(3, 10, "euclidean", tolerance=1e-5, init_strategy="kmeans++", fixed_seed=42, n_jobs=1)

@@ -95,3 +95,51 @@ def test_mini_batch_kmeans(oracle):
     np.testing.assert_allclose(np.sort(cl2.clustercenters[:, 0]), means, atol=0.2)
     with pytest.raises(ValueError):
         cluster_mini_batch_kmeans(X, k=3, batch_size=1.5)
+
+
+def _regspace_minrmsd_data():
+    from test_oracle_pins import rotated_clusters
+    rng = np.random.default_rng(22)
+    return np.concatenate([rotated_clusters(rng, n_clusters=4, n_particles=4, per_cluster=30),
+                           rng.uniform(-2, 2, size=(60, 12)).astype(np.float32)])
+
+
+@pytest.mark.parametrize("dmin,max_centers", [(0.9, 1000), (0.5, 1000), (0.5, 7)])
+def test_regspace_minrmsd_equals_oracle(oracle, dmin, max_centers):
+    # test_regspace.py:107-115,137-141: regular space under minRMSD, centers
+    # equal to the oracle's sequential walk, dtrajs to its assignment
+    from pyemma_gb300.coordinates import cluster_regspace
+    X = _regspace_minrmsd_data()
+    want, conv = oracle.regspace_minrmsd(X, dmin, max_centers)
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        cl = cluster_regspace(X, dmin=dmin, max_centers=max_centers, metric="minRMSD")
+    np.testing.assert_array_equal(cl.clustercenters, want)
+    assert cl.converged == conv
+    np.testing.assert_array_equal(cl.dtrajs[0], oracle.assign_minrmsd(X, want))
+
+
+def test_regspace_minrmsd_block_boundaries_and_one_atom(oracle):
+    import torch
+    from pyemma_gb300.coordinates import cluster_regspace
+    from pyemma_gb300.coordinates.clustering.regspace import minrmsd_leader_walk
+    X = _regspace_minrmsd_data()
+    Xd = torch.from_numpy(X).cuda()
+    for block in (1, 7, 100):
+        idx, done = minrmsd_leader_walk(Xd, 0.5, 1000, block=block)
+        np.testing.assert_array_equal(X[idx], oracle.regspace_minrmsd(X, 0.5, 1000)[0])
+        assert done
+    # the reference test's data: single atoms are all at distance 0 after centering
+    one = np.random.default_rng(3).uniform(-2, 2, size=(1000, 3)).astype(np.float32)
+    cl = cluster_regspace(one, dmin=2.0, metric="minRMSD")
+    assert len(cl.clustercenters) == 1
+    assert (cl.assign(np.random.default_rng(4).random((1000, 3)).astype(np.float32), stride=1) == 0).all()
+
+
+def test_regspace_minrmsd_through_deeptime_names(oracle):
+    from pyemma_gb300 import deeptime_clustering as dc
+    X = _regspace_minrmsd_data()
+    est = dc.RegularSpace(dmin=0.5, max_centers=1000, metric="minRMSD")
+    for a in range(0, len(X), 70):
+        est.partial_fit(X[a:a + 70])
+    np.testing.assert_array_equal(est.fetch_model().cluster_centers, oracle.regspace_minrmsd(X, 0.5, 1000)[0])

@@ -301,3 +301,31 @@ def test_minrmsd_lloyd_inertia_decreases(oracle):
     r = oracle.lloyd_minrmsd(out, C0, 20, 1e-9)
     assert r["n_iter"] >= 1
     assert np.all(np.diff(r["inertias"]) <= 1e-6 * r["inertias"][0])
+
+
+def test_regspace_minrmsd_oracle(oracle):
+    # test_regspace.py:107-115,137-141 run regular space under minRMSD: the
+    # walk equals a frame-by-frame loop over compute_metric, the centers are
+    # pairwise at least dmin apart, and single atoms (d = 3) are all at
+    # distance 0 after centering, so one center remains.
+    rng = np.random.default_rng(21)
+    X = rotated_clusters(rng, n_clusters=4, n_particles=4, per_cluster=30)
+    X = np.concatenate([X, rng.uniform(-2, 2, size=(60, 12)).astype(np.float32)])
+    for dmin, max_centers in ((0.9, 1000), (0.5, 1000), (0.5, 7)):
+        C, conv = oracle.regspace_minrmsd(X, dmin, max_centers)
+        want, full = [], True
+        for i in range(len(X)):
+            if all(float(oracle.minrmsd_rows(X[i:i + 1], X[c:c + 1])[0]) >= dmin for c in want):
+                if len(want) == max_centers:
+                    full = False
+                    break
+                want.append(i)
+        np.testing.assert_array_equal(C, X[want])
+        assert conv == full
+        for a in range(len(C)):
+            for b in range(a):
+                assert float(oracle.minrmsd_rows(C[a:a + 1], C[b:b + 1])[0]) >= dmin
+    assert not oracle.regspace_minrmsd(X, 0.5, 7)[1]
+    one_atom = np.random.default_rng(2).uniform(-2, 2, size=(1000, 3)).astype(np.float32)
+    C1, conv1 = oracle.regspace_minrmsd(one_atom, 2.0, 1000)
+    assert conv1 and len(C1) == 1
