@@ -291,3 +291,23 @@ def test_minrmsd_leader_walk_equals_sequential_walk(oracle, monkeypatch):
     want, conv = oracle.regspace_minrmsd(Xn, 0.5, 1000)
     idx, done = regspace.minrmsd_leader_walk(torch.from_numpy(Xn), 0.5, 1000, block=16)
     assert idx == [0] and len(want) == 1 and done == conv
+
+
+def test_index_clusters_and_samples():
+    # test_cluster_samples.py:30-73: the catalogue of (trajectory, time)
+    # indexes per cluster and samples drawn from it, on dtrajs set directly
+    # (these helpers are host-only; the assignment that makes the dtrajs is
+    # tested on the GPU)
+    from pyemma_gb300.coordinates import AssignCenters
+    trajs = [[0, 1, 2], [3, 4, 5], [6, 7, 8], [0, 1, 2], [3, 4, 5], [6, 7, 8]]
+    obj = AssignCenters(np.arange(9, dtype=np.float32).reshape(-1, 1))
+    obj._dtrajs = [np.asarray(t, dtype=np.int32) for t in trajs]
+    ref = [[[i // 3, i % 3], [i // 3 + 3, i % 3]] for i in range(9)]
+    for cc in range(9):
+        np.testing.assert_array_equal(obj.index_clusters[cc], ref[cc])
+    samples = obj.sample_indexes_by_cluster(np.arange(9), 10)
+    for ii, isample in enumerate(samples):
+        assert isample.shape == (10, 2)
+        assert all(obj.dtrajs[a][b] == ii for a, b in isample)
+    distinct = obj.sample_indexes_by_cluster([4], 10, replace=False)[0]
+    assert len(distinct) == 2 and len({tuple(p) for p in distinct}) == 2
