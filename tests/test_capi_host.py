@@ -311,3 +311,27 @@ def test_index_clusters_and_samples():
         assert all(obj.dtrajs[a][b] == ii for a, b in isample)
     distinct = obj.sample_indexes_by_cluster([4], 10, replace=False)[0]
     assert len(distinct) == 2 and len({tuple(p) for p in distinct}) == 2
+
+
+def test_save_dtrajs_formats(tmp_path):
+    # interface.py:233-302 (test_cluster.py:137-150, test_assign.py:157-166):
+    # file names from the prefix and trajectory index or from trajfiles, ascii
+    # and npy output, no silent overwrite
+    from pyemma_gb300.coordinates import AssignCenters
+    obj = AssignCenters(np.arange(4, dtype=np.float32).reshape(-1, 1))
+    obj._dtrajs = [np.array([0, 3, 3, 1], dtype=np.int32), np.array([2], dtype=np.int32)]
+    out = str(tmp_path)
+    obj.save_dtrajs(prefix="run", output_dir=out, extension="dtraj")
+    for i, d in enumerate(obj._dtrajs):
+        np.testing.assert_array_equal(np.atleast_1d(np.loadtxt(os.path.join(out, "run_%i.dtraj" % i), dtype=int)), d)
+    obj.save_dtrajs(output_dir=out, output_format="npy", extension=".npy")
+    for i, d in enumerate(obj._dtrajs):
+        np.testing.assert_array_equal(np.load(os.path.join(out, "%i.npy" % i)), d)
+    obj.save_dtrajs(trajfiles=["/data/a.xtc", "/data/b.xtc"], output_dir=out)
+    assert os.path.exists(os.path.join(out, "a.dtraj")) and os.path.exists(os.path.join(out, "b.dtraj"))
+    obj._dtrajs = [np.array([1, 1], dtype=np.int32), np.array([0], dtype=np.int32)]
+    obj.save_dtrajs(prefix="run", output_dir=out, extension=".dtraj")  # exists: kept, error logged
+    np.testing.assert_array_equal(np.loadtxt(os.path.join(out, "run_0.dtraj"), dtype=int), [0, 3, 3, 1])
+    obj.overwrite_dtrajs = True
+    obj.save_dtrajs(prefix="run", output_dir=out, extension=".dtraj")
+    np.testing.assert_array_equal(np.loadtxt(os.path.join(out, "run_0.dtraj"), dtype=int), [1, 1])
