@@ -7,3 +7,4 @@ kernels behind the C ABI of ``libkmgpu.so`` (include/kmgpu.h).
 __version__ = "0.1.0"
 
 from . import coordinates  # noqa: E402,F401
+from .serialization import list_models, load  # noqa: E402,F401

@@ -114,6 +114,24 @@ class AbstractClustering(object):
     def _param_names(self):
         return ("metric", "n_jobs", "precision")
 
+    # ---- persistence (serialization.py:212-290) ----------------------------
+    def save(self, file_name, model_name="default", overwrite=False, save_streaming_chain=False):
+        """Stores the parameters and the model (centers, dtrajs, convergence)
+        in file_name under model_name; see pyemma_gb300.serialization."""
+        from ... import serialization
+        serialization.save(self, file_name, model_name=model_name, overwrite=overwrite,
+                           save_streaming_chain=save_streaming_chain)
+
+    @classmethod
+    def load(cls, file_name, model_name="default"):
+        """The estimator stored in file_name under model_name."""
+        from ... import serialization
+        obj = serialization.load(file_name, model_name=model_name)
+        if not isinstance(obj, cls):
+            raise TypeError("model %r in %s is a %s, not a %s" % (model_name, file_name, type(obj).__name__,
+                                                                  cls.__name__))
+        return obj
+
     # ---- data producer ---------------------------------------------------
     @property
     def data_producer(self):

@@ -335,3 +335,54 @@ def test_save_dtrajs_formats(tmp_path):
     obj.overwrite_dtrajs = True
     obj.save_dtrajs(prefix="run", output_dir=out, extension=".dtraj")
     np.testing.assert_array_equal(np.loadtxt(os.path.join(out, "run_0.dtraj"), dtype=int), [1, 1])
+
+
+def test_save_and_load_estimators(tmp_path):
+    # test_serialization.py:73-90: a saved estimator comes back with its
+    # parameters and model fields; several models share a file
+    import pyemma_gb300
+    from pyemma_gb300.coordinates import (AssignCenters, KmeansClustering, MiniBatchKmeansClustering,
+                                          RegularSpaceClustering, UniformTimeClustering)
+    fn = str(tmp_path / "models.pyemma")
+    rng = np.random.default_rng(0)
+    km = KmeansClustering(n_clusters=10, init_strategy="uniform", max_iter=42, metric="minRMSD", stride=1,
+                          fixed_seed=463498, precision="fp16")
+    km.clustercenters = rng.random((10, 3))
+    km.initial_centers_ = rng.random((10, 3)).astype(np.float32)
+    km._converged = True
+    km.inertias = np.array([3.0, 2.5, 2.4])
+    km.n_iter = 3
+    km._dtrajs = [np.array([0, 3, 9], dtype=np.int32), np.array([], dtype=np.int32)]
+    km.save(fn)
+    back = pyemma_gb300.load(fn)
+    assert type(back) is KmeansClustering
+    for k in ("n_clusters", "init_strategy", "max_iter", "metric", "stride", "fixed_seed", "precision", "tolerance"):
+        assert getattr(back, k) == getattr(km, k), k
+    np.testing.assert_array_equal(back.clustercenters, km.clustercenters)
+    np.testing.assert_array_equal(back.initial_centers_, km.initial_centers_)
+    assert back.converged and back.n_iter == 3
+    np.testing.assert_array_equal(back.inertias, km.inertias)
+    assert [d.tolist() for d in back.dtrajs] == [[0, 3, 9], []]
+    others = {"regspace": RegularSpaceClustering(dmin=0.1, max_centers=100, metric="minRMSD", n_jobs=4, stride=2),
+              "uniform": UniformTimeClustering(n_clusters=3, metric="minRMSD", n_jobs=4),
+              "mini": MiniBatchKmeansClustering(n_clusters=5, batch_size=0.3, max_iter=7),
+              "assign": AssignCenters(rng.random((4, 6)), metric="minRMSD", skip=2)}
+    for name, obj in others.items():
+        obj.save(fn, model_name=name)
+    assert pyemma_gb300.list_models(fn) == ["assign", "default", "mini", "regspace", "uniform"]
+    for name, obj in others.items():
+        back = type(obj).load(fn, model_name=name)
+        for k, v in obj.get_params().items():
+            if isinstance(v, np.ndarray):
+                np.testing.assert_array_equal(getattr(back, k), v)
+            else:
+                assert getattr(back, k) == v, (name, k)
+    with pytest.raises(RuntimeError):
+        km.save(fn)
+    km.max_iter = 7
+    km.save(fn, overwrite=True)
+    assert pyemma_gb300.load(fn).max_iter == 7
+    with pytest.raises(KeyError):
+        pyemma_gb300.load(fn, model_name="missing")
+    with pytest.raises(TypeError):
+        KmeansClustering.load(fn, model_name="regspace")
