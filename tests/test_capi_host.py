@@ -386,3 +386,22 @@ def test_save_and_load_estimators(tmp_path):
         pyemma_gb300.load(fn, model_name="missing")
     with pytest.raises(TypeError):
         KmeansClustering.load(fn, model_name="regspace")
+
+
+def test_synthetic_workloads_are_seeded():
+    # the benchmark inputs: deterministic per seed, with the stated shapes
+    # and value ranges (c1 mixture, c2 trajectories, c3 C-alpha distances)
+    from pyemma_gb300 import datasets
+    a, b = datasets.small_mixture(seed=3), datasets.small_mixture(seed=3)
+    assert a.shape == (100000, 2) and a.dtype == np.float32
+    np.testing.assert_array_equal(a, b)
+    assert not np.array_equal(a, datasets.small_mixture(seed=4))
+    trajs = datasets.metastable_trajectories(n_traj=5, d=10, lmin=500, lmax=5000, seed=1)
+    assert len(trajs) == 5 and all(t.shape[1] == 10 and t.dtype == np.float32 for t in trajs)
+    assert all(500 <= len(t) <= 5000 for t in trajs)
+    again = datasets.metastable_trajectories(n_traj=5, d=10, lmin=500, lmax=5000, seed=1)
+    assert all(np.array_equal(x, y) for x, y in zip(trajs, again))
+    D = datasets.calpha_distances(n_frames=3000, seed=2)
+    assert D.shape == (3000, 528) and D.dtype == np.float32
+    assert 0.0 < D.min() and D.max() < 12.0 and np.isfinite(D).all()
+    np.testing.assert_array_equal(D, datasets.calpha_distances(n_frames=3000, seed=2))
