@@ -329,3 +329,21 @@ def test_regspace_minrmsd_oracle(oracle):
     one_atom = np.random.default_rng(2).uniform(-2, 2, size=(1000, 3)).astype(np.float32)
     C1, conv1 = oracle.regspace_minrmsd(one_atom, 2.0, 1000)
     assert conv1 and len(C1) == 1
+
+
+def test_lloyd_matches_scikit_learn(oracle):
+    # Independent cross-check of the update step: from the same initial
+    # centers on well-separated data (float32 and float64 labels agree),
+    # n oracle iterations give scikit-learn's Lloyd centers up to float32
+    # rounding, and the fixed point's inertia.
+    cluster = pytest.importorskip("sklearn.cluster")
+    rng = np.random.default_rng(31)
+    means = rng.uniform(-6, 6, size=(8, 5))
+    X = (means[rng.integers(0, 8, 4000)] + 0.6 * rng.normal(size=(4000, 5))).astype(np.float32)
+    C0 = X[rng.choice(4000, 8, replace=False)].copy()
+    for iters in (1, 3, 10, 50):
+        ref = oracle.lloyd(X, C0, iters, -1.0)
+        km = cluster.KMeans(n_clusters=8, init=C0.astype(np.float64), n_init=1, max_iter=iters, tol=0.0,
+                            algorithm="lloyd").fit(X.astype(np.float64))
+        np.testing.assert_allclose(ref["centers"], km.cluster_centers_, rtol=0, atol=1e-5)
+    assert abs(ref["inertias"][-1] - km.inertia_) <= 1e-6 * km.inertia_
