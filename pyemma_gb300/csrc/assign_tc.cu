@@ -69,7 +69,6 @@ constexpr int kThreadsTC = 192;   // warp 0 TMA, warp 1 MMA, warps 2-5 epilogue
 constexpr int kMaxNkc = 10;       // resident A tile up to kp = 640
 constexpr int kSmemLimit = 232448;
 constexpr int kABytesPerChunk = kBM * kKC * 2;  // 16 KB
-constexpr float kFp16Max = 65504.0f;
 
 // Scalars shared by the prep kernels and the main kernel (uint32 words).
 enum ScalarSlot { kScale = 0, kInvScale2 = 1, kScaleMax = 2, kCmax = 3, kHcMax = 4, kNumScalars = 8 };
