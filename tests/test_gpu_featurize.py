@@ -35,7 +35,6 @@ def test_ca_distances_match_oracle(oracle, excl):
 
 
 def test_cluster_device_features_equals_host(oracle):
-    import torch
     from pyemma_gb300.coordinates import cluster_kmeans, assign_to_centers
     from pyemma_gb300.featurize import ca_distances
     rng = np.random.default_rng(9)
