@@ -1,5 +1,6 @@
 """The oracle reproduces the committed golden vectors (tests/golden/)."""
 import numpy as np
+import pytest
 
 
 def test_assign_golden(oracle, golden):
@@ -42,3 +43,17 @@ def test_kmpp_golden(oracle, golden):
     C, idx = oracle.kmpp(golden["kmpp_X"], 20, int(golden["kmpp_seed"][0]))
     np.testing.assert_array_equal(idx, golden["kmpp_idx"])
     np.testing.assert_array_equal(C, golden["kmpp_X"][idx])
+
+
+def test_make_golden_reproduces_the_fixtures(oracle, golden, monkeypatch):
+    # the committed generator, run again, gives the committed arrays
+    pytest.importorskip("sklearn")
+    import os
+    import runpy
+    captured = {}
+    monkeypatch.setattr(np, "savez_compressed", lambda path, **kw: captured.update(kw))
+    root = os.path.dirname(os.path.abspath(__file__))
+    runpy.run_path(os.path.join(root, "golden", "make_golden.py"), run_name="__main__")
+    assert set(captured) == set(golden)
+    for key, value in golden.items():
+        np.testing.assert_array_equal(captured[key], value, err_msg=key)
