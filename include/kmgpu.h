@@ -91,6 +91,14 @@ const char *km_last_error(void);
 int km_profile_enable(int on);
 int km_profile_read(int32_t kind, double *ms_total, int64_t *launches);
 
+/* ---- test hook (diagnostics; no reference counterpart) --------------------
+ * The next km_update or km_update_noalloc call ORs `bits` into the device
+ * error word it reads back, as if a kernel had set them (1, 2, 4: a
+ * device-side wait ran out; 8: a label out of range), and returns the
+ * status that word maps to.  Lets tests check the mapping without making a
+ * device wait run out. */
+int km_debug_fake_device_error(uint32_t bits);
+
 /* ---- assignment: ClusterModel(centers, 'euclidean').transform(X) ----------
  * interface.py:157-167.  labels[i] = argmin_j ||X[i]-C[j]||^2, float32
  * distances summed in feature order, lowest index on ties.  stats (host,
@@ -134,17 +142,21 @@ int km_update(const float *X, int64_t n, int32_t d, const int32_t *labels, int32
               size_t workspace_bytes, void *stream);
 
 /* ---- centroid update without a workspace (no counterpart in the reference) --
- * Same arithmetic and outputs as km_update, for callers that cannot provide
- * device memory (a plugin inside a host program that owns all device
- * allocations, or a loop that must not call cudaMalloc).  Its scratch is a
- * fixed array inside the library of km_update_noalloc_max_bytes() bytes
+ * Same arithmetic, outputs and statuses as km_update, for callers that
+ * cannot provide device memory (a plugin inside a host program that owns all
+ * device allocations, or a loop that must not call cudaMalloc).  Its scratch
+ * is a fixed array inside the library of km_update_noalloc_max_bytes() bytes
  * (32 MiB), held on every GPU that loads the library until the process
- * exits; shapes whose scratch (about 4 n + 8 k d + 28 k bytes) does not fit
- * return KM_ERR_WORKSPACE.  The first call on a device looks up the array's
- * device address; make that first call before any stream capture.  All calls
- * share the array, so the library runs them one at a time: a call holds a
- * process-wide lock from its first launch until `stream` has drained (the
- * call synchronises `stream`). */
+ * exits.  A shape fits when km_update_workspace_size(n, d, k) is at most that
+ * (8 n + 8 k d + 32 k bytes plus about 2.5 KB of alignment, so n up to about
+ * 4 million frames at small k d); larger shapes return KM_ERR_WORKSPACE.  The
+ * first call on a device looks up the array's device address.  Every call
+ * reads the device error word back and synchronises `stream`, so it must not
+ * be called on a stream that is being captured: it returns
+ * KM_ERR_UNSUPPORTED there, before enqueuing anything.  Calls on one device
+ * share that device's array, so the library runs them one at a time: a call
+ * holds that device's lock from its first launch until `stream` has drained.
+ * Calls on different devices do not wait for each other. */
 size_t km_update_noalloc_max_bytes(void);
 int km_update_noalloc(const float *X, int64_t n, int32_t d, const int32_t *labels, int32_t k,
                       const float *C_old, float *C_new, int64_t *counts, double *cost, void *stream);

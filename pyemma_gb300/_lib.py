@@ -27,6 +27,7 @@ KM_PENDING = 8
 
 EXPORTED = (
     "km_version", "km_status_string", "km_last_error", "km_profile_enable", "km_profile_read",
+    "km_debug_fake_device_error",
     "km_assign_workspace_size", "km_assign", "km_batch_assign", "km_debug_tc_distances",
     "km_update_workspace_size", "km_update", "km_update_noalloc_max_bytes", "km_update_noalloc",
     "km_kmpp_workspace_size", "km_kmpp",
@@ -114,6 +115,8 @@ def load(build_if_missing=False):
     L.km_profile_enable.restype = ctypes.c_int
     L.km_profile_read.argtypes = [i32, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int64)]
     L.km_profile_read.restype = ctypes.c_int
+    L.km_debug_fake_device_error.argtypes = [u32]
+    L.km_debug_fake_device_error.restype = ctypes.c_int
     L.km_assign_workspace_size.argtypes = [i64, i32, i32, i32]
     L.km_assign_workspace_size.restype = sz
     L.km_assign.argtypes = [P, i64, i32, P, i32, i32, P, P, sz, ctypes.POINTER(AssignStats), P]

@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <cstring>
 #include <map>
+#include <atomic>
 #include <mutex>
 #include <utility>
 #include <vector>
@@ -323,6 +324,13 @@ size_t assign_centers_ws_bytes(int64_t n, const km_centers *h) { return resident
 int centers_d(const km_centers *h) { return h->d; }
 int centers_device(const km_centers *h) { return h->device; }
 int device_error_status(uint32_t e) { return check_device_errors(e); }
+
+// Test hook: bits that the next km_update / km_update_noalloc call adds to
+// the error word it reads back from the device, as if a kernel had set them.
+// It lets the tests check how each bit maps to a status without making a
+// device-side wait run out.
+static std::atomic<uint32_t> g_fake_device_error{0};
+uint32_t take_fake_device_error() { return g_fake_device_error.exchange(0u); }
 }  // namespace km
 
 extern "C" {
@@ -344,6 +352,11 @@ const char *km_status_string(int status) {
 }
 
 const char *km_last_error(void) { return g_last_error; }
+
+int km_debug_fake_device_error(uint32_t bits) {
+    g_fake_device_error.store(bits);
+    return KM_OK;
+}
 
 int km_profile_enable(int on) {
     std::lock_guard<std::mutex> lk(g_prof.m);
@@ -459,7 +472,7 @@ int km_update(const float *X, int64_t n, int32_t d, const int32_t *labels, int32
     uint32_t e = 0;
     KM_CUDA(cudaMemcpyAsync(&e, err, sizeof(e), cudaMemcpyDeviceToHost, s));
     KM_CUDA(cudaStreamSynchronize(s));
-    return check_device_errors(e);
+    return check_device_errors(e | take_fake_device_error());
 }
 
 size_t km_kmpp_workspace_size(int64_t n, int32_t d, int32_t k) {

@@ -184,5 +184,7 @@ size_t assign_centers_ws_bytes(int64_t n, const km_centers *h);
 int centers_d(const km_centers *h);
 int centers_device(const km_centers *h);
 int device_error_status(uint32_t e);
+// Bits set by km_debug_fake_device_error, cleared as they are taken.
+uint32_t take_fake_device_error();
 
 }  // namespace km

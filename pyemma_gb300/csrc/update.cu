@@ -858,20 +858,24 @@ static __device__ __align__(256) unsigned char g_update_scratch[kNoAllocScratchB
 constexpr int kMaxDevices = 64;
 std::mutex g_scratch_mutex;
 void *g_scratch_ptr[kMaxDevices] = {};
-// Held by km_update_noalloc from its first launch until its stream has
-// drained: the calls share the scratch array, so they run one at a time.
-std::mutex g_noalloc_call_mutex;
+// One lock per device, held by km_update_noalloc from its first launch until
+// its stream has drained: calls on one device share that device's copy of
+// the scratch array, so they run one at a time; calls on different devices
+// use different copies and do not wait for each other.
+std::mutex g_noalloc_call_mutex[kMaxDevices];
 
 // Device address of g_update_scratch on the current device.  In host code the
 // array's name is only a stand-in, so the address is looked up once per
-// device (with that device current) and cached.
-int scratch_address(void **out) {
+// device (with that device current) and cached.  *dev_out receives the
+// device ordinal.
+int scratch_address(void **out, int *dev_out) {
     int dev = 0;
     KM_CUDA(cudaGetDevice(&dev));
     if (dev < 0 || dev >= kMaxDevices) {
         set_error("device ordinal %d is beyond the %d devices this library tracks", dev, kMaxDevices);
         return KM_ERR_UNSUPPORTED;
     }
+    *dev_out = dev;
     std::lock_guard<std::mutex> lk(g_scratch_mutex);
     if (!g_scratch_ptr[dev]) {
         void *p = nullptr;
@@ -905,18 +909,29 @@ extern "C" int km_update_noalloc(const float *X, int64_t n, int32_t d, const int
     const size_t need = update_ws_size(n, d, k) + 256;
     if (need > kNoAllocScratchBytes) {
         set_error("km_update_noalloc needs %zu bytes of scratch for n=%lld, d=%d, k=%d; its fixed array "
-                  "holds %zu (about 4 n + 8 k d + 28 k bytes must fit); use km_update with a workspace",
+                  "holds %zu (8 n + 8 k d + 32 k bytes plus about 2.5 KB of alignment must fit; "
+                  "km_update_workspace_size gives the exact figure); use km_update with a workspace",
                   need, (long long)n, d, k, kNoAllocScratchBytes);
         return KM_ERR_WORKSPACE;
     }
-    void *scratch = nullptr;
-    KM_TRY(scratch_address(&scratch));
     cudaStream_t s = static_cast<cudaStream_t>(stream);
+    // Every call reads the device error word back and synchronises `stream`,
+    // which a stream capture does not allow: refuse before enqueuing anything.
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    cudaError_t ce = cudaStreamIsCapturing(s, &cap);
+    if (ce != cudaSuccess) return cuda_fail(ce, "cudaStreamIsCapturing");
+    if (cap != cudaStreamCaptureStatusNone) {
+        set_error("km_update_noalloc cannot run on a stream that is being captured (it synchronises the stream)");
+        return KM_ERR_UNSUPPORTED;
+    }
+    void *scratch = nullptr;
+    int dev = 0;
+    KM_TRY(scratch_address(&scratch, &dev));
     uint32_t *err = reinterpret_cast<uint32_t *>(static_cast<char *>(scratch) + update_ws_size(n, d, k));
-    std::lock_guard<std::mutex> call_lock(g_noalloc_call_mutex);
+    std::lock_guard<std::mutex> call_lock(g_noalloc_call_mutex[dev]);
     // The array keeps the previous call's contents: the error word is cleared
     // here, and launch_update clears its own counters and sums.
-    cudaError_t ce = cudaMemsetAsync(err, 0, sizeof(uint32_t), s);
+    ce = cudaMemsetAsync(err, 0, sizeof(uint32_t), s);
     if (ce != cudaSuccess) return cuda_fail(ce, "cudaMemsetAsync(error word)");
     int rc = launch_update(X, n, d, labels, k, C_old, C_new, counts, cost, err, scratch, s);
     uint32_t e = 0;
@@ -928,9 +943,7 @@ extern "C" int km_update_noalloc(const float *X, int64_t n, int32_t d, const int
     ce = cudaStreamSynchronize(s);
     if (rc != KM_OK) return rc;
     if (ce != cudaSuccess) return cuda_fail(ce, "cudaStreamSynchronize");
-    if (e & kDevBadLabel) {
-        set_error("a label is outside [0, k)");
-        return KM_ERR_BAD_LABEL;
-    }
-    return KM_OK;
+    // Every bit of the error word maps to a status, as in km_update: a label
+    // out of range, or a device-side wait of the segment sums that ran out.
+    return device_error_status(e | take_fake_device_error());
 }

@@ -64,7 +64,8 @@ def test_noalloc_rejects_oversized_shapes_and_bad_labels():
     lib = L.load()
     limit = lib.km_update_noalloc_max_bytes()
     assert limit == 32 << 20
-    # 20 M frames need 80 MB of sorted indices: beyond the fixed array.
+    # 20 M frames need 160 MB (two int32 arrays of n: the sorted indices and
+    # their labels): beyond the fixed array.
     dummy = ctypes.c_void_p(256)
     rc = lib.km_update_noalloc(dummy, 20_000_000, 4, dummy, 8, dummy, ctypes.c_void_p(512), None,
                                ctypes.c_void_p(768), None)
@@ -114,3 +115,55 @@ def test_noalloc_concurrent_threads_and_streams():
         t.join(timeout=120)
     assert not any(t.is_alive() for t in threads)
     assert not failures, failures
+
+
+def test_noalloc_maps_every_device_error_bit_like_km_update():
+    # The error word of a call carries a bit per failure site.  A wait of the
+    # segment sums that ran out (bit 1) must come back as KM_ERR_TIMEOUT, as
+    # from km_update, not as KM_OK with stale outputs.  The bit is planted by
+    # the library's test hook on the host side; no device wait is made to
+    # run out.
+    import torch
+    from pyemma_gb300 import _lib as L
+    lib = L.load()
+    X, labels, C = _case(torch, 7, 2000, 8, 12)
+    for bits, want in ((1, L.KM_ERR_TIMEOUT), (2, L.KM_ERR_TIMEOUT), (4, L.KM_ERR_TIMEOUT),
+                       (8, L.KM_ERR_BAD_LABEL)):
+        assert lib.km_debug_fake_device_error(bits) == L.KM_OK
+        rc, _, _, _ = _call_noalloc(L, torch, X, labels, C)
+        assert rc == want, (bits, rc, lib.km_last_error())
+        assert lib.km_debug_fake_device_error(bits) == L.KM_OK
+        with pytest.raises(L.KmError) as ei:
+            L.update(X, labels, C)
+        assert ei.value.status == want
+    rc, _, _, _ = _call_noalloc(L, torch, X, labels, C)  # the planted bits are used up
+    assert rc == L.KM_OK
+
+
+def test_noalloc_refuses_a_capturing_stream():
+    # Each call reads its error word back and synchronises its stream, which
+    # a stream capture cannot hold: the call refuses before enqueuing work,
+    # and the capture stays valid.
+    import torch
+    from pyemma_gb300 import _lib as L
+    lib = L.load()
+    X, labels, C = _case(torch, 8, 1000, 4, 6)
+    C_new = torch.empty_like(C)
+    cost = torch.empty(1, dtype=torch.float64, device="cuda")
+    s = torch.cuda.Stream()
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(s):
+        g.capture_begin()
+        try:
+            rc = lib.km_update_noalloc(ctypes.c_void_p(X.data_ptr()), X.shape[0], X.shape[1],
+                                       ctypes.c_void_p(labels.data_ptr()), C.shape[0], ctypes.c_void_p(C.data_ptr()),
+                                       ctypes.c_void_p(C_new.data_ptr()), None, ctypes.c_void_p(cost.data_ptr()),
+                                       ctypes.c_void_p(s.cuda_stream))
+            C_new.add_(1.0)  # the capture still records work
+        finally:
+            g.capture_end()
+    assert rc == L.KM_ERR_UNSUPPORTED
+    assert b"captured" in lib.km_last_error()
+    rc, C_na, _, _ = _call_noalloc(L, torch, X, labels, C)
+    assert rc == L.KM_OK
