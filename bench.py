@@ -12,8 +12,14 @@ near ties (labels equal the plain FP32 kernel's bit for bit).  A "step" is one L
   e2e         the same metric through the public API (KmeansClustering.estimate
               with max_iter=1) from pinned host frames, copies inside the clock
   roofline    the tensor-core distance kernel: 2*N*k*d flops per launch over its
-              CUDA-event launch time, against the measured sustained BF16 peak
-              (FP16 and BF16 share the kind::f16 tensor rate)
+              CUDA-event launch time, against the measured BF16 peak (FP16 and
+              BF16 share the kind::f16 tensor rate): the burst peak for a timed
+              region under 2 s, the sustained one beyond; frac_issued counts
+              the padded MMA work the kernel issues
+  centers_rel_err_vs_fp64 / inertia_rel_err_vs_fp64
+              one more Lloyd iteration against the float64 NumPy reference
+              (member means and inertia of the GPU's labels, all frames)
+  kmeans++    km_kmpp with k=2000 on all frames, timed with CUDA events
   plain_fp32  the same Lloyd iteration with the exact FP32 CUDA-core kernel
   cpu_baseline  the CPU oracle (C/OpenMP restatement of the reference path) on
               a bounded sample, all host cores
@@ -63,6 +69,7 @@ def parse_args():
     p.add_argument("--no-fp32", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-fp64", action="store_true", help="skip the float64 reference check of the centers")
     p.add_argument("--config", default="c3", choices=["c1", "c2", "c3", "c4", "c5", "minrmsd"])
     p.add_argument("--serve-seconds", type=float, default=10.0)
     return p.parse_args()
@@ -166,6 +173,62 @@ def profiled_traffic():
     except OSError:
         pass
     return None
+
+
+# Timed regions at least this long are compared with the sustained (power-
+# capped) bf16 peak; shorter ones with the burst peak.
+SUSTAINED_AFTER_MS = 2000.0
+
+
+def padded_mma_flops(n, k, d):
+    """MMA work the tensor-core kernel issues per launch: frames padded to the
+    256-row CTA-pair tile, centers to the 256-row B tile, and K to 64-column
+    chunks holding d features plus the two norm columns."""
+    n_pad = -(-n // 256) * 256
+    k_pad = -(-k // 256) * 256
+    kp = 64 * (-(-(d + 2) // 64))
+    return 2.0 * n_pad * k_pad * kp
+
+
+def tc_roofline(n, tc_ms, tc_n, timed_ms, k=K, d=D):
+    """Roofline record of the tensor-core distance kernel: 2 n k d flops per
+    launch over its mean CUDA-event launch time, against the measured bf16
+    peak (FP16 and BF16 share the kind::f16 rate).  The burst peak applies
+    unless the timed region ran long enough to settle under the power cap."""
+    peaks, peak_kind = measured_peaks()
+    flops = 2.0 * n * k * d
+    issued = padded_mma_flops(n, k, d)
+    t = tc_ms / tc_n / 1e3 if tc_n else None
+    achieved = flops / t / 1e12 if t else None
+    if timed_ms >= SUSTAINED_AFTER_MS:
+        key, rule = "bf16_tflops_sustained", "timed region %.0f ms >= %.0f ms: sustained" % (timed_ms,
+                                                                                             SUSTAINED_AFTER_MS)
+    else:
+        key, rule = "bf16_tflops", "timed region %.0f ms < %.0f ms: burst" % (timed_ms, SUSTAINED_AFTER_MS)
+    peak = float(peaks.get(key, 1900.0 if key == "bf16_tflops" else 1700.0))
+    return {"bound": "tensor", "kernel": "tc_assign_kernel", "achieved": achieved, "peak": peak,
+            "unit": "TFLOP/s", "frac": achieved / peak if achieved else None, "traffic": profiled_traffic(),
+            "peak_source": "%s %s of MEASURED_PEAKS.json (%s)" % (peak_kind, key, rule),
+            "issued_tflops": issued / t / 1e12 if t else None,
+            "frac_issued": issued / t / 1e12 / peak if t else None,
+            "issued_flops_per_launch": issued,
+            "launches": tc_n, "ms_per_launch": t * 1e3 if t else None, "flops_per_launch": flops}
+
+
+def fp64_reference_check(X_host, labels, C_prev, C_new, inertia):
+    """Centers and inertia of one GPU Lloyd iteration against the float64
+    NumPy member means and inertia of the same labels (the oracle's
+    centers_fp64 / inertia_fp64)."""
+    from oracle import oracle
+    mu, cnt = oracle.centers_fp64(X_host, labels, C_prev)
+    ref_inertia = oracle.inertia_fp64(X_host, labels, mu)
+    got = np.asarray(C_new, dtype=np.float64)
+    rel = np.abs(got - mu) / np.maximum(np.abs(mu), 1e-30)
+    return {"centers_rel_err_vs_fp64": float(rel.max()),
+            "inertia_rel_err_vs_fp64": abs(inertia - ref_inertia) / ref_inertia,
+            "fp64_reference": "oracle.centers_fp64 / inertia_fp64 on the GPU's labels of one Lloyd iteration "
+                              "(all %d frames)" % len(labels),
+            "empty_clusters": int((cnt == 0).sum())}
 
 
 # ---------------------------------------------------------------------------
@@ -311,17 +374,9 @@ def run_ours(args):
         sampler = None
 
     # ---- roofline of the tensor-core distance kernel ----
-    peaks, peak_kind = measured_peaks()
     tc_ms, tc_n = prof["tc"]
-    flops = 2.0 * n * K * D
-    achieved = flops / (tc_ms / tc_n / 1e3) / 1e12 if tc_n else None
-    peak = float(peaks.get("bf16_tflops_sustained", 1700.0))
-    roofline = {"bound": "tensor", "kernel": "tc_assign_kernel", "achieved": achieved, "peak": peak,
-                "unit": "TFLOP/s", "frac": achieved / peak if achieved else None, "traffic": profiled_traffic(),
-                "peak_source": "%s bf16_tflops_sustained (same kind::f16 rate as fp16)" % peak_kind,
-                "launches": tc_n, "ms_per_launch": tc_ms / tc_n if tc_n else None,
-                "flops_per_launch": flops,
-                "step_breakdown_ms": {k: (v[0] / v[1] if v[1] else None) for k, v in prof.items()}}
+    roofline = tc_roofline(n, tc_ms, tc_n, ms)
+    roofline["step_breakdown_ms"] = {k: (v[0] / v[1] if v[1] else None) for k, v in prof.items()}
 
     extra = {}
     if rank == 0:
@@ -348,6 +403,22 @@ def run_ours(args):
             extra["plain_fp32"] = {"value": fp32_value, "unit": UNIT, "steps": steps32}
             extra["mixed_vs_plain_fp32"] = (value / world) / fp32_value
         del lab16
+        # kmeans++ (k rounds of D^2 sampling) on the same frames
+        _lib.kmpp(X[:65536].contiguous(), 8, 42)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        _, kidx = _lib.kmpp(X, K, 42)
+        e1.record()
+        torch.cuda.synchronize()
+        kmpp_ms = e0.elapsed_time(e1)
+        unpruned = float(K) * n * (4 * D + 8)
+        extra["kmeans++"] = {"ms": kmpp_ms, "rounds": K, "ms_per_round": kmpp_ms / K,
+                             "unpruned_bytes": unpruned,
+                             "unpruned_bytes_per_s": unpruned / (kmpp_ms / 1e3),
+                             "note": "km_kmpp, k=%d on all %d frames (seed 42); unpruned_bytes = k N (4d + 8), "
+                                     "the bytes a pass without distance bounds would read" % (K, n)}
+        del kidx
 
     # ---- e2e through the public API from pinned host frames ----
     e2e = None
@@ -356,6 +427,14 @@ def run_ours(args):
         Xh.copy_(X)
         Xh_np = Xh.numpy()
         C0h = C0.cpu().numpy()
+        if not args.no_fp64:
+            # centers and inertia of one more iteration (from the timed run's
+            # centers) against the float64 reference on the same labels
+            C_prev = C.clone()
+            r1 = _lib.lloyd(X, C, 1, -1.0, precision="fp16")
+            extra.update(fp64_reference_check(Xh_np, r1["labels"].cpu().numpy(), C_prev.cpu().numpy(),
+                                              C.cpu().numpy(), float(r1["inertias"][0])))
+            del r1, C_prev
         # the bare pinned host-to-device rate of this machine, for reading e2e
         ec0, ec1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         X.copy_(Xh, non_blocking=True)
@@ -544,7 +623,8 @@ def run_c2(args):
     peak = _fp32_sgemm_tflops(torch)
     achieved = flops / (fp32_ms / 1e3) / 1e12
     tc_ms = prof["tc"][0] / max(1, prof["tc"][1]) if prof["tc"][1] else None
-    tpeak = float(measured_peaks()[0].get("bf16_tflops_sustained", 1700.0))
+    tpeak = float(measured_peaks()[0].get("bf16_tflops" if ms * args.steps < SUSTAINED_AFTER_MS
+                                          else "bf16_tflops_sustained", 1900.0))
     # e2e: the public estimator on the 20 host trajectories (pinned), one iteration
     pinned = []
     for t in trajs:

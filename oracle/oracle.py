@@ -282,25 +282,61 @@ def pair_distances(xyz, pairs):
 # ---------------------------------------------------------------------------
 # float64 NumPy reference (independent of the C code)
 # ---------------------------------------------------------------------------
-def centers_fp64(X, labels, C_old):
-    """Member means in float64; empty clusters keep their previous center."""
-    X = np.asarray(X, dtype=np.float64)
+_CHUNK_FP64 = 1 << 16
+
+
+def _chunks_fp64(n, fn, n_threads=None):
+    """fn(a, b) over the row chunks [a, b) of n rows on a thread pool (NumPy
+    releases the interpreter lock inside its array loops); returns the
+    results in chunk order."""
+    from concurrent.futures import ThreadPoolExecutor
+    bounds = [(a, min(n, a + _CHUNK_FP64)) for a in range(0, n, _CHUNK_FP64)]
+    workers = max(1, min(len(bounds), n_threads or default_threads()))
+    if workers == 1:
+        return [fn(a, b) for a, b in bounds]
+    with ThreadPoolExecutor(max_workers=workers) as ex:
+        return list(ex.map(lambda ab: fn(*ab), bounds))
+
+
+def centers_fp64(X, labels, C_old, n_threads=None):
+    """Member means in float64; empty clusters keep their previous center.
+
+    Works through X in chunks of 65,536 rows (each converted to float64 on
+    its own), so that a 2,000,000 x 528 float32 X needs no float64 copy of
+    the whole array.  Within a chunk the rows are summed cluster by cluster
+    in frame order (np.add.reduceat over the rows sorted by label); the
+    chunk sums are added in chunk order."""
+    labels = np.asarray(labels).astype(np.int64, copy=False)
     k, d = C_old.shape
+    cnt = np.bincount(labels, minlength=k).astype(np.float64)[:k]
+
+    def part(a, b):
+        lab = labels[a:b]
+        order = np.argsort(lab, kind="stable")
+        ls = lab[order]
+        starts = np.flatnonzero(np.r_[True, ls[1:] != ls[:-1]])
+        return ls[starts], np.add.reduceat(np.asarray(X[a:b], dtype=np.float64)[order], starts, axis=0)
+
     S = np.zeros((k, d))
-    np.add.at(S, labels, X)
-    cnt = np.bincount(labels, minlength=k).astype(np.float64)
+    for rows, sums in _chunks_fp64(len(labels), part, n_threads):
+        S[rows] += sums
     out = np.asarray(C_old, dtype=np.float64).copy()
     nz = cnt > 0
     out[nz] = S[nz] / cnt[nz, None]
     return out, cnt
 
 
-def inertia_fp64(X, labels, C):
-    """sum_i ||x_i - c_{label_i}||^2 in float64."""
-    X = np.asarray(X, dtype=np.float64)
+def inertia_fp64(X, labels, C, n_threads=None):
+    """sum_i ||x_i - c_{label_i}||^2 in float64 (chunks of 65,536 rows, added
+    in chunk order)."""
+    labels = np.asarray(labels).astype(np.int64, copy=False)
     C = np.asarray(C, dtype=np.float64)
-    diff = X - C[labels]
-    return float(np.einsum("ij,ij->", diff, diff))
+
+    def part(a, b):
+        diff = np.asarray(X[a:b], dtype=np.float64) - C[labels[a:b]]
+        return float(np.einsum("ij,ij->", diff, diff))
+
+    return float(sum(_chunks_fp64(len(labels), part, n_threads)))
 
 
 def sqdist_fp32_sequential(X, C):

@@ -301,21 +301,6 @@ def test_lloyd_zero_iterations(torch, L):
     assert float(C.abs().sum()) == 0.0
 
 
-def test_full_size_wide_fp16_equals_fp32(torch, L, oracle):
-    """2,000,000 x 528 Calpha distances, k=2000: tensor-core labels equal the exact kernel's."""
-    from pyemma_gb300 import datasets
-    X = datasets.calpha_distances(2_000_000, seed=3, device="cuda")
-    rng = np.random.default_rng(3)
-    C = X[torch.from_numpy(rng.choice(X.shape[0], 2000, replace=False)).cuda()].contiguous()
-    lab32, _ = L.assign(X, C, precision="fp32")
-    lab16, stats = L.assign(X, C, precision="fp16")
-    assert torch.equal(lab32, lab16)
-    assert stats["n_recheck"] + stats["n_full"] < X.shape[0]
-    sample = rng.choice(X.shape[0], 2000, replace=False)
-    Xs = X[torch.from_numpy(sample).cuda()].cpu().numpy()
-    np.testing.assert_array_equal(lab16.cpu().numpy()[sample], oracle.assign(Xs, C.cpu().numpy()))
-
-
 def test_profile_counts_graph_replays(torch, L):
     rng = np.random.default_rng(21)
     X = dev(torch, rng.normal(size=(20000, 96)))
