@@ -182,12 +182,12 @@ SUSTAINED_AFTER_MS = 2000.0
 
 def padded_mma_flops(n, k, d):
     """MMA work the tensor-core kernel issues per launch: frames padded to the
-    256-row CTA-pair tile, centers to the 256-row B tile, and K to 64-column
-    chunks holding d features plus the two norm columns."""
+    256-row CTA-pair tile, centers to the 256-row B tile, and K to the 16-wide
+    MMA steps that hold the d features plus the two norm columns."""
     n_pad = -(-n // 256) * 256
     k_pad = -(-k // 256) * 256
-    kp = 64 * (-(-(d + 2) // 64))
-    return 2.0 * n_pad * k_pad * kp
+    k_steps = 16 * (-(-(d + 2) // 16))
+    return 2.0 * n_pad * k_pad * k_steps
 
 
 def tc_roofline(n, tc_ms, tc_n, timed_ms, k=K, d=D):

@@ -256,6 +256,31 @@ def test_kmpp_sparse_weights_many_tiles(torch, L, oracle):
     np.testing.assert_array_equal(idx.cpu().numpy(), idx_ref)
 
 
+@pytest.mark.parametrize("case", ["mixture", "lattice", "collinear"])
+def test_kmpp_pruned_pass_matches_oracle(torch, L, oracle, case):
+    # Data on which the bound ||c_new - c_a||^2 >= 4 D^2 skips most frames
+    # (well separated clusters), and data with exact boundary cases: integer
+    # lattice points and points on a line, where a new center often sits at
+    # exactly twice a frame's distance from its nearest center, and many
+    # distances tie.  The running minima and so the draws must stay the
+    # oracle's, which evaluates every frame in every round.
+    rng = np.random.default_rng(31)
+    if case == "mixture":
+        from pyemma_gb300 import datasets
+        X = datasets.gaussian_mixture(200000, 16, 50, 0.3, 5.0, seed=31)
+        k = 300
+    elif case == "lattice":
+        X = rng.integers(0, 8, size=(60000, 3)).astype(np.float32)
+        k = 120
+    else:
+        X = np.zeros((50000, 4), dtype=np.float32)
+        X[:, 0] = rng.integers(-64, 65, size=50000).astype(np.float32) * 0.5
+        k = 60
+    _, idx_ref = oracle.kmpp(X, k, 13)
+    _, idx = L.kmpp(dev(torch, X), k, 13)
+    np.testing.assert_array_equal(idx.cpu().numpy(), idx_ref)
+
+
 def test_kmpp_duplicates(torch, L, oracle):
     X = np.ones((100, 4), dtype=np.float32)
     X[50:] = 2.0
