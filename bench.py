@@ -461,7 +461,24 @@ def run_ours(args):
                "copy_bound_frames_per_s": link_gbs * 1e9 / (D * 4),
                "overlap": "frames copied in chunks on a side stream while the first iteration assigns "
                           "the chunks already copied (km_lloyd_host)"}
+        # The same call with the frames in an ordinary (pageable) numpy
+        # array, as PyEMMA callers hold them: the library stages the copy
+        # through page-locked buffers on worker threads.
+        Xpg = np.empty_like(Xh_np)
+        Xpg[...] = Xh_np
         del Xh, Xh_np
+        KmeansClustering(n_clusters=K, max_iter=1, tolerance=-1.0, clustercenters=C0h, precision="fp16").estimate(Xpg)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            km = KmeansClustering(n_clusters=K, max_iter=1, tolerance=-1.0, clustercenters=C0h, precision="fp16")
+            km.estimate(Xpg)
+            _ = km.clustercenters
+        dtp = (time.perf_counter() - t0) / e2e_steps
+        e2e["pageable"] = {"value": n / dtp, "unit": UNIT, "h2d_bytes_per_step": n * D * 4,
+                           "d2h_bytes_per_step": K * D * 4 + 8, "vs_pinned": (n / dtp) / e2e["value"],
+                           "api": "KmeansClustering(max_iter=1, clustercenters=C).estimate(pageable numpy X)"}
+        del Xpg
         # The same iteration from pinned host C-alpha coordinates: the
         # 528 distance features are computed on the device (featurize.ca_distances)
         # and clustered there, so 396 bytes per frame cross the host link.
@@ -882,12 +899,20 @@ def run_c5(args):
         if sel.any():
             per_d[str(dd)] = {"requests": int(sel.sum()), "p50_ms": float(np.percentile(lat[sel], 50)),
                               "p99_ms": float(np.percentile(lat[sel], 99))}
+    per_size = {}
+    for name, lo_, hi_ in (("<10k", 0, 10_000), ("10k-100k", 10_000, 100_000), (">=100k", 100_000, 1 << 62)):
+        sel = (lengths >= lo_) & (lengths < hi_)
+        if sel.any():
+            per_size[name] = {"requests": int(sel.sum()), "p50_ms": float(np.percentile(lat[sel], 50)),
+                              "p99_ms": float(np.percentile(lat[sel], 99)),
+                              "queue_p99_ms": float(np.percentile(qlat[sel], 99))}
     _emit({"metric": "serving frames/s with p50/p99 request latency", "value": total / t_end, "unit": "frames/s",
            "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
            "max_ms": float(lat.max()), "queue_p99_ms": float(np.percentile(qlat, 99)), "n_gpus": 1,
            "requests": m, "frames": total, "offered_frames_per_s": total / dur,
            "offered_tflops": flops / dur / 1e12, "wall_s": t_end, "server": st,
            "labels_same_alone_and_mixed": same, "checked_requests": checked, "per_d": per_d,
+           "per_request_frames": per_size,
            "config": {"workload": "c5: Poisson arrivals at %.0f req/s for %.0f s, lengths log-uniform [1k, 1M], "
                                   "8 resident center sets (d, k) = %s, 40 GB admission budget, pinned host "
                                   "buffers, copies included" % (rate, dur, specs)}})

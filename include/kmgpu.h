@@ -307,12 +307,16 @@ int km_assign_centers(const float *X, int64_t n, int32_t d, const km_centers *ce
 /* ---- serving loop (no counterpart in the reference) ------------------------
  * A native worker thread assigns trajectories submitted from any host
  * thread against resident center sets.  Requests for the same center set
- * are packed into one batch (continuous batching, FIFO by the oldest
- * request); a request longer than a batch is split across batches.  Two
- * batch slots alternate so that the copies of one batch overlap the
- * kernels of the other.  The slots (frames, labels, assignment workspace)
- * are the device memory held for requests in flight; their total stays
- * within hbm_budget_bytes, which sets the batch size.
+ * are packed into one batch (continuous batching); the batch is led by the
+ * queued request with the fewest frames left, or by the oldest request once
+ * it has waited 25 ms, and filled with the other requests of the leader's
+ * set, fewest frames left first.  A request longer than a batch is split
+ * across batches.  A batch holds at most 64 MiB of frames (or
+ * max_batch_frames frames), so short requests do not queue behind the copy
+ * of a long one.  Three batch slots rotate so that the copies of one batch
+ * overlap the kernels of the others.  The slots (frames, labels, assignment
+ * workspace) are the device memory held for requests in flight; their total
+ * stays within hbm_budget_bytes.
  *   km_serve_submit: X_host (host, n*d float32) and labels_host (host, n
  *     int32) must stay valid until the request completes; page-locked
  *     buffers let the copies run asynchronously.  d must match the set.

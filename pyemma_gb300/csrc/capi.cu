@@ -2,10 +2,14 @@
 // include/kmgpu.h).  Each one validates its arguments, carves the caller's
 // workspace and enqueues kernels on the caller's stream.
 #include <algorithm>
+#include <atomic>
+#include <condition_variable>
 #include <cstring>
 #include <map>
-#include <atomic>
+#include <memory>
 #include <mutex>
+#include <string>
+#include <thread>
 #include <utility>
 #include <vector>
 
@@ -516,6 +520,201 @@ int64_t stream_chunk_rows(int64_t n) {
     return (c + 255) / 256 * 256;
 }
 
+// ---------------------------------------------------------------------------
+// Staged copies of pageable host frames.  A cudaMemcpyAsync from pageable
+// memory is staged by the driver and returns only when the copy is done, so
+// the host could not enqueue the first iteration's kernels until every frame
+// had crossed the link.  Here worker threads copy blocks of at most
+// kStageBytes from the caller's arrays into page-locked buffers (two per
+// worker) and issue each block's host-to-device copy on the worker's own
+// stream, with an event per block; the enqueue of a chunk's kernels waits on
+// the host until the chunk's blocks are issued, then on their events on the
+// device.  The page-locked ring is allocated once per process and kept.
+// ---------------------------------------------------------------------------
+constexpr size_t kStageBytes = size_t(16) << 20;
+
+struct StagePool {
+    std::mutex use;  // held by the call that stages (one at a time)
+    std::vector<void *> bufs;
+    int device = -1;
+};
+StagePool &stage_pool() {
+    static StagePool *p = new StagePool();  // kept until exit: buffers may be in use at static destruction
+    return *p;
+}
+
+int stage_workers() {
+    const unsigned hw = std::thread::hardware_concurrency();
+    int w = hw ? (int)hw / 2 : 4;
+    return std::max(2, std::min(8, w));
+}
+
+// True when some part of the host frames is ordinary pageable memory.
+bool has_pageable_part(const float *const *parts, const int64_t *rows, int32_t n_parts) {
+    for (int32_t q = 0; q < n_parts; ++q) {
+        if (rows[q] <= 0) continue;
+        cudaPointerAttributes a{};
+        if (cudaPointerGetAttributes(&a, parts[q]) != cudaSuccess) {
+            cudaGetLastError();
+            return true;
+        }
+        if (a.type == cudaMemoryTypeUnregistered) return true;
+    }
+    return false;
+}
+
+struct Stager {
+    struct Block {
+        int64_t row0, rows;
+        cudaEvent_t ev = nullptr;
+    };
+    const float *const *parts = nullptr;
+    const int64_t *part_rows = nullptr;
+    int32_t n_parts = 0;
+    float *X = nullptr;
+    int d = 0;
+    int device = 0;
+    std::vector<Block> blocks;
+    std::vector<size_t> chunk_first;  // first block of each chunk (plus blocks.size())
+    std::vector<cudaStream_t> streams;
+    std::vector<std::thread> threads;
+    std::unique_lock<std::mutex> pool_lock;
+    std::mutex m;
+    std::condition_variable cv;
+    std::vector<char> issued;  // per block: its copy is enqueued
+    int failed = KM_OK;
+    std::string fail_msg;
+
+    // Copies rows [row0, row0 + rows) of the concatenated parts to dst.
+    void gather(float *dst, int64_t row0, int64_t rows) const {
+        int64_t base = 0;
+        for (int32_t q = 0; q < n_parts && rows > 0; ++q) {
+            const int64_t r = part_rows[q];
+            if (row0 < base + r) {
+                const int64_t off = row0 - base, take = std::min(rows, r - off);
+                std::memcpy(dst, parts[q] + off * d, sizeof(float) * (size_t)take * d);
+                dst += take * d;
+                row0 += take;
+                rows -= take;
+            }
+            base += r;
+        }
+    }
+
+    void worker(int w, int nw, void *buf0, void *buf1) {
+        cudaSetDevice(device);
+        cudaEvent_t slot_free[2] = {nullptr, nullptr};
+        void *buf[2] = {buf0, buf1};
+        int use = 0;
+        for (size_t b = (size_t)w; b < blocks.size(); b += (size_t)nw, use ^= 1) {
+            cudaError_t e = cudaSuccess;
+            if (slot_free[use]) e = cudaEventSynchronize(slot_free[use]);  // the slot's last copy is done
+            if (e == cudaSuccess) {
+                gather(static_cast<float *>(buf[use]), blocks[b].row0, blocks[b].rows);
+                e = cudaMemcpyAsync(X + blocks[b].row0 * d, buf[use], sizeof(float) * (size_t)blocks[b].rows * d,
+                                    cudaMemcpyHostToDevice, streams[w]);
+            }
+            if (e == cudaSuccess) e = cudaEventRecord(blocks[b].ev, streams[w]);
+            if (e == cudaSuccess) {
+                if (!slot_free[use]) e = cudaEventCreateWithFlags(&slot_free[use], cudaEventDisableTiming);
+                if (e == cudaSuccess) e = cudaEventRecord(slot_free[use], streams[w]);
+            }
+            std::lock_guard<std::mutex> lk(m);
+            if (e != cudaSuccess && failed == KM_OK) {
+                failed = KM_ERR_CUDA;
+                fail_msg = std::string("staged host-to-device copy: ") + cudaGetErrorString(e);
+            }
+            issued[b] = 1;  // also after a failure, so that nobody waits for it forever
+            cv.notify_all();
+        }
+        for (cudaEvent_t ev : slot_free)
+            if (ev) {
+                cudaEventSynchronize(ev);
+                cudaEventDestroy(ev);
+            }
+    }
+
+    // Splits [0, n) into blocks that never cross a chunk boundary and starts
+    // the workers.
+    int start(const std::vector<int64_t> &chunk_begin) {
+        const int64_t block_rows = std::max<int64_t>(1, (int64_t)(kStageBytes / (sizeof(float) * (size_t)d)));
+        for (size_t c = 0; c + 1 < chunk_begin.size(); ++c) {
+            chunk_first.push_back(blocks.size());
+            for (int64_t a = chunk_begin[c]; a < chunk_begin[c + 1]; a += block_rows)
+                blocks.push_back(Block{a, std::min(block_rows, chunk_begin[c + 1] - a)});
+        }
+        chunk_first.push_back(blocks.size());
+        issued.assign(blocks.size(), 0);
+        for (Block &b : blocks) KM_CUDA(cudaEventCreateWithFlags(&b.ev, cudaEventDisableTiming));
+        const int nw = std::min<int>(stage_workers(), (int)std::max<size_t>(1, blocks.size()));
+        StagePool &pool = stage_pool();
+        pool_lock = std::unique_lock<std::mutex>(pool.use);
+        if (pool.device != device) {
+            for (void *p : pool.bufs) cudaFreeHost(p);
+            pool.bufs.clear();
+            pool.device = device;
+        }
+        while ((int)pool.bufs.size() < 2 * nw) {
+            void *p = nullptr;
+            KM_CUDA(cudaHostAlloc(&p, kStageBytes, cudaHostAllocPortable));
+            pool.bufs.push_back(p);
+        }
+        streams.assign(nw, nullptr);
+        for (cudaStream_t &st : streams) KM_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        for (int w = 0; w < nw; ++w)
+            threads.emplace_back(&Stager::worker, this, w, nw, pool.bufs[2 * w], pool.bufs[2 * w + 1]);
+        return KM_OK;
+    }
+
+    // Makes st wait for the copies of chunk c (host wait until they are
+    // issued, then a device wait on each block's event).
+    int wait_chunk(cudaStream_t st, size_t c) {
+        {
+            std::unique_lock<std::mutex> lk(m);
+            cv.wait(lk, [&] {
+                for (size_t b = chunk_first[c]; b < chunk_first[c + 1]; ++b)
+                    if (!issued[b]) return false;
+                return true;
+            });
+            if (failed != KM_OK) {
+                set_error("%s", fail_msg.c_str());
+                return failed;
+            }
+        }
+        for (size_t b = chunk_first[c]; b < chunk_first[c + 1]; ++b) KM_CUDA(cudaStreamWaitEvent(st, blocks[b].ev, 0));
+        return KM_OK;
+    }
+
+    // Joins the workers and waits for every copy (the page-locked ring is
+    // free for the next call, the caller's arrays are no longer read).
+    int finish() {
+        for (std::thread &t : threads)
+            if (t.joinable()) t.join();
+        threads.clear();
+        int st = KM_OK;
+        for (cudaStream_t &s : streams) {
+            if (s) {
+                cudaError_t e = cudaStreamSynchronize(s);
+                if (e != cudaSuccess && st == KM_OK) st = cuda_fail(e, "staged copies");
+                cudaStreamDestroy(s);
+                s = nullptr;
+            }
+        }
+        if (pool_lock.owns_lock()) pool_lock.unlock();
+        if (st == KM_OK && failed != KM_OK) {
+            set_error("%s", fail_msg.c_str());
+            st = failed;
+        }
+        return st;
+    }
+
+    ~Stager() {
+        finish();
+        for (Block &b : blocks)
+            if (b.ev) cudaEventDestroy(b.ev);
+    }
+};
+
 int lloyd_run(const float *X_in, const HostFrames *hf, int64_t n, int32_t d, int32_t k, float *C, int32_t max_iter,
               double tolerance, int32_t precision, int32_t *labels, double *inertias, int32_t *n_iter,
               int32_t *converged, km_callback cb, void *cb_user, void *workspace, size_t workspace_bytes,
@@ -549,6 +748,7 @@ int lloyd_run(const float *X_in, const HostFrames *hf, int64_t n, int32_t d, int
             if (cs) cudaStreamDestroy(cs);
         }
     } sm;
+    std::unique_ptr<Stager> stager;  // pageable host frames: staged copies
     if (hf) {
         int64_t total = 0;
         for (int32_t q = 0; q < hf->n_parts; ++q) {
@@ -565,6 +765,22 @@ int lloyd_run(const float *X_in, const HostFrames *hf, int64_t n, int32_t d, int
         const int64_t chunk = stream_chunk_rows(n);
         for (int64_t a = 0; a < n; a += chunk) sm.begin.push_back(a);
         sm.begin.push_back(n);
+        if (has_pageable_part(hf->parts, hf->rows, hf->n_parts)) {
+            // Workers stage the pageable frames; X must not be in use on s
+            // any more (the caller's stream is drained first).
+            KM_CUDA(cudaStreamSynchronize(s));
+            stager.reset(new Stager());
+            stager->parts = hf->parts;
+            stager->part_rows = hf->rows;
+            stager->n_parts = hf->n_parts;
+            stager->X = X;
+            stager->d = d;
+            KM_CUDA(cudaGetDevice(&stager->device));
+            KM_TRY(stager->start(sm.begin));
+            if (max_iter == 0) return stager->finish();
+        }
+    }
+    if (hf && !stager) {
         KM_CUDA(cudaStreamCreateWithFlags(&sm.cs, cudaStreamNonBlocking));
         sm.ev.assign(sm.begin.size(), nullptr);  // [0]: the caller's stream reached this call
         for (cudaEvent_t &e : sm.ev) KM_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
@@ -689,7 +905,10 @@ int lloyd_run(const float *X_in, const HostFrames *hf, int64_t n, int32_t d, int
         KM_TRY(launch_update_parts_begin(n, d, k, ws_update, st));
         for (size_t c = 0; c + 1 < sm.begin.size(); ++c) {
             const int64_t a = sm.begin[c], rows = sm.begin[c + 1] - a;
-            KM_CUDA(cudaStreamWaitEvent(st, sm.ev[c + 1], 0));
+            if (stager)
+                KM_TRY(stager->wait_chunk(st, c));
+            else
+                KM_CUDA(cudaStreamWaitEvent(st, sm.ev[c + 1], 0));
             if (is_tc(prec)) {
                 TcBuffers v = tc_rows_from(b, a);
                 v.keep_err = 1;
@@ -850,7 +1069,10 @@ int lloyd_run(const float *X_in, const HostFrames *hf, int64_t n, int32_t d, int
         }
     }
     if (exec) cudaGraphExecDestroy(exec);
-    if (hf && status != KM_OK) {
+    if (stager) {
+        const int st2 = stager->finish();
+        if (status == KM_OK) status = st2;
+    } else if (hf && status != KM_OK) {
         // The copies may still be running into X: wait for them before
         // returning the caller's buffer.
         cudaStreamSynchronize(sm.cs);

@@ -1,14 +1,18 @@
 // serve.cu -- the serving loop of libkmgpu (km_serve_* in include/kmgpu.h).
 //
 // One native worker thread per server.  Submitted trajectories wait in a
-// FIFO queue; the worker packs the frames of every queued request that
-// shares the oldest request's center set into one batch (a request longer
-// than the batch continues in the next one), copies them into a device
-// batch slot, runs the assignment against the resident center set and
-// copies the labels back.  Two slots on two streams alternate, so the
-// copies of one batch overlap the kernels of the other.  The slots are the
-// only device memory the server holds; their size is the largest batch that
-// fits twice into the admission budget.
+// queue; for every batch the worker picks a leading request -- the one with
+// the fewest frames left, or the oldest once it has waited kMaxWaitMs -- and
+// packs the queued requests of the leader's center set, fewest frames left
+// first, into the batch (a request longer than the batch continues in later
+// ones).  It copies them into a device batch slot, runs the assignment
+// against the resident center set and copies the labels back.  kSlots slots
+// on their own streams rotate, so the copies of one batch overlap the
+// kernels of the others.  A batch holds at most kBatchBytes of frames (about
+// 0.3 ms on a 200 GB/s host link), so a short request never queues behind
+// more than a few short batches, however long the requests ahead of it are.
+// The slots are the only device memory the server holds; together they stay
+// within the admission budget.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -29,6 +33,10 @@ namespace {
 using Clock = std::chrono::steady_clock;
 
 constexpr int64_t kDefaultBudget = int64_t(40) << 30;  // 40 GiB
+constexpr int kSlots = 3;
+constexpr int64_t kBatchBytes = int64_t(64) << 20;  // frame bytes per batch (default)
+constexpr int64_t kMinBatchFrames = 4096;
+constexpr double kMaxWaitMs = 25.0;  // a request waiting this long leads the next batch
 
 struct Request {
     int32_t set_id = 0;
@@ -85,7 +93,7 @@ struct km_server {
     bool stop = false;
     km_serve_stats stats{};
     // owned by the worker thread
-    km::Slot slots[2];
+    km::Slot slots[km::kSlots];
     int slots_version = -1;
     int64_t cap = 0;
     int32_t d_max = 0;
@@ -108,12 +116,24 @@ void free_slot_memory(km_server *S) {
     S->cap = 0;
 }
 
-// Sizes both slots for the registered center sets: the largest batch whose
-// frames, labels and assignment workspace fit twice into the budget.
+// Frames per batch for center sets of d features: kBatchBytes of frames (at
+// least kMinBatchFrames), or max_batch_frames when the caller set it.
+int64_t batch_frames_for(const km_server *S, int32_t d) {
+    if (S->cfg.max_batch_frames > 0) return S->cfg.max_batch_frames;
+    return std::max<int64_t>(kMinBatchFrames, kBatchBytes / ((int64_t)d * (int64_t)sizeof(float)));
+}
+
+// Sizes the slots for the registered center sets: every slot holds the
+// largest batch of any set (frames, labels and assignment workspace), and
+// all kSlots slots together fit into the budget.
 int size_slots(km_server *S, const std::vector<const km_centers *> &sets) {
     free_slot_memory(S);
     int32_t dmax = 1;
-    for (const km_centers *h : sets) dmax = std::max(dmax, centers_d(h));
+    int64_t want = 1;
+    for (const km_centers *h : sets) {
+        dmax = std::max(dmax, centers_d(h));
+        want = std::max(want, batch_frames_for(S, centers_d(h)));
+    }
     auto ws_for = [&](int64_t n) {
         size_t ws = 0;
         for (const km_centers *h : sets) ws = std::max(ws, assign_centers_ws_bytes(n, h));
@@ -124,16 +144,15 @@ int size_slots(km_server *S, const std::vector<const km_centers *> &sets) {
                round256(ws_for(n));
     };
     const uint64_t budget = (uint64_t)S->cfg.hbm_budget_bytes;
-    int64_t hi = S->cfg.max_batch_frames > 0 ? S->cfg.max_batch_frames : (int64_t(1) << 31) - 1;
-    hi = std::min<int64_t>(hi, (int64_t(1) << 31) - 1);
-    if (2 * (uint64_t)slot_bytes(1) > budget) {
+    int64_t hi = std::min<int64_t>(want, (int64_t(1) << 31) - 1);
+    if (kSlots * (uint64_t)slot_bytes(1) > budget) {
         set_error("admission budget of %lld bytes holds no batch", (long long)budget);
         return KM_ERR_WORKSPACE;
     }
     int64_t lo = 1;
     while (lo < hi) {
         const int64_t mid = lo + (hi - lo + 1) / 2;
-        if (2 * (uint64_t)slot_bytes(mid) <= budget)
+        if (kSlots * (uint64_t)slot_bytes(mid) <= budget)
             lo = mid;
         else
             hi = mid - 1;
@@ -149,7 +168,7 @@ int size_slots(km_server *S, const std::vector<const km_centers *> &sets) {
     S->d_max = dmax;
     std::lock_guard<std::mutex> lk(S->m);
     S->stats.batch_cap_frames = cap;
-    S->stats.device_bytes = (int64_t)(2 * slot_bytes(cap));
+    S->stats.device_bytes = (int64_t)(kSlots * slot_bytes(cap));
     return KM_OK;
 }
 
@@ -241,6 +260,9 @@ void worker_main(km_server *S) {
         cudaMallocHost(&sl.err_host, sizeof(uint32_t));
     }
     int cur = 0;
+    auto finish_all = [&]() {  // oldest batch first
+        for (int q = 0; q < kSlots; ++q) finish(S, S->slots[(cur + q) % kSlots]);
+    };
     for (;;) {
         std::unique_lock<std::mutex> lk(S->m);
         S->cv_work.wait(lk, [S] { return S->stop || !S->queue.empty(); });
@@ -249,8 +271,7 @@ void worker_main(km_server *S) {
             const std::vector<const km_centers *> sets = S->sets;
             const int version = S->sets_version;
             lk.unlock();
-            finish(S, S->slots[cur]);
-            finish(S, S->slots[cur ^ 1]);
+            finish_all();
             const int st = size_slots(S, sets);
             const std::string msg = st == KM_OK ? std::string() : std::string(km_last_error());
             lk.lock();
@@ -268,19 +289,38 @@ void worker_main(km_server *S) {
             finish(S, sl);
             lk.lock();
         }
-        // Pack: the oldest request fixes the center set; later requests of
-        // the same set follow in arrival order until the slot is full.
-        const int32_t set_id = S->reqs[S->queue.front()].set_id;
-        const km_centers *h = S->sets[set_id];
+        // Pack.  The leader is the queued request with the fewest frames
+        // left (ties: the older), unless the oldest has waited kMaxWaitMs;
+        // the leader fixes the center set, and the queued requests of that
+        // set follow, fewest frames left first, until the batch is full.
         const Clock::time_point now = Clock::now();
-        int64_t filled = 0;
-        for (auto it = S->queue.begin(); it != S->queue.end() && filled < S->cap;) {
-            Request &r = S->reqs[*it];
-            if (r.set_id != set_id) {
-                ++it;
-                continue;
+        uint64_t lead = S->queue.front();
+        if (std::chrono::duration<double, std::milli>(now - S->reqs[lead].t_submit).count() < kMaxWaitMs) {
+            int64_t best = -1;
+            for (uint64_t t : S->queue) {
+                const Request &r = S->reqs[t];
+                if (best < 0 || r.n - r.next < best) {
+                    best = r.n - r.next;
+                    lead = t;
+                }
             }
-            const int64_t take = std::min(r.n - r.next, S->cap - filled);
+        }
+        const int32_t set_id = S->reqs[lead].set_id;
+        const km_centers *h = S->sets[set_id];
+        const int64_t cap = std::min<int64_t>(S->cap, batch_frames_for(S, centers_d(h)));
+        std::vector<uint64_t> order;  // the leader, then the set's other requests by frames left
+        order.push_back(lead);
+        for (uint64_t t : S->queue)
+            if (t != lead && S->reqs[t].set_id == set_id) order.push_back(t);
+        std::stable_sort(order.begin() + 1, order.end(), [S](uint64_t a, uint64_t b) {
+            const Request &ra = S->reqs[a], &rb = S->reqs[b];
+            return ra.n - ra.next < rb.n - rb.next;
+        });
+        int64_t filled = 0;
+        for (uint64_t t : order) {
+            if (filled >= cap) break;
+            Request &r = S->reqs[t];
+            const int64_t take = std::min(r.n - r.next, cap - filled);
             sl.pieces.push_back(Piece{&r, r.next, filled, take});
             r.next += take;
             r.pieces_left += 1;
@@ -289,28 +329,21 @@ void worker_main(km_server *S) {
                 r.started = true;
                 r.t_start = now;
             }
-            if (r.next == r.n)
-                it = S->queue.erase(it);
-            else
-                ++it;
+            if (r.next == r.n) S->queue.erase(std::find(S->queue.begin(), S->queue.end(), t));
         }
         for (const Piece &pc : sl.pieces) pc.req->batch_frames = std::max(pc.req->batch_frames, filled);
         sl.frames = filled;
         lk.unlock();
         launch(S, sl, h);
-        cur ^= 1;
+        cur = (cur + 1) % kSlots;
         bool more;
         {
             std::lock_guard<std::mutex> g(S->m);
             more = !S->queue.empty();
         }
-        if (!more) {  // nothing waiting: deliver what is in flight, oldest first
-            finish(S, S->slots[cur]);
-            finish(S, S->slots[cur ^ 1]);
-        }
+        if (!more) finish_all();  // nothing waiting: deliver what is in flight, oldest first
     }
-    finish(S, S->slots[cur]);
-    finish(S, S->slots[cur ^ 1]);
+    finish_all();
     free_slot_memory(S);
     for (Slot &sl : S->slots) {
         if (sl.stream) cudaStreamDestroy(sl.stream);

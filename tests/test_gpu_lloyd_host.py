@@ -90,3 +90,28 @@ def test_api_host_input_matches_device_input(torch):
                                max_iter=20, tolerance=-1.0)
     assert km_h.n_iter == km_d.n_iter == 20
     np.testing.assert_allclose(km_h.clustercenters, km_d.clustercenters, rtol=1e-5, atol=1e-5)
+
+
+@pytest.mark.parametrize("d", [333, 528])
+def test_host_pageable_staged_many_blocks(torch, L, d):
+    # Ordinary numpy parts (pageable) are staged through page-locked buffers
+    # by worker threads in 16 MiB blocks; here about 80 blocks over several
+    # chunks, parts of uneven size, one of them pinned.  The device copy is
+    # bit-exact and the run equals km_lloyd on the same frames.
+    rng = np.random.default_rng(d)
+    sizes = [250_000, 1, 130_001, 0, 220_000]
+    parts = _parts(rng, sizes, d)
+    pinned = torch.empty((sizes[2], d), dtype=torch.float32, pin_memory=True)
+    pinned.numpy()[...] = parts[2]
+    parts[2] = pinned.numpy()
+    Xh = np.concatenate(parts)
+    C0 = torch.from_numpy(Xh[rng.choice(len(Xh), 500, replace=False)] + 0.01).cuda()
+    Ca, Cb = C0.clone(), C0.clone()
+    ra = L.lloyd_host(parts, Ca, 2, -1.0, precision="fp16")
+    assert torch.equal(ra["X"].cpu(), torch.from_numpy(Xh))
+    rb = L.lloyd(torch.from_numpy(Xh).cuda(), Cb, 2, -1.0, precision="fp16")
+    assert ra["n_iter"] == rb["n_iter"] == 2
+    torch.testing.assert_close(Ca, Cb, rtol=1e-5, atol=1e-5)
+    np.testing.assert_allclose(ra["inertias"], rb["inertias"], rtol=1e-5)
+    r0 = L.lloyd_host(parts, C0.clone(), 0, -1.0, precision="fp16")  # copy only
+    assert torch.equal(r0["X"].cpu(), torch.from_numpy(Xh))
