@@ -32,10 +32,6 @@ constexpr int kFC = 32;  // features per shared-memory chunk
 // made on the device from the list's length.
 constexpr int64_t kFullFew = 64;
 
-// Re-checks of rows of at least this many features use the warp-cooperative
-// evaluation; narrower rows fit a thread's loads well enough.
-constexpr int kRcWarpMinD = 32;
-
 // SPLIT: blockIdx.y selects one block of 32*G centers and the result of the
 // block goes to keys[entry] by atomicMin of (distance bits << 32 | center),
 // which recheck_finalize_kernel turns into labels.
@@ -205,125 +201,6 @@ __global__ void __launch_bounds__(256) recheck_rest_kernel(
     }
 }
 
-// Warp-cooperative form of the same evaluations.  One thread walking its
-// own two rows makes every warp load touch 32 different rows; that form is
-// bound by L1 wavefronts (one per 16 bytes).  Here a warp evaluates up to 32
-// (frame, center) pairs together: for each 32-feature slice, lane l loads
-// feature f0 + l of every pair's two rows (coalesced, one 128-byte line per
-// row), rounds (x - c)^2 on its own and stores it transposed in shared
-// memory; then lane b adds pair b's 32 squares in feature order.  The sum of
-// pair b is therefore the sequential float32 sum of sqdist_exact, bit for
-// bit.  Pairs are gathered per warp in a shared-memory queue (a pair of the
-// second pass is dropped there when its lower bound exceeds the entry's
-// exact best), and evaluated 32 at a time.
-constexpr int kRcWarps = 4;
-constexpr int kRcQueue = 64;
-
-struct RcWarpSmem {
-    float sq[32][33];      // sq[l][b]: rounded square of feature f0 + l of pair b
-    int32_t qf[kRcQueue];  // frame row
-    int32_t qc[kRcQueue];  // center row
-    int32_t qe[kRcQueue];  // entry
-};
-
-// Evaluates the first nb (<= 32) queued pairs; lane b < nb returns the
-// sequential float32 distance of pair b.
-__device__ __forceinline__ float rc_eval_batch(const float *__restrict__ X, const float *__restrict__ C, int d,
-                                               RcWarpSmem &w, int nb, int lane) {
-    float acc = 0.0f;
-    for (int f0 = 0; f0 < d; f0 += 32) {
-        const int f = f0 + lane;
-        if (f < d) {
-#pragma unroll 8
-            for (int b = 0; b < 32; ++b) {
-                if (b < nb) {
-                    const float x = __ldg(X + (int64_t)w.qf[b] * d + f);
-                    const float c = __ldg(C + (int64_t)w.qc[b] * d + f);
-                    w.sq[lane][b] = sq_term(x, c);
-                }
-            }
-        }
-        __syncwarp();
-        const int fw = min(32, d - f0);
-        if (lane < nb)
-            for (int l = 0; l < fw; ++l) acc = __fadd_rn(acc, w.sq[l][lane]);
-        __syncwarp();
-    }
-    return acc;
-}
-
-// REST = false: pair e = (rc_frames[e], rc_best[e]) for every entry, its key
-// stored.  REST = true: pair q of the candidate list, skipped when it is the
-// entry's best or its lower bound exceeds the best's exact distance; the key
-// joins the entry's minimum by atomicMin.
-template <bool REST>
-__global__ void __launch_bounds__(kRcWarps * 32) recheck_warp_kernel(
-    const float *__restrict__ X, int d, const float *__restrict__ C, const int32_t *__restrict__ rc_frames,
-    const int32_t *__restrict__ rc_best, const int32_t *__restrict__ pair_entry,
-    const int32_t *__restrict__ pair_center, const float *__restrict__ pair_lo, const int32_t *__restrict__ count_p,
-    int64_t max_items, unsigned long long *__restrict__ keys) {
-    __shared__ RcWarpSmem sm[kRcWarps];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    RcWarpSmem &w = sm[warp];
-    int64_t count = *count_p;
-    if (count > max_items) count = max_items;
-    const int64_t nwin = (count + 31) / 32;
-    const int64_t gw = (int64_t)blockIdx.x * kRcWarps + warp;
-    const int64_t nw = (int64_t)gridDim.x * kRcWarps;
-    int qn = 0;  // queued pairs (warp-uniform)
-    auto flush = [&](int nb) {
-        const float dd = rc_eval_batch(X, C, d, w, nb, lane);
-        if (lane < nb) {
-            const unsigned long long key = ((unsigned long long)__float_as_uint(dd) << 32) | (unsigned)w.qc[lane];
-            if (REST)
-                atomicMin(&keys[w.qe[lane]], key);
-            else
-                keys[w.qe[lane]] = key;
-        }
-        __syncwarp();
-    };
-    for (int64_t win = gw; win < nwin; win += nw) {
-        const int64_t q = win * 32 + lane;
-        bool act = false;
-        int32_t fr = 0, ce = 0, en = 0;
-        if (q < count) {
-            if (REST) {
-                en = pair_entry[q];
-                ce = pair_center[q];
-                const float dstar = __uint_as_float((uint32_t)(keys[en] >> 32));
-                act = ce != rc_best[en] && !(pair_lo[q] > dstar);  // a NaN bound is evaluated
-                if (act) fr = rc_frames[en];
-            } else {
-                en = (int32_t)q;
-                fr = rc_frames[q];
-                ce = rc_best[q];
-                act = true;
-            }
-        }
-        const unsigned m = __ballot_sync(0xffffffffu, act);
-        if (act) {
-            const int slot = qn + __popc(m & ((1u << lane) - 1u));
-            w.qf[slot] = fr;
-            w.qc[slot] = ce;
-            w.qe[slot] = en;
-        }
-        qn += __popc(m);
-        __syncwarp();
-        if (qn >= 32) {
-            flush(32);
-            qn -= 32;
-            if (lane < qn) {  // the rest (slots 32 .. 32 + qn) moves to the front
-                const int32_t a = w.qf[32 + lane], b = w.qc[32 + lane], c = w.qe[32 + lane];
-                w.qf[lane] = a;
-                w.qc[lane] = b;
-                w.qe[lane] = c;
-            }
-            __syncwarp();
-        }
-    }
-    if (qn > 0) flush(qn);
-}
-
 // Full re-check of a short list: one warp per (frame, 32 consecutive
 // centers), one exact distance per lane (sqdist_exact: the assignment's
 // arithmetic and order), the warp's smallest key, one atomicMin per warp.
@@ -410,32 +287,16 @@ int launch_recheck_pairs(const float *X, int d, const float *C, const int32_t *r
                          int blocks_per_sm) {
     if (max_entries == 0) return KM_OK;
     const int64_t cap = (int64_t)num_sms() * blocks_per_sm;
-    if (d >= kRcWarpMinD) {
-        // Warp-cooperative evaluation (coalesced rows); the grid covers every
-        // SM with blocks_per_sm * 2 CTAs of 4 warps at most.
-        const int64_t wcap = cap * 2;
-        int64_t g0 = (max_entries + 32 * kRcWarps - 1) / (32 * kRcWarps);
-        if (g0 > wcap) g0 = wcap;
-        recheck_warp_kernel<false><<<(unsigned)(g0 < 1 ? 1 : g0), kRcWarps * 32, 0, s>>>(
-            X, d, C, rc_frames, rc_best, pair_entry, pair_center, pair_lo, counters, max_entries, keys);
-        KM_CUDA(cudaGetLastError());
-        int64_t g1 = (max_pairs + 32 * kRcWarps - 1) / (32 * kRcWarps);
-        if (g1 > wcap) g1 = wcap;
-        recheck_warp_kernel<true><<<(unsigned)(g1 < 1 ? 1 : g1), kRcWarps * 32, 0, s>>>(
-            X, d, C, rc_frames, rc_best, pair_entry, pair_center, pair_lo, counters + 2, max_pairs, keys);
-        KM_CUDA(cudaGetLastError());
-    } else {
-        int64_t g0 = (max_entries + 255) / 256;
-        if (g0 > cap) g0 = cap;
-        recheck_best_kernel<<<(unsigned)(g0 < 1 ? 1 : g0), 256, 0, s>>>(X, d, C, rc_frames, rc_best, counters,
-                                                                      max_entries, keys);
-        KM_CUDA(cudaGetLastError());
-        int64_t g1 = (max_pairs + 255) / 256;
-        if (g1 > cap) g1 = cap;
-        recheck_rest_kernel<<<(unsigned)(g1 < 1 ? 1 : g1), 256, 0, s>>>(
-            X, d, C, rc_frames, rc_best, pair_entry, pair_center, pair_lo, counters + 2, max_pairs, keys);
-        KM_CUDA(cudaGetLastError());
-    }
+    int64_t g0 = (max_entries + 255) / 256;
+    if (g0 > cap) g0 = cap;
+    recheck_best_kernel<<<(unsigned)(g0 < 1 ? 1 : g0), 256, 0, s>>>(X, d, C, rc_frames, rc_best, counters,
+                                                                  max_entries, keys);
+    KM_CUDA(cudaGetLastError());
+    int64_t g1 = (max_pairs + 255) / 256;
+    if (g1 > cap) g1 = cap;
+    recheck_rest_kernel<<<(unsigned)(g1 < 1 ? 1 : g1), 256, 0, s>>>(X, d, C, rc_frames, rc_best, pair_entry,
+                                                                  pair_center, pair_lo, counters + 2, max_pairs, keys);
+    KM_CUDA(cudaGetLastError());
     int64_t g2 = (max_entries + 255) / 256;
     if (g2 > cap) g2 = cap;
     recheck_finalize_kernel<<<(unsigned)(g2 < 1 ? 1 : g2), 256, 0, s>>>(

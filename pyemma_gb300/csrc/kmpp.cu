@@ -20,17 +20,26 @@
 // finishes last (a fenced atomic count, no waiting) draws the round's frame
 // and copies it into the centers.
 //
-// Pruning (Euclidean metric): each frame keeps, besides D^2 = mind, the index
-// a of a center whose exact distance is mind.  Before round r's pass a small
-// kernel bounds cc_j = ||c_new - c_j||^2 for every earlier center j.  By the
-// triangle inequality ||x - c_new|| >= ||c_new - c_a|| - ||x - c_a||, so when
-// cc_a >= 4 mind (times a factor covering the float32 rounding of mind, of
-// the new distance and of cc) the exact new distance cannot fall below mind
-// and the frame's row is not read.  The running minima, and so the draws,
-// are the same as without pruning, bit for bit; a skipped frame costs 8 bytes
-// (mind, a) instead of 4d + 4.
+// Pruning (Euclidean metric, large n d): each frame keeps, besides
+// D^2 = mind, the index a of a center whose exact distance is mind.  Round r
+// (r >= 2) runs three launches:
+//   1. cc_j = ||c_new - c_j||^2 for every earlier center j (float32);
+//   2. a pass over (mind, a) only: by the triangle inequality
+//      ||x - c_new|| >= ||c_new - c_a|| - ||x - c_a||, so when cc_a >= 4 mind
+//      (times a factor covering the float32 rounding of mind, of the new
+//      distance and of cc) the exact new distance cannot fall below mind;
+//      the other frames go into a list;
+//   3. the listed frames' exact distances, spread over every SM; a frame
+//      whose minimum drops updates mind and a, and adds the change of its
+//      integer weight to its tile's sum; the CTA that finishes last draws.
+// The running minima, and so the draws, are the same as without pruning, bit
+// for bit.  A skipped frame costs 8 bytes (mind, a) instead of 4d + 4, and
+// the tile sums are kept exact by the integer deltas (the first round stores
+// them in full).
+#include <algorithm>
 #include <climits>
 #include <cmath>
+#include <cstdlib>
 
 #include "km_common.cuh"
 #include "km_internal.h"
@@ -51,6 +60,8 @@ struct KmppWs {
     uint32_t *maxbits;
     int *qexp;      // e of the weights floor(D^2 2^e); INT_MIN: every weight is 0
     unsigned int *done;  // CTAs of the current round that have finished
+    int32_t *list;       // frames of the round that the bound does not rule out
+    int32_t *list_n;
 };
 
 KmppWs carve(void *ws, int64_t n, int k, size_t *bytes) {
@@ -64,6 +75,8 @@ KmppWs carve(void *ws, int64_t n, int k, size_t *bytes) {
     w.maxbits = c.take<uint32_t>(1);
     w.qexp = c.take<int>(1);
     w.done = c.take<unsigned int>(1);
+    w.list = c.take<int32_t>(n > 0 ? n : 1);
+    w.list_n = c.take<int32_t>(1);
     if (bytes) *bytes = c.bytes();
     return w;
 }
@@ -195,38 +208,25 @@ __device__ __forceinline__ unsigned long long cta_exclusive_scan_u64(unsigned lo
     return (warp > 0 ? warp_tot[warp - 1] : 0ull) + x - v;
 }
 
-// The end of a round, after the pass: the tile's weight sum s (any thread's
-// share) is reduced and stored; the CTA that finishes last draws frame r:
-// t = floor(u W / 2^64) for the weight total W, the first frame whose
-// inclusive prefix weight exceeds t (a uniform frame when W = 0), copied into
-// C0[r].  The other CTAs return.
+// The draw of round r by the CTA that finished last (the tile sums and the
+// minima of the other CTAs are read past L1): t = floor(u W / 2^64) for the
+// weight total W over the ntiles tiles, the first frame whose inclusive
+// prefix weight exceeds t (a uniform frame when W = 0), copied into C0[r].
 template <int THREADS>
-__device__ __forceinline__ void kmpp_finish_round(unsigned long long s, const float *__restrict__ X, int64_t n,
-                                                  int d, float *__restrict__ C0, int64_t *__restrict__ idx_out,
-                                                  const float *__restrict__ mind, int qexp,
-                                                  unsigned long long *__restrict__ tile_sum,
-                                                  unsigned int *__restrict__ done, int r, uint32_t seed) {
+__device__ __forceinline__ void kmpp_draw_round(int64_t ntiles, const float *__restrict__ X, int64_t n, int d,
+                                                float *__restrict__ C0, int64_t *__restrict__ idx_out,
+                                                const float *__restrict__ mind, int qexp,
+                                                const unsigned long long *__restrict__ tile_sum,
+                                                unsigned int *__restrict__ done, int r, uint32_t seed) {
     constexpr int kPer = kTile / THREADS;  // frames per thread in the draw's tile
     __shared__ unsigned long long red[THREADS / 32];
-    __shared__ bool last;
     __shared__ long long tile_hit, pick;
     __shared__ unsigned long long target;
-    s = block_sum_u64(s, red);
-    __threadfence();  // this thread's running minimum before the count
-    __syncthreads();
     if (threadIdx.x == 0) {
-        tile_sum[blockIdx.x] = s;
-        __threadfence();
-        last = atomicAdd(done, 1u) == gridDim.x - 1;
         tile_hit = -1;
         pick = -1;
     }
     __syncthreads();
-    if (!last) return;
-    __threadfence();
-
-    // The draw (the other CTAs' sums and minima are read past L1).
-    const int64_t ntiles = gridDim.x;
     const uint64_t u = kmpp_draw(seed, (uint32_t)r);
     const int64_t per = (ntiles + THREADS - 1) / THREADS;
     const int64_t lo = min((int64_t)threadIdx.x * per, ntiles), hi = min(lo + per, ntiles);
@@ -284,26 +284,34 @@ __device__ __forceinline__ void kmpp_finish_round(unsigned long long s, const fl
     }
 }
 
-// The skip test of the pruned pass: the bound shows that the exact distance
-// to the new center is at least mi (finite mi only; a NaN bound never skips).
-__device__ __forceinline__ bool kmpp_skip(float mi, int32_t a, const float *__restrict__ cc, float prune_factor) {
-    return mi <= 3.4028234663852886e38f && __ldg(cc + a) >= __fmul_ru(mi, prune_factor);
+// True in every thread of the CTA that counts itself last among gridDim.x
+// (after a fence of this thread's writes); the others' writes are visible
+// to it past L1.
+__device__ __forceinline__ bool kmpp_last_cta(unsigned int *__restrict__ done) {
+    __shared__ bool last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(done, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (last) __threadfence();
+    return last;
 }
 
 // Round r >= 1, one CTA per tile of kTile frames, one thread per frame (at
 // a time).  With r_center >= 0 the running minimum first takes the distance
 // to center r_center (rounds >= 2; round 1 uses the minimum of
-// kmpp_first_kernel as it is); PRUNE skips the frames that the bound rules
-// out.  Then kmpp_finish_round.  THREADS = 1024 for narrow Euclidean rows
+// kmpp_first_kernel as it is).  Then the tile's weight sum is stored and the
+// CTA that finishes last draws.  THREADS = 1024 for the Euclidean metric
 // (two frames per thread: the pass is latency-bound at small n), 256 for
-// minRMSD (the QCP solve needs the registers).
-template <int THREADS, bool RMSD, bool PRUNE>
+// minRMSD (the QCP solve needs the registers).  The pruned rounds' first
+// round runs here too (r_center = -1), which stores every tile sum.
+template <int THREADS, bool RMSD>
 __global__ void __launch_bounds__(THREADS) kmpp_round_kernel(
     const float *__restrict__ X, int64_t n, int d, float *__restrict__ C0, int64_t *__restrict__ idx_out,
-    float *__restrict__ mind, int32_t *__restrict__ near, const float *__restrict__ cc,
-    float prune_factor, const int *__restrict__ qexp_p, unsigned long long *__restrict__ tile_sum,
+    float *__restrict__ mind, const int *__restrict__ qexp_p, unsigned long long *__restrict__ tile_sum,
     unsigned int *__restrict__ done, KmppMetric m, int r_center, int r, uint32_t seed) {
     constexpr int kPer = kTile / THREADS;
+    __shared__ unsigned long long red[THREADS / 32];
     const int qexp = *qexp_p;
     const int64_t t0 = (int64_t)blockIdx.x * kTile;
     unsigned long long s = 0;
@@ -311,110 +319,97 @@ __global__ void __launch_bounds__(THREADS) kmpp_round_kernel(
         const int64_t i = t0 + u * THREADS + threadIdx.x;
         if (i < n) {
             float mi = mind[i];
-            if (r_center >= 0 && !(PRUNE && kmpp_skip(mi, near[i], cc, prune_factor))) {
+            if (r_center >= 0) {
                 const float *c = C0 + (int64_t)r_center * d;
                 const float dd = RMSD ? kmpp_d2(X, i, d, c, m, r_center) : sqdist_exact(X + i * d, c, d);
                 if (dd < mi) {
                     mi = dd;
                     mind[i] = mi;
-                    if (PRUNE) near[i] = r_center;
                 }
             }
             s += quant_weight(mi, qexp);
         }
     }
-    kmpp_finish_round<THREADS>(s, X, n, d, C0, idx_out, mind, qexp, tile_sum, done, r, seed);
+    s = block_sum_u64(s, red);
+    if (threadIdx.x == 0) tile_sum[blockIdx.x] = s;
+    if (!kmpp_last_cta(done)) return;
+    kmpp_draw_round<THREADS>(gridDim.x, X, n, d, C0, idx_out, mind, qexp, tile_sum, done, r, seed);
 }
 
-// The pruned Euclidean pass for rows of at least 32 features, warp by warp.
-// A warp owns 8 windows of 32 frames of the tile; the frames that the bound
-// does not rule out are queued in shared memory and evaluated 32 at a time:
-// for each 32-feature slice lane l loads feature f0 + l of every queued row
-// (coalesced) and of the new center, rounds (x - c)^2 and stores it
-// transposed; lane b then adds row b's squares in feature order, which is
-// sqdist_exact's sum bit for bit.  One thread per row would make every warp
-// load touch 32 rows, and that pass is bound by L1 wavefronts.
-constexpr int kWarpThreads = 256;
-constexpr int kWarpWin = kTile / kWarpThreads;  // windows of 32 frames per warp
-
-struct KmppWarpSmem {
-    float sq[32][33];         // sq[l][b]: rounded square of feature f0 + l of queued row b
-    int32_t q[64];            // queued frames (window * 32 + lane)
-    float m[kWarpWin * 32];   // the warp's running minima
-};
-
-__global__ void __launch_bounds__(kWarpThreads) kmpp_round_warp_kernel(
-    const float *__restrict__ X, int64_t n, int d, float *__restrict__ C0, int64_t *__restrict__ idx_out,
-    float *__restrict__ mind, int32_t *__restrict__ near, const float *__restrict__ cc, float prune_factor,
-    const int *__restrict__ qexp_p, unsigned long long *__restrict__ tile_sum, unsigned int *__restrict__ done,
-    int r_center, int r, uint32_t seed) {
-    __shared__ KmppWarpSmem wsm[kWarpThreads / 32];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    KmppWarpSmem &w = wsm[warp];
-    const int qexp = *qexp_p;
-    const int64_t t0 = (int64_t)blockIdx.x * kTile + warp * 32;  // frame of window 0, lane 0
-    const float *c = C0 + (int64_t)(r_center > 0 ? r_center : 0) * d;
-
-    auto process = [&](int nb) {
-        float acc = 0.0f;
-        for (int f0 = 0; f0 < d; f0 += 32) {
-            const int f = f0 + lane;
-            if (f < d) {
-                const float cf = __ldg(c + f);
-#pragma unroll 8
-                for (int b = 0; b < 32; ++b) {
-                    if (b < nb) {
-                        const int li = w.q[b];
-                        const int64_t i = t0 + (int64_t)(li >> 5) * kWarpThreads + (li & 31);
-                        w.sq[lane][b] = sq_term(__ldg(X + i * d + f), cf);
-                    }
+// Pruned round, launch 2: four frames per thread (vector loads of mind and
+// a); the frames that the bound does not rule out are appended to the list,
+// one atomic per warp.  The skip needs a finite mind; a NaN bound never
+// skips.
+__global__ void __launch_bounds__(256) kmpp_prune_kernel(int64_t n, const float *__restrict__ mind,
+                                                         const int32_t *__restrict__ near,
+                                                         const float *__restrict__ cc, float prune_factor,
+                                                         int32_t *__restrict__ list, int32_t *__restrict__ list_n) {
+    const int lane = threadIdx.x & 31;
+    const int64_t nq = (n + 3) / 4;
+    for (int64_t q0 = (int64_t)blockIdx.x * blockDim.x; q0 < nq; q0 += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t q = q0 + threadIdx.x;
+        float mi[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        int32_t a[4] = {0, 0, 0, 0};
+        const int64_t i0 = 4 * q;
+        if (i0 + 3 < n) {
+            const float4 m4 = __ldg(reinterpret_cast<const float4 *>(mind) + q);
+            const int4 a4 = __ldg(reinterpret_cast<const int4 *>(near) + q);
+            mi[0] = m4.x, mi[1] = m4.y, mi[2] = m4.z, mi[3] = m4.w;
+            a[0] = a4.x, a[1] = a4.y, a[2] = a4.z, a[3] = a4.w;
+        } else {
+            for (int v = 0; v < 4; ++v)
+                if (i0 + v < n) {
+                    mi[v] = mind[i0 + v];
+                    a[v] = near[i0 + v];
                 }
-            }
-            __syncwarp();
-            const int fw = min(32, d - f0);
-            if (lane < nb)
-                for (int l = 0; l < fw; ++l) acc = __fadd_rn(acc, w.sq[l][lane]);
-            __syncwarp();
         }
-        if (lane < nb) {
-            const int li = w.q[lane];
-            if (acc < w.m[li]) {
-                const int64_t i = t0 + (int64_t)(li >> 5) * kWarpThreads + (li & 31);
-                w.m[li] = acc;
-                mind[i] = acc;
-                near[i] = r_center;
-            }
+        unsigned keep = 0u;
+#pragma unroll
+        for (int v = 0; v < 4; ++v)
+            if (i0 + v < n && !(mi[v] <= 3.4028234663852886e38f && __ldg(cc + a[v]) >= __fmul_ru(mi[v], prune_factor)))
+                keep |= 1u << v;
+        const int cnt = __popc(keep);
+        int excl = cnt;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, excl, off);
+            if (lane >= off) excl += y;
         }
-        __syncwarp();
-    };
+        const int total = __shfl_sync(0xffffffffu, excl, 31);
+        int base = 0;
+        if (lane == 31 && total > 0) base = atomicAdd(list_n, total);
+        base = __shfl_sync(0xffffffffu, base, 31) + excl - cnt;
+        for (int v = 0; v < 4; ++v)
+            if ((keep >> v) & 1u) list[base++] = (int32_t)(i0 + v);
+    }
+}
 
-    int qn = 0;  // queued frames (warp-uniform)
-    for (int u = 0; u < kWarpWin; ++u) {
-        const int64_t i = t0 + (int64_t)u * kWarpThreads + lane;
-        const int li = u * 32 + lane;
-        bool act = false;
-        float mi = 0.0f;
-        if (i < n) {
-            mi = mind[i];
-            act = r_center >= 0 && !kmpp_skip(mi, near[i], cc, prune_factor);
-        }
-        w.m[li] = mi;
-        const unsigned msk = __ballot_sync(0xffffffffu, act);
-        if (act) w.q[qn + __popc(msk & ((1u << lane) - 1u))] = li;
-        qn += __popc(msk);
-        __syncwarp();
-        if (qn >= 32) {
-            process(32);
-            qn -= 32;
-            if (lane < qn) w.q[lane] = w.q[32 + lane];  // slots 32 .. 32 + qn move to the front
-            __syncwarp();
+// Pruned round, launch 3: one listed frame per thread (grid-stride); a
+// smaller exact distance replaces mind and a and moves the frame's integer
+// weight in its tile's sum (modular 64-bit deltas, exact).  The CTA that
+// finishes last clears the list and draws.
+__global__ void __launch_bounds__(256) kmpp_eval_kernel(
+    const float *__restrict__ X, int64_t n, int d, float *__restrict__ C0, int64_t *__restrict__ idx_out,
+    float *__restrict__ mind, int32_t *__restrict__ near, const int *__restrict__ qexp_p,
+    unsigned long long *__restrict__ tile_sum, unsigned int *__restrict__ done, const int32_t *__restrict__ list,
+    int32_t *__restrict__ list_n, int64_t ntiles, int r_center, int r, uint32_t seed) {
+    const int qexp = *qexp_p;
+    const int64_t cnt = *list_n;
+    const float *c = C0 + (int64_t)r_center * d;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < cnt; e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = list[e];
+        const float dd = sqdist_exact(X + i * d, c, d);
+        const float mi = mind[i];
+        if (dd < mi) {
+            mind[i] = dd;
+            near[i] = r_center;
+            const unsigned long long delta = quant_weight(dd, qexp) - quant_weight(mi, qexp);
+            if (delta) atomicAdd(&tile_sum[i / kTile], delta);
         }
     }
-    if (qn > 0) process(qn);
-    unsigned long long s = 0;
-    for (int u = 0; u < kWarpWin; ++u)
-        if (t0 + (int64_t)u * kWarpThreads + lane < n) s += quant_weight(w.m[u * 32 + lane], qexp);
-    kmpp_finish_round<kWarpThreads>(s, X, n, d, C0, idx_out, mind, qexp, tile_sum, done, r, seed);
+    if (!kmpp_last_cta(done)) return;
+    if (threadIdx.x == 0) *list_n = 0;  // for the next round
+    kmpp_draw_round<256>(ntiles, X, n, d, C0, idx_out, mind, qexp, tile_sum, done, r, seed);
 }
 
 // Round 0: a uniformly drawn frame, copied into C0[0].
@@ -475,22 +470,30 @@ int run_kmpp(const float *X, int64_t n, int d, int k, uint32_t seed, float *C0, 
     kmpp_scale_kernel<<<1, 1, 0, s>>>(w.maxbits, n, w.qexp);
     KM_CUDA(cudaGetLastError());
     const float pf = prune_factor(d);
+    // Pruned rounds pay three launches per round; below this size the
+    // unpruned pass is about as short as a launch.  KM_KMPP_PRUNE=0 or 1 in
+    // the environment forces the choice (both give the same draws).
+    bool prune = !m.Xc && n * (int64_t)d >= (int64_t(1) << 22);
+    if (const char *e = std::getenv("KM_KMPP_PRUNE")) prune = !m.Xc && e[0] == '1';
+    if (prune) KM_CUDA(cudaMemsetAsync(w.list_n, 0, sizeof(int32_t), s));
+    const int64_t nq = (n + 3) / 4;
+    const unsigned prune_grid = (unsigned)std::min<int64_t>((nq + 255) / 256, (int64_t)num_sms() * 8);
+    const unsigned eval_grid = (unsigned)num_sms() * 4;
     for (int r = 1; r < k; ++r) {
         const int rc = r >= 2 ? r - 1 : -1;
         if (m.Xc) {
-            kmpp_round_kernel<256, true, false><<<(unsigned)ntiles, 256, 0, s>>>(
-                X, n, d, C0, idx, w.mind, w.near, w.cc, pf, w.qexp, w.tile_sum, w.done, m, rc, r, seed);
+            kmpp_round_kernel<256, true><<<(unsigned)ntiles, 256, 0, s>>>(X, n, d, C0, idx, w.mind, w.qexp,
+                                                                          w.tile_sum, w.done, m, rc, r, seed);
+        } else if (!prune || rc < 0) {
+            kmpp_round_kernel<1024, false><<<(unsigned)ntiles, 1024, 0, s>>>(X, n, d, C0, idx, w.mind, w.qexp,
+                                                                             w.tile_sum, w.done, m, rc, r, seed);
         } else {
-            if (rc >= 1) {
-                kmpp_cc_kernel<<<(unsigned)((rc + 7) / 8), 256, 0, s>>>(C0, d, rc, w.cc);
-                KM_CUDA(cudaGetLastError());
-            }
-            if (d >= 32)
-                kmpp_round_warp_kernel<<<(unsigned)ntiles, kWarpThreads, 0, s>>>(
-                    X, n, d, C0, idx, w.mind, w.near, w.cc, pf, w.qexp, w.tile_sum, w.done, rc, r, seed);
-            else
-                kmpp_round_kernel<1024, false, true><<<(unsigned)ntiles, 1024, 0, s>>>(
-                    X, n, d, C0, idx, w.mind, w.near, w.cc, pf, w.qexp, w.tile_sum, w.done, m, rc, r, seed);
+            kmpp_cc_kernel<<<(unsigned)((rc + 7) / 8), 256, 0, s>>>(C0, d, rc, w.cc);
+            KM_CUDA(cudaGetLastError());
+            kmpp_prune_kernel<<<prune_grid, 256, 0, s>>>(n, w.mind, w.near, w.cc, pf, w.list, w.list_n);
+            KM_CUDA(cudaGetLastError());
+            kmpp_eval_kernel<<<eval_grid, 256, 0, s>>>(X, n, d, C0, idx, w.mind, w.near, w.qexp, w.tile_sum, w.done,
+                                                       w.list, w.list_n, ntiles, rc, r, seed);
         }
         KM_CUDA(cudaGetLastError());
         if (cb) cb(cb_user);

@@ -234,7 +234,7 @@ def test_kmpp_golden(torch, L, golden):
 @pytest.mark.parametrize("n,d,k,seed", [(1, 3, 1, 0), (5, 2, 5, 1), (3000, 2, 50, 42), (10000, 10, 200, 7),
                                         (4100, 528, 30, 3), (2049, 7, 64, 2 ** 32 - 1), (600000, 2, 20, 11),
                                         (1100001, 3, 8, 5)])
-def test_kmpp_matches_oracle(torch, L, oracle, n, d, k, seed):
+def test_kmpp_matches_oracle(torch, L, oracle, n, d, k, seed, kmpp_prune):
     rng = np.random.default_rng(seed % 1000)
     X = rng.normal(size=(n, d)).astype(np.float32)
     _, idx_ref = oracle.kmpp(X, k, seed)
@@ -244,7 +244,7 @@ def test_kmpp_matches_oracle(torch, L, oracle, n, d, k, seed):
     assert len(calls) == k
 
 
-def test_kmpp_sparse_weights_many_tiles(torch, L, oracle):
+def test_kmpp_sparse_weights_many_tiles(torch, L, oracle, kmpp_prune):
     # 700,000 frames (342 weight tiles, more than one per thread of the draw):
     # all but 30 frames equal, so after a few rounds most tiles weigh 0 and
     # the last rounds find no weight at all (uniform fallback).
@@ -256,8 +256,16 @@ def test_kmpp_sparse_weights_many_tiles(torch, L, oracle):
     np.testing.assert_array_equal(idx.cpu().numpy(), idx_ref)
 
 
+@pytest.fixture(params=["0", "1"], ids=["unpruned", "pruned"])
+def kmpp_prune(request, monkeypatch):
+    # KM_KMPP_PRUNE forces the pruned (bound, list, evaluation) or the plain
+    # kmeans++ round; both must draw the oracle's frames.
+    monkeypatch.setenv("KM_KMPP_PRUNE", request.param)
+    return request.param
+
+
 @pytest.mark.parametrize("case", ["mixture", "lattice", "collinear"])
-def test_kmpp_pruned_pass_matches_oracle(torch, L, oracle, case):
+def test_kmpp_pruned_pass_matches_oracle(torch, L, oracle, case, kmpp_prune):
     # Data on which the bound ||c_new - c_a||^2 >= 4 D^2 skips most frames
     # (well separated clusters), and data with exact boundary cases: integer
     # lattice points and points on a line, where a new center often sits at
@@ -281,7 +289,7 @@ def test_kmpp_pruned_pass_matches_oracle(torch, L, oracle, case):
     np.testing.assert_array_equal(idx.cpu().numpy(), idx_ref)
 
 
-def test_kmpp_duplicates(torch, L, oracle):
+def test_kmpp_duplicates(torch, L, oracle, kmpp_prune):
     X = np.ones((100, 4), dtype=np.float32)
     X[50:] = 2.0
     _, idx_ref = oracle.kmpp(X, 6, 5)
