@@ -245,6 +245,36 @@ int km_tune(const float *X, int64_t n, int32_t d, const float *C, int32_t k, voi
             size_t workspace_bytes, int32_t *chosen, double *ms_fp32, double *ms_fp16, void *stream);
 int km_tune_clear(void);
 
+/* ---- tile-shape autotuning (no counterpart in the reference) --------------
+ * The tensor-core kernel's tile shape: bn center columns per tile (64, 128
+ * or 256; k rounded up to 32 below that), pair = 1 for the CTA-pair form
+ * (tcgen05 cta_group::2, M = 256 frames over two SMs; bn = 256 only),
+ * stages of its TMA ring, and list_len candidates kept per frame (8 or 16;
+ * a frame with more near-ties goes to the exact re-check over all centers).
+ * Every shape gives the same labels.  km_tune_tiles times every shape that
+ * fits (d, k) on the given frames and centers (one warm-up and three timed
+ * km_assign calls each, precision KM_PREC_FP16 or KM_PREC_BF16), writes
+ * the fastest to *best and up to max_tried timed shapes to tried (host,
+ * nullable; *n_tried gets their number), and stores the fastest in a
+ * process-wide table behind a mutex: later tensor-core calls for (d, k)
+ * use it (km_tune_clear empties the table).  Workspace as km_tune.
+ * Synchronises `stream`; refuses to run while the stream is captured.
+ * km_tile_plan_get reports the shape that calls for (d, k) use now
+ * (*tuned = 1 when it comes from the table). */
+typedef struct {
+    int32_t bn, pair, stages, list_len;
+    double ms; /* mean time of one km_assign call with this shape (km_tune_tiles) */
+} km_tile_plan;
+int km_tune_tiles(const float *X, int64_t n, int32_t d, const float *C, int32_t k, int32_t precision,
+                  void *workspace, size_t workspace_bytes, km_tile_plan *best, km_tile_plan *tried,
+                  int32_t max_tried, int32_t *n_tried, void *stream);
+int km_tile_plan_get(int32_t d, int32_t k, km_tile_plan *plan, int32_t *tuned);
+
+/* Test hook (diagnostics): tensor-core calls of the calling host thread use
+ * `plan` until the hook is called with NULL; a shape that does not fit
+ * makes them return KM_ERR_UNSUPPORTED. */
+int km_debug_force_tile_plan(const km_tile_plan *plan);
+
 /* ---- regular space clustering, first pass ----------------------------------
  * RegularSpaceClustering._estimate, pyemma/coordinates/clustering/
  * regspace.py:140-152 (deeptime RegularSpace.partial_fit).  Walks the n

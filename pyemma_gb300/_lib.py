@@ -35,7 +35,8 @@ EXPORTED = (
     "km_centers_create", "km_centers_destroy", "km_centers_info", "km_assign_centers_workspace_size",
     "km_assign_centers",
     "km_serve_create", "km_serve_add_centers", "km_serve_submit", "km_serve_poll", "km_serve_stats_read",
-    "km_serve_shutdown", "km_tune_workspace_size", "km_tune", "km_tune_clear",
+    "km_serve_shutdown", "km_tune_workspace_size", "km_tune", "km_tune_clear", "km_tune_tiles", "km_tile_plan_get",
+    "km_debug_force_tile_plan",
     "km_regspace_workspace_size", "km_regspace", "km_count_matrix_workspace_size", "km_count_matrix",
     "km_pair_distances", "km_assign_minrmsd_workspace_size", "km_assign_minrmsd", "km_minrmsd_rows_workspace_size",
     "km_minrmsd_rows", "km_kmpp_minrmsd_workspace_size", "km_kmpp_minrmsd", "km_lloyd_minrmsd_workspace_size",
@@ -63,6 +64,14 @@ class AssignStats(ctypes.Structure):
 
 
 CALLBACK = ctypes.CFUNCTYPE(None, ctypes.c_void_p)
+
+
+class TilePlan(ctypes.Structure):
+    _fields_ = [("bn", ctypes.c_int32), ("pair", ctypes.c_int32), ("stages", ctypes.c_int32),
+                ("list_len", ctypes.c_int32), ("ms", ctypes.c_double)]
+
+    def as_dict(self):
+        return dict(bn=self.bn, pair=self.pair, stages=self.stages, list_len=self.list_len, ms=self.ms)
 
 
 class ServeConfig(ctypes.Structure):
@@ -166,6 +175,13 @@ def load(build_if_missing=False):
                           ctypes.POINTER(f64), P]
     L.km_tune.restype = ctypes.c_int
     L.km_tune_clear.restype = ctypes.c_int
+    L.km_tune_tiles.argtypes = [P, i64, i32, P, i32, i32, P, sz, ctypes.POINTER(TilePlan), ctypes.POINTER(TilePlan),
+                                i32, ctypes.POINTER(i32), P]
+    L.km_tune_tiles.restype = ctypes.c_int
+    L.km_tile_plan_get.argtypes = [i32, i32, ctypes.POINTER(TilePlan), ctypes.POINTER(i32)]
+    L.km_tile_plan_get.restype = ctypes.c_int
+    L.km_debug_force_tile_plan.argtypes = [ctypes.POINTER(TilePlan)]
+    L.km_debug_force_tile_plan.restype = ctypes.c_int
     L.km_regspace_workspace_size.argtypes = [i32]
     L.km_regspace_workspace_size.restype = sz
     L.km_regspace.argtypes = [P, i64, i32, f64, i32, P, ctypes.POINTER(i32), ctypes.POINTER(i32), P, sz, P]
@@ -651,6 +667,49 @@ def tune(X, C):
 
 def tune_clear():
     check(load().km_tune_clear())
+
+
+def tune_tiles(X, C, precision="fp16"):
+    """Times every tensor-core tile shape that fits (d, k) on X against C and
+    stores the fastest for (d, k).  Returns dict(best, tried) of plan dicts
+    (bn, pair, stages, list_len, ms)."""
+    torch = _torch()
+    L = load()
+    _check_frames(torch, X)
+    _check_frames(torch, C, "C")
+    n, d = X.shape
+    k = C.shape[0]
+    ws_bytes = L.km_tune_workspace_size(n, d, k)
+    ws = _workspace(torch, ws_bytes, X.device)
+    best = TilePlan()
+    tried = (TilePlan * 64)()
+    n_tried = ctypes.c_int32(0)
+    check(L.km_tune_tiles(_ptr(X), n, d, _ptr(C), k, precision_code(precision), _ptr(ws), ws_bytes,
+                          ctypes.byref(best), tried, 64, ctypes.byref(n_tried), _stream(torch, X.device)))
+    return dict(best=best.as_dict(), tried=[tried[i].as_dict() for i in range(n_tried.value)])
+
+
+def tile_plan(d, k):
+    """The tile shape tensor-core calls for (d, k) use now: dict(bn, pair,
+    stages, list_len, tuned)."""
+    plan = TilePlan()
+    tuned = ctypes.c_int32(0)
+    check(load().km_tile_plan_get(int(d), int(k), ctypes.byref(plan), ctypes.byref(tuned)))
+    out = plan.as_dict()
+    out.pop("ms")
+    out["tuned"] = bool(tuned.value)
+    return out
+
+
+def force_tile_plan(plan):
+    """Test hook: this thread's tensor-core calls use `plan` (a dict with bn,
+    pair, stages, list_len) until force_tile_plan(None)."""
+    L = load()
+    if plan is None:
+        check(L.km_debug_force_tile_plan(None))
+        return
+    tp = TilePlan(int(plan["bn"]), int(plan["pair"]), int(plan["stages"]), int(plan["list_len"]), 0.0)
+    check(L.km_debug_force_tile_plan(ctypes.byref(tp)))
 
 
 def regspace(X, dmin, max_centers):

@@ -56,7 +56,10 @@
 
 #include <cmath>
 #include <cstdlib>
+#include <map>
 #include <mutex>
+#include <utility>
+#include <vector>
 
 namespace km {
 
@@ -711,7 +714,8 @@ __device__ __forceinline__ float window_threshold(float best, float xn2, float i
 // own accumulator rows.  All barriers the MMAs wait on live in the leader
 // (the peer's copies and accumulator releases arrive there); the MMA commits
 // arrive in both CTAs.
-template <bool PAIR>
+// L: candidates kept per frame (a register list; 8 or 16).
+template <bool PAIR, int L>
 __global__ void __launch_bounds__(kThreadsTC, 1)
     tc_assign_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                      const TcParams p) {
@@ -996,10 +1000,10 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
             const float Rpad = __fadd_ru(Rmax, 1e-18f);
             float best = kNegInf, thr = kNegInf;
             bool ovf = false;
-            float la[kL];
-            int lid[kL];
+            float la[L];
+            int lid[L];
 #pragma unroll
-            for (int m = 0; m < kL; ++m) {
+            for (int m = 0; m < L; ++m) {
                 la[m] = kNegInf;
                 lid[m] = -1;
             }
@@ -1072,9 +1076,9 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                                 for (int q = 0; q < 2; ++q) t2[q] = (c & 2) ? t4[q + 2] : t4[q];
                                 vc = (c & 1) ? t2[1] : t2[0];
                             }
-                            if (lid[kL - 1] >= 0 && la[kL - 1] >= thr) ovf = true;
+                            if (lid[L - 1] >= 0 && la[L - 1] >= thr) ovf = true;
 #pragma unroll
-                            for (int m = kL - 1; m > 0; --m) {
+                            for (int m = L - 1; m > 0; --m) {
                                 la[m] = la[m - 1];
                                 lid[m] = lid[m - 1];
                             }
@@ -1099,12 +1103,12 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
             bool need_rc = false, need_full = false;
             unsigned cmask = 0;  // bit m: list entry m is a candidate
             int jb = 0;          // candidate with the largest accumulator
-            float lo[kL];        // lower bounds of the candidates' exact distances
+            float lo[L];        // lower bounds of the candidates' exact distances
             if (i < p.n) {
-                float vv[kL], RR[kL], EE[kL];
+                float vv[L], RR[L], EE[L];
                 float H = kInf;
 #pragma unroll
-                for (int m = 0; m < kL; ++m) {
+                for (int m = 0; m < L; ++m) {
                     vv[m] = kInf;
                     RR[m] = 0.0f;
                     EE[m] = 0.0f;
@@ -1122,7 +1126,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                     need_full = true;
                 } else {
 #pragma unroll
-                    for (int m = 0; m < kL; ++m) {
+                    for (int m = 0; m < L; ++m) {
                         lo[m] = vv[m] < kInf ? lo_bound(vv[m], EE[m], RR[m], p.g_lo) : kInf;
                         if (lo[m] <= H) cmask |= 1u << m;
                     }
@@ -1135,7 +1139,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                 // the re-checks overwrite the others).
                 float vb = kNegInf;
 #pragma unroll
-                for (int m = 0; m < kL; ++m) {
+                for (int m = 0; m < L; ++m) {
                     if (((cmask >> m) & 1u) && la[m] > vb) {
                         vb = la[m];
                         jb = lid[m];
@@ -1173,7 +1177,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                     p.rc_best[e] = jb;
                     p.rc_keys[e] = ~0ull;
 #pragma unroll
-                    for (int m = 0; m < kL; ++m) {
+                    for (int m = 0; m < L; ++m) {
                         if ((cmask >> m) & 1u) {
                             const int q = pbase + excl + __popc(cmask & ((1u << m) - 1u));
                             p.pair_entry[q] = e;
@@ -1278,9 +1282,18 @@ int k_pad_of(int k) { return (k + 255) / 256 * 256; }
 
 struct Plan {
     int bn, stages, nkc, smem, stream_a;
-    int pair;  // CTA-pair form (cta_group::2, M = 256)
+    int pair;      // CTA-pair form (cta_group::2, M = 256)
+    int list_len;  // candidates kept per frame (8 or 16)
     uint32_t tmem_cols;
 };
+
+// Tile shapes chosen by km_tune_tiles, per (d, k), and the shape a tuning
+// thread forces while it times the candidates.
+struct PlanTable {
+    std::mutex m;
+    std::map<std::pair<int, int>, TilePlan> choice;
+} g_plans;
+thread_local const TilePlan *t_forced_plan = nullptr;
 
 // The CTA-pair form is used for full-width center tiles with a resident frame
 // tile; KM_TC_PAIR=0 or 1 in the environment forces the choice (both forms
@@ -1291,42 +1304,74 @@ bool pair_wanted() {
     return true;
 }
 
-bool make_plan(int d, int k, Plan &pl) {
+// The plan of a given tile shape: bn columns per center tile (a multiple of
+// 32, at most 256), the CTA-pair form (bn = 256, resident frame tile only),
+// max_stages caps the TMA ring (0: as many as fit).  False when the shape
+// does not fit.
+bool build_plan(int d, int bn, bool pair, int max_stages, int list_len, Plan &pl) {
+    if (bn < 32 || bn > 256 || bn % 32 || (list_len != 8 && list_len != 16)) return false;
     pl.nkc = kp_of(d) / kKC;
-    pl.bn = pick_bn(k);
+    pl.bn = bn;
+    pl.list_len = list_len;
     pl.stream_a = 0;
+    pl.pair = 0;
+    const int cap = max_stages > 0 ? std::min(8, max_stages) : 8;
     const int fixed = 1024 + 512;
     int stages = 0;
     if (pl.nkc <= kMaxNkc) {
         const int res = fixed + pl.nkc * kABytesPerChunk;
-        stages = std::min(8, (kSmemLimit - res) / (pl.bn * kKC * 2));
-        if (stages >= 2) pl.smem = res + stages * pl.bn * kKC * 2;
+        if (pair) {
+            // Each CTA of the pair stages half of the B tile: 16 KB per stage.
+            if (bn != 256) return false;
+            const int half = pl.bn / 2 * kKC * 2;
+            stages = std::min(cap, (kSmemLimit - res) / half);
+            if (stages < 3) return false;
+            pl.pair = 1;
+            pl.smem = res + stages * half;
+        } else {
+            stages = std::min(cap, (kSmemLimit - res) / (pl.bn * kKC * 2));
+            if (stages >= 2) pl.smem = res + stages * pl.bn * kKC * 2;
+        }
+    } else if (pair) {
+        return false;
     }
     if (stages < 2) {
         // Streaming: each stage carries an A chunk and a full-width B chunk.
         pl.stream_a = 1;
-        stages = std::min(8, (kSmemLimit - fixed) / (kABytesPerChunk + pl.bn * kKC * 2));
+        stages = std::min(cap, (kSmemLimit - fixed) / (kABytesPerChunk + pl.bn * kKC * 2));
         if (stages < 2) return false;
         pl.smem = fixed + stages * (kABytesPerChunk + pl.bn * kKC * 2);
     }
     pl.stages = stages;
-    pl.pair = 0;
-    if (!pl.stream_a && pl.bn == 256 && pair_wanted()) {
-        // Each CTA of the pair stages half of the B tile: 16 KB per stage.
-        const int res = fixed + pl.nkc * kABytesPerChunk;
-        const int half = pl.bn / 2 * kKC * 2;
-        const int pst = std::min(8, (kSmemLimit - res) / half);
-        if (pst >= 3) {
-            pl.pair = 1;
-            pl.stages = pst;
-            pl.smem = res + pst * half;
-        }
-    }
     if (pl.smem < 120 * 1024) pl.smem = 120 * 1024;  // one CTA per SM: TMEM is sized for one
     uint32_t cols = 32;
     while (cols < (uint32_t)(2 * pl.bn)) cols <<= 1;
     pl.tmem_cols = cols;
     return true;
+}
+
+// The default shape: full-width center tiles (256 columns, or k rounded up
+// to 32), the CTA pair where it applies, as many stages as fit, 16
+// candidates.  A shape forced by the tuning thread, or stored by
+// km_tune_tiles for (d, k), replaces it.
+bool make_plan(int d, int k, Plan &pl) {
+    const TilePlan *tp = t_forced_plan;
+    TilePlan stored;
+    if (!tp) {
+        std::lock_guard<std::mutex> lk(g_plans.m);
+        auto it = g_plans.choice.find(std::make_pair(d, k));
+        if (it != g_plans.choice.end()) {
+            stored = it->second;
+            tp = &stored;
+        }
+    }
+    if (tp) {
+        if (tp->bn <= pick_bn(k) && build_plan(d, tp->bn, tp->pair != 0, tp->stages, tp->list_len, pl)) return true;
+        if (t_forced_plan) return false;
+    }
+    const int bn = pick_bn(k);
+    if (bn == 256 && pair_wanted() && build_plan(d, bn, true, 0, kL, pl)) return true;
+    return build_plan(d, bn, false, 0, kL, pl);
 }
 
 bool device_is_sm10x() {
@@ -1357,6 +1402,53 @@ int64_t prep_blocks(int64_t rows) {
 bool tc_plan_exists(int d, int k) {
     Plan pl;
     return make_plan(d, k, pl);
+}
+
+void tc_enumerate_plans(int d, int k, std::vector<TilePlan> &out) {
+    out.clear();
+    const int bn_max = pick_bn(k);
+    for (int bn : {256, 128, 64}) {
+        if (bn > bn_max) continue;
+        for (int pair = 1; pair >= 0; --pair) {
+            Plan full;
+            if (!build_plan(d, bn, pair != 0, 0, kL, full)) continue;
+            // the fullest ring, and shallower ones down to two (three for pairs)
+            std::vector<int> st = {full.stages};
+            for (int q : {4, 3, 2})
+                if (q < full.stages && (pair == 0 || q >= 3)) st.push_back(q);
+            for (int q : st)
+                for (int len : {16, 8}) {
+                    Plan pl;
+                    if (build_plan(d, bn, pair != 0, q, len, pl)) out.push_back(TilePlan{bn, pair, pl.stages, len});
+                }
+        }
+    }
+    if (bn_max < 64) {
+        Plan pl;
+        for (int len : {16, 8})
+            if (build_plan(d, bn_max, false, 0, len, pl)) out.push_back(TilePlan{bn_max, 0, pl.stages, len});
+    }
+}
+
+void tc_force_plan(const TilePlan *plan) { t_forced_plan = plan; }
+
+void tc_store_plan(int d, int k, const TilePlan &plan) {
+    std::lock_guard<std::mutex> lk(g_plans.m);
+    g_plans.choice[std::make_pair(d, k)] = plan;
+}
+
+void tc_clear_plans() {
+    std::lock_guard<std::mutex> lk(g_plans.m);
+    g_plans.choice.clear();
+}
+
+bool tc_current_plan(int d, int k, TilePlan *out, bool *tuned) {
+    Plan pl;
+    if (!make_plan(d, k, pl)) return false;
+    *out = TilePlan{pl.bn, pl.pair, pl.stages, pl.list_len};
+    std::lock_guard<std::mutex> lk(g_plans.m);
+    *tuned = g_plans.choice.count(std::make_pair(d, k)) > 0;
+    return true;
 }
 
 bool tc_supported(int d, int k) {
@@ -1512,13 +1604,17 @@ int tc_assign_impl(const float *X, int64_t n, int d, const float *C, int k, int3
     static std::once_flag attr_once;
     static cudaError_t attr_err = cudaSuccess;
     std::call_once(attr_once, [] {
-        attr_err = cudaFuncSetAttribute(tc_assign_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        kSmemLimit);
-        if (attr_err == cudaSuccess)
-            attr_err = cudaFuncSetAttribute(tc_assign_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                            kSmemLimit);
+        const void *fns[4] = {(const void *)tc_assign_kernel<false, 16>, (const void *)tc_assign_kernel<true, 16>,
+                              (const void *)tc_assign_kernel<false, 8>, (const void *)tc_assign_kernel<true, 8>};
+        for (const void *f : fns)
+            if (attr_err == cudaSuccess)
+                attr_err = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemLimit);
     });
     KM_CUDA(attr_err);
+    const void *kfn = pl.pair ? (pl.list_len == 8 ? (const void *)tc_assign_kernel<true, 8>
+                                                  : (const void *)tc_assign_kernel<true, 16>)
+                              : (pl.list_len == 8 ? (const void *)tc_assign_kernel<false, 8>
+                                                  : (const void *)tc_assign_kernel<false, 16>);
 
     CUtensorMap tmA, tmB;
     KM_TRY(make_map(&tmA, b.xh, n, b.kp, kBM, kKC, CU_TENSOR_MAP_SWIZZLE_128B, b.bf16 != 0));
@@ -1587,18 +1683,18 @@ int tc_assign_impl(const float *X, int64_t n, int d, const float *C, int k, int3
         cfg.attrs = attr;
         cfg.numAttrs = 1;
         static std::mutex cl_mu;
-        static int cached_smem = -1, cached_clusters = 0;
+        static std::map<std::pair<int, int>, int> cached_clusters;  // (smem, list length) -> clusters
         int clusters_fit = 0;
         {
             std::lock_guard<std::mutex> lk(cl_mu);
-            if (cached_smem != pl.smem) {
+            auto it = cached_clusters.find(std::make_pair(pl.smem, pl.list_len));
+            if (it == cached_clusters.end()) {
                 cfg.gridDim = dim3((unsigned)(2 * (num_sms() / 2)), 1, 1);
                 int nc = 0;
-                KM_CUDA(cudaOccupancyMaxActiveClusters(&nc, tc_assign_kernel<true>, &cfg));
-                cached_clusters = nc;
-                cached_smem = pl.smem;
+                KM_CUDA(cudaOccupancyMaxActiveClusters(&nc, kfn, &cfg));
+                it = cached_clusters.emplace(std::make_pair(pl.smem, pl.list_len), nc).first;
             }
-            clusters_fit = cached_clusters;
+            clusters_fit = it->second;
         }
         if (clusters_fit < 1) {
             set_error("no CTA pair of the tensor-core kernel fits on this device");
@@ -1608,12 +1704,18 @@ int tc_assign_impl(const float *X, int64_t n, int d, const float *C, int k, int3
         int64_t clusters = clusters_fit;
         if (clusters > n_units) clusters = n_units;
         cfg.gridDim = dim3((unsigned)(2 * clusters), 1, 1);
-        KM_CUDA(cudaLaunchKernelEx(&cfg, tc_assign_kernel<true>, tmA, tmB, p));
+        if (pl.list_len == 8)
+            KM_CUDA(cudaLaunchKernelEx(&cfg, tc_assign_kernel<true, 8>, tmA, tmB, p));
+        else
+            KM_CUDA(cudaLaunchKernelEx(&cfg, tc_assign_kernel<true, 16>, tmA, tmB, p));
     } else {
         const int64_t n_ftiles = (n + kBM - 1) / kBM;
         int64_t grid = num_sms();
         if (grid > n_ftiles) grid = n_ftiles;
-        tc_assign_kernel<false><<<(unsigned)grid, kThreadsTC, pl.smem, s>>>(tmA, tmB, p);
+        if (pl.list_len == 8)
+            tc_assign_kernel<false, 8><<<(unsigned)grid, kThreadsTC, pl.smem, s>>>(tmA, tmB, p);
+        else
+            tc_assign_kernel<false, 16><<<(unsigned)grid, kThreadsTC, pl.smem, s>>>(tmA, tmB, p);
     }
     KM_CUDA(cudaGetLastError());
     if (prof) prof->end(kProfTc, s);

@@ -1283,9 +1283,125 @@ int km_tune(const float *X, int64_t n, int32_t d, const float *C, int32_t k, voi
     return KM_OK;
 }
 
+namespace {
+// Clears the thread's forced tile shape when a tuning call returns.
+struct ForcedPlanGuard {
+    ~ForcedPlanGuard() { tc_force_plan(nullptr); }
+};
+thread_local TilePlan t_debug_plan;
+}  // namespace
+
+int km_tune_tiles(const float *X, int64_t n, int32_t d, const float *C, int32_t k, int32_t precision,
+                  void *workspace, size_t workspace_bytes, km_tile_plan *best, km_tile_plan *tried,
+                  int32_t max_tried, int32_t *n_tried, void *stream) {
+    KM_TRY(check_shape(n, d, k));
+    if (n < 1 || !X || !C || !best) {
+        set_error("km_tune_tiles needs n >= 1 and non-NULL X, C, best");
+        return KM_ERR_BAD_SHAPE;
+    }
+    if (precision != KM_PREC_FP16 && precision != KM_PREC_BF16) {
+        set_error("km_tune_tiles tunes the tensor-core precisions (KM_PREC_FP16, KM_PREC_BF16)");
+        return KM_ERR_BAD_SHAPE;
+    }
+    if (!tc_supported(d, k)) {
+        set_error("no tensor-core kernel for d=%d, k=%d on this device", d, k);
+        return KM_ERR_UNSUPPORTED;
+    }
+    KM_TRY(check_ws(workspace, workspace_bytes, km_tune_workspace_size(n, d, k)));
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cap) == cudaSuccess && cap != cudaStreamCaptureStatusNone) {
+        set_error("km_tune_tiles synchronises and cannot run while the stream is captured");
+        return KM_ERR_BAD_SHAPE;
+    }
+    std::vector<TilePlan> cands;
+    tc_enumerate_plans(d, k, cands);
+    if (cands.empty()) {
+        set_error("no tile shape fits d=%d, k=%d", d, k);
+        return KM_ERR_UNSUPPORTED;
+    }
+    Carver cv(workspace);
+    int32_t *labels = cv.take<int32_t>(n);
+    const size_t ws_bytes = assign_ws_bytes(n, d, k, KM_PREC_FP16);
+    void *ws = cv.take<char>(ws_bytes);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    KM_CUDA(cudaEventCreate(&e0));
+    cudaError_t ce = cudaEventCreate(&e1);
+    if (ce != cudaSuccess) {
+        cudaEventDestroy(e0);
+        return cuda_fail(ce, "cudaEventCreate");
+    }
+    ForcedPlanGuard guard;
+    int st = KM_OK;
+    int ibest = -1;
+    double tbest = 0.0;
+    if (n_tried) *n_tried = 0;
+    for (size_t c = 0; c < cands.size() && st == KM_OK; ++c) {
+        tc_force_plan(&cands[c]);
+        // one warm-up call, then the mean of three
+        st = assign_impl(X, n, d, C, k, precision, labels, ws, ws_bytes, nullptr, s);
+        if (st == KM_OK) st = cudaEventRecord(e0, s) == cudaSuccess ? KM_OK : KM_ERR_CUDA;
+        for (int r = 0; r < 3 && st == KM_OK; ++r)
+            st = assign_impl(X, n, d, C, k, precision, labels, ws, ws_bytes, nullptr, s);
+        float t = 0.0f;
+        if (st == KM_OK) {
+            cudaError_t e = cudaEventRecord(e1, s);
+            if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&t, e0, e1);
+            if (e != cudaSuccess) st = cuda_fail(e, "timing a tile shape");
+        }
+        if (st != KM_OK) break;
+        const double ms = t / 3.0;
+        if (tried && n_tried && *n_tried < max_tried) {
+            tried[*n_tried] = km_tile_plan{cands[c].bn, cands[c].pair, cands[c].stages, cands[c].list_len, ms};
+            *n_tried += 1;
+        }
+        if (ibest < 0 || ms < tbest) {
+            ibest = (int)c;
+            tbest = ms;
+        }
+    }
+    tc_force_plan(nullptr);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (st != KM_OK) return st;
+    const TilePlan &b = cands[ibest];
+    tc_store_plan(d, k, b);
+    *best = km_tile_plan{b.bn, b.pair, b.stages, b.list_len, tbest};
+    return KM_OK;
+}
+
+int km_tile_plan_get(int32_t d, int32_t k, km_tile_plan *plan, int32_t *tuned) {
+    KM_TRY(check_shape(1, d, k));
+    if (!plan) {
+        set_error("plan must be non-NULL");
+        return KM_ERR_BAD_SHAPE;
+    }
+    TilePlan tp;
+    bool tu = false;
+    if (!tc_current_plan(d, k, &tp, &tu)) {
+        set_error("no tile shape fits d=%d, k=%d", d, k);
+        return KM_ERR_UNSUPPORTED;
+    }
+    *plan = km_tile_plan{tp.bn, tp.pair, tp.stages, tp.list_len, 0.0};
+    if (tuned) *tuned = tu ? 1 : 0;
+    return KM_OK;
+}
+
+int km_debug_force_tile_plan(const km_tile_plan *plan) {
+    if (!plan) {
+        tc_force_plan(nullptr);
+        return KM_OK;
+    }
+    t_debug_plan = TilePlan{plan->bn, plan->pair, plan->stages, plan->list_len};
+    tc_force_plan(&t_debug_plan);
+    return KM_OK;
+}
+
 int km_tune_clear(void) {
     std::lock_guard<std::mutex> lk(g_tune.m);
     g_tune.choice.clear();
+    tc_clear_plans();
     return KM_OK;
 }
 

@@ -6,6 +6,7 @@
 #include <stdint.h>
 
 #include <cstddef>
+#include <vector>
 
 #include "../../include/kmgpu.h"
 
@@ -114,6 +115,22 @@ int run_kmpp(const float *X, int64_t n, int d, int k, uint32_t seed, float *C0, 
 // Tensor-core (tcgen05, FP16 operands) assignment with exact FP32 recheck.
 bool tc_supported(int d, int k);   // a plan exists and the device is sm_10x
 bool tc_plan_exists(int d, int k); // shape check only (no device query)
+
+// Tile shape of the tensor-core kernel: center columns per tile, CTA pair
+// (0/1), TMA ring stages, candidates kept per frame (8 or 16).
+struct TilePlan {
+    int bn = 0, pair = 0, stages = 0, list_len = 0;
+};
+// Every shape that fits for (d, k), widest first.
+void tc_enumerate_plans(int d, int k, std::vector<TilePlan> &out);
+// While set (nullptr clears), tensor-core calls of this host thread use
+// `plan` (and fail with KM_ERR_UNSUPPORTED when it does not fit).
+void tc_force_plan(const TilePlan *plan);
+// The shape later calls use for (d, k) (km_tune_tiles' choice).
+void tc_store_plan(int d, int k, const TilePlan &plan);
+void tc_clear_plans();
+// The shape a call for (d, k) uses now; *tuned: it comes from the table.
+bool tc_current_plan(int d, int k, TilePlan *out, bool *tuned);
 size_t tc_frames_ws_size(int64_t n, int d);     // fp16 frame copy + norms
 size_t tc_centers_ws_size(int d, int k);        // fp16 centers + norms + shift + scalars
 size_t tc_assign_ws_size(int64_t n, int d, int k);  // candidate lists + counters
