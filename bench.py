@@ -583,6 +583,24 @@ def _lloyd_rate(torch, _lib, X, C0, steps, precision):
     return e0.elapsed_time(e1) / steps, prof
 
 
+def tile_tuning(torch, _lib, X, C0, steps):
+    """The fixed tile plan's Lloyd iteration against the one km_tune_tiles
+    picks for (d, k) on these frames; the table is cleared afterwards."""
+    d, k = X.shape[1], C0.shape[0]
+    _lib.tune_clear()
+    fixed = _lib.tile_plan(d, k)
+    ms_fixed, _ = _lloyd_rate(torch, _lib, X, C0, steps, "fp16")
+    r = _lib.tune_tiles(X, C0)
+    tuned = _lib.tile_plan(d, k)
+    ms_tuned, _ = _lloyd_rate(torch, _lib, X, C0, steps, "fp16")
+    lab_t, _ = _lib.assign(X, C0, precision="fp16")
+    _lib.tune_clear()
+    lab_f, _ = _lib.assign(X, C0, precision="fp16")
+    return {"fixed_plan": fixed, "fixed_ms_per_iter": ms_fixed, "tuned_plan": tuned, "tuned_ms_per_iter": ms_tuned,
+            "speedup": ms_fixed / ms_tuned, "labels_identical": bool(torch.equal(lab_t, lab_f)),
+            "assign_ms_by_plan": [dict(t) for t in r["tried"]]}
+
+
 def run_c1(args):
     """100,000 x 2, k=50, kmeans++ (fixed_seed=42), max_iter=100, tol 1e-5, then dtrajs."""
     import torch
@@ -635,6 +653,8 @@ def run_c2(args):
     lab_32, _ = _lib.assign(X, C0, precision="fp32")
     same = bool(torch.equal(lab_a, lab_32))
     del lab_a, lab_32
+    # tile shapes: the fixed plan against km_tune_tiles' choice for (10, 1000)
+    tiles = tile_tuning(torch, _lib, X, C0, args.steps)
     flops = 2.0 * n * 1000 * 10
     fp32_ms = prof32["fp32"][0] / max(1, prof32["fp32"][1])
     peak = _fp32_sgemm_tflops(torch)
@@ -676,6 +696,7 @@ def run_c2(args):
                                   "(%d frames), d=10, k=1000, one CUDA graph per Lloyd iteration" % n,
                       "lengths": [len(t) for t in trajs]},
            "labels_identical_to_fp32": same, "recheck_fraction": st_a["n_recheck"] / float(n),
+           "tile_tuning": tiles,
            "roofline": {"bound": "tensor-core epilogue (K = 10 padded to 64: 2 n k d is 16% of the MMA work)",
                         "kernel": "tc_assign_kernel", "achieved": flops / (tc_ms / 1e3) / 1e12 if tc_ms else None,
                         "peak": tpeak, "unit": "TFLOP/s",
@@ -777,7 +798,7 @@ def run_c4(args):
             C0 = X[torch.randperm(n, device="cuda", generator=g)[:k]].contiguous()
             row = {"d": d, "k": k}
             steps = 2
-            for prec in ("fp32", "fp16", "bf16"):
+            for prec in ("fp32", "fp16", "bf16", "fp8"):
                 try:
                     ms, prof = _lloyd_rate(torch, _lib, X, C0, steps, prec)
                     row[prec + "_ms_per_iter"] = ms
@@ -792,19 +813,24 @@ def run_c4(args):
                 row["full_recheck_fraction"] = st["n_full"] / float(n)
                 row["labels_identical"] = bool(torch.equal(lab16, lab32))
                 row["tflops_fp16_iter"] = 2.0 * n * k * d / (row["fp16_ms_per_iter"] / 1e3) / 1e12
-                if row.get("bf16_ms_per_iter"):
-                    labb, stb = _lib.assign(X, C0, precision="bf16")
-                    row["bf16_recheck_fraction"] = (stb["n_recheck"] + stb["n_full"]) / float(n)
-                    row["bf16_labels_identical"] = bool(torch.equal(labb, lab32))
-                    del labb
+                for other in ("bf16", "fp8"):
+                    if row.get(other + "_ms_per_iter"):
+                        labb, stb = _lib.assign(X, C0, precision=other)
+                        row[other + "_recheck_fraction"] = (stb["n_recheck"] + stb["n_full"]) / float(n)
+                        row[other + "_full_recheck_fraction"] = stb["n_full"] / float(n)
+                        row[other + "_labels_identical"] = bool(torch.equal(labb, lab32))
+                        del labb
+                tt = tile_tuning(torch, _lib, X, C0, steps)
+                row["tile_tuning"] = {key: tt[key] for key in ("fixed_plan", "fixed_ms_per_iter", "tuned_plan",
+                                                               "tuned_ms_per_iter", "speedup", "labels_identical")}
             rows.append(row)
             del X, C0
             torch.cuda.empty_cache()
     _emit({"metric": "Lloyd iteration time per precision (precision sweep)", "unit": "ms", "n_gpus": 1,
            "higher_is_better": False,
            "config": {"workload": "c4: 1,000,000 frames, 4k Gaussian clusters (sigma 0.3, means U[-5,5]^d), "
-                                  "d in {16,64,256,1024}, k in {100,1000,5000}; fp32 exact vs fp16 and bf16 tensor "
-                                  "cores with exact recheck"},
+                                  "d in {16,64,256,1024}, k in {100,1000,5000}; fp32 exact vs fp16, bf16 and fp8 "
+                                  "(e4m3, per-frame scales) tensor cores with exact recheck"},
            "rows": rows})
 
 

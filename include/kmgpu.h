@@ -58,8 +58,19 @@ typedef enum {
  *                 for bit.
  *   KM_PREC_BF16: the same with BF16 operands (8-bit mantissa: a wider bound,
  *                 so more frames are re-checked; same labels).
+ *   KM_PREC_FP8:  the same with FP8 e4m3 operands (tcgen05 kind::f8f6f4):
+ *                 each frame scaled by its own power of two, the centers by
+ *                 one; the center norms are applied in the epilogue.  A
+ *                 3-bit mantissa makes the bound wide, so most frames are
+ *                 re-checked; same labels.
  *   KM_PREC_AUTO: the library picks by (d, k) (km_tune can measure it). */
-typedef enum { KM_PREC_FP32 = 0, KM_PREC_FP16 = 1, KM_PREC_AUTO = 2, KM_PREC_BF16 = 3 } km_precision;
+typedef enum {
+    KM_PREC_FP32 = 0,
+    KM_PREC_FP16 = 1,
+    KM_PREC_AUTO = 2,
+    KM_PREC_BF16 = 3,
+    KM_PREC_FP8 = 4
+} km_precision;
 
 /* Progress hook, called on the calling host thread (kmeans.py:241-251
  * passes callback_init_centers / callback_loop into the native fit). */
@@ -109,16 +120,18 @@ int km_assign(const float *X, int64_t n, int32_t d, const float *C, int32_t k, i
               void *stream);
 
 /* ---- diagnostics: tensor-core distances (no reference counterpart) --------
- * Runs the KM_PREC_FP16 assignment (labels as km_assign).  V (device, n*k
+ * Runs the assignment in a tensor-core precision (KM_PREC_FP16, KM_PREC_BF16
+ * or KM_PREC_FP8; labels as km_assign).  V (device, n*k
  * floats, nullable) receives the tensor-core approximation of every squared
  * distance, V[i*k + j]; the tests use it to check the error bound pair by
  * pair.  wait_cycles (host, 8 counters, nullable) receives the SM cycles the
  * kernel's roles spent waiting: producer on free B / A buffers, MMA issuer on
  * loaded B / A and on a drained accumulator, epilogue on a ready
  * accumulator, then the epilogue's and the MMA issuer's total cycles.
- * Workspace as km_assign with KM_PREC_FP16. */
-int km_debug_tc_distances(const float *X, int64_t n, int32_t d, const float *C, int32_t k, float *V,
-                          int32_t *labels, uint64_t *wait_cycles, void *workspace, size_t workspace_bytes,
+ * Workspace as km_assign with KM_PREC_FP16 (enough for every tensor-core
+ * precision). */
+int km_debug_tc_distances(const float *X, int64_t n, int32_t d, const float *C, int32_t k, int32_t precision,
+                          float *V, int32_t *labels, uint64_t *wait_cycles, void *workspace, size_t workspace_bytes,
                           void *stream);
 
 /* ---- batched assignment of uneven trajectories --------------------------

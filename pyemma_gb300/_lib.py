@@ -12,7 +12,7 @@ import numpy as np
 
 from . import _build
 
-PRECISIONS = {"fp32": 0, "fp16": 1, "auto": 2, "bf16": 3}
+PRECISIONS = {"fp32": 0, "fp16": 1, "auto": 2, "bf16": 3, "fp8": 4}
 PRECISION_NAMES = {v: k for k, v in PRECISIONS.items()}
 
 KM_OK = 0
@@ -129,7 +129,7 @@ def load(build_if_missing=False):
     L.km_assign_workspace_size.argtypes = [i64, i32, i32, i32]
     L.km_assign_workspace_size.restype = sz
     L.km_assign.argtypes = [P, i64, i32, P, i32, i32, P, P, sz, ctypes.POINTER(AssignStats), P]
-    L.km_debug_tc_distances.argtypes = [P, i64, i32, P, i32, P, P, P, P, sz, P]
+    L.km_debug_tc_distances.argtypes = [P, i64, i32, P, i32, i32, P, P, P, P, sz, P]
     L.km_debug_tc_distances.restype = ctypes.c_int
     L.km_batch_assign.argtypes = [P, P, i32, i32, P, i32, i32, P, P, sz, ctypes.POINTER(AssignStats), P]
     L.km_update_workspace_size.argtypes = [i64, i32, i32]
@@ -292,9 +292,10 @@ WAIT_SLOTS = ("producer_b", "producer_a", "mma_b", "mma_a", "mma_acc", "epilogue
               "mma_total")
 
 
-def debug_tc_distances(X, C, distances=True):
-    """(labels, V or None, wait cycles): the tensor-core assignment, its n x k
-    approximate distances and the cycles each kernel role spent waiting."""
+def debug_tc_distances(X, C, distances=True, precision="fp16"):
+    """(labels, V or None, wait cycles): the tensor-core assignment in the
+    given precision (fp16, bf16 or fp8), its n x k approximate distances and
+    the cycles each kernel role spent waiting."""
     torch = _torch()
     L = load()
     _check_frames(torch, X)
@@ -306,8 +307,8 @@ def debug_tc_distances(X, C, distances=True):
     ws_bytes = L.km_assign_workspace_size(n, d, k, PRECISIONS["fp16"])
     ws = _workspace(torch, ws_bytes, X.device)
     wait = (ctypes.c_uint64 * 8)()
-    check(L.km_debug_tc_distances(_ptr(X), n, d, _ptr(C), k, _ptr(V), _ptr(labels), wait, _ptr(ws), ws_bytes,
-                                  _stream(torch, X.device)))
+    check(L.km_debug_tc_distances(_ptr(X), n, d, _ptr(C), k, precision_code(precision), _ptr(V), _ptr(labels), wait,
+                                  _ptr(ws), ws_bytes, _stream(torch, X.device)))
     return labels, V, dict(zip(WAIT_SLOTS, list(wait)))
 
 

@@ -53,6 +53,7 @@
 
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
+#include <cuda_fp8.h>
 
 #include <cmath>
 #include <cstdlib>
@@ -96,6 +97,7 @@ struct TcParams {
     float g_ratio;  // sqrt(g_hi / g_lo), inflated
     const float4 *xnorm;
     const float2 *cnorm;
+    const float *chn;  // FP8: -||c~_j||^2 / 2 per center
     const uint32_t *scal;
     int32_t *labels;
     int32_t *rc_frames;
@@ -232,6 +234,18 @@ __device__ __forceinline__ void mma_f16(uint32_t d_tmem, uint64_t adesc, uint64_
         : "memory");
 }
 
+// FP8 (e4m3 x e4m3 -> F32): the same operand layout, 32 elements (32 bytes)
+// per K step.
+__device__ __forceinline__ void mma_f8(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                        uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
 __device__ __forceinline__ void mma_commit(uint64_t *bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                      smem_u32(bar))
@@ -330,6 +344,34 @@ __device__ __forceinline__ void mma_f16_pair(uint32_t d_tmem, uint64_t adesc, ui
         : "memory");
 }
 
+__device__ __forceinline__ void mma_f8_pair(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                             uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::2.kind::f8f6f4 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+template <bool F8>
+__device__ __forceinline__ void mma_op(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                       uint32_t accumulate) {
+    if constexpr (F8)
+        mma_f8(d_tmem, adesc, bdesc, idesc, accumulate);
+    else
+        mma_f16(d_tmem, adesc, bdesc, idesc, accumulate);
+}
+
+template <bool F8>
+__device__ __forceinline__ void mma_op_pair(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                            uint32_t accumulate) {
+    if constexpr (F8)
+        mma_f8_pair(d_tmem, adesc, bdesc, idesc, accumulate);
+    else
+        mma_f16_pair(d_tmem, adesc, bdesc, idesc, accumulate);
+}
+
 // Arrive on the barrier at this offset in both CTAs of the pair once the
 // issuing thread's earlier MMAs are complete.
 __device__ __forceinline__ void mma_commit_pair(uint64_t *bar) {
@@ -370,7 +412,8 @@ __device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
 }
 
 // Instruction descriptor of kind::f16: FP16 x FP16 (or BF16 x BF16) -> F32,
-// both K-major.
+// both K-major.  The operand-type code 0 is E4M3 under kind::f8f6f4, so the
+// FP16 descriptor also serves the FP8 MMA.
 __host__ __device__ constexpr uint32_t make_idesc(int M, int N, bool bf16 = false) {
     return (1u << 4) | (bf16 ? ((1u << 7) | (1u << 10)) : 0u) | ((uint32_t)(N >> 3) << 17) |
            ((uint32_t)(M >> 4) << 24);
@@ -672,6 +715,178 @@ __global__ void prep_centers_kernel(const float *__restrict__ C, int k, int k_pa
 }
 
 // ---------------------------------------------------------------------------
+// FP8 (e4m3) operands.  e4m3 has 3 mantissa bits and spans 2^-9 .. 448, too
+// narrow to carry the center norms in extra GEMM columns, so the epilogue
+// adds -||c~_j||^2 / 2 itself.  A frame row may take its own power-of-two
+// scale s_i (a row's scale does not change its argmin): max |x'| s_i lies in
+// [128, 256).  The centers share one scale t with max |c'| t in [128, 256).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint8_t to_e4m3(float v) {
+    return (uint8_t)__nv_cvt_float_to_fp8(v, __NV_SATFINITE, __NV_E4M3);
+}
+
+__device__ __forceinline__ float from_e4m3(uint8_t q) {
+    const __half_raw h = __nv_cvt_fp8_to_halfraw((__nv_fp8_storage_t)q, __NV_E4M3);
+    return __half2float(__half(h));
+}
+
+// The power of two s with m s in [128, 256) (m > 0 finite), else 0.
+__device__ __forceinline__ float fp8_scale_for(float m) {
+    if (!(m > 0.0f) || !(m <= 3.4028234663852886e38f)) return 0.0f;
+    int e;
+    frexpf(m, &e);  // 2^(e-1) <= m < 2^e
+    const int sigma = 8 - e;
+    if (sigma > 126 || sigma < -126) return 0.0f;
+    return ldexpf(1.0f, sigma);
+}
+
+// max |c'_jf| over all centers (float bits; a NaN poisons it to +inf).
+__global__ void center_absmax_kernel(const float *__restrict__ C, int k, int d, const float *__restrict__ shift,
+                                     uint32_t *__restrict__ scal) {
+    float m = 0.0f;
+    const int64_t total = (int64_t)k * d;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+        const float a = fabsf(__fsub_rn(C[e], shift[e % d]));
+        m = a == a ? fmaxf(m, a) : __int_as_float(0x7f800000);
+    }
+    for (int off = 16; off > 0; off >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, off));
+    if ((threadIdx.x & 31) == 0 && m > 0.0f) atomicMax(&scal[kScaleMax], __float_as_uint(m));
+}
+
+// t for the FP8 centers (1 when they coincide or are not finite).
+__global__ void scale_fp8_finalize_kernel(uint32_t *__restrict__ scal) {
+    const float t = fp8_scale_for(__uint_as_float(scal[kScaleMax]));
+    scal[kScale] = __float_as_uint(t > 0.0f ? t : 1.0f);
+    scal[kInvScale2] = __float_as_uint(1.0f);
+}
+
+// Frames: one warp per row.  xnorm = (||x~||^2, upper bound of ||x'||, upper
+// bound of ||x~ - x'||, 1 / (s_i t)), x~ = e4m3(x' s_i) / s_i, in unscaled
+// units.  A row without a usable scale (all zero: s_i = 1; non-finite:
+// infinite bounds, which send it to the exact pass) is still written.
+__global__ void prep_frames_fp8_kernel(const float *__restrict__ X, int64_t n, int d, int kp,
+                                       const float *__restrict__ shift, const uint32_t *__restrict__ scal,
+                                       uint8_t *__restrict__ xq, float4 *__restrict__ xnorm, float norm_inflate) {
+    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    const float t = __uint_as_float(scal[kScale]);
+    for (int64_t i = w; i < n; i += nw) {
+        const float *src = X + i * d;
+        float m = 0.0f;
+        bool bad = false;
+        for (int f = lane; f < d; f += 32) {
+            const float a = fabsf(__fsub_rn(src[f], shift[f]));
+            bad |= !(a <= 3.4028234663852886e38f);
+            m = fmaxf(m, a);
+        }
+        for (int off = 16; off > 0; off >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, off));
+        bad = __any_sync(0xffffffffu, bad);
+        float si = fp8_scale_for(m);
+        if (si == 0.0f) {
+            bad |= m != 0.0f;
+            si = 1.0f;
+        }
+        const float inv_si = 1.0f / si;  // exact: a power of two
+        float hs = 0.0f, hc = 0.0f, s2 = 0.0f, e2 = 0.0f;
+        uint32_t *dst = reinterpret_cast<uint32_t *>(xq + i * kp);
+        for (int f = 4 * lane; f < kp; f += 128) {
+            uint32_t word = 0u;
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const int c = f + e;
+                if (c < d) {
+                    const float a = __fsub_rn(src[c], shift[c]);
+                    const float as = a * si;
+                    const uint8_t q = to_e4m3(as);
+                    const float qv = from_e4m3(q);
+                    word |= (uint32_t)q << (8 * e);
+                    const float xt = qv * inv_si;  // exact
+                    const float y = __fsub_rn(__fmul_rn(xt, xt), hc);
+                    const float tt = __fadd_rn(hs, y);
+                    hc = __fsub_rn(__fsub_rn(tt, hs), y);
+                    hs = tt;
+                    s2 = __fmaf_rn(a, a, s2);
+                    const float ee = qv - as;
+                    e2 = __fmaf_rn(ee, ee, e2);
+                }
+            }
+            dst[f >> 2] = word;
+        }
+        const float th = warp_sum_ff(hs, -hc);
+        const float ts = warp_sum_ff(s2, 0.0f);
+        const float te = warp_sum_ff(e2, 0.0f);
+        if (lane == 0) {
+            const float inf = __int_as_float(0x7f800000);
+            const float inv_st = 1.0f / (si * t);  // exact while si t is a normal float
+            bad |= !(inv_st >= 1.1754943508222875e-38f && inv_st <= 3.4028234663852886e38f);
+            const float sx = bad ? inf : __fsqrt_ru(__fmul_ru(ts, norm_inflate));
+            const float hx = bad ? inf : __fmul_ru(__fadd_ru(__fsqrt_ru(__fmul_ru(te, norm_inflate)), 1e-30f), inv_si);
+            xnorm[i] = make_float4(bad ? 0.0f : th, sx, hx, bad ? 1.0f : inv_st);
+        }
+    }
+}
+
+// Centers: one warp per row of the k_pad-row block.  cnorm = (upper bound of
+// ||c'||, upper bound of ||c~ - c'||), chn = -||c~||^2 / 2 (in double, then
+// rounded), c~ = e4m3(c' t) / t.  A center that e4m3 cannot represent
+// poisons cmax (every frame then takes the exact path).
+__global__ void prep_centers_fp8_kernel(const float *__restrict__ C, int k, int k_pad, int d, int kp,
+                                        const float *__restrict__ shift, uint32_t *__restrict__ scal,
+                                        uint8_t *__restrict__ cq, float2 *__restrict__ cnorm, float *__restrict__ chn,
+                                        float norm_inflate) {
+    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    const float t = __uint_as_float(scal[kScale]);
+    const float inv_t = 1.0f / t;
+    for (int64_t j = w; j < k; j += nw) {
+        const float *src = C + j * d;
+        uint32_t *dst = reinterpret_cast<uint32_t *>(cq + j * kp);
+        double h2 = 0.0;
+        CSum s2, e2;
+        for (int f = 4 * lane; f < kp; f += 128) {
+            uint32_t word = 0u;
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const int c = f + e;
+                if (c < d) {
+                    const float a = __fsub_rn(src[c], shift[c]);
+                    const float at = a * t;
+                    const uint8_t q = to_e4m3(at);
+                    const float qv = from_e4m3(q);
+                    word |= (uint32_t)q << (8 * e);
+                    const double ct = (double)qv * (double)inv_t;
+                    h2 += ct * ct;
+                    s2.add(a * a);
+                    const float ee = qv - at;
+                    e2.add(ee * ee);
+                }
+            }
+            dst[f >> 2] = word;
+        }
+        const double tot = warp_sum_d(h2);
+        const double ts = warp_sum_d(s2.value());
+        const double te = warp_sum_d(e2.value());
+        if (lane == 0) {
+            const float nrm = __fsqrt_ru(__fmul_ru((float)ts, norm_inflate));
+            const float hc = __fmul_ru(__fadd_ru(__fsqrt_ru(__fmul_ru((float)te, norm_inflate)), 1e-30f), inv_t);
+            cnorm[j] = make_float2(nrm, hc);
+            const float hn = (float)(-0.5 * tot);
+            chn[j] = hn;
+            const bool ok = hn == hn && fabsf(hn) <= 3.4028234663852886e38f && nrm == nrm && hc == hc;
+            atomicMax(&scal[kCmax], ok ? __float_as_uint(nrm) : 0x7f800000u);
+            atomicMax(&scal[kHcMax], ok ? __float_as_uint(hc) : 0x7f800000u);
+        }
+    }
+    for (int64_t j = k + w; j < k_pad; j += nw)
+        if (lane == 0) {
+            cnorm[j] = make_float2(0.0f, 0.0f);
+            chn[j] = 0.0f;
+        }
+}
+
+// ---------------------------------------------------------------------------
 // Main kernel
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ float lo_bound(float v, float E, float R, float g_lo) {
@@ -714,8 +929,11 @@ __device__ __forceinline__ float window_threshold(float best, float xn2, float i
 // own accumulator rows.  All barriers the MMAs wait on live in the leader
 // (the peer's copies and accumulator releases arrive there); the MMA commits
 // arrive in both CTAs.
-// L: candidates kept per frame (a register list; 8 or 16).
-template <bool PAIR, int L>
+// L: candidates kept per frame (a register list; 8 or 16).  F8: e4m3
+// operands (128 elements per 128-byte chunk, kind::f8f6f4); the epilogue
+// turns the accumulator into a_j = acc_j / (s_i t) - ||c~_j||^2 / 2 with the
+// frame's scale s_i and the centers' t, in unscaled units.
+template <bool PAIR, int L, bool F8>
 __global__ void __launch_bounds__(kThreadsTC, 1)
     tc_assign_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                      const TcParams p) {
@@ -742,6 +960,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
     uint32_t *tmem_holder = reinterpret_cast<uint32_t *>(drain + 1);
     volatile uint32_t *abort_flag = tmem_holder + 1;
 
+    constexpr int KC = F8 ? 128 : kKC;  // elements per 128-byte chunk
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
     const uint32_t rank = PAIR ? cluster_ctarank() : 0u;
@@ -811,11 +1030,11 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                         if (elect_one() && ok) {
                             if (PAIR) {
                                 if (leader) mbar_arrive_expect_tx(&a_full[t], 2 * kABytesPerChunk);
-                                tma_load_2d_pair(sA + t * kABytesPerChunk, &tmA, t * kKC, frame_row,
+                                tma_load_2d_pair(sA + t * kABytesPerChunk, &tmA, t * KC, frame_row,
                                                  mapa_shared(smem_u32(&a_full[t]), 0));
                             } else {
                                 mbar_arrive_expect_tx(&a_full[t], kABytesPerChunk);
-                                tma_load_2d(sA + t * kABytesPerChunk, &tmA, t * kKC, frame_row, &a_full[t]);
+                                tma_load_2d(sA + t * kABytesPerChunk, &tmA, t * KC, frame_row, &a_full[t]);
                             }
                         }
                         __syncwarp();
@@ -825,12 +1044,12 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                         uint8_t *st = sB + s * stage_bytes;
                         if (PAIR) {
                             if (leader) mbar_arrive_expect_tx(&b_full[s], 2 * stage_bytes);
-                            tma_load_2d_pair(st, &tmB, t * kKC, ct * p.bn + (int)rank * (p.bn / 2),
+                            tma_load_2d_pair(st, &tmB, t * KC, ct * p.bn + (int)rank * (p.bn / 2),
                                              mapa_shared(smem_u32(&b_full[s]), 0));
                         } else {
                             mbar_arrive_expect_tx(&b_full[s], stage_bytes);
-                            if (stream) tma_load_2d(st, &tmA, t * kKC, frame_row, &b_full[s]);
-                            tma_load_2d(st + b_off, &tmB, t * kKC, ct * p.bn, &b_full[s]);
+                            if (stream) tma_load_2d(st, &tmA, t * KC, frame_row, &b_full[s]);
+                            tma_load_2d(st + b_off, &tmB, t * KC, ct * p.bn, &b_full[s]);
                         }
                         ++issued;
                     }
@@ -914,17 +1133,17 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                     const int steps = t == p.nbst - 1 ? last_steps : 4;
                     if (elect_one() && ok) {
                         if (PAIR) {
-                            mma_f16_pair(d_tmem, a_d, b_d, idesc, t != 0);
+                            mma_op_pair<F8>(d_tmem, a_d, b_d, idesc, t != 0);
 #pragma unroll
                             for (int kk = 1; kk < 4; ++kk)
-                                if (kk < steps) mma_f16_pair(d_tmem, a_d + 2 * kk, b_d + 2 * kk, idesc, 1u);
+                                if (kk < steps) mma_op_pair<F8>(d_tmem, a_d + 2 * kk, b_d + 2 * kk, idesc, 1u);
                             mma_commit_pair(&b_empty[s]);
                             if (last) mma_commit_pair(&a_empty[t]);
                         } else {
-                            mma_f16(d_tmem, a_d, b_d, idesc, t != 0);
+                            mma_op<F8>(d_tmem, a_d, b_d, idesc, t != 0);
 #pragma unroll
                             for (int kk = 1; kk < 4; ++kk)  // 32-byte K steps: +2 in the start-address field
-                                if (kk < steps) mma_f16(d_tmem, a_d + 2 * kk, b_d + 2 * kk, idesc, 1u);
+                                if (kk < steps) mma_op<F8>(d_tmem, a_d + 2 * kk, b_d + 2 * kk, idesc, 1u);
                             mma_commit(&b_empty[s]);
                             if (!stream && last) mma_commit(&a_empty[t]);
                         }
@@ -978,7 +1197,8 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
         const int quarter = warp & 3;
         const int row = quarter * 32 + lane;
         const uint32_t lane_off = (uint32_t)(quarter * 32) << 16;
-        const float inv_s2 = __uint_as_float(p.scal[kInvScale2]);
+        // FP8 works in unscaled units (the epilogue divides by s_i t).
+        const float inv_s2 = F8 ? 1.0f : __uint_as_float(p.scal[kInvScale2]);
         const float s2 = 1.0f / inv_s2;  // exact: a power of two
         const float sc_max = __uint_as_float(p.scal[kCmax]);
         const float hc_max = __uint_as_float(p.scal[kHcMax]);
@@ -1022,8 +1242,21 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                     tmem_wait_ld();
                     const int j0 = ct * p.bn + cc;
                     float v[32];
+                    if (F8) {
+                        // a_j = acc_j / (s_i t) - ||c~_j||^2 / 2 (xn.w = 1 / (s_i t), a power of two)
+                        const float4 *hn = reinterpret_cast<const float4 *>(p.chn + j0);
 #pragma unroll
-                    for (int c = 0; c < 32; ++c) v[c] = __uint_as_float(r[c]);
+                        for (int q = 0; q < 8; ++q) {
+                            const float4 h = __ldg(hn + q);
+                            v[4 * q + 0] = fmaf(__uint_as_float(r[4 * q + 0]), xn.w, h.x);
+                            v[4 * q + 1] = fmaf(__uint_as_float(r[4 * q + 1]), xn.w, h.y);
+                            v[4 * q + 2] = fmaf(__uint_as_float(r[4 * q + 2]), xn.w, h.z);
+                            v[4 * q + 3] = fmaf(__uint_as_float(r[4 * q + 3]), xn.w, h.w);
+                        }
+                    } else {
+#pragma unroll
+                        for (int c = 0; c < 32; ++c) v[c] = __uint_as_float(r[c]);
+                    }
                     if (j0 + 32 > p.k) {
 #pragma unroll
                         for (int c = 0; c < 32; ++c)
@@ -1247,18 +1480,22 @@ EncodeTiledFn get_encode() {
     return fn;
 }
 
-int make_map(CUtensorMap *tm, const void *base, int64_t rows, int kp, int box_rows, int box_k,
-             CUtensorMapSwizzle swizzle, bool bf16) {
+// Tensor map of an operand (rows x kp elements, row-major): boxes of
+// box_rows rows and one 128-byte chunk (64 16-bit or 128 8-bit elements).
+int make_map(CUtensorMap *tm, const void *base, int64_t rows, int kp, int box_rows, const TcBuffers &b,
+             CUtensorMapSwizzle swizzle) {
     EncodeTiledFn enc = get_encode();
     if (!enc) {
         set_error("cuTensorMapEncodeTiled is not available from the driver");
         return KM_ERR_UNSUPPORTED;
     }
     cuuint64_t dims[2] = {(cuuint64_t)kp, (cuuint64_t)rows};
-    cuuint64_t strides[1] = {(cuuint64_t)kp * 2};
-    cuuint32_t box[2] = {(cuuint32_t)box_k, (cuuint32_t)box_rows};
+    cuuint64_t strides[1] = {(cuuint64_t)kp * (cuuint64_t)b.esize};
+    cuuint32_t box[2] = {(cuuint32_t)(128 / b.esize), (cuuint32_t)box_rows};
     cuuint32_t estr[2] = {1, 1};
-    CUresult r = enc(tm, bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2,
+    const CUtensorMapDataType dt = b.fp8 ? CU_TENSOR_MAP_DATA_TYPE_UINT8
+                                         : (b.bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16);
+    CUresult r = enc(tm, dt, 2,
                      const_cast<void *>(base), dims, strides, box, estr,
                      CU_TENSOR_MAP_INTERLEAVE_NONE, swizzle,
                      CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
@@ -1271,6 +1508,8 @@ int make_map(CUtensorMap *tm, const void *base, int64_t rows, int kp, int box_ro
 }
 
 int kp_of(int d) { return (d + 2 + kKC - 1) / kKC * kKC; }
+// FP8 rows: the d features in 128-element (128-byte) chunks; no norm columns.
+int kp8_of(int d) { return (d + 127) / 128 * 128; }
 
 int pick_bn(int k) {
     if (k >= 256) return 256;
@@ -1308,9 +1547,9 @@ bool pair_wanted() {
 // 32, at most 256), the CTA-pair form (bn = 256, resident frame tile only),
 // max_stages caps the TMA ring (0: as many as fit).  False when the shape
 // does not fit.
-bool build_plan(int d, int bn, bool pair, int max_stages, int list_len, Plan &pl) {
+bool build_plan(int d, int bn, bool pair, int max_stages, int list_len, Plan &pl, bool fp8 = false) {
     if (bn < 32 || bn > 256 || bn % 32 || (list_len != 8 && list_len != 16)) return false;
-    pl.nkc = kp_of(d) / kKC;
+    pl.nkc = fp8 ? kp8_of(d) / 128 : kp_of(d) / kKC;
     pl.bn = bn;
     pl.list_len = list_len;
     pl.stream_a = 0;
@@ -1354,7 +1593,7 @@ bool build_plan(int d, int bn, bool pair, int max_stages, int list_len, Plan &pl
 // to 32), the CTA pair where it applies, as many stages as fit, 16
 // candidates.  A shape forced by the tuning thread, or stored by
 // km_tune_tiles for (d, k), replaces it.
-bool make_plan(int d, int k, Plan &pl) {
+bool make_plan(int d, int k, Plan &pl, bool fp8 = false) {
     const TilePlan *tp = t_forced_plan;
     TilePlan stored;
     if (!tp) {
@@ -1366,12 +1605,15 @@ bool make_plan(int d, int k, Plan &pl) {
         }
     }
     if (tp) {
-        if (tp->bn <= pick_bn(k) && build_plan(d, tp->bn, tp->pair != 0, tp->stages, tp->list_len, pl)) return true;
+        // (the FP8 kernel keeps 16 candidates)
+        if (tp->bn <= pick_bn(k) &&
+            build_plan(d, tp->bn, tp->pair != 0, tp->stages, fp8 ? kL : tp->list_len, pl, fp8))
+            return true;
         if (t_forced_plan) return false;
     }
     const int bn = pick_bn(k);
-    if (bn == 256 && pair_wanted() && build_plan(d, bn, true, 0, kL, pl)) return true;
-    return build_plan(d, bn, false, 0, kL, pl);
+    if (bn == 256 && pair_wanted() && build_plan(d, bn, true, 0, kL, pl, fp8)) return true;
+    return build_plan(d, bn, false, 0, kL, pl, fp8);
 }
 
 bool device_is_sm10x() {
@@ -1476,6 +1718,7 @@ size_t tc_centers_ws_size(int d, int k) {
     c.take<float2>(k_pad_of(k));
     c.take<float>(d);
     c.take<uint32_t>(kNumScalars);
+    c.take<float>(k_pad_of(k));
     return c.bytes();
 }
 
@@ -1486,6 +1729,16 @@ void tc_carve_centers(void *ws, int d, int k, TcBuffers &b) {
     b.cnorm = c.take<float2>(k_pad_of(k));
     b.shift = c.take<float>(d);
     b.scal = c.take<uint32_t>(kNumScalars);
+    b.chn = c.take<float>(k_pad_of(k));
+}
+
+// The 16-bit buffers hold kp_of(d) 2-byte elements per row; an FP8 row of
+// kp8_of(d) bytes fits in them.
+void tc_set_operand(TcBuffers &b, int d, int prec) {
+    b.bf16 = prec == KM_PREC_BF16;
+    b.fp8 = prec == KM_PREC_FP8;
+    b.esize = b.fp8 ? 1 : 2;
+    b.kp = b.fp8 ? kp8_of(d) : kp_of(d);
 }
 
 namespace {
@@ -1525,9 +1778,15 @@ int tc_prepare_shift_from_centers(const float *C, int d, int k, TcBuffers &b, cu
     shift_mean_kernel<<<(d + 127) / 128, 128, 0, s>>>(C, d, k, b.shift);
     KM_CUDA(cudaGetLastError());
     KM_CUDA(cudaMemsetAsync(b.scal, 0, kNumScalars * sizeof(uint32_t), s));
-    center_norm_max_kernel<<<(unsigned)prep_blocks(k), 256, 0, s>>>(C, k, d, b.shift, b.scal);
-    KM_CUDA(cudaGetLastError());
-    scale_finalize_kernel<<<1, 1, 0, s>>>(b.scal);
+    if (b.fp8) {
+        center_absmax_kernel<<<(unsigned)prep_blocks(k), 256, 0, s>>>(C, k, d, b.shift, b.scal);
+        KM_CUDA(cudaGetLastError());
+        scale_fp8_finalize_kernel<<<1, 1, 0, s>>>(b.scal);
+    } else {
+        center_norm_max_kernel<<<(unsigned)prep_blocks(k), 256, 0, s>>>(C, k, d, b.shift, b.scal);
+        KM_CUDA(cudaGetLastError());
+        scale_finalize_kernel<<<1, 1, 0, s>>>(b.scal);
+    }
     KM_CUDA(cudaGetLastError());
     return KM_OK;
 }
@@ -1565,7 +1824,10 @@ void prepare_frames_t(const float *X, int64_t n, int d, TcBuffers &b, cudaStream
 
 int tc_prepare_frames(const float *X, int64_t n, int d, TcBuffers &b, cudaStream_t s) {
     if (n == 0) return KM_OK;
-    if (b.bf16)
+    if (b.fp8)
+        prep_frames_fp8_kernel<<<(unsigned)prep_blocks(n), 256, 0, s>>>(
+            X, n, d, b.kp, b.shift, b.scal, static_cast<uint8_t *>(b.xh), b.xnorm, norm_inflate_of(d));
+    else if (b.bf16)
         prepare_frames_t<__nv_bfloat16>(X, n, d, b, s);
     else
         prepare_frames_t<__half>(X, n, d, b, s);
@@ -1576,8 +1838,11 @@ int tc_prepare_frames(const float *X, int64_t n, int d, TcBuffers &b, cudaStream
 int tc_prepare_centers(const float *C, int d, int k, TcBuffers &b, cudaStream_t s) {
     const int kpad = k_pad_of(k);
     KM_CUDA(cudaMemsetAsync(b.scal + kCmax, 0, 2 * sizeof(uint32_t), s));  // kCmax, kHcMax
-    KM_CUDA(cudaMemsetAsync(b.ch, 0, (size_t)kpad * b.kp * 2, s));
-    if (b.bf16)
+    KM_CUDA(cudaMemsetAsync(b.ch, 0, (size_t)kpad * b.kp * b.esize, s));
+    if (b.fp8)
+        prep_centers_fp8_kernel<<<(unsigned)prep_blocks(kpad), 256, 0, s>>>(
+            C, k, kpad, d, b.kp, b.shift, b.scal, static_cast<uint8_t *>(b.ch), b.cnorm, b.chn, norm_inflate_of(d));
+    else if (b.bf16)
         prep_centers_kernel<__nv_bfloat16><<<(unsigned)prep_blocks(kpad), 256, 0, s>>>(
             C, k, kpad, d, b.kp, b.shift, b.scal, reinterpret_cast<__nv_bfloat16 *>(b.ch), b.cnorm,
             norm_inflate_of(d));
@@ -1597,29 +1862,35 @@ int tc_assign_impl(const float *X, int64_t n, int d, const float *C, int k, int3
                    cudaEvent_t ev_fork, const FlipList *fl) {
     if (n == 0) return KM_OK;
     Plan pl;
-    if (!make_plan(d, k, pl) || !device_is_sm10x()) {
+    if (!make_plan(d, k, pl, b.fp8 != 0) || !device_is_sm10x()) {
         set_error("no tensor-core plan for d=%d k=%d on this device", d, k);
         return KM_ERR_UNSUPPORTED;
     }
     static std::once_flag attr_once;
     static cudaError_t attr_err = cudaSuccess;
     std::call_once(attr_once, [] {
-        const void *fns[4] = {(const void *)tc_assign_kernel<false, 16>, (const void *)tc_assign_kernel<true, 16>,
-                              (const void *)tc_assign_kernel<false, 8>, (const void *)tc_assign_kernel<true, 8>};
+        const void *fns[6] = {(const void *)tc_assign_kernel<false, 16, false>,
+                              (const void *)tc_assign_kernel<true, 16, false>,
+                              (const void *)tc_assign_kernel<false, 8, false>,
+                              (const void *)tc_assign_kernel<true, 8, false>,
+                              (const void *)tc_assign_kernel<false, 16, true>,
+                              (const void *)tc_assign_kernel<true, 16, true>};
         for (const void *f : fns)
             if (attr_err == cudaSuccess)
                 attr_err = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemLimit);
     });
     KM_CUDA(attr_err);
-    const void *kfn = pl.pair ? (pl.list_len == 8 ? (const void *)tc_assign_kernel<true, 8>
-                                                  : (const void *)tc_assign_kernel<true, 16>)
-                              : (pl.list_len == 8 ? (const void *)tc_assign_kernel<false, 8>
-                                                  : (const void *)tc_assign_kernel<false, 16>);
+    // (the FP8 kernel keeps 16 candidates: make_plan set list_len)
+    const void *kfn = b.fp8 ? (pl.pair ? (const void *)tc_assign_kernel<true, 16, true>
+                                       : (const void *)tc_assign_kernel<false, 16, true>)
+                            : pl.pair ? (pl.list_len == 8 ? (const void *)tc_assign_kernel<true, 8, false>
+                                                          : (const void *)tc_assign_kernel<true, 16, false>)
+                                      : (pl.list_len == 8 ? (const void *)tc_assign_kernel<false, 8, false>
+                                                          : (const void *)tc_assign_kernel<false, 16, false>);
 
     CUtensorMap tmA, tmB;
-    KM_TRY(make_map(&tmA, b.xh, n, b.kp, kBM, kKC, CU_TENSOR_MAP_SWIZZLE_128B, b.bf16 != 0));
-    KM_TRY(make_map(&tmB, b.ch, k_pad_of(k), b.kp, pl.pair ? pl.bn / 2 : pl.bn, kKC, CU_TENSOR_MAP_SWIZZLE_128B,
-                    b.bf16 != 0));
+    KM_TRY(make_map(&tmA, b.xh, n, b.kp, kBM, b, CU_TENSOR_MAP_SWIZZLE_128B));
+    KM_TRY(make_map(&tmB, b.ch, k_pad_of(k), b.kp, pl.pair ? pl.bn / 2 : pl.bn, b, CU_TENSOR_MAP_SWIZZLE_128B));
 
     KM_CUDA(cudaMemsetAsync(b.counters, 0, 4 * sizeof(int32_t), s));
     KM_CUDA(cudaMemsetAsync(b.flipped, 0, sizeof(unsigned long long), s));
@@ -1632,7 +1903,9 @@ int tc_assign_impl(const float *X, int64_t n, int d, const float *C, int k, int3
     p.d = d;
     p.kp = b.kp;
     p.nkc = pl.nkc;
-    p.ksteps_total = (d + 2 + 15) / 16;
+    // K steps holding data: 16 elements (d features and two norm columns) in
+    // the 16-bit forms, 32 elements (d features) in FP8.
+    p.ksteps_total = b.fp8 ? (d + 31) / 32 : (d + 2 + 15) / 16;
     p.stream_a = pl.stream_a;
     p.nbst = (p.ksteps_total + 3) / 4;
     p.bn = pl.bn;
@@ -1644,6 +1917,15 @@ int tc_assign_impl(const float *X, int64_t n, int d, const float *C, int k, int3
     // (BF16) of it; the bound allows 2^-21 and 2^-17.
     p.bf16 = b.bf16;
     p.e_coef = (float)((gamma_acc * 1.003 + std::ldexp(1.0, b.bf16 ? -17 : -21) + 8.0 * u) * 1.01);
+    if (b.fp8) {
+        // FP8: the accumulation of the e4m3 products in the MMA (its internal
+        // precision is not published; the allowance is 2^-18 of the row norms
+        // per 32-element K step, 8 times the FP16 form's per-step allowance,
+        // and the bound test measures the share the hardware uses), the
+        // epilogue's fused multiply-add and the rounded norms ||x~||^2 and
+        // ||c~||^2 / 2 (16 u of (sx + sc)^2 in all).
+        p.e_coef = (float)((2.0 * p.ksteps_total * std::ldexp(1.0, -18) + 16.0 * u) * 1.25);
+    }
     const double g = (d + 2) * u / (1.0 - (d + 2) * u) * 1.01;
     p.g_lo = (float)((1.0 - g) * (1.0 - 4.0 * u));
     p.g_hi = (float)((1.0 + g) * (1.0 + 4.0 * u));
@@ -1652,6 +1934,7 @@ int tc_assign_impl(const float *X, int64_t n, int d, const float *C, int k, int3
                                INFINITY);
     p.xnorm = b.xnorm;
     p.cnorm = b.cnorm;
+    p.chn = b.chn;
     p.scal = b.scal;
     p.labels = labels;
     p.rc_frames = b.rc_frames;
@@ -1704,18 +1987,22 @@ int tc_assign_impl(const float *X, int64_t n, int d, const float *C, int k, int3
         int64_t clusters = clusters_fit;
         if (clusters > n_units) clusters = n_units;
         cfg.gridDim = dim3((unsigned)(2 * clusters), 1, 1);
-        if (pl.list_len == 8)
-            KM_CUDA(cudaLaunchKernelEx(&cfg, tc_assign_kernel<true, 8>, tmA, tmB, p));
+        if (b.fp8)
+            KM_CUDA(cudaLaunchKernelEx(&cfg, tc_assign_kernel<true, 16, true>, tmA, tmB, p));
+        else if (pl.list_len == 8)
+            KM_CUDA(cudaLaunchKernelEx(&cfg, tc_assign_kernel<true, 8, false>, tmA, tmB, p));
         else
-            KM_CUDA(cudaLaunchKernelEx(&cfg, tc_assign_kernel<true, 16>, tmA, tmB, p));
+            KM_CUDA(cudaLaunchKernelEx(&cfg, tc_assign_kernel<true, 16, false>, tmA, tmB, p));
     } else {
         const int64_t n_ftiles = (n + kBM - 1) / kBM;
         int64_t grid = num_sms();
         if (grid > n_ftiles) grid = n_ftiles;
-        if (pl.list_len == 8)
-            tc_assign_kernel<false, 8><<<(unsigned)grid, kThreadsTC, pl.smem, s>>>(tmA, tmB, p);
+        if (b.fp8)
+            tc_assign_kernel<false, 16, true><<<(unsigned)grid, kThreadsTC, pl.smem, s>>>(tmA, tmB, p);
+        else if (pl.list_len == 8)
+            tc_assign_kernel<false, 8, false><<<(unsigned)grid, kThreadsTC, pl.smem, s>>>(tmA, tmB, p);
         else
-            tc_assign_kernel<false, 16><<<(unsigned)grid, kThreadsTC, pl.smem, s>>>(tmA, tmB, p);
+            tc_assign_kernel<false, 16, false><<<(unsigned)grid, kThreadsTC, pl.smem, s>>>(tmA, tmB, p);
     }
     KM_CUDA(cudaGetLastError());
     if (prof) prof->end(kProfTc, s);

@@ -97,8 +97,8 @@ void ProfEvents::collect() {
 
 namespace {
 
-// The tensor-core precisions (FP16 or BF16 operands, exact re-check).
-inline bool is_tc(int prec) { return prec == KM_PREC_FP16 || prec == KM_PREC_BF16; }
+// The tensor-core precisions (FP16, BF16 or FP8 operands, exact re-check).
+inline bool is_tc(int prec) { return prec == KM_PREC_FP16 || prec == KM_PREC_BF16 || prec == KM_PREC_FP8; }
 
 // Precisions chosen by km_tune, per (d, k).
 struct TuneCache {
@@ -156,7 +156,7 @@ int check_device_errors(uint32_t e) {
 }
 
 // The assignment once the precision is resolved and the workspace checked.
-// For the tensor-core precisions, b holds the carved buffers (b.bf16 set);
+// For the tensor-core precisions, b holds the carved buffers (operand type set);
 // centers_ready means the
 // center half (FP16 copy, norms, shift, scale) is already prepared.
 int assign_core(const float *X, int64_t n, int32_t d, const float *C, int32_t k, int prec, int32_t *labels,
@@ -228,7 +228,7 @@ int assign_impl(const float *X, int64_t n, int32_t d, const float *C, int32_t k,
     TcBuffers b;
     if (is_tc(prec) && n > 0) {
         carve_assign(ws, n, d, k, b);
-        b.bf16 = prec == KM_PREC_BF16;
+        tc_set_operand(b, d, prec);
     }
     return assign_core(X, n, d, C, k, prec, labels, b, false, stats, s);
 }
@@ -318,6 +318,7 @@ int assign_centers_enqueue(const float *X, int64_t n, const km_centers *h, int32
     tc_carve_frames(p, n, h->d, b);
     p += (tc_frames_ws_size(n, h->d) + 255) / 256 * 256;
     tc_carve_assign(p, n, h->d, h->k, b);
+    tc_set_operand(b, h->d, h->prec);
     KM_TRY(tc_prepare_frames(X, n, h->d, b, s));
     KM_TRY(tc_assign(X, n, h->d, h->C, h->k, labels, b, s, nullptr));
     KM_CUDA(cudaMemcpyAsync(err_host, b.err, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
@@ -417,12 +418,16 @@ int km_batch_assign(const float *X_packed, const int64_t *offsets, int32_t n_tra
                        static_cast<cudaStream_t>(stream));
 }
 
-int km_debug_tc_distances(const float *X, int64_t n, int32_t d, const float *C, int32_t k, float *V,
-                          int32_t *labels, uint64_t *wait_cycles, void *workspace, size_t workspace_bytes,
+int km_debug_tc_distances(const float *X, int64_t n, int32_t d, const float *C, int32_t k, int32_t precision,
+                          float *V, int32_t *labels, uint64_t *wait_cycles, void *workspace, size_t workspace_bytes,
                           void *stream) {
     KM_TRY(check_shape(n, d, k));
     if (n > 0 && (!X || !labels || !C)) {
         set_error("X, C and labels must be non-NULL");
+        return KM_ERR_BAD_SHAPE;
+    }
+    if (!is_tc(precision)) {
+        set_error("km_debug_tc_distances runs a tensor-core precision (FP16, BF16 or FP8), not %d", precision);
         return KM_ERR_BAD_SHAPE;
     }
     if (!tc_supported(d, k)) {
@@ -434,6 +439,7 @@ int km_debug_tc_distances(const float *X, int64_t n, int32_t d, const float *C, 
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     TcBuffers b;
     carve_assign(workspace, n, d, k, b);
+    tc_set_operand(b, d, precision);
     KM_TRY(tc_prepare_shift_from_centers(C, d, k, b, s));
     KM_TRY(tc_prepare_centers(C, d, k, b, s));
     KM_TRY(tc_prepare_frames(X, n, d, b, s));
@@ -848,7 +854,7 @@ int lloyd_run(const float *X_in, const HostFrames *hf, int64_t n, int32_t d, int
         // The shift and scale stay fixed for the whole run so that the 16-bit
         // frame copy is made once.
         carve_assign(ws_assign, n, d, k, b);
-        b.bf16 = prec == KM_PREC_BF16;
+        tc_set_operand(b, d, prec);
         KM_TRY(tc_prepare_shift_from_centers(C, d, k, b, s));
         if (!hf) KM_TRY(tc_prepare_frames(X, n, d, b, s));
     }
@@ -1145,7 +1151,7 @@ int km_centers_create(const float *C, int32_t k, int32_t d, int32_t precision, v
     if (e != cudaSuccess) st = cuda_fail(e, "cudaMemcpyAsync (resident centers)");
     if (st == KM_OK && is_tc(prec)) {
         tc_carve_centers(static_cast<char *>(h->mem) + c_bytes, d, k, h->tc);
-        h->tc.bf16 = prec == KM_PREC_BF16;
+        tc_set_operand(h->tc, d, prec);
         st = tc_prepare_shift_from_centers(h->C, d, k, h->tc, s);
         if (st == KM_OK) st = tc_prepare_centers(h->C, d, k, h->tc, s);
     }
@@ -1214,6 +1220,7 @@ int km_assign_centers(const float *X, int64_t n, int32_t d, const km_centers *h,
         tc_carve_frames(p, n, d, b);
         p += (tc_frames_ws_size(n, d) + 255) / 256 * 256;
         tc_carve_assign(p, n, d, h->k, b);
+        tc_set_operand(b, d, h->prec);
     }
     return assign_core(X, n, d, h->C, h->k, h->prec, labels, b, true, stats, static_cast<cudaStream_t>(stream));
 }

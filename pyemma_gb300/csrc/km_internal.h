@@ -158,19 +158,25 @@ struct TcBuffers {
     int32_t *counters = nullptr;  // [0] recheck entries, [1] full entries, [2] pairs
     unsigned long long *flipped = nullptr;
     uint32_t *err = nullptr;
-    int kp = 0;
+    float *chn = nullptr;        // FP8 only: -||c~_j||^2 / 2 per center (the norm is not folded into the GEMM)
+    int kp = 0;        // operand row length in elements
+    int esize = 2;     // operand bytes per element: 2 (FP16, BF16) or 1 (FP8 e4m3)
     int bf16 = 0;      // operand type of xh / ch: 0 FP16, 1 BF16
+    int fp8 = 0;       // 1: e4m3 operands (frames scaled per row), norms applied in the epilogue
     int keep_err = 0;  // 1: tc_assign leaves err as it is (the caller clears it once for several calls)
 };
 
 // The same buffers for frames [a, ...): the per-frame arrays start at row a.
 inline TcBuffers tc_rows_from(const TcBuffers &b, int64_t a) {
     TcBuffers v = b;
-    v.xh = static_cast<char *>(b.xh) + (size_t)a * b.kp * 2;
+    v.xh = static_cast<char *>(b.xh) + (size_t)a * b.kp * b.esize;
     v.xnorm = b.xnorm + a;
     return v;
 }
 
+// Sets the operand type of carved buffers from the precision (KM_PREC_FP16,
+// KM_PREC_BF16 or KM_PREC_FP8): element size and row length.
+void tc_set_operand(TcBuffers &b, int d, int prec);
 void tc_carve_frames(void *ws, int64_t n, int d, TcBuffers &b);
 void tc_carve_centers(void *ws, int d, int k, TcBuffers &b);
 void tc_carve_assign(void *ws, int64_t n, int d, int k, TcBuffers &b);

@@ -145,7 +145,7 @@ def _sweep_data(torch, d, k, n=1_000_000):
 def test_c4_grid_tensor_core_labels_equal_fp32_and_oracle(torch, L, oracle, d, k):
     X, C = _sweep_data(torch, d, k)
     lab32, _ = L.assign(X, C, precision="fp32")
-    for prec in ("fp16", "bf16"):
+    for prec in ("fp16", "bf16", "fp8"):
         lab, _ = L.assign(X, C, precision=prec)
         assert torch.equal(lab, lab32), prec
     rng = np.random.default_rng(SEED + d + k)

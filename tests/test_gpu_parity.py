@@ -45,7 +45,7 @@ def gpu_assign(torch, L, X, C, precision):
     return lab.cpu().numpy(), stats
 
 
-PRECS = ["fp32", "fp16", "bf16"]
+PRECS = ["fp32", "fp16", "bf16", "fp8"]
 
 
 @pytest.mark.parametrize("prec", PRECS)
