@@ -14,6 +14,7 @@
 // and a lexicographic warp-shuffle (distance, index) reduction finishes the
 // argmin.
 #include <algorithm>
+#include <cmath>
 
 #include "km_common.cuh"
 #include "km_internal.h"
@@ -158,44 +159,145 @@ int launch_cfg(const float *X, const int32_t *frame_idx, const int32_t *n_dev, i
     return KM_OK;
 }
 
-// Kernel (b'): exact float32 distances of the candidates of re-checked frames.
-// A key (distance bits << 32 | center) of a non-negative float orders
-// lexicographically as an unsigned integer, so atomicMin keeps the smallest
-// distance and, among equal distances, the lowest center.
+// Kernel (b'): the candidates of re-checked frames.
 //
-// Phase 1 evaluates, for every entry, the candidate with the smallest
-// tensor-core distance.  Phase 2 evaluates the other candidates whose lower
-// bound does not exceed that exact distance (the rest can neither win nor
-// tie).  One thread per evaluation, sqdist_exact over the two rows: the many
-// independent 16-byte loads of each thread keep the memory system busy.
-__global__ void __launch_bounds__(256) recheck_best_kernel(
-    const float *__restrict__ X, int d, const float *__restrict__ C, const int32_t *__restrict__ rc_frames,
-    const int32_t *__restrict__ rc_best, const int32_t *__restrict__ entry_count, int64_t max_entries,
-    unsigned long long *__restrict__ keys) {
-    int64_t count = *entry_count;
-    if (count > max_entries) count = max_entries;
-    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < count;
-         e += (int64_t)gridDim.x * blockDim.x) {
-        const int j = rc_best[e];
-        const float dd = sqdist_exact(X + (int64_t)rc_frames[e] * d, C + (int64_t)j * d, d);
-        keys[e] = ((unsigned long long)__float_as_uint(dd) << 32) | (unsigned)j;
+// Pass 1 (recheck_fast_kernel), one warp per entry: the float32 squared
+// distance F of the frame to each candidate, lanes over the features (16-byte
+// loads where rows allow, coalesced), fused multiply-adds and a shuffle tree.
+// F differs from the oracle's sequential float32 distance D by a factor
+// within [1 - gamma, 1 + gamma] (rounding of the differences, of each lane's
+// n_l fused steps and of the 5 tree sums, against D's d + 2 roundings per
+// term; gamma = (d + n_l + 10) u, inflated).  With Fu = F (1 + gamma) and
+// Fl = F (1 - gamma), a candidate whose Fl exceeds the smallest Fu can
+// neither win nor tie.  The candidate with the best tensor-core value goes
+// first, and a candidate whose tensor-core lower bound already exceeds the
+// smallest Fu so far is not evaluated.  One survivor: the label is settled.
+// Several (or a non-finite F): the entry and its survivors go to pass 2.
+//
+// Pass 2 (recheck_exact_kernel), one thread per surviving candidate:
+// sqdist_exact, the assignment's arithmetic and order; the key
+// (distance bits << 32 | center) of a non-negative float orders
+// lexicographically as an unsigned integer, so atomicMin keeps the smallest
+// distance and, among equal distances, the lowest center.  Then
+// recheck_finalize_kernel over the pass-2 entries.
+
+// Lane sum of (x - c)^2 over the row pair, lanes over features.
+__device__ __forceinline__ float rc_lane_sum(const float *__restrict__ x, const float *__restrict__ c, int d,
+                                             bool vec4, int lane) {
+    float acc = 0.0f;
+    if (vec4) {
+        const float4 *x4 = reinterpret_cast<const float4 *>(x);
+        const float4 *c4 = reinterpret_cast<const float4 *>(c);
+        for (int f = lane; f < (d >> 2); f += 32) {
+            const float4 a = __ldg(x4 + f), b = __ldg(c4 + f);
+            float t = __fsub_rn(a.x, b.x);
+            acc = __fmaf_rn(t, t, acc);
+            t = __fsub_rn(a.y, b.y);
+            acc = __fmaf_rn(t, t, acc);
+            t = __fsub_rn(a.z, b.z);
+            acc = __fmaf_rn(t, t, acc);
+            t = __fsub_rn(a.w, b.w);
+            acc = __fmaf_rn(t, t, acc);
+        }
+    } else {
+        for (int f = lane; f < d; f += 32) {
+            const float t = __fsub_rn(__ldg(x + f), __ldg(c + f));
+            acc = __fmaf_rn(t, t, acc);
+        }
     }
+    return acc;
 }
 
-__global__ void __launch_bounds__(256) recheck_rest_kernel(
+__global__ void __launch_bounds__(256) recheck_fast_kernel(
     const float *__restrict__ X, int d, const float *__restrict__ C, const int32_t *__restrict__ rc_frames,
-    const int32_t *__restrict__ rc_best, const int32_t *__restrict__ pair_entry,
-    const int32_t *__restrict__ pair_center, const float *__restrict__ pair_lo,
-    const int32_t *__restrict__ pair_count, int64_t max_pairs, unsigned long long *__restrict__ keys) {
-    int64_t count = *pair_count;
-    if (count > max_pairs) count = max_pairs;
-    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < count;
-         q += (int64_t)gridDim.x * blockDim.x) {
-        const int e = pair_entry[q];
-        const int j = pair_center[q];
-        if (j == rc_best[e]) continue;
-        const float dstar = __uint_as_float((uint32_t)(keys[e] >> 32));
-        if (pair_lo[q] > dstar) continue;  // false for NaN: evaluated
+    const int32_t *__restrict__ rc_best, const int64_t *__restrict__ rc_pairs, const int32_t *__restrict__ pair_center,
+    const float *__restrict__ pair_lo, const int32_t *__restrict__ entry_count, int64_t max_entries, float gamma_lo,
+    float gamma_hi, int32_t *__restrict__ labels, unsigned long long *flipped, int32_t *__restrict__ flips,
+    int32_t *__restrict__ n_flips, int64_t max_flips, int32_t *__restrict__ amb_entries,
+    int32_t *__restrict__ amb_mask, int32_t *__restrict__ amb_count) {
+    int64_t count = *entry_count;
+    if (count > max_entries) count = max_entries;
+    const int lane = threadIdx.x & 31;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const bool vec4 = (d & 3) == 0 && ((reinterpret_cast<uintptr_t>(X) | reinterpret_cast<uintptr_t>(C)) & 15) == 0;
+    const float kInf = __int_as_float(0x7f800000);
+    unsigned long long nflip = 0;
+    for (int64_t e = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; e < count; e += nw) {
+        const int64_t i = rc_frames[e];
+        const int64_t word = rc_pairs[e];
+        const int64_t q0 = word >> 8;
+        const int m = (int)(word & 0xFF);
+        const int jb = rc_best[e];
+        const float *x = X + i * d;
+        // Lane t (< m) holds candidate t's bracket; unevaluated: Fl = +inf.
+        float my_fl = kInf;
+        bool my_bad = false;
+        int my_j = -1;
+        if (lane < m) my_j = pair_center[q0 + lane];
+        const float my_lo = lane < m ? pair_lo[q0 + lane] : kInf;
+        const int tb = __ffs(__ballot_sync(0xffffffffu, lane < m && my_j == jb)) - 1;  // the best tensor-core slot
+        float fu_min = kInf;
+        for (int k = 0; k < m; ++k) {
+            const int t = k == 0 ? (tb >= 0 ? tb : 0) : (k <= tb ? k - 1 : k);
+            const float lo_t = __shfl_sync(0xffffffffu, my_lo, t);
+            if (lo_t > fu_min) continue;  // cannot win or tie (false for NaN: evaluated)
+            const int j = __shfl_sync(0xffffffffu, my_j, t);
+            float acc = rc_lane_sum(x, C + (int64_t)j * d, d, vec4, lane);
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) acc = __fadd_rn(acc, __shfl_xor_sync(0xffffffffu, acc, off));
+            const float fu = __fmul_ru(acc, gamma_hi);
+            const float fl = __fmul_rd(acc, gamma_lo);
+            if (lane == t) {
+                my_fl = fl;
+                my_bad = !(acc <= 3.4028234663852886e38f);  // NaN or infinite
+            }
+            if (fu < fu_min) fu_min = fu;
+        }
+        const bool any_bad = __any_sync(0xffffffffu, my_bad);
+        const unsigned alive = __ballot_sync(0xffffffffu, lane < m && (any_bad ? my_fl < kInf || my_bad : my_fl <= fu_min));
+        if (!any_bad && __popc(alive) == 1) {
+            const int t = __ffs(alive) - 1;
+            const int lbl = __shfl_sync(0xffffffffu, my_j, t);
+            if (lane == 0) {
+                const int before = labels[i];
+                if (before != lbl) {
+                    ++nflip;
+                    if (flips) {
+                        const int slot = atomicAdd(n_flips, 1);
+                        if (slot < max_flips) {
+                            flips[3 * (int64_t)slot] = (int32_t)i;
+                            flips[3 * (int64_t)slot + 1] = before;
+                            flips[3 * (int64_t)slot + 2] = lbl;
+                        }
+                    } else {
+                        labels[i] = lbl;
+                    }
+                }
+            }
+        } else if (lane == 0) {
+            // every evaluated candidate when some F is not finite
+            const int slot = atomicAdd(amb_count, 1);
+            amb_entries[slot] = (int32_t)e;
+            amb_mask[slot] = (int32_t)alive;
+        }
+    }
+    if (flipped && lane == 0 && nflip) atomicAdd(flipped, nflip);
+}
+
+__global__ void __launch_bounds__(256) recheck_exact_kernel(
+    const float *__restrict__ X, int d, const float *__restrict__ C, const int32_t *__restrict__ rc_frames,
+    const int64_t *__restrict__ rc_pairs, const int32_t *__restrict__ pair_center,
+    const int32_t *__restrict__ amb_entries, const int32_t *__restrict__ amb_mask,
+    const int32_t *__restrict__ amb_count, int64_t max_entries, unsigned long long *__restrict__ keys) {
+    int64_t count = *amb_count;
+    if (count > max_entries) count = max_entries;
+    for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < count * 16;
+         w += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t s = w >> 4;
+        const int t = (int)(w & 15);
+        if (!((amb_mask[s] >> t) & 1)) continue;
+        const int e = amb_entries[s];
+        const int j = pair_center[(rc_pairs[e] >> 8) + t];
         const float dd = sqdist_exact(X + (int64_t)rc_frames[e] * d, C + (int64_t)j * d, d);
         atomicMin(&keys[e], ((unsigned long long)__float_as_uint(dd) << 32) | (unsigned)j);
     }
@@ -231,18 +333,21 @@ __global__ void __launch_bounds__(256) full_few_kernel(const float *__restrict__
     }
 }
 
-// One thread per entry: the winning key becomes the label (label 0 when no
-// candidate distance is finite, as in the exact kernel).  With a flip list
-// (flips non-null) a changed label is listed instead of written.
+// One thread per entry (entries[s] with an entry list, else s): the winning
+// key becomes the label (label 0 when no candidate distance is finite, as in
+// the exact kernel).  With a flip list (flips non-null) a changed label is
+// listed instead of written.
 __global__ void __launch_bounds__(256) recheck_finalize_kernel(
     const int32_t *__restrict__ rc_frames, const unsigned long long *__restrict__ keys,
-    const int32_t *__restrict__ entry_count, int64_t max_entries, int32_t *__restrict__ labels,
-    unsigned long long *flipped, int32_t *__restrict__ flips, int32_t *__restrict__ n_flips, int64_t max_flips) {
+    const int32_t *__restrict__ entries, const int32_t *__restrict__ entry_count, int64_t max_entries,
+    int32_t *__restrict__ labels, unsigned long long *flipped, int32_t *__restrict__ flips,
+    int32_t *__restrict__ n_flips, int64_t max_flips) {
     int64_t count = *entry_count;
     if (count > max_entries) count = max_entries;
     unsigned long long nflip = 0;
-    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < count;
-         e += (int64_t)gridDim.x * blockDim.x) {
+    for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < count;
+         s += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t e = entries ? entries[s] : s;
         const unsigned long long key = keys[e];
         const uint32_t dbits = (uint32_t)(key >> 32);
         const int lbl = dbits < 0x7f800000u ? (int)(uint32_t)key : 0;
@@ -281,27 +386,38 @@ int launch_assign_fp32(const float *X, const int32_t *frame_idx, const int32_t *
 }
 
 int launch_recheck_pairs(const float *X, int d, const float *C, const int32_t *rc_frames, const int32_t *rc_best,
-                         const int32_t *pair_entry, const int32_t *pair_center, const float *pair_lo,
-                         unsigned long long *keys, const int32_t *counters, int64_t max_entries, int64_t max_pairs,
-                         int32_t *labels, unsigned long long *flipped, cudaStream_t s, const FlipList *fl,
-                         int blocks_per_sm) {
+                         const int64_t *rc_pairs, const int32_t *pair_center, const float *pair_lo,
+                         unsigned long long *keys, int32_t *amb_entries, int32_t *amb_mask, int32_t *counters,
+                         int64_t max_entries, int32_t *labels, unsigned long long *flipped, cudaStream_t s,
+                         const FlipList *fl, int blocks_per_sm) {
     if (max_entries == 0) return KM_OK;
     const int64_t cap = (int64_t)num_sms() * blocks_per_sm;
-    int64_t g0 = (max_entries + 255) / 256;
+    // gamma = (d + n_l + 10) u, n_l = the largest number of fused steps a
+    // lane makes (ceil(d/32), or 4 ceil(d/128) with 16-byte loads), inflated
+    // by 1%; the factors are rounded outwards.
+    const double u = std::ldexp(1.0, -24);
+    const int n_l = std::max((d + 31) / 32, 4 * ((d + 127) / 128));
+    const double gamma = (d + n_l + 10) * u * 1.01;
+    const float g_lo = std::nextafter((float)(1.0 - gamma), 0.0f);
+    const float g_hi = std::nextafter((float)(1.0 + gamma), 2.0f);
+    int64_t g0 = (max_entries * 32 + 255) / 256;
     if (g0 > cap) g0 = cap;
-    recheck_best_kernel<<<(unsigned)(g0 < 1 ? 1 : g0), 256, 0, s>>>(X, d, C, rc_frames, rc_best, counters,
-                                                                  max_entries, keys);
+    recheck_fast_kernel<<<(unsigned)(g0 < 1 ? 1 : g0), 256, 0, s>>>(
+        X, d, C, rc_frames, rc_best, rc_pairs, pair_center, pair_lo, counters, max_entries, g_lo, g_hi, labels,
+        flipped, fl ? fl->rows : nullptr, fl ? fl->count : nullptr, fl ? fl->cap : 0, amb_entries, amb_mask,
+        counters + 3);
     KM_CUDA(cudaGetLastError());
-    int64_t g1 = (max_pairs + 255) / 256;
+    int64_t g1 = (max_entries * 16 + 255) / 256;
     if (g1 > cap) g1 = cap;
-    recheck_rest_kernel<<<(unsigned)(g1 < 1 ? 1 : g1), 256, 0, s>>>(X, d, C, rc_frames, rc_best, pair_entry,
-                                                                  pair_center, pair_lo, counters + 2, max_pairs, keys);
+    recheck_exact_kernel<<<(unsigned)(g1 < 1 ? 1 : g1), 256, 0, s>>>(X, d, C, rc_frames, rc_pairs, pair_center,
+                                                                   amb_entries, amb_mask, counters + 3, max_entries,
+                                                                   keys);
     KM_CUDA(cudaGetLastError());
     int64_t g2 = (max_entries + 255) / 256;
     if (g2 > cap) g2 = cap;
     recheck_finalize_kernel<<<(unsigned)(g2 < 1 ? 1 : g2), 256, 0, s>>>(
-        rc_frames, keys, counters, max_entries, labels, flipped, fl ? fl->rows : nullptr, fl ? fl->count : nullptr,
-        fl ? fl->cap : 0);
+        rc_frames, keys, amb_entries, counters + 3, max_entries, labels, flipped, fl ? fl->rows : nullptr,
+        fl ? fl->count : nullptr, fl ? fl->cap : 0);
     KM_CUDA(cudaGetLastError());
     return KM_OK;
 }
@@ -340,7 +456,7 @@ int launch_full_recheck(const float *X, const int32_t *frames, const int32_t *n_
     int64_t g2 = (n_max + 255) / 256;
     const int64_t cap2 = (int64_t)num_sms() * 8;
     if (g2 > cap2) g2 = cap2;
-    recheck_finalize_kernel<<<(unsigned)g2, 256, 0, s>>>(frames, keys, n_dev, n_max, labels, flipped,
+    recheck_finalize_kernel<<<(unsigned)g2, 256, 0, s>>>(frames, keys, nullptr, n_dev, n_max, labels, flipped,
                                                           fl ? fl->rows : nullptr, fl ? fl->count : nullptr,
                                                           fl ? fl->cap : 0);
     KM_CUDA(cudaGetLastError());

@@ -101,10 +101,10 @@ struct TcParams {
     const uint32_t *scal;
     int32_t *labels;
     int32_t *rc_frames;
-    int32_t *pair_entry;
     int32_t *pair_center;
     unsigned long long *rc_keys;
     int32_t *rc_best;
+    int64_t *rc_pairs;
     float *pair_lo;
     int32_t *full_frames;
     unsigned long long *full_keys;
@@ -1409,11 +1409,11 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                     p.rc_frames[e] = (int32_t)i;
                     p.rc_best[e] = jb;
                     p.rc_keys[e] = ~0ull;
+                    p.rc_pairs[e] = ((int64_t)(pbase + excl) << 8) | (int64_t)npairs;
 #pragma unroll
                     for (int m = 0; m < L; ++m) {
                         if ((cmask >> m) & 1u) {
                             const int q = pbase + excl + __popc(cmask & ((1u << m) - 1u));
-                            p.pair_entry[q] = e;
                             p.pair_center[q] = lid[m];
                             p.pair_lo[q] = lo[m];
                         }
@@ -1747,14 +1747,17 @@ size_t carve_assign(void *ws, int64_t n, TcBuffers &b) {
     Carver c(ws);
     const size_t nn = n > 0 ? n : 1;
     b.rc_frames = c.take<int32_t>(nn);
-    b.pair_entry = c.take<int32_t>(nn * kL);
     b.pair_center = c.take<int32_t>(nn * kL);
     b.rc_keys = c.take<unsigned long long>(nn);
     b.rc_best = c.take<int32_t>(nn);
     b.pair_lo = c.take<float>(nn * kL);
+    b.rc_pairs = c.take<int64_t>(nn);
+    b.amb_entries = c.take<int32_t>(nn);
+    b.amb_mask = c.take<int32_t>(nn);
     b.full_frames = c.take<int32_t>(nn);
     b.full_keys = c.take<unsigned long long>(nn);
-    b.counters = c.take<int32_t>(20);  // [0] recheck entries, [1] full entries, [2] pairs, [4..20) diagnostics
+    // [0] recheck entries, [1] full entries, [2] pairs, [3] entries left to the exact pass, [4..20) diagnostics
+    b.counters = c.take<int32_t>(20);
     b.flipped = c.take<unsigned long long>(1);
     b.err = c.take<uint32_t>(1);
     return c.bytes();
@@ -1938,10 +1941,10 @@ int tc_assign_impl(const float *X, int64_t n, int d, const float *C, int k, int3
     p.scal = b.scal;
     p.labels = labels;
     p.rc_frames = b.rc_frames;
-    p.pair_entry = b.pair_entry;
     p.pair_center = b.pair_center;
     p.rc_keys = b.rc_keys;
     p.rc_best = b.rc_best;
+    p.rc_pairs = b.rc_pairs;
     p.pair_lo = b.pair_lo;
     p.full_frames = b.full_frames;
     p.full_keys = b.full_keys;
@@ -2017,8 +2020,9 @@ int tc_assign_impl(const float *X, int64_t n, int d, const float *C, int k, int3
     if (prof) prof->begin(kProfRecheck, r);
     // Beside the centroid update the re-check keeps to half of each SM's
     // threads, so that both stay resident.
-    KM_TRY(launch_recheck_pairs(X, d, C, b.rc_frames, b.rc_best, b.pair_entry, b.pair_center, b.pair_lo, b.rc_keys,
-                                b.counters, n, n * kL, labels, b.flipped, r, fl, side ? kRecheckBesidePerSm : 8));
+    KM_TRY(launch_recheck_pairs(X, d, C, b.rc_frames, b.rc_best, b.rc_pairs, b.pair_center, b.pair_lo, b.rc_keys,
+                                b.amb_entries, b.amb_mask, b.counters, n, labels, b.flipped, r, fl,
+                                side ? kRecheckBesidePerSm : 8));
     if (prof) prof->end(kProfRecheck, r);
     if (prof) prof->begin(kProfFull, r);
     KM_TRY(launch_full_recheck(X, b.full_frames, b.counters + 1, n, d, C, k, b.full_keys, labels, b.flipped, r, fl));

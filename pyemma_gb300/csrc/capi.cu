@@ -549,10 +549,13 @@ StagePool &stage_pool() {
     return *p;
 }
 
+// One worker per host core but one (the calling thread enqueues the
+// kernels), at most 16: a single core's memcpy moves far less than the host
+// link carries.
 int stage_workers() {
     const unsigned hw = std::thread::hardware_concurrency();
-    int w = hw ? (int)hw / 2 : 4;
-    return std::max(2, std::min(8, w));
+    int w = hw ? (int)hw - 1 : 4;
+    return std::max(2, std::min(16, w));
 }
 
 // True when some part of the host frames is ordinary pageable memory.

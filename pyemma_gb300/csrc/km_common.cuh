@@ -120,11 +120,35 @@ __device__ __forceinline__ void ldg_f32x8(const float *p, float (&v)[8]) {
         : "l"(p));
 }
 
+// 32 consecutive floats by four 256-bit loads issued together (one asm
+// block, so that the compiler cannot spread them between the sums).
+__device__ __forceinline__ void ldg_f32x32(const float *p, float (&v)[32]) {
+    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%32];\n\t"
+        "ld.global.nc.v8.f32 {%8, %9, %10, %11, %12, %13, %14, %15}, [%32+32];\n\t"
+        "ld.global.nc.v8.f32 {%16, %17, %18, %19, %20, %21, %22, %23}, [%32+64];\n\t"
+        "ld.global.nc.v8.f32 {%24, %25, %26, %27, %28, %29, %30, %31}, [%32+96];"
+        : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]), "=f"(v[4]), "=f"(v[5]), "=f"(v[6]), "=f"(v[7]),
+          "=f"(v[8]), "=f"(v[9]), "=f"(v[10]), "=f"(v[11]), "=f"(v[12]), "=f"(v[13]), "=f"(v[14]), "=f"(v[15]),
+          "=f"(v[16]), "=f"(v[17]), "=f"(v[18]), "=f"(v[19]), "=f"(v[20]), "=f"(v[21]), "=f"(v[22]), "=f"(v[23]),
+          "=f"(v[24]), "=f"(v[25]), "=f"(v[26]), "=f"(v[27]), "=f"(v[28]), "=f"(v[29]), "=f"(v[30]), "=f"(v[31])
+        : "l"(p));
+}
+
 __device__ __forceinline__ float sqdist_exact(const float *__restrict__ x, const float *__restrict__ c,
                                               int d) {
     float acc = 0.0f;
     if ((d & 7) == 0 && ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(c)) & 31) == 0) {
-        for (int f = 0; f < d; f += 8) {
+        // Groups of four 32-byte loads per row are issued before their sums,
+        // so a thread waits for memory once per 32 features, not per 8.
+        int f = 0;
+        for (; f + 32 <= d; f += 32) {
+            float a[32], b[32];
+            ldg_f32x32(x + f, a);
+            ldg_f32x32(c + f, b);
+#pragma unroll
+            for (int q = 0; q < 32; ++q) acc = __fadd_rn(acc, sq_term(a[q], b[q]));
+        }
+        for (; f < d; f += 8) {
             float a[8], b[8];
             ldg_f32x8(x + f, a);
             ldg_f32x8(c + f, b);

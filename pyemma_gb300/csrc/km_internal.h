@@ -56,16 +56,21 @@ int launch_full_recheck(const float *X, const int32_t *frames, const int32_t *n_
                         const float *C, int k, unsigned long long *keys, int32_t *labels,
                         unsigned long long *flipped, cudaStream_t s, const FlipList *fl = nullptr);
 
-// Exact float32 re-evaluation of the candidates the tensor-core kernel could
-// not separate: pair q = (entry pair_entry[q], center pair_center[q]); entry e
-// stands for frame rc_frames[e] and keys[e] (initialised to ~0) collects the
-// winner.  counters[0] = entries, counters[2] = pairs (device).  With fl the
+// Re-evaluation of the candidates the tensor-core kernel could not
+// separate.  Entry e stands for frame rc_frames[e]; its candidates are the
+// pairs rc_pairs[e] >> 8 .. + (rc_pairs[e] & 255) (centers pair_center[q],
+// tensor-core lower bounds pair_lo[q]), rc_best[e] the one with the best
+// tensor-core value.  A warp per entry evaluates them in float32 with
+// coalesced loads; the bracket of that sum settles most entries, and the
+// rest (amb_entries / amb_mask, counters[3]) get the exact float32 distance
+// of their remaining candidates in feature order, the minimum collected in
+// keys[e] (initialised to ~0).  counters[0] = entries (device).  With fl the
 // changed labels go to the list and labels stays as it is.
 int launch_recheck_pairs(const float *X, int d, const float *C, const int32_t *rc_frames, const int32_t *rc_best,
-                         const int32_t *pair_entry, const int32_t *pair_center, const float *pair_lo,
-                         unsigned long long *keys, const int32_t *counters, int64_t max_entries, int64_t max_pairs,
-                         int32_t *labels, unsigned long long *flipped, cudaStream_t s, const FlipList *fl = nullptr,
-                         int blocks_per_sm = 8);
+                         const int64_t *rc_pairs, const int32_t *pair_center, const float *pair_lo,
+                         unsigned long long *keys, int32_t *amb_entries, int32_t *amb_mask, int32_t *counters,
+                         int64_t max_entries, int32_t *labels, unsigned long long *flipped, cudaStream_t s,
+                         const FlipList *fl = nullptr, int blocks_per_sm = 8);
 
 // ---- update.cu -------------------------------------------------------------
 size_t update_ws_size(int64_t n, int d, int k);
@@ -148,14 +153,16 @@ struct TcBuffers {
     uint32_t *scal = nullptr;    // scale, 1/scale^2, norm maxima (float bits)
     // candidate lists
     int32_t *rc_frames = nullptr;           // entry -> frame
-    int32_t *pair_entry = nullptr;          // pair -> entry
     int32_t *pair_center = nullptr;         // pair -> candidate center
     unsigned long long *rc_keys = nullptr;  // entry -> (distance bits, center) minimum
     int32_t *rc_best = nullptr;             // entry -> candidate with the smallest tensor-core distance
     float *pair_lo = nullptr;               // pair -> lower bound of the candidate's exact distance
+    int64_t *rc_pairs = nullptr;            // entry -> (first pair << 8) | number of pairs
+    int32_t *amb_entries = nullptr;         // entries the FP32 bracket could not settle
+    int32_t *amb_mask = nullptr;            // their candidates (bit t: pair first + t) for the exact pass
     int32_t *full_frames = nullptr;
     unsigned long long *full_keys = nullptr;
-    int32_t *counters = nullptr;  // [0] recheck entries, [1] full entries, [2] pairs
+    int32_t *counters = nullptr;  // [0] recheck entries, [1] full entries, [2] pairs, [3] unsettled entries
     unsigned long long *flipped = nullptr;
     uint32_t *err = nullptr;
     float *chn = nullptr;        // FP8 only: -||c~_j||^2 / 2 per center (the norm is not folded into the GEMM)
