@@ -284,6 +284,31 @@ __global__ void __launch_bounds__(256) recheck_fast_kernel(
     if (flipped && lane == 0 && nflip) atomicAdd(flipped, nflip);
 }
 
+// The exact float32 distance of one row pair by a whole warp: lanes load and
+// square 32 features at a time (coalesced), and the 32 squares go to every
+// lane in feature order by shuffles, so each lane adds them in the oracle's
+// sequence: the result is sqdist_exact's, bit for bit, in every lane.  One
+// thread walking the row waits on memory for every group of loads; here the
+// wait is shared by 32 lanes.
+__device__ __forceinline__ float warp_sqdist_exact(const float *__restrict__ x, const float *__restrict__ c, int d,
+                                                   int lane) {
+    float acc = 0.0f;
+    for (int f0 = 0; f0 < d; f0 += 32) {
+        const int f = f0 + lane;
+        const float q = f < d ? sq_term(__ldg(x + f), __ldg(c + f)) : 0.0f;
+        const int fw = min(32, d - f0);
+        if (fw == 32) {
+#pragma unroll
+            for (int l = 0; l < 32; ++l) acc = __fadd_rn(acc, __shfl_sync(0xffffffffu, q, l));
+        } else {
+            for (int l = 0; l < fw; ++l) acc = __fadd_rn(acc, __shfl_sync(0xffffffffu, q, l));
+        }
+    }
+    return acc;
+}
+
+// Pass 2, one warp per (unsettled entry, candidate slot); slots outside the
+// entry's mask are skipped.
 __global__ void __launch_bounds__(256) recheck_exact_kernel(
     const float *__restrict__ X, int d, const float *__restrict__ C, const int32_t *__restrict__ rc_frames,
     const int64_t *__restrict__ rc_pairs, const int32_t *__restrict__ pair_center,
@@ -291,21 +316,21 @@ __global__ void __launch_bounds__(256) recheck_exact_kernel(
     const int32_t *__restrict__ amb_count, int64_t max_entries, unsigned long long *__restrict__ keys) {
     int64_t count = *amb_count;
     if (count > max_entries) count = max_entries;
-    for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < count * 16;
-         w += (int64_t)gridDim.x * blockDim.x) {
+    const int lane = threadIdx.x & 31;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < count * 16; w += nw) {
         const int64_t s = w >> 4;
         const int t = (int)(w & 15);
         if (!((amb_mask[s] >> t) & 1)) continue;
         const int e = amb_entries[s];
         const int j = pair_center[(rc_pairs[e] >> 8) + t];
-        const float dd = sqdist_exact(X + (int64_t)rc_frames[e] * d, C + (int64_t)j * d, d);
-        atomicMin(&keys[e], ((unsigned long long)__float_as_uint(dd) << 32) | (unsigned)j);
+        const float dd = warp_sqdist_exact(X + (int64_t)rc_frames[e] * d, C + (int64_t)j * d, d, lane);
+        if (lane == 0) atomicMin(&keys[e], ((unsigned long long)__float_as_uint(dd) << 32) | (unsigned)j);
     }
 }
 
-// Full re-check of a short list: one warp per (frame, 32 consecutive
-// centers), one exact distance per lane (sqdist_exact: the assignment's
-// arithmetic and order), the warp's smallest key, one atomicMin per warp.
+// Full re-check of a short list: one warp per (frame, center), the exact
+// distance by warp_sqdist_exact, one atomicMin per warp.
 __global__ void __launch_bounds__(256) full_few_kernel(const float *__restrict__ X, const int32_t *__restrict__ frames,
                                                        const int32_t *__restrict__ n_dev, int64_t n_max, int d,
                                                        const float *__restrict__ C, int k,
@@ -314,22 +339,12 @@ __global__ void __launch_bounds__(256) full_few_kernel(const float *__restrict__
     if (n > n_max) n = n_max;
     if (n > kFullFew) return;  // the tiled kernel takes long lists
     const int lane = threadIdx.x & 31;
-    const int64_t groups = (k + 31) / 32;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < n * groups; w += nw) {
-        const int64_t e = w / groups;
-        const int j = (int)((w - e * groups) * 32) + lane;
-        unsigned long long key = ~0ull;
-        if (j < k) {
-            const float dd = sqdist_exact(X + (int64_t)frames[e] * d, C + (int64_t)j * d, d);
-            key = ((unsigned long long)__float_as_uint(dd) << 32) | (unsigned)j;
-        }
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) {
-            const unsigned long long o = __shfl_xor_sync(0xffffffffu, key, off);
-            key = o < key ? o : key;
-        }
-        if (lane == 0) atomicMin(&keys[e], key);
+    for (int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < n * k; w += nw) {
+        const int64_t e = w / k;
+        const int j = (int)(w - e * k);
+        const float dd = warp_sqdist_exact(X + (int64_t)frames[e] * d, C + (int64_t)j * d, d, lane);
+        if (lane == 0) atomicMin(&keys[e], ((unsigned long long)__float_as_uint(dd) << 32) | (unsigned)j);
     }
 }
 
@@ -407,14 +422,14 @@ int launch_recheck_pairs(const float *X, int d, const float *C, const int32_t *r
         flipped, fl ? fl->rows : nullptr, fl ? fl->count : nullptr, fl ? fl->cap : 0, amb_entries, amb_mask,
         counters + 3);
     KM_CUDA(cudaGetLastError());
-    int64_t g1 = (max_entries * 16 + 255) / 256;
+    int64_t g1 = (max_entries * 16 * 32 + 255) / 256;  // a warp per (entry, slot)
     if (g1 > cap) g1 = cap;
     recheck_exact_kernel<<<(unsigned)(g1 < 1 ? 1 : g1), 256, 0, s>>>(X, d, C, rc_frames, rc_pairs, pair_center,
                                                                    amb_entries, amb_mask, counters + 3, max_entries,
                                                                    keys);
     KM_CUDA(cudaGetLastError());
-    int64_t g2 = (max_entries + 255) / 256;
-    if (g2 > cap) g2 = cap;
+    int64_t g2 = (max_entries + 255) / 256;  // the unsettled list is short: one CTA per SM at most
+    if (g2 > num_sms()) g2 = num_sms();
     recheck_finalize_kernel<<<(unsigned)(g2 < 1 ? 1 : g2), 256, 0, s>>>(
         rc_frames, keys, amb_entries, counters + 3, max_entries, labels, flipped, fl ? fl->rows : nullptr,
         fl ? fl->count : nullptr, fl ? fl->cap : 0);
@@ -436,17 +451,21 @@ int launch_full_recheck(const float *X, const int32_t *frames, const int32_t *n_
         KM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, assign_fp32_kernel<FT, G, true>, kThreads, 0));
         per_sm = v > 0 ? v : 1;
     }
+    // The list is usually empty or short (full_few_kernel takes up to
+    // kFullFew frames and this kernel then exits at once); the grid walks
+    // the frame tiles, two CTAs per SM in all.
     const int64_t gy = (k + BN - 1) / BN;
     int64_t gx = (n_max + BM - 1) / BM;
-    int64_t cap = (int64_t)num_sms() * per_sm * 2;
+    int64_t cap = (int64_t)num_sms() * 2;
     cap = cap / gy > 0 ? cap / gy : 1;
     if (gx > cap) gx = cap;
+    (void)per_sm;
     if (gy > 65535) {
         set_error("k=%d: too many center blocks for the full re-check", k);
         return KM_ERR_BAD_SHAPE;
     }
-    int64_t gf = (std::min(n_max, kFullFew) * ((k + 31) / 32) + 7) / 8;  // 8 warps per block
-    const int64_t capf = (int64_t)num_sms() * 8;
+    int64_t gf = (std::min(n_max, kFullFew) * k + 7) / 8;  // a warp per (frame, center), 8 warps per block
+    const int64_t capf = (int64_t)num_sms() * 4;
     if (gf > capf) gf = capf;
     full_few_kernel<<<(unsigned)(gf < 1 ? 1 : gf), 256, 0, s>>>(X, frames, n_dev, n_max, d, C, k, keys);
     KM_CUDA(cudaGetLastError());
@@ -454,7 +473,7 @@ int launch_full_recheck(const float *X, const int32_t *frames, const int32_t *n_
         X, frames, n_dev, n_max, d, C, k, nullptr, nullptr, nullptr, keys);
     KM_CUDA(cudaGetLastError());
     int64_t g2 = (n_max + 255) / 256;
-    const int64_t cap2 = (int64_t)num_sms() * 8;
+    const int64_t cap2 = (int64_t)num_sms();
     if (g2 > cap2) g2 = cap2;
     recheck_finalize_kernel<<<(unsigned)g2, 256, 0, s>>>(frames, keys, nullptr, n_dev, n_max, labels, flipped,
                                                           fl ? fl->rows : nullptr, fl ? fl->count : nullptr,
