@@ -70,6 +70,7 @@ def parse_args():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-fp64", action="store_true", help="skip the float64 reference check of the centers")
+    p.add_argument("--no-kmpp", action="store_true", help="skip the kmeans++ timing")
     p.add_argument("--config", default="c3", choices=["c1", "c2", "c3", "c4", "c5", "minrmsd"])
     p.add_argument("--serve-seconds", type=float, default=10.0)
     return p.parse_args()
@@ -403,6 +404,7 @@ def run_ours(args):
             extra["plain_fp32"] = {"value": fp32_value, "unit": UNIT, "steps": steps32}
             extra["mixed_vs_plain_fp32"] = (value / world) / fp32_value
         del lab16
+    if rank == 0 and not args.no_kmpp:
         # kmeans++ (k rounds of D^2 sampling) on the same frames
         _lib.kmpp(X[:65536].contiguous(), 8, 42)
         torch.cuda.synchronize()
