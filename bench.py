@@ -481,31 +481,46 @@ def run_ours(args):
                            "d2h_bytes_per_step": K * D * 4 + 8, "vs_pinned": (n / dtp) / e2e["value"],
                            "api": "KmeansClustering(max_iter=1, clustercenters=C).estimate(pageable numpy X)"}
         del Xpg
-        # The same iteration from pinned host C-alpha coordinates: the
-        # 528 distance features are computed on the device (featurize.ca_distances)
-        # and clustered there, so 396 bytes per frame cross the host link.
+        # The same iteration from pinned host C-alpha coordinates: the 528
+        # pair distances are never written out; every kernel that reads a
+        # feature computes it from the coordinates (km_lloyd_pairs), so 396
+        # bytes per frame cross the host link and no n x 528 matrix exists.
         from pyemma_gb300 import featurize
         xyz_d = datasets.calpha_coordinates(n_frames=n, seed=SEED + rank)
         xyz_h = torch.empty(tuple(xyz_d.shape), dtype=torch.float32, pin_memory=True)
         xyz_h.copy_(xyz_d)
-        del xyz_d
+        src = featurize.pair_distance_frames(xyz_d, excluded_neighbors=0)
+        # Lloyd iterations on device-resident coordinates, for the step time
+        Cp = C0.clone()
+        _lib.lloyd_pairs(src.xyz, src.pairs, Cp, 2, -1.0, precision="fp16")
+        Cp = C0.clone()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        _lib.lloyd_pairs(src.xyz, src.pairs, Cp, 5, -1.0, precision="fp16")
+        e1.record()
+        torch.cuda.synchronize()
+        pair_ms = e0.elapsed_time(e1) / 5
+        del src, xyz_d, Cp
         torch.cuda.empty_cache()
-        F = featurize.ca_distances(xyz_h, excluded_neighbors=0)
-        KmeansClustering(n_clusters=K, max_iter=1, tolerance=-1.0, clustercenters=C0h, precision="fp16").estimate(F)
-        del F
+        km = KmeansClustering(n_clusters=K, max_iter=1, tolerance=-1.0, clustercenters=C0h, precision="fp16")
+        km.estimate(featurize.pair_distance_frames(xyz_h, excluded_neighbors=0))
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for _ in range(e2e_steps):
-            F = featurize.ca_distances(xyz_h, excluded_neighbors=0)
             km = KmeansClustering(n_clusters=K, max_iter=1, tolerance=-1.0, clustercenters=C0h, precision="fp16")
-            km.estimate(F)
+            km.estimate(featurize.pair_distance_frames(xyz_h, excluded_neighbors=0))
             _ = km.clustercenters
-            del F
         dtc = (time.perf_counter() - t0) / e2e_steps
+        kp = 64 * (-(-(D + 2) // 64))
         e2e["from_coordinates"] = {
             "value": n / dtc, "unit": UNIT, "h2d_bytes_per_step": n * 33 * 3 * 4, "d2h_bytes_per_step": K * D * 4 + 8,
-            "api": "featurize.ca_distances(pinned host xyz (n, 33, 3)) -> KmeansClustering(max_iter=1).estimate",
-            "workload": "same chain model, coordinates instead of precomputed distances"}
+            "api": "KmeansClustering(max_iter=1).estimate(featurize.pair_distance_frames(pinned host xyz (n, 33, 3)))",
+            "feature_matrix_bytes": 0,
+            "device_lloyd_ms_per_iter": pair_ms,
+            "hbm_bytes_per_iter": {"fp16_copy": n * kp * 2, "coordinates": n * 33 * 3 * 4,
+                                   "dense_path_float32_features": n * D * 4},
+            "workload": "same chain model, coordinates instead of precomputed distances; the features are computed "
+                        "where they are read (km_lloyd_pairs)"}
         del xyz_h
 
     # ---- CPU baseline (rank 0, N=1) ----

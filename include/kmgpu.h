@@ -322,9 +322,40 @@ int km_count_matrix(const int32_t *dtrajs, const int64_t *offsets, int32_t n_tra
  * unit cell).  xyz (device, n * n_atoms * 3 float32, frame-major), pairs
  * (device, npairs * 2 int32 atom indices), out (device, n * npairs float32):
  * out[t*npairs + p] = sqrt((dx*dx + dy*dy) + dz*dz) in float32 with
- * d = xyz[t, pairs[p][1]] - xyz[t, pairs[p][0]]. */
+ * d = xyz[t, pairs[p][1]] - xyz[t, pairs[p][0]].  The pair table is read
+ * back and checked on the host first (KM_ERR_BAD_SHAPE for an atom index
+ * outside [0, n_atoms)), which synchronises `stream`. */
 int km_pair_distances(const float *xyz, int64_t n, int32_t n_atoms, const int32_t *pairs, int32_t npairs,
                       float *out, void *stream);
+
+/* ---- frames given as atom coordinates: the featurization fused in ---------
+ * The reference featurizes on the host (featurizer.py:305-372 add_distances
+ * / add_distances_ca -> distances.py:53-54 mdtraj.compute_distances) and
+ * hands (T, n_pairs) float32 features to the clustering; km_pair_distances
+ * does that step on the device.  These calls skip it: they take the
+ * coordinates xyz (device, n x n_atoms x 3 float32, frame-major) and the
+ * atom pairs (device, d x 2 int32, every index in [0, n_atoms), checked on
+ * the host after a read-back of the d x 2 table), and every kernel that
+ * needs a float32 feature computes it where it reads it, with the
+ * arithmetic of km_pair_distances, so no n x d feature matrix is ever
+ * written.  Results equal km_assign / km_lloyd / km_kmpp on the output of
+ * km_pair_distances, bit for bit (labels, kmeans++ draws) or to the
+ * rounding of the float64 centroid sums (centers, inertia).  Workspaces are
+ * those of the dense calls with the same n, d, k.  KM_PREC_FP8 is not built
+ * for coordinate frames (KM_ERR_UNSUPPORTED). */
+size_t km_assign_pairs_workspace_size(int64_t n, int32_t d, int32_t k, int32_t precision);
+int km_assign_pairs(const float *xyz, int64_t n, int32_t n_atoms, const int32_t *pairs, int32_t d, const float *C,
+                    int32_t k, int32_t precision, int32_t *labels, void *workspace, size_t workspace_bytes,
+                    km_assign_stats *stats, void *stream);
+size_t km_lloyd_pairs_workspace_size(int64_t n, int32_t d, int32_t k, int32_t precision);
+int km_lloyd_pairs(const float *xyz, int64_t n, int32_t n_atoms, const int32_t *pairs, int32_t d, int32_t k,
+                   float *C, int32_t max_iter, double tolerance, int32_t precision, int32_t *labels,
+                   double *inertias, int32_t *n_iter, int32_t *converged, km_callback cb, void *cb_user,
+                   void *workspace, size_t workspace_bytes, void *stream);
+size_t km_kmpp_pairs_workspace_size(int64_t n, int32_t d, int32_t k);
+int km_kmpp_pairs(const float *xyz, int64_t n, int32_t n_atoms, const int32_t *pairs, int32_t d, int32_t k,
+                  uint32_t seed, float *C0, int64_t *idx, km_callback cb, void *cb_user, void *workspace,
+                  size_t workspace_bytes, void *stream);
 
 /* ---- resident center sets: ClusterModel(centers, metric) built once -------
  * interface.py:164-165 constructs ClusterModel(cluster_centers, metric) for

@@ -38,7 +38,8 @@ EXPORTED = (
     "km_serve_shutdown", "km_tune_workspace_size", "km_tune", "km_tune_clear", "km_tune_tiles", "km_tile_plan_get",
     "km_debug_force_tile_plan",
     "km_regspace_workspace_size", "km_regspace", "km_count_matrix_workspace_size", "km_count_matrix",
-    "km_pair_distances", "km_assign_minrmsd_workspace_size", "km_assign_minrmsd", "km_minrmsd_rows_workspace_size",
+    "km_pair_distances", "km_assign_pairs_workspace_size", "km_assign_pairs", "km_lloyd_pairs_workspace_size",
+    "km_lloyd_pairs", "km_kmpp_pairs_workspace_size", "km_kmpp_pairs", "km_assign_minrmsd_workspace_size", "km_assign_minrmsd", "km_minrmsd_rows_workspace_size",
     "km_minrmsd_rows", "km_kmpp_minrmsd_workspace_size", "km_kmpp_minrmsd", "km_lloyd_minrmsd_workspace_size",
     "km_lloyd_minrmsd",
 )
@@ -175,6 +176,18 @@ def load(build_if_missing=False):
                           ctypes.POINTER(f64), P]
     L.km_tune.restype = ctypes.c_int
     L.km_tune_clear.restype = ctypes.c_int
+    L.km_assign_pairs_workspace_size.argtypes = [i64, i32, i32, i32]
+    L.km_assign_pairs_workspace_size.restype = sz
+    L.km_assign_pairs.argtypes = [P, i64, i32, P, i32, P, i32, i32, P, P, sz, ctypes.POINTER(AssignStats), P]
+    L.km_assign_pairs.restype = ctypes.c_int
+    L.km_lloyd_pairs_workspace_size.argtypes = [i64, i32, i32, i32]
+    L.km_lloyd_pairs_workspace_size.restype = sz
+    L.km_lloyd_pairs.argtypes = [P, i64, i32, P, i32, i32, P, i32, f64, i32, P, P, P, P, CALLBACK, P, P, sz, P]
+    L.km_lloyd_pairs.restype = ctypes.c_int
+    L.km_kmpp_pairs_workspace_size.argtypes = [i64, i32, i32]
+    L.km_kmpp_pairs_workspace_size.restype = sz
+    L.km_kmpp_pairs.argtypes = [P, i64, i32, P, i32, i32, u32, P, P, CALLBACK, P, P, sz, P]
+    L.km_kmpp_pairs.restype = ctypes.c_int
     L.km_tune_tiles.argtypes = [P, i64, i32, P, i32, i32, P, sz, ctypes.POINTER(TilePlan), ctypes.POINTER(TilePlan),
                                 i32, ctypes.POINTER(i32), P]
     L.km_tune_tiles.restype = ctypes.c_int
@@ -664,6 +677,79 @@ def tune(X, C):
                     ctypes.byref(t16), _stream(torch, X.device)))
     return dict(chosen=PRECISION_NAMES[chosen.value], ms_fp32=t32.value,
                 ms_fp16=t16.value if t16.value >= 0 else None)
+
+
+def _pair_args(torch, xyz, pairs):
+    if not (isinstance(xyz, torch.Tensor) and xyz.device.type == "cuda" and xyz.dtype == torch.float32
+            and xyz.is_contiguous() and xyz.dim() == 3 and xyz.shape[2] == 3):
+        raise ValueError("xyz must be a contiguous float32 CUDA tensor of shape (n, n_atoms, 3)")
+    if not (isinstance(pairs, torch.Tensor) and pairs.device == xyz.device and pairs.dtype == torch.int32
+            and pairs.is_contiguous() and pairs.dim() == 2 and pairs.shape[1] == 2):
+        raise ValueError("pairs must be a contiguous int32 tensor of shape (d, 2) on the device of xyz")
+    return int(xyz.shape[0]), int(xyz.shape[1]), int(pairs.shape[0])
+
+
+def assign_pairs(xyz, pairs, C, precision="auto", labels=None):
+    """Labels of the pair-distance features of coordinate frames, the
+    features computed where the kernels read them (no feature matrix)."""
+    torch = _torch()
+    L = load()
+    n, n_atoms, d = _pair_args(torch, xyz, pairs)
+    _check_frames(torch, C, "C")
+    if C.shape[1] != d:
+        raise ValueError("centers have dimension %d, the pairs %d" % (C.shape[1], d))
+    k = C.shape[0]
+    p = precision_code(precision)
+    if labels is None:
+        labels = torch.empty(n, dtype=torch.int32, device=xyz.device)
+    ws_bytes = L.km_assign_pairs_workspace_size(n, d, k, p)
+    ws = _workspace(torch, ws_bytes, xyz.device)
+    stats = AssignStats()
+    check(L.km_assign_pairs(_ptr(xyz), n, n_atoms, _ptr(pairs), d, _ptr(C), k, p, _ptr(labels), _ptr(ws), ws_bytes,
+                            ctypes.byref(stats), _stream(torch, xyz.device)))
+    return labels, stats.as_dict()
+
+
+def lloyd_pairs(xyz, pairs, C, max_iter, tolerance, precision="auto", callback=None, labels=None):
+    """Lloyd iterations (in place on C) on the pair-distance features of
+    coordinate frames; returns dict(labels, inertias, n_iter, converged)."""
+    torch = _torch()
+    L = load()
+    n, n_atoms, d = _pair_args(torch, xyz, pairs)
+    _check_frames(torch, C, "C")
+    k = C.shape[0]
+    p = precision_code(precision)
+    if labels is None:
+        labels = torch.empty(n, dtype=torch.int32, device=xyz.device)
+    inertias = np.zeros(max(1, max_iter), dtype=np.float64)
+    n_iter = ctypes.c_int32(0)
+    conv = ctypes.c_int32(0)
+    ws_bytes = L.km_lloyd_pairs_workspace_size(n, d, k, p)
+    ws = _workspace(torch, ws_bytes, xyz.device)
+    cb, keep = _callback(callback)
+    check(L.km_lloyd_pairs(_ptr(xyz), n, n_atoms, _ptr(pairs), d, k, _ptr(C), int(max_iter), float(tolerance), p,
+                           _ptr(labels), inertias.ctypes.data_as(ctypes.c_void_p), ctypes.byref(n_iter),
+                           ctypes.byref(conv), cb, None, _ptr(ws), ws_bytes, _stream(torch, xyz.device)))
+    del keep
+    return dict(labels=labels, inertias=inertias[:n_iter.value].copy(), n_iter=n_iter.value,
+                converged=bool(conv.value))
+
+
+def kmpp_pairs(xyz, pairs, k, seed, callback=None):
+    """kmeans++ initial centers (k, d) and chosen frame indices for the
+    pair-distance features of coordinate frames."""
+    torch = _torch()
+    L = load()
+    n, n_atoms, d = _pair_args(torch, xyz, pairs)
+    C0 = torch.empty((k, d), dtype=torch.float32, device=xyz.device)
+    idx = torch.empty(k, dtype=torch.int64, device=xyz.device)
+    ws_bytes = L.km_kmpp_pairs_workspace_size(n, d, k)
+    ws = _workspace(torch, ws_bytes, xyz.device)
+    cb, keep = _callback(callback)
+    check(L.km_kmpp_pairs(_ptr(xyz), n, n_atoms, _ptr(pairs), d, k, int(seed) & 0xFFFFFFFF, _ptr(C0), _ptr(idx), cb,
+                          None, _ptr(ws), ws_bytes, _stream(torch, xyz.device)))
+    del keep
+    return C0, idx
 
 
 def tune_clear():

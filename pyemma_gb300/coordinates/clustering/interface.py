@@ -9,6 +9,7 @@ import os
 
 import numpy as np
 
+from ... import _lib
 from .. import _device
 from ..data import DeviceSource, InMemorySource, default_chunksize, get_n_jobs, is_device_data, make_logger
 
@@ -146,7 +147,8 @@ class AbstractClustering(object):
         return False
 
     def _source(self, X, chunksize=None):
-        if isinstance(X, InMemorySource):
+        from ...featurize import PairDistanceFrames
+        if isinstance(X, (InMemorySource, PairDistanceFrames)):
             return X
         if is_device_data(X):
             return DeviceSource(X, chunksize=chunksize)
@@ -207,6 +209,17 @@ class AbstractClustering(object):
         self.last_assign_stats = stats
         return labels
 
+    def _assign_pairs(self, src):
+        """int32 labels of PairDistanceFrames (km_assign_pairs)."""
+        if self.clustercenters is None or len(self.clustercenters) == 0:
+            raise ValueError("no cluster centers to assign to")
+        if self.metric != "euclidean":
+            raise ValueError("pair-distance frames are assigned under the euclidean metric")
+        C = _device.centers_to_device(self.clustercenters)
+        lab, stats = _lib.assign_pairs(src.xyz, src.pairs, C, precision=self.precision)
+        self.last_assign_stats = stats
+        return lab.cpu().numpy()
+
     def _transform_array(self, X):
         """get closest index of point in clustercenters to x (column vector)."""
         if not is_device_data(X):
@@ -217,6 +230,9 @@ class AbstractClustering(object):
 
     def transform(self, X):
         """Maps X (ndarray, CUDA tensor or a list of them) to (T, 1) int32 column vector(s)."""
+        from ...featurize import PairDistanceFrames
+        if isinstance(X, PairDistanceFrames):
+            return self._assign_pairs(X)[:, None]
         source = DeviceSource(X) if is_device_data(X) else InMemorySource(X)
         if isinstance(X, (list, tuple)):
             return [lab[:, None] for lab in self._assign_arrays(source.data)]
@@ -226,6 +242,9 @@ class AbstractClustering(object):
         """Assigns all frames of the data producer; list of (T_i, 1) int32 arrays."""
         if self.data_producer is None:
             raise RuntimeError("no data producer: call estimate() first")
+        from ...featurize import PairDistanceFrames
+        if isinstance(self.data_producer, PairDistanceFrames):
+            return [self._assign_pairs(self.data_producer.strided(stride, skip))[:, None][:, dimensions]]
         trajs = self.data_producer.frames(stride=stride, skip=skip)
         labels = self._assign_arrays(trajs)
         return [lab[:, None][:, dimensions] for lab in labels]

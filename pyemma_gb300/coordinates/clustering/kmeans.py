@@ -148,7 +148,49 @@ class KmeansClustering(AbstractClustering):
         dim = trajs[0].shape[1]
         return np.asarray(picked).reshape(-1, dim)
 
+    def _estimate_pairs(self, source):
+        """The estimate on PairDistanceFrames: the pair-distance features are
+        computed where the kernels read them (km_kmpp_pairs, km_lloyd_pairs).
+        The dtrajs are assigned on demand to the final centers
+        (km_assign_pairs), as for array input."""
+        stride = self.stride if self.stride else 1
+        src = source.strided(stride, self.skip)
+        total_length = src.n_frames
+        if total_length == 0:
+            raise ValueError("no frames to cluster (stride=%s, skip=%s)" % (stride, self.skip))
+        if not self.n_clusters:
+            self.n_clusters = min(int(math.sqrt(total_length)), 5000)
+        if self.metric == "minRMSD":
+            raise ValueError("minRMSD needs atom coordinates as frames, not pair-distance features")
+        dim = src.dimension()
+        if not self._check_resume_iteration() and self.init_strategy == "uniform":
+            indices = self._uniform_indices(np.array([total_length]), total_length)
+            rows = np.array(sorted(indices.get(0, ())), dtype=np.int64)[:self.n_clusters]
+            self.clustercenters = src.features(_device.torch_module().from_numpy(rows).to(src.xyz.device)).cpu().numpy()
+        if self._check_resume_iteration():
+            if self.clustercenters.ndim != 2 or self.clustercenters.shape[1] != dim:
+                raise ValueError("initial centers have shape %s, data has dimension %d"
+                                 % (self.clustercenters.shape, dim))
+            C = _device.centers_to_device(self.clustercenters)
+        else:
+            C, _ = _lib.kmpp_pairs(src.xyz, src.pairs, int(self.n_clusters), self.fixed_seed)
+        self.initial_centers_ = C.cpu().numpy()
+        res = _lib.lloyd_pairs(src.xyz, src.pairs, C, int(self.max_iter), float(self.tolerance),
+                               precision=self.precision)
+        self.clustercenters = C.cpu().numpy()
+        self._converged = res["converged"]
+        self.inertias = res["inertias"]
+        self.n_iter = res["n_iter"]
+        self._in_memory_chunks_set = False
+        if not self.converged:
+            self.logger.warning("Algorithm did not reach convergence criterion of %g in %i iterations. "
+                                "Consider increasing max_iter.", self.tolerance, self.max_iter)
+        return self
+
     def _estimate(self, source):
+        from ...featurize import PairDistanceFrames
+        if isinstance(source, PairDistanceFrames):
+            return self._estimate_pairs(source)
         stride = self.stride if self.stride else 1
         traj_lengths = source.trajectory_lengths(stride=stride, skip=self.skip)
         total_length = int(sum(traj_lengths))

@@ -14,6 +14,7 @@
 // and a lexicographic warp-shuffle (distance, index) reduction finishes the
 // argmin.
 #include <algorithm>
+#include <type_traits>
 #include <cmath>
 
 #include "km_common.cuh"
@@ -36,9 +37,9 @@ constexpr int64_t kFullFew = 64;
 // SPLIT: blockIdx.y selects one block of 32*G centers and the result of the
 // block goes to keys[entry] by atomicMin of (distance bits << 32 | center),
 // which recheck_finalize_kernel turns into labels.
-template <int FT, int G, bool SPLIT>
+template <int FT, int G, bool SPLIT, class Src>
 __global__ void __launch_bounds__(kThreads) assign_fp32_kernel(
-    const float *__restrict__ X, const int32_t *__restrict__ frame_idx,
+    const Src src, const int32_t *__restrict__ frame_idx,
     const int32_t *__restrict__ n_dev, int64_t n_max, int d, const float *__restrict__ C, int k,
     int32_t *__restrict__ labels, float *__restrict__ dist, unsigned long long *flipped,
     unsigned long long *__restrict__ keys) {
@@ -85,7 +86,7 @@ __global__ void __launch_bounds__(kThreads) assign_fp32_kernel(
                     float v = 0.0f;
                     if (i < n) {
                         const int64_t row = frame_idx ? (int64_t)frame_idx[i] : i;
-                        v = __ldg(X + row * d + fc + f);
+                        v = src.get(row, fc + f);
                     }
                     Xs[r][f] = v;
                 }
@@ -138,23 +139,23 @@ __global__ void __launch_bounds__(kThreads) assign_fp32_kernel(
     if (flipped && nflip) atomicAdd(flipped, nflip);
 }
 
-template <int FT, int G>
-int launch_cfg(const float *X, const int32_t *frame_idx, const int32_t *n_dev, int64_t n, int d,
+template <int FT, int G, class Src>
+int launch_cfg(const Src &src, const int32_t *frame_idx, const int32_t *n_dev, int64_t n, int d,
                const float *C, int k, int32_t *labels, float *dist, unsigned long long *flipped,
                cudaStream_t s) {
     constexpr int BM = kWarps * FT;
     static int per_sm = -1;  // cached: no queries while a stream is being captured
     if (per_sm < 0) {
         int v = 0;
-        KM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, assign_fp32_kernel<FT, G, false>, kThreads, 0));
+        KM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, assign_fp32_kernel<FT, G, false, Src>, kThreads, 0));
         per_sm = v;
     }
     int64_t ntiles = (n + BM - 1) / BM;
     int64_t grid = (int64_t)num_sms() * (per_sm > 0 ? per_sm : 1);
     if (grid > ntiles) grid = ntiles;
     if (grid < 1) grid = 1;
-    assign_fp32_kernel<FT, G, false><<<(unsigned)grid, kThreads, 0, s>>>(X, frame_idx, n_dev, n, d, C, k,
-                                                                        labels, dist, flipped, nullptr);
+    assign_fp32_kernel<FT, G, false, Src><<<(unsigned)grid, kThreads, 0, s>>>(src, frame_idx, n_dev, n, d, C, k,
+                                                                             labels, dist, flipped, nullptr);
     KM_CUDA(cudaGetLastError());
     return KM_OK;
 }
@@ -183,6 +184,24 @@ int launch_cfg(const float *X, const int32_t *frame_idx, const int32_t *n_dev, i
 
 // Lane sum of (x - c)^2 over the row pair, lanes over features.
 __device__ __forceinline__ float rc_lane_sum(const float *__restrict__ x, const float *__restrict__ c, int d,
+                                             bool vec4, int lane);
+
+template <class Src>
+__device__ __forceinline__ float rc_lane_sum_src(const Src &src, int64_t i, const float *__restrict__ c, int d,
+                                                 bool vec4, int lane) {
+    if constexpr (std::is_same<Src, DenseRows>::value) {
+        return rc_lane_sum(src.X + i * d, c, d, vec4, lane);
+    } else {
+        float acc = 0.0f;
+        for (int f = lane; f < d; f += 32) {
+            const float t = __fsub_rn(src.get(i, f), __ldg(c + f));
+            acc = __fmaf_rn(t, t, acc);
+        }
+        return acc;
+    }
+}
+
+__device__ __forceinline__ float rc_lane_sum(const float *__restrict__ x, const float *__restrict__ c, int d,
                                              bool vec4, int lane) {
     float acc = 0.0f;
     if (vec4) {
@@ -208,8 +227,9 @@ __device__ __forceinline__ float rc_lane_sum(const float *__restrict__ x, const 
     return acc;
 }
 
+template <class Src>
 __global__ void __launch_bounds__(256) recheck_fast_kernel(
-    const float *__restrict__ X, int d, const float *__restrict__ C, const int32_t *__restrict__ rc_frames,
+    const Src src, int d, const float *__restrict__ C, const int32_t *__restrict__ rc_frames,
     const int32_t *__restrict__ rc_best, const int64_t *__restrict__ rc_pairs, const int32_t *__restrict__ pair_center,
     const float *__restrict__ pair_lo, const int32_t *__restrict__ entry_count, int64_t max_entries, float gamma_lo,
     float gamma_hi, int32_t *__restrict__ labels, unsigned long long *flipped, int32_t *__restrict__ flips,
@@ -219,7 +239,8 @@ __global__ void __launch_bounds__(256) recheck_fast_kernel(
     if (count > max_entries) count = max_entries;
     const int lane = threadIdx.x & 31;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    const bool vec4 = (d & 3) == 0 && ((reinterpret_cast<uintptr_t>(X) | reinterpret_cast<uintptr_t>(C)) & 15) == 0;
+    bool vec4 = (d & 3) == 0 && (reinterpret_cast<uintptr_t>(C) & 15) == 0;
+    if constexpr (std::is_same<Src, DenseRows>::value) vec4 = vec4 && (reinterpret_cast<uintptr_t>(src.X) & 15) == 0;
     const float kInf = __int_as_float(0x7f800000);
     unsigned long long nflip = 0;
     for (int64_t e = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; e < count; e += nw) {
@@ -228,7 +249,6 @@ __global__ void __launch_bounds__(256) recheck_fast_kernel(
         const int64_t q0 = word >> 8;
         const int m = (int)(word & 0xFF);
         const int jb = rc_best[e];
-        const float *x = X + i * d;
         // Lane t (< m) holds candidate t's bracket; unevaluated: Fl = +inf.
         float my_fl = kInf;
         bool my_bad = false;
@@ -242,7 +262,7 @@ __global__ void __launch_bounds__(256) recheck_fast_kernel(
             const float lo_t = __shfl_sync(0xffffffffu, my_lo, t);
             if (lo_t > fu_min) continue;  // cannot win or tie (false for NaN: evaluated)
             const int j = __shfl_sync(0xffffffffu, my_j, t);
-            float acc = rc_lane_sum(x, C + (int64_t)j * d, d, vec4, lane);
+            float acc = rc_lane_sum_src(src, i, C + (int64_t)j * d, d, vec4, lane);
 #pragma unroll
             for (int off = 16; off > 0; off >>= 1) acc = __fadd_rn(acc, __shfl_xor_sync(0xffffffffu, acc, off));
             const float fu = __fmul_ru(acc, gamma_hi);
@@ -290,12 +310,13 @@ __global__ void __launch_bounds__(256) recheck_fast_kernel(
 // sequence: the result is sqdist_exact's, bit for bit, in every lane.  One
 // thread walking the row waits on memory for every group of loads; here the
 // wait is shared by 32 lanes.
-__device__ __forceinline__ float warp_sqdist_exact(const float *__restrict__ x, const float *__restrict__ c, int d,
+template <class Src>
+__device__ __forceinline__ float warp_sqdist_exact(const Src &src, int64_t i, const float *__restrict__ c, int d,
                                                    int lane) {
     float acc = 0.0f;
     for (int f0 = 0; f0 < d; f0 += 32) {
         const int f = f0 + lane;
-        const float q = f < d ? sq_term(__ldg(x + f), __ldg(c + f)) : 0.0f;
+        const float q = f < d ? sq_term(src.get(i, f), __ldg(c + f)) : 0.0f;
         const int fw = min(32, d - f0);
         if (fw == 32) {
 #pragma unroll
@@ -309,8 +330,9 @@ __device__ __forceinline__ float warp_sqdist_exact(const float *__restrict__ x, 
 
 // Pass 2, one warp per (unsettled entry, candidate slot); slots outside the
 // entry's mask are skipped.
+template <class Src>
 __global__ void __launch_bounds__(256) recheck_exact_kernel(
-    const float *__restrict__ X, int d, const float *__restrict__ C, const int32_t *__restrict__ rc_frames,
+    const Src src, int d, const float *__restrict__ C, const int32_t *__restrict__ rc_frames,
     const int64_t *__restrict__ rc_pairs, const int32_t *__restrict__ pair_center,
     const int32_t *__restrict__ amb_entries, const int32_t *__restrict__ amb_mask,
     const int32_t *__restrict__ amb_count, int64_t max_entries, unsigned long long *__restrict__ keys) {
@@ -324,14 +346,15 @@ __global__ void __launch_bounds__(256) recheck_exact_kernel(
         if (!((amb_mask[s] >> t) & 1)) continue;
         const int e = amb_entries[s];
         const int j = pair_center[(rc_pairs[e] >> 8) + t];
-        const float dd = warp_sqdist_exact(X + (int64_t)rc_frames[e] * d, C + (int64_t)j * d, d, lane);
+        const float dd = warp_sqdist_exact(src, (int64_t)rc_frames[e], C + (int64_t)j * d, d, lane);
         if (lane == 0) atomicMin(&keys[e], ((unsigned long long)__float_as_uint(dd) << 32) | (unsigned)j);
     }
 }
 
 // Full re-check of a short list: one warp per (frame, center), the exact
 // distance by warp_sqdist_exact, one atomicMin per warp.
-__global__ void __launch_bounds__(256) full_few_kernel(const float *__restrict__ X, const int32_t *__restrict__ frames,
+template <class Src>
+__global__ void __launch_bounds__(256) full_few_kernel(const Src src, const int32_t *__restrict__ frames,
                                                        const int32_t *__restrict__ n_dev, int64_t n_max, int d,
                                                        const float *__restrict__ C, int k,
                                                        unsigned long long *__restrict__ keys) {
@@ -343,7 +366,7 @@ __global__ void __launch_bounds__(256) full_few_kernel(const float *__restrict__
     for (int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < n * k; w += nw) {
         const int64_t e = w / k;
         const int j = (int)(w - e * k);
-        const float dd = warp_sqdist_exact(X + (int64_t)frames[e] * d, C + (int64_t)j * d, d, lane);
+        const float dd = warp_sqdist_exact(src, (int64_t)frames[e], C + (int64_t)j * d, d, lane);
         if (lane == 0) atomicMin(&keys[e], ((unsigned long long)__float_as_uint(dd) << 32) | (unsigned)j);
     }
 }
@@ -387,25 +410,26 @@ __global__ void __launch_bounds__(256) recheck_finalize_kernel(
 
 }  // namespace
 
-int launch_assign_fp32(const float *X, const int32_t *frame_idx, const int32_t *n_dev, int64_t n,
-                       int d, const float *C, int k, int32_t *labels, float *dist,
-                       unsigned long long *flipped, cudaStream_t s) {
-    if (n == 0) return KM_OK;
-    if (k <= 32) return launch_cfg<4, 1>(X, frame_idx, n_dev, n, d, C, k, labels, dist, flipped, s);
-    if (k <= 64) return launch_cfg<4, 2>(X, frame_idx, n_dev, n, d, C, k, labels, dist, flipped, s);
-    if (k <= 128) return launch_cfg<4, 4>(X, frame_idx, n_dev, n, d, C, k, labels, dist, flipped, s);
+namespace {
+
+template <class Src>
+int assign_fp32_src(const Src &src, const int32_t *frame_idx, const int32_t *n_dev, int64_t n, int d, const float *C,
+                    int k, int32_t *labels, float *dist, unsigned long long *flipped, cudaStream_t s) {
+    if (k <= 32) return launch_cfg<4, 1>(src, frame_idx, n_dev, n, d, C, k, labels, dist, flipped, s);
+    if (k <= 64) return launch_cfg<4, 2>(src, frame_idx, n_dev, n, d, C, k, labels, dist, flipped, s);
+    if (k <= 128) return launch_cfg<4, 4>(src, frame_idx, n_dev, n, d, C, k, labels, dist, flipped, s);
     // Narrow frames: more frames per thread, so each shared-memory center
     // value feeds more distances (the chunk loop is short at small d).
-    if (d <= 32) return launch_cfg<8, 8>(X, frame_idx, n_dev, n, d, C, k, labels, dist, flipped, s);
-    return launch_cfg<4, 8>(X, frame_idx, n_dev, n, d, C, k, labels, dist, flipped, s);
+    if (d <= 32) return launch_cfg<8, 8>(src, frame_idx, n_dev, n, d, C, k, labels, dist, flipped, s);
+    return launch_cfg<4, 8>(src, frame_idx, n_dev, n, d, C, k, labels, dist, flipped, s);
 }
 
-int launch_recheck_pairs(const float *X, int d, const float *C, const int32_t *rc_frames, const int32_t *rc_best,
-                         const int64_t *rc_pairs, const int32_t *pair_center, const float *pair_lo,
-                         unsigned long long *keys, int32_t *amb_entries, int32_t *amb_mask, int32_t *counters,
-                         int64_t max_entries, int32_t *labels, unsigned long long *flipped, cudaStream_t s,
-                         const FlipList *fl, int blocks_per_sm) {
-    if (max_entries == 0) return KM_OK;
+template <class Src>
+int recheck_pairs_src(const Src &src, int d, const float *C, const int32_t *rc_frames, const int32_t *rc_best,
+                      const int64_t *rc_pairs, const int32_t *pair_center, const float *pair_lo,
+                      unsigned long long *keys, int32_t *amb_entries, int32_t *amb_mask, int32_t *counters,
+                      int64_t max_entries, int32_t *labels, unsigned long long *flipped, cudaStream_t s,
+                      const FlipList *fl, int blocks_per_sm) {
     const int64_t cap = (int64_t)num_sms() * blocks_per_sm;
     // gamma = (d + n_l + 10) u, n_l = the largest number of fused steps a
     // lane makes (ceil(d/32), or 4 ceil(d/128) with 16-byte loads), inflated
@@ -417,16 +441,15 @@ int launch_recheck_pairs(const float *X, int d, const float *C, const int32_t *r
     const float g_hi = std::nextafter((float)(1.0 + gamma), 2.0f);
     int64_t g0 = (max_entries * 32 + 255) / 256;
     if (g0 > cap) g0 = cap;
-    recheck_fast_kernel<<<(unsigned)(g0 < 1 ? 1 : g0), 256, 0, s>>>(
-        X, d, C, rc_frames, rc_best, rc_pairs, pair_center, pair_lo, counters, max_entries, g_lo, g_hi, labels,
+    recheck_fast_kernel<Src><<<(unsigned)(g0 < 1 ? 1 : g0), 256, 0, s>>>(
+        src, d, C, rc_frames, rc_best, rc_pairs, pair_center, pair_lo, counters, max_entries, g_lo, g_hi, labels,
         flipped, fl ? fl->rows : nullptr, fl ? fl->count : nullptr, fl ? fl->cap : 0, amb_entries, amb_mask,
         counters + 3);
     KM_CUDA(cudaGetLastError());
     int64_t g1 = (max_entries * 16 * 32 + 255) / 256;  // a warp per (entry, slot)
     if (g1 > cap) g1 = cap;
-    recheck_exact_kernel<<<(unsigned)(g1 < 1 ? 1 : g1), 256, 0, s>>>(X, d, C, rc_frames, rc_pairs, pair_center,
-                                                                   amb_entries, amb_mask, counters + 3, max_entries,
-                                                                   keys);
+    recheck_exact_kernel<Src><<<(unsigned)(g1 < 1 ? 1 : g1), 256, 0, s>>>(
+        src, d, C, rc_frames, rc_pairs, pair_center, amb_entries, amb_mask, counters + 3, max_entries, keys);
     KM_CUDA(cudaGetLastError());
     int64_t g2 = (max_entries + 255) / 256;  // the unsettled list is short: one CTA per SM at most
     if (g2 > num_sms()) g2 = num_sms();
@@ -437,29 +460,20 @@ int launch_recheck_pairs(const float *X, int d, const float *C, const int32_t *r
     return KM_OK;
 }
 
-int launch_full_recheck(const float *X, const int32_t *frames, const int32_t *n_dev, int64_t n_max, int d,
-                        const float *C, int k, unsigned long long *keys, int32_t *labels,
-                        unsigned long long *flipped, cudaStream_t s, const FlipList *fl) {
-    if (n_max == 0) return KM_OK;
-    // The list is short next to n_max: tiles of 32 frames x 256 centers,
-    // one CTA per (frame tile, center block), so that a few thousand frames
-    // still occupy every SM.
-    constexpr int FT = 4, G = 8, BM = kWarps * FT, BN = 32 * G;
-    static int per_sm = -1;
-    if (per_sm < 0) {
-        int v = 0;
-        KM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, assign_fp32_kernel<FT, G, true>, kThreads, 0));
-        per_sm = v > 0 ? v : 1;
-    }
-    // The list is usually empty or short (full_few_kernel takes up to
-    // kFullFew frames and this kernel then exits at once); the grid walks
+template <class Src>
+int full_recheck_src(const Src &src, const int32_t *frames, const int32_t *n_dev, int64_t n_max, int d,
+                     const float *C, int k, unsigned long long *keys, int32_t *labels, unsigned long long *flipped,
+                     cudaStream_t s, const FlipList *fl) {
+    // Tiles of 32 frames x 256 centers, one CTA per (frame tile, center
+    // block).  The list is usually empty or short (full_few_kernel takes up
+    // to kFullFew frames and this kernel then exits at once); the grid walks
     // the frame tiles, two CTAs per SM in all.
+    constexpr int FT = 4, G = 8, BM = kWarps * FT, BN = 32 * G;
     const int64_t gy = (k + BN - 1) / BN;
     int64_t gx = (n_max + BM - 1) / BM;
     int64_t cap = (int64_t)num_sms() * 2;
     cap = cap / gy > 0 ? cap / gy : 1;
     if (gx > cap) gx = cap;
-    (void)per_sm;
     if (gy > 65535) {
         set_error("k=%d: too many center blocks for the full re-check", k);
         return KM_ERR_BAD_SHAPE;
@@ -467,10 +481,10 @@ int launch_full_recheck(const float *X, const int32_t *frames, const int32_t *n_
     int64_t gf = (std::min(n_max, kFullFew) * k + 7) / 8;  // a warp per (frame, center), 8 warps per block
     const int64_t capf = (int64_t)num_sms() * 4;
     if (gf > capf) gf = capf;
-    full_few_kernel<<<(unsigned)(gf < 1 ? 1 : gf), 256, 0, s>>>(X, frames, n_dev, n_max, d, C, k, keys);
+    full_few_kernel<Src><<<(unsigned)(gf < 1 ? 1 : gf), 256, 0, s>>>(src, frames, n_dev, n_max, d, C, k, keys);
     KM_CUDA(cudaGetLastError());
-    assign_fp32_kernel<FT, G, true><<<dim3((unsigned)gx, (unsigned)gy), kThreads, 0, s>>>(
-        X, frames, n_dev, n_max, d, C, k, nullptr, nullptr, nullptr, keys);
+    assign_fp32_kernel<FT, G, true, Src><<<dim3((unsigned)gx, (unsigned)gy), kThreads, 0, s>>>(
+        src, frames, n_dev, n_max, d, C, k, nullptr, nullptr, nullptr, keys);
     KM_CUDA(cudaGetLastError());
     int64_t g2 = (n_max + 255) / 256;
     const int64_t cap2 = (int64_t)num_sms();
@@ -480,6 +494,41 @@ int launch_full_recheck(const float *X, const int32_t *frames, const int32_t *n_
                                                           fl ? fl->cap : 0);
     KM_CUDA(cudaGetLastError());
     return KM_OK;
+}
+
+PairRows pair_rows(const PairSrc &ps, int d) {
+    return PairRows{ps.xyz, reinterpret_cast<const int2 *>(ps.pairs), ps.n_atoms, d};
+}
+
+}  // namespace
+
+int launch_assign_fp32(const float *X, const int32_t *frame_idx, const int32_t *n_dev, int64_t n,
+                       int d, const float *C, int k, int32_t *labels, float *dist,
+                       unsigned long long *flipped, cudaStream_t s, const PairSrc *ps) {
+    if (n == 0) return KM_OK;
+    if (ps) return assign_fp32_src(pair_rows(*ps, d), frame_idx, n_dev, n, d, C, k, labels, dist, flipped, s);
+    return assign_fp32_src(DenseRows{X, d}, frame_idx, n_dev, n, d, C, k, labels, dist, flipped, s);
+}
+
+int launch_recheck_pairs(const float *X, int d, const float *C, const int32_t *rc_frames, const int32_t *rc_best,
+                         const int64_t *rc_pairs, const int32_t *pair_center, const float *pair_lo,
+                         unsigned long long *keys, int32_t *amb_entries, int32_t *amb_mask, int32_t *counters,
+                         int64_t max_entries, int32_t *labels, unsigned long long *flipped, cudaStream_t s,
+                         const FlipList *fl, int blocks_per_sm, const PairSrc *ps) {
+    if (max_entries == 0) return KM_OK;
+    if (ps)
+        return recheck_pairs_src(pair_rows(*ps, d), d, C, rc_frames, rc_best, rc_pairs, pair_center, pair_lo, keys,
+                                 amb_entries, amb_mask, counters, max_entries, labels, flipped, s, fl, blocks_per_sm);
+    return recheck_pairs_src(DenseRows{X, d}, d, C, rc_frames, rc_best, rc_pairs, pair_center, pair_lo, keys,
+                             amb_entries, amb_mask, counters, max_entries, labels, flipped, s, fl, blocks_per_sm);
+}
+
+int launch_full_recheck(const float *X, const int32_t *frames, const int32_t *n_dev, int64_t n_max, int d,
+                        const float *C, int k, unsigned long long *keys, int32_t *labels,
+                        unsigned long long *flipped, cudaStream_t s, const FlipList *fl, const PairSrc *ps) {
+    if (n_max == 0) return KM_OK;
+    if (ps) return full_recheck_src(pair_rows(*ps, d), frames, n_dev, n_max, d, C, k, keys, labels, flipped, s, fl);
+    return full_recheck_src(DenseRows{X, d}, frames, n_dev, n_max, d, C, k, keys, labels, flipped, s, fl);
 }
 
 }  // namespace km

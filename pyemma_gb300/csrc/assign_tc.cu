@@ -513,8 +513,8 @@ __global__ void scale_finalize_kernel(uint32_t *__restrict__ scal) {
 
 // Frames: one warp per row.  xnorm = (||x_hat||^2 in scaled units, upper
 // bound of ||x'||, upper bound of ||x_hat/s - x'||, 0) in unscaled units.
-template <typename T>
-__global__ void prep_frames_kernel(const float *__restrict__ X, int64_t n, int d, int kp,
+template <typename T, class Src>
+__global__ void prep_frames_kernel(const Src rows, int64_t n, int d, int kp,
                                    const float *__restrict__ shift, const uint32_t *__restrict__ scal,
                                    T *__restrict__ xh, float4 *__restrict__ xnorm, float norm_inflate) {
     using O = Op16<T>;
@@ -524,7 +524,6 @@ __global__ void prep_frames_kernel(const float *__restrict__ X, int64_t n, int d
     const float sc = __uint_as_float(scal[kScale]);
     const float inv_sc = 1.0f / sc;  // exact: a power of two
     for (int64_t i = w; i < n; i += nw) {
-        const float *src = X + i * d;
         typename O::T2 *dst = reinterpret_cast<typename O::T2 *>(xh + i * kp);
         CSum h2, s2, e2;
         for (int f = 2 * lane; f < kp; f += 64) {
@@ -532,13 +531,13 @@ __global__ void prep_frames_kernel(const float *__restrict__ X, int64_t n, int d
             // meet the hi/lo norm columns of the centers); the rest: 0.
             float a = 0.0f, b = 0.0f, ia, ib;
             if (f < d) {
-                a = __fsub_rn(src[f], shift[f]);
+                a = __fsub_rn(rows.get(i, f), shift[f]);
                 ia = a * sc;
             } else {
                 ia = (f == d || f == d + 1) ? 1.0f : 0.0f;
             }
             if (f + 1 < d) {
-                b = __fsub_rn(src[f + 1], shift[f + 1]);
+                b = __fsub_rn(rows.get(i, f + 1), shift[f + 1]);
                 ib = b * sc;
             } else {
                 ib = (f + 1 == d || f + 1 == d + 1) ? 1.0f : 0.0f;
@@ -1819,14 +1818,30 @@ void prepare_frames_t(const float *X, int64_t n, int d, TcBuffers &b, cudaStream
             default: launch_prep_v4<T, 9>(X, n, d, b, s); break;
         }
     } else {
-        prep_frames_kernel<T><<<(unsigned)prep_blocks(n), 256, 0, s>>>(X, n, d, b.kp, b.shift, b.scal,
+        prep_frames_kernel<T><<<(unsigned)prep_blocks(n), 256, 0, s>>>(DenseRows{X, d}, n, d, b.kp, b.shift, b.scal,
                                                                      reinterpret_cast<T *>(b.xh), b.xnorm,
                                                                      norm_inflate_of(d));
     }
 }
 
-int tc_prepare_frames(const float *X, int64_t n, int d, TcBuffers &b, cudaStream_t s) {
+int tc_prepare_frames(const float *X, int64_t n, int d, TcBuffers &b, cudaStream_t s, const PairSrc *ps) {
     if (n == 0) return KM_OK;
+    if (ps) {
+        // pair features computed in the conversion: no float32 copy of them
+        if (b.fp8) {
+            set_error("FP8 operands are not built for coordinate frames");
+            return KM_ERR_UNSUPPORTED;
+        }
+        const PairRows pr{ps->xyz, reinterpret_cast<const int2 *>(ps->pairs), ps->n_atoms, d};
+        if (b.bf16)
+            prep_frames_kernel<__nv_bfloat16><<<(unsigned)prep_blocks(n), 256, 0, s>>>(
+                pr, n, d, b.kp, b.shift, b.scal, reinterpret_cast<__nv_bfloat16 *>(b.xh), b.xnorm, norm_inflate_of(d));
+        else
+            prep_frames_kernel<__half><<<(unsigned)prep_blocks(n), 256, 0, s>>>(
+                pr, n, d, b.kp, b.shift, b.scal, reinterpret_cast<__half *>(b.xh), b.xnorm, norm_inflate_of(d));
+        KM_CUDA(cudaGetLastError());
+        return KM_OK;
+    }
     if (b.fp8)
         prep_frames_fp8_kernel<<<(unsigned)prep_blocks(n), 256, 0, s>>>(
             X, n, d, b.kp, b.shift, b.scal, static_cast<uint8_t *>(b.xh), b.xnorm, norm_inflate_of(d));
@@ -1862,7 +1877,7 @@ constexpr int kRecheckBesidePerSm = 4;
 
 int tc_assign_impl(const float *X, int64_t n, int d, const float *C, int k, int32_t *labels, TcBuffers &b,
                    cudaStream_t s, ProfEvents *prof, float *dump, unsigned long long *wait_cycles, cudaStream_t side,
-                   cudaEvent_t ev_fork, const FlipList *fl) {
+                   cudaEvent_t ev_fork, const FlipList *fl, const PairSrc *ps) {
     if (n == 0) return KM_OK;
     Plan pl;
     if (!make_plan(d, k, pl, b.fp8 != 0) || !device_is_sm10x()) {
@@ -2022,10 +2037,11 @@ int tc_assign_impl(const float *X, int64_t n, int d, const float *C, int k, int3
     // threads, so that both stay resident.
     KM_TRY(launch_recheck_pairs(X, d, C, b.rc_frames, b.rc_best, b.rc_pairs, b.pair_center, b.pair_lo, b.rc_keys,
                                 b.amb_entries, b.amb_mask, b.counters, n, labels, b.flipped, r, fl,
-                                side ? kRecheckBesidePerSm : 8));
+                                side ? kRecheckBesidePerSm : 8, ps));
     if (prof) prof->end(kProfRecheck, r);
     if (prof) prof->begin(kProfFull, r);
-    KM_TRY(launch_full_recheck(X, b.full_frames, b.counters + 1, n, d, C, k, b.full_keys, labels, b.flipped, r, fl));
+    KM_TRY(launch_full_recheck(X, b.full_frames, b.counters + 1, n, d, C, k, b.full_keys, labels, b.flipped, r, fl,
+                               ps));
     if (prof) prof->end(kProfFull, r);
     return KM_OK;
 }
@@ -2033,14 +2049,14 @@ int tc_assign_impl(const float *X, int64_t n, int d, const float *C, int k, int3
 }  // namespace
 
 int tc_assign(const float *X, int64_t n, int d, const float *C, int k, int32_t *labels, TcBuffers &b,
-              cudaStream_t s, ProfEvents *prof, float *dump, unsigned long long *wait_cycles) {
-    return tc_assign_impl(X, n, d, C, k, labels, b, s, prof, dump, wait_cycles, nullptr, nullptr, nullptr);
+              cudaStream_t s, ProfEvents *prof, float *dump, unsigned long long *wait_cycles, const PairSrc *ps) {
+    return tc_assign_impl(X, n, d, C, k, labels, b, s, prof, dump, wait_cycles, nullptr, nullptr, nullptr, ps);
 }
 
 int tc_assign_deferred(const float *X, int64_t n, int d, const float *C, int k, int32_t *labels, TcBuffers &b,
                        cudaStream_t s, cudaStream_t side, cudaEvent_t ev_fork, const FlipList &fl,
-                       ProfEvents *prof) {
-    return tc_assign_impl(X, n, d, C, k, labels, b, s, prof, nullptr, nullptr, side, ev_fork, &fl);
+                       ProfEvents *prof, const PairSrc *ps) {
+    return tc_assign_impl(X, n, d, C, k, labels, b, s, prof, nullptr, nullptr, side, ev_fork, &fl, ps);
 }
 
 }  // namespace km

@@ -160,7 +160,8 @@ int check_device_errors(uint32_t e) {
 // centers_ready means the
 // center half (FP16 copy, norms, shift, scale) is already prepared.
 int assign_core(const float *X, int64_t n, int32_t d, const float *C, int32_t k, int prec, int32_t *labels,
-                TcBuffers &b, bool centers_ready, km_assign_stats *stats, cudaStream_t s) {
+                TcBuffers &b, bool centers_ready, km_assign_stats *stats, cudaStream_t s,
+                const PairSrc *ps = nullptr) {
     if (stats) {
         std::memset(stats, 0, sizeof(*stats));
         stats->n_frames = n;
@@ -175,7 +176,7 @@ int assign_core(const float *X, int64_t n, int32_t d, const float *C, int32_t k,
     } closer{prof};
     if (prec == KM_PREC_FP32) {
         prof.begin(kProfFp32, s);
-        KM_TRY(launch_assign_fp32(X, nullptr, nullptr, n, d, C, k, labels, nullptr, nullptr, s));
+        KM_TRY(launch_assign_fp32(X, nullptr, nullptr, n, d, C, k, labels, nullptr, nullptr, s, ps));
         prof.end(kProfFp32, s);
         if (stats || prof.active) KM_CUDA(cudaStreamSynchronize(s));
         prof.collect();
@@ -185,8 +186,8 @@ int assign_core(const float *X, int64_t n, int32_t d, const float *C, int32_t k,
         KM_TRY(tc_prepare_shift_from_centers(C, d, k, b, s));
         KM_TRY(tc_prepare_centers(C, d, k, b, s));
     }
-    KM_TRY(tc_prepare_frames(X, n, d, b, s));
-    KM_TRY(tc_assign(X, n, d, C, k, labels, b, s, &prof));
+    KM_TRY(tc_prepare_frames(X, n, d, b, s, ps));
+    KM_TRY(tc_assign(X, n, d, C, k, labels, b, s, &prof, nullptr, nullptr, ps));
     if (prof.active) {
         KM_CUDA(cudaStreamSynchronize(s));
         prof.collect();
@@ -209,9 +210,10 @@ int assign_core(const float *X, int64_t n, int32_t d, const float *C, int32_t k,
 }
 
 int assign_impl(const float *X, int64_t n, int32_t d, const float *C, int32_t k, int32_t precision,
-                int32_t *labels, void *ws, size_t ws_bytes, km_assign_stats *stats, cudaStream_t s) {
+                int32_t *labels, void *ws, size_t ws_bytes, km_assign_stats *stats, cudaStream_t s,
+                const PairSrc *ps = nullptr) {
     KM_TRY(check_shape(n, d, k));
-    if ((n > 0 && (!X || !labels)) || !C) {
+    if ((n > 0 && ((!X && !ps) || !labels)) || !C) {
         set_error("X, C and labels must be non-NULL");
         return KM_ERR_BAD_SHAPE;
     }
@@ -230,7 +232,11 @@ int assign_impl(const float *X, int64_t n, int32_t d, const float *C, int32_t k,
         carve_assign(ws, n, d, k, b);
         tc_set_operand(b, d, prec);
     }
-    return assign_core(X, n, d, C, k, prec, labels, b, false, stats, s);
+    if (ps && prec == KM_PREC_FP8) {
+        set_error("FP8 operands are not built for coordinate frames");
+        return KM_ERR_UNSUPPORTED;
+    }
+    return assign_core(X, n, d, C, k, prec, labels, b, false, stats, s, ps);
 }
 
 // Workspace of an assignment whose centers are prepared: frames + lists.
@@ -245,6 +251,23 @@ size_t resident_ws_bytes(int64_t n, int d, int k, int prec) {
 // condition, so a run of iterations costs one launch and one read-back.
 // A launch runs at most kLoopBatch iterations (the size of the inertia
 // buffer in the workspace).
+// dst (device) <- src (pageable host, readable by the device): 16-byte
+// words where both ends and the length allow, else 4-byte words.
+__global__ void __launch_bounds__(256) host_copy_kernel(const float *__restrict__ src, float *__restrict__ dst,
+                                                        int64_t count) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    if (((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst)) & 15) == 0) {
+        const int64_t n4 = count >> 2;
+        const float4 *s4 = reinterpret_cast<const float4 *>(src);
+        float4 *d4 = reinterpret_cast<float4 *>(dst);
+        for (int64_t i = t; i < n4; i += stride) d4[i] = s4[i];
+        for (int64_t i = (n4 << 2) + t; i < count; i += stride) dst[i] = src[i];
+    } else {
+        for (int64_t i = t; i < count; i += stride) dst[i] = src[i];
+    }
+}
+
 struct LoopState {
     double prev;
     double tol;
@@ -558,19 +581,39 @@ int stage_workers() {
     return std::max(2, std::min(16, w));
 }
 
+// True when the host memory at p is ordinary pageable memory.
+bool is_pageable(const void *p) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return true;
+    }
+    return a.type == cudaMemoryTypeUnregistered;
+}
+
 // True when some part of the host frames is ordinary pageable memory.
 bool has_pageable_part(const float *const *parts, const int64_t *rows, int32_t n_parts) {
-    for (int32_t q = 0; q < n_parts; ++q) {
-        if (rows[q] <= 0) continue;
-        cudaPointerAttributes a{};
-        if (cudaPointerGetAttributes(&a, parts[q]) != cudaSuccess) {
-            cudaGetLastError();
-            return true;
-        }
-        if (a.type == cudaMemoryTypeUnregistered) return true;
-    }
+    for (int32_t q = 0; q < n_parts; ++q)
+        if (rows[q] > 0 && is_pageable(parts[q])) return true;
     return false;
 }
+
+// True when kernels on the current device may read pageable host memory in
+// place through the host's page tables (Grace-based systems: NVLink-C2C with
+// address translation).  Then a copy kernel moves pageable frames at the
+// link's rate without host-side staging, and, unlike a cudaMemcpyAsync from
+// pageable memory, its launch returns at once.
+bool gpu_reads_pageable_host() {
+    int dev = 0, pma = 0, pht = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&pma, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&pht, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return pma == 1 && pht == 1;
+}
+
 
 struct Stager {
     struct Block {
@@ -727,9 +770,9 @@ struct Stager {
 int lloyd_run(const float *X_in, const HostFrames *hf, int64_t n, int32_t d, int32_t k, float *C, int32_t max_iter,
               double tolerance, int32_t precision, int32_t *labels, double *inertias, int32_t *n_iter,
               int32_t *converged, km_callback cb, void *cb_user, void *workspace, size_t workspace_bytes,
-              void *stream) {
+              void *stream, const PairSrc *ps = nullptr) {
     KM_TRY(check_shape(n, d, k));
-    if (n < 1 || !X_in || !C || !labels || !n_iter || !converged || max_iter < 0) {
+    if (n < 1 || (!X_in && !ps) || !C || !labels || !n_iter || !converged || max_iter < 0) {
         set_error("Lloyd needs n >= 1, max_iter >= 0 and non-NULL X, C, labels, n_iter, converged");
         return KM_ERR_BAD_SHAPE;
     }
@@ -774,7 +817,7 @@ int lloyd_run(const float *X_in, const HostFrames *hf, int64_t n, int32_t d, int
         const int64_t chunk = stream_chunk_rows(n);
         for (int64_t a = 0; a < n; a += chunk) sm.begin.push_back(a);
         sm.begin.push_back(n);
-        if (has_pageable_part(hf->parts, hf->rows, hf->n_parts)) {
+        if (has_pageable_part(hf->parts, hf->rows, hf->n_parts) && !gpu_reads_pageable_host()) {
             // Workers stage the pageable frames; X must not be in use on s
             // any more (the caller's stream is drained first).
             KM_CUDA(cudaStreamSynchronize(s));
@@ -790,6 +833,8 @@ int lloyd_run(const float *X_in, const HostFrames *hf, int64_t n, int32_t d, int
         }
     }
     if (hf && !stager) {
+        std::vector<char> pageable_part(hf->n_parts, 0);
+        for (int32_t q = 0; q < hf->n_parts; ++q) pageable_part[q] = hf->rows[q] > 0 && is_pageable(hf->parts[q]);
         KM_CUDA(cudaStreamCreateWithFlags(&sm.cs, cudaStreamNonBlocking));
         sm.ev.assign(sm.begin.size(), nullptr);  // [0]: the caller's stream reached this call
         for (cudaEvent_t &e : sm.ev) KM_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
@@ -806,8 +851,17 @@ int lloyd_run(const float *X_in, const HostFrames *hf, int64_t n, int32_t d, int
                     q_off = 0;
                 }
                 const int64_t take = std::min(stop - row, hf->rows[q] - q_off);
-                KM_CUDA(cudaMemcpyAsync(X + row * d, hf->parts[q] + q_off * d, sizeof(float) * (size_t)take * d,
-                                        cudaMemcpyHostToDevice, sm.cs));
+                if (pageable_part[q]) {
+                    // read in place by the device (gpu_reads_pageable_host)
+                    const int64_t count = take * d;
+                    const int64_t g = std::min<int64_t>((count / 4 + 255) / 256, (int64_t)num_sms() * 4);
+                    host_copy_kernel<<<(unsigned)(g < 1 ? 1 : g), 256, 0, sm.cs>>>(hf->parts[q] + q_off * d,
+                                                                                  X + row * d, count);
+                    KM_CUDA(cudaGetLastError());
+                } else {
+                    KM_CUDA(cudaMemcpyAsync(X + row * d, hf->parts[q] + q_off * d, sizeof(float) * (size_t)take * d,
+                                            cudaMemcpyHostToDevice, sm.cs));
+                }
                 row += take;
                 q_off += take;
             }
@@ -859,7 +913,7 @@ int lloyd_run(const float *X_in, const HostFrames *hf, int64_t n, int32_t d, int
         carve_assign(ws_assign, n, d, k, b);
         tc_set_operand(b, d, prec);
         KM_TRY(tc_prepare_shift_from_centers(C, d, k, b, s));
-        if (!hf) KM_TRY(tc_prepare_frames(X, n, d, b, s));
+        if (!hf) KM_TRY(tc_prepare_frames(X, n, d, b, s, ps));
     }
     KM_CUDA(cudaMemsetAsync(err, 0, sizeof(uint32_t), s));
 
@@ -876,7 +930,7 @@ int lloyd_run(const float *X_in, const HostFrames *hf, int64_t n, int32_t d, int
     } closer{prof};
     auto enqueue_update = [&](cudaStream_t st) -> int {
         prof.begin(kProfUpdate, st);
-        KM_TRY(launch_update(X, n, d, labels, k, C, C_new, nullptr, cost, err, ws_update, st));
+        KM_TRY(launch_update(X, n, d, labels, k, C, C_new, nullptr, cost, err, ws_update, st, ps));
         prof.end(kProfUpdate, st);
         KM_CUDA(cudaMemcpyAsync(C, C_new, sizeof(float) * k * d, cudaMemcpyDeviceToDevice, st));
         return KM_OK;
@@ -885,20 +939,20 @@ int lloyd_run(const float *X_in, const HostFrames *hf, int64_t n, int32_t d, int
         if (is_tc(prec)) {
             KM_TRY(tc_prepare_centers(C, d, k, b, st));
             KM_CUDA(cudaMemsetAsync(fl.count, 0, sizeof(int32_t), st));
-            KM_TRY(tc_assign_deferred(X, n, d, C, k, labels, b, st, side.st, side.fork, fl, &prof));
+            KM_TRY(tc_assign_deferred(X, n, d, C, k, labels, b, st, side.st, side.fork, fl, &prof, ps));
             prof.begin(kProfUpdate, st);
             // one segment-sum CTA per SM: room for the re-check beside it
-            KM_TRY(launch_update_accumulate(X, n, d, labels, k, C, err, ws_update, st, 1));
+            KM_TRY(launch_update_accumulate(X, n, d, labels, k, C, err, ws_update, st, 1, ps));
             KM_CUDA(cudaEventRecord(side.join, side.st));
             KM_CUDA(cudaStreamWaitEvent(st, side.join, 0));
-            KM_TRY(launch_apply_flips(X, n, d, k, C, fl, labels, ws_update, st));
+            KM_TRY(launch_apply_flips(X, n, d, k, C, fl, labels, ws_update, st, ps));
             KM_TRY(launch_update_finish(n, d, k, C, C_new, nullptr, cost, ws_update, st));
             prof.end(kProfUpdate, st);
             KM_CUDA(cudaMemcpyAsync(C, C_new, sizeof(float) * k * d, cudaMemcpyDeviceToDevice, st));
             return KM_OK;
         } else {
             prof.begin(kProfFp32, st);
-            KM_TRY(launch_assign_fp32(X, nullptr, nullptr, n, d, C, k, labels, nullptr, nullptr, st));
+            KM_TRY(launch_assign_fp32(X, nullptr, nullptr, n, d, C, k, labels, nullptr, nullptr, st, ps));
             prof.end(kProfFp32, st);
         }
         return enqueue_update(st);
@@ -1098,6 +1152,79 @@ int km_lloyd(const float *X, int64_t n, int32_t d, int32_t k, float *C, int32_t 
              km_callback cb, void *cb_user, void *workspace, size_t workspace_bytes, void *stream) {
     return lloyd_run(X, nullptr, n, d, k, C, max_iter, tolerance, precision, labels, inertias, n_iter, converged, cb,
                      cb_user, workspace, workspace_bytes, stream);
+}
+
+// ---- frames given as atom coordinates (the featurization fused in) ---------
+
+namespace {
+int check_pair_args(const float *xyz, int64_t n, int32_t n_atoms, const int32_t *pairs, int32_t d,
+                    cudaStream_t s) {
+    if (n_atoms < 1 || (n > 0 && !xyz) || !pairs) {
+        set_error("coordinates need n_atoms >= 1 and non-NULL xyz and pairs");
+        return KM_ERR_BAD_SHAPE;
+    }
+    return check_pairs(pairs, d, n_atoms, s);
+}
+}  // namespace
+
+size_t km_assign_pairs_workspace_size(int64_t n, int32_t d, int32_t k, int32_t precision) {
+    return km_assign_workspace_size(n, d, k, precision);
+}
+
+int km_assign_pairs(const float *xyz, int64_t n, int32_t n_atoms, const int32_t *pairs, int32_t d, const float *C,
+                    int32_t k, int32_t precision, int32_t *labels, void *workspace, size_t workspace_bytes,
+                    km_assign_stats *stats, void *stream) {
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    KM_TRY(check_shape(n, d, k));
+    KM_TRY(check_pair_args(xyz, n, n_atoms, pairs, d, s));
+    PairSrc ps;
+    ps.xyz = xyz;
+    ps.pairs = pairs;
+    ps.n_atoms = n_atoms;
+    return assign_impl(nullptr, n, d, C, k, precision, labels, workspace, workspace_bytes, stats, s, &ps);
+}
+
+size_t km_lloyd_pairs_workspace_size(int64_t n, int32_t d, int32_t k, int32_t precision) {
+    return km_lloyd_workspace_size(n, d, k, precision);
+}
+
+int km_lloyd_pairs(const float *xyz, int64_t n, int32_t n_atoms, const int32_t *pairs, int32_t d, int32_t k,
+                   float *C, int32_t max_iter, double tolerance, int32_t precision, int32_t *labels,
+                   double *inertias, int32_t *n_iter, int32_t *converged, km_callback cb, void *cb_user,
+                   void *workspace, size_t workspace_bytes, void *stream) {
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    KM_TRY(check_shape(n, d, k));
+    KM_TRY(check_pair_args(xyz, n, n_atoms, pairs, d, s));
+    if (resolve_precision(precision, d, k, true) == KM_PREC_FP8) {
+        set_error("FP8 operands are not built for coordinate frames");
+        return KM_ERR_UNSUPPORTED;
+    }
+    PairSrc ps;
+    ps.xyz = xyz;
+    ps.pairs = pairs;
+    ps.n_atoms = n_atoms;
+    return lloyd_run(nullptr, nullptr, n, d, k, C, max_iter, tolerance, precision, labels, inertias, n_iter, converged,
+                     cb, cb_user, workspace, workspace_bytes, stream, &ps);
+}
+
+size_t km_kmpp_pairs_workspace_size(int64_t n, int32_t d, int32_t k) { return km_kmpp_workspace_size(n, d, k); }
+
+int km_kmpp_pairs(const float *xyz, int64_t n, int32_t n_atoms, const int32_t *pairs, int32_t d, int32_t k,
+                  uint32_t seed, float *C0, int64_t *idx, km_callback cb, void *cb_user, void *workspace,
+                  size_t workspace_bytes, void *stream) {
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    KM_TRY(check_shape(n, d, k));
+    if (n < 1 || !C0) {
+        set_error("kmeans++ needs n >= 1 and non-NULL C0");
+        return KM_ERR_BAD_SHAPE;
+    }
+    KM_TRY(check_pair_args(xyz, n, n_atoms, pairs, d, s));
+    KM_TRY(check_ws(workspace, workspace_bytes, kmpp_ws_size(n, d, k)));
+    PairSrc ps;
+    ps.xyz = xyz;
+    ps.pairs = pairs;
+    ps.n_atoms = n_atoms;
+    return run_kmpp(nullptr, n, d, k, seed, C0, idx, cb, cb_user, workspace, s, nullptr, &ps);
 }
 
 int km_lloyd_host(const float *const *X_parts, const int64_t *part_rows, int32_t n_parts, float *X, int64_t n,

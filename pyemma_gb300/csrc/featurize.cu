@@ -14,6 +14,8 @@
 //
 // One thread per output feature in frame-major order, so the writes of a
 // warp are coalesced; the coordinates of the frame come through L1.
+#include <vector>
+
 #include "km_common.cuh"
 #include "km_internal.h"
 
@@ -42,6 +44,22 @@ __global__ void __launch_bounds__(256) pair_distances_kernel(const float *__rest
 
 }  // namespace
 
+// Atom pairs (device, npairs x 2) are read back (a few KB) and checked on the
+// host: an index outside [0, n_atoms) would make every kernel that computes
+// the features read outside the coordinates.
+int check_pairs(const int32_t *pairs, int32_t npairs, int32_t n_atoms, cudaStream_t s) {
+    if (npairs <= 0) return KM_OK;
+    std::vector<int32_t> h((size_t)npairs * 2);
+    KM_CUDA(cudaMemcpyAsync(h.data(), pairs, h.size() * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    KM_CUDA(cudaStreamSynchronize(s));
+    for (size_t q = 0; q < h.size(); ++q)
+        if (h[q] < 0 || h[q] >= n_atoms) {
+            set_error("pair %zu names atom %d, outside [0, %d)", q / 2, h[q], n_atoms);
+            return KM_ERR_BAD_SHAPE;
+        }
+    return KM_OK;
+}
+
 }  // namespace km
 
 using namespace km;
@@ -56,6 +74,7 @@ int km_pair_distances(const float *xyz, int64_t n, int32_t n_atoms, const int32_
     }
     const int64_t total = n * (int64_t)npairs;
     if (total == 0) return KM_OK;
+    KM_TRY(check_pairs(pairs, npairs, n_atoms, static_cast<cudaStream_t>(stream)));
     int64_t g = (total + 255) / 256;
     const int64_t cap = (int64_t)num_sms() * 16;
     if (g > cap) g = cap;

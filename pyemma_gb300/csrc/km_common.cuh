@@ -172,6 +172,43 @@ __device__ __forceinline__ float sqdist_exact(const float *__restrict__ x, const
     return acc;
 }
 
+// ---------------------------------------------------------------------------
+// Frame rows of the kernels that read float32 features: a dense row-major
+// (n, d) matrix, or atom-pair distances computed from coordinates on the fly
+// (the featurization fused into the discretization).  A pair feature is the
+// float32 value km_pair_distances writes, bit for bit:
+//   sqrt((dx*dx + dy*dy) + dz*dz),  (dx, dy, dz) = xyz[pair.y] - xyz[pair.x].
+// ---------------------------------------------------------------------------
+struct DenseRows {
+    const float *X;
+    int d;
+    __device__ __forceinline__ float get(int64_t i, int f) const { return __ldg(X + i * d + f); }
+};
+
+struct PairRows {
+    const float *xyz;   // (n, n_atoms, 3) frame-major
+    const int2 *pairs;  // d atom pairs
+    int n_atoms;
+    int d;
+    __device__ __forceinline__ float get(int64_t i, int f) const {
+        const int2 p = __ldg(pairs + f);
+        const float *a = xyz + (i * n_atoms + p.x) * 3;
+        const float *b = xyz + (i * n_atoms + p.y) * 3;
+        const float dx = __fsub_rn(__ldg(b), __ldg(a));
+        const float dy = __fsub_rn(__ldg(b + 1), __ldg(a + 1));
+        const float dz = __fsub_rn(__ldg(b + 2), __ldg(a + 2));
+        return __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)));
+    }
+};
+
+// The exact float32 squared distance of sqdist_exact for a row source.
+template <class Src>
+__device__ __forceinline__ float sqdist_exact_src(const Src &src, int64_t i, const float *__restrict__ c, int d) {
+    float acc = 0.0f;
+    for (int f = 0; f < d; ++f) acc = __fadd_rn(acc, sq_term(src.get(i, f), __ldg(c + f)));
+    return acc;
+}
+
 // Neumaier-compensated float32 sum: value() is within a few u of the exact
 // sum of the added terms (plus an O(n u^2) remainder).
 struct CSum {

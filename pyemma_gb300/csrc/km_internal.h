@@ -12,6 +12,20 @@
 
 namespace km {
 
+// Frames given as atom coordinates: feature f of frame i is the distance
+// between atoms pairs[2f] and pairs[2f+1] of xyz[i] (device arrays).  The
+// launchers below take a nullable PairSrc; when it is set, X is ignored and
+// every float32 feature is computed from the coordinates where it is read.
+struct PairSrc {
+    const float *xyz = nullptr;   // (n, n_atoms, 3)
+    const int32_t *pairs = nullptr;  // (d, 2)
+    int n_atoms = 0;
+};
+
+// featurize.cu: KM_ERR_BAD_SHAPE unless every atom index of the pairs (device,
+// npairs x 2) lies in [0, n_atoms); synchronises s.
+int check_pairs(const int32_t *pairs, int32_t npairs, int32_t n_atoms, cudaStream_t s);
+
 // ---- profiling (capi.cu) ------------------------------------------------------
 // Event pairs recorded around the main kernels of one pass when profiling is
 // on (km_profile_enable).  Inside a captured graph the records become event
@@ -36,7 +50,7 @@ struct ProfEvents {
 // counts frames whose new label differs from the one already in labels.
 int launch_assign_fp32(const float *X, const int32_t *frame_idx, const int32_t *n_dev, int64_t n,
                        int d, const float *C, int k, int32_t *labels, float *dist,
-                       unsigned long long *flipped, cudaStream_t s);
+                       unsigned long long *flipped, cudaStream_t s, const PairSrc *ps = nullptr);
 
 // Labels that an exact re-check changes, listed instead of written: entry i
 // is (frame, label before, exact label) at rows[3i..3i+2]; *count (device)
@@ -54,7 +68,8 @@ struct FlipList {
 // With fl the changed labels go to the list and labels stays as it is.
 int launch_full_recheck(const float *X, const int32_t *frames, const int32_t *n_dev, int64_t n_max, int d,
                         const float *C, int k, unsigned long long *keys, int32_t *labels,
-                        unsigned long long *flipped, cudaStream_t s, const FlipList *fl = nullptr);
+                        unsigned long long *flipped, cudaStream_t s, const FlipList *fl = nullptr,
+                        const PairSrc *ps = nullptr);
 
 // Re-evaluation of the candidates the tensor-core kernel could not
 // separate.  Entry e stands for frame rc_frames[e]; its candidates are the
@@ -70,7 +85,7 @@ int launch_recheck_pairs(const float *X, int d, const float *C, const int32_t *r
                          const int64_t *rc_pairs, const int32_t *pair_center, const float *pair_lo,
                          unsigned long long *keys, int32_t *amb_entries, int32_t *amb_mask, int32_t *counters,
                          int64_t max_entries, int32_t *labels, unsigned long long *flipped, cudaStream_t s,
-                         const FlipList *fl = nullptr, int blocks_per_sm = 8);
+                         const FlipList *fl = nullptr, int blocks_per_sm = 8, const PairSrc *ps = nullptr);
 
 // ---- update.cu -------------------------------------------------------------
 size_t update_ws_size(int64_t n, int d, int k);
@@ -78,12 +93,13 @@ size_t update_ws_size(int64_t n, int d, int k);
 // uint32) receives kDevBadLabel when a label is outside [0, k).
 int launch_update(const float *X, int64_t n, int d, const int32_t *labels, int k,
                   const float *C_old, float *C_new, int64_t *counts_out, double *cost,
-                  uint32_t *err, void *ws, cudaStream_t s);
+                  uint32_t *err, void *ws, cudaStream_t s, const PairSrc *ps = nullptr);
 // launch_update in two halves: the sums over the members (counting sort and
 // segment sums) and the new centers and inertia from those sums.
 // seg_per_sm > 0 caps the segment-sum CTAs per SM (room for a kernel beside it).
 int launch_update_accumulate(const float *X, int64_t n, int d, const int32_t *labels, int k, const float *C_old,
-                             uint32_t *err, void *ws, cudaStream_t s, int seg_per_sm = 0);
+                             uint32_t *err, void *ws, cudaStream_t s, int seg_per_sm = 0,
+                             const PairSrc *ps = nullptr);
 int launch_update_finish(int64_t n, int d, int k, const float *C_old, float *C_new, int64_t *counts_out,
                          double *cost, void *ws, cudaStream_t s);
 // The update of frames that arrive in parts: begin clears the totals, each
@@ -100,7 +116,7 @@ int launch_update_parts_finish(int64_t n, int d, int k, const float *C_old, floa
 // their first label to that of their exact label (sums, squared sums, counts,
 // with the accumulation's float32 deviations) and writes the exact labels.
 int launch_apply_flips(const float *X, int64_t n, int d, int k, const float *C_old, const FlipList &fl,
-                       int32_t *labels, void *ws, cudaStream_t s);
+                       int32_t *labels, void *ws, cudaStream_t s, const PairSrc *ps = nullptr);
 
 // ---- kmpp.cu -----------------------------------------------------------------
 size_t kmpp_ws_size(int64_t n, int d, int k);
@@ -113,7 +129,8 @@ struct KmppMetric {
     const int64_t *idx;
 };
 int run_kmpp(const float *X, int64_t n, int d, int k, uint32_t seed, float *C0, int64_t *idx,
-             void (*cb)(void *), void *cb_user, void *ws, cudaStream_t s, const KmppMetric *metric = nullptr);
+             void (*cb)(void *), void *cb_user, void *ws, cudaStream_t s, const KmppMetric *metric = nullptr,
+             const PairSrc *ps = nullptr);
 
 
 // ---- assign_tc.cu ------------------------------------------------------------
@@ -190,7 +207,7 @@ void tc_carve_assign(void *ws, int64_t n, int d, int k, TcBuffers &b);
 
 // shift == nullptr: the shift is the mean of the centers (computed on device).
 int tc_prepare_shift_from_centers(const float *C, int d, int k, TcBuffers &b, cudaStream_t s);
-int tc_prepare_frames(const float *X, int64_t n, int d, TcBuffers &b, cudaStream_t s);
+int tc_prepare_frames(const float *X, int64_t n, int d, TcBuffers &b, cudaStream_t s, const PairSrc *ps = nullptr);
 int tc_prepare_centers(const float *C, int d, int k, TcBuffers &b, cudaStream_t s);
 // Runs the tensor-core pass, the candidate recheck and the full recheck.
 // dump (nullable, n x k floats) receives every tensor-core distance;
@@ -198,14 +215,14 @@ int tc_prepare_centers(const float *C, int d, int k, TcBuffers &b, cudaStream_t 
 // spent waiting (diagnostics).
 int tc_assign(const float *X, int64_t n, int d, const float *C, int k, int32_t *labels,
               TcBuffers &b, cudaStream_t s, ProfEvents *prof = nullptr, float *dump = nullptr,
-              unsigned long long *wait_cycles = nullptr);
+              unsigned long long *wait_cycles = nullptr, const PairSrc *ps = nullptr);
 // The tensor-core pass on s, then the exact re-checks on `side` (after
 // ev_fork, recorded on s) with their changed labels in fl (whose count must
 // be zero when the re-checks start).  labels holds the tensor-core labels;
 // the caller joins `side` back into s before it applies fl.
 int tc_assign_deferred(const float *X, int64_t n, int d, const float *C, int k, int32_t *labels, TcBuffers &b,
                        cudaStream_t s, cudaStream_t side, cudaEvent_t ev_fork, const FlipList &fl,
-                       ProfEvents *prof = nullptr);
+                       ProfEvents *prof = nullptr, const PairSrc *ps = nullptr);
 
 // Resident center sets (capi.cu), used by the serving loop (serve.cu).
 int assign_centers_enqueue(const float *X, int64_t n, const km_centers *h, int32_t *labels, void *ws,

@@ -40,6 +40,7 @@
 #include <climits>
 #include <cmath>
 #include <cstdlib>
+#include <type_traits>
 
 #include "km_common.cuh"
 #include "km_internal.h"
@@ -115,16 +116,30 @@ __device__ __forceinline__ float kmpp_d2(const float *__restrict__ X, int64_t i,
     return __double2float_rn(rmsd_msd_rows(m.Xc + i * d, m.Xc + p * d, m.G[i], m.G[p], d / 3));
 }
 
+// The exact float32 D^2 of frame i of a row source to the center c.
+template <class Src>
+__device__ __forceinline__ float src_d2(const Src &src, int64_t i, const float *__restrict__ c, int d) {
+    if constexpr (std::is_same<Src, DenseRows>::value)
+        return sqdist_exact(src.X + i * d, c, d);
+    else
+        return sqdist_exact_src(src, i, c, d);
+}
+
 // Round 1 pass: mind = D^2 to center 0 (near = 0); max of the finite values.
+template <class Src>
 __global__ void __launch_bounds__(kTileThreads) kmpp_first_kernel(
-    const float *__restrict__ X, int64_t n, int d, const float *__restrict__ c0,
+    const Src src, int64_t n, int d, const float *__restrict__ c0,
     float *__restrict__ mind, int32_t *__restrict__ near, uint32_t *__restrict__ maxbits, KmppMetric m) {
     float mx = 0.0f;
     const int64_t t0 = (int64_t)blockIdx.x * kTile;
     for (int u = 0; u < kTile / kTileThreads; ++u) {
         const int64_t i = t0 + u * kTileThreads + threadIdx.x;
         if (i < n) {
-            const float dd = kmpp_d2(X, i, d, c0, m, 0);
+            float dd;
+            if constexpr (std::is_same<Src, DenseRows>::value)
+                dd = kmpp_d2(src.X, i, d, c0, m, 0);
+            else
+                dd = src_d2(src, i, c0, d);
             mind[i] = dd;
             near[i] = 0;
             if (dd < __int_as_float(0x7f800000) && dd > mx) mx = dd;
@@ -212,8 +227,8 @@ __device__ __forceinline__ unsigned long long cta_exclusive_scan_u64(unsigned lo
 // minima of the other CTAs are read past L1): t = floor(u W / 2^64) for the
 // weight total W over the ntiles tiles, the first frame whose inclusive
 // prefix weight exceeds t (a uniform frame when W = 0), copied into C0[r].
-template <int THREADS>
-__device__ __forceinline__ void kmpp_draw_round(int64_t ntiles, const float *__restrict__ X, int64_t n, int d,
+template <int THREADS, class Src>
+__device__ __forceinline__ void kmpp_draw_round(int64_t ntiles, const Src &src, int64_t n, int d,
                                                 float *__restrict__ C0, int64_t *__restrict__ idx_out,
                                                 const float *__restrict__ mind, int qexp,
                                                 const unsigned long long *__restrict__ tile_sum,
@@ -277,7 +292,7 @@ __device__ __forceinline__ void kmpp_draw_round(int64_t ntiles, const float *__r
     if (pick < 0 && threadIdx.x == 0) pick = (long long)__umul64hi(u, (unsigned long long)n);
     __syncthreads();
     const int64_t p = pick;
-    for (int f = threadIdx.x; f < d; f += THREADS) C0[(int64_t)r * d + f] = X[p * d + f];
+    for (int f = threadIdx.x; f < d; f += THREADS) C0[(int64_t)r * d + f] = src.get(p, f);
     if (threadIdx.x == 0) {
         if (idx_out) idx_out[r] = p;
         *done = 0u;  // for the next round's launch
@@ -305,9 +320,9 @@ __device__ __forceinline__ bool kmpp_last_cta(unsigned int *__restrict__ done) {
 // (two frames per thread: the pass is latency-bound at small n), 256 for
 // minRMSD (the QCP solve needs the registers).  The pruned rounds' first
 // round runs here too (r_center = -1), which stores every tile sum.
-template <int THREADS, bool RMSD>
+template <int THREADS, bool RMSD, class Src>
 __global__ void __launch_bounds__(THREADS) kmpp_round_kernel(
-    const float *__restrict__ X, int64_t n, int d, float *__restrict__ C0, int64_t *__restrict__ idx_out,
+    const Src src, int64_t n, int d, float *__restrict__ C0, int64_t *__restrict__ idx_out,
     float *__restrict__ mind, const int *__restrict__ qexp_p, unsigned long long *__restrict__ tile_sum,
     unsigned int *__restrict__ done, KmppMetric m, int r_center, int r, uint32_t seed) {
     constexpr int kPer = kTile / THREADS;
@@ -321,7 +336,11 @@ __global__ void __launch_bounds__(THREADS) kmpp_round_kernel(
             float mi = mind[i];
             if (r_center >= 0) {
                 const float *c = C0 + (int64_t)r_center * d;
-                const float dd = RMSD ? kmpp_d2(X, i, d, c, m, r_center) : sqdist_exact(X + i * d, c, d);
+                float dd;
+                if constexpr (RMSD)
+                    dd = kmpp_d2(src.X, i, d, c, m, r_center);
+                else
+                    dd = src_d2(src, i, c, d);
                 if (dd < mi) {
                     mi = dd;
                     mind[i] = mi;
@@ -333,7 +352,7 @@ __global__ void __launch_bounds__(THREADS) kmpp_round_kernel(
     s = block_sum_u64(s, red);
     if (threadIdx.x == 0) tile_sum[blockIdx.x] = s;
     if (!kmpp_last_cta(done)) return;
-    kmpp_draw_round<THREADS>(gridDim.x, X, n, d, C0, idx_out, mind, qexp, tile_sum, done, r, seed);
+    kmpp_draw_round<THREADS>(gridDim.x, src, n, d, C0, idx_out, mind, qexp, tile_sum, done, r, seed);
 }
 
 // Pruned round, launch 2: four frames per thread (vector loads of mind and
@@ -388,8 +407,9 @@ __global__ void __launch_bounds__(256) kmpp_prune_kernel(int64_t n, const float 
 // smaller exact distance replaces mind and a and moves the frame's integer
 // weight in its tile's sum (modular 64-bit deltas, exact).  The CTA that
 // finishes last clears the list and draws.
+template <class Src>
 __global__ void __launch_bounds__(256) kmpp_eval_kernel(
-    const float *__restrict__ X, int64_t n, int d, float *__restrict__ C0, int64_t *__restrict__ idx_out,
+    const Src src, int64_t n, int d, float *__restrict__ C0, int64_t *__restrict__ idx_out,
     float *__restrict__ mind, int32_t *__restrict__ near, const int *__restrict__ qexp_p,
     unsigned long long *__restrict__ tile_sum, unsigned int *__restrict__ done, const int32_t *__restrict__ list,
     int32_t *__restrict__ list_n, int64_t ntiles, int r_center, int r, uint32_t seed) {
@@ -398,7 +418,7 @@ __global__ void __launch_bounds__(256) kmpp_eval_kernel(
     const float *c = C0 + (int64_t)r_center * d;
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < cnt; e += (int64_t)gridDim.x * blockDim.x) {
         const int64_t i = list[e];
-        const float dd = sqdist_exact(X + i * d, c, d);
+        const float dd = src_d2(src, i, c, d);
         const float mi = mind[i];
         if (dd < mi) {
             mind[i] = dd;
@@ -409,15 +429,16 @@ __global__ void __launch_bounds__(256) kmpp_eval_kernel(
     }
     if (!kmpp_last_cta(done)) return;
     if (threadIdx.x == 0) *list_n = 0;  // for the next round
-    kmpp_draw_round<256>(ntiles, X, n, d, C0, idx_out, mind, qexp, tile_sum, done, r, seed);
+    kmpp_draw_round<256>(ntiles, src, n, d, C0, idx_out, mind, qexp, tile_sum, done, r, seed);
 }
 
 // Round 0: a uniformly drawn frame, copied into C0[0].
-__global__ void __launch_bounds__(kTileThreads) kmpp_uniform_kernel(const float *__restrict__ X, int64_t n, int d,
+template <class Src>
+__global__ void __launch_bounds__(kTileThreads) kmpp_uniform_kernel(const Src src, int64_t n, int d,
                                                                     float *__restrict__ C0,
                                                                     int64_t *__restrict__ idx_out, uint32_t seed) {
     const int64_t p = (int64_t)__umul64hi(kmpp_draw(seed, 0u), (unsigned long long)n);
-    for (int f = threadIdx.x; f < d; f += blockDim.x) C0[f] = X[p * d + f];
+    for (int f = threadIdx.x; f < d; f += blockDim.x) C0[f] = src.get(p, f);
     if (idx_out && threadIdx.x == 0) idx_out[0] = p;
 }
 
@@ -450,22 +471,20 @@ float prune_factor(int d) {
     return ff;
 }
 
-int run_kmpp(const float *X, int64_t n, int d, int k, uint32_t seed, float *C0, int64_t *idx,
-             void (*cb)(void *), void *cb_user, void *ws, cudaStream_t s, const KmppMetric *metric) {
-    const KmppMetric m = metric ? *metric : KmppMetric{nullptr, nullptr, nullptr};
-    if (n <= 0) {
-        set_error("kmeans++ needs at least one frame");
-        return KM_ERR_BAD_SHAPE;
-    }
+namespace {
+
+template <class Src>
+int run_kmpp_src(const Src &src, int64_t n, int d, int k, uint32_t seed, float *C0, int64_t *idx,
+                 void (*cb)(void *), void *cb_user, void *ws, cudaStream_t s, const KmppMetric &m) {
     KmppWs w = carve(ws, n, k, nullptr);
     const int64_t ntiles = (n + kTile - 1) / kTile;
-    kmpp_uniform_kernel<<<1, kTileThreads, 0, s>>>(X, n, d, C0, idx, seed);
+    kmpp_uniform_kernel<<<1, kTileThreads, 0, s>>>(src, n, d, C0, idx, seed);
     KM_CUDA(cudaGetLastError());
     if (cb) cb(cb_user);
     if (k == 1) return KM_OK;
     KM_CUDA(cudaMemsetAsync(w.maxbits, 0, sizeof(uint32_t), s));
     KM_CUDA(cudaMemsetAsync(w.done, 0, sizeof(unsigned int), s));
-    kmpp_first_kernel<<<(unsigned)ntiles, kTileThreads, 0, s>>>(X, n, d, C0, w.mind, w.near, w.maxbits, m);
+    kmpp_first_kernel<<<(unsigned)ntiles, kTileThreads, 0, s>>>(src, n, d, C0, w.mind, w.near, w.maxbits, m);
     KM_CUDA(cudaGetLastError());
     kmpp_scale_kernel<<<1, 1, 0, s>>>(w.maxbits, n, w.qexp);
     KM_CUDA(cudaGetLastError());
@@ -482,23 +501,45 @@ int run_kmpp(const float *X, int64_t n, int d, int k, uint32_t seed, float *C0, 
     for (int r = 1; r < k; ++r) {
         const int rc = r >= 2 ? r - 1 : -1;
         if (m.Xc) {
-            kmpp_round_kernel<256, true><<<(unsigned)ntiles, 256, 0, s>>>(X, n, d, C0, idx, w.mind, w.qexp,
-                                                                          w.tile_sum, w.done, m, rc, r, seed);
+            if constexpr (std::is_same<Src, DenseRows>::value)
+                kmpp_round_kernel<256, true><<<(unsigned)ntiles, 256, 0, s>>>(src, n, d, C0, idx, w.mind, w.qexp,
+                                                                              w.tile_sum, w.done, m, rc, r, seed);
         } else if (!prune || rc < 0) {
-            kmpp_round_kernel<1024, false><<<(unsigned)ntiles, 1024, 0, s>>>(X, n, d, C0, idx, w.mind, w.qexp,
+            kmpp_round_kernel<1024, false><<<(unsigned)ntiles, 1024, 0, s>>>(src, n, d, C0, idx, w.mind, w.qexp,
                                                                              w.tile_sum, w.done, m, rc, r, seed);
         } else {
             kmpp_cc_kernel<<<(unsigned)((rc + 7) / 8), 256, 0, s>>>(C0, d, rc, w.cc);
             KM_CUDA(cudaGetLastError());
             kmpp_prune_kernel<<<prune_grid, 256, 0, s>>>(n, w.mind, w.near, w.cc, pf, w.list, w.list_n);
             KM_CUDA(cudaGetLastError());
-            kmpp_eval_kernel<<<eval_grid, 256, 0, s>>>(X, n, d, C0, idx, w.mind, w.near, w.qexp, w.tile_sum, w.done,
+            kmpp_eval_kernel<<<eval_grid, 256, 0, s>>>(src, n, d, C0, idx, w.mind, w.near, w.qexp, w.tile_sum, w.done,
                                                        w.list, w.list_n, ntiles, rc, r, seed);
         }
         KM_CUDA(cudaGetLastError());
         if (cb) cb(cb_user);
     }
     return KM_OK;
+}
+
+}  // namespace
+
+int run_kmpp(const float *X, int64_t n, int d, int k, uint32_t seed, float *C0, int64_t *idx,
+             void (*cb)(void *), void *cb_user, void *ws, cudaStream_t s, const KmppMetric *metric,
+             const PairSrc *ps) {
+    const KmppMetric m = metric ? *metric : KmppMetric{nullptr, nullptr, nullptr};
+    if (n <= 0) {
+        set_error("kmeans++ needs at least one frame");
+        return KM_ERR_BAD_SHAPE;
+    }
+    if (ps) {
+        if (m.Xc) {
+            set_error("kmeans++ under the minRMSD metric takes dense frames");
+            return KM_ERR_UNSUPPORTED;
+        }
+        const PairRows pr{ps->xyz, reinterpret_cast<const int2 *>(ps->pairs), ps->n_atoms, d};
+        return run_kmpp_src(pr, n, d, k, seed, C0, idx, cb, cb_user, ws, s, m);
+    }
+    return run_kmpp_src(DenseRows{X, d}, n, d, k, seed, C0, idx, cb, cb_user, ws, s, m);
 }
 
 }  // namespace km

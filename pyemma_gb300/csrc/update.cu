@@ -130,9 +130,9 @@ __global__ void scatter_kernel(const int32_t *__restrict__ labels, int64_t n, in
 // launch per 1024-feature slice.  Indices and labels of the piece
 // sit in registers (8 per lane) and are broadcast by shuffles; label changes
 // are warp-uniform.
-template <int MW>
+template <int MW, class Src>
 __global__ void __launch_bounds__(256) seg_accumulate_wide_kernel(
-    const float *__restrict__ X, int d, int f_base, const int32_t *__restrict__ perm,
+    const Src src, int d, int f_base, const int32_t *__restrict__ perm,
     const int32_t *__restrict__ slab, int64_t n_max, const int32_t *__restrict__ n_sorted,
     const float *__restrict__ C_old, double *__restrict__ S, double *__restrict__ Q) {
     // Only the frames the scatter placed (valid labels) are in perm.
@@ -180,12 +180,11 @@ __global__ void __launch_bounds__(256) seg_accumulate_wide_kernel(
                         cold[m] = f < d ? __ldg(C_old + (int64_t)l * d + f) : 0.0f;
                     }
                 }
-                const float *x = X + i * d;
                 float xv[MW];
 #pragma unroll
                 for (int m = 0; m < MW; ++m) {
                     const int f = f_base + lane + 32 * m;
-                    xv[m] = f < d ? __ldg(x + f) : 0.0f;
+                    xv[m] = f < d ? src.get(i, f) : 0.0f;
                 }
 #pragma unroll
                 for (int m = 0; m < MW; ++m) {
@@ -377,9 +376,9 @@ __global__ void __launch_bounds__(kBulkWarps * 32, (MW > 17 ? 1 : 2)) seg_accumu
 
 // d < 32: the warp is split into 32/DP row slots of DP lanes (DP = next
 // power of two >= d); slot s walks positions p0+s, p0+s+R, ...
-template <int DP>
+template <int DP, class Src>
 __global__ void __launch_bounds__(256) seg_accumulate_narrow_kernel(
-    const float *__restrict__ X, int d, const int32_t *__restrict__ perm, const int32_t *__restrict__ slab,
+    const Src src, int d, const int32_t *__restrict__ perm, const int32_t *__restrict__ slab,
     int64_t n_max, const int32_t *__restrict__ n_sorted, const float *__restrict__ C_old, double *__restrict__ S,
     double *__restrict__ Q) {
     constexpr int R = 32 / DP;
@@ -411,7 +410,7 @@ __global__ void __launch_bounds__(256) seg_accumulate_narrow_kernel(
                 cold = fvalid ? __ldg(C_old + (int64_t)l * d + f) : 0.0f;
             }
             if (fvalid) {
-                const float t = __ldg(X + i * d + f) - cold;
+                const float t = src.get(i, f) - cold;
                 acc.add(t);
                 qacc.add(t * t);
             }
@@ -460,7 +459,8 @@ __global__ void finalize_kernel(const double *__restrict__ S, const double *__re
 // One warp per listed frame: its contribution (float32 deviations from the
 // previous centers, as the segment sums take them) leaves the cluster of its
 // first label and joins that of its exact label.
-__global__ void apply_flips_kernel(const float *__restrict__ X, int d, const float *__restrict__ C_old,
+template <class Src>
+__global__ void apply_flips_kernel(const Src src, int d, const float *__restrict__ C_old,
                                    const int32_t *__restrict__ flips, const int32_t *__restrict__ n_flips,
                                    int64_t max_flips, int32_t *__restrict__ labels, int32_t *__restrict__ counts,
                                    double *__restrict__ S, double *__restrict__ Q) {
@@ -472,13 +472,13 @@ __global__ void apply_flips_kernel(const float *__restrict__ X, int d, const flo
         const int64_t frame = flips[3 * w];
         const int from = flips[3 * w + 1];
         const int to = flips[3 * w + 2];
-        const float *x = X + frame * d;
         const float *cf = C_old + (int64_t)from * d;
         const float *ct = C_old + (int64_t)to * d;
         double qf = 0.0, qt = 0.0;
         for (int f = lane; f < d; f += 32) {
-            const float tf = __fsub_rn(x[f], cf[f]);
-            const float tt = __fsub_rn(x[f], ct[f]);
+            const float xf = src.get(frame, f);
+            const float tf = __fsub_rn(xf, cf[f]);
+            const float tt = __fsub_rn(xf, ct[f]);
             atomicAdd(&S[(int64_t)from * d + f], -(double)tf);
             atomicAdd(&S[(int64_t)to * d + f], (double)tt);
             qf += (double)__fmul_rn(tf, tf);
@@ -603,6 +603,10 @@ __global__ void __launch_bounds__(1024) reduce_cost_kernel(const double *__restr
     if (threadIdx.x == 0) *cost = part[0];
 }
 
+PairRows pair_rows_of(const PairSrc &ps, int d) {
+    return PairRows{ps.xyz, reinterpret_cast<const int2 *>(ps.pairs), ps.n_atoms, d};
+}
+
 unsigned grid_for(int64_t work, int threads, int per_sm) {
     int64_t g = (work + threads - 1) / threads;
     int64_t cap = (int64_t)num_sms() * per_sm;
@@ -610,22 +614,23 @@ unsigned grid_for(int64_t work, int threads, int per_sm) {
     return (unsigned)(g < 1 ? 1 : g);
 }
 
-template <int MW>
-void launch_wide(const float *X, int64_t n, int d, const UpdateWs &u, int k, const float *C_old, unsigned g,
+template <int MW, class Src>
+void launch_wide(const Src &X, int64_t n, int d, const UpdateWs &u, int k, const float *C_old, unsigned g,
                  cudaStream_t s) {
     for (int f_base = 0; f_base < d; f_base += 32 * MW)
-        seg_accumulate_wide_kernel<MW><<<g, 256, 0, s>>>(X, d, f_base, u.perm, u.slab, n, u.offsets + k, C_old,
-                                                         u.S, u.Q);
+        seg_accumulate_wide_kernel<MW, Src><<<g, 256, 0, s>>>(X, d, f_base, u.perm, u.slab, n, u.offsets + k,
+                                                              C_old, u.S, u.Q);
 }
 
-template <int DP>
-void launch_narrow(const float *X, int64_t n, int d, const UpdateWs &u, int k, const float *C_old, unsigned g,
+template <int DP, class Src>
+void launch_narrow(const Src &X, int64_t n, int d, const UpdateWs &u, int k, const float *C_old, unsigned g,
                    cudaStream_t s) {
-    seg_accumulate_narrow_kernel<DP><<<g, 256, 0, s>>>(X, d, u.perm, u.slab, n, u.offsets + k, C_old, u.S, u.Q);
+    seg_accumulate_narrow_kernel<DP, Src><<<g, 256, 0, s>>>(X, d, u.perm, u.slab, n, u.offsets + k, C_old, u.S,
+                                                            u.Q);
 }
 
-template <int MW>
-bool try_wide(int mw, const float *X, int64_t n, int d, const UpdateWs &u, int k, const float *C_old, unsigned g,
+template <int MW, class Src>
+bool try_wide(int mw, const Src &X, int64_t n, int d, const UpdateWs &u, int k, const float *C_old, unsigned g,
               cudaStream_t s) {
     if (mw > MW) return false;
     launch_wide<MW>(X, n, d, u, k, C_old, g, s);
@@ -686,7 +691,8 @@ bool bulk_ok(const float *X, int d) {
     return d >= 32 && d <= 1024 && (d % 4) == 0 && (reinterpret_cast<uintptr_t>(X) % 16) == 0;
 }
 
-int launch_segments(const float *X, int64_t n, int d, const UpdateWs &u, int k, const float *C_old, unsigned g,
+template <class Src>
+int launch_segments(const Src &X, int64_t n, int d, const UpdateWs &u, int k, const float *C_old, unsigned g,
                     cudaStream_t s) {
     if (d >= 32) {
         const int mw = (d + 31) / 32;
@@ -722,12 +728,12 @@ size_t update_ws_size(int64_t n, int d, int k) {
 }
 
 int launch_update_accumulate(const float *X, int64_t n, int d, const int32_t *labels, int k, const float *C_old,
-                             uint32_t *err, void *ws, cudaStream_t s, int seg_per_sm) {
+                             uint32_t *err, void *ws, cudaStream_t s, int seg_per_sm, const PairSrc *ps) {
     UpdateWs u = carve(ws, n, d, k, nullptr);
     KM_CUDA(cudaMemsetAsync(u.counts, 0, sizeof(int32_t) * k, s));
     KM_CUDA(cudaMemsetAsync(u.S, 0, sizeof(double) * (size_t)k * d, s));
     KM_CUDA(cudaMemsetAsync(u.Q, 0, sizeof(double) * k, s));
-    if (n > 0 && small_ok(d, k)) {
+    if (n > 0 && !ps && small_ok(d, k)) {
         const int dp = d <= 1 ? 1 : d <= 2 ? 2 : d <= 4 ? 4 : d <= 8 ? 8 : 16;
         // one frame per thread while the frames fill 8 CTAs of every SM, runs
         // of up to kSmallMaxRun frames beyond that
@@ -756,12 +762,17 @@ int launch_update_accumulate(const float *X, int64_t n, int d, const int32_t *la
     if (n > 0) {
         scatter_kernel<<<grid_for(n, 256, 8), 256, 0, s>>>(labels, n, k, u.cursor, u.perm, u.slab);
         KM_CUDA(cudaGetLastError());
-        if (bulk_ok(X, d)) {
+        if (ps) {
+            // pair features: computed where the segment sums read them
+            const int64_t npieces = (n + kPiece - 1) / kPiece;
+            const unsigned g = grid_for(npieces * 32, 256, 8);
+            KM_TRY(launch_segments(pair_rows_of(*ps, d), n, d, u, k, C_old, g, s));
+        } else if (bulk_ok(X, d)) {
             KM_TRY(launch_segments_bulk(X, n, d, u, k, C_old, err, s, seg_per_sm));
         } else {
             const int64_t npieces = (n + kPiece - 1) / kPiece;
             const unsigned g = grid_for(npieces * 32, 256, 8);
-            KM_TRY(launch_segments(X, n, d, u, k, C_old, g, s));
+            KM_TRY(launch_segments(DenseRows{X, d}, n, d, u, k, C_old, g, s));
         }
     }
     return KM_OK;
@@ -779,19 +790,24 @@ int launch_update_finish(int64_t n, int d, int k, const float *C_old, float *C_n
 }
 
 int launch_apply_flips(const float *X, int64_t n, int d, int k, const float *C_old, const FlipList &fl,
-                       int32_t *labels, void *ws, cudaStream_t s) {
+                       int32_t *labels, void *ws, cudaStream_t s, const PairSrc *ps) {
     if (fl.cap == 0) return KM_OK;
     UpdateWs u = carve(ws, n, d, k, nullptr);
-    apply_flips_kernel<<<grid_for(fl.cap * 32, 256, 4), 256, 0, s>>>(X, d, C_old, fl.rows, fl.count, fl.cap, labels,
-                                                                     u.counts, u.S, u.Q);
+    const unsigned g = grid_for(fl.cap * 32, 256, 4);
+    if (ps)
+        apply_flips_kernel<<<g, 256, 0, s>>>(pair_rows_of(*ps, d), d, C_old, fl.rows, fl.count, fl.cap, labels,
+                                              u.counts, u.S, u.Q);
+    else
+        apply_flips_kernel<<<g, 256, 0, s>>>(DenseRows{X, d}, d, C_old, fl.rows, fl.count, fl.cap, labels, u.counts,
+                                              u.S, u.Q);
     KM_CUDA(cudaGetLastError());
     return KM_OK;
 }
 
 int launch_update(const float *X, int64_t n, int d, const int32_t *labels, int k,
                   const float *C_old, float *C_new, int64_t *counts_out, double *cost,
-                  uint32_t *err, void *ws, cudaStream_t s) {
-    KM_TRY(launch_update_accumulate(X, n, d, labels, k, C_old, err, ws, s));
+                  uint32_t *err, void *ws, cudaStream_t s, const PairSrc *ps) {
+    KM_TRY(launch_update_accumulate(X, n, d, labels, k, C_old, err, ws, s, 0, ps));
     return launch_update_finish(n, d, k, C_old, C_new, counts_out, cost, ws, s);
 }
 
@@ -820,7 +836,7 @@ int launch_update_part(const float *X, int64_t n, int d, const int32_t *labels, 
         KM_TRY(launch_segments_bulk(X, rows, d, u, k, C_old, err, s, 0));
     } else {
         const int64_t npieces = (rows + kPiece - 1) / kPiece;
-        KM_TRY(launch_segments(X, rows, d, u, k, C_old, grid_for(npieces * 32, 256, 8), s));
+        KM_TRY(launch_segments(DenseRows{X, d}, rows, d, u, k, C_old, grid_for(npieces * 32, 256, 8), s));
     }
     add_counts_kernel<<<(unsigned)((k + 255) / 256), 256, 0, s>>>(u.counts, k, u.total);
     KM_CUDA(cudaGetLastError());
