@@ -142,21 +142,50 @@ float kmo_sqdist(const float *x, const float *c, int32_t d) {
     return acc;
 }
 
-#define KMO_CB 8
+/* Centers regrouped in blocks, feature-major inside a block, so that the
+ * compiler can evaluate a block's independent sequential sums at once: blocks
+ * of 32 centers first, then blocks of 8 for the remainder, then single
+ * centers.  Each sum keeps its own feature order, so every distance equals
+ * kmo_sqdist's, and the scan visits centers in index order (lowest index on
+ * ties). */
+#define KMO_CB_WIDE 32
+#define KMO_CB_NARROW 8
 
-/* Centers regrouped in blocks of KMO_CB, feature-major inside a block, so
- * that the compiler can evaluate KMO_CB independent sequential sums at once.
- * Each sum keeps its own feature order, so the result equals kmo_sqdist. */
 static float *transpose_center_blocks(const float *C, int32_t k, int32_t d) {
-    int32_t nb = k / KMO_CB;
-    if (nb == 0) return NULL;
-    float *ct = (float *)malloc((size_t)nb * KMO_CB * d * sizeof(float));
+    int32_t nw = k / KMO_CB_WIDE;
+    int32_t nn = (k - nw * KMO_CB_WIDE) / KMO_CB_NARROW;
+    int32_t kb = nw * KMO_CB_WIDE + nn * KMO_CB_NARROW;
+    if (kb == 0) return NULL;
+    float *ct = (float *)malloc((size_t)kb * d * sizeof(float));
     if (!ct) return NULL;
-    for (int32_t b = 0; b < nb; ++b)
+    for (int32_t j0 = 0; j0 < kb;) {
+        int32_t cb = j0 < nw * KMO_CB_WIDE ? KMO_CB_WIDE : KMO_CB_NARROW;
+        float *blk = ct + (size_t)j0 * d;
         for (int32_t f = 0; f < d; ++f)
-            for (int32_t u = 0; u < KMO_CB; ++u)
-                ct[((size_t)b * d + f) * KMO_CB + u] = C[(size_t)(b * KMO_CB + u) * d + f];
+            for (int32_t u = 0; u < cb; ++u) blk[(size_t)f * cb + u] = C[(size_t)(j0 + u) * d + f];
+        j0 += cb;
+    }
     return ct;
+}
+
+static inline __attribute__((always_inline)) void scan_block(const float *x, int32_t d, const float *blk,
+                                                             const int cb, int32_t j0, float *best,
+                                                             int32_t *bj) {
+    float acc[KMO_CB_WIDE];
+    for (int u = 0; u < cb; ++u) acc[u] = 0.0f;
+    for (int32_t f = 0; f < d; ++f) {
+        float xf = x[f];
+        for (int u = 0; u < cb; ++u) {
+            float t = xf - blk[(size_t)f * cb + u];
+            float s = t * t;
+            acc[u] = acc[u] + s;
+        }
+    }
+    for (int u = 0; u < cb; ++u)
+        if (acc[u] < *best) {
+            *best = acc[u];
+            *bj = j0 + u;
+        }
 }
 
 static void assign_one(const float *x, int32_t d, const float *C, const float *ct, int32_t k,
@@ -165,24 +194,10 @@ static void assign_one(const float *x, int32_t d, const float *C, const float *c
     int32_t bj = 0;
     int32_t j = 0;
     if (ct) {
-        for (; j + KMO_CB <= k; j += KMO_CB) {
-            const float *blk = ct + (size_t)(j / KMO_CB) * d * KMO_CB;
-            float acc[KMO_CB];
-            for (int u = 0; u < KMO_CB; ++u) acc[u] = 0.0f;
-            for (int32_t f = 0; f < d; ++f) {
-                float xf = x[f];
-                for (int u = 0; u < KMO_CB; ++u) {
-                    float t = xf - blk[f * KMO_CB + u];
-                    float s = t * t;
-                    acc[u] = acc[u] + s;
-                }
-            }
-            for (int u = 0; u < KMO_CB; ++u)
-                if (acc[u] < best) {
-                    best = acc[u];
-                    bj = j + u;
-                }
-        }
+        for (; j + KMO_CB_WIDE <= k; j += KMO_CB_WIDE)
+            scan_block(x, d, ct + (size_t)j * d, KMO_CB_WIDE, j, &best, &bj);
+        for (; j + KMO_CB_NARROW <= k; j += KMO_CB_NARROW)
+            scan_block(x, d, ct + (size_t)j * d, KMO_CB_NARROW, j, &best, &bj);
     }
     for (; j < k; ++j) {
         float dd = kmo_sqdist(x, C + (size_t)j * d, d);
