@@ -167,6 +167,9 @@ class KmeansClustering(AbstractClustering):
             indices = self._uniform_indices(np.array([total_length]), total_length)
             rows = np.array(sorted(indices.get(0, ())), dtype=np.int64)[:self.n_clusters]
             self.clustercenters = src.features(_device.torch_module().from_numpy(rows).to(src.xyz.device)).cpu().numpy()
+        # as for array input: the centers known before kmeans++ (none for a
+        # kmeans++ start)
+        self.initial_centers_ = self.clustercenters[:]
         if self._check_resume_iteration():
             if self.clustercenters.ndim != 2 or self.clustercenters.shape[1] != dim:
                 raise ValueError("initial centers have shape %s, data has dimension %d"
@@ -174,7 +177,6 @@ class KmeansClustering(AbstractClustering):
             C = _device.centers_to_device(self.clustercenters)
         else:
             C, _ = _lib.kmpp_pairs(src.xyz, src.pairs, int(self.n_clusters), self.fixed_seed)
-        self.initial_centers_ = C.cpu().numpy()
         res = _lib.lloyd_pairs(src.xyz, src.pairs, C, int(self.max_iter), float(self.tolerance),
                                precision=self.precision)
         self.clustercenters = C.cpu().numpy()

@@ -134,16 +134,18 @@ def test_estimators_on_pair_frames_equal_on_features():
     F = src.features()
     a = cluster_kmeans(src, k=50, max_iter=6, fixed_seed=4)
     b = cluster_kmeans(F, k=50, max_iter=6, fixed_seed=4)
-    np.testing.assert_array_equal(a.initial_centers_, b.initial_centers_)
+    # a kmeans++ start keeps no initial centers on either input
+    assert len(a.initial_centers_) == 0 and len(b.initial_centers_) == 0
     np.testing.assert_allclose(a.clustercenters, b.clustercenters, rtol=1e-5, atol=1e-5)
     assert a.n_iter == b.n_iter
     np.testing.assert_array_equal(a.dtrajs[0], assign_to_centers(F, centers=a.clustercenters)[0])
     np.testing.assert_array_equal(assign_to_centers(src, centers=a.clustercenters)[0],
                                   assign_to_centers(F, centers=a.clustercenters)[0])
     # stride and skip take the same frames as on the features
-    c = cluster_kmeans(src, k=20, max_iter=3, fixed_seed=5, stride=3, skip=11)
-    e = cluster_kmeans(F, k=20, max_iter=3, fixed_seed=5, stride=3, skip=11)
+    c = cluster_kmeans(src, k=20, max_iter=3, fixed_seed=5, stride=3, skip=11, init_strategy="uniform")
+    e = cluster_kmeans(F, k=20, max_iter=3, fixed_seed=5, stride=3, skip=11, init_strategy="uniform")
     np.testing.assert_array_equal(c.initial_centers_, e.initial_centers_)
+    assert c.initial_centers_.shape == (20, F.shape[1])
     np.testing.assert_allclose(c.clustercenters, e.clustercenters, rtol=1e-5, atol=1e-5)
 
 
