@@ -78,7 +78,8 @@ constexpr int kABytesPerChunk = kBM * kKC * 2;  // 16 KB
 enum ScalarSlot { kScale = 0, kInvScale2 = 1, kScaleMax = 2, kCmax = 3, kHcMax = 4, kNumScalars = 8 };
 
 struct TcParams {
-    int64_t n;
+    int64_t n;       // one past the last frame of this launch
+    int64_t frame0;  // its first frame (frames [frame0, n) of the operand rows)
     int k;
     int d;
     int kp;
@@ -446,12 +447,42 @@ struct Op16<__nv_bfloat16> {
 // ---------------------------------------------------------------------------
 // Prep kernels
 // ---------------------------------------------------------------------------
-__global__ void shift_mean_kernel(const float *__restrict__ C, int d, int k, float *__restrict__ shift) {
-    const int f = blockIdx.x * blockDim.x + threadIdx.x;
-    if (f >= d) return;
-    double s = 0.0;
-    for (int j = 0; j < k; ++j) s += (double)C[(int64_t)j * d + f];
-    shift[f] = (float)(s / k);
+// The mean of the centers per feature: a CTA per 32 features, lanes over
+// features (coalesced rows), its 32 warps over the centers with four
+// independent sums each (four loads in flight), the partial sums added in a
+// fixed order (the same shift for the same centers).  Any shift keeps the
+// labels exact: the bounds use the measured norms of the shifted, rounded
+// operands.
+constexpr int kShiftWarps = 32;
+__global__ void __launch_bounds__(kShiftWarps * 32) shift_mean_kernel(const float *__restrict__ C, int d, int k,
+                                                                      float *__restrict__ shift) {
+    __shared__ double part[kShiftWarps][32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int f = blockIdx.x * 32 + lane;
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+    if (f < d) {
+        const float *c = C + f;
+        int j = w;
+        for (; j + 3 * kShiftWarps < k; j += 4 * kShiftWarps) {
+            const float a0 = __ldg(c + (int64_t)j * d);
+            const float a1 = __ldg(c + (int64_t)(j + kShiftWarps) * d);
+            const float a2 = __ldg(c + (int64_t)(j + 2 * kShiftWarps) * d);
+            const float a3 = __ldg(c + (int64_t)(j + 3 * kShiftWarps) * d);
+            s0 += (double)a0;
+            s1 += (double)a1;
+            s2 += (double)a2;
+            s3 += (double)a3;
+        }
+        for (; j < k; j += kShiftWarps) s0 += (double)__ldg(c + (int64_t)j * d);
+    }
+    part[w][lane] = (s0 + s1) + (s2 + s3);
+    __syncthreads();
+    if (w == 0 && f < d) {
+        double t = 0.0;
+#pragma unroll 8
+        for (int q = 0; q < kShiftWarps; ++q) t += part[q][lane];
+        shift[f] = (float)(t / k);
+    }
 }
 
 // Warp sum of per-lane compensated sums (s + c) in float32 (double-float
@@ -967,7 +998,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
     // Frame units: 128 frames per CTA; a pair takes 256 consecutive frames,
     // its rank-r CTA the r-th half.
     const int64_t unit = PAIR ? 2 * kBM : kBM;
-    const int64_t n_units = (p.n + unit - 1) / unit;
+    const int64_t n_units = (p.n - p.frame0 + unit - 1) / unit;
     const int64_t unit0 = PAIR ? blockIdx.x / 2 : blockIdx.x;
     const int64_t unit_stride = PAIR ? gridDim.x / 2 : gridDim.x;
 
@@ -1021,7 +1052,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
         unsigned long long *pw_a = (p.wait_cycles && lane == 0) ? &w_a : nullptr;
         uint32_t s = 0, sph = 0;
         for (int64_t ft = unit0; ft < n_units && ok; ft += unit_stride, ++t_local) {
-            const int frame_row = (int)(ft * unit + rank * kBM);
+            const int frame_row = (int)(p.frame0 + ft * unit + rank * kBM);
             for (int ct = 0; ct < p.n_ctiles && ok; ++ct) {
                 for (int t = 0; t < p.nbst; ++t) {
                     if (!stream && ct == 0) {
@@ -1209,7 +1240,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
         const long long t_start = clock64();
         unsigned long long *pw_acc = (p.wait_cycles && warp == 2 && lane == 0) ? &w_acc : nullptr;
         for (int64_t ft = unit0; ft < n_units && ok; ft += unit_stride) {
-            const int64_t i = ft * unit + (int64_t)rank * kBM + row;
+            const int64_t i = p.frame0 + ft * unit + (int64_t)rank * kBM + row;
             const float4 xn = i < p.n ? p.xnorm[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
             // Worst-case bound terms over all centers: the acceptance window
             // and the overflow decision use them.
@@ -1741,6 +1772,13 @@ void tc_set_operand(TcBuffers &b, int d, int prec) {
 }
 
 namespace {
+// A deferred pass (tc_assign_deferred) runs in up to kMaxTcChunks launches
+// over consecutive frame ranges; chunk c's candidate lists start at the
+// chunk's first frame (an entry per frame at most), its counters at
+// kChunkCounters0 + 4 (c - 1) (chunk 0 uses counters[0..4)).
+constexpr int kMaxTcChunks = kTcMaxChunks;
+constexpr int kChunkCounters0 = 20;
+
 // One carving sequence for sizing (ws == nullptr) and for carving.
 size_t carve_assign(void *ws, int64_t n, TcBuffers &b) {
     Carver c(ws);
@@ -1755,8 +1793,9 @@ size_t carve_assign(void *ws, int64_t n, TcBuffers &b) {
     b.amb_mask = c.take<int32_t>(nn);
     b.full_frames = c.take<int32_t>(nn);
     b.full_keys = c.take<unsigned long long>(nn);
-    // [0] recheck entries, [1] full entries, [2] pairs, [3] entries left to the exact pass, [4..20) diagnostics
-    b.counters = c.take<int32_t>(20);
+    // [0] recheck entries, [1] full entries, [2] pairs, [3] entries left to the exact pass, [4..20) diagnostics,
+    // then the same four for chunks 1.. of a chunked pass
+    b.counters = c.take<int32_t>(kChunkCounters0 + 4 * (kMaxTcChunks - 1));
     b.flipped = c.take<unsigned long long>(1);
     b.err = c.take<uint32_t>(1);
     return c.bytes();
@@ -1777,7 +1816,7 @@ void tc_carve_assign(void *ws, int64_t n, int d, int k, TcBuffers &b) {
 }
 
 int tc_prepare_shift_from_centers(const float *C, int d, int k, TcBuffers &b, cudaStream_t s) {
-    shift_mean_kernel<<<(d + 127) / 128, 128, 0, s>>>(C, d, k, b.shift);
+    shift_mean_kernel<<<(d + 31) / 32, kShiftWarps * 32, 0, s>>>(C, d, k, b.shift);
     KM_CUDA(cudaGetLastError());
     KM_CUDA(cudaMemsetAsync(b.scal, 0, kNumScalars * sizeof(uint32_t), s));
     if (b.fp8) {
@@ -1875,9 +1914,70 @@ namespace {
 
 constexpr int kRecheckBesidePerSm = 4;
 
+// The launches of a pass over frames [0, n): one, or with a side stream and
+// n_fork > 1 fork events, consecutive ranges of at least 256k frames each
+// (KM_TC_CHUNKS sets the number, default 4), so that chunk c's re-check runs
+// beside the tensor-core launch of chunk c + 1.
+int tc_chunks_for(int64_t n, int n_fork) {
+    if (n_fork <= 1) return 1;
+    int want = 4;
+    if (const char *e = std::getenv("KM_TC_CHUNKS")) want = std::atoi(e);
+    want = std::max(1, std::min(want, std::min(n_fork, kMaxTcChunks)));
+    const int64_t by_size = n >> 18;
+    if (want > by_size) want = (int)std::max<int64_t>(1, by_size);
+    return want;
+}
+
+// First frame of chunk c (of n_chunks) over n frames: a multiple of `wave`
+// (the frames one launch's CTAs take in one round of units, a multiple of
+// 256) where a chunk holds at least one wave, so that every chunk but the
+// last ends without a partial round; else a multiple of 256.
+int64_t chunk_first(int64_t n, int n_chunks, int c, int64_t wave) {
+    if (c >= n_chunks) return n;
+    const int64_t step = n / n_chunks >= wave ? wave : 256;
+    return (n / n_chunks * c + step / 2) / step * step;
+}
+
+// Candidate lists and counters of chunk c, which starts at frame a.
+void chunk_lists(const TcBuffers &b, int64_t a, int c, TcBuffers &v) {
+    v = b;
+    if (c == 0) return;
+    v.rc_frames = b.rc_frames + a;
+    v.pair_center = b.pair_center + a * kL;
+    v.rc_keys = b.rc_keys + a;
+    v.rc_best = b.rc_best + a;
+    v.pair_lo = b.pair_lo + a * kL;
+    v.rc_pairs = b.rc_pairs + a;
+    v.amb_entries = b.amb_entries + a;
+    v.amb_mask = b.amb_mask + a;
+    v.full_frames = b.full_frames + a;
+    v.full_keys = b.full_keys + a;
+    v.counters = b.counters + kChunkCounters0 + 4 * (c - 1);
+}
+
+void set_lists(TcParams &p, const TcBuffers &v) {
+    p.rc_frames = v.rc_frames;
+    p.pair_center = v.pair_center;
+    p.rc_keys = v.rc_keys;
+    p.rc_best = v.rc_best;
+    p.rc_pairs = v.rc_pairs;
+    p.pair_lo = v.pair_lo;
+    p.full_frames = v.full_frames;
+    p.full_keys = v.full_keys;
+    p.counters = v.counters;
+}
+
+template <bool PAIR>
+cudaError_t launch_tc_variant(const cudaLaunchConfig_t &cfg, int list_len, bool fp8, const CUtensorMap &tmA,
+                              const CUtensorMap &tmB, const TcParams &p) {
+    if (fp8) return cudaLaunchKernelEx(&cfg, tc_assign_kernel<PAIR, 16, true>, tmA, tmB, p);
+    if (list_len == 8) return cudaLaunchKernelEx(&cfg, tc_assign_kernel<PAIR, 8, false>, tmA, tmB, p);
+    return cudaLaunchKernelEx(&cfg, tc_assign_kernel<PAIR, 16, false>, tmA, tmB, p);
+}
+
 int tc_assign_impl(const float *X, int64_t n, int d, const float *C, int k, int32_t *labels, TcBuffers &b,
                    cudaStream_t s, ProfEvents *prof, float *dump, unsigned long long *wait_cycles, cudaStream_t side,
-                   cudaEvent_t ev_fork, const FlipList *fl, const PairSrc *ps) {
+                   const cudaEvent_t *ev_fork, int n_fork, const FlipList *fl, const PairSrc *ps) {
     if (n == 0) return KM_OK;
     Plan pl;
     if (!make_plan(d, k, pl, b.fp8 != 0) || !device_is_sm10x()) {
@@ -1910,13 +2010,17 @@ int tc_assign_impl(const float *X, int64_t n, int d, const float *C, int k, int3
     KM_TRY(make_map(&tmA, b.xh, n, b.kp, kBM, b, CU_TENSOR_MAP_SWIZZLE_128B));
     KM_TRY(make_map(&tmB, b.ch, k_pad_of(k), b.kp, pl.pair ? pl.bn / 2 : pl.bn, b, CU_TENSOR_MAP_SWIZZLE_128B));
 
+    const int n_chunks = side ? tc_chunks_for(n, n_fork) : 1;
     KM_CUDA(cudaMemsetAsync(b.counters, 0, 4 * sizeof(int32_t), s));
+    if (n_chunks > 1)
+        KM_CUDA(cudaMemsetAsync(b.counters + kChunkCounters0, 0, 4 * (size_t)(n_chunks - 1) * sizeof(int32_t), s));
     KM_CUDA(cudaMemsetAsync(b.flipped, 0, sizeof(unsigned long long), s));
     if (!b.keep_err) KM_CUDA(cudaMemsetAsync(b.err, 0, sizeof(uint32_t), s));
 
     const double u = 5.9604644775390625e-08;  // 2^-24
     TcParams p;
     p.n = n;
+    p.frame0 = 0;
     p.k = k;
     p.d = d;
     p.kp = b.kp;
@@ -1955,94 +2059,133 @@ int tc_assign_impl(const float *X, int64_t n, int d, const float *C, int k, int3
     p.chn = b.chn;
     p.scal = b.scal;
     p.labels = labels;
-    p.rc_frames = b.rc_frames;
-    p.pair_center = b.pair_center;
-    p.rc_keys = b.rc_keys;
-    p.rc_best = b.rc_best;
-    p.rc_pairs = b.rc_pairs;
-    p.pair_lo = b.pair_lo;
-    p.full_frames = b.full_frames;
-    p.full_keys = b.full_keys;
-    p.counters = b.counters;
+    set_lists(p, b);
     p.err = b.err;
     p.dump = dump;
     p.wait_cycles = wait_cycles;
 
-    if (prof) prof->begin(kProfTc, s);
+    // The launches of a chunked pass run at the device's greatest priority:
+    // when a chunk ends, the next chunk's CTAs are placed before the CTAs of
+    // the re-check that waits for it.  The kernel walks its frame units in a
+    // fixed order per CTA, so one CTA placed late would delay its launch; the
+    // re-check beside it takes one CTA per SM, which fits next to a
+    // tensor-core CTA (no shared memory, few registers).
+    int prio = 0;
+    if (n_chunks > 1) {
+        int least = 0;
+        KM_CUDA(cudaDeviceGetStreamPriorityRange(&least, &prio));
+    }
+    // CTA pairs: as many clusters of two CTAs as fit at once (one CTA per
+    // SM), each walking 256-frame units.
+    int clusters_fit = 0;
     if (pl.pair) {
-        // Clusters of two CTAs, as many as fit at once (one CTA per SM),
-        // each walking 256-frame units.
-        cudaLaunchConfig_t cfg = {};
-        cudaLaunchAttribute attr[1];
-        attr[0].id = cudaLaunchAttributeClusterDimension;
-        attr[0].val.clusterDim.x = 2;
-        attr[0].val.clusterDim.y = 1;
-        attr[0].val.clusterDim.z = 1;
-        cfg.blockDim = dim3(kThreadsTC, 1, 1);
-        cfg.dynamicSmemBytes = (size_t)pl.smem;
-        cfg.stream = s;
-        cfg.attrs = attr;
-        cfg.numAttrs = 1;
         static std::mutex cl_mu;
         static std::map<std::pair<int, int>, int> cached_clusters;  // (smem, list length) -> clusters
-        int clusters_fit = 0;
-        {
-            std::lock_guard<std::mutex> lk(cl_mu);
-            auto it = cached_clusters.find(std::make_pair(pl.smem, pl.list_len));
-            if (it == cached_clusters.end()) {
-                cfg.gridDim = dim3((unsigned)(2 * (num_sms() / 2)), 1, 1);
-                int nc = 0;
-                KM_CUDA(cudaOccupancyMaxActiveClusters(&nc, kfn, &cfg));
-                it = cached_clusters.emplace(std::make_pair(pl.smem, pl.list_len), nc).first;
-            }
-            clusters_fit = it->second;
+        std::lock_guard<std::mutex> lk(cl_mu);
+        auto it = cached_clusters.find(std::make_pair(pl.smem, pl.list_len));
+        if (it == cached_clusters.end()) {
+            cudaLaunchConfig_t qc = {};
+            cudaLaunchAttribute qa[1];
+            qa[0].id = cudaLaunchAttributeClusterDimension;
+            qa[0].val.clusterDim.x = 2;
+            qa[0].val.clusterDim.y = 1;
+            qa[0].val.clusterDim.z = 1;
+            qc.blockDim = dim3(kThreadsTC, 1, 1);
+            qc.dynamicSmemBytes = (size_t)pl.smem;
+            qc.stream = s;
+            qc.attrs = qa;
+            qc.numAttrs = 1;
+            qc.gridDim = dim3((unsigned)(2 * (num_sms() / 2)), 1, 1);
+            int nc = 0;
+            KM_CUDA(cudaOccupancyMaxActiveClusters(&nc, kfn, &qc));
+            it = cached_clusters.emplace(std::make_pair(pl.smem, pl.list_len), nc).first;
         }
+        clusters_fit = it->second;
         if (clusters_fit < 1) {
             set_error("no CTA pair of the tensor-core kernel fits on this device");
             return KM_ERR_UNSUPPORTED;
         }
-        const int64_t n_units = (n + 2 * kBM - 1) / (2 * kBM);
-        int64_t clusters = clusters_fit;
-        if (clusters > n_units) clusters = n_units;
-        cfg.gridDim = dim3((unsigned)(2 * clusters), 1, 1);
-        if (b.fp8)
-            KM_CUDA(cudaLaunchKernelEx(&cfg, tc_assign_kernel<true, 16, true>, tmA, tmB, p));
-        else if (pl.list_len == 8)
-            KM_CUDA(cudaLaunchKernelEx(&cfg, tc_assign_kernel<true, 8, false>, tmA, tmB, p));
-        else
-            KM_CUDA(cudaLaunchKernelEx(&cfg, tc_assign_kernel<true, 16, false>, tmA, tmB, p));
-    } else {
-        const int64_t n_ftiles = (n + kBM - 1) / kBM;
-        int64_t grid = num_sms();
-        if (grid > n_ftiles) grid = n_ftiles;
-        if (b.fp8)
-            tc_assign_kernel<false, 16, true><<<(unsigned)grid, kThreadsTC, pl.smem, s>>>(tmA, tmB, p);
-        else if (pl.list_len == 8)
-            tc_assign_kernel<false, 8, false><<<(unsigned)grid, kThreadsTC, pl.smem, s>>>(tmA, tmB, p);
-        else
-            tc_assign_kernel<false, 16, false><<<(unsigned)grid, kThreadsTC, pl.smem, s>>>(tmA, tmB, p);
     }
-    KM_CUDA(cudaGetLastError());
-    if (prof) prof->end(kProfTc, s);
+    // Frames one launch takes in one round of units over all its CTAs.
+    const int64_t wave = pl.pair ? 2 * kBM * (int64_t)clusters_fit : kBM * (int64_t)num_sms();
+    auto launch_pass = [&](const TcParams &q) -> int {
+        const int64_t rows = q.n - q.frame0;
+        cudaLaunchConfig_t cfg = {};
+        cudaLaunchAttribute attr[2];
+        int na = 0;
+        cfg.blockDim = dim3(kThreadsTC, 1, 1);
+        cfg.dynamicSmemBytes = (size_t)pl.smem;
+        cfg.stream = s;
+        cfg.attrs = attr;
+        if (pl.pair) {
+            attr[na].id = cudaLaunchAttributeClusterDimension;
+            attr[na].val.clusterDim.x = 2;
+            attr[na].val.clusterDim.y = 1;
+            attr[na].val.clusterDim.z = 1;
+            ++na;
+            const int64_t n_units = (rows + 2 * kBM - 1) / (2 * kBM);
+            int64_t clusters = clusters_fit;
+            if (clusters > n_units) clusters = n_units;
+            cfg.gridDim = dim3((unsigned)(2 * clusters), 1, 1);
+        } else {
+            const int64_t n_ftiles = (rows + kBM - 1) / kBM;
+            int64_t grid = num_sms();
+            if (grid > n_ftiles) grid = n_ftiles;
+            cfg.gridDim = dim3((unsigned)grid, 1, 1);
+        }
+        if (n_chunks > 1) {
+            attr[na].id = cudaLaunchAttributePriority;
+            attr[na].val.priority = prio;
+            ++na;
+        }
+        cfg.numAttrs = na;
+        KM_CUDA(pl.pair ? launch_tc_variant<true>(cfg, pl.list_len, b.fp8 != 0, tmA, tmB, q)
+                        : launch_tc_variant<false>(cfg, pl.list_len, b.fp8 != 0, tmA, tmB, q));
+        KM_CUDA(cudaGetLastError());
+        return KM_OK;
+    };
 
-    // The exact re-checks: on s, or on `side` beside the caller's next work.
-    cudaStream_t r = s;
-    if (side) {
-        KM_CUDA(cudaEventRecord(ev_fork, s));
-        KM_CUDA(cudaStreamWaitEvent(side, ev_fork, 0));
-        r = side;
+    // Each chunk: the tensor-core launch on s, then its exact re-checks on s,
+    // or on `side` beside the next chunk (and, after the last chunk, beside
+    // the caller's next work).  Beside the centroid update the re-check keeps
+    // to half of each SM's threads, beside a tensor-core launch to one CTA
+    // per SM, so that both stay resident.
+    cudaStream_t r = side ? side : s;
+    if (prof) prof->begin(kProfTc, s);
+    int64_t f_next = 0;
+    for (int c = 0; c < n_chunks; ++c) {
+        const int64_t f0 = f_next;
+        TcBuffers v;
+        chunk_lists(b, f0, c, v);
+        TcParams q = p;
+        q.frame0 = f0;
+        q.n = n;
+        if (c + 1 < n_chunks) q.n = std::min(n, std::max(f0 + 256, chunk_first(n, n_chunks, c + 1, wave)));
+        const int64_t f1 = q.n;
+        f_next = f1;
+        set_lists(q, v);
+        KM_TRY(launch_pass(q));
+        if (prof && c + 1 == n_chunks) prof->end(kProfTc, s);
+        if (side) {
+            KM_CUDA(cudaEventRecord(ev_fork[c], s));
+            KM_CUDA(cudaStreamWaitEvent(side, ev_fork[c], 0));
+        }
+        if (prof && c == 0) prof->begin(kProfRecheck, r);
+        const int per_sm = !side ? 8 : c + 1 < n_chunks ? 1 : kRecheckBesidePerSm;
+        KM_TRY(launch_recheck_pairs(X, d, C, v.rc_frames, v.rc_best, v.rc_pairs, v.pair_center, v.pair_lo,
+                                    v.rc_keys, v.amb_entries, v.amb_mask, v.counters, f1 - f0, labels, b.flipped, r,
+                                    fl, per_sm, ps));
+        if (n_chunks > 1)
+            KM_TRY(launch_full_recheck(X, v.full_frames, v.counters + 1, f1 - f0, d, C, k, v.full_keys, labels,
+                                       b.flipped, r, fl, ps));
     }
-    if (prof) prof->begin(kProfRecheck, r);
-    // Beside the centroid update the re-check keeps to half of each SM's
-    // threads, so that both stay resident.
-    KM_TRY(launch_recheck_pairs(X, d, C, b.rc_frames, b.rc_best, b.rc_pairs, b.pair_center, b.pair_lo, b.rc_keys,
-                                b.amb_entries, b.amb_mask, b.counters, n, labels, b.flipped, r, fl,
-                                side ? kRecheckBesidePerSm : 8, ps));
     if (prof) prof->end(kProfRecheck, r);
-    if (prof) prof->begin(kProfFull, r);
-    KM_TRY(launch_full_recheck(X, b.full_frames, b.counters + 1, n, d, C, k, b.full_keys, labels, b.flipped, r, fl,
-                               ps));
-    if (prof) prof->end(kProfFull, r);
+    if (n_chunks == 1) {
+        if (prof) prof->begin(kProfFull, r);
+        KM_TRY(launch_full_recheck(X, b.full_frames, b.counters + 1, n, d, C, k, b.full_keys, labels, b.flipped, r,
+                                   fl, ps));
+        if (prof) prof->end(kProfFull, r);
+    }
     return KM_OK;
 }
 
@@ -2050,13 +2193,13 @@ int tc_assign_impl(const float *X, int64_t n, int d, const float *C, int k, int3
 
 int tc_assign(const float *X, int64_t n, int d, const float *C, int k, int32_t *labels, TcBuffers &b,
               cudaStream_t s, ProfEvents *prof, float *dump, unsigned long long *wait_cycles, const PairSrc *ps) {
-    return tc_assign_impl(X, n, d, C, k, labels, b, s, prof, dump, wait_cycles, nullptr, nullptr, nullptr, ps);
+    return tc_assign_impl(X, n, d, C, k, labels, b, s, prof, dump, wait_cycles, nullptr, nullptr, 0, nullptr, ps);
 }
 
 int tc_assign_deferred(const float *X, int64_t n, int d, const float *C, int k, int32_t *labels, TcBuffers &b,
-                       cudaStream_t s, cudaStream_t side, cudaEvent_t ev_fork, const FlipList &fl,
+                       cudaStream_t s, cudaStream_t side, const cudaEvent_t *ev_fork, int n_fork, const FlipList &fl,
                        ProfEvents *prof, const PairSrc *ps) {
-    return tc_assign_impl(X, n, d, C, k, labels, b, s, prof, nullptr, nullptr, side, ev_fork, &fl, ps);
+    return tc_assign_impl(X, n, d, C, k, labels, b, s, prof, nullptr, nullptr, side, ev_fork, n_fork, &fl, ps);
 }
 
 }  // namespace km

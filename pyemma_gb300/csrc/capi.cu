@@ -268,6 +268,18 @@ __global__ void __launch_bounds__(256) host_copy_kernel(const float *__restrict_
     }
 }
 
+// Graphs keep the launch priority of their kernel nodes (the chunked
+// tensor-core pass runs at the greatest priority); without that flag a graph
+// runs every node at its stream's priority.
+cudaError_t instantiate_with_priorities(cudaGraphExec_t *gx, cudaGraph_t g) {
+    cudaError_t e = cudaGraphInstantiate(gx, g, cudaGraphInstantiateFlagUseNodePriority);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        e = cudaGraphInstantiate(gx, g, 0);
+    }
+    return e;
+}
+
 struct LoopState {
     double prev;
     double tol;
@@ -890,9 +902,10 @@ int lloyd_run(const float *X_in, const HostFrames *hf, int64_t n, int32_t d, int
     FlipList fl;
     struct Side {
         cudaStream_t st = nullptr;
-        cudaEvent_t fork = nullptr, join = nullptr;
+        cudaEvent_t fork[kTcMaxChunks] = {}, join = nullptr;
         ~Side() {
-            if (fork) cudaEventDestroy(fork);
+            for (cudaEvent_t e : fork)
+                if (e) cudaEventDestroy(e);
             if (join) cudaEventDestroy(join);
             if (st) cudaStreamDestroy(st);
         }
@@ -902,7 +915,7 @@ int lloyd_run(const float *X_in, const HostFrames *hf, int64_t n, int32_t d, int
         fl.count = cv.take<int32_t>(1);
         fl.cap = n;
         KM_CUDA(cudaStreamCreateWithFlags(&side.st, cudaStreamNonBlocking));
-        KM_CUDA(cudaEventCreateWithFlags(&side.fork, cudaEventDisableTiming));
+        for (cudaEvent_t &e : side.fork) KM_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
         KM_CUDA(cudaEventCreateWithFlags(&side.join, cudaEventDisableTiming));
     }
 
@@ -939,7 +952,7 @@ int lloyd_run(const float *X_in, const HostFrames *hf, int64_t n, int32_t d, int
         if (is_tc(prec)) {
             KM_TRY(tc_prepare_centers(C, d, k, b, st));
             KM_CUDA(cudaMemsetAsync(fl.count, 0, sizeof(int32_t), st));
-            KM_TRY(tc_assign_deferred(X, n, d, C, k, labels, b, st, side.st, side.fork, fl, &prof, ps));
+            KM_TRY(tc_assign_deferred(X, n, d, C, k, labels, b, st, side.st, side.fork, kTcMaxChunks, fl, &prof, ps));
             prof.begin(kProfUpdate, st);
             // one segment-sum CTA per SM: room for the re-check beside it
             KM_TRY(launch_update_accumulate(X, n, d, labels, k, C, err, ws_update, st, 1, ps));
@@ -1027,7 +1040,7 @@ int lloyd_run(const float *X_in, const HostFrames *hf, int64_t n, int32_t d, int
                 ok = st == KM_OK && e2 == cudaSuccess;
             }
         }
-        if (ok) ok = cudaGraphInstantiate(&gx, g, 0) == cudaSuccess;
+        if (ok) ok = instantiate_with_priorities(&gx, g) == cudaSuccess;
         if (!ok) {
             cudaGetLastError();  // not fatal: the host loop takes over
             cleanup();
@@ -1089,7 +1102,7 @@ int lloyd_run(const float *X_in, const HostFrames *hf, int64_t n, int32_t d, int
                     cudaError_t e2 = cudaStreamEndCapture(cs, &graph);
                     if (status == KM_OK && e2 != cudaSuccess) status = cuda_fail(e2, "cudaStreamEndCapture");
                     if (status == KM_OK) {
-                        e2 = cudaGraphInstantiate(&exec, graph, 0);
+                        e2 = instantiate_with_priorities(&exec, graph);
                         if (e2 != cudaSuccess) status = cuda_fail(e2, "cudaGraphInstantiate");
                     }
                     if (graph) cudaGraphDestroy(graph);

@@ -34,11 +34,7 @@ __global__ void __launch_bounds__(256) pair_distances_kernel(const float *__rest
         const int2 ij = __ldg(pairs + p);
         const float *a = xyz + (t * n_atoms + ij.x) * 3;
         const float *b = xyz + (t * n_atoms + ij.y) * 3;
-        const float dx = __fsub_rn(__ldg(b), __ldg(a));
-        const float dy = __fsub_rn(__ldg(b + 1), __ldg(a + 1));
-        const float dz = __fsub_rn(__ldg(b + 2), __ldg(a + 2));
-        const float r2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
-        out[q] = __fsqrt_rn(r2);
+        out[q] = pair_feature(__ldg(a), __ldg(a + 1), __ldg(a + 2), __ldg(b), __ldg(b + 1), __ldg(b + 2));
     }
 }
 

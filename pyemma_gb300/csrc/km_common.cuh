@@ -185,6 +185,16 @@ struct DenseRows {
     __device__ __forceinline__ float get(int64_t i, int f) const { return __ldg(X + i * d + f); }
 };
 
+// The distance of atoms a and b: one rounding per operation, in the order
+// sqrt((dx^2 + dy^2) + dz^2) with d = b - a.  Every kernel that computes a
+// pair feature goes through this function.
+__device__ __forceinline__ float pair_feature(float ax, float ay, float az, float bx, float by, float bz) {
+    const float dx = __fsub_rn(bx, ax);
+    const float dy = __fsub_rn(by, ay);
+    const float dz = __fsub_rn(bz, az);
+    return __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)));
+}
+
 struct PairRows {
     const float *xyz;   // (n, n_atoms, 3) frame-major
     const int2 *pairs;  // d atom pairs
@@ -194,10 +204,7 @@ struct PairRows {
         const int2 p = __ldg(pairs + f);
         const float *a = xyz + (i * n_atoms + p.x) * 3;
         const float *b = xyz + (i * n_atoms + p.y) * 3;
-        const float dx = __fsub_rn(__ldg(b), __ldg(a));
-        const float dy = __fsub_rn(__ldg(b + 1), __ldg(a + 1));
-        const float dz = __fsub_rn(__ldg(b + 2), __ldg(a + 2));
-        return __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)));
+        return pair_feature(__ldg(a), __ldg(a + 1), __ldg(a + 2), __ldg(b), __ldg(b + 1), __ldg(b + 2));
     }
 };
 

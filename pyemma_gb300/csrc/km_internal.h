@@ -216,13 +216,17 @@ int tc_prepare_centers(const float *C, int d, int k, TcBuffers &b, cudaStream_t 
 int tc_assign(const float *X, int64_t n, int d, const float *C, int k, int32_t *labels,
               TcBuffers &b, cudaStream_t s, ProfEvents *prof = nullptr, float *dump = nullptr,
               unsigned long long *wait_cycles = nullptr, const PairSrc *ps = nullptr);
-// The tensor-core pass on s, then the exact re-checks on `side` (after
-// ev_fork, recorded on s) with their changed labels in fl (whose count must
-// be zero when the re-checks start).  labels holds the tensor-core labels;
-// the caller joins `side` back into s before it applies fl.
+// The tensor-core pass on s, then the exact re-checks on `side` with their
+// changed labels in fl (whose count must be zero when the re-checks start).
+// With n_fork > 1 events the pass runs in up to min(n_fork, kTcMaxChunks)
+// launches over consecutive frame ranges, each chunk's re-check on `side`
+// (after ev_fork[c], recorded on s) beside the next chunk's launch.  labels
+// holds the tensor-core labels; the caller joins `side` back into s before
+// it applies fl.
+constexpr int kTcMaxChunks = 8;
 int tc_assign_deferred(const float *X, int64_t n, int d, const float *C, int k, int32_t *labels, TcBuffers &b,
-                       cudaStream_t s, cudaStream_t side, cudaEvent_t ev_fork, const FlipList &fl,
-                       ProfEvents *prof = nullptr, const PairSrc *ps = nullptr);
+                       cudaStream_t s, cudaStream_t side, const cudaEvent_t *ev_fork, int n_fork,
+                       const FlipList &fl, ProfEvents *prof = nullptr, const PairSrc *ps = nullptr);
 
 // Resident center sets (capi.cu), used by the serving loop (serve.cu).
 int assign_centers_enqueue(const float *X, int64_t n, const km_centers *h, int32_t *labels, void *ws,

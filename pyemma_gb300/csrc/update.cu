@@ -20,6 +20,7 @@
 //   inertia_j = Q_j - 2 delta_j . S_j + n_j ||delta_j||^2
 // which is sum_i ||x_i - mu_j||^2 without the cancellation of raw moments.
 #include <algorithm>
+#include <map>
 #include <mutex>
 
 #include "km_common.cuh"
@@ -376,6 +377,145 @@ __global__ void __launch_bounds__(kBulkWarps * 32, (MW > 17 ? 1 : 2)) seg_accumu
 
 // d < 32: the warp is split into 32/DP row slots of DP lanes (DP = next
 // power of two >= d); slot s walks positions p0+s, p0+s+R, ...
+// ---------------------------------------------------------------------------
+// Segment sums of coordinate frames (pair features).  The walk of
+// seg_accumulate_wide_kernel, with the coordinates of each sorted frame
+// staged in a ring of kPairSlots per-warp shared-memory slots by 4-byte
+// cp.async copies, kPairSlots - 1 frames ahead (a frame's 12 n_atoms bytes
+// are not a 16-byte multiple, so no bulk copy), and each lane's atom pairs
+// held in registers as offsets into a slot (two 16-bit halves).  The
+// features are those of PairRows (pair_feature).
+// ---------------------------------------------------------------------------
+constexpr int kPairSlots = 4;
+constexpr int kPairMaxAtoms = 128;  // slots of up to 384 floats: 48 KB per CTA at most
+
+__device__ __forceinline__ void cp_async4(float *dst, const float *src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(sh_addr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+int pair_slot_floats(int n_atoms) { return (3 * n_atoms + 3) & ~3; }
+size_t pair_seg_smem(int n_atoms) { return (size_t)8 * kPairSlots * pair_slot_floats(n_atoms) * sizeof(float); }
+
+template <int MW>
+__global__ void __launch_bounds__(256) seg_accumulate_pairs_kernel(
+    const PairRows src, int d, int f_base, const int32_t *__restrict__ perm, const int32_t *__restrict__ slab,
+    int64_t n_max, const int32_t *__restrict__ n_sorted, const float *__restrict__ C_old, double *__restrict__ S,
+    double *__restrict__ Q) {
+    extern __shared__ float pair_ring[];
+    const int64_t n = min(n_max, (int64_t)*n_sorted);
+    const int lane = threadIdx.x & 31;
+    const int row_floats = 3 * src.n_atoms;
+    const int slot = (row_floats + 3) & ~3;
+    float *ring = pair_ring + (threadIdx.x >> 5) * kPairSlots * slot;
+    const int64_t gwarp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int64_t npieces = (n + kPiece - 1) / kPiece;
+    uint32_t ofs[MW];  // 3 a | 3 b << 16 of the lane's pair m
+#pragma unroll
+    for (int m = 0; m < MW; ++m) {
+        const int f = f_base + lane + 32 * m;
+        ofs[m] = 0u;
+        if (f < d) {
+            const int2 pr = __ldg(src.pairs + f);
+            ofs[m] = (uint32_t)(3 * pr.x) | ((uint32_t)(3 * pr.y) << 16);
+        }
+    }
+    auto fetch = [&](int64_t i, int q) {
+        const float *g = src.xyz + i * row_floats;
+        float *dst = ring + q * slot;
+        for (int t = lane; t < row_floats; t += 32) cp_async4(dst + t, g + t);
+    };
+    for (int64_t piece = gwarp; piece < npieces; piece += nwarps) {
+        const int64_t p0 = piece * kPiece;
+        int my_i[kGroups], my_l[kGroups];
+#pragma unroll
+        for (int g = 0; g < kGroups; ++g) {
+            const int64_t p = p0 + 32 * g + lane;
+            my_i[g] = p < n ? perm[p] : 0;
+            my_l[g] = p < n ? slab[p] : -1;
+        }
+        // the first kPairSlots - 1 frames of the piece (the valid positions
+        // are a prefix of it), a copy group each
+#pragma unroll
+        for (int t = 0; t < kPairSlots - 1; ++t) {
+            if (__shfl_sync(0xffffffffu, my_l[0], t) >= 0) fetch(__shfl_sync(0xffffffffu, my_i[0], t), t);
+            cp_async_commit();
+        }
+        CSum acc[MW], qacc;
+        float cold[MW];
+        int cur = -1;
+        auto flush = [&]() {
+#pragma unroll
+            for (int m = 0; m < MW; ++m) {
+                const int f = f_base + lane + 32 * m;
+                if (f < d) atomicAdd(&S[(int64_t)cur * d + f], acc[m].value());
+            }
+            double q = qacc.value();
+            for (int off = 16; off > 0; off >>= 1) q += __shfl_xor_sync(0xffffffffu, q, off);
+            if (lane == 0) atomicAdd(&Q[cur], q);
+        };
+#pragma unroll
+        for (int g = 0; g < kGroups; ++g) {
+            for (int r = 0; r < 32; ++r) {
+                const int l = __shfl_sync(0xffffffffu, my_l[g], r);
+                if (l < 0) break;
+                // Position t + kPairSlots - 1 into the slot that frame t - 1
+                // used (read by every lane before the last __syncwarp).
+                const int t = 32 * g + r;
+                {
+                    const int tn = r + kPairSlots - 1;
+                    const int gn = g + 1 < kGroups ? g + 1 : g;  // a constant once unrolled
+                    int ln = -1, in = 0;
+                    if (tn < 32) {
+                        ln = __shfl_sync(0xffffffffu, my_l[g], tn);
+                        in = __shfl_sync(0xffffffffu, my_i[g], tn);
+                    } else if (g + 1 < kGroups) {
+                        ln = __shfl_sync(0xffffffffu, my_l[gn], tn - 32);
+                        in = __shfl_sync(0xffffffffu, my_i[gn], tn - 32);
+                    }
+                    if (ln >= 0) fetch(in, (t + kPairSlots - 1) % kPairSlots);
+                    cp_async_commit();
+                }
+                cp_async_wait<kPairSlots - 1>();  // frame t's group has landed (this lane's part)
+                __syncwarp();                     // ... and every lane's
+                const float *xr = ring + (t % kPairSlots) * slot;
+                if (l != cur) {
+                    if (cur >= 0) flush();
+                    cur = l;
+                    qacc.reset();
+#pragma unroll
+                    for (int m = 0; m < MW; ++m) {
+                        const int f = f_base + lane + 32 * m;
+                        acc[m].reset();
+                        cold[m] = f < d ? __ldg(C_old + (int64_t)l * d + f) : 0.0f;
+                    }
+                }
+#pragma unroll
+                for (int m = 0; m < MW; ++m) {
+                    const int f = f_base + lane + 32 * m;
+                    if (f < d) {
+                        const float *a = xr + (ofs[m] & 0xFFFFu);
+                        const float *b = xr + (ofs[m] >> 16);
+                        const float x = pair_feature(a[0], a[1], a[2], b[0], b[1], b[2]);
+                        const float t2 = x - cold[m];
+                        acc[m].add(t2);
+                        qacc.add(t2 * t2);
+                    }
+                }
+                __syncwarp();
+            }
+        }
+        if (cur >= 0) flush();
+        cp_async_wait<0>();  // no copy into the ring outlives the piece
+        __syncwarp();
+    }
+}
+
 template <int DP, class Src>
 __global__ void __launch_bounds__(256) seg_accumulate_narrow_kernel(
     const Src src, int d, const int32_t *__restrict__ perm, const int32_t *__restrict__ slab,
@@ -719,6 +859,47 @@ int launch_segments(const Src &X, int64_t n, int d, const UpdateWs &u, int k, co
     return KM_OK;
 }
 
+template <int MW>
+int launch_pairs_mw(const PairRows &src, int64_t n, int d, const UpdateWs &u, int k, const float *C_old,
+                    cudaStream_t s) {
+    const size_t smem = pair_seg_smem(src.n_atoms);
+    // resident CTAs per SM for this slot size (the grid walks its pieces in
+    // a fixed order per warp, so it is sized to what is resident at once)
+    static std::mutex mu;
+    static std::map<size_t, int> per_sm_of;
+    int per_sm = 0;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        auto it = per_sm_of.find(smem);
+        if (it == per_sm_of.end()) {
+            int v = 0;
+            KM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, seg_accumulate_pairs_kernel<MW>, 256, smem));
+            it = per_sm_of.emplace(smem, v > 0 ? v : 1).first;
+        }
+        per_sm = it->second;
+    }
+    const int64_t npieces = (n + kPiece - 1) / kPiece;
+    const unsigned g = grid_for(npieces * 32, 256, per_sm);
+    for (int f_base = 0; f_base < d; f_base += 32 * MW)
+        seg_accumulate_pairs_kernel<MW><<<g, 256, smem, s>>>(src, d, f_base, u.perm, u.slab, n, u.offsets + k,
+                                                              C_old, u.S, u.Q);
+    KM_CUDA(cudaGetLastError());
+    return KM_OK;
+}
+
+int launch_segments_pairs(const PairRows &src, int64_t n, int d, const UpdateWs &u, int k, const float *C_old,
+                          cudaStream_t s) {
+    const int mw = (d + 31) / 32;
+    if (mw <= 1) return launch_pairs_mw<1>(src, n, d, u, k, C_old, s);
+    if (mw <= 2) return launch_pairs_mw<2>(src, n, d, u, k, C_old, s);
+    if (mw <= 4) return launch_pairs_mw<4>(src, n, d, u, k, C_old, s);
+    if (mw <= 8) return launch_pairs_mw<8>(src, n, d, u, k, C_old, s);
+    if (mw <= 12) return launch_pairs_mw<12>(src, n, d, u, k, C_old, s);
+    if (mw <= 17) return launch_pairs_mw<17>(src, n, d, u, k, C_old, s);
+    if (mw <= 24) return launch_pairs_mw<24>(src, n, d, u, k, C_old, s);
+    return launch_pairs_mw<32>(src, n, d, u, k, C_old, s);  // d > 1024: slices of 1024 features
+}
+
 }  // namespace
 
 size_t update_ws_size(int64_t n, int d, int k) {
@@ -764,9 +945,13 @@ int launch_update_accumulate(const float *X, int64_t n, int d, const int32_t *la
         KM_CUDA(cudaGetLastError());
         if (ps) {
             // pair features: computed where the segment sums read them
-            const int64_t npieces = (n + kPiece - 1) / kPiece;
-            const unsigned g = grid_for(npieces * 32, 256, 8);
-            KM_TRY(launch_segments(pair_rows_of(*ps, d), n, d, u, k, C_old, g, s));
+            if (ps->n_atoms <= kPairMaxAtoms) {
+                KM_TRY(launch_segments_pairs(pair_rows_of(*ps, d), n, d, u, k, C_old, s));
+            } else {
+                const int64_t npieces = (n + kPiece - 1) / kPiece;
+                const unsigned g = grid_for(npieces * 32, 256, 8);
+                KM_TRY(launch_segments(pair_rows_of(*ps, d), n, d, u, k, C_old, g, s));
+            }
         } else if (bulk_ok(X, d)) {
             KM_TRY(launch_segments_bulk(X, n, d, u, k, C_old, err, s, seg_per_sm));
         } else {

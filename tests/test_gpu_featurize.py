@@ -106,6 +106,29 @@ def test_lloyd_pairs_equals_lloyd_on_features(prec):
     assert torch.equal(ra["labels"], rb["labels"])
 
 
+@pytest.mark.parametrize("n_atoms,excl", [(50, 0), (130, 120), (12, 0)])
+def test_lloyd_pairs_other_shapes_equal_lloyd_on_features(n_atoms, excl):
+    # 50 atoms: 1,225 features, two 1024-feature slices of the segment sums;
+    # 130 atoms: beyond the ring-staged kernel's atom limit (the per-feature
+    # gather kernel); 12 atoms: 66 features
+    import torch
+    from pyemma_gb300 import _lib as L
+    from pyemma_gb300.featurize import pair_distance_frames
+    rng = np.random.default_rng(60 + n_atoms)
+    T = 12000
+    xyz = np.concatenate([_chain(rng, T // 4 + 1, n_atoms) for _ in range(4)])[:T]
+    src = pair_distance_frames(xyz[rng.permutation(T)], excluded_neighbors=excl)
+    F = src.features()
+    C0 = F[torch.from_numpy(rng.choice(T, 64, replace=False)).cuda()].contiguous()
+    for prec in ("fp32", "fp16"):
+        Ca, Cb = C0.clone(), C0.clone()
+        ra = L.lloyd_pairs(src.xyz, src.pairs, Ca, 1, -1.0, precision=prec)
+        rb = L.lloyd(F, Cb, 1, -1.0, precision=prec)
+        assert torch.equal(ra["labels"], rb["labels"]), prec
+        torch.testing.assert_close(Ca, Cb, rtol=1e-5, atol=1e-5)
+        np.testing.assert_allclose(ra["inertias"], rb["inertias"], rtol=1e-6)
+
+
 def test_kmpp_pairs_draws_equal_kmpp_on_features(oracle):
     import torch
     from pyemma_gb300 import _lib as L
