@@ -191,6 +191,14 @@ def padded_mma_flops(n, k, d):
     return 2.0 * n_pad * k_pad * k_steps
 
 
+def tc_chunks(n):
+    """Launches of one iteration's tensor-core pass: the library splits a
+    Lloyd pass into KM_TC_CHUNKS (default 4) launches of at least 2^18
+    frames each, so that each chunk's exact re-check runs beside the next."""
+    want = max(1, min(int(os.environ.get("KM_TC_CHUNKS", "4")), 8))
+    return max(1, min(want, n >> 18))
+
+
 def tc_roofline(n, tc_ms, tc_n, timed_ms, k=K, d=D):
     """Roofline record of the tensor-core distance kernel: 2 n k d flops per
     launch over its mean CUDA-event launch time, against the measured bf16
@@ -375,9 +383,46 @@ def run_ours(args):
         sampler = None
 
     # ---- roofline of the tensor-core distance kernel ----
+    # In the step, one iteration's pass is tc_chunks(n) launches with the
+    # exact re-check of each chunk beside the next: ms_per_launch is the span
+    # from the first launch's start to the last one's end.  The same kernel
+    # alone (one launch over all frames, the re-check after it) is timed
+    # below as "isolated".
     tc_ms, tc_n = prof["tc"]
     roofline = tc_roofline(n, tc_ms, tc_n, ms)
     roofline["step_breakdown_ms"] = {k: (v[0] / v[1] if v[1] else None) for k, v in prof.items()}
+    roofline["chunks_per_iteration"] = tc_chunks(n)
+    roofline["span"] = ("ms_per_launch: one iteration's tensor-core pass, %d launches over consecutive frame "
+                        "ranges, from the first start to the last end, each chunk's exact re-check running "
+                        "beside the next launch" % tc_chunks(n))
+    if rank == 0:
+        old = os.environ.get("KM_TC_CHUNKS")
+        os.environ["KM_TC_CHUNKS"] = "1"
+        try:
+            Ci = C0.clone()
+            _lib.lloyd(X, Ci, 2, -1.0, precision="fp16")
+            Ci = C0.clone()
+            iso_steps = 20
+            _lib.profile_enable(True)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            _lib.lloyd(X, Ci, iso_steps, -1.0, precision="fp16")
+            e1.record()
+            torch.cuda.synchronize()
+            iprof = _lib.profile_read()
+            _lib.profile_enable(False)
+            iso = tc_roofline(n, iprof["tc"][0], iprof["tc"][1], e0.elapsed_time(e1))
+            roofline["isolated"] = {key: iso[key] for key in ("achieved", "frac", "issued_tflops", "frac_issued",
+                                                               "ms_per_launch", "launches", "peak_source")}
+            roofline["isolated"]["ms_per_step"] = e0.elapsed_time(e1) / iso_steps
+            roofline["isolated"]["how"] = ("the same kernel as one launch over all %d frames per iteration "
+                                           "(KM_TC_CHUNKS=1), %d iterations" % (n, iso_steps))
+            del Ci
+        finally:
+            if old is None:
+                del os.environ["KM_TC_CHUNKS"]
+            else:
+                os.environ["KM_TC_CHUNKS"] = old
 
     extra = {}
     if rank == 0:
@@ -540,11 +585,12 @@ def run_ours(args):
         dist.destroy_process_group()
     if rank != 0:
         return
-    # Per iteration: prep_centers, tc_assign, 3 candidate re-check kernels,
-    # 3 full re-check kernels (short list, tiled, finalize), 7 centroid-update
-    # kernels (count, scan, scatter, segment sums, flips, finalize, cost).
-    # Once per km_lloyd call: shift, center norms, scale, FP16 frame copy.
-    launches_per_step = 15
+    # Per iteration: prep_centers; per chunk of the tensor-core pass the
+    # tensor-core launch, 3 candidate re-check kernels and 3 full re-check
+    # kernels (short list, tiled, finalize); 7 centroid-update kernels (count,
+    # scan, scatter, segment sums, flips, finalize, cost).  Once per km_lloyd
+    # call: shift, center norms, scale, FP16 frame copy.
+    launches_per_step = 1 + 7 * tc_chunks(n) + 7
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "fp16 distances (fp32 accumulate), fp32 recheck, f64 sums",
