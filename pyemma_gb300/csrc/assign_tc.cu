@@ -544,61 +544,131 @@ __global__ void scale_finalize_kernel(uint32_t *__restrict__ scal) {
 
 // Frames: one warp per row.  xnorm = (||x_hat||^2 in scaled units, upper
 // bound of ||x'||, upper bound of ||x_hat/s - x'||, 0) in unscaled units.
+// get(f) gives feature f of row i.
+template <typename T, class Get>
+__device__ __forceinline__ void prep_one_row(const Get &get, int64_t i, int d, int kp,
+                                             const float *__restrict__ shift, float sc, float inv_sc,
+                                             T *__restrict__ xh, float4 *__restrict__ xnorm, float norm_inflate,
+                                             int lane) {
+    using O = Op16<T>;
+    typename O::T2 *dst = reinterpret_cast<typename O::T2 *>(xh + i * kp);
+    CSum h2, s2, e2;
+    for (int f = 2 * lane; f < kp; f += 64) {
+        // Columns < d: centered, scaled frame values; d and d+1: 1 (they
+        // meet the hi/lo norm columns of the centers); the rest: 0.
+        float a = 0.0f, b = 0.0f, ia, ib;
+        if (f < d) {
+            a = __fsub_rn(get(f), shift[f]);
+            ia = a * sc;
+        } else {
+            ia = (f == d || f == d + 1) ? 1.0f : 0.0f;
+        }
+        if (f + 1 < d) {
+            b = __fsub_rn(get(f + 1), shift[f + 1]);
+            ib = b * sc;
+        } else {
+            ib = (f + 1 == d || f + 1 == d + 1) ? 1.0f : 0.0f;
+        }
+        const typename O::T2 h = O::pack(ia, ib);
+        dst[f >> 1] = h;
+        if (f < d) {
+            const float ha = O::lo(h);
+            const float ea = ha - ia;
+            h2.add(ha * ha);
+            s2.add(a * a);
+            e2.add(ea * ea);
+        }
+        if (f + 1 < d) {
+            const float hb = O::hi(h);
+            const float eb = hb - ib;
+            h2.add(hb * hb);
+            s2.add(b * b);
+            e2.add(eb * eb);
+        }
+    }
+    const float th = warp_sum_ff(h2.s, h2.c);
+    const float ts = warp_sum_ff(s2.s, s2.c);
+    const float te = warp_sum_ff(e2.s, e2.c);
+    if (lane == 0) {
+        const float sx = __fsqrt_ru(__fmul_ru(ts, norm_inflate));
+        const float hx = __fmul_ru(__fadd_ru(__fsqrt_ru(__fmul_ru(te, norm_inflate)), 1e-30f), inv_sc);
+        xnorm[i] = make_float4(th, sx, hx, 0.0f);
+    }
+}
+
 template <typename T, class Src>
 __global__ void prep_frames_kernel(const Src rows, int64_t n, int d, int kp,
                                    const float *__restrict__ shift, const uint32_t *__restrict__ scal,
                                    T *__restrict__ xh, float4 *__restrict__ xnorm, float norm_inflate) {
-    using O = Op16<T>;
     const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
     const int lane = threadIdx.x & 31;
     const float sc = __uint_as_float(scal[kScale]);
     const float inv_sc = 1.0f / sc;  // exact: a power of two
-    for (int64_t i = w; i < n; i += nw) {
-        typename O::T2 *dst = reinterpret_cast<typename O::T2 *>(xh + i * kp);
-        CSum h2, s2, e2;
-        for (int f = 2 * lane; f < kp; f += 64) {
-            // Columns < d: centered, scaled frame values; d and d+1: 1 (they
-            // meet the hi/lo norm columns of the centers); the rest: 0.
-            float a = 0.0f, b = 0.0f, ia, ib;
-            if (f < d) {
-                a = __fsub_rn(rows.get(i, f), shift[f]);
-                ia = a * sc;
-            } else {
-                ia = (f == d || f == d + 1) ? 1.0f : 0.0f;
-            }
-            if (f + 1 < d) {
-                b = __fsub_rn(rows.get(i, f + 1), shift[f + 1]);
-                ib = b * sc;
-            } else {
-                ib = (f + 1 == d || f + 1 == d + 1) ? 1.0f : 0.0f;
-            }
-            const typename O::T2 h = O::pack(ia, ib);
-            dst[f >> 1] = h;
-            if (f < d) {
-                const float ha = O::lo(h);
-                const float ea = ha - ia;
-                h2.add(ha * ha);
-                s2.add(a * a);
-                e2.add(ea * ea);
-            }
-            if (f + 1 < d) {
-                const float hb = O::hi(h);
-                const float eb = hb - ib;
-                h2.add(hb * hb);
-                s2.add(b * b);
-                e2.add(eb * eb);
-            }
-        }
-        const float th = warp_sum_ff(h2.s, h2.c);
-        const float ts = warp_sum_ff(s2.s, s2.c);
-        const float te = warp_sum_ff(e2.s, e2.c);
-        if (lane == 0) {
-            const float sx = __fsqrt_ru(__fmul_ru(ts, norm_inflate));
-            const float hx = __fmul_ru(__fadd_ru(__fsqrt_ru(__fmul_ru(te, norm_inflate)), 1e-30f), inv_sc);
-            xnorm[i] = make_float4(th, sx, hx, 0.0f);
-        }
+    for (int64_t i = w; i < n; i += nw)
+        prep_one_row<T>([&](int f) { return rows.get(i, f); }, i, d, kp, shift, sc, inv_sc, xh, xnorm,
+                        norm_inflate, lane);
+}
+
+// The same for coordinate frames, with each frame's coordinates staged in
+// one of two per-warp shared-memory slots by 4-byte cp.async copies (the
+// next frame lands while this one is converted) and the atom pairs of all
+// features in a CTA table of packed slot offsets (3 a | 3 b << 16).  The
+// features are pair_feature's, as in PairRows.
+constexpr int kPrepPairThreads = 256;
+constexpr int kPrepPairMaxAtoms = 128;
+
+size_t prep_pairs_smem(int d, int n_atoms) {
+    const size_t slot = (size_t)((3 * n_atoms + 3) & ~3);
+    return (size_t)((d + 3) & ~3) * 4 + (size_t)(kPrepPairThreads / 32) * 2 * slot * 4;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kPrepPairThreads) prep_frames_pairs_kernel(
+    const PairRows rows, int64_t n, int d, int kp, const float *__restrict__ shift,
+    const uint32_t *__restrict__ scal, T *__restrict__ xh, float4 *__restrict__ xnorm, float norm_inflate) {
+    extern __shared__ uint32_t prep_sm[];
+    uint32_t *ofs = prep_sm;
+    const int row_floats = 3 * rows.n_atoms;
+    const int slot = (row_floats + 3) & ~3;
+    const int lane = threadIdx.x & 31;
+    float *ring = reinterpret_cast<float *>(prep_sm + ((d + 3) & ~3)) + (threadIdx.x >> 5) * 2 * slot;
+    for (int f = threadIdx.x; f < d; f += blockDim.x) {
+        const int2 pr = __ldg(rows.pairs + f);
+        ofs[f] = (uint32_t)(3 * pr.x) | ((uint32_t)(3 * pr.y) << 16);
     }
+    __syncthreads();
+    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const float sc = __uint_as_float(scal[kScale]);
+    const float inv_sc = 1.0f / sc;  // exact: a power of two
+    auto fetch = [&](int64_t i, int q) {
+        const float *g = rows.xyz + i * row_floats;
+        float *dst = ring + q * slot;
+        for (int t = lane; t < row_floats; t += 32) cp_async4(dst + t, g + t);
+    };
+    if (w < n) fetch(w, 0);
+    cp_async_commit();
+    int q = 0;
+    for (int64_t i = w; i < n; i += nw, q ^= 1) {
+        // the next frame into the other slot, read by every lane before the
+        // __syncwarp that closed the previous row
+        if (i + nw < n) fetch(i + nw, q ^ 1);
+        cp_async_commit();
+        cp_async_wait<1>();
+        __syncwarp();
+        const float *xr = ring + q * slot;
+        prep_one_row<T>(
+            [&](int f) {
+                const uint32_t o = ofs[f];
+                const float *a = xr + (o & 0xFFFFu);
+                const float *b = xr + (o >> 16);
+                return pair_feature(a[0], a[1], a[2], b[0], b[1], b[2]);
+            },
+            i, d, kp, shift, sc, inv_sc, xh, xnorm, norm_inflate, lane);
+        __syncwarp();
+    }
+    cp_async_wait<0>();
 }
 
 // The same conversion with 16-byte loads (d % 4 == 0, 16-byte aligned X and
@@ -1872,6 +1942,18 @@ int tc_prepare_frames(const float *X, int64_t n, int d, TcBuffers &b, cudaStream
             return KM_ERR_UNSUPPORTED;
         }
         const PairRows pr{ps->xyz, reinterpret_cast<const int2 *>(ps->pairs), ps->n_atoms, d};
+        const size_t smem = prep_pairs_smem(d, ps->n_atoms);
+        if (ps->n_atoms <= kPrepPairMaxAtoms && smem <= 48 * 1024) {
+            if (b.bf16)
+                prep_frames_pairs_kernel<__nv_bfloat16><<<(unsigned)prep_blocks(n), kPrepPairThreads, smem, s>>>(
+                    pr, n, d, b.kp, b.shift, b.scal, reinterpret_cast<__nv_bfloat16 *>(b.xh), b.xnorm,
+                    norm_inflate_of(d));
+            else
+                prep_frames_pairs_kernel<__half><<<(unsigned)prep_blocks(n), kPrepPairThreads, smem, s>>>(
+                    pr, n, d, b.kp, b.shift, b.scal, reinterpret_cast<__half *>(b.xh), b.xnorm, norm_inflate_of(d));
+            KM_CUDA(cudaGetLastError());
+            return KM_OK;
+        }
         if (b.bf16)
             prep_frames_kernel<__nv_bfloat16><<<(unsigned)prep_blocks(n), 256, 0, s>>>(
                 pr, n, d, b.kp, b.shift, b.scal, reinterpret_cast<__nv_bfloat16 *>(b.xh), b.xnorm, norm_inflate_of(d));

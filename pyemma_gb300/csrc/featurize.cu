@@ -23,18 +23,24 @@ namespace km {
 
 namespace {
 
+// A warp per frame (frames in a grid-stride walk), lanes over the pairs:
+// coalesced writes, the frame's coordinates from L1 after their first read,
+// and no 64-bit division per feature.
 __global__ void __launch_bounds__(256) pair_distances_kernel(const float *__restrict__ xyz, int64_t n, int n_atoms,
                                                              const int2 *__restrict__ pairs, int npairs,
                                                              float *__restrict__ out) {
-    const int64_t total = n * (int64_t)npairs;
-    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total;
-         q += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t t = q / npairs;
-        const int p = (int)(q - t * npairs);
-        const int2 ij = __ldg(pairs + p);
-        const float *a = xyz + (t * n_atoms + ij.x) * 3;
-        const float *b = xyz + (t * n_atoms + ij.y) * 3;
-        out[q] = pair_feature(__ldg(a), __ldg(a + 1), __ldg(a + 2), __ldg(b), __ldg(b + 1), __ldg(b + 2));
+    const int lane = threadIdx.x & 31;
+    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t t = w; t < n; t += nw) {
+        const float *x = xyz + t * n_atoms * 3;
+        float *o = out + t * npairs;
+        for (int p = lane; p < npairs; p += 32) {
+            const int2 ij = __ldg(pairs + p);
+            const float *a = x + ij.x * 3;
+            const float *b = x + ij.y * 3;
+            o[p] = pair_feature(__ldg(a), __ldg(a + 1), __ldg(a + 2), __ldg(b), __ldg(b + 1), __ldg(b + 2));
+        }
     }
 }
 
@@ -71,7 +77,7 @@ int km_pair_distances(const float *xyz, int64_t n, int32_t n_atoms, const int32_
     const int64_t total = n * (int64_t)npairs;
     if (total == 0) return KM_OK;
     KM_TRY(check_pairs(pairs, npairs, n_atoms, static_cast<cudaStream_t>(stream)));
-    int64_t g = (total + 255) / 256;
+    int64_t g = (n * 32 + 255) / 256;  // a warp per frame
     const int64_t cap = (int64_t)num_sms() * 16;
     if (g > cap) g = cap;
     pair_distances_kernel<<<(unsigned)g, 256, 0, static_cast<cudaStream_t>(stream)>>>(

@@ -185,6 +185,21 @@ struct DenseRows {
     __device__ __forceinline__ float get(int64_t i, int f) const { return __ldg(X + i * d + f); }
 };
 
+// 4-byte asynchronous copies global -> shared (no alignment rule beyond 4
+// bytes), committed in groups; cp_async_wait<N> returns once at most N of
+// this thread's groups are still in flight.  Other lanes see the data after
+// their own wait and a __syncwarp.
+__device__ __forceinline__ void cp_async4(float *dst, const float *src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)),
+                 "l"(src)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
 // The distance of atoms a and b: one rounding per operation, in the order
 // sqrt((dx^2 + dy^2) + dz^2) with d = b - a.  Every kernel that computes a
 // pair feature goes through this function.

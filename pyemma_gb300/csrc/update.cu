@@ -389,15 +389,6 @@ __global__ void __launch_bounds__(kBulkWarps * 32, (MW > 17 ? 1 : 2)) seg_accumu
 constexpr int kPairSlots = 4;
 constexpr int kPairMaxAtoms = 128;  // slots of up to 384 floats: 48 KB per CTA at most
 
-__device__ __forceinline__ void cp_async4(float *dst, const float *src) {
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(sh_addr(dst)), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() {
-    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
-}
-
 int pair_slot_floats(int n_atoms) { return (3 * n_atoms + 3) & ~3; }
 size_t pair_seg_smem(int n_atoms) { return (size_t)8 * kPairSlots * pair_slot_floats(n_atoms) * sizeof(float); }
 
