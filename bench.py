@@ -496,29 +496,40 @@ def run_ours(args):
         link_gbs = n * D * 4 / (min(copy_ms) / 1e3) / 1e9
         del X  # the API makes its own device copy
         torch.cuda.empty_cache()
-        km = KmeansClustering(n_clusters=K, max_iter=1, tolerance=-1.0, clustercenters=C0h, precision="fp16")
-        km.estimate(Xh_np)  # warm-up
+        # Warm-up: the first passes over a freshly allocated multi-GB pinned
+        # buffer run slower (32 against 21 ms per call here) while its pages
+        # are first mapped for the device; W >= 3 calls precede the timing.
+        e2e_warm = max(3, args.warmup)
+        for _ in range(e2e_warm):
+            KmeansClustering(n_clusters=K, max_iter=1, tolerance=-1.0, clustercenters=C0h,
+                             precision="fp16").estimate(Xh_np)
         e2e_steps = max(1, min(args.steps, 5))
+        step_ms = []
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for _ in range(e2e_steps):
+            ts = time.perf_counter()
             km = KmeansClustering(n_clusters=K, max_iter=1, tolerance=-1.0, clustercenters=C0h, precision="fp16")
             km.estimate(Xh_np)
             _ = km.clustercenters  # host result (already copied back by estimate)
+            step_ms.append((time.perf_counter() - ts) * 1e3)
         dt = (time.perf_counter() - t0) / e2e_steps
         e2e = {"value": n / dt, "unit": UNIT, "h2d_bytes_per_step": n * D * 4, "d2h_bytes_per_step": K * D * 4 + 8,
                "api": "KmeansClustering(n_clusters=2000, max_iter=1, clustercenters=C).estimate(pinned host X)",
-               "steps": e2e_steps, "h2d_link_gbs": link_gbs,
+               "steps": e2e_steps, "warmup": e2e_warm, "step_ms": step_ms, "h2d_link_gbs": link_gbs,
                "copy_bound_frames_per_s": link_gbs * 1e9 / (D * 4),
                "overlap": "frames copied in chunks on a side stream while the first iteration assigns "
                           "the chunks already copied (km_lloyd_host)"}
         # The same call with the frames in an ordinary (pageable) numpy
-        # array, as PyEMMA callers hold them: the library stages the copy
-        # through page-locked buffers on worker threads.
+        # array, as PyEMMA callers hold them: where the GPU reads host memory
+        # in place (Grace), a device kernel copies the chunks; elsewhere the
+        # library stages them through page-locked buffers on worker threads.
         Xpg = np.empty_like(Xh_np)
         Xpg[...] = Xh_np
         del Xh, Xh_np
-        KmeansClustering(n_clusters=K, max_iter=1, tolerance=-1.0, clustercenters=C0h, precision="fp16").estimate(Xpg)
+        for _ in range(e2e_warm):
+            KmeansClustering(n_clusters=K, max_iter=1, tolerance=-1.0, clustercenters=C0h,
+                             precision="fp16").estimate(Xpg)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for _ in range(e2e_steps):
@@ -551,8 +562,9 @@ def run_ours(args):
         pair_ms = e0.elapsed_time(e1) / 5
         del src, xyz_d, Cp
         torch.cuda.empty_cache()
-        km = KmeansClustering(n_clusters=K, max_iter=1, tolerance=-1.0, clustercenters=C0h, precision="fp16")
-        km.estimate(featurize.pair_distance_frames(xyz_h, excluded_neighbors=0))
+        for _ in range(e2e_warm):
+            km = KmeansClustering(n_clusters=K, max_iter=1, tolerance=-1.0, clustercenters=C0h, precision="fp16")
+            km.estimate(featurize.pair_distance_frames(xyz_h, excluded_neighbors=0))
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for _ in range(e2e_steps):
@@ -736,8 +748,9 @@ def run_c2(args):
         p.numpy()[...] = t
         pinned.append(p.numpy())
     Ch = C0.cpu().numpy()
-    km = KmeansClustering(n_clusters=1000, max_iter=1, tolerance=-1.0, clustercenters=Ch)
-    km.estimate(pinned)
+    for _ in range(max(3, args.warmup)):  # first passes over fresh pinned buffers run slower
+        km = KmeansClustering(n_clusters=1000, max_iter=1, tolerance=-1.0, clustercenters=Ch)
+        km.estimate(pinned)
     reps = 3
     t0 = time.perf_counter()
     for _ in range(reps):
