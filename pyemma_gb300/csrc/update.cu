@@ -569,10 +569,14 @@ __global__ void finalize_kernel(const double *__restrict__ S, const double *__re
         if (lane == 0) ccost[j] = 0.0;
     } else {
         const double dc = (double)cnt;
+        // one float64 division per center, not per element (FP64 divisions
+        // are slow on this part): S_j / n_j as S_j times the reciprocal, at
+        // most a float64 rounding apart before mu is rounded to float
+        const double inv = 1.0 / dc;
         const double *s = S + j * d;
         double cross = 0.0, sq = 0.0;
         for (int f = lane; f < d; f += 32) {
-            const float mu = (float)((double)c[f] + s[f] / dc);
+            const float mu = (float)((double)c[f] + s[f] * inv);
             const double dl = (double)mu - (double)c[f];
             cross += dl * s[f];
             sq += dl * dl;
