@@ -396,6 +396,14 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
         : "r"(taddr));
 }
 
+// max of three floats in one instruction (PTX max.f32 with three inputs,
+// sm_100 and later): NaN inputs are ignored as by fmaxf.
+__device__ __forceinline__ float max3f(float a, float b, float c) {
+    float d;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+
 __device__ __forceinline__ void tmem_wait_ld() {
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
@@ -1367,15 +1375,18 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                         for (int c = 0; c < 32; ++c)
                             if (j0 + c < p.k) p.dump[i * p.k + j0 + c] = fmaf(-2.0f, v[c], xn.x) * inv_s2;
                     }
-                    // Chunk maximum by a tree (five dependent steps, not 31).
-                    float m16[16];
+                    // Chunk maximum by a tree of three-input maxima: 16
+                    // instructions in four dependent steps (32 -> 12 -> 4 -> 2 -> 1).
+                    float m12[12];
 #pragma unroll
-                    for (int q = 0; q < 16; ++q) m16[q] = fmaxf(v[q], v[q + 16]);
-#pragma unroll
-                    for (int w = 8; w >= 1; w >>= 1)
-#pragma unroll
-                        for (int q = 0; q < w; ++q) m16[q] = fmaxf(m16[q], m16[q + w]);
-                    const float mx = m16[0];
+                    for (int q = 0; q < 10; ++q) m12[q] = max3f(v[3 * q], v[3 * q + 1], v[3 * q + 2]);
+                    m12[10] = v[30];
+                    m12[11] = v[31];
+                    const float m4a = max3f(m12[0], m12[1], m12[2]);
+                    const float m4b = max3f(m12[3], m12[4], m12[5]);
+                    const float m4c = max3f(m12[6], m12[7], m12[8]);
+                    const float m4d = max3f(m12[9], m12[10], m12[11]);
+                    const float mx = fmaxf(max3f(m4a, m4b, m4c), m4d);
                     if (mx >= thr && mx > kNegInf) {
                         if (mx > best) {
                             best = mx;

@@ -326,6 +326,43 @@ def test_lloyd_matches_oracle(torch, L, oracle, prec, d, k):
     np.testing.assert_array_equal(r["labels"].cpu().numpy(), ref["labels"])
 
 
+@pytest.mark.parametrize("prec", ["fp16", "bf16"])
+def test_lloyd_chunked_pass_equals_one_launch(torch, L, oracle, monkeypatch, prec):
+    # From 2^19 frames a Lloyd iteration runs its tensor-core pass in up to 4
+    # launches over consecutive frame ranges (KM_TC_CHUNKS), each chunk with
+    # its own candidate lists and counters and its exact re-check beside the
+    # next launch.  Labels must not depend on the chunking; centers only to
+    # the rounding of the float64 sums (the flips of different chunks arrive
+    # in another order).  An odd frame count puts a partial unit in the last
+    # chunk.
+    from pyemma_gb300 import datasets
+    n = (1 << 20) + 12345
+    X = dev(torch, datasets.gaussian_mixture(n, 48, 400, 0.3, 5.0, seed=77))
+    rng = np.random.default_rng(77)
+    C0 = X[torch.from_numpy(rng.choice(n, 300, replace=False)).cuda()].contiguous()
+    out = {}
+    for chunks in ("1", "2", "3", "4", "8"):
+        monkeypatch.setenv("KM_TC_CHUNKS", chunks)
+        C = C0.clone()
+        r = L.lloyd(X, C, 1, -1.0, precision=prec)  # labels of C0: exact, whatever the chunking
+        r2 = L.lloyd(X, C, 2, -1.0, precision=prec)
+        out[chunks] = (C, r, r2)
+    C1, r1, r21 = out["1"]
+    for chunks, (C, r, r2) in out.items():
+        assert torch.equal(r["labels"], r1["labels"]), chunks
+        np.testing.assert_allclose(r["inertias"], r1["inertias"], rtol=1e-9)
+        torch.testing.assert_close(C, C1, rtol=1e-6, atol=1e-6)
+        np.testing.assert_allclose(r2["inertias"], r21["inertias"], rtol=1e-6)
+    # the last iteration's labels against the oracle on a sample
+    monkeypatch.setenv("KM_TC_CHUNKS", "4")
+    C = C0.clone()
+    L.lloyd(X, C, 2, -1.0, precision=prec)
+    lab, _ = L.assign(X, C, precision=prec)
+    sample = np.sort(rng.choice(n, 20000, replace=False))
+    Xs = X[torch.from_numpy(sample).cuda()].cpu().numpy()
+    np.testing.assert_array_equal(lab.cpu().numpy()[sample], oracle.assign(Xs, C.cpu().numpy()))
+
+
 def test_lloyd_zero_iterations(torch, L):
     X = torch.ones((10, 3), dtype=torch.float32, device="cuda")
     C = torch.zeros((2, 3), dtype=torch.float32, device="cuda")
