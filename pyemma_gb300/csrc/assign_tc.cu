@@ -80,6 +80,7 @@ enum ScalarSlot { kScale = 0, kInvScale2 = 1, kScaleMax = 2, kCmax = 3, kHcMax =
 struct TcParams {
     int64_t n;       // one past the last frame of this launch
     int64_t frame0;  // its first frame (frames [frame0, n) of the operand rows)
+    int32_t *label_counts;  // nullable: each frame's tensor-core label is counted here
     int k;
     int d;
     int kp;
@@ -1491,6 +1492,13 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                 }
                 p.labels[i] = jb;
             }
+            if (p.label_counts) {
+                // member counts for the centroid update: one atomic per label
+                // and warp
+                const int lab = i < p.n ? jb : -1;
+                const unsigned peers = __match_any_sync(0xffffffffu, lab);
+                if (lab >= 0 && lane == __ffs(peers) - 1) atomicAdd(&p.label_counts[lab], __popc(peers));
+            }
             const unsigned m_rc = __ballot_sync(0xffffffffu, need_rc);
             if (m_rc) {
                 // One entry per re-checked frame and one pair per candidate,
@@ -2070,7 +2078,8 @@ cudaError_t launch_tc_variant(const cudaLaunchConfig_t &cfg, int list_len, bool 
 
 int tc_assign_impl(const float *X, int64_t n, int d, const float *C, int k, int32_t *labels, TcBuffers &b,
                    cudaStream_t s, ProfEvents *prof, float *dump, unsigned long long *wait_cycles, cudaStream_t side,
-                   const cudaEvent_t *ev_fork, int n_fork, const FlipList *fl, const PairSrc *ps) {
+                   const cudaEvent_t *ev_fork, int n_fork, const FlipList *fl, const PairSrc *ps,
+                   int32_t *label_counts) {
     if (n == 0) return KM_OK;
     Plan pl;
     if (!make_plan(d, k, pl, b.fp8 != 0) || !device_is_sm10x()) {
@@ -2114,6 +2123,7 @@ int tc_assign_impl(const float *X, int64_t n, int d, const float *C, int k, int3
     TcParams p;
     p.n = n;
     p.frame0 = 0;
+    p.label_counts = label_counts;
     p.k = k;
     p.d = d;
     p.kp = b.kp;
@@ -2286,13 +2296,15 @@ int tc_assign_impl(const float *X, int64_t n, int d, const float *C, int k, int3
 
 int tc_assign(const float *X, int64_t n, int d, const float *C, int k, int32_t *labels, TcBuffers &b,
               cudaStream_t s, ProfEvents *prof, float *dump, unsigned long long *wait_cycles, const PairSrc *ps) {
-    return tc_assign_impl(X, n, d, C, k, labels, b, s, prof, dump, wait_cycles, nullptr, nullptr, 0, nullptr, ps);
+    return tc_assign_impl(X, n, d, C, k, labels, b, s, prof, dump, wait_cycles, nullptr, nullptr, 0, nullptr, ps,
+                          nullptr);
 }
 
 int tc_assign_deferred(const float *X, int64_t n, int d, const float *C, int k, int32_t *labels, TcBuffers &b,
                        cudaStream_t s, cudaStream_t side, const cudaEvent_t *ev_fork, int n_fork, const FlipList &fl,
-                       ProfEvents *prof, const PairSrc *ps) {
-    return tc_assign_impl(X, n, d, C, k, labels, b, s, prof, nullptr, nullptr, side, ev_fork, n_fork, &fl, ps);
+                       ProfEvents *prof, const PairSrc *ps, int32_t *label_counts) {
+    return tc_assign_impl(X, n, d, C, k, labels, b, s, prof, nullptr, nullptr, side, ev_fork, n_fork, &fl, ps,
+                          label_counts);
 }
 
 }  // namespace km

@@ -952,10 +952,14 @@ int lloyd_run(const float *X_in, const HostFrames *hf, int64_t n, int32_t d, int
         if (is_tc(prec)) {
             KM_TRY(tc_prepare_centers(C, d, k, b, st));
             KM_CUDA(cudaMemsetAsync(fl.count, 0, sizeof(int32_t), st));
-            KM_TRY(tc_assign_deferred(X, n, d, C, k, labels, b, st, side.st, side.fork, kTcMaxChunks, fl, &prof, ps));
+            // the tensor-core pass counts the members as it writes the labels
+            int32_t *counts = update_counts_from_labels(d, k, ps) ? update_counts(ws_update, n, d, k) : nullptr;
+            if (counts) KM_CUDA(cudaMemsetAsync(counts, 0, sizeof(int32_t) * k, st));
+            KM_TRY(tc_assign_deferred(X, n, d, C, k, labels, b, st, side.st, side.fork, kTcMaxChunks, fl, &prof, ps,
+                                      counts));
             prof.begin(kProfUpdate, st);
             // one segment-sum CTA per SM: room for the re-check beside it
-            KM_TRY(launch_update_accumulate(X, n, d, labels, k, C, err, ws_update, st, 1, ps));
+            KM_TRY(launch_update_accumulate(X, n, d, labels, k, C, err, ws_update, st, 1, ps, counts != nullptr));
             KM_CUDA(cudaEventRecord(side.join, side.st));
             KM_CUDA(cudaStreamWaitEvent(st, side.join, 0));
             KM_TRY(launch_apply_flips(X, n, d, k, C, fl, labels, ws_update, st, ps));

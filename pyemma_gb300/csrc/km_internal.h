@@ -97,9 +97,17 @@ int launch_update(const float *X, int64_t n, int d, const int32_t *labels, int k
 // launch_update in two halves: the sums over the members (counting sort and
 // segment sums) and the new centers and inertia from those sums.
 // seg_per_sm > 0 caps the segment-sum CTAs per SM (room for a kernel beside it).
+// counted: the member counts of `labels` are already in the workspace (added
+// by the tensor-core pass into update_counts(), cleared before it); only
+// valid where update_counts_from_labels() holds.
 int launch_update_accumulate(const float *X, int64_t n, int d, const int32_t *labels, int k, const float *C_old,
                              uint32_t *err, void *ws, cudaStream_t s, int seg_per_sm = 0,
-                             const PairSrc *ps = nullptr);
+                             const PairSrc *ps = nullptr, bool counted = false);
+// The member-count array of an update workspace, and whether the update of
+// (d, k) counts its members from the labels in a pass of its own (the
+// counting-sort path; the one-pass small-shape path counts as it sums).
+int32_t *update_counts(void *ws, int64_t n, int d, int k);
+bool update_counts_from_labels(int d, int k, const PairSrc *ps);
 int launch_update_finish(int64_t n, int d, int k, const float *C_old, float *C_new, int64_t *counts_out,
                          double *cost, void *ws, cudaStream_t s);
 // The update of frames that arrive in parts: begin clears the totals, each
@@ -224,9 +232,12 @@ int tc_assign(const float *X, int64_t n, int d, const float *C, int k, int32_t *
 // holds the tensor-core labels; the caller joins `side` back into s before
 // it applies fl.
 constexpr int kTcMaxChunks = 8;
+// label_counts (nullable, k ints, zeroed by the caller): the pass adds each
+// frame's tensor-core label to it.
 int tc_assign_deferred(const float *X, int64_t n, int d, const float *C, int k, int32_t *labels, TcBuffers &b,
                        cudaStream_t s, cudaStream_t side, const cudaEvent_t *ev_fork, int n_fork,
-                       const FlipList &fl, ProfEvents *prof = nullptr, const PairSrc *ps = nullptr);
+                       const FlipList &fl, ProfEvents *prof = nullptr, const PairSrc *ps = nullptr,
+                       int32_t *label_counts = nullptr);
 
 // Resident center sets (capi.cu), used by the serving loop (serve.cu).
 int assign_centers_enqueue(const float *X, int64_t n, const km_centers *h, int32_t *labels, void *ws,

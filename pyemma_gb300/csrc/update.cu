@@ -903,10 +903,19 @@ size_t update_ws_size(int64_t n, int d, int k) {
     return b;
 }
 
+int32_t *update_counts(void *ws, int64_t n, int d, int k) { return carve(ws, n, d, k, nullptr).counts; }
+
+bool update_counts_from_labels(int d, int k, const PairSrc *ps) { return ps || !small_ok(d, k); }
+
 int launch_update_accumulate(const float *X, int64_t n, int d, const int32_t *labels, int k, const float *C_old,
-                             uint32_t *err, void *ws, cudaStream_t s, int seg_per_sm, const PairSrc *ps) {
+                             uint32_t *err, void *ws, cudaStream_t s, int seg_per_sm, const PairSrc *ps,
+                             bool counted) {
     UpdateWs u = carve(ws, n, d, k, nullptr);
-    KM_CUDA(cudaMemsetAsync(u.counts, 0, sizeof(int32_t) * k, s));
+    if (counted && !update_counts_from_labels(d, k, ps)) {
+        set_error("precounted members only on the counting-sort path of the update");
+        return KM_ERR_UNSUPPORTED;
+    }
+    if (!counted) KM_CUDA(cudaMemsetAsync(u.counts, 0, sizeof(int32_t) * k, s));
     KM_CUDA(cudaMemsetAsync(u.S, 0, sizeof(double) * (size_t)k * d, s));
     KM_CUDA(cudaMemsetAsync(u.Q, 0, sizeof(double) * k, s));
     if (n > 0 && !ps && small_ok(d, k)) {
@@ -929,7 +938,7 @@ int launch_update_accumulate(const float *X, int64_t n, int d, const int32_t *la
         KM_CUDA(cudaGetLastError());
         return KM_OK;
     }
-    if (n > 0) {
+    if (n > 0 && !counted) {
         count_labels_kernel<<<grid_for(n, 256, 8), 256, 0, s>>>(labels, n, k, u.counts, err);
         KM_CUDA(cudaGetLastError());
     }
