@@ -1492,13 +1492,10 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                 }
                 p.labels[i] = jb;
             }
-            if (p.label_counts) {
-                // member counts for the centroid update: one atomic per label
-                // and warp
-                const int lab = i < p.n ? jb : -1;
-                const unsigned peers = __match_any_sync(0xffffffffu, lab);
-                if (lab >= 0 && lane == __ffs(peers) - 1) atomicAdd(&p.label_counts[lab], __popc(peers));
-            }
+            // member counts for the centroid update: one reduction per frame
+            // (its value unused, so the warp does not wait for it; gathering
+            // equal labels of a warp first cost the kernel more than it saved)
+            if (p.label_counts && i < p.n) atomicAdd(&p.label_counts[jb], 1);
             const unsigned m_rc = __ballot_sync(0xffffffffu, need_rc);
             if (m_rc) {
                 // One entry per re-checked frame and one pair per candidate,
