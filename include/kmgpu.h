@@ -195,13 +195,15 @@ int km_lloyd(const float *X, int64_t n, int32_t d, int32_t k, float *C, int32_t 
              size_t workspace_bytes, void *stream);
 
 /* km_lloyd on frames that are still in host memory: X_parts[q] (host,
- * part_rows[q] x d row-major float32, pinned for an overlapped copy) are
- * copied one after the other into X (device, n x d, caller-owned; it holds
- * the frames afterwards), in chunks on a stream of the library's own.  The
- * first iteration assigns each chunk as soon as its copy has landed, so the
- * transfer and the assignment overlap; the run is otherwise km_lloyd's (same
- * workspace, results equal to km_lloyd on the copied X).  With max_iter = 0
- * it only copies.  Stands in for the same fit as km_lloyd, reached with
+ * part_rows[q] x d row-major float32) are copied one after the other into X
+ * (device, n x d, caller-owned; it holds the frames afterwards), in chunks on
+ * a stream of the library's own.  The first iteration assigns each chunk as
+ * soon as its copy has landed, so the transfer and the assignment overlap;
+ * the run is otherwise km_lloyd's (same workspace, results equal to km_lloyd
+ * on the copied X).  Page-locked parts are copied by the copy engines;
+ * pageable parts by a device kernel where the GPU reads host memory in place
+ * (cudaDevAttrPageableMemoryAccess), else by worker threads through
+ * page-locked blocks; both forms overlap.  With max_iter = 0 it only copies.  Stands in for the same fit as km_lloyd, reached with
  * frames that the reference holds in host memory (kmeans.py:253-258 with the
  * in-memory chunks that kmeans.py:218-234 and 326-338 gather). */
 int km_lloyd_host(const float *const *X_parts, const int64_t *part_rows, int32_t n_parts, float *X, int64_t n,
