@@ -274,8 +274,10 @@ int km_tune_clear(void);
  * process-wide table behind a mutex: later tensor-core calls for (d, k)
  * use it (km_tune_clear empties the table).  Workspace as km_tune.
  * Synchronises `stream`; refuses to run while the stream is captured.
- * km_tile_plan_get reports the shape that calls for (d, k) use now
- * (*tuned = 1 when it comes from the table). */
+ * km_tile_plan_get reports the shape that FP16 calls for (d, k) use now
+ * (*tuned = 1 when it comes from the table).  Without a stored shape, FP16
+ * keeps 8 candidates per frame up to d = 256 and 16 above; BF16 and FP8
+ * keep 16. */
 typedef struct {
     int32_t bn, pair, stages, list_len;
     double ms; /* mean time of one km_assign call with this shape (km_tune_tiles) */

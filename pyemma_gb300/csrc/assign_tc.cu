@@ -1706,10 +1706,10 @@ bool build_plan(int d, int bn, bool pair, int max_stages, int list_len, Plan &pl
 }
 
 // The default shape: full-width center tiles (256 columns, or k rounded up
-// to 32), the CTA pair where it applies, as many stages as fit, 16
-// candidates.  A shape forced by the tuning thread, or stored by
-// km_tune_tiles for (d, k), replaces it.
-bool make_plan(int d, int k, Plan &pl, bool fp8 = false) {
+// to 32), the CTA pair where it applies, as many stages as fit, 8 candidates
+// (FP16 up to d = 256) or 16.  A shape forced by the tuning thread, or
+// stored by km_tune_tiles for (d, k), replaces it.
+bool make_plan(int d, int k, Plan &pl, bool fp8 = false, bool bf16 = false) {
     const TilePlan *tp = t_forced_plan;
     TilePlan stored;
     if (!tp) {
@@ -1728,8 +1728,15 @@ bool make_plan(int d, int k, Plan &pl, bool fp8 = false) {
         if (t_forced_plan) return false;
     }
     const int bn = pick_bn(k);
-    if (bn == 256 && pair_wanted() && build_plan(d, bn, true, 0, kL, pl, fp8)) return true;
-    return build_plan(d, bn, false, 0, kL, pl, fp8);
+    // FP16: 8 candidates up to d = 256, 16 above: km_tune_tiles picked 8 on
+    // every measured shape with d <= 256 (fewer list shifts in the epilogue)
+    // and 16 at d = 528 and 1024, where 8 overflow too often (20% slower at
+    // d = 528, k = 2000).  BF16 and FP8 keep 16: their wider bounds leave
+    // more candidates per frame (BF16 with 8 at d = 256, k = 5000: 4.3 ->
+    // 24.9 ms per iteration, most frames re-checked over all centers).
+    const int len = !fp8 && !bf16 && d <= 256 ? 8 : kL;
+    if (bn == 256 && pair_wanted() && build_plan(d, bn, true, 0, len, pl, fp8)) return true;
+    return build_plan(d, bn, false, 0, len, pl, fp8);
 }
 
 bool device_is_sm10x() {
@@ -2079,7 +2086,7 @@ int tc_assign_impl(const float *X, int64_t n, int d, const float *C, int k, int3
                    int32_t *label_counts) {
     if (n == 0) return KM_OK;
     Plan pl;
-    if (!make_plan(d, k, pl, b.fp8 != 0) || !device_is_sm10x()) {
+    if (!make_plan(d, k, pl, b.fp8 != 0, b.bf16 != 0) || !device_is_sm10x()) {
         set_error("no tensor-core plan for d=%d k=%d on this device", d, k);
         return KM_ERR_UNSUPPORTED;
     }
