@@ -1729,9 +1729,10 @@ bool make_plan(int d, int k, Plan &pl, bool fp8 = false, bool bf16 = false) {
     }
     const int bn = pick_bn(k);
     // FP16: 8 candidates up to d = 256, 16 above: km_tune_tiles picked 8 on
-    // every measured shape with d <= 256 (fewer list shifts in the epilogue)
-    // and 16 at d = 528 and 1024, where 8 overflow too often (20% slower at
-    // d = 528, k = 2000).  BF16 and FP8 keep 16: their wider bounds leave
+    // every measured shape with d <= 256 (fewer list shifts in the epilogue);
+    // at d = 528, k = 2000 8 candidates are 20% slower (more lists overflow
+    // to the re-check over all centers), at d = 1024 the two tie.  BF16 and
+    // FP8 keep 16: their wider bounds leave
     // more candidates per frame (BF16 with 8 at d = 256, k = 5000: 4.3 ->
     // 24.9 ms per iteration, most frames re-checked over all centers).
     const int len = !fp8 && !bf16 && d <= 256 ? 8 : kL;
