@@ -963,11 +963,20 @@ def run_c5(args):
     # warm-up: three host-to-device passes over every pinned pool (the first
     # passes over freshly pinned memory run slower; a production server's
     # buffers are warm), then one small request per set
+    h2d_gbs = None
     for d in pools:
         tmp = torch.empty(tuple(pools[d].shape), dtype=torch.float32, device="cuda")
         for _ in range(3):
             tmp.copy_(pools[d], non_blocking=True)
         torch.cuda.synchronize()
+        if d == 528:
+            # this process's pinned host-to-device rate, for reading the latencies
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            tmp.copy_(pools[d], non_blocking=True)
+            e1.record()
+            torch.cuda.synchronize()
+            h2d_gbs = pools[d].numel() * 4 / (e0.elapsed_time(e1) / 1e3) / 1e9
         del tmp
     tmp = torch.zeros(total, dtype=torch.int32, device="cuda")  # and over the label arena, device to host
     for _ in range(3):
@@ -1036,7 +1045,7 @@ def run_c5(args):
            "requests": m, "frames": total, "offered_frames_per_s": total / dur,
            "offered_tflops": flops / dur / 1e12, "wall_s": t_end, "server": st,
            "labels_same_alone_and_mixed": same, "checked_requests": checked, "per_d": per_d,
-           "per_request_frames": per_size,
+           "per_request_frames": per_size, "h2d_gbs_pinned_pool": h2d_gbs,
            "config": {"workload": "c5: Poisson arrivals at %.0f req/s for %.0f s, lengths log-uniform [1k, 1M], "
                                   "8 resident center sets (d, k) = %s, 40 GB admission budget, pinned host "
                                   "buffers, copies included" % (rate, dur, specs)}})
