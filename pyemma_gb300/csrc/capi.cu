@@ -252,7 +252,10 @@ size_t resident_ws_bytes(int64_t n, int d, int k, int prec) {
 // A launch runs at most kLoopBatch iterations (the size of the inertia
 // buffer in the workspace).
 // dst (device) <- src (pageable host, readable by the device): 16-byte
-// words where both ends and the length allow, else 4-byte words.
+// words where both ends and the length allow, else 4-byte words.  Launched
+// with one CTA per SM, which fits beside a tensor-core CTA (no shared memory):
+// more copy CTAs on an SM would keep the assignment's CTAs off it.  Four
+// independent loads per thread keep enough bytes in flight for the host link.
 __global__ void __launch_bounds__(256) host_copy_kernel(const float *__restrict__ src, float *__restrict__ dst,
                                                         int64_t count) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -261,8 +264,16 @@ __global__ void __launch_bounds__(256) host_copy_kernel(const float *__restrict_
         const int64_t n4 = count >> 2;
         const float4 *s4 = reinterpret_cast<const float4 *>(src);
         float4 *d4 = reinterpret_cast<float4 *>(dst);
-        for (int64_t i = t; i < n4; i += stride) d4[i] = s4[i];
-        for (int64_t i = (n4 << 2) + t; i < count; i += stride) dst[i] = src[i];
+        int64_t i = t;
+        for (; i + 3 * stride < n4; i += 4 * stride) {
+            const float4 a = s4[i], b = s4[i + stride], c = s4[i + 2 * stride], e = s4[i + 3 * stride];
+            d4[i] = a;
+            d4[i + stride] = b;
+            d4[i + 2 * stride] = c;
+            d4[i + 3 * stride] = e;
+        }
+        for (; i < n4; i += stride) d4[i] = s4[i];
+        for (int64_t j = (n4 << 2) + t; j < count; j += stride) dst[j] = src[j];
     } else {
         for (int64_t i = t; i < count; i += stride) dst[i] = src[i];
     }
@@ -866,7 +877,7 @@ int lloyd_run(const float *X_in, const HostFrames *hf, int64_t n, int32_t d, int
                 if (pageable_part[q]) {
                     // read in place by the device (gpu_reads_pageable_host)
                     const int64_t count = take * d;
-                    const int64_t g = std::min<int64_t>((count / 4 + 255) / 256, (int64_t)num_sms() * 4);
+                    const int64_t g = std::min<int64_t>((count / 4 + 255) / 256, (int64_t)num_sms());
                     host_copy_kernel<<<(unsigned)(g < 1 ? 1 : g), 256, 0, sm.cs>>>(hf->parts[q] + q_off * d,
                                                                                   X + row * d, count);
                     KM_CUDA(cudaGetLastError());
