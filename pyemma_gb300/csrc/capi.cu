@@ -856,8 +856,16 @@ int lloyd_run(const float *X_in, const HostFrames *hf, int64_t n, int32_t d, int
         }
     }
     if (hf && !stager) {
-        std::vector<char> pageable_part(hf->n_parts, 0);
-        for (int32_t q = 0; q < hf->n_parts; ++q) pageable_part[q] = hf->rows[q] > 0 && is_pageable(hf->parts[q]);
+        // Where the GPU reads host memory in place, a copy kernel takes every
+        // part, page-locked or not: the copy engines' reads of page-locked
+        // memory stalled for 10-50 ms in some calls (c3 end to end, 20 calls:
+        // mean 25.0 ms, up to 69.6, against 22.4 ms, at most 24.2, by the
+        // kernel).  Elsewhere only page-locked parts reach this point, and the
+        // copy engines take them.
+        const bool in_place = gpu_reads_pageable_host();
+        std::vector<char> kernel_copy(hf->n_parts, 0);
+        for (int32_t q = 0; q < hf->n_parts; ++q)
+            kernel_copy[q] = hf->rows[q] > 0 && (in_place || is_pageable(hf->parts[q]));
         KM_CUDA(cudaStreamCreateWithFlags(&sm.cs, cudaStreamNonBlocking));
         sm.ev.assign(sm.begin.size(), nullptr);  // [0]: the caller's stream reached this call
         for (cudaEvent_t &e : sm.ev) KM_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
@@ -874,13 +882,9 @@ int lloyd_run(const float *X_in, const HostFrames *hf, int64_t n, int32_t d, int
                     q_off = 0;
                 }
                 const int64_t take = std::min(stop - row, hf->rows[q] - q_off);
-                if (pageable_part[q]) {
+                if (kernel_copy[q]) {
                     // read in place by the device (gpu_reads_pageable_host)
-                    const int64_t count = take * d;
-                    const int64_t g = std::min<int64_t>((count / 4 + 255) / 256, (int64_t)num_sms());
-                    host_copy_kernel<<<(unsigned)(g < 1 ? 1 : g), 256, 0, sm.cs>>>(hf->parts[q] + q_off * d,
-                                                                                  X + row * d, count);
-                    KM_CUDA(cudaGetLastError());
+                    KM_TRY(launch_host_copy(hf->parts[q] + q_off * d, X + row * d, take * d, sm.cs));
                 } else {
                     KM_CUDA(cudaMemcpyAsync(X + row * d, hf->parts[q] + q_off * d, sizeof(float) * (size_t)take * d,
                                             cudaMemcpyHostToDevice, sm.cs));
@@ -1571,3 +1575,17 @@ int km_tune_clear(void) {
 }
 
 }  // extern "C"
+
+namespace km {
+
+bool gpu_reads_host_in_place() { return gpu_reads_pageable_host(); }
+
+int launch_host_copy(const float *src, float *dst, int64_t count, cudaStream_t s) {
+    if (count <= 0) return KM_OK;
+    const int64_t g = std::min<int64_t>((count / 4 + 255) / 256, (int64_t)num_sms());
+    host_copy_kernel<<<(unsigned)(g < 1 ? 1 : g), 256, 0, s>>>(src, dst, count);
+    KM_CUDA(cudaGetLastError());
+    return KM_OK;
+}
+
+}  // namespace km

@@ -244,6 +244,12 @@ int assign_centers_enqueue(const float *X, int64_t n, const km_centers *h, int32
                            size_t ws_bytes, uint32_t *err_host, cudaStream_t s);
 size_t assign_centers_ws_bytes(int64_t n, const km_centers *h);
 int centers_d(const km_centers *h);
+// Whether kernels of the current device read host memory (page-locked or
+// not) in place through the host's page tables, as on Grace.
+bool gpu_reads_host_in_place();
+// dst (device) <- src (host memory the device reads in place): a copy kernel
+// on s, one CTA per SM (it fits beside a tensor-core CTA).
+int launch_host_copy(const float *src, float *dst, int64_t count, cudaStream_t s);
 int centers_device(const km_centers *h);
 int device_error_status(uint32_t e);
 // Bits set by km_debug_fake_device_error, cleared as they are taken.

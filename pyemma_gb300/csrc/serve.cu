@@ -177,7 +177,16 @@ void launch(km_server *S, Slot &sl, const km_centers *h) {
     cudaStream_t s = sl.stream;
     const int d = centers_d(h);
     int st = KM_OK;
+    // Frames into the slot: by a copy kernel where the device reads host
+    // memory in place (steadier than the copy engines' reads of page-locked
+    // memory, and any host memory works), else by the copy engines.
+    const bool in_place = gpu_reads_host_in_place();
     for (const Piece &pc : sl.pieces) {
+        if (in_place) {
+            st = launch_host_copy(pc.req->X + pc.src * d, sl.X + pc.dst * d, pc.n * d, s);
+            if (st != KM_OK) break;
+            continue;
+        }
         cudaError_t e = cudaMemcpyAsync(sl.X + pc.dst * d, pc.req->X + pc.src * d, (size_t)pc.n * d * sizeof(float),
                                         cudaMemcpyHostToDevice, s);
         if (e != cudaSuccess) {
