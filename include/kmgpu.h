@@ -200,10 +200,11 @@ int km_lloyd(const float *X, int64_t n, int32_t d, int32_t k, float *C, int32_t 
  * a stream of the library's own.  The first iteration assigns each chunk as
  * soon as its copy has landed, so the transfer and the assignment overlap;
  * the run is otherwise km_lloyd's (same workspace, results equal to km_lloyd
- * on the copied X).  Page-locked parts are copied by the copy engines;
- * pageable parts by a device kernel where the GPU reads host memory in place
- * (cudaDevAttrPageableMemoryAccess), else by worker threads through
- * page-locked blocks; both forms overlap.  With max_iter = 0 it only copies.  Stands in for the same fit as km_lloyd, reached with
+ * on the copied X).  Where the GPU reads host memory in place
+ * (cudaDevAttrPageableMemoryAccess) a device kernel copies every part,
+ * page-locked or pageable; elsewhere page-locked parts go through the copy
+ * engines and pageable ones through worker threads and page-locked blocks;
+ * all forms overlap.  With max_iter = 0 it only copies.  Stands in for the same fit as km_lloyd, reached with
  * frames that the reference holds in host memory (kmeans.py:253-258 with the
  * in-memory chunks that kmeans.py:218-234 and 326-338 gather). */
 int km_lloyd_host(const float *const *X_parts, const int64_t *part_rows, int32_t n_parts, float *X, int64_t n,
@@ -396,8 +397,10 @@ int km_assign_centers(const float *X, int64_t n, int32_t d, const km_centers *ce
  * workspace) are the device memory held for requests in flight; their total
  * stays within hbm_budget_bytes.
  *   km_serve_submit: X_host (host, n*d float32) and labels_host (host, n
- *     int32) must stay valid until the request completes; page-locked
- *     buffers let the copies run asynchronously.  d must match the set.
+ *     int32) must stay valid until the request completes.  Where the GPU
+ *     reads host memory in place a device kernel copies the frames, from
+ *     any host memory; elsewhere page-locked buffers let the copies run
+ *     asynchronously.  d must match the set.
  *   km_serve_poll: waits up to timeout_ms (-1: no limit) for the request;
  *     returns KM_PENDING if it has not completed, else its final status,
  *     after which the ticket is released.  info (host, nullable) receives
