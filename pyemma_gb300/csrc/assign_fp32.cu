@@ -144,11 +144,14 @@ int launch_cfg(const Src &src, const int32_t *frame_idx, const int32_t *n_dev, i
                const float *C, int k, int32_t *labels, float *dist, unsigned long long *flipped,
                cudaStream_t s) {
     constexpr int BM = kWarps * FT;
-    static int per_sm = -1;  // cached: no queries while a stream is being captured
-    if (per_sm < 0) {
+    static int per_sm_dev[kDeviceSlots] = {};  // per device, cached: no queries while a stream is being captured
+    const int dev = current_device();
+    int per_sm = dev >= 0 && dev < kDeviceSlots ? per_sm_dev[dev] : 0;
+    if (per_sm <= 0) {
         int v = 0;
         KM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, assign_fp32_kernel<FT, G, false, Src>, kThreads, 0));
-        per_sm = v;
+        per_sm = v > 0 ? v : 1;
+        if (dev >= 0 && dev < kDeviceSlots) per_sm_dev[dev] = per_sm;
     }
     int64_t ntiles = (n + BM - 1) / BM;
     int64_t grid = (int64_t)num_sms() * (per_sm > 0 ? per_sm : 1);

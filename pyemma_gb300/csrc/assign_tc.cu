@@ -59,6 +59,7 @@
 #include <cstdlib>
 #include <map>
 #include <mutex>
+#include <tuple>
 #include <utility>
 #include <vector>
 
@@ -1741,14 +1742,13 @@ bool make_plan(int d, int k, Plan &pl, bool fp8 = false, bool bf16 = false) {
 }
 
 bool device_is_sm10x() {
-    static int cc = -1;
-    if (cc < 0) {
-        int dev = 0, major = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
-        cc = major;
-    }
-    return cc == 10;
+    static int cc[kDeviceSlots] = {};  // compute capability major + 1 (0: not read yet)
+    const int dev = current_device();
+    if (dev >= 0 && dev < kDeviceSlots && cc[dev]) return cc[dev] == 11;
+    int major = 0;
+    cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
+    if (dev >= 0 && dev < kDeviceSlots) cc[dev] = major + 1;
+    return major == 10;
 }
 
 float norm_inflate_of(int d) {
@@ -2091,20 +2091,24 @@ int tc_assign_impl(const float *X, int64_t n, int d, const float *C, int k, int3
         set_error("no tensor-core plan for d=%d k=%d on this device", d, k);
         return KM_ERR_UNSUPPORTED;
     }
-    static std::once_flag attr_once;
-    static cudaError_t attr_err = cudaSuccess;
-    std::call_once(attr_once, [] {
-        const void *fns[6] = {(const void *)tc_assign_kernel<false, 16, false>,
-                              (const void *)tc_assign_kernel<true, 16, false>,
-                              (const void *)tc_assign_kernel<false, 8, false>,
-                              (const void *)tc_assign_kernel<true, 8, false>,
-                              (const void *)tc_assign_kernel<false, 16, true>,
-                              (const void *)tc_assign_kernel<true, 16, true>};
-        for (const void *f : fns)
-            if (attr_err == cudaSuccess)
-                attr_err = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemLimit);
-    });
-    KM_CUDA(attr_err);
+    {
+        // The shared-memory opt-in holds per device: set it once on each.
+        static std::mutex attr_mu;
+        static bool attr_done[kDeviceSlots] = {};
+        const int dev = current_device();
+        std::lock_guard<std::mutex> lk(attr_mu);
+        if (dev < 0 || dev >= kDeviceSlots || !attr_done[dev]) {
+            const void *fns[6] = {(const void *)tc_assign_kernel<false, 16, false>,
+                                  (const void *)tc_assign_kernel<true, 16, false>,
+                                  (const void *)tc_assign_kernel<false, 8, false>,
+                                  (const void *)tc_assign_kernel<true, 8, false>,
+                                  (const void *)tc_assign_kernel<false, 16, true>,
+                                  (const void *)tc_assign_kernel<true, 16, true>};
+            for (const void *f : fns)
+                KM_CUDA(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemLimit));
+            if (dev >= 0 && dev < kDeviceSlots) attr_done[dev] = true;
+        }
+    }
     // (the FP8 kernel keeps 16 candidates: make_plan set list_len)
     const void *kfn = b.fp8 ? (pl.pair ? (const void *)tc_assign_kernel<true, 16, true>
                                        : (const void *)tc_assign_kernel<false, 16, true>)
@@ -2188,9 +2192,11 @@ int tc_assign_impl(const float *X, int64_t n, int d, const float *C, int k, int3
     int clusters_fit = 0;
     if (pl.pair) {
         static std::mutex cl_mu;
-        static std::map<std::pair<int, int>, int> cached_clusters;  // (smem, list length) -> clusters
+        // (device, shared memory, list length, FP8) -> clusters
+        static std::map<std::tuple<int, int, int, int>, int> cached_clusters;
+        const auto key = std::make_tuple(current_device(), pl.smem, pl.list_len, b.fp8 != 0 ? 1 : 0);
         std::lock_guard<std::mutex> lk(cl_mu);
-        auto it = cached_clusters.find(std::make_pair(pl.smem, pl.list_len));
+        auto it = cached_clusters.find(key);
         if (it == cached_clusters.end()) {
             cudaLaunchConfig_t qc = {};
             cudaLaunchAttribute qa[1];
@@ -2206,7 +2212,7 @@ int tc_assign_impl(const float *X, int64_t n, int d, const float *C, int k, int3
             qc.gridDim = dim3((unsigned)(2 * (num_sms() / 2)), 1, 1);
             int nc = 0;
             KM_CUDA(cudaOccupancyMaxActiveClusters(&nc, kfn, &qc));
-            it = cached_clusters.emplace(std::make_pair(pl.smem, pl.list_len), nc).first;
+            it = cached_clusters.emplace(key, nc).first;
         }
         clusters_fit = it->second;
         if (clusters_fit < 1) {

@@ -80,15 +80,29 @@ inline int check_ws(void *ws, size_t have, size_t need) {
     return KM_OK;
 }
 
-inline int num_sms() {
-    static int cached = 0;
-    if (!cached) {
-        int dev = 0, v = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
-        cached = v > 0 ? v : 1;
+// Per-device caches (function attributes, occupancy, SM counts) are indexed
+// by the current device's ordinal; ordinals from kDeviceSlots on are queried
+// each time.
+constexpr int kDeviceSlots = 64;
+
+inline int current_device() {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        dev = 0;
     }
-    return cached;
+    return dev;
+}
+
+inline int num_sms() {
+    static int cached[kDeviceSlots] = {};
+    const int dev = current_device();
+    if (dev >= 0 && dev < kDeviceSlots && cached[dev]) return cached[dev];
+    int v = 0;
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    v = v > 0 ? v : 1;
+    if (dev >= 0 && dev < kDeviceSlots) cached[dev] = v;
+    return v;
 }
 
 // Device error word written by kernels whose waits ran out (bit set per site).

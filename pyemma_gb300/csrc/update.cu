@@ -776,14 +776,19 @@ template <int MW, int RING>
 int launch_bulk_ring(const float *X, int64_t n, int d, const UpdateWs &u, int k, const float *C_old, uint32_t *err,
                      cudaStream_t s, int seg_per_sm) {
     const size_t smem = bulk_smem_bytes(MW, RING);
-    static int per_sm = -1;  // cached: no attribute calls while a stream is being captured
-    if (per_sm < 0) {
+    // Per device (the shared-memory opt-in holds per device), cached so that
+    // no attribute call happens while a stream is being captured.
+    static int per_sm_dev[kDeviceSlots] = {};
+    const int dev = current_device();
+    int per_sm = dev >= 0 && dev < kDeviceSlots ? per_sm_dev[dev] : 0;
+    if (per_sm <= 0) {
         KM_CUDA(cudaFuncSetAttribute(seg_accumulate_bulk_kernel<MW, RING>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(232448)));
         int v = 0;
         KM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, seg_accumulate_bulk_kernel<MW, RING>,
                                                               kBulkWarps * 32, smem));
         per_sm = v > 0 ? v : 1;
+        if (dev >= 0 && dev < kDeviceSlots) per_sm_dev[dev] = per_sm;
     }
     const int64_t npieces = (n + kPiece - 1) / kPiece;
     int64_t g = (npieces + kBulkWarps - 1) / kBulkWarps;
@@ -861,15 +866,16 @@ int launch_pairs_mw(const PairRows &src, int64_t n, int d, const UpdateWs &u, in
     // resident CTAs per SM for this slot size (the grid walks its pieces in
     // a fixed order per warp, so it is sized to what is resident at once)
     static std::mutex mu;
-    static std::map<size_t, int> per_sm_of;
+    static std::map<std::pair<int, size_t>, int> per_sm_of;  // (device, shared memory) -> CTAs per SM
     int per_sm = 0;
     {
+        const auto key = std::make_pair(current_device(), smem);
         std::lock_guard<std::mutex> lk(mu);
-        auto it = per_sm_of.find(smem);
+        auto it = per_sm_of.find(key);
         if (it == per_sm_of.end()) {
             int v = 0;
             KM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, seg_accumulate_pairs_kernel<MW>, 256, smem));
-            it = per_sm_of.emplace(smem, v > 0 ? v : 1).first;
+            it = per_sm_of.emplace(key, v > 0 ? v : 1).first;
         }
         per_sm = it->second;
     }
