@@ -129,6 +129,26 @@ def test_lloyd_pairs_other_shapes_equal_lloyd_on_features(n_atoms, excl):
         np.testing.assert_allclose(ra["inertias"], rb["inertias"], rtol=1e-6)
 
 
+def test_lloyd_pairs_chunked_pass_equals_features():
+    # 600,000 coordinate frames: the tensor-core pass runs in chunks, each
+    # chunk's re-check computing the pair features of its listed frames
+    import torch
+    from pyemma_gb300 import _lib as L
+    from pyemma_gb300.featurize import pair_distance_frames
+    rng = np.random.default_rng(71)
+    T = 600_000
+    xyz = np.concatenate([_chain(rng, T // 8 + 1, 12) for _ in range(8)])[:T]
+    src = pair_distance_frames(xyz[rng.permutation(T)], excluded_neighbors=0)
+    F = src.features()
+    C0 = F[torch.from_numpy(rng.choice(T, 256, replace=False)).cuda()].contiguous()
+    Ca, Cb = C0.clone(), C0.clone()
+    ra = L.lloyd_pairs(src.xyz, src.pairs, Ca, 1, -1.0, precision="fp16")
+    rb = L.lloyd(F, Cb, 1, -1.0, precision="fp16")
+    assert torch.equal(ra["labels"], rb["labels"])
+    torch.testing.assert_close(Ca, Cb, rtol=1e-5, atol=1e-5)
+    np.testing.assert_allclose(ra["inertias"], rb["inertias"], rtol=1e-6)
+
+
 def test_kmpp_pairs_draws_equal_kmpp_on_features(oracle):
     import torch
     from pyemma_gb300 import _lib as L
