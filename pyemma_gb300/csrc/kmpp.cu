@@ -403,22 +403,38 @@ __global__ void __launch_bounds__(256) kmpp_prune_kernel(int64_t n, const float 
     }
 }
 
-// Pruned round, launch 3: one listed frame per thread (grid-stride); a
-// smaller exact distance replaces mind and a and moves the frame's integer
-// weight in its tile's sum (modular 64-bit deltas, exact).  The CTA that
-// finishes last clears the list and draws.
+// Pruned round, launch 3: the listed frames' exact distances, 32 frames per
+// warp at a time (grid-stride over the groups of 32 list entries; rows of
+// fewer than 32 features take one frame per thread instead).  For
+// each run of 32 features, lane f holds feature f0 + f of one listed frame
+// at a time (stored rows: one coalesced 128-byte load per frame, where a
+// thread per frame makes every load touch 32 rows), squares its difference
+// to the center and stores it transposed in shared memory; lane j then adds
+// frame j's 32 squares in feature order.  So each distance is the same
+// sequence of float32 operations as sqdist_exact (every subtraction, square
+// and addition rounded once, features in order), bit for bit.  A smaller
+// distance replaces mind and a and moves the frame's integer weight in its
+// tile's sum (modular 64-bit deltas, exact).  The CTA that finishes last
+// clears the list and draws.
+constexpr int kEvalWarps = 8;
+
 template <class Src>
-__global__ void __launch_bounds__(256) kmpp_eval_kernel(
+__global__ void __launch_bounds__(kEvalWarps * 32) kmpp_eval_kernel(
     const Src src, int64_t n, int d, float *__restrict__ C0, int64_t *__restrict__ idx_out,
     float *__restrict__ mind, int32_t *__restrict__ near, const int *__restrict__ qexp_p,
     unsigned long long *__restrict__ tile_sum, unsigned int *__restrict__ done, const int32_t *__restrict__ list,
     int32_t *__restrict__ list_n, int64_t ntiles, int r_center, int r, uint32_t seed) {
+    __shared__ float sq_s[kEvalWarps][32][33];  // [feature][frame], padded: conflict-free both ways
+    __shared__ int32_t frame_s[kEvalWarps][32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float(*sq)[33] = sq_s[warp];
+    int32_t *frames = frame_s[warp];
     const int qexp = *qexp_p;
     const int64_t cnt = *list_n;
     const float *c = C0 + (int64_t)r_center * d;
-    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < cnt; e += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t i = list[e];
-        const float dd = src_d2(src, i, c, d);
+    // A smaller distance dd of frame i replaces mind and a, and moves the
+    // frame's integer weight in its tile's sum.
+    auto lower = [&](int64_t i, float dd) {
         const float mi = mind[i];
         if (dd < mi) {
             mind[i] = dd;
@@ -426,10 +442,48 @@ __global__ void __launch_bounds__(256) kmpp_eval_kernel(
             const unsigned long long delta = quant_weight(dd, qexp) - quant_weight(mi, qexp);
             if (delta) atomicAdd(&tile_sum[i / kTile], delta);
         }
+    };
+    if (d < 32) {
+        // Rows shorter than a warp: one frame per thread.
+        for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < cnt;
+             e += (int64_t)gridDim.x * blockDim.x) {
+            const int64_t i = list[e];
+            lower(i, src_d2(src, i, c, d));
+        }
+    } else {
+        const int64_t groups = (cnt + 31) / 32;
+        for (int64_t g = (int64_t)blockIdx.x * kEvalWarps + warp; g < groups;
+             g += (int64_t)gridDim.x * kEvalWarps) {
+            const int m = (int)(cnt - g * 32 < 32 ? cnt - g * 32 : 32);  // frames in this group
+            const int32_t mine = lane < m ? list[g * 32 + lane] : 0;
+            frames[lane] = mine;
+            __syncwarp();
+            float acc = 0.0f;
+            for (int f0 = 0; f0 < d; f0 += 32) {
+                const int f = f0 + lane;
+                const bool in = f < d;
+                const float cf = in ? __ldg(c + f) : 0.0f;
+                float v[32];
+#pragma unroll
+                for (int j = 0; j < 32; ++j) v[j] = (j < m && in) ? src.get(frames[j], f) : 0.0f;
+#pragma unroll
+                for (int j = 0; j < 32; ++j) sq[lane][j] = sq_term(v[j], cf);
+                __syncwarp();
+                if (f0 + 32 <= d) {
+#pragma unroll
+                    for (int q = 0; q < 32; ++q) acc = __fadd_rn(acc, sq[q][lane]);
+                } else {
+                    for (int q = 0; q < d - f0; ++q) acc = __fadd_rn(acc, sq[q][lane]);
+                }
+                __syncwarp();  // sq is overwritten by the next run of features
+            }
+            if (lane < m) lower(mine, acc);
+            __syncwarp();  // frames is overwritten by the next group
+        }
     }
     if (!kmpp_last_cta(done)) return;
     if (threadIdx.x == 0) *list_n = 0;  // for the next round
-    kmpp_draw_round<256>(ntiles, src, n, d, C0, idx_out, mind, qexp, tile_sum, done, r, seed);
+    kmpp_draw_round<kEvalWarps * 32>(ntiles, src, n, d, C0, idx_out, mind, qexp, tile_sum, done, r, seed);
 }
 
 // Round 0: a uniformly drawn frame, copied into C0[0].
@@ -512,8 +566,9 @@ int run_kmpp_src(const Src &src, int64_t n, int d, int k, uint32_t seed, float *
             KM_CUDA(cudaGetLastError());
             kmpp_prune_kernel<<<prune_grid, 256, 0, s>>>(n, w.mind, w.near, w.cc, pf, w.list, w.list_n);
             KM_CUDA(cudaGetLastError());
-            kmpp_eval_kernel<<<eval_grid, 256, 0, s>>>(src, n, d, C0, idx, w.mind, w.near, w.qexp, w.tile_sum, w.done,
-                                                       w.list, w.list_n, ntiles, rc, r, seed);
+            kmpp_eval_kernel<<<eval_grid, kEvalWarps * 32, 0, s>>>(src, n, d, C0, idx, w.mind, w.near, w.qexp,
+                                                                   w.tile_sum, w.done, w.list, w.list_n, ntiles, rc, r,
+                                                                   seed);
         }
         KM_CUDA(cudaGetLastError());
         if (cb) cb(cb_user);

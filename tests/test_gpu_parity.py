@@ -233,7 +233,7 @@ def test_kmpp_golden(torch, L, golden):
 
 @pytest.mark.parametrize("n,d,k,seed", [(1, 3, 1, 0), (5, 2, 5, 1), (3000, 2, 50, 42), (10000, 10, 200, 7),
                                         (4100, 528, 30, 3), (2049, 7, 64, 2 ** 32 - 1), (600000, 2, 20, 11),
-                                        (1100001, 3, 8, 5)])
+                                        (1100001, 3, 8, 5), (20000, 33, 40, 9), (7001, 64, 25, 4)])
 def test_kmpp_matches_oracle(torch, L, oracle, n, d, k, seed, kmpp_prune):
     rng = np.random.default_rng(seed % 1000)
     X = rng.normal(size=(n, d)).astype(np.float32)
@@ -264,7 +264,7 @@ def kmpp_prune(request, monkeypatch):
     return request.param
 
 
-@pytest.mark.parametrize("case", ["mixture", "lattice", "collinear"])
+@pytest.mark.parametrize("case", ["mixture", "mixture_wide", "lattice", "collinear"])
 def test_kmpp_pruned_pass_matches_oracle(torch, L, oracle, case, kmpp_prune):
     # Data on which the bound ||c_new - c_a||^2 >= 4 D^2 skips most frames
     # (well separated clusters), and data with exact boundary cases: integer
@@ -277,6 +277,12 @@ def test_kmpp_pruned_pass_matches_oracle(torch, L, oracle, case, kmpp_prune):
         from pyemma_gb300 import datasets
         X = datasets.gaussian_mixture(200000, 16, 50, 0.3, 5.0, seed=31)
         k = 300
+    elif case == "mixture_wide":
+        # 100 features: the listed frames are evaluated 32 to a warp, with a
+        # partial last run of features and partial groups of frames.
+        from pyemma_gb300 import datasets
+        X = datasets.gaussian_mixture(100000, 100, 40, 0.3, 5.0, seed=32)
+        k = 150
     elif case == "lattice":
         X = rng.integers(0, 8, size=(60000, 3)).astype(np.float32)
         k = 120
