@@ -202,7 +202,9 @@ int km_lloyd(const float *X, int64_t n, int32_t d, int32_t k, float *C, int32_t 
  * the run is otherwise km_lloyd's (same workspace, results equal to km_lloyd
  * on the copied X).  Where the GPU reads host memory in place
  * (cudaDevAttrPageableMemoryAccess) a device kernel copies every part,
- * page-locked or pageable; elsewhere page-locked parts go through the copy
+ * page-locked or pageable, on a stream of the device's greatest priority
+ * (its CTAs claim 16 KB blocks in turn, so a CTA placed late behind the
+ * assignment's CTAs does not hold back a chunk); elsewhere page-locked parts go through the copy
  * engines and pageable ones through worker threads and page-locked blocks;
  * all forms overlap.  With max_iter = 0 it only copies.  Stands in for the same fit as km_lloyd, reached with
  * frames that the reference holds in host memory (kmeans.py:253-258 with the

@@ -245,37 +245,60 @@ size_t resident_ws_bytes(int64_t n, int d, int k, int prec) {
     return tc_frames_ws_size(n, d) + tc_assign_ws_size(n, d, k) + 2 * 256;
 }
 
-// Iterations after the first one can run as a CUDA graph WHILE loop: its
-// body is one iteration plus lloyd_loop_step_kernel, which records the
-// inertia, applies the stopping rule on the device and sets the loop's
-// condition, so a run of iterations costs one launch and one read-back.
-// A launch runs at most kLoopBatch iterations (the size of the inertia
-// buffer in the workspace).
-// dst (device) <- src (pageable host, readable by the device): 16-byte
-// words where both ends and the length allow, else 4-byte words.  Launched
-// with one CTA per SM, which fits beside a tensor-core CTA (no shared memory):
-// more copy CTAs on an SM would keep the assignment's CTAs off it.  Four
-// independent loads per thread keep enough bytes in flight for the host link.
-__global__ void __launch_bounds__(256) host_copy_kernel(const float *__restrict__ src, float *__restrict__ dst,
-                                                        int64_t count) {
-    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    if (((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst)) & 15) == 0) {
-        const int64_t n4 = count >> 2;
-        const float4 *s4 = reinterpret_cast<const float4 *>(src);
-        float4 *d4 = reinterpret_cast<float4 *>(dst);
-        int64_t i = t;
-        for (; i + 3 * stride < n4; i += 4 * stride) {
-            const float4 a = s4[i], b = s4[i + stride], c = s4[i + 2 * stride], e = s4[i + 3 * stride];
-            d4[i] = a;
-            d4[i + stride] = b;
-            d4[i + 2 * stride] = c;
-            d4[i + 3 * stride] = e;
+// dst (device) <- src (host memory that the device reads in place, or any
+// device-visible memory), count floats.  The CTAs claim blocks of
+// kCopyBlock floats in order from ctr[0], so a CTA that is placed late
+// (behind the CTAs of a kernel that fills the SM's registers or threads)
+// takes fewer blocks instead of holding back the end of the copy; each CTA
+// asks for its next block while it copies the current one.  The CTA that
+// finishes last sets the counter pair ctr = {next block, CTAs done} back to
+// zero for the next launch on the stream (it is zero before the first).
+// One CTA of 128 threads per SM with at most 32 registers a thread fits
+// beside a tensor-core CTA and beside the re-check's CTAs; 16-byte words
+// where both ends are aligned, else 4-byte words.
+constexpr int kCopyThreads = 128;
+constexpr int64_t kCopyBlock = 4096;  // floats per claimed block (16 KB)
+
+__global__ void __launch_bounds__(kCopyThreads, 16) host_copy_kernel(const float *__restrict__ src,
+                                                                     float *__restrict__ dst, int64_t count,
+                                                                     unsigned long long *__restrict__ ctr) {
+    __shared__ unsigned long long claim[2];
+    const unsigned long long nblk = (unsigned long long)((count + kCopyBlock - 1) / kCopyBlock);
+    const bool vec = ((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst)) & 15) == 0;
+    if (threadIdx.x == 0) claim[0] = atomicAdd(ctr, 1ull);
+    __syncthreads();
+    int cur = 0;
+    for (;;) {
+        const unsigned long long b = claim[cur];
+        if (b >= nblk) break;  // the same value in every thread
+        const int64_t a = (int64_t)b * kCopyBlock;
+        const int64_t e = count - a < kCopyBlock ? count : a + kCopyBlock;
+        if (vec && e - a == kCopyBlock) {
+            // 1024 float4 words: two rounds of four per thread
+            const float4 *s4 = reinterpret_cast<const float4 *>(src + a);
+            float4 *d4 = reinterpret_cast<float4 *>(dst + a);
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                float4 v[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) v[q] = s4[(h * 4 + q) * kCopyThreads + threadIdx.x];
+                if (h == 0 && threadIdx.x == 0) claim[cur ^ 1] = atomicAdd(ctr, 1ull);
+#pragma unroll
+                for (int q = 0; q < 4; ++q) d4[(h * 4 + q) * kCopyThreads + threadIdx.x] = v[q];
+            }
+        } else {
+            if (threadIdx.x == 0) claim[cur ^ 1] = atomicAdd(ctr, 1ull);
+            for (int64_t i = a + threadIdx.x; i < e; i += kCopyThreads) dst[i] = src[i];
         }
-        for (; i < n4; i += stride) d4[i] = s4[i];
-        for (int64_t j = (n4 << 2) + t; j < count; j += stride) dst[j] = src[j];
-    } else {
-        for (int64_t i = t; i < count; i += stride) dst[i] = src[i];
+        __syncthreads();  // the next claim is visible; this one is no longer read
+        cur ^= 1;
+    }
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(ctr + 1, 1ull) == (unsigned long long)gridDim.x - 1) {
+            ctr[0] = 0ull;
+            ctr[1] = 0ull;
+        }
     }
 }
 
@@ -291,6 +314,12 @@ cudaError_t instantiate_with_priorities(cudaGraphExec_t *gx, cudaGraph_t g) {
     return e;
 }
 
+// Iterations after the first one can run as a CUDA graph WHILE loop: its
+// body is one iteration plus lloyd_loop_step_kernel, which records the
+// inertia, applies the stopping rule on the device and sets the loop's
+// condition, so a run of iterations costs one launch and one read-back.
+// A launch runs at most kLoopBatch iterations (the size of the inertia
+// buffer in the workspace).
 struct LoopState {
     double prev;
     double tol;
@@ -319,6 +348,7 @@ __global__ void lloyd_loop_step_kernel(LoopState *st, const double *cost, const 
 
 size_t lloyd_ws_bytes(int64_t n, int d, int k, int prec) {
     Carver c(nullptr);
+    c.take<unsigned long long>(2);  // host copy counter pair
     c.take<LoopState>(1);
     c.take<double>(kLoopBatch);
     c.take<char>(update_ws_size(n, d, k));
@@ -565,7 +595,9 @@ struct HostFrames {
 };
 
 // Rows per streamed chunk of the first iteration: about 1/24 of the run,
-// at least 16384 frames, a multiple of 256.
+// at least 16384 frames, a multiple of 256.  (Halving the last chunks down
+// to 16384 frames did not shorten the run: every chunk carries a fixed
+// train of small launches.)
 int64_t stream_chunk_rows(int64_t n) {
     int64_t c = (n + 23) / 24;
     if (c < 16384) c = 16384;
@@ -812,6 +844,16 @@ int lloyd_run(const float *X_in, const HostFrames *hf, int64_t n, int32_t d, int
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     float *X = const_cast<float *>(X_in);  // written only by the host-frame copies
 
+    Carver cv(workspace);
+    unsigned long long *copy_ctr = cv.take<unsigned long long>(2);
+    LoopState *loop_st = cv.take<LoopState>(1);
+    double *loop_inertias = cv.take<double>(kLoopBatch);
+    void *ws_update = cv.take<char>(update_ws_size(n, d, k));
+    float *C_new = cv.take<float>((size_t)k * d);
+    double *cost = cv.take<double>(1);
+    uint32_t *err = cv.take<uint32_t>(1);
+    void *ws_assign = cv.take<char>(assign_ws_bytes(n, d, k, prec));
+
     // Host frames: one chunked copy on a side stream, an event per chunk.
     struct Streamed {
         cudaStream_t cs = nullptr;
@@ -866,11 +908,17 @@ int lloyd_run(const float *X_in, const HostFrames *hf, int64_t n, int32_t d, int
         std::vector<char> kernel_copy(hf->n_parts, 0);
         for (int32_t q = 0; q < hf->n_parts; ++q)
             kernel_copy[q] = hf->rows[q] > 0 && (in_place || is_pageable(hf->parts[q]));
-        KM_CUDA(cudaStreamCreateWithFlags(&sm.cs, cudaStreamNonBlocking));
+        // The copies are the run's critical path: their stream has the
+        // device's greatest priority, so their CTAs are placed before the
+        // assignment's waiting CTAs whenever an SM has room.
+        int least_prio = 0, greatest_prio = 0;
+        KM_CUDA(cudaDeviceGetStreamPriorityRange(&least_prio, &greatest_prio));
+        KM_CUDA(cudaStreamCreateWithPriority(&sm.cs, cudaStreamNonBlocking, greatest_prio));
         sm.ev.assign(sm.begin.size(), nullptr);  // [0]: the caller's stream reached this call
         for (cudaEvent_t &e : sm.ev) KM_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
         KM_CUDA(cudaEventRecord(sm.ev[0], s));
         KM_CUDA(cudaStreamWaitEvent(sm.cs, sm.ev[0], 0));
+        KM_CUDA(cudaMemsetAsync(copy_ctr, 0, 2 * sizeof(unsigned long long), sm.cs));
         int32_t q = 0;
         int64_t q_off = 0;  // rows of part q already copied
         for (size_t c = 0; c + 1 < sm.begin.size(); ++c) {
@@ -884,7 +932,7 @@ int lloyd_run(const float *X_in, const HostFrames *hf, int64_t n, int32_t d, int
                 const int64_t take = std::min(stop - row, hf->rows[q] - q_off);
                 if (kernel_copy[q]) {
                     // read in place by the device (gpu_reads_pageable_host)
-                    KM_TRY(launch_host_copy(hf->parts[q] + q_off * d, X + row * d, take * d, sm.cs));
+                    KM_TRY(launch_host_copy(hf->parts[q] + q_off * d, X + row * d, take * d, copy_ctr, sm.cs));
                 } else {
                     KM_CUDA(cudaMemcpyAsync(X + row * d, hf->parts[q] + q_off * d, sizeof(float) * (size_t)take * d,
                                             cudaMemcpyHostToDevice, sm.cs));
@@ -900,15 +948,6 @@ int lloyd_run(const float *X_in, const HostFrames *hf, int64_t n, int32_t d, int
             return KM_OK;
         }
     }
-
-    Carver cv(workspace);
-    LoopState *loop_st = cv.take<LoopState>(1);
-    double *loop_inertias = cv.take<double>(kLoopBatch);
-    void *ws_update = cv.take<char>(update_ws_size(n, d, k));
-    float *C_new = cv.take<float>((size_t)k * d);
-    double *cost = cv.take<double>(1);
-    uint32_t *err = cv.take<uint32_t>(1);
-    void *ws_assign = cv.take<char>(assign_ws_bytes(n, d, k, prec));
 
     // Tensor-core iterations run the exact re-check on a side stream beside
     // the centroid update, which sums by the tensor-core labels; the frames
@@ -1580,10 +1619,10 @@ namespace km {
 
 bool gpu_reads_host_in_place() { return gpu_reads_pageable_host(); }
 
-int launch_host_copy(const float *src, float *dst, int64_t count, cudaStream_t s) {
+int launch_host_copy(const float *src, float *dst, int64_t count, unsigned long long *ctr, cudaStream_t s) {
     if (count <= 0) return KM_OK;
-    const int64_t g = std::min<int64_t>((count / 4 + 255) / 256, (int64_t)num_sms());
-    host_copy_kernel<<<(unsigned)(g < 1 ? 1 : g), 256, 0, s>>>(src, dst, count);
+    const int64_t g = std::min<int64_t>((count + kCopyBlock - 1) / kCopyBlock, (int64_t)num_sms());
+    host_copy_kernel<<<(unsigned)(g < 1 ? 1 : g), kCopyThreads, 0, s>>>(src, dst, count, ctr);
     KM_CUDA(cudaGetLastError());
     return KM_OK;
 }

@@ -248,8 +248,11 @@ int centers_d(const km_centers *h);
 // not) in place through the host's page tables, as on Grace.
 bool gpu_reads_host_in_place();
 // dst (device) <- src (host memory the device reads in place): a copy kernel
-// on s, one CTA per SM (it fits beside a tensor-core CTA).
-int launch_host_copy(const float *src, float *dst, int64_t count, cudaStream_t s);
+// on s, one small CTA per SM (it fits beside a tensor-core CTA) claiming
+// 16 KB blocks from the counter pair ctr (two words, zero before the first
+// launch; each launch leaves it zero).  Launches that share ctr must run one
+// after the other (one stream).
+int launch_host_copy(const float *src, float *dst, int64_t count, unsigned long long *ctr, cudaStream_t s);
 int centers_device(const km_centers *h);
 int device_error_status(uint32_t e);
 // Bits set by km_debug_fake_device_error, cleared as they are taken.

@@ -68,6 +68,7 @@ struct Slot {
     int32_t *labels = nullptr;
     void *ws = nullptr;
     size_t ws_bytes = 0;
+    unsigned long long *copy_ctr = nullptr;  // the host copy kernel's counter pair
     uint32_t *err_host = nullptr;  // page-locked
     std::vector<Piece> pieces;
     int64_t frames = 0;
@@ -108,9 +109,11 @@ void free_slot_memory(km_server *S) {
         if (sl.X) cudaFree(sl.X);
         if (sl.labels) cudaFree(sl.labels);
         if (sl.ws) cudaFree(sl.ws);
+        if (sl.copy_ctr) cudaFree(sl.copy_ctr);
         sl.X = nullptr;
         sl.labels = nullptr;
         sl.ws = nullptr;
+        sl.copy_ctr = nullptr;
         sl.ws_bytes = 0;
     }
     S->cap = 0;
@@ -141,7 +144,7 @@ int size_slots(km_server *S, const std::vector<const km_centers *> &sets) {
     };
     auto slot_bytes = [&](int64_t n) {
         return round256((size_t)n * dmax * sizeof(float)) + round256((size_t)n * sizeof(int32_t)) +
-               round256(ws_for(n));
+               round256(ws_for(n)) + round256(2 * sizeof(unsigned long long));
     };
     const uint64_t budget = (uint64_t)S->cfg.hbm_budget_bytes;
     int64_t hi = std::min<int64_t>(want, (int64_t(1) << 31) - 1);
@@ -163,6 +166,8 @@ int size_slots(km_server *S, const std::vector<const km_centers *> &sets) {
         KM_CUDA(cudaMalloc(&sl.X, (size_t)cap * dmax * sizeof(float)));
         KM_CUDA(cudaMalloc(&sl.labels, (size_t)cap * sizeof(int32_t)));
         if (sl.ws_bytes) KM_CUDA(cudaMalloc(&sl.ws, sl.ws_bytes));
+        KM_CUDA(cudaMalloc(&sl.copy_ctr, 2 * sizeof(unsigned long long)));
+        KM_CUDA(cudaMemset(sl.copy_ctr, 0, 2 * sizeof(unsigned long long)));
     }
     S->cap = cap;
     S->d_max = dmax;
@@ -183,7 +188,7 @@ void launch(km_server *S, Slot &sl, const km_centers *h) {
     const bool in_place = gpu_reads_host_in_place();
     for (const Piece &pc : sl.pieces) {
         if (in_place) {
-            st = launch_host_copy(pc.req->X + pc.src * d, sl.X + pc.dst * d, pc.n * d, s);
+            st = launch_host_copy(pc.req->X + pc.src * d, sl.X + pc.dst * d, pc.n * d, sl.copy_ctr, s);
             if (st != KM_OK) break;
             continue;
         }
