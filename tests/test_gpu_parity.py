@@ -318,7 +318,7 @@ def test_lloyd_golden(torch, L, golden, prec):
 
 
 @pytest.mark.parametrize("prec", PRECS)
-@pytest.mark.parametrize("d,k", [(10, 100), (64, 64), (528, 40)])
+@pytest.mark.parametrize("d,k", [(10, 100), (64, 64), (528, 40), (12, 2100)])
 def test_lloyd_matches_oracle(torch, L, oracle, prec, d, k):
     from pyemma_gb300 import datasets
     X = datasets.gaussian_mixture(20000, d, 2 * k, 0.3, 5.0, seed=d)
@@ -330,6 +330,49 @@ def test_lloyd_matches_oracle(torch, L, oracle, prec, d, k):
     np.testing.assert_allclose(C.cpu().numpy(), ref["centers"], rtol=RTOL_CENTERS, atol=1e-5)
     np.testing.assert_allclose(r["inertias"], ref["inertias"], rtol=RTOL_INERTIA)
     np.testing.assert_array_equal(r["labels"].cpu().numpy(), ref["labels"])
+
+
+@pytest.mark.parametrize("prec", ["fp16", "bf16"])
+@pytest.mark.parametrize("fill", ["exact", "random", "shifted", "out_of_range"])
+def test_tc_seed_from_label_array(torch, L, oracle, monkeypatch, prec, fill):
+    # With short operand rows and many centers (KM_TC_SEED=1 here, for 700
+    # centers; by default from 2048) the tensor-core pass starts each
+    # frame's running best at a lower bound of the accumulator of the center
+    # that the label array already names (the previous iteration's label in
+    # a Lloyd run).  Whatever the array holds, the labels must be the
+    # oracle's: half-integer lattice frames with many exact ties, centers a
+    # hair off lattice points.
+    monkeypatch.setenv("KM_TC_SEED", "1")
+    rng = np.random.default_rng(71)
+    n, d, k = 40000, 6, 700
+    X = (rng.integers(0, 6, size=(n, d)) * 0.5).astype(np.float32)
+    C = (X[rng.choice(n, k, replace=False)] + rng.normal(scale=1e-3, size=(k, d))).astype(np.float32)
+    ref = oracle.assign(X, C)
+    if fill == "exact":
+        pre = ref.astype(np.int32)
+    elif fill == "random":
+        pre = rng.integers(0, k, size=n).astype(np.int32)
+    elif fill == "shifted":
+        pre = ((ref + 1) % k).astype(np.int32)
+    else:
+        pre = rng.choice(np.array([-1, -7, k, k + 5, 2 ** 31 - 1], dtype=np.int64), size=n).astype(np.int32)
+    labels = torch.from_numpy(pre).cuda()
+    out, _ = L.assign(dev(torch, X), dev(torch, C), precision=prec, labels=labels)
+    np.testing.assert_array_equal(out.cpu().numpy(), ref)
+
+
+def test_tc_seed_forced_on_long_rows(torch, L, oracle, monkeypatch):
+    # KM_TC_SEED=1 seeds rows of any length (here kp = 320 and 64 centers,
+    # where the default leaves the seed off); the labels stay the oracle's.
+    monkeypatch.setenv("KM_TC_SEED", "1")
+    from pyemma_gb300 import datasets
+    X = datasets.gaussian_mixture(6000, 300, 80, 0.3, 5.0, seed=5)
+    rng = np.random.default_rng(5)
+    C = X[rng.choice(len(X), 64, replace=False)]
+    ref = oracle.assign(X, C)
+    labels = torch.from_numpy(((ref + 3) % 64).astype(np.int32)).cuda()
+    out, _ = L.assign(dev(torch, X), dev(torch, C), precision="fp16", labels=labels)
+    np.testing.assert_array_equal(out.cpu().numpy(), ref)
 
 
 @pytest.mark.parametrize("prec", ["fp16", "bf16"])
