@@ -10,7 +10,10 @@ near ties (labels equal the plain FP32 kernel's bit for bit).  A "step" is one L
 
   value       frames/s over the timed steps, inputs resident in HBM, whole job
   e2e         the same metric through the public API (KmeansClustering.estimate
-              with max_iter=1) from pinned host frames, copies inside the clock
+              with max_iter=1) from pinned host frames, copies inside the clock;
+              a round of calls in which one call took more than twice the bare
+              copy time (a disturbed host link) is kept as rejected and taken
+              once more
   roofline    the tensor-core distance kernel: 2*N*k*d flops per launch over its
               CUDA-event launch time, against the measured BF16 peak (FP16 and
               BF16 share the kind::f16 tensor rate): the burst peak for a timed
@@ -516,19 +519,37 @@ def run_ours(args):
             KmeansClustering(n_clusters=K, max_iter=1, tolerance=-1.0, clustercenters=C0h,
                              precision="fp16").estimate(Xh_np)
         e2e_steps = max(1, min(args.steps, 8))
-        step_ms = []
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        for _ in range(e2e_steps):
-            ts = time.perf_counter()
-            km = KmeansClustering(n_clusters=K, max_iter=1, tolerance=-1.0, clustercenters=C0h, precision="fp16")
-            km.estimate(Xh_np)
-            _ = km.clustercenters  # host result (already copied back by estimate)
-            step_ms.append((time.perf_counter() - ts) * 1e3)
-        dt = (time.perf_counter() - t0) / e2e_steps
+        copy_ms_best = n * D * 4 / (link_gbs * 1e9) * 1e3
+
+        def e2e_round(frames):
+            # e2e_steps calls, each with its own clock; the mean is the rate.
+            # A call that took more than twice the bare copy of its frames met
+            # a disturbed host link (other users' traffic on the shared host):
+            # such a round is kept in the line as rejected and taken once more.
+            rounds = []
+            for _ in range(2):
+                step = []
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                for _ in range(e2e_steps):
+                    ts = time.perf_counter()
+                    km = KmeansClustering(n_clusters=K, max_iter=1, tolerance=-1.0, clustercenters=C0h,
+                                          precision="fp16")
+                    km.estimate(frames)
+                    _ = km.clustercenters  # host result (already copied back by estimate)
+                    step.append((time.perf_counter() - ts) * 1e3)
+                rounds.append(((time.perf_counter() - t0) / e2e_steps, step))
+                if max(step) <= 2.0 * copy_ms_best:
+                    break
+            rejected = [{"step_ms": st, "reason": "a call took more than twice the bare copy (%.1f ms)"
+                         % copy_ms_best} for _, st in rounds[:-1]]
+            return rounds[-1][0], rounds[-1][1], rejected
+
+        dt, step_ms, rejected = e2e_round(Xh_np)
         e2e = {"value": n / dt, "unit": UNIT, "h2d_bytes_per_step": n * D * 4, "d2h_bytes_per_step": K * D * 4 + 8,
                "api": "KmeansClustering(n_clusters=2000, max_iter=1, clustercenters=C).estimate(pinned host X)",
-               "steps": e2e_steps, "warmup": e2e_warm, "step_ms": step_ms, "h2d_link_gbs": link_gbs,
+               "steps": e2e_steps, "warmup": e2e_warm, "step_ms": step_ms, "rejected_rounds": rejected,
+               "h2d_link_gbs": link_gbs,
                "h2d_link_gbs_copy_engine": link_gbs_engine, "h2d_link_gbs_copy_kernel": link_gbs_kernel,
                "copy_bound_frames_per_s": link_gbs * 1e9 / (D * 4),
                "overlap": "frames copied in chunks on a side stream while the first iteration assigns "
@@ -543,19 +564,10 @@ def run_ours(args):
         for _ in range(e2e_warm):
             KmeansClustering(n_clusters=K, max_iter=1, tolerance=-1.0, clustercenters=C0h,
                              precision="fp16").estimate(Xpg)
-        torch.cuda.synchronize()
-        step_ms_pg = []
-        t0 = time.perf_counter()
-        for _ in range(e2e_steps):
-            ts = time.perf_counter()
-            km = KmeansClustering(n_clusters=K, max_iter=1, tolerance=-1.0, clustercenters=C0h, precision="fp16")
-            km.estimate(Xpg)
-            _ = km.clustercenters
-            step_ms_pg.append((time.perf_counter() - ts) * 1e3)
-        dtp = (time.perf_counter() - t0) / e2e_steps
+        dtp, step_ms_pg, rejected_pg = e2e_round(Xpg)
         e2e["pageable"] = {"value": n / dtp, "unit": UNIT, "h2d_bytes_per_step": n * D * 4,
                            "d2h_bytes_per_step": K * D * 4 + 8, "vs_pinned": (n / dtp) / e2e["value"],
-                           "step_ms": step_ms_pg,
+                           "step_ms": step_ms_pg, "rejected_rounds": rejected_pg,
                            "api": "KmeansClustering(max_iter=1, clustercenters=C).estimate(pageable numpy X)"}
         del Xpg
         # The same iteration from pinned host C-alpha coordinates: the 528
