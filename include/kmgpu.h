@@ -113,7 +113,11 @@ int km_debug_fake_device_error(uint32_t bits);
 /* ---- assignment: ClusterModel(centers, 'euclidean').transform(X) ----------
  * interface.py:157-167.  labels[i] = argmin_j ||X[i]-C[j]||^2, float32
  * distances summed in feature order, lowest index on ties.  stats (host,
- * nullable) synchronises the stream. */
+ * nullable) synchronises the stream.  The tensor-core forms read labels
+ * before they write it: a value in [0, k) seeds the frame's search (a
+ * previous labelling makes it faster where k >= 2048 and d <= 126); the
+ * result does not depend on what the array held, and the array need not be
+ * initialised. */
 size_t km_assign_workspace_size(int64_t n, int32_t d, int32_t k, int32_t precision);
 int km_assign(const float *X, int64_t n, int32_t d, const float *C, int32_t k, int32_t precision,
               int32_t *labels, void *workspace, size_t workspace_bytes, km_assign_stats *stats,
